@@ -1,0 +1,200 @@
+/*
+ * nairn_mpm_gpu.h -- C ABI of the GB300 explicit MPM time step.
+ *
+ * This is the drop-in boundary for NairnMPM's explicit step.  In the
+ * reference the step is a linked list of MPMTask objects built by
+ * NairnMPM::CreateTasks (NairnMPM/src/NairnMPM_Class/NairnMPM.cpp:870-1110) and
+ * walked by NairnMPM::MPMStep (NairnMPM.cpp:284-335).  A host integration
+ * replaces the tasks from InitializationTask through ResetElementsTask with one
+ * task that calls mpmgpu_step(); everything else (XML input, archiving,
+ * warnings) stays host code.  The plugin APIs the device re-implements are
+ *   - MaterialBase::MPMConstitutiveLaw / GetCopyOfMechanicalProps
+ *     (Common/Materials/MaterialBase.hpp:144,164; NairnMPM/src/Materials/MaterialBaseMPM.cpp:865),
+ *   - ElementBase::GetShapeFunctions / GetShapeGradients
+ *     (NairnMPM/src/Elements/MoreMPMElementBase.cpp:120,202),
+ *   - ContactLaw::GetFrictionalDeltaMomentum (NairnMPM/src/Materials/CoulombFriction.cpp:146).
+ *
+ * Conventions
+ *   - Plain C types, FP64 on the wire, NairnMPM "Legacy" units: mm, g, s;
+ *     stresses held per unit density (Pa*mm^3/g) exactly as MPMBase::sp.
+ *   - Every function returns an int status (MPMGPU_OK == 0) and never throws;
+ *     the reference's error convention is CommonException
+ *     (Common/Exceptions/CommonException.hpp:14-35), which the host side raises
+ *     from a non-zero status.  mpmgpu_last_error() gives the message.
+ *   - A context is driven from one host thread; it is not re-entrant.
+ *   - Unsupported options are refused with MPMGPU_ERR_UNSUPPORTED: there is no
+ *     CPU fallback.
+ */
+#ifndef NAIRN_MPM_GPU_H
+#define NAIRN_MPM_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define MPMGPU_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+    MPMGPU_OK = 0,
+    MPMGPU_ERR_INVALID = 1,      /* bad argument or inconsistent sizes          */
+    MPMGPU_ERR_UNSUPPORTED = 2,  /* option the device path does not implement   */
+    MPMGPU_ERR_CUDA = 3,         /* CUDA runtime error                          */
+    MPMGPU_ERR_OOM = 4,          /* device allocation failed / over HBM budget  */
+    MPMGPU_ERR_NAN = 5,          /* a particle position became NaN (LEFT_GRID_NAN) */
+    MPMGPU_ERR_LEFT_GRID = 6,    /* a particle left the grid (LEFT_GRID)        */
+    MPMGPU_ERR_CPDI_NODES = 7,   /* CPDI domain needs more nodes than allowed   */
+    MPMGPU_ERR_TIMEOUT = 8,      /* a bounded device wait gave up               */
+    MPMGPU_ERR_BUSY = 9          /* request still running (serving API)        */
+};
+
+/* ---- analysis options (values follow the reference's constants) -------- */
+/* MPMMethod: NairnMPM/src/System/MPMPrefix.hpp:110 */
+enum { MPMGPU_USF = 0, MPMGPU_USAVG = 2, MPMGPU_USL = 3 };
+/* GIMP type: NairnMPM/src/System/MPMPrefix.hpp:127-140 */
+enum { MPMGPU_SHAPE_LINEAR = 0, MPMGPU_SHAPE_UGIMP = 1, MPMGPU_SHAPE_LCPDI = 10 };
+/* Analysis type (np): NairnMPM/src/System/MPMPrefix.hpp:115 */
+enum { MPMGPU_PLANE_STRAIN = 10, MPMGPU_THREED = 12 };
+/* Arithmetic of the transfers (P2G/G2P and grid); the constitutive update,
+ * deformation gradient and particle displacement are FP64 in both modes. */
+enum { MPMGPU_PREC_FP64 = 0, MPMGPU_PREC_MIXED = 1 };
+/* P2G accumulation: hardware FP64/FP32 atomics, or a fixed-order gather */
+enum { MPMGPU_P2G_ATOMIC = 0, MPMGPU_P2G_DETERMINISTIC = 1 };
+/* Material types: Common/Read_XML/MaterialController.cpp:105-231 */
+enum { MPMGPU_MAT_ISOTROPIC = 1, MPMGPU_MAT_ISOPLASTICITY = 9, MPMGPU_MAT_NEOHOOKEAN = 28 };
+
+/* Structured background grid, as MPMReadHandler::grid() builds it
+ * (NairnMPM/src/Read_MPM/Generators.cpp:1675-1990): nx*ny(*nz) elements
+ * including the one-cell border layer, nodes numbered x fastest.  The node
+ * coordinates are passed so element extents match the host's bit for bit
+ * (ElementBase::FindExtent, Common/Elements/ElementBase.cpp:62). */
+typedef struct {
+    int32_t dim;              /* 2 or 3                                      */
+    int32_t nx, ny, nz;       /* element counts (nz = 0 in 2D)               */
+    double xmin, ymin, zmin;  /* MeshInfo xmin,ymin,zmin (grid origin)       */
+    double dx, dy, dz;        /* MeshInfo grid.x,.y,.z (dz = 0 in 2D)        */
+    double thickness;         /* 2D thickness (mm); ignored in 3D            */
+    const double *xnodes;     /* nx+1 node x coordinates                     */
+    const double *ynodes;     /* ny+1 node y coordinates                     */
+    const double *znodes;     /* nz+1 node z coordinates (NULL in 2D)        */
+} MpmGpuGrid;
+
+/* Material input properties in XML units (MPa, g/cm^3).  The library derives
+ * the specific constants exactly as the reference's VerifyAndLoadProperties. */
+typedef struct {
+    int32_t type;             /* MPMGPU_MAT_*                                */
+    int32_t field;            /* material velocity field (0 .. nfields-1)    */
+    double rho;               /* g/cm^3                                      */
+    double E, nu;             /* isotropic (types 1, 9)                      */
+    double yield, Ep;         /* type 9, linear hardening (MPa)              */
+    double G, K;              /* type 28 (MPa)                               */
+    int32_t UJOption;         /* type 28 volumetric energy option (0..2)     */
+    int32_t pad;
+} MpmGpuMaterial;
+
+/* Multimaterial contact (config with more than one material field).  Coulomb
+ * friction law CoulombFriction (NairnMPM/src/Materials/CoulombFriction.cpp). */
+typedef struct {
+    int32_t enabled;
+    int32_t normals;          /* MeshInfo materialNormalMethod 0..4 (volume gradients) */
+    double friction;          /* Coulomb coefficient; <0 stick; 0 frictionless */
+    double contact_cutoff;    /* position-based contact cutoff (cells); <0 displacement based */
+    double rigid_gradient_bias;
+} MpmGpuContact;
+
+/* One nodal velocity condition (NodalVelBC, NairnMPM/src/Boundary_Conditions/NodalVelBC.cpp).
+ * Applied in list order, as VelocityBCLoop does. */
+typedef struct {
+    int32_t node;             /* 1-based node number                         */
+    int32_t dir;              /* 1 = x, 2 = y, 4 = z                         */
+    double value;             /* velocity (mm/s) in that direction           */
+    double ftime;             /* active for t >= ftime                       */
+} MpmGpuVelBC;
+
+typedef struct {
+    int32_t np;               /* MPMGPU_PLANE_STRAIN or MPMGPU_THREED        */
+    int32_t method;           /* MPMGPU_USF / _USAVG / _USL                  */
+    int32_t shape;            /* MPMGPU_SHAPE_*                              */
+    int32_t precision;        /* MPMGPU_PREC_*                               */
+    int32_t p2g;              /* MPMGPU_P2G_*                                */
+    int32_t inc_defgrad_terms;/* Exponential() terms for hyperelastic (2D: 2, 3D: 1) */
+    int32_t nfields;          /* material velocity fields (1 unless contact) */
+    int32_t sort_interval;    /* re-sort particles by cell every k steps (>=1) */
+    double timestep;          /* s                                           */
+    double fraction_usf;      /* USAVG split (0.5)                           */
+} MpmGpuOptions;
+
+/* Particle state, structure of arrays, length n each.  Fields mirror MPMBase
+ * (NairnMPM/src/MPM_Classes/MPMBase.hpp:225-263).  In 2D the z arrays and the
+ * xz/yz components may be NULL.  The deformation gradient is carried the way
+ * MatPoint2D/3D store it: strain ep (normal + engineering shear) and rotation
+ * wrot, F = I + ep/2 +- wrot/2 off the diagonal. */
+typedef struct {
+    int64_t n;
+    double *x, *y, *z;               /* position (mm)                        */
+    double *vx, *vy, *vz;            /* velocity (mm/s)                      */
+    double *x0, *y0, *z0;            /* original position (mm)               */
+    double *mass;                    /* g                                    */
+    int32_t *mat;                    /* 0-based material index               */
+    int32_t *elem;                   /* 0-based element (ElemID())           */
+    double *lpx, *lpy, *lpz;         /* dimensionless semi-size (mpm_lp)     */
+    double *exx, *eyy, *ezz, *exy, *exz, *eyz;   /* ep                       */
+    double *wxy, *wxz, *wyz;         /* wrot                                 */
+    double *sxx, *syy, *szz, *sxy, *sxz, *syz;   /* sp (specific stress)     */
+    double *pressure;                /* specific pressure (type 9 deviatoric split) */
+    double *pxx, *pyy, *pzz, *pxy, *pxz, *pyz;   /* eplast (plastic strain or B) */
+    double *hist0, *hist1;           /* history doubles (alpha; J, Jres)     */
+    double *work, *plast;            /* work and plastic energy per unit mass */
+} MpmGpuParticles;
+
+/* ---- single-run context --------------------------------------------------- */
+typedef struct MpmGpuCtx MpmGpuCtx;
+
+/* Library ABI version (MPMGPU_ABI_VERSION). */
+int mpmgpu_abi_version(void);
+
+/* Create a context on the current CUDA device for one run.
+ * Replaces the set-up the reference does in NairnMPM::CMPreparations
+ * (NairnMPM.cpp:135-168) for the step's own data. */
+int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx **out);
+
+/* Materials (index = MpmGpuParticles.mat).  Replaces the property copies of
+ * MaterialBase::GetCopyOfMechanicalProps (MaterialBase.hpp:144). */
+int mpmgpu_set_materials(MpmGpuCtx *ctx, const MpmGpuMaterial *mats, int32_t nmat);
+
+/* Contact settings (MeshInfo::MaterialContactPairs, MeshInfo.cpp:1231). */
+int mpmgpu_set_contact(MpmGpuCtx *ctx, const MpmGpuContact *contact);
+
+/* Nodal velocity conditions in the reference's list order (firstVelocityBC). */
+int mpmgpu_set_velocity_bcs(MpmGpuCtx *ctx, const MpmGpuVelBC *bcs, int32_t nbc);
+
+/* Copy particle state host -> device (the mpm[] sync before the first step). */
+int mpmgpu_upload_particles(MpmGpuCtx *ctx, const MpmGpuParticles *p);
+
+/* Advance nsteps explicit steps from time t0 (s).  One call replaces
+ * nsteps passes of NairnMPM::MPMStep (NairnMPM.cpp:284-335). */
+int mpmgpu_step(MpmGpuCtx *ctx, int32_t nsteps, double t0);
+
+/* Copy particle state device -> host (the mpm[] sync before ArchiveResults,
+ * NairnMPM.cpp:199).  Arrays of p must be allocated by the caller. */
+int mpmgpu_download_particles(MpmGpuCtx *ctx, MpmGpuParticles *p);
+
+/* Message of the last failing call on ctx (static storage when ctx is NULL). */
+const char *mpmgpu_last_error(const MpmGpuCtx *ctx);
+
+/* Free all device memory of ctx. */
+void mpmgpu_destroy(MpmGpuCtx *ctx);
+
+/* Milliseconds of device time spent in each kernel family during the last
+ * mpmgpu_step call (CUDA events on the context stream); names[i] is static.
+ * Returns the number of entries written (<= cap).  Mirrors the per-task
+ * profile NairnMPM prints (NairnMPM.cpp:246-275, MPMTask.cpp:57-72). */
+int mpmgpu_profile(const MpmGpuCtx *ctx, const char **names, double *ms, int32_t cap);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* NAIRN_MPM_GPU_H */

@@ -1,0 +1,131 @@
+"""ctypes mirror of include/nairn_mpm_gpu.h and helpers to fill it from a Model.
+
+This is the same binding a NairnMPM maintainer would write to drive the C ABI
+from Python; the product's C++ host code uses the header directly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from .model import Model, PARTICLE_FIELDS
+
+c_double_p = C.POINTER(C.c_double)
+c_int32_p = C.POINTER(C.c_int32)
+
+MPMGPU_OK = 0
+STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "UNSUPPORTED", 3: "CUDA", 4: "OOM", 5: "NAN",
+                6: "LEFT_GRID", 7: "CPDI_NODES", 8: "TIMEOUT", 9: "BUSY"}
+
+
+class MpmGpuGrid(C.Structure):
+    _fields_ = [("dim", C.c_int32), ("nx", C.c_int32), ("ny", C.c_int32), ("nz", C.c_int32),
+                ("xmin", C.c_double), ("ymin", C.c_double), ("zmin", C.c_double),
+                ("dx", C.c_double), ("dy", C.c_double), ("dz", C.c_double),
+                ("thickness", C.c_double),
+                ("xnodes", c_double_p), ("ynodes", c_double_p), ("znodes", c_double_p)]
+
+
+class MpmGpuMaterial(C.Structure):
+    _fields_ = [("type", C.c_int32), ("field", C.c_int32), ("rho", C.c_double),
+                ("E", C.c_double), ("nu", C.c_double), ("yield_", C.c_double), ("Ep", C.c_double),
+                ("G", C.c_double), ("K", C.c_double), ("UJOption", C.c_int32), ("pad", C.c_int32)]
+
+
+class MpmGpuContact(C.Structure):
+    _fields_ = [("enabled", C.c_int32), ("normals", C.c_int32), ("friction", C.c_double),
+                ("contact_cutoff", C.c_double), ("rigid_gradient_bias", C.c_double)]
+
+
+class MpmGpuVelBC(C.Structure):
+    _fields_ = [("node", C.c_int32), ("dir", C.c_int32), ("value", C.c_double), ("ftime", C.c_double)]
+
+
+class MpmGpuOptions(C.Structure):
+    _fields_ = [("np", C.c_int32), ("method", C.c_int32), ("shape", C.c_int32), ("precision", C.c_int32),
+                ("p2g", C.c_int32), ("inc_defgrad_terms", C.c_int32), ("nfields", C.c_int32),
+                ("sort_interval", C.c_int32), ("timestep", C.c_double), ("fraction_usf", C.c_double)]
+
+
+_PFIELDS = ["x", "y", "z", "vx", "vy", "vz", "x0", "y0", "z0", "mass", "mat", "elem", "lpx", "lpy", "lpz",
+            "exx", "eyy", "ezz", "exy", "exz", "eyz", "wxy", "wxz", "wyz",
+            "sxx", "syy", "szz", "sxy", "sxz", "syz", "pressure",
+            "pxx", "pyy", "pzz", "pxy", "pxz", "pyz", "hist0", "hist1", "work", "plast"]
+
+
+class MpmGpuParticles(C.Structure):
+    _fields_ = [("n", C.c_int64)] + [(f, c_int32_p if f in ("mat", "elem") else c_double_p) for f in _PFIELDS]
+
+
+def _dptr(a: np.ndarray):
+    return a.ctypes.data_as(c_double_p)
+
+
+class Bound:
+    """Keeps numpy arrays alive while their pointers sit in ctypes structs."""
+
+    def __init__(self):
+        self.keep = []
+
+    def hold(self, a):
+        self.keep.append(a)
+        return a
+
+
+def grid_struct(m: Model, b: Bound) -> MpmGpuGrid:
+    g = m.grid
+    xs = b.hold(np.ascontiguousarray(g.xnodes, dtype=np.float64))
+    ys = b.hold(np.ascontiguousarray(g.ynodes, dtype=np.float64))
+    zs = b.hold(np.ascontiguousarray(g.znodes, dtype=np.float64)) if g.znodes is not None else None
+    return MpmGpuGrid(g.dim, g.nx, g.ny, g.nz, g.xmin, g.ymin, g.zmin, g.dx, g.dy, g.dz, g.thickness,
+                      _dptr(xs), _dptr(ys), _dptr(zs) if zs is not None else None)
+
+
+def options_struct(m: Model, precision: int = 0, p2g: int = 0, sort_interval: int = 1) -> MpmGpuOptions:
+    o = m.options
+    return MpmGpuOptions(o["np"], o["method"], o["shape"], precision, p2g, o.get("inc_defgrad_terms", 1),
+                         o.get("nfields", 1), sort_interval, o["timestep"], o.get("fraction_usf", 0.5))
+
+
+def materials_array(m: Model):
+    arr = (MpmGpuMaterial * len(m.materials))()
+    for i, d in enumerate(m.materials):
+        arr[i] = MpmGpuMaterial(d["type"], d.get("field", 0), d["rho"], d.get("E", 0.), d.get("nu", 0.),
+                                d.get("yield_", 0.), d.get("Ep", 0.), d.get("G", 0.), d.get("K", 0.),
+                                d.get("UJOption", 0), 0)
+    return arr
+
+
+def bcs_array(m: Model):
+    n = len(m.bcs)
+    arr = (MpmGpuVelBC * max(n, 1))()
+    for i in range(n):
+        r = m.bcs[i]
+        arr[i] = MpmGpuVelBC(int(r["node"]), int(r["dir"]), float(r["value"]), float(r["ftime"]))
+    return arr, n
+
+
+def particles_struct(p: dict, b: Bound) -> MpmGpuParticles:
+    """Struct whose pointers alias the arrays of p (which must be contiguous
+    float64 / int32 arrays of equal length)."""
+    s = MpmGpuParticles()
+    s.n = int(p["x"].shape[0])
+    for f in _PFIELDS:
+        a = p[f]
+        if f in ("mat", "elem"):
+            assert a.dtype == np.int32 and a.flags.c_contiguous
+            setattr(s, f, a.ctypes.data_as(c_int32_p))
+        else:
+            assert a.dtype == np.float64 and a.flags.c_contiguous, f
+            setattr(s, f, _dptr(a))
+        b.hold(a)
+    return s
+
+
+def copy_particles(p: dict) -> dict:
+    return {k: np.array(v, copy=True) for k, v in p.items()}
+
+
+def empty_like_particles(p: dict) -> dict:
+    return {k: np.zeros_like(v) for k, v in p.items()}

@@ -1,0 +1,146 @@
+"""Seeded synthetic NairnMPM XML inputs for the explicit-step workloads.
+
+The files use only the reference's own input vocabulary (NairnMPM/input/NairnMPM.dtd;
+handlers in NairnMPM/src/Read_MPM/MPMReadHandler.cpp and Generators.cpp), so the
+same file runs through the reference NairnMPM and through this project's host
+reader.  Units are NairnMPM "Legacy" units: mm, g/cm^3, MPa, mm/s, ms.
+
+Workloads (sizes are parameters so tests can run small copies):
+  cantilever_2d  -- 2D plane-strain elastic cantilever, uGIMP, USAVG
+  taylor_3d      -- 3D von Mises (linear hardening) Taylor bar onto a rigid wall
+"""
+from __future__ import annotations
+
+import math
+
+# IsotropicMat::WaveSpeed (NairnMPM/src/Materials/MoreIsotropicMat.cpp:388-395)
+# evaluated in the reference's units: G in Pa, rho in g/mm^3 -> mm/s.
+
+
+def iso_wave_speed(E_mpa: float, nu: float, rho_gcc: float) -> float:
+    E = E_mpa * 1.e6
+    G = E / (2. * (1. + nu))
+    rho = rho_gcc * 0.001
+    return math.sqrt(2. * G * (1. - nu) / (rho * (1. - 2. * nu)))
+
+
+def cfl_timestep(cell_mm: float, wave_speed: float, cfl: float) -> float:
+    """Time step of NairnMPM::CFLTimeStep (NairnMPM.cpp:1207-1240), seconds."""
+    return cfl * (cell_mm / wave_speed)
+
+
+def _fmt(v: float) -> str:
+    return repr(float(v))
+
+
+def _header(analysis: int, method: int, gimp: str, maxtime_s: float, cfl: float,
+            archive_root: str, ppe: int, order: str) -> str:
+    return f"""<?xml version='1.0'?>
+<!DOCTYPE JANFEAInput SYSTEM "NairnMPM.dtd">
+<JANFEAInput version='3'>
+  <Header>
+    <Description>synthetic workload</Description>
+    <Analysis>{analysis}</Analysis>
+  </Header>
+  <MPMHeader>
+    <MPMMethod>{method}</MPMMethod>
+    <GIMP type="{gimp}"/>
+    <MatlPtsPerElement>{ppe}</MatlPtsPerElement>
+    <Timing CFL="{_fmt(cfl)}"/>
+    <MaxTime units="ms">{_fmt(maxtime_s * 1.e3)}</MaxTime>
+    <ArchiveTime units="ms">{_fmt(maxtime_s * 1.e3 * 10.)}</ArchiveTime>
+    <ArchiveRoot>{archive_root}</ArchiveRoot>
+    <MPMArchiveOrder>{order}</MPMArchiveOrder>
+  </MPMHeader>
+"""
+
+
+# archive items: velocity, stress, strain, plastic strain, work energy,
+# plastic energy, history 1 (ArchiveData.hpp:22-32)
+ARCHIVE_ORDER = "iYYYYYNYNYNNNYNNNN"
+
+
+def cantilever_2d(nx: int = 100, ny: int = 20, cell: float = 1.0, ppc_side: int = 2,
+                  E: float = 1000., nu: float = 0.33, rho: float = 1.0, v0: float = 1000.,
+                  steps: int = 1000, cfl: float = 0.4, gimp: str = "uGIMP", method: int = 2,
+                  margin_cells: int = 4, archive_root: str = "Results/cant.") -> tuple[str, dict]:
+    """2D plane-strain cantilever of nx*ny cells, left edge fixed, initial
+    v_y = v0*sin(pi*x/(2L)) (mm/s).  Returns (xml, info)."""
+    L = nx * cell
+    H = ny * cell
+    c = iso_wave_speed(E, nu, rho)
+    dt = cfl_timestep(cell, c, cfl)
+    maxtime = (steps - 0.5) * dt
+    m = margin_cells * cell
+    xml = _header(10, method, gimp, maxtime, cfl, archive_root, ppc_side * ppc_side, ARCHIVE_ORDER)
+    xml += f"""  <Mesh output="file">
+    <Grid xmin="{_fmt(-m)}" xmax="{_fmt(L + m)}" ymin="{_fmt(-m)}" ymax="{_fmt(H + m)}" thickness="1">
+      <Horiz cellsize="{_fmt(cell)}"/>
+      <Vert cellsize="{_fmt(cell)}"/>
+    </Grid>
+  </Mesh>
+  <MaterialPoints>
+    <Body mat="1" angle="0" thick="1" vx="0" vy="0">
+      <!-- velocity expressions apply to the shapes that follow them -->
+      <vel0Y>{_fmt(v0)}*sin(pi*x/(2*{_fmt(L)}))</vel0Y>
+      <Rect xmin="0" xmax="{_fmt(L)}" ymin="0" ymax="{_fmt(H)}"/>
+    </Body>
+  </MaterialPoints>
+  <Material Type="1" Name="beam">
+    <rho>{_fmt(rho)}</rho>
+    <E>{_fmt(E)}</E>
+    <nu>{_fmt(nu)}</nu>
+    <alpha>0</alpha>
+  </Material>
+  <GridBCs>
+    <BCLine x1="0" y1="{_fmt(-0.5 * cell)}" x2="0" y2="{_fmt(H + 0.5 * cell)}" tolerance="{_fmt(0.01)}">
+      <DisBC dir="1" disp="0"/>
+      <DisBC dir="2" disp="0"/>
+    </BCLine>
+  </GridBCs>
+</JANFEAInput>
+"""
+    return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 2}
+
+
+def taylor_3d(radius: float = 5.0, length: float = 25.0, cell: float = 0.25, ppc_side: int = 2,
+              v0: float = -200000., E: float = 200000., nu: float = 0.3, yield_: float = 300.,
+              Ep: float = 2000., rho: float = 7.8, steps: int = 2000, cfl: float = 0.5,
+              gimp: str = "uGIMP", method: int = 2, lateral_margin: float | None = None,
+              archive_root: str = "Results/taylor.") -> tuple[str, dict]:
+    """3D Taylor impact: cylinder along z from z=0 to z=length moving at v0
+    (mm/s) onto a rigid wall at z=0 (zero z-velocity on the z=0 node plane)."""
+    c = iso_wave_speed(E, nu, rho)
+    dt = cfl_timestep(cell, c, cfl)
+    maxtime = (steps - 0.5) * dt
+    lm = lateral_margin if lateral_margin is not None else max(4 * cell, 0.8 * radius)
+    xr = radius + lm
+    xml = _header(12, method, gimp, maxtime, cfl, archive_root, ppc_side ** 3, ARCHIVE_ORDER)
+    xml += f"""  <Mesh output="file">
+    <Grid xmin="{_fmt(-xr)}" xmax="{_fmt(xr)}" ymin="{_fmt(-xr)}" ymax="{_fmt(xr)}" zmin="{_fmt(-4 * cell)}" zmax="{_fmt(length + 4 * cell)}">
+      <Horiz cellsize="{_fmt(cell)}"/>
+      <Vert cellsize="{_fmt(cell)}"/>
+      <Depth cellsize="{_fmt(cell)}"/>
+    </Grid>
+  </Mesh>
+  <MaterialPoints>
+    <Body mat="1" angle="0" vx="0" vy="0" vz="{_fmt(v0)}">
+      <Cylinder xmin="{_fmt(-radius)}" xmax="{_fmt(radius)}" ymin="{_fmt(-radius)}" ymax="{_fmt(radius)}" zmin="0" zmax="{_fmt(length)}" axis="z"/>
+    </Body>
+  </MaterialPoints>
+  <Material Type="9" Name="steel">
+    <rho>{_fmt(rho)}</rho>
+    <E>{_fmt(E)}</E>
+    <nu>{_fmt(nu)}</nu>
+    <alpha>0</alpha>
+    <yield>{_fmt(yield_)}</yield>
+    <Ep>{_fmt(Ep)}</Ep>
+  </Material>
+  <GridBCs>
+    <BCBox xmin="{_fmt(-xr - cell)}" xmax="{_fmt(xr + cell)}" ymin="{_fmt(-xr - cell)}" ymax="{_fmt(xr + cell)}" zmin="{_fmt(-0.01 * cell)}" zmax="{_fmt(0.01 * cell)}">
+      <DisBC dir="3" disp="0"/>
+    </BCBox>
+  </GridBCs>
+</JANFEAInput>
+"""
+    return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 3}

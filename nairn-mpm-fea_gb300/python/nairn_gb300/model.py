@@ -1,0 +1,290 @@
+"""Host-side model construction for the synthetic workloads.
+
+Builds the structured grid, the material points and the nodal velocity
+conditions the same way NairnMPM's input stage does for the XML produced by
+``inputs.py``, so the GPU step and the CPU oracle start from the state the
+reference starts from:
+
+  grid        MPMReadHandler::grid()            NairnMPM/src/Read_MPM/Generators.cpp:1675-1990
+  particles   MPMReadHandler::MPMPts()          Generators.cpp:1423-1545
+              ElementBase::MPMPoints()          NairnMPM/src/Elements/MoreMPMElementBase.cpp:348-440
+  mass        NairnMPM::PreliminaryParticleCalcs NairnMPM/src/NairnMPM_Class/NairnMPM.cpp:589-730
+  velocity BC DisBC on BCLine/BCBox             Generators.cpp:822-1010, ShapeController::nextNode
+
+All arrays are numpy; ``abi.py`` turns them into the C ABI structs.
+"""
+from __future__ import annotations
+
+import math
+from dataclasses import dataclass, field
+
+import numpy as np
+
+PLANE_STRAIN, THREED = 10, 12
+USF, USAVG, USL = 0, 2, 3
+SHAPE_LINEAR, SHAPE_UGIMP, SHAPE_LCPDI = 0, 1, 10
+MAT_ISO, MAT_PLASTIC, MAT_NEOHOOKEAN = 1, 9, 28
+
+PARTICLE_FIELDS = ("x", "y", "z", "vx", "vy", "vz", "x0", "y0", "z0", "mass", "lpx", "lpy", "lpz",
+                   "exx", "eyy", "ezz", "exy", "exz", "eyz", "wxy", "wxz", "wyz",
+                   "sxx", "syy", "szz", "sxy", "sxz", "syz", "pressure",
+                   "pxx", "pyy", "pzz", "pxy", "pxz", "pyz", "hist0", "hist1", "work", "plast")
+
+
+@dataclass
+class Grid:
+    dim: int
+    nx: int
+    ny: int
+    nz: int
+    xmin: float
+    ymin: float
+    zmin: float
+    dx: float
+    dy: float
+    dz: float
+    thickness: float
+    xnodes: np.ndarray
+    ynodes: np.ndarray
+    znodes: np.ndarray | None
+
+    @property
+    def nnodes(self) -> int:
+        n = (self.nx + 1) * (self.ny + 1)
+        return n * (self.nz + 1) if self.dim == 3 else n
+
+    @property
+    def nelems(self) -> int:
+        return self.nx * self.ny * (self.nz if self.dim == 3 else 1)
+
+
+@dataclass
+class Model:
+    grid: Grid
+    particles: dict
+    materials: list
+    bcs: np.ndarray
+    options: dict
+    nsteps: int
+    name: str = ""
+    extra: dict = field(default_factory=dict)
+
+    @property
+    def n(self) -> int:
+        return int(self.particles["x"].shape[0])
+
+
+BC_DTYPE = np.dtype([("node", "<i4"), ("dir", "<i4"), ("value", "<f8"), ("ftime", "<f8")])
+
+
+def _axis(vmin: float, vmax: float, cell: float):
+    """One axis of MPMReadHandler::grid() for a regular grid with cellsize set:
+    round the max up to a grid line, add one border cell each side, then
+    points vmin + i*delta."""
+    n = int((vmax - vmin) / cell)
+    newmax = vmin + n * cell
+    if newmax < vmax:
+        vmax = newmax + cell
+        n += 1
+    c = (vmax - vmin) / float(n)
+    n += 2
+    vmin -= c
+    vmax += c
+    delta = (vmax - vmin) / float(n)
+    pts = vmin + np.arange(n + 1, dtype=np.float64) * delta
+    return n, vmin, vmax, delta, pts
+
+
+def make_grid(dim: int, xlim, ylim, zlim, cell: float, thickness: float = 1.0) -> Grid:
+    nx, x0, x1, gx, xp = _axis(xlim[0], xlim[1], cell)
+    ny, y0, y1, gy, yp = _axis(ylim[0], ylim[1], cell)
+    if dim == 3:
+        nz, z0, z1, gz, zp = _axis(zlim[0], zlim[1], cell)
+        zmin = z0
+    else:
+        nz, gz, zp, zmin = 0, 0.0, None, thickness
+    return Grid(dim, nx, ny, nz, x0, y0, zmin, gx, gy, gz, thickness, xp, yp, zp)
+
+
+def _element_points(g: Grid, ppc_side: int):
+    """Positions (nelems*ppe, 3) and element index of every candidate point, in
+    the order MPMPts visits them (element-major, then ElementBase::MPMPoints
+    order: z, then y, then x)."""
+    n = ppc_side
+    gap = 1. / float(n)
+    vals = np.array([-1. + (2. * j + 1.) * gap for j in range(n)])
+    if g.dim == 2:
+        xi = np.array([(vals[j], vals[i], 0.) for i in range(n) for j in range(n)])
+    else:
+        xi = np.array([(vals[j], vals[ii], vals[i]) for i in range(n) for ii in range(n) for j in range(n)])
+    ne = g.nelems
+    e = np.arange(ne)
+    col = e % g.nx
+    row = (e // g.nx) % g.ny
+    x0, x1 = g.xnodes[col], g.xnodes[col + 1]
+    y0, y1 = g.ynodes[row], g.ynodes[row + 1]
+    npp = xi.shape[0]
+    pos = np.zeros((ne, npp, 3))
+    if g.dim == 2:
+        # Sum over element nodes (FourNodeIsoparam node order) of x_i * N_i
+        # with N_i = 4*((1+xii*x)/4)*((1+eti*y)/4) (FourNodeIsoparam.cpp:71-87)
+        xii = (-1., 1., 1., -1.)
+        eti = (-1., -1., 1., 1.)
+        nx_ = (x0, x1, x1, x0)
+        ny_ = (y0, y0, y1, y1)
+        for k in range(npp):
+            px = np.zeros(ne)
+            py = np.zeros(ne)
+            for i in range(4):
+                t1 = (1. + xii[i] * xi[k, 0]) / 4.
+                t2 = (1. + eti[i] * xi[k, 1]) / 4.
+                f = 4. * t1 * t2
+                px = px + nx_[i] * f
+                py = py + ny_[i] * f
+            pos[:, k, 0] = px
+            pos[:, k, 1] = py
+    else:
+        zr = e // (g.nx * g.ny)
+        z0, z1 = g.znodes[zr], g.znodes[zr + 1]
+        xii = (-1., 1., 1., -1., -1., 1., 1., -1.)
+        eti = (-1., -1., 1., 1., -1., -1., 1., 1.)
+        zti = (-1., -1., -1., -1., 1., 1., 1., 1.)
+        nx_ = (x0, x1, x1, x0, x0, x1, x1, x0)
+        ny_ = (y0, y0, y1, y1, y0, y0, y1, y1)
+        nz_ = (z0, z0, z0, z0, z1, z1, z1, z1)
+        # EightNodeIsoparamBrick::ShapeFunction (9-argument form): t1*t2*t3/8
+        for k in range(npp):
+            px = np.zeros(ne)
+            py = np.zeros(ne)
+            pz = np.zeros(ne)
+            for i in range(8):
+                t1 = (1. + xii[i] * xi[k, 0])
+                t2 = (1. + eti[i] * xi[k, 1])
+                t3 = (1. + zti[i] * xi[k, 2])
+                f = t1 * t2 * t3 / 8.
+                px = px + nx_[i] * f
+                py = py + ny_[i] * f
+                pz = pz + nz_[i] * f
+            pos[:, k, 0] = px
+            pos[:, k, 1] = py
+            pos[:, k, 2] = pz
+    elem = np.repeat(e, npp)
+    return pos.reshape(-1, 3), elem
+
+
+def _new_particles(pos, elem, g: Grid, ppc_side: int, rho_gcc: float, thick: float):
+    n = pos.shape[0]
+    p = {k: np.zeros(n) for k in PARTICLE_FIELDS}
+    p["x"][:] = pos[:, 0]
+    p["y"][:] = pos[:, 1]
+    p["z"][:] = pos[:, 2]
+    p["x0"][:] = pos[:, 0]
+    p["y0"][:] = pos[:, 1]
+    p["z0"][:] = pos[:, 2]
+    lp = 1. / float(ppc_side)
+    p["lpx"][:] = lp
+    p["lpy"][:] = lp
+    p["lpz"][:] = lp if g.dim == 3 else 1.
+    col = elem % g.nx
+    row = (elem // g.nx) % g.ny
+    dxe = g.xnodes[col + 1] - g.xnodes[col]
+    dye = g.ynodes[row + 1] - g.ynodes[row]
+    psx = dxe * (0.5 * lp)
+    psy = dye * (0.5 * lp)
+    rho = rho_gcc * 0.001
+    if g.dim == 3:
+        zr = elem // (g.nx * g.ny)
+        dze = g.znodes[zr + 1] - g.znodes[zr]
+        psz = dze * (0.5 * lp)
+        vol = 8. * psx * psy * psz
+    else:
+        vol = 4. * psx * psy * thick
+    p["mass"][:] = rho * vol
+    p["mat"] = np.zeros(n, dtype=np.int32)
+    p["elem"] = elem.astype(np.int32)
+    return p
+
+
+def cantilever_2d(nx=100, ny=20, cell=1.0, ppc_side=2, E=1000., nu=0.33, rho=1.0, v0=1000.,
+                  steps=1000, cfl=0.4, shape=SHAPE_UGIMP, method=USAVG, margin_cells=4) -> Model:
+    """Model of inputs.cantilever_2d (same arguments)."""
+    from . import inputs
+    L, H, m = nx * cell, ny * cell, margin_cells * cell
+    g = make_grid(2, (-m, L + m), (-m, H + m), None, cell, 1.0)
+    pos, elem = _element_points(g, ppc_side)
+    inside = (pos[:, 0] <= L) & (pos[:, 0] >= 0.) & (pos[:, 1] <= H) & (pos[:, 1] >= 0.)
+    p = _new_particles(pos[inside], elem[inside], g, ppc_side, rho, 1.0)
+    # <vel0Y> expression v0*sin(pi*x/(2*L)) (Expression.cpp evaluates left to right)
+    p["vy"][:] = v0 * np.sin(math.pi * p["x"] / (2. * L))
+    mats = [dict(type=MAT_ISO, field=0, rho=rho, E=E, nu=nu, yield_=0., Ep=0., G=0., K=0., UJOption=0)]
+    # BCLine x=0 from y=-cell/2 to H+cell/2 (LineController::ContainsPoint with the
+    # 2D tolerance test); node order is increasing node number, one DisBC at a time
+    nn = g.nnodes
+    ids = np.arange(1, nn + 1)
+    ndx = g.xnodes[(ids - 1) % (g.nx + 1)]
+    ndy = g.ynodes[(ids - 1) // (g.nx + 1)]
+    on = _line_contains(ndx, ndy, 0., -0.5 * cell, 0., H + 0.5 * cell, 0.01)
+    nodes = ids[on]
+    bcs = np.zeros(2 * nodes.size, dtype=BC_DTYPE)
+    bcs["node"][:nodes.size] = nodes
+    bcs["dir"][:nodes.size] = 1
+    bcs["node"][nodes.size:] = nodes
+    bcs["dir"][nodes.size:] = 2
+    c = inputs.iso_wave_speed(E, nu, rho)
+    dt = inputs.cfl_timestep(g.dx, c, cfl)  # MeshInfo::GetMinCellDimension: grid.x for square grids
+    opts = dict(np=PLANE_STRAIN, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
+                inc_defgrad_terms=2, nfields=1)
+    return Model(g, p, mats, bcs, opts, steps, name=f"cantilever_2d_{nx}x{ny}")
+
+
+def _line_contains(x, y, x1, y1, x2, y2, tol):
+    """LineController::ContainsPoint, 2D branch (Common/Read_XML/LineController.cpp:33-66)."""
+    distSq = (x2 - x1) * (x2 - x1) + (y2 - y1) * (y2 - y1)
+    dtol = math.sqrt(distSq) * tol
+    dx, dy = x2 - x1, y2 - y1
+    px, py = x - x1, y - y1
+    ypr = -dy * px + dx * py
+    xpr = dx * px + dy * py
+    return (ypr <= dtol) & (ypr >= -dtol) & (xpr >= 0.) & (xpr <= distSq)
+
+
+def taylor_3d(radius=5.0, length=25.0, cell=0.25, ppc_side=2, v0=-200000., E=200000., nu=0.3,
+              yield_=300., Ep=2000., rho=7.8, steps=2000, cfl=0.5, shape=SHAPE_UGIMP, method=USAVG,
+              lateral_margin=None) -> Model:
+    """Model of inputs.taylor_3d (same arguments)."""
+    from . import inputs
+    lm = lateral_margin if lateral_margin is not None else max(4 * cell, 0.8 * radius)
+    xr = radius + lm
+    g = make_grid(3, (-xr, xr), (-xr, xr), (-4 * cell, length + 4 * cell), cell)
+    pos, elem = _element_points(g, ppc_side)
+    # BoxController::ContainsPoint, cylinder along z (BoxController.cpp:47-98)
+    xmin, xmax, ymin, ymax, zmin, zmax = -radius, radius, -radius, radius, 0., length
+    xmid, ymid = (xmin + xmax) / 2., (ymin + ymax) / 2.
+    a2 = (xmax - xmid) ** 2
+    b2 = (ymax - ymid) ** 2
+    z = pos[:, 2]
+    dz = zmax - zmin
+    R = (zmax - z + 1. * (z - zmin)) / dz
+    ddx = pos[:, 0] - xmid
+    ddy = pos[:, 1] - ymid
+    inside = (z <= zmax) & (z >= zmin) & ((ddx * ddx / a2 + ddy * ddy / b2) <= R * R)
+    p = _new_particles(pos[inside], elem[inside], g, ppc_side, rho, 1.0)
+    p["vz"][:] = v0
+    mats = [dict(type=MAT_PLASTIC, field=0, rho=rho, E=E, nu=nu, yield_=yield_, Ep=Ep, G=0., K=0., UJOption=0)]
+    nn = g.nnodes
+    ids = np.arange(1, nn + 1)
+    plane = (g.nx + 1) * (g.ny + 1)
+    ndx = g.xnodes[(ids - 1) % (g.nx + 1)]
+    ndy = g.ynodes[((ids - 1) % plane) // (g.nx + 1)]
+    ndz = g.znodes[(ids - 1) // plane]
+    bx = (-xr - cell, xr + cell, -xr - cell, xr + cell, -0.01 * cell, 0.01 * cell)
+    on = (ndx <= bx[1]) & (ndx >= bx[0]) & (ndy <= bx[3]) & (ndy >= bx[2]) & (ndz <= bx[5]) & (ndz >= bx[4])
+    nodes = ids[on]
+    bcs = np.zeros(nodes.size, dtype=BC_DTYPE)
+    bcs["node"] = nodes
+    bcs["dir"] = 4
+    c = inputs.iso_wave_speed(E, nu, rho)
+    dt = inputs.cfl_timestep(g.dx, c, cfl)  # cubic grid: grid.x
+    opts = dict(np=THREED, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
+                inc_defgrad_terms=1, nfields=1)
+    return Model(g, p, mats, bcs, opts, steps, name=f"taylor_3d_r{radius}_c{cell}")

@@ -1,0 +1,1059 @@
+/*
+ * mpm_oracle.c -- CPU restatement of NairnMPM's explicit time step (FP64).
+ *
+ * TEST INFRASTRUCTURE ONLY: the checker for the GPU path.  Not part of the
+ * product; nothing outside tests/, the smoke check and the bench CPU baseline
+ * uses it.
+ *
+ * Each function cites the reference function it restates.  Paths are relative
+ * to the nairn-mpm-fea source tree.  With nthreads == 1 the particle loops run
+ * in the reference's single-patch order: P2G and grid-force loops walk the
+ * patch's particle list, which GridPatch::AddParticle builds by prepending
+ * (NairnMPM/src/Patches/GridPatch.cpp:256-278), i.e. in decreasing particle
+ * index; the strain and particle updates walk mpm[] forward.
+ */
+#include "mpm_oracle.h"
+
+#include <math.h>
+#include <stdio.h>
+#include <stdlib.h>
+#include <string.h>
+#ifdef _OPENMP
+#include <omp.h>
+#endif
+
+#define SQRT_TWOTHIRDS 0.8164965809277260   /* sqrt(2/3) */
+
+static char g_err[512];
+const char *mpm_oracle_last_error(void) { return g_err; }
+static int fail(int code, const char *msg) {
+    snprintf(g_err, sizeof(g_err), "%s", msg);
+    return code;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Materials: derived constants (VerifyAndLoadProperties of each class)       */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int type, field;
+    double rho;                 /* g/mm^3                                      */
+    double E, nu, G;            /* Pa                                          */
+    double C2[6][6];            /* 2D specific stiffness, Elastic::FillUnrotatedElasticProperties */
+    double C3[6][6];            /* 3D specific stiffness                       */
+    double Gred, Kred;          /* IsoPlasticity specific moduli               */
+    double yldred, Epred, alphaMax, yldredMin;  /* LinearHardening             */
+} OMat;
+
+/* Elastic::SetAnalysisProps (Common/Materials/Elastic.cpp:194-330) for an
+ * isotropic material (e1=e2=e3=E, v12=v13=v23=nu, g=G), then
+ * FillUnrotatedElasticProperties (Elastic.cpp:43-160) with makeSpecific. */
+static void iso_constants(OMat *m, int np) {
+    double e1 = m->E, e2 = m->E, e3 = m->E;
+    double v12 = m->nu, v13 = m->nu, v23 = m->nu;
+    double g12 = m->G, g13 = m->G, g23 = m->G;
+    double v32 = v23 * e3 / e2, v31 = v13 * e3 / e1, v21 = v12 * e2 / e1;
+    double xx, C11, C12, C13, C22, C23, C33, C44, C55, C66;
+    memset(m->C2, 0, sizeof(m->C2));
+    memset(m->C3, 0, sizeof(m->C3));
+    if (np == MPMGPU_THREED) {
+        xx = 1. - v13 * v31 - v23 * v32 - v12 * v21 - 2. * v13 * v32 * v21;
+        C11 = e1 * (1. - v23 * v32) / xx;
+        C12 = e2 * (v12 + v13 * v32) / xx;
+        C13 = e3 * (v13 + v12 * v23) / xx;
+        C22 = e2 * (1. - v13 * v31) / xx;
+        C23 = e3 * (v23 + v21 * v13) / xx;
+        C33 = e3 * (1. - v21 * v12) / xx;
+        C66 = g12; C44 = g23; C55 = g13;
+        double rrho = 1. / m->rho;
+        m->C3[0][0] = C11 * rrho; m->C3[0][1] = C12 * rrho; m->C3[0][2] = C13 * rrho;
+        m->C3[1][0] = m->C3[0][1]; m->C3[1][1] = C22 * rrho; m->C3[1][2] = C23 * rrho;
+        m->C3[2][0] = m->C3[0][2]; m->C3[2][1] = m->C3[1][2]; m->C3[2][2] = C33 * rrho;
+        m->C3[3][3] = C44 * rrho; m->C3[4][4] = C55 * rrho; m->C3[5][5] = C66 * rrho;
+    } else {
+        /* plane strain */
+        xx = 1. - v13 * v31 - v23 * v32 - v12 * v21 - 2. * v12 * v23 * v31;
+        C11 = e1 * (1. - v23 * v32) / xx;
+        C12 = e2 * (v12 + v13 * v32) / xx;
+        C22 = e2 * (1. - v13 * v31) / xx;
+        C66 = g12;
+        C13 = e3 * (v13 + v12 * v23) / xx;
+        C23 = e3 * (v23 + v21 * v13) / xx;
+        C33 = e3 * (1. - v21 * v12) / xx;
+        double rrho = 1. / m->rho;
+        m->C2[1][1] = C11 * rrho; m->C2[1][2] = C12 * rrho; m->C2[2][2] = C22 * rrho;
+        m->C2[3][3] = C66 * rrho;
+        m->C2[4][1] = C13 * rrho; m->C2[4][2] = C23 * rrho; m->C2[4][4] = C33 * rrho;
+        m->C2[2][1] = m->C2[1][2];
+    }
+    /* IsoPlasticity::VerifyAndLoadProperties (IsoPlasticity.cpp:58-65) uses the
+     * 3D/plane-strain C66 and C33, identical expressions in both branches */
+    m->Gred = C66 / m->rho;
+    m->Kred = C33 / m->rho - 4. * m->Gred / 3.;
+}
+
+static int load_materials(const MpmGpuMaterial *in, int nmat, int np, OMat *out) {
+    for (int i = 0; i < nmat; i++) {
+        OMat *m = &out[i];
+        memset(m, 0, sizeof(*m));
+        m->type = in[i].type;
+        m->field = in[i].field;
+        m->rho = in[i].rho * 0.001;              /* MaterialBaseMPM.cpp:58 */
+        if (m->type == MPMGPU_MAT_ISOTROPIC || m->type == MPMGPU_MAT_ISOPLASTICITY) {
+            m->E = in[i].E * 1.e6;               /* IsotropicMat.cpp:40 */
+            m->nu = in[i].nu;
+            m->G = m->E / (2. * (1. + m->nu));   /* IsotropicMat.cpp:96 */
+            iso_constants(m, np);
+            if (m->type == MPMGPU_MAT_ISOPLASTICITY) {
+                /* HardeningLawBase::VerifyAndLoadProperties, LinearHardening.cpp:45-58 */
+                double yield = in[i].yield * 1.e6, Ep = in[i].Ep * 1.e6, beta;
+                m->yldred = yield / m->rho;
+                m->yldredMin = 0. / m->rho;
+                if (Ep >= 0.) beta = Ep / yield;
+                else beta = 0.;
+                m->Epred = m->yldred * beta;
+                m->alphaMax = 1.e50;
+                if (beta < 0.) m->alphaMax = ((m->yldredMin / m->yldred) - 1.) / beta;
+            }
+        } else {
+            return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: material type not implemented");
+        }
+    }
+    return MPMGPU_OK;
+}
+
+/* IsotropicMat::WaveSpeed (MoreIsotropicMat.cpp:388-395) */
+static double wave_speed(const OMat *m) {
+    return sqrt(2. * m->G * (1. - m->nu) / (m->rho * (1. - 2. * m->nu)));
+}
+
+double mpm_oracle_cfl_timestep(const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int nmat,
+                               const int32_t *mat_used, double cfl) {
+    OMat *om = (OMat *)calloc((size_t)nmat, sizeof(OMat));
+    int np = grid->dim == 3 ? MPMGPU_THREED : MPMGPU_PLANE_STRAIN;
+    if (load_materials(mats, nmat, np, om) != MPMGPU_OK) {
+        free(om);
+        return -1.;
+    }
+    double dcell = grid->dx;
+    if (grid->dy < dcell) dcell = grid->dy;
+    if (grid->dim == 3 && grid->dz < dcell) dcell = grid->dz;
+    double tmin = 1.e30;
+    for (int i = 0; i < nmat; i++) {
+        if (mat_used && !mat_used[i]) continue;
+        double tst = dcell / wave_speed(&om[i]);
+        if (tst < tmin) tmin = tst;
+    }
+    free(om);
+    return cfl * tmin;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Grid                                                                      */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    int dim, nx, ny, nz;
+    long xplane, yplane, zplane, nnodes, nelems;
+    const double *xn, *yn, *zn;
+    double xmin, ymin, zmin, gx, gy, gz;
+} OGrid;
+
+typedef struct {            /* one material velocity field on every node */
+    double *mass, *px, *py, *pz, *fx, *fy, *fz, *vx, *vy, *vz, *cx, *cy, *cz;
+    int *npts;
+} OField;
+
+static void elem_extent(const OGrid *g, int e, double *x0, double *x1, double *y0, double *y1,
+                        double *z0, double *z1) {
+    int col = e % g->nx, row = (e / g->nx) % g->ny, zr = g->dim == 3 ? e / (g->nx * g->ny) : 0;
+    *x0 = g->xn[col]; *x1 = g->xn[col + 1];
+    *y0 = g->yn[row]; *y1 = g->yn[row + 1];
+    if (g->dim == 3) { *z0 = g->zn[zr]; *z1 = g->zn[zr + 1]; }
+    else { *z0 = 0.; *z1 = 0.; }
+}
+
+static long elem_node0(const OGrid *g, int e) {
+    int col = e % g->nx, row = (e / g->nx) % g->ny, zr = g->dim == 3 ? e / (g->nx * g->ny) : 0;
+    return (long)zr * g->zplane + (long)row * g->yplane + col + 1;
+}
+
+/* MeshInfo::EdgeElement2D/3D (MeshInfo.cpp:171-199), num is 1-based */
+static int edge_element(const OGrid *g, int num) {
+    int horiz = g->nx, vert = g->ny;
+    if (g->dim == 2) {
+        long total = (long)horiz * vert;
+        if (num <= horiz || num > total - horiz) return 1;
+        int col = num % horiz;
+        return col <= 1;
+    }
+    long total = (long)horiz * vert * g->nz;
+    if (num <= horiz * vert || num > total - (long)horiz * vert) return 1;
+    if (num % horiz <= 1) return 1;
+    int xz = num % (horiz * vert);
+    return xz <= horiz || xz > horiz * (vert - 1);
+}
+
+/* ------------------------------------------------------------------------ */
+/* Shape functions                                                           */
+/* ------------------------------------------------------------------------ */
+/* candidate tables, FourNodeIsoparam.cpp:27-30 and EightNodeIsoparamBrick.cpp */
+static const double gxii[16] = {-1., 1., 1., -1., -3., -1., 1., 3., 3., 3., 3., 1., -1., -3., -3., -3.};
+static const double geti[16] = {-1., -1., 1., 1., -3., -3., -3., -3., -1., 1., 3., 3., 3., 3., 1., -1.};
+static const int xoff2[16] = {0, 1, 1, 0, -1, 0, 1, 2, 2, 2, 2, 1, 0, -1, -1, -1};
+static const int yoff2[16] = {0, 0, 1, 1, -1, -1, -1, -1, 0, 1, 2, 2, 2, 2, 1, 0};
+static const double xii2[4] = {-1., 1., 1., -1.};
+static const double eti2[4] = {-1., -1., 1., 1.};
+static const double xii3[8] = {-1., 1., 1., -1., -1., 1., 1., -1.};
+static const double eti3[8] = {-1., -1., 1., 1., -1., -1., 1., 1.};
+static const double zti3[8] = {-1., -1., -1., -1., 1., 1., 1., 1.};
+static const int x3off[64] = {0, 1, 1, 0, 0, 1, 1, 0, -1, 0, 1, 2, 2, 2, 2, 1, 0, -1, -1, -1, -1, 0,
+                              1, 2, 2, 2, 2, 1, 0, -1, -1, -1, 0, 1, 1, 0, -1, 0, 1, 2, 2, 2, 2, 1,
+                              0, -1, -1, -1, 0, 1, 1, 0, -1, 0, 1, 2, 2, 2, 2, 1, 0, -1, -1, -1};
+static const int y3off[64] = {0, 0, 1, 1, 0, 0, 1, 1, -1, -1, -1, -1, 0, 1, 2, 2, 2, 2, 1, 0, -1, -1,
+                              -1, -1, 0, 1, 2, 2, 2, 2, 1, 0, 0, 0, 1, 1, -1, -1, -1, -1, 0, 1, 2, 2,
+                              2, 2, 1, 0, 0, 0, 1, 1, -1, -1, -1, -1, 0, 1, 2, 2, 2, 2, 1, 0};
+static const int z3off[64] = {0, 0, 0, 0, 1, 1, 1, 1, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 0, 1, 1,
+                              1, 1, 1, 1, 1, 1, 1, 1, 1, 1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1, -1,
+                              -1, -1, -1, -1, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2, 2};
+
+typedef struct {
+    int n;
+    long nds[64];
+    double fn[64], dx[64], dy[64], dz[64];
+} OShape;
+
+/* FourNodeIsoparam::GetXiPos / EightNodeIsoparamBrick::GetXiPos for rectangular
+ * elements (FourNodeIsoparam.cpp:351-366, EightNodeIsoparamBrick.cpp:276-281) */
+static void xi_pos(const OGrid *g, int e, double x, double y, double z, double *xi) {
+    double x0, x1, y0, y1, z0, z1;
+    elem_extent(g, e, &x0, &x1, &y0, &y1, &z0, &z1);
+    xi[0] = (2. * x - x0 - x1) / (x1 - x0);
+    xi[1] = (2. * y - y0 - y1) / (y1 - y0);
+    xi[2] = g->dim == 3 ? (2. * z - z0 - z1) / (z1 - z0) : 0.;
+}
+
+/* ElementBase::GetShapeFunctions / GetShapeGradients dispatch
+ * (NairnMPM/src/Elements/MoreMPMElementBase.cpp:120-284) for POINT_GIMP and
+ * UNIFORM_GIMP. */
+static void shape_eval(const OGrid *g, int shape, int e, const double *xi, const double *lp,
+                       int grad, OShape *s) {
+    double x0, x1, y0, y1, z0, z1;
+    elem_extent(g, e, &x0, &x1, &y0, &y1, &z0, &z1);
+    long n0 = elem_node0(g, e);
+    double DX = x1 - x0, DY = y1 - y0, DZ = z1 - z0;
+    if (shape == MPMGPU_SHAPE_LINEAR) {
+        if (g->dim == 2) {
+            /* FourNodeIsoparam::ShapeFunction (6 args), FourNodeIsoparam.cpp:189-212 */
+            long nodes[4] = {n0, n0 + 1, n0 + g->yplane + 1, n0 + g->yplane};
+            for (int i = 0; i < 4; i++) {
+                double t1 = (1. + xii2[i] * xi[0]);
+                double t2 = (1. + eti2[i] * xi[1]);
+                s->nds[i] = nodes[i];
+                s->fn[i] = 0.25 * t1 * t2;
+                if (grad) {
+                    s->dx[i] = 0.5 * xii2[i] * t2 / DX;
+                    s->dy[i] = 0.5 * eti2[i] * t1 / DY;
+                    s->dz[i] = 0.;
+                }
+            }
+            s->n = 4;
+        } else {
+            /* EightNodeIsoparamBrick::ShapeFunction (6 args), EightNodeIsoparamBrick.cpp:90-104 */
+            long nodes[8] = {n0, n0 + 1, n0 + 1 + g->yplane, n0 + g->yplane,
+                             n0 + g->zplane, n0 + 1 + g->zplane, n0 + 1 + g->yplane + g->zplane,
+                             n0 + g->yplane + g->zplane};
+            for (int i = 0; i < 8; i++) {
+                double t1 = (1. + xii3[i] * xi[0]);
+                double t2 = (1. + eti3[i] * xi[1]);
+                double t3 = (1. + zti3[i] * xi[2]);
+                s->nds[i] = nodes[i];
+                s->fn[i] = 0.125 * t1 * t2 * t3;
+                if (grad) {
+                    s->dx[i] = 0.25 * xii3[i] * t2 * t3 / DX;
+                    s->dy[i] = 0.25 * eti3[i] * t1 * t3 / DY;
+                    s->dz[i] = 0.25 * zti3[i] * t1 * t2 / DZ;
+                }
+            }
+            s->n = 8;
+        }
+        return;
+    }
+    /* UNIFORM_GIMP */
+    if (g->dim == 2) {
+        /* FourNodeIsoparam::GimpShapeFunction, FourNodeIsoparam.cpp:431-519 */
+        double q1x = 2. - lp[0], q2x = 2. + lp[0];
+        double q1y = 2. - lp[1], q2y = 2. + lp[1];
+        double inv_size_x = 1. / (4. * lp[0]);
+        double inv_size_y = 1. / (4. * lp[1]);
+        double inv_dx = 0., inv_dy = 0.;
+        if (grad) {
+            inv_dx = 2.0 / DX;
+            inv_dy = 2.0 / DY;
+        }
+        int i = 0;
+        for (int id = 0; id < 16; id++) {
+            double xp = fabs(xi[0] - gxii[id]);
+            if (xp >= q2x) continue;
+            double yp = fabs(xi[1] - geti[id]);
+            if (yp >= q2y) continue;
+            double Svpx, Svpy, argx = 0., argy = 0.;
+            if (xp < lp[0]) Svpx = ((4. - lp[0]) * lp[0] - xp * xp) * inv_size_x;
+            else if (xp <= q1x) Svpx = (2. - xp) / 2.;
+            else { argx = (q2x - xp) * inv_size_x; Svpx = 2. * lp[0] * argx * argx; }
+            if (yp < lp[1]) Svpy = ((4. - lp[1]) * lp[1] - yp * yp) * inv_size_y;
+            else if (yp <= q1y) Svpy = (2. - yp) / 2.;
+            else { argy = (q2y - yp) * inv_size_y; Svpy = 2. * lp[1] * argy * argy; }
+            s->fn[i] = Svpx * Svpy;
+            if (grad) {
+                double xsign = xi[0] > gxii[id] ? 1. : -1.;
+                double ysign = xi[1] > geti[id] ? 1. : -1.;
+                double dSvpx, dSvpy;
+                if (xp < lp[0]) dSvpx = -xp * inv_size_x * 2.0;
+                else if (xp <= q1x) dSvpx = -0.5;
+                else dSvpx = -argx;
+                if (yp < lp[1]) dSvpy = -yp * inv_size_y * 2.0;
+                else if (yp <= q1y) dSvpy = -0.5;
+                else dSvpy = -argy;
+                s->dx[i] = xsign * dSvpx * Svpy * inv_dx;
+                s->dy[i] = ysign * Svpx * dSvpy * inv_dy;
+                s->dz[i] = 0.;
+            }
+            s->nds[i] = n0 + xoff2[id] * g->xplane + yoff2[id] * g->yplane;
+            i++;
+        }
+        s->n = i;
+        return;
+    }
+    /* EightNodeIsoparamBrick::GimpShapeFunction, EightNodeIsoparamBrick.cpp:289-403
+     * (including its z size factor taken from lp.y) */
+    double q1x = 2. - lp[0], q2x = 2. + lp[0];
+    double q1y = 2. - lp[1], q2y = 2. + lp[1];
+    double q1z = 2. - lp[2], q2z = 2. + lp[2];
+    double inv_size_x = 1. / (4. * lp[0]);
+    double inv_size_y = 1. / (4. * lp[1]);
+    double inv_size_z = 1. / (4. * lp[1]);
+    double inv_dx = 0., inv_dy = 0., inv_dz = 0.;
+    if (grad) {
+        inv_dx = 2.0 / DX;
+        inv_dy = 2.0 / DY;
+        inv_dz = 2.0 / DZ;
+    }
+    int i = 0;
+    for (int id = 0; id < 64; id++) {
+        double gx = (double)(2 * x3off[id] - 1), gy = (double)(2 * y3off[id] - 1),
+               gz = (double)(2 * z3off[id] - 1);
+        double xp = fabs(xi[0] - gx);
+        if (xp >= q2x) continue;
+        double yp = fabs(xi[1] - gy);
+        if (yp >= q2y) continue;
+        double zp = fabs(xi[2] - gz);
+        if (zp >= q2z) continue;
+        double Svpx, Svpy, Svpz, argx = 0., argy = 0., argz = 0.;
+        if (xp < lp[0]) Svpx = ((4. - lp[0]) * lp[0] - xp * xp) * inv_size_x;
+        else if (xp <= q1x) Svpx = 0.5 * (2. - xp);
+        else { argx = (q2x - xp) * inv_size_x; Svpx = 2. * lp[0] * argx * argx; }
+        if (yp < lp[1]) Svpy = ((4. - lp[1]) * lp[1] - yp * yp) * inv_size_y;
+        else if (yp <= q1y) Svpy = 0.5 * (2. - yp);
+        else { argy = (q2y - yp) * inv_size_y; Svpy = 2. * lp[1] * argy * argy; }
+        if (zp < lp[2]) Svpz = ((4. - lp[2]) * lp[2] - zp * zp) * inv_size_z;
+        else if (zp <= q1z) Svpz = 0.5 * (2. - zp);
+        else { argz = (q2z - zp) * inv_size_z; Svpz = 2. * lp[2] * argz * argz; }
+        s->fn[i] = Svpx * Svpy * Svpz;
+        if (grad) {
+            double xsign = xi[0] > gx ? 1. : -1.;
+            double ysign = xi[1] > gy ? 1. : -1.;
+            double zsign = xi[2] > gz ? 1. : -1.;
+            double dSvpx, dSvpy, dSvpz;
+            if (xp < lp[0]) dSvpx = -xp / (2. * lp[0]);
+            else if (xp <= q1x) dSvpx = -0.5;
+            else dSvpx = -argx;
+            if (yp < lp[1]) dSvpy = -yp / (2. * lp[1]);
+            else if (yp <= q1y) dSvpy = -0.5;
+            else dSvpy = -argy;
+            if (zp < lp[2]) dSvpz = -zp / (2. * lp[2]);
+            else if (zp <= q1z) dSvpz = -0.5;
+            else dSvpz = -argz;
+            s->dx[i] = xsign * dSvpx * Svpy * Svpz * inv_dx;
+            s->dy[i] = ysign * Svpx * dSvpy * Svpz * inv_dy;
+            s->dz[i] = zsign * Svpx * Svpy * dSvpz * inv_dz;
+        }
+        s->nds[i] = n0 + x3off[id] * g->xplane + y3off[id] * g->yplane + z3off[id] * g->zplane;
+        i++;
+    }
+    s->n = i;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Constitutive laws                                                         */
+/* ------------------------------------------------------------------------ */
+typedef struct {
+    double m[3][3];
+} M3;
+
+/* Elastic::HypoIncrementDeformation (ElasticMPM.cpp:392-403): F <- (I+du)F,
+ * with F stored as ep/wrot (MatPoint2D.cpp:309-366, MatPoint3D.cpp:320-376);
+ * Matrix3::Exponential(1) and operator*= (Common/System/Matrix3.cpp:312-351,920-966). */
+static void hypo_increment_F(MpmGpuParticles *p, long i, const M3 *du, int is3d) {
+    if (!is3d) {
+        double a00 = 1. + du->m[0][0], a01 = du->m[0][1], a10 = du->m[1][0], a11 = 1. + du->m[1][1],
+               a22 = 1. + du->m[2][2];
+        double b00 = 1. + p->exx[i], b01 = 0.5 * (p->exy[i] - p->wxy[i]),
+               b10 = 0.5 * (p->exy[i] + p->wxy[i]), b11 = 1. + p->eyy[i], b22 = 1. + p->ezz[i];
+        double f00 = a00 * b00 + a01 * b10;
+        double f01 = a00 * b01 + a01 * b11;
+        double f10 = a10 * b00 + a11 * b10;
+        double f11 = a10 * b01 + a11 * b11;
+        double f22 = a22 * b22;
+        p->exx[i] = f00 - 1.;
+        p->eyy[i] = f11 - 1.;
+        p->ezz[i] = f22 - 1.;
+        p->exy[i] = f10 + f01;
+        p->wxy[i] = f10 - f01;
+        return;
+    }
+    double a[3][3], b[3][3], f[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) a[r][c] = du->m[r][c] + (r == c ? 1. : 0.);
+    b[0][0] = 1. + p->exx[i];
+    b[1][1] = 1. + p->eyy[i];
+    b[2][2] = 1. + p->ezz[i];
+    b[0][1] = 0.5 * (p->exy[i] - p->wxy[i]);
+    b[1][0] = 0.5 * (p->exy[i] + p->wxy[i]);
+    b[0][2] = 0.5 * (p->exz[i] - p->wxz[i]);
+    b[2][0] = 0.5 * (p->exz[i] + p->wxz[i]);
+    b[1][2] = 0.5 * (p->eyz[i] - p->wyz[i]);
+    b[2][1] = 0.5 * (p->eyz[i] + p->wyz[i]);
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) f[r][c] = a[r][0] * b[0][c] + a[r][1] * b[1][c] + a[r][2] * b[2][c];
+    p->exx[i] = f[0][0] - 1.;
+    p->eyy[i] = f[1][1] - 1.;
+    p->ezz[i] = f[2][2] - 1.;
+    p->exy[i] = f[1][0] + f[0][1];
+    p->exz[i] = f[2][0] + f[0][2];
+    p->eyz[i] = f[2][1] + f[1][2];
+    p->wxy[i] = f[1][0] - f[0][1];
+    p->wxz[i] = f[2][0] - f[0][2];
+    p->wyz[i] = f[2][1] - f[1][2];
+}
+
+/* IsotropicMat::SRConstitutiveLaw2D (plane strain, no residual strains),
+ * MoreIsotropicMat.cpp:185-279, with MaterialBase::Hypo2DCalculations
+ * (MaterialBaseMPM.cpp:1012-1020). */
+static void iso_2d(const OMat *m, MpmGpuParticles *p, long i, const M3 *du) {
+    double dvxx = du->m[0][0], dvyy = du->m[1][1];
+    double dgam = du->m[0][1] + du->m[1][0];
+    double dwrotxy = du->m[1][0] - du->m[0][1];
+    double st0xx = p->sxx[i], st0yy = p->syy[i], st0xy = p->sxy[i], st0zz = p->szz[i];
+    double c1 = m->C2[1][1] * dvxx + m->C2[1][2] * dvyy;
+    double c2 = m->C2[1][2] * dvxx + m->C2[2][2] * dvyy;
+    double c3 = m->C2[3][3] * dgam;
+    double dnorm = dwrotxy * p->sxy[i];
+    double dshear = 0.5 * dwrotxy * (p->sxx[i] - p->syy[i]);
+    p->sxx[i] += c1 - dnorm;
+    p->syy[i] += c2 + dnorm;
+    p->sxy[i] += c3 + dshear;
+    double work = 0.5 * ((st0xx + p->sxx[i]) * dvxx + (st0yy + p->syy[i]) * dvyy + (st0xy + p->sxy[i]) * dgam);
+    p->szz[i] += m->C2[4][1] * dvxx + m->C2[4][2] * dvyy + m->C2[4][4] * 0.;
+    work += 0.5 * (st0zz + p->szz[i]) * 0.;
+    if (p->work) p->work[i] += work;
+}
+
+/* IsotropicMat::SRConstitutiveLaw3D, MoreIsotropicMat.cpp:286-348, with
+ * MaterialBase::Hypo3DCalculations (MaterialBaseMPM.cpp:1026-1047). */
+static void iso_3d(const OMat *m, MpmGpuParticles *p, long i, const M3 *du) {
+    double dvxx = du->m[0][0], dvyy = du->m[1][1], dvzz = du->m[2][2];
+    double dgamxy = du->m[0][1] + du->m[1][0];
+    double dgamxz = du->m[0][2] + du->m[2][0];
+    double dgamyz = du->m[1][2] + du->m[2][1];
+    double dwxy = du->m[1][0] - du->m[0][1];
+    double dwxz = du->m[2][0] - du->m[0][2];
+    double dwyz = du->m[2][1] - du->m[1][2];
+    double s0xx = p->sxx[i], s0yy = p->syy[i], s0zz = p->szz[i];
+    double s0yz = p->syz[i], s0xz = p->sxz[i], s0xy = p->sxy[i];
+    double d[6];
+    d[0] = m->C3[0][0] * dvxx + m->C3[0][1] * dvyy + m->C3[0][2] * dvzz;
+    d[1] = m->C3[1][0] * dvxx + m->C3[1][1] * dvyy + m->C3[1][2] * dvzz;
+    d[2] = m->C3[2][0] * dvxx + m->C3[2][1] * dvyy + m->C3[2][2] * dvzz;
+    d[3] = m->C3[3][3] * dgamyz;
+    d[4] = m->C3[4][4] * dgamxz;
+    d[5] = m->C3[5][5] * dgamxy;
+    double stxx = -dwxy * s0xy - dwxz * s0xz;
+    double styy = dwxy * s0xy - dwyz * s0yz;
+    double stzz = dwxz * s0xz + dwyz * s0yz;
+    double styz = 0.5 * (dwxy * s0xz + dwxz * s0xy + dwyz * (s0yy - s0zz));
+    double stxz = 0.5 * (-dwxy * s0yz + dwxz * (s0xx - s0zz) + dwyz * s0xy);
+    double stxy = 0.5 * (dwxy * (s0xx - s0yy) - dwxz * s0yz - dwyz * s0xz);
+    p->sxx[i] += d[0] + stxx;
+    p->syy[i] += d[1] + styy;
+    p->szz[i] += d[2] + stzz;
+    p->syz[i] += d[3] + styz;
+    p->sxz[i] += d[4] + stxz;
+    p->sxy[i] += d[5] + stxy;
+    if (p->work)
+        p->work[i] += 0.5 * ((s0xx + p->sxx[i]) * dvxx + (s0yy + p->syy[i]) * dvyy + (s0zz + p->szz[i]) * dvzz +
+                             (s0yz + p->syz[i]) * dgamyz + (s0xz + p->sxz[i]) * dgamxz +
+                             (s0xy + p->sxy[i]) * dgamxy);
+}
+
+/* IsoPlasticity::MPMConstitutiveLaw + PlasticityConstLaw (small rotation, no
+ * residual strains, linear hardening), IsoPlasticity.cpp:128-451, with
+ * UpdatePressure (:462-492), GetPlasticPotential (:513-517),
+ * IsotropicMat::GetMagnitudeSFromDev (MoreIsotropicMat.cpp:356-370) and
+ * LinearHardening::SolveForLambdaBracketed (LinearHardening.cpp:124-145). */
+static void isoplastic(const OMat *m, MpmGpuParticles *p, long i, const M3 *de, int is3d) {
+    double delV = de->m[0][0] + de->m[1][1] + de->m[2][2];   /* du.trace() - 3*eres */
+    double dgxy = de->m[0][1] + de->m[1][0], dgxz = 0., dgyz = 0.;
+    if (is3d) {
+        dgxz = de->m[0][2] + de->m[2][0];
+        dgyz = de->m[1][2] + de->m[2][1];
+    }
+    double dexxr = de->m[0][0], deyyr = de->m[1][1], dezzr = de->m[2][2];
+    /* UpdatePressure */
+    double dP = -m->Kred * delV;
+    double dVoverV = delV;
+    p->pressure[i] += dP;
+    double Pfinal = p->pressure[i];
+    if (p->work) p->work[i] += -Pfinal * dVoverV;
+    /* rotate plastic strain and stress (small rotation) */
+    double dwrotxy = de->m[1][0] - de->m[0][1], dwrotxz = 0., dwrotyz = 0.;
+    double epxx = p->pxx[i], epyy = p->pyy[i], epzz = p->pzz[i], epxy = p->pxy[i];
+    double epxz = is3d ? p->pxz[i] : 0., epyz = is3d ? p->pyz[i] : 0.;
+    double s0xx, s0yy, s0zz, s0xy, s0xz = 0., s0yz = 0.;
+    double spxx = p->sxx[i], spyy = p->syy[i], spzz = p->szz[i], spxy = p->sxy[i];
+    double spxz = is3d ? p->sxz[i] : 0., spyz = is3d ? p->syz[i] : 0.;
+    if (!is3d) {
+        double dnorm = 0.5 * dwrotxy * epxy;
+        p->pxx[i] -= dnorm;
+        p->pyy[i] += dnorm;
+        p->pxy[i] += dwrotxy * (epxx - epyy);
+        s0xx = spxx; s0yy = spyy; s0zz = spzz; s0xy = spxy;
+        double dn = dwrotxy * spxy;
+        s0xx -= dn;
+        s0yy += dn;
+        s0xy += 0.5 * dwrotxy * (epxx - epyy);
+    } else {
+        dwrotxz = de->m[2][0] - de->m[0][2];
+        dwrotyz = de->m[2][1] - de->m[1][2];
+        double dxy = 0.5 * dwrotxy * epxy, dxz = 0.5 * dwrotxz * epxz, dyz = 0.5 * dwrotyz * epyz;
+        p->pxx[i] += -dxy - dxz;
+        p->pyy[i] += dxy - dyz;
+        p->pzz[i] += dxz + dyz;
+        p->pyz[i] += dwrotyz * (epyy - epzz) + 0.5 * (dwrotxz * epxy + dwrotxy * epxz);
+        p->pxz[i] += dwrotxz * (epxx - epzz) + 0.5 * (dwrotyz * epxy - dwrotxy * epyz);
+        p->pxy[i] += dwrotxy * (epxx - epyy) - 0.5 * (dwrotyz * epxz + dwrotxz * epyz);
+        s0xx = spxx; s0yy = spyy; s0zz = spzz; s0xy = spxy; s0xz = spxz; s0yz = spyz;
+        double sxy = dwrotxy * spxy, sxz = dwrotxz * spxz, syz = dwrotyz * spyz;
+        s0xx += -sxy - sxz;
+        s0yy += sxy - syz;
+        s0zz += sxz + syz;
+        s0yz += 0.5 * (dwrotyz * (spyy - spzz) + dwrotxz * spxy + dwrotxy * spxz);
+        s0xz += 0.5 * (dwrotxz * (spxx - spzz) + dwrotyz * spxy - dwrotxy * spyz);
+        s0xy += 0.5 * (dwrotxy * (spxx - spyy) - dwrotyz * spxz - dwrotxz * spyz);
+    }
+    /* trial stress */
+    double thirdDelV = delV / 3.;
+    double dsxx = 2. * m->Gred * (dexxr - thirdDelV);
+    double dsyy = 2. * m->Gred * (deyyr - thirdDelV);
+    double dsxy = m->Gred * dgxy;
+    double dszz = 2. * m->Gred * (dezzr - thirdDelV);
+    double dsyz = 0., dsxz = 0.;
+    if (is3d) {
+        dsyz = m->Gred * dgyz;
+        dsxz = m->Gred * dgxz;
+    }
+    double trxx = s0xx + dsxx, tryy = s0yy + dsyy, trzz = s0zz + dszz, trxy = s0xy + dsxy;
+    double tryz = s0yz + dsyz, trxz = s0xz + dsxz;
+    double alpint = p->hist0[i];
+    double s2 = trxx * trxx + tryy * tryy + trzz * trzz;
+    double t2 = is3d ? trxy * trxy + trxz * trxz + tryz * tryz : trxy * trxy;
+    double strialmag = sqrt(s2 + t2 + t2);
+    double yld = alpint < m->alphaMax ? m->yldred + m->Epred * alpint : m->yldredMin;
+    double ftrial = strialmag - SQRT_TWOTHIRDS * yld;
+    if (ftrial < 0.) {
+        p->sxx[i] = trxx; p->syy[i] = tryy; p->szz[i] = trzz; p->sxy[i] = trxy;
+        if (is3d) { p->syz[i] = tryz; p->sxz[i] = trxz; }
+        if (p->work) {
+            if (is3d)
+                p->work[i] += trxx * de->m[0][0] + tryy * de->m[1][1] + trzz * de->m[2][2] + tryz * dgyz +
+                              trxz * dgxz + trxy * dgxy;
+            else
+                p->work[i] += trxx * de->m[0][0] + tryy * de->m[1][1] + trxy * dgxy;
+        }
+        return;
+    }
+    /* radial return, LinearHardening::SolveForLambdaBracketed */
+    double lambdak = (strialmag - SQRT_TWOTHIRDS * (m->yldred + m->Epred * alpint)) / (2. * (m->Gred + m->Epred / 3.));
+    if (alpint + SQRT_TWOTHIRDS * lambdak > m->alphaMax)
+        lambdak = (strialmag - SQRT_TWOTHIRDS * m->yldredMin) / (2. * m->Gred);
+    double dalpha = SQRT_TWOTHIRDS * lambdak;
+    double alpnew = alpint + dalpha;
+    /* GetDfDsigma */
+    double nxx = trxx / strialmag, nyy = tryy / strialmag, nzz = trzz / strialmag, nxy = trxy / strialmag;
+    double nxz = 0., nyz = 0.;
+    if (is3d) { nxz = trxz / strialmag; nyz = tryz / strialmag; }
+    double depxx = lambdak * nxx, depyy = lambdak * nyy, depzz = lambdak * nzz, depxy = 2. * lambdak * nxy;
+    double depxz = 0., depyz = 0.;
+    if (is3d) { depxz = 2. * lambdak * nxz; depyz = 2. * lambdak * nyz; }
+    p->pxx[i] += depxx; p->pyy[i] += depyy; p->pzz[i] += depzz; p->pxy[i] += depxy;
+    if (is3d) { p->pxz[i] += depxz; p->pyz[i] += depyz; }
+    double sxx = trxx - 2. * m->Gred * depxx;
+    double syy = tryy - 2. * m->Gred * depyy;
+    double szz = trzz - 2. * m->Gred * depzz;
+    double sxy = trxy - m->Gred * depxy;
+    double syz = 0., sxz = 0.;
+    if (is3d) {
+        syz = tryz - m->Gred * depyz;
+        sxz = trxz - m->Gred * depxz;
+    }
+    p->sxx[i] = sxx; p->syy[i] = syy; p->szz[i] = szz; p->sxy[i] = sxy;
+    if (is3d) { p->syz[i] = syz; p->sxz[i] = sxz; }
+    double workEnergy = sxx * de->m[0][0] + syy * de->m[1][1] + sxy * dgxy;
+    if (is3d) workEnergy += szz * de->m[2][2] + syz * dgyz + sxz * dgxz;
+    if (is3d) workEnergy += szz * de->m[2][2];   /* np != PLANE_STRAIN_MPM adds zz again */
+    if (p->work) p->work[i] += workEnergy;
+    double plastEnergy = sxx * depxx + syy * depyy + szz * depzz + sxy * depxy;
+    if (is3d) plastEnergy += sxz * depxz + syz * depyz;
+    double qdalpha = lambdak * SQRT_TWOTHIRDS * fmax(m->Epred * alpnew, m->yldredMin - m->yldred);
+    if (p->plast) p->plast[i] += plastEnergy - qdalpha;
+    p->hist0[i] = alpnew;
+}
+
+/* ------------------------------------------------------------------------ */
+/* Step                                                                      */
+/* ------------------------------------------------------------------------ */
+enum { MASS_MOMENTUM_CALL = 0, UPDATE_MOMENTUM_CALL, UPDATE_STRAINS_LAST_CALL, GRID_FORCES_CALL };
+
+typedef struct {
+    OGrid g;
+    OField f;               /* single material field */
+    const MpmGpuOptions *o;
+    OMat *mats;
+    const MpmGpuVelBC *bcs;
+    int nbc;
+    MpmGpuParticles *p;
+    double *xi;             /* 3 per particle: natural coordinates (ncpos) */
+    double dt, mtime;
+    int nthreads;
+} OCtx;
+
+static void bc_norm(int dir, double *n) {
+    n[0] = dir == 1 ? 1. : 0.;
+    n[1] = dir == 2 ? 1. : 0.;
+    n[2] = dir == 4 ? 1. : 0.;
+}
+
+/* NodalVelBC::VelocityBCLoop (NodalVelBC.cpp:386-400) with
+ * MatVelocityField::ZeroVelocityBC / AddVelocityBC (MatVelocityField.cpp:490-575). */
+static void velocity_bc_loop(OCtx *c, int pass) {
+    OField *f = &c->f;
+    double dt = c->dt;
+    for (int b = 0; b < c->nbc; b++) {
+        const MpmGpuVelBC *bc = &c->bcs[b];
+        if (c->mtime < bc->ftime) continue;
+        long i = bc->node;
+        if (f->npts[i] <= 0) continue;
+        double n[3];
+        bc_norm(bc->dir, n);
+        double dotn, dotf, dotp;
+        switch (pass) {
+        case UPDATE_MOMENTUM_CALL:
+            dotn = f->px[i] * n[0] + f->py[i] * n[1] + f->pz[i] * n[2];
+            f->px[i] += n[0] * (-dotn); f->py[i] += n[1] * (-dotn); f->pz[i] += n[2] * (-dotn);
+            f->fx[i] += n[0] * (-dotn / dt); f->fy[i] += n[1] * (-dotn / dt); f->fz[i] += n[2] * (-dotn / dt);
+            break;
+        case MASS_MOMENTUM_CALL:
+        case UPDATE_STRAINS_LAST_CALL:
+            dotn = f->px[i] * n[0] + f->py[i] * n[1] + f->pz[i] * n[2];
+            f->px[i] += n[0] * (-dotn); f->py[i] += n[1] * (-dotn); f->pz[i] += n[2] * (-dotn);
+            break;
+        case GRID_FORCES_CALL: {
+            dotf = f->fx[i] * n[0] + f->fy[i] * n[1] + f->fz[i] * n[2];
+            dotp = f->px[i] * n[0] + f->py[i] * n[1] + f->pz[i] * n[2];
+            double s = -dotf - dotp / dt;
+            f->fx[i] += n[0] * s; f->fy[i] += n[1] * s; f->fz[i] += n[2] * s;
+            break;
+        }
+        }
+    }
+    for (int b = 0; b < c->nbc; b++) {
+        const MpmGpuVelBC *bc = &c->bcs[b];
+        if (c->mtime < bc->ftime) continue;
+        long i = bc->node;
+        if (f->npts[i] <= 0) continue;
+        double n[3], vel = bc->value;
+        bc_norm(bc->dir, n);
+        double mass = f->mass[i];
+        switch (pass) {
+        case MASS_MOMENTUM_CALL:
+        case UPDATE_STRAINS_LAST_CALL: {
+            double s = mass * vel;
+            f->px[i] += n[0] * s; f->py[i] += n[1] * s; f->pz[i] += n[2] * s;
+            break;
+        }
+        case UPDATE_MOMENTUM_CALL: {
+            double pvel = mass * vel;
+            f->px[i] += n[0] * pvel; f->py[i] += n[1] * pvel; f->pz[i] += n[2] * pvel;
+            double s = pvel / dt;
+            f->fx[i] += n[0] * s; f->fy[i] += n[1] * s; f->fz[i] += n[2] * s;
+            break;
+        }
+        case GRID_FORCES_CALL: {
+            double s = mass * vel / dt;
+            f->fx[i] += n[0] * s; f->fy[i] += n[1] * s; f->fz[i] += n[2] * s;
+            break;
+        }
+        }
+    }
+}
+
+static long particle_order(const OCtx *c, long k) {
+    /* reverse order of the patch list when single-threaded */
+    return c->p->n - 1 - k;
+}
+
+/* MassAndMomentumTask::Execute (MassAndMomentumTask.cpp:48-127) and
+ * NodalPoint::AddMassMomentum (NodalPointMPM.cpp:419-453); when last is set,
+ * UpdateStrainsLastContactTask's AddMassMomentumLast (NodalPointMPM.cpp:470-486). */
+static void p2g_mass_momentum(OCtx *c, int last) {
+    MpmGpuParticles *p = c->p;
+    OField *f = &c->f;
+    int is3d = c->g.dim == 3;
+#pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
+    for (long k = 0; k < p->n; k++) {
+        long q = particle_order(c, k);
+        OShape s;
+        double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
+        shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, 0, &s);
+        double mp = p->mass[q];
+        double vx = p->vx[q], vy = p->vy[q], vz = is3d ? p->vz[q] : 0.;
+        for (int j = 0; j < s.n; j++) {
+            long nd = s.nds[j];
+            double fnmp = s.fn[j] * mp;
+            double ax = vx * fnmp, ay = vy * fnmp, az = vz * fnmp;
+            if (c->nthreads > 1) {
+#pragma omp atomic
+                f->px[nd] += ax;
+#pragma omp atomic
+                f->py[nd] += ay;
+#pragma omp atomic
+                f->pz[nd] += az;
+                if (!last) {
+#pragma omp atomic
+                    f->npts[nd] += 1;
+#pragma omp atomic
+                    f->mass[nd] += fnmp;
+                }
+            } else {
+                f->px[nd] += ax;
+                f->py[nd] += ay;
+                f->pz[nd] += az;
+                if (!last) {
+                    f->npts[nd] += 1;
+                    f->mass[nd] += fnmp;
+                }
+            }
+        }
+    }
+}
+
+/* MatVelocityField::GridValueCalculation (MatVelocityField.cpp:239-251) */
+static void grid_velocity(OCtx *c) {
+    OField *f = &c->f;
+    for (long i = 1; i <= c->g.nnodes; i++) {
+        if (f->npts[i] <= 0 || f->mass[i] == 0.) continue;
+        double r = 1. / f->mass[i];
+        f->vx[i] = f->px[i] * r;
+        f->vy[i] = f->py[i] * r;
+        f->vz[i] = f->pz[i] * r;
+    }
+}
+
+/* UpdateStrainsFirstTask::FullStrainUpdate (UpdateStrainsFirstTask.cpp:101-168),
+ * MatPoint2D/3D::UpdateStrain and ExtrapVelocityGradient
+ * (MatPoint2D.cpp:37-87, MatPoint3D.cpp:40-75). */
+static void strain_update(OCtx *c, double strainTime) {
+    MpmGpuParticles *p = c->p;
+    OField *f = &c->f;
+    int is3d = c->g.dim == 3;
+    grid_velocity(c);
+#pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
+    for (long q = 0; q < p->n; q++) {
+        OShape s;
+        double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
+        shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, 1, &s);
+        M3 dv;
+        memset(&dv, 0, sizeof(dv));
+        for (int j = 0; j < s.n; j++) {
+            long nd = s.nds[j];
+            double vx = f->vx[nd], vy = f->vy[nd], vz = f->vz[nd];
+            if (!is3d) {
+                dv.m[0][0] += vx * s.dx[j];
+                dv.m[0][1] += vx * s.dy[j];
+                dv.m[1][0] += vy * s.dx[j];
+                dv.m[1][1] += vy * s.dy[j];
+            } else {
+                double v[3] = {vx, vy, vz}, gr[3] = {s.dx[j], s.dy[j], s.dz[j]};
+                for (int r = 0; r < 3; r++)
+                    for (int cc = 0; cc < 3; cc++) dv.m[r][cc] += v[r] * gr[cc];
+            }
+        }
+        for (int r = 0; r < 3; r++)
+            for (int cc = 0; cc < 3; cc++) dv.m[r][cc] *= strainTime;
+        const OMat *m = &c->mats[p->mat[q]];
+        hypo_increment_F(p, q, &dv, is3d);
+        if (m->type == MPMGPU_MAT_ISOTROPIC) {
+            if (is3d) iso_3d(m, p, q, &dv);
+            else iso_2d(m, p, q, &dv);
+        } else {
+            isoplastic(m, p, q, &dv, is3d);
+        }
+    }
+}
+
+/* GridForcesTask::Execute (GridForcesTask.cpp:40-153) with
+ * MatPoint2D/3D::GetFintPlusFext (MatPoint2D.cpp:242-262, MatPoint3D.cpp:248-269). */
+static void p2g_forces(OCtx *c) {
+    MpmGpuParticles *p = c->p;
+    OField *f = &c->f;
+    int is3d = c->g.dim == 3;
+#pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
+    for (long k = 0; k < p->n; k++) {
+        long q = particle_order(c, k);
+        OShape s;
+        double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
+        shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, 1, &s);
+        double mp = p->mass[q], P = p->pressure ? p->pressure[q] : 0.;
+        double sxx = p->sxx[q], syy = p->syy[q], sxy = p->sxy[q];
+        double szz = is3d ? p->szz[q] : 0., sxz = is3d ? p->sxz[q] : 0., syz = is3d ? p->syz[q] : 0.;
+        for (int j = 0; j < s.n; j++) {
+            long nd = s.nds[j];
+            double fx, fy, fz;
+            if (!is3d) {
+                fx = -mp * ((sxx - P) * s.dx[j] + sxy * s.dy[j]) + s.fn[j] * 0.;
+                fy = -mp * (sxy * s.dx[j] + (syy - P) * s.dy[j]) + s.fn[j] * 0.;
+                fz = 0.0;
+            } else {
+                fx = -mp * ((sxx - P) * s.dx[j] + sxy * s.dy[j] + sxz * s.dz[j]) + s.fn[j] * 0.;
+                fy = -mp * (sxy * s.dx[j] + (syy - P) * s.dy[j] + syz * s.dz[j]) + s.fn[j] * 0.;
+                fz = -mp * (sxz * s.dx[j] + syz * s.dy[j] + (szz - P) * s.dz[j]) + s.fn[j] * 0.;
+            }
+            if (c->nthreads > 1) {
+#pragma omp atomic
+                f->fx[nd] += fx;
+#pragma omp atomic
+                f->fy[nd] += fy;
+#pragma omp atomic
+                f->fz[nd] += fz;
+            } else {
+                f->fx[nd] += fx;
+                f->fy[nd] += fy;
+                f->fz[nd] += fz;
+            }
+        }
+    }
+}
+
+/* UpdateParticlesTask::Execute (UpdateParticlesTask.cpp:44-178),
+ * MatVelocityField::IncrementNodalVelAcc (MatVelocityField.cpp:410-426) and the
+ * FLIP branch of MatPoint2D/3D::MoveParticle (MatPoint2D.cpp:99-196) with no damping. */
+static void g2p_move(OCtx *c) {
+    MpmGpuParticles *p = c->p;
+    OField *f = &c->f;
+    int is3d = c->g.dim == 3;
+    double dt = c->dt;
+    grid_velocity(c);
+#pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
+    for (long q = 0; q < p->n; q++) {
+        OShape s;
+        double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
+        shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, 0, &s);
+        double Svx = 0., Svy = 0., Svz = 0., Sax = 0., Say = 0., Saz = 0.;
+        for (int j = 0; j < s.n; j++) {
+            long nd = s.nds[j];
+            double fi = s.fn[j];
+            Svx += f->vx[nd] * fi;
+            Svy += f->vy[nd] * fi;
+            Svz += f->vz[nd] * fi;
+            double mnode = fi / f->mass[nd];
+            Sax += f->fx[nd] * mnode;
+            Say += f->fy[nd] * mnode;
+            Saz += f->fz[nd] * mnode;
+        }
+        double vmx = Svx - Sax * dt, vmy = Svy - Say * dt, vmz = Svz - Saz * dt;
+        /* Adamp0 = 0 (no grid or particle damping) */
+        double a0x = 0. * vmx + 0. * p->vx[q], a0y = 0. * vmy + 0. * p->vy[q];
+        double dvx = (Sax - a0x) * dt, dvy = (Say - a0y) * dt;
+        p->vx[q] += dvx;
+        p->vy[q] += dvy;
+        p->x[q] += (vmx + 0.5 * dvx) * dt;
+        p->y[q] += (vmy + 0.5 * dvy) * dt;
+        if (is3d) {
+            double a0z = 0. * vmz + 0. * p->vz[q];
+            double dvz = (Saz - a0z) * dt;
+            p->vz[q] += dvz;
+            p->z[q] += (vmz + 0.5 * dvz) * dt;
+        }
+    }
+}
+
+/* ResetElementsTask::ResetElement (ResetElementsTask.cpp:196-228) with
+ * MeshInfo::FindElementFromPoint (MeshInfo.cpp:593-633) for equal elements. */
+static int reset_elements(OCtx *c) {
+    MpmGpuParticles *p = c->p;
+    const OGrid *g = &c->g;
+    int is3d = g->dim == 3;
+    int status = MPMGPU_OK;
+    for (long q = 0; q < p->n; q++) {
+        double x = p->x[q], y = p->y[q], z = is3d ? p->z[q] : 0.;
+        if (x != x || y != y || z != z) return fail(MPMGPU_ERR_NAN, "oracle: particle position is NaN");
+        double x0, x1, y0, y1, z0, z1;
+        elem_extent(g, p->elem[q], &x0, &x1, &y0, &y1, &z0, &z1);
+        int in = !(x < x0 || x >= x1) && !(y < y0 || y >= y1) && (!is3d || !(z < z0 || z >= z1));
+        if (in) continue;
+        int col = (int)((x - g->xmin) / g->gx);
+        if (col < 0 || col >= g->nx) {
+            if (x == g->xmin + g->nx * g->gx) col = g->nx - 1;
+            else status = MPMGPU_ERR_LEFT_GRID;
+        }
+        int row = (int)((y - g->ymin) / g->gy);
+        if (row < 0 || row >= g->ny) {
+            if (y == g->ymin + g->ny * g->gy) row = g->ny - 1;
+            else status = MPMGPU_ERR_LEFT_GRID;
+        }
+        int zr = 0;
+        if (is3d) {
+            zr = (int)((z - g->zmin) / g->gz);
+            if (zr < 0 || zr >= g->nz) {
+                if (z == g->zmin + g->nz * g->gz) zr = g->nz - 1;
+                else status = MPMGPU_ERR_LEFT_GRID;
+            }
+        }
+        if (status != MPMGPU_OK) return fail(status, "oracle: particle left the grid");
+        int num = is3d ? g->nx * (zr * g->ny + row) + col + 1 : row * g->nx + col + 1;
+        if (edge_element(g, num)) return fail(MPMGPU_ERR_LEFT_GRID, "oracle: particle entered an edge element");
+        p->elem[q] = num - 1;
+    }
+    return status;
+}
+
+static void zero_field(OField *f, long nn) {
+    memset(f->mass, 0, nn * sizeof(double));
+    memset(f->px, 0, nn * sizeof(double)); memset(f->py, 0, nn * sizeof(double)); memset(f->pz, 0, nn * sizeof(double));
+    memset(f->fx, 0, nn * sizeof(double)); memset(f->fy, 0, nn * sizeof(double)); memset(f->fz, 0, nn * sizeof(double));
+    memset(f->vx, 0, nn * sizeof(double)); memset(f->vy, 0, nn * sizeof(double)); memset(f->vz, 0, nn * sizeof(double));
+    memset(f->cx, 0, nn * sizeof(double)); memset(f->cy, 0, nn * sizeof(double)); memset(f->cz, 0, nn * sizeof(double));
+    memset(f->npts, 0, nn * sizeof(int));
+}
+
+/* One NairnMPM::MPMStep with the task chain of NairnMPM::CreateTasks
+ * (NairnMPM.cpp:870-1110) for FLIP, no cracks, no transport, no custom tasks. */
+static int one_step(OCtx *c) {
+    MpmGpuParticles *p = c->p;
+    OField *f = &c->f;
+    long nn = c->g.nnodes + 1;
+    int method = c->o->method;
+    double dt = c->dt;
+    double fusf = c->o->fraction_usf;
+    double stFirst = method == MPMGPU_USAVG ? fusf * dt : dt;
+    double stLast = method == MPMGPU_USAVG ? dt - stFirst : dt;
+    int is3d = c->g.dim == 3;
+
+    /* InitializationTask: zero nodes, natural coordinates */
+    zero_field(f, nn);
+    for (long q = 0; q < p->n; q++)
+        xi_pos(&c->g, p->elem[q], p->x[q], p->y[q], is3d ? p->z[q] : 0., &c->xi[3 * q]);
+
+    /* MassAndMomentumTask */
+    p2g_mass_momentum(c, 0);
+
+    /* PostExtrapolationTask: copy momenta, BCs (MASS_MOMENTUM_CALL) */
+    for (long i = 1; i < nn; i++) {
+        if (f->npts[i] > 0) { f->cx[i] = f->px[i]; f->cy[i] = f->py[i]; f->cz[i] = f->pz[i]; }
+    }
+    if (method == MPMGPU_USF || method == MPMGPU_USAVG) velocity_bc_loop(c, MASS_MOMENTUM_CALL);
+
+    /* UpdateStrainsFirstTask */
+    if (method == MPMGPU_USF || method == MPMGPU_USAVG) strain_update(c, stFirst);
+
+    /* GridForcesTask */
+    p2g_forces(c);
+
+    /* PostForcesTask: restore momenta, BCs (GRID_FORCES_CALL) */
+    for (long i = 1; i < nn; i++) {
+        if (f->npts[i] > 0) { f->px[i] = f->cx[i]; f->py[i] = f->cy[i]; f->pz[i] = f->cz[i]; }
+    }
+    velocity_bc_loop(c, GRID_FORCES_CALL);
+
+    /* UpdateMomentaTask */
+    for (long i = 1; i < nn; i++) {
+        if (f->npts[i] > 0) {
+            f->px[i] += f->fx[i] * dt;
+            f->py[i] += f->fy[i] * dt;
+            f->pz[i] += f->fz[i] * dt;
+        }
+    }
+    velocity_bc_loop(c, UPDATE_MOMENTUM_CALL);
+
+    /* UpdateParticlesTask */
+    g2p_move(c);
+
+    /* UpdateStrainsLastContactTask */
+    if (method == MPMGPU_USL || method == MPMGPU_USAVG) {
+        for (long i = 1; i < nn; i++) {
+            if (f->npts[i] > 0) { f->px[i] = 0.; f->py[i] = 0.; f->pz[i] = 0.; }
+        }
+        p2g_mass_momentum(c, 1);
+        velocity_bc_loop(c, UPDATE_STRAINS_LAST_CALL);
+        strain_update(c, stLast);
+    }
+
+    /* ResetElementsTask */
+    return reset_elements(c);
+}
+
+int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmGpuMaterial *mats, int nmat,
+                   const MpmGpuVelBC *bcs, int nbc, const MpmGpuContact *contact, MpmGpuParticles *p,
+                   int nsteps, double t0, int nthreads) {
+    g_err[0] = 0;
+    if (!grid || !opts || !mats || !p) return fail(MPMGPU_ERR_INVALID, "oracle: null argument");
+    if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP)
+        return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: shape function not implemented");
+    if (contact && contact->enabled) return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: contact not implemented");
+    OCtx c;
+    memset(&c, 0, sizeof(c));
+    c.g.dim = grid->dim;
+    c.g.nx = grid->nx; c.g.ny = grid->ny; c.g.nz = grid->dim == 3 ? grid->nz : 0;
+    c.g.xplane = 1;
+    c.g.yplane = grid->nx + 1;
+    c.g.zplane = (long)(grid->nx + 1) * (grid->ny + 1);
+    c.g.nnodes = grid->dim == 3 ? c.g.zplane * (grid->nz + 1) : c.g.zplane;
+    c.g.nelems = (long)grid->nx * grid->ny * (grid->dim == 3 ? grid->nz : 1);
+    c.g.xn = grid->xnodes; c.g.yn = grid->ynodes; c.g.zn = grid->znodes;
+    c.g.xmin = grid->xmin; c.g.ymin = grid->ymin; c.g.zmin = grid->zmin;
+    c.g.gx = grid->dx; c.g.gy = grid->dy; c.g.gz = grid->dz;
+    c.o = opts;
+    c.bcs = bcs;
+    c.nbc = nbc;
+    c.p = p;
+    c.dt = opts->timestep;
+    c.nthreads = nthreads < 1 ? 1 : nthreads;
+    c.mats = (OMat *)calloc((size_t)nmat, sizeof(OMat));
+    int np = grid->dim == 3 ? MPMGPU_THREED : MPMGPU_PLANE_STRAIN;
+    int st = load_materials(mats, nmat, np, c.mats);
+    if (st != MPMGPU_OK) { free(c.mats); return st; }
+    long nn = c.g.nnodes + 1;
+    double **fl[] = {&c.f.mass, &c.f.px, &c.f.py, &c.f.pz, &c.f.fx, &c.f.fy, &c.f.fz,
+                     &c.f.vx, &c.f.vy, &c.f.vz, &c.f.cx, &c.f.cy, &c.f.cz};
+    for (unsigned k = 0; k < sizeof(fl) / sizeof(fl[0]); k++) *fl[k] = (double *)calloc((size_t)nn, sizeof(double));
+    c.f.npts = (int *)calloc((size_t)nn, sizeof(int));
+    c.xi = (double *)calloc((size_t)(3 * (p->n > 0 ? p->n : 1)), sizeof(double));
+    c.mtime = t0;
+    for (int s = 0; s < nsteps && st == MPMGPU_OK; s++) {
+        st = one_step(&c);
+        c.mtime += c.dt;
+    }
+    for (unsigned k = 0; k < sizeof(fl) / sizeof(fl[0]); k++) free(*fl[k]);
+    free(c.f.npts);
+    free(c.xi);
+    free(c.mats);
+    return st;
+}
