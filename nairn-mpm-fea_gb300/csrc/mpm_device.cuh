@@ -1,0 +1,393 @@
+// mpm_device.cuh -- device data structures and per-particle math of the
+// explicit MPM step: GIMP/linear shape functions, the hypoelastic isotropic law
+// and J2 plasticity with linear hardening.  Every function restates one
+// reference function, cited beside it (paths relative to nairn-mpm-fea).
+#pragma once
+
+#include <cstdint>
+
+namespace nmg {
+
+constexpr double kSqrtTwoThirds = 0.8164965809277260;  // sqrt(2/3)
+
+// error bits raised by kernels (reported through the C ABI status)
+enum : unsigned { ERR_NAN = 1u, ERR_LEFT_GRID = 2u, ERR_EDGE = 4u };
+
+struct DevGrid {
+    int dim, nx, ny, nz;
+    int xplane, yplane, zplane, nnodes;  // node-number strides, node count
+    double xmin, ymin, zmin, gx, gy, gz;  // origin and cell size (MeshInfo)
+    const double *xn, *yn, *zn;           // node coordinates per axis
+};
+
+// Specific material constants, derived on the host exactly as the reference's
+// VerifyAndLoadProperties does.
+struct DevMat {
+    int type;
+    int field;
+    double c11, c12, c22, c33, c41, c42, c44;    // 2D: Elastic::FillUnrotatedElasticProperties
+    double C00, C01, C02, C11, C12, C22, C33, C44, C55;  // 3D specific stiffness
+    double Gred, Kred;                           // IsoPlasticity specific moduli
+    double yldred, Epred, alphaMax, yldredMin;   // LinearHardening
+};
+
+struct DevParticles {
+    int n;
+    double *x, *y, *z, *vx, *vy, *vz;
+    double *mass;
+    int *mat, *elem;
+    double *lpx, *lpy, *lpz;
+    double *exx, *eyy, *ezz, *exy, *exz, *eyz, *wxy, *wxz, *wyz;
+    double *sxx, *syy, *szz, *sxy, *sxz, *syz, *pressure;
+    double *pxx, *pyy, *pzz, *pxy, *pxz, *pyz;
+    double *hist0, *hist1, *work, *plast;
+    double *xi, *eta, *zeta;   // natural coordinates of the step (ncpos)
+};
+
+struct DevNodes {
+    double *mass;
+    double *px, *py, *pz;      // momentum
+    double *fx, *fy, *fz;      // total force
+    double *cx, *cy, *cz;      // copy of extrapolated momentum (vk[pkCopy])
+    double *vx, *vy, *vz;      // velocity p/m
+    double *ux, *uy, *uz;      // second (update-strains-last) momentum extrapolation
+    unsigned char *active;     // numberPoints > 0
+};
+
+// Velocity conditions grouped by node, list order kept inside a node.
+struct DevBCs {
+    int nnodes_bc;
+    const int *node;           // 0-based node index per group
+    const int *start;          // group g uses entries [start[g], start[g+1])
+    const int *dir;            // 1, 2, 4
+    const double *value;
+    const double *ftime;
+};
+
+// ---------------------------------------------------------------------------
+// element geometry
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void elem_coords(const DevGrid &g, int e, int &col, int &row, int &zr) {
+    col = e % g.nx;
+    int r = e / g.nx;
+    row = r % g.ny;
+    zr = g.dim == 3 ? r / g.ny : 0;
+}
+
+// FourNodeIsoparam::GetXiPos / EightNodeIsoparamBrick::GetXiPos for
+// rectangular elements (Common/Elements/FourNodeIsoparam.cpp:351-366,
+// NairnMPM/src/Elements/EightNodeIsoparamBrick.cpp:276-281).
+__device__ __forceinline__ void xi_position(const DevGrid &g, int e, double x, double y, double z,
+                                            double &xi, double &eta, double &zeta) {
+    int col, row, zr;
+    elem_coords(g, e, col, row, zr);
+    double x0 = g.xn[col], x1 = g.xn[col + 1];
+    double y0 = g.yn[row], y1 = g.yn[row + 1];
+    xi = (2. * x - x0 - x1) / (x1 - x0);
+    eta = (2. * y - y0 - y1) / (y1 - y0);
+    if (g.dim == 3) {
+        double z0 = g.zn[zr], z1 = g.zn[zr + 1];
+        zeta = (2. * z - z0 - z1) / (z1 - z0);
+    } else {
+        zeta = 0.;
+    }
+}
+
+// ---------------------------------------------------------------------------
+// uGIMP, evaluated per axis.  Candidate k = 0..3 sits at natural coordinate
+// 2k-3 (i.e. -3,-1,1,3) and at node offset k-1 from the element's first node.
+// FourNodeIsoparam::GimpShapeFunction (FourNodeIsoparam.cpp:431-519) and
+// EightNodeIsoparamBrick::GimpShapeFunction (EightNodeIsoparamBrick.cpp:289-403)
+// compute the same 1D factors inline; the products below keep their order.
+// ---------------------------------------------------------------------------
+struct Axis {
+    double S[4];
+    double dS[4];   // sign * dS
+    unsigned act;   // bit k set when candidate k is inside the support
+};
+
+// inv_size is 1/(4*lp) of this axis (3D z uses lp.y, as the reference does)
+template <bool kThreeD, bool kGrad>
+__device__ __forceinline__ void gimp_axis(double xi, double lp, double inv_size, Axis &a) {
+    const double q1 = 2. - lp, q2 = 2. + lp;
+    a.act = 0u;
+#pragma unroll
+    for (int k = 0; k < 4; k++) {
+        const double gk = (double)(2 * k - 3);
+        const double xp = fabs(xi - gk);
+        double S = 0., dS = 0.;
+        if (xp < q2) {
+            a.act |= 1u << k;
+            double arg = 0.;
+            if (xp < lp) {
+                S = ((4. - lp) * lp - xp * xp) * inv_size;
+            } else if (xp <= q1) {
+                S = kThreeD ? 0.5 * (2. - xp) : (2. - xp) / 2.;
+            } else {
+                arg = (q2 - xp) * inv_size;
+                S = 2. * lp * arg * arg;
+            }
+            if (kGrad) {
+                const double sgn = xi > gk ? 1. : -1.;
+                double d;
+                if (xp < lp) d = kThreeD ? -xp / (2. * lp) : -xp * inv_size * 2.0;
+                else if (xp <= q1) d = -0.5;
+                else d = -arg;
+                dS = sgn * d;
+            }
+        }
+        a.S[k] = S;
+        a.dS[k] = dS;
+    }
+}
+
+// candidate order of the reference tables, packed (k_x | k_y<<2 | k_z<<4)
+__constant__ unsigned char c_cand2d[16] = {
+    0x05, 0x06, 0x0A, 0x09, 0x00, 0x01, 0x02, 0x03, 0x07, 0x0B, 0x0F, 0x0E, 0x0D, 0x0C, 0x08, 0x04};
+__constant__ unsigned char c_cand3d[64] = {
+    0x15, 0x16, 0x1A, 0x19, 0x25, 0x26, 0x2A, 0x29,
+    0x10, 0x11, 0x12, 0x13, 0x17, 0x1B, 0x1F, 0x1E, 0x1D, 0x1C, 0x18, 0x14,
+    0x20, 0x21, 0x22, 0x23, 0x27, 0x2B, 0x2F, 0x2E, 0x2D, 0x2C, 0x28, 0x24,
+    0x05, 0x06, 0x0A, 0x09, 0x00, 0x01, 0x02, 0x03, 0x07, 0x0B, 0x0F, 0x0E, 0x0D, 0x0C, 0x08, 0x04,
+    0x35, 0x36, 0x3A, 0x39, 0x30, 0x31, 0x32, 0x33, 0x37, 0x3B, 0x3F, 0x3E, 0x3D, 0x3C, 0x38, 0x34};
+
+// ---------------------------------------------------------------------------
+// Constitutive updates (FP64).  du is the velocity gradient times the strain
+// time step, row-major 3x3.
+// ---------------------------------------------------------------------------
+
+// Elastic::HypoIncrementDeformation (NairnMPM/src/Materials/ElasticMPM.cpp:392-403):
+// F <- (I + du) F with F kept as strain ep and rotation wrot
+// (MatPoint2D.cpp:309-366, MatPoint3D.cpp:320-376; Matrix3.cpp:312-351, 920-966).
+__device__ __forceinline__ void hypo_increment_F_2d(const DevParticles &p, int i, const double du[9]) {
+    const double a00 = 1. + du[0], a01 = du[1], a10 = du[3], a11 = 1. + du[4], a22 = 1. + du[8];
+    const double exy = p.exy[i], wxy = p.wxy[i];
+    const double b00 = 1. + p.exx[i], b01 = 0.5 * (exy - wxy), b10 = 0.5 * (exy + wxy), b11 = 1. + p.eyy[i],
+                 b22 = 1. + p.ezz[i];
+    const double f00 = a00 * b00 + a01 * b10;
+    const double f01 = a00 * b01 + a01 * b11;
+    const double f10 = a10 * b00 + a11 * b10;
+    const double f11 = a10 * b01 + a11 * b11;
+    const double f22 = a22 * b22;
+    p.exx[i] = f00 - 1.;
+    p.eyy[i] = f11 - 1.;
+    p.ezz[i] = f22 - 1.;
+    p.exy[i] = f10 + f01;
+    p.wxy[i] = f10 - f01;
+}
+
+__device__ __forceinline__ void hypo_increment_F_3d(const DevParticles &p, int i, const double du[9]) {
+    double b[9];
+    const double exy = p.exy[i], exz = p.exz[i], eyz = p.eyz[i];
+    const double wxy = p.wxy[i], wxz = p.wxz[i], wyz = p.wyz[i];
+    b[0] = 1. + p.exx[i];
+    b[4] = 1. + p.eyy[i];
+    b[8] = 1. + p.ezz[i];
+    b[1] = 0.5 * (exy - wxy);
+    b[3] = 0.5 * (exy + wxy);
+    b[2] = 0.5 * (exz - wxz);
+    b[6] = 0.5 * (exz + wxz);
+    b[5] = 0.5 * (eyz - wyz);
+    b[7] = 0.5 * (eyz + wyz);
+    double f[9];
+#pragma unroll
+    for (int r = 0; r < 3; r++) {
+        const double a0 = du[3 * r] + (r == 0 ? 1. : 0.);
+        const double a1 = du[3 * r + 1] + (r == 1 ? 1. : 0.);
+        const double a2 = du[3 * r + 2] + (r == 2 ? 1. : 0.);
+#pragma unroll
+        for (int c = 0; c < 3; c++) f[3 * r + c] = a0 * b[c] + a1 * b[3 + c] + a2 * b[6 + c];
+    }
+    p.exx[i] = f[0] - 1.;
+    p.eyy[i] = f[4] - 1.;
+    p.ezz[i] = f[8] - 1.;
+    p.exy[i] = f[3] + f[1];
+    p.exz[i] = f[6] + f[2];
+    p.eyz[i] = f[7] + f[5];
+    p.wxy[i] = f[3] - f[1];
+    p.wxz[i] = f[6] - f[2];
+    p.wyz[i] = f[7] - f[5];
+}
+
+// IsotropicMat::SRConstitutiveLaw2D, plane strain without residual strains
+// (NairnMPM/src/Materials/MoreIsotropicMat.cpp:185-279) and
+// MaterialBase::Hypo2DCalculations (MaterialBaseMPM.cpp:1012-1020).
+__device__ __forceinline__ void iso_law_2d(const DevMat &m, const DevParticles &p, int i, const double du[9]) {
+    const double dvxx = du[0], dvyy = du[4];
+    const double dgam = du[1] + du[3];
+    const double dwrotxy = du[3] - du[1];
+    const double s0xx = p.sxx[i], s0yy = p.syy[i], s0xy = p.sxy[i], s0zz = p.szz[i];
+    const double c1 = m.c11 * dvxx + m.c12 * dvyy;
+    const double c2 = m.c12 * dvxx + m.c22 * dvyy;
+    const double c3 = m.c33 * dgam;
+    const double dnorm = dwrotxy * s0xy;
+    const double dshear = 0.5 * dwrotxy * (s0xx - s0yy);
+    const double sxx = s0xx + (c1 - dnorm);
+    const double syy = s0yy + (c2 + dnorm);
+    const double sxy = s0xy + (c3 + dshear);
+    const double szz = s0zz + (m.c41 * dvxx + m.c42 * dvyy);
+    p.sxx[i] = sxx;
+    p.syy[i] = syy;
+    p.sxy[i] = sxy;
+    p.szz[i] = szz;
+    p.work[i] += 0.5 * ((s0xx + sxx) * dvxx + (s0yy + syy) * dvyy + (s0xy + sxy) * dgam);
+}
+
+// IsotropicMat::SRConstitutiveLaw3D (MoreIsotropicMat.cpp:286-348) with
+// MaterialBase::Hypo3DCalculations (MaterialBaseMPM.cpp:1026-1047).
+__device__ __forceinline__ void iso_law_3d(const DevMat &m, const DevParticles &p, int i, const double du[9]) {
+    const double dvxx = du[0], dvyy = du[4], dvzz = du[8];
+    const double dgamxy = du[1] + du[3], dgamxz = du[2] + du[6], dgamyz = du[5] + du[7];
+    const double dwxy = du[3] - du[1], dwxz = du[6] - du[2], dwyz = du[7] - du[5];
+    const double s0xx = p.sxx[i], s0yy = p.syy[i], s0zz = p.szz[i];
+    const double s0yz = p.syz[i], s0xz = p.sxz[i], s0xy = p.sxy[i];
+    const double d0 = m.C00 * dvxx + m.C01 * dvyy + m.C02 * dvzz;
+    const double d1 = m.C01 * dvxx + m.C11 * dvyy + m.C12 * dvzz;
+    const double d2 = m.C02 * dvxx + m.C12 * dvyy + m.C22 * dvzz;
+    const double d3 = m.C33 * dgamyz, d4 = m.C44 * dgamxz, d5 = m.C55 * dgamxy;
+    const double stxx = -dwxy * s0xy - dwxz * s0xz;
+    const double styy = dwxy * s0xy - dwyz * s0yz;
+    const double stzz = dwxz * s0xz + dwyz * s0yz;
+    const double styz = 0.5 * (dwxy * s0xz + dwxz * s0xy + dwyz * (s0yy - s0zz));
+    const double stxz = 0.5 * (-dwxy * s0yz + dwxz * (s0xx - s0zz) + dwyz * s0xy);
+    const double stxy = 0.5 * (dwxy * (s0xx - s0yy) - dwxz * s0yz - dwyz * s0xz);
+    const double sxx = s0xx + (d0 + stxx), syy = s0yy + (d1 + styy), szz = s0zz + (d2 + stzz);
+    const double syz = s0yz + (d3 + styz), sxz = s0xz + (d4 + stxz), sxy = s0xy + (d5 + stxy);
+    p.sxx[i] = sxx;
+    p.syy[i] = syy;
+    p.szz[i] = szz;
+    p.syz[i] = syz;
+    p.sxz[i] = sxz;
+    p.sxy[i] = sxy;
+    p.work[i] += 0.5 * ((s0xx + sxx) * dvxx + (s0yy + syy) * dvyy + (s0zz + szz) * dvzz + (s0yz + syz) * dgamyz +
+                        (s0xz + sxz) * dgamxz + (s0xy + sxy) * dgamxy);
+}
+
+// IsoPlasticity::MPMConstitutiveLaw + PlasticityConstLaw, small rotation, no
+// residual strains (NairnMPM/src/Materials/IsoPlasticity.cpp:128-451), with
+// UpdatePressure (:462-492), IsotropicMat::GetMagnitudeSFromDev
+// (MoreIsotropicMat.cpp:356-370) and LinearHardening's closed-form return
+// (LinearHardening.cpp:124-145).  Stress on the particle is deviatoric; the
+// pressure is carried separately.
+template <bool kThreeD>
+__device__ __forceinline__ void plastic_law(const DevMat &m, const DevParticles &p, int i, const double de[9]) {
+    const double dexx = de[0], deyy = de[4], dezz = de[8];
+    const double delV = dexx + deyy + dezz;
+    const double dgxy = de[1] + de[3];
+    const double dgxz = kThreeD ? de[2] + de[6] : 0.;
+    const double dgyz = kThreeD ? de[5] + de[7] : 0.;
+    // UpdatePressure
+    const double Pfinal = p.pressure[i] + (-m.Kred * delV);
+    p.pressure[i] = Pfinal;
+    double work = p.work[i] + (-Pfinal * delV);   // work energy accumulates in the reference's order
+    // rotate plastic strain and stress
+    const double dwxy = de[3] - de[1];
+    const double epxx = p.pxx[i], epyy = p.pyy[i], epzz = p.pzz[i], epxy = p.pxy[i];
+    const double spxx = p.sxx[i], spyy = p.syy[i], spzz = p.szz[i], spxy = p.sxy[i];
+    double epxz = 0., epyz = 0., spxz = 0., spyz = 0.;
+    double s0xx, s0yy, s0zz, s0xy, s0xz = 0., s0yz = 0.;
+    double qxx, qyy, qzz, qxy, qxz = 0., qyz = 0.;   // rotated plastic strain
+    if (!kThreeD) {
+        const double dnorm = 0.5 * dwxy * epxy;
+        qxx = epxx - dnorm;
+        qyy = epyy + dnorm;
+        qzz = epzz;
+        qxy = epxy + dwxy * (epxx - epyy);
+        const double dn = dwxy * spxy;
+        s0xx = spxx - dn;
+        s0yy = spyy + dn;
+        s0zz = spzz;
+        s0xy = spxy + 0.5 * dwxy * (epxx - epyy);
+    } else {
+        epxz = p.pxz[i];
+        epyz = p.pyz[i];
+        spxz = p.sxz[i];
+        spyz = p.syz[i];
+        const double dwxz = de[6] - de[2], dwyz = de[7] - de[5];
+        const double dxy = 0.5 * dwxy * epxy, dxz = 0.5 * dwxz * epxz, dyz = 0.5 * dwyz * epyz;
+        qxx = epxx + (-dxy - dxz);
+        qyy = epyy + (dxy - dyz);
+        qzz = epzz + (dxz + dyz);
+        qyz = epyz + (dwyz * (epyy - epzz) + 0.5 * (dwxz * epxy + dwxy * epxz));
+        qxz = epxz + (dwxz * (epxx - epzz) + 0.5 * (dwyz * epxy - dwxy * epyz));
+        qxy = epxy + (dwxy * (epxx - epyy) - 0.5 * (dwyz * epxz + dwxz * epyz));
+        const double sxy = dwxy * spxy, sxz = dwxz * spxz, syz = dwyz * spyz;
+        s0xx = spxx + (-sxy - sxz);
+        s0yy = spyy + (sxy - syz);
+        s0zz = spzz + (sxz + syz);
+        s0yz = spyz + 0.5 * (dwyz * (spyy - spzz) + dwxz * spxy + dwxy * spxz);
+        s0xz = spxz + 0.5 * (dwxz * (spxx - spzz) + dwyz * spxy - dwxy * spyz);
+        s0xy = spxy + 0.5 * (dwxy * (spxx - spyy) - dwyz * spxz - dwxz * spyz);
+    }
+    // trial deviatoric stress
+    const double third = delV / 3.;
+    const double G = m.Gred;
+    const double trxx = s0xx + 2. * G * (dexx - third);
+    const double tryy = s0yy + 2. * G * (deyy - third);
+    const double trzz = s0zz + 2. * G * (dezz - third);
+    const double trxy = s0xy + G * dgxy;
+    const double tryz = kThreeD ? s0yz + G * dgyz : 0.;
+    const double trxz = kThreeD ? s0xz + G * dgxz : 0.;
+    const double alpint = p.hist0[i];
+    const double s2 = trxx * trxx + tryy * tryy + trzz * trzz;
+    const double t2 = kThreeD ? trxy * trxy + trxz * trxz + tryz * tryz : trxy * trxy;
+    const double smag = sqrt(s2 + t2 + t2);
+    const double yld = alpint < m.alphaMax ? m.yldred + m.Epred * alpint : m.yldredMin;
+    if (smag - kSqrtTwoThirds * yld < 0.) {
+        p.sxx[i] = trxx;
+        p.syy[i] = tryy;
+        p.szz[i] = trzz;
+        p.sxy[i] = trxy;
+        p.pxx[i] = qxx;
+        p.pyy[i] = qyy;
+        p.pzz[i] = qzz;
+        p.pxy[i] = qxy;
+        if (kThreeD) {
+            p.syz[i] = tryz;
+            p.sxz[i] = trxz;
+            p.pxz[i] = qxz;
+            p.pyz[i] = qyz;
+            work += trxx * dexx + tryy * deyy + trzz * dezz + tryz * dgyz + trxz * dgxz + trxy * dgxy;
+        } else {
+            work += trxx * dexx + tryy * deyy + trxy * dgxy;
+        }
+        p.work[i] = work;
+        return;
+    }
+    // radial return
+    double lam = (smag - kSqrtTwoThirds * (m.yldred + m.Epred * alpint)) / (2. * (G + m.Epred / 3.));
+    if (alpint + kSqrtTwoThirds * lam > m.alphaMax) lam = (smag - kSqrtTwoThirds * m.yldredMin) / (2. * G);
+    const double alpnew = alpint + kSqrtTwoThirds * lam;
+    const double dpxx = lam * (trxx / smag), dpyy = lam * (tryy / smag), dpzz = lam * (trzz / smag);
+    const double dpxy = 2. * lam * (trxy / smag);
+    const double dpxz = kThreeD ? 2. * lam * (trxz / smag) : 0.;
+    const double dpyz = kThreeD ? 2. * lam * (tryz / smag) : 0.;
+    const double sxx = trxx - 2. * G * dpxx, syy = tryy - 2. * G * dpyy, szz = trzz - 2. * G * dpzz;
+    const double sxy = trxy - G * dpxy;
+    p.sxx[i] = sxx;
+    p.syy[i] = syy;
+    p.szz[i] = szz;
+    p.sxy[i] = sxy;
+    p.pxx[i] = qxx + dpxx;
+    p.pyy[i] = qyy + dpyy;
+    p.pzz[i] = qzz + dpzz;
+    p.pxy[i] = qxy + dpxy;
+    double w = sxx * dexx + syy * deyy + sxy * dgxy;
+    double pe = sxx * dpxx + syy * dpyy + szz * dpzz + sxy * dpxy;
+    if (kThreeD) {
+        const double syz = tryz - G * dpyz, sxz = trxz - G * dpxz;
+        p.syz[i] = syz;
+        p.sxz[i] = sxz;
+        p.pxz[i] = qxz + dpxz;
+        p.pyz[i] = qyz + dpyz;
+        w += szz * dezz + syz * dgyz + sxz * dgxz;
+        w += szz * dezz;   // the reference adds the zz term again when np != plane strain
+        pe += sxz * dpxz + syz * dpyz;
+    }
+    p.work[i] = work + w;
+    const double qdalpha = lam * kSqrtTwoThirds * fmax(m.Epred * alpnew, m.yldredMin - m.yldred);
+    p.plast[i] += pe - qdalpha;
+    p.hist0[i] = alpnew;
+}
+
+}  // namespace nmg

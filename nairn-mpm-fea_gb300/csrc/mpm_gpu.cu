@@ -1,0 +1,598 @@
+// mpm_gpu.cu -- C ABI (include/nairn_mpm_gpu.h) of the GB300 explicit MPM step.
+//
+// One context = one run resident on the current device: particle state as
+// structure-of-arrays FP64 columns, the background grid node fields, the
+// material table and the velocity conditions grouped by node.  mpmgpu_step()
+// enqueues the step kernels (mpm_kernels.cuh) on the context stream and checks
+// the device error word once per call.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <map>
+#include <string>
+#include <vector>
+
+#include "mpm_kernels.cuh"
+#include "nairn_mpm_gpu.h"
+#include "sort.cuh"
+
+using namespace nmg;
+
+namespace {
+
+const int kParticleDoubles = 38;  // double columns of DevParticles besides zeta
+
+struct Profile {
+    const char *name;
+    cudaEvent_t a, b;
+    double ms;
+};
+
+}  // namespace
+
+struct MpmGpuCtx {
+    MpmGpuOptions opts{};
+    int dim = 2;
+    DevGrid g{};
+    DevParticles p{};
+    DevNodes nd{};
+    DevBCs bcs{};
+    int *bc_group = nullptr;
+    DevMat *mats = nullptr;
+    int nmat = 0;
+    std::vector<DevMat> hmats;
+    double *grid_coords = nullptr;
+    double *pblock = nullptr;            // particle double columns
+    int *iblock = nullptr;               // mat, elem, original index
+    int *orig = nullptr;                 // original (host) index of each slot
+    double *nblock = nullptr;            // node double columns
+    size_t nblock_zero_bytes = 0;        // bytes cleared at each step start
+    unsigned char *active = nullptr;
+    unsigned *err = nullptr;
+    void *bc_block = nullptr;
+    cudaStream_t stream = nullptr;
+    SortWorkspace sort{};
+    long long steps_done = 0;
+    std::string msg;
+    std::vector<Profile> prof;
+    bool profile = false;
+};
+
+namespace {
+
+std::string g_static_err;
+
+int set_err(MpmGpuCtx *c, int code, const std::string &m) {
+    if (c) c->msg = m;
+    else g_static_err = m;
+    return code;
+}
+
+int cuda_fail(MpmGpuCtx *c, cudaError_t e, const char *where) {
+    return set_err(c, MPMGPU_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
+}
+
+#define CK(call)                                            \
+    do {                                                    \
+        cudaError_t e_ = (call);                            \
+        if (e_ != cudaSuccess) return cuda_fail(c, e_, #call); \
+    } while (0)
+
+// Elastic::SetAnalysisProps + FillUnrotatedElasticProperties for an isotropic
+// material (Common/Materials/Elastic.cpp:43-160, 194-330), IsotropicMat
+// (Common/Materials/IsotropicMat.cpp:93-170), IsoPlasticity (IsoPlasticity.cpp:58-65),
+// HardeningLawBase/LinearHardening::VerifyAndLoadProperties (LinearHardening.cpp:45-58).
+int derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::string &why) {
+    std::memset(&m, 0, sizeof(m));
+    m.type = in.type;
+    m.field = in.field;
+    if (in.type != MPMGPU_MAT_ISOTROPIC && in.type != MPMGPU_MAT_ISOPLASTICITY) {
+        why = "material type " + std::to_string(in.type) + " is not implemented on the device";
+        return MPMGPU_ERR_UNSUPPORTED;
+    }
+    const double rho = in.rho * 0.001;
+    const double E = in.E * 1.e6, nu = in.nu;
+    if (!(rho > 0.) || !(E > 0.)) {
+        why = "material needs rho > 0 and E > 0";
+        return MPMGPU_ERR_INVALID;
+    }
+    const double G = E / (2. * (1. + nu));
+    const double e1 = E, e2 = E, e3 = E, v12 = nu, v13 = nu, v23 = nu;
+    const double v32 = v23 * e3 / e2, v31 = v13 * e3 / e1, v21 = v12 * e2 / e1;
+    const double rrho = 1. / rho;
+    double C33;
+    if (np == MPMGPU_THREED) {
+        const double xx = 1. - v13 * v31 - v23 * v32 - v12 * v21 - 2. * v13 * v32 * v21;
+        const double C11 = e1 * (1. - v23 * v32) / xx, C12 = e2 * (v12 + v13 * v32) / xx;
+        const double C13 = e3 * (v13 + v12 * v23) / xx, C22 = e2 * (1. - v13 * v31) / xx;
+        const double C23 = e3 * (v23 + v21 * v13) / xx;
+        C33 = e3 * (1. - v21 * v12) / xx;
+        m.C00 = C11 * rrho;
+        m.C01 = C12 * rrho;
+        m.C02 = C13 * rrho;
+        m.C11 = C22 * rrho;
+        m.C12 = C23 * rrho;
+        m.C22 = C33 * rrho;
+        m.C33 = G * rrho;
+        m.C44 = G * rrho;
+        m.C55 = G * rrho;
+    } else {
+        const double xx = 1. - v13 * v31 - v23 * v32 - v12 * v21 - 2. * v12 * v23 * v31;
+        const double C11 = e1 * (1. - v23 * v32) / xx, C12 = e2 * (v12 + v13 * v32) / xx;
+        const double C22 = e2 * (1. - v13 * v31) / xx;
+        const double C13 = e3 * (v13 + v12 * v23) / xx, C23 = e3 * (v23 + v21 * v13) / xx;
+        C33 = e3 * (1. - v21 * v12) / xx;
+        m.c11 = C11 * rrho;
+        m.c12 = C12 * rrho;
+        m.c22 = C22 * rrho;
+        m.c33 = G * rrho;
+        m.c41 = C13 * rrho;
+        m.c42 = C23 * rrho;
+        m.c44 = C33 * rrho;
+    }
+    m.Gred = G / rho;
+    m.Kred = C33 / rho - 4. * m.Gred / 3.;
+    if (in.type == MPMGPU_MAT_ISOPLASTICITY) {
+        const double yield = in.yield * 1.e6, Ep = in.Ep * 1.e6;
+        if (!(yield > 0.)) {
+            why = "isoplasticity needs yield > 0";
+            return MPMGPU_ERR_INVALID;
+        }
+        m.yldred = yield / rho;
+        m.yldredMin = 0. / rho;
+        const double beta = Ep >= 0. ? Ep / yield : 0.;
+        m.Epred = m.yldred * beta;
+        m.alphaMax = 1.e50;
+        if (beta < 0.) m.alphaMax = ((m.yldredMin / m.yldred) - 1.) / beta;
+    }
+    return MPMGPU_OK;
+}
+
+// Point the particle columns at a block of kParticleDoubles+1 double columns
+// (the last three are the step's natural coordinates) and 3 int columns.
+void link_columns(DevParticles &p, double *pb, int *ib, int **orig) {
+    const size_t n = (size_t)p.n;
+    double **cols[kParticleDoubles + 1] = {&p.x, &p.y, &p.z, &p.vx, &p.vy, &p.vz, &p.mass, &p.lpx, &p.lpy, &p.lpz,
+                                           &p.exx, &p.eyy, &p.ezz, &p.exy, &p.exz, &p.eyz, &p.wxy, &p.wxz, &p.wyz,
+                                           &p.sxx, &p.syy, &p.szz, &p.sxy, &p.sxz, &p.syz, &p.pressure,
+                                           &p.pxx, &p.pyy, &p.pzz, &p.pxy, &p.pxz, &p.pyz,
+                                           &p.hist0, &p.hist1, &p.work, &p.plast, &p.xi, &p.eta, &p.zeta};
+    for (int k = 0; k <= kParticleDoubles; k++) *cols[k] = pb + (size_t)k * n;
+    p.mat = ib;
+    p.elem = ib + n;
+    *orig = ib + 2 * n;
+}
+
+// the matching host columns of MpmGpuParticles (nullptr for the natural coordinates)
+void hcols(const MpmGpuParticles *h, double *out[kParticleDoubles]) {
+    double *tmp[kParticleDoubles] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->mass, h->lpx, h->lpy, h->lpz,
+                                     h->exx, h->eyy, h->ezz, h->exy, h->exz, h->eyz, h->wxy, h->wxz, h->wyz,
+                                     h->sxx, h->syy, h->szz, h->sxy, h->sxz, h->syz, h->pressure,
+                                     h->pxx, h->pyy, h->pzz, h->pxy, h->pxz, h->pyz,
+                                     h->hist0, h->hist1, h->work, h->plast, nullptr, nullptr};
+    std::memcpy(out, tmp, sizeof(tmp));
+}
+
+void free_particles(MpmGpuCtx *c) {
+    if (c->pblock) cudaFree(c->pblock);
+    if (c->iblock) cudaFree(c->iblock);
+    c->pblock = nullptr;
+    c->iblock = nullptr;
+    sort_free(c->sort);
+    c->p.n = 0;
+}
+
+}  // namespace
+
+void nmg::relink_particles(DevParticles &p, double *pblock, int *iblock, int **orig) {
+    link_columns(p, pblock, iblock, orig);
+}
+
+extern "C" {
+
+int mpmgpu_abi_version(void) { return MPMGPU_ABI_VERSION; }
+
+const char *mpmgpu_last_error(const MpmGpuCtx *c) { return c ? c->msg.c_str() : g_static_err.c_str(); }
+
+int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx **out) {
+    MpmGpuCtx *c = nullptr;
+    if (!grid || !opts || !out) return set_err(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_create: null argument");
+    *out = nullptr;
+    if (grid->dim != 2 && grid->dim != 3) return set_err(nullptr, MPMGPU_ERR_INVALID, "grid dim must be 2 or 3");
+    if ((grid->dim == 3) != (opts->np == MPMGPU_THREED) ||
+        (grid->dim == 2 && opts->np != MPMGPU_PLANE_STRAIN))
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "analysis type must be 2D plane strain or 3D");
+    if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
+    if (opts->method != MPMGPU_USF && opts->method != MPMGPU_USAVG && opts->method != MPMGPU_USL)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
+    if (opts->precision != MPMGPU_PREC_FP64)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "only the FP64 transfer mode is built in this library");
+    if (opts->nfields > 1)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "multimaterial contact is not implemented on the device");
+    if (!(opts->timestep > 0.)) return set_err(nullptr, MPMGPU_ERR_INVALID, "timestep must be > 0");
+    if (grid->nx < 3 || grid->ny < 3 || (grid->dim == 3 && grid->nz < 3) || !grid->xnodes || !grid->ynodes ||
+        (grid->dim == 3 && !grid->znodes))
+        return set_err(nullptr, MPMGPU_ERR_INVALID, "grid needs >= 3 elements per axis and node coordinates");
+    long long nn = (long long)(grid->nx + 1) * (grid->ny + 1) * (grid->dim == 3 ? grid->nz + 1 : 1);
+    if (nn > (1LL << 30)) return set_err(nullptr, MPMGPU_ERR_INVALID, "grid too large");
+    c = new MpmGpuCtx();
+    c->opts = *opts;
+    if (c->opts.sort_interval < 0) c->opts.sort_interval = 0;
+    c->dim = grid->dim;
+    DevGrid &g = c->g;
+    g.dim = grid->dim;
+    g.nx = grid->nx;
+    g.ny = grid->ny;
+    g.nz = grid->dim == 3 ? grid->nz : 0;
+    g.xplane = 1;
+    g.yplane = grid->nx + 1;
+    g.zplane = (grid->nx + 1) * (grid->ny + 1);
+    g.nnodes = (int)nn;
+    g.xmin = grid->xmin;
+    g.ymin = grid->ymin;
+    g.zmin = grid->zmin;
+    g.gx = grid->dx;
+    g.gy = grid->dy;
+    g.gz = grid->dz;
+    cudaError_t e;
+    if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
+        int st = cuda_fail(nullptr, e, "cudaStreamCreate");
+        delete c;
+        return st;
+    }
+    size_t ncoord = (size_t)(g.nx + 1) + (g.ny + 1) + (g.dim == 3 ? g.nz + 1 : 0);
+    std::vector<double> coords;
+    coords.insert(coords.end(), grid->xnodes, grid->xnodes + g.nx + 1);
+    coords.insert(coords.end(), grid->ynodes, grid->ynodes + g.ny + 1);
+    if (g.dim == 3) coords.insert(coords.end(), grid->znodes, grid->znodes + g.nz + 1);
+    // node columns: mass, p(3), f(3), u(3) are cleared each step; c(3), v(3) are not
+    const size_t NN = (size_t)g.nnodes;
+    const int ncleared = 10, nkept = 6;
+    if ((e = cudaMalloc(&c->grid_coords, ncoord * sizeof(double))) != cudaSuccess ||
+        (e = cudaMalloc(&c->nblock, NN * (ncleared + nkept) * sizeof(double) + NN)) != cudaSuccess ||
+        (e = cudaMalloc(&c->bc_group, NN * sizeof(int))) != cudaSuccess ||
+        (e = cudaMalloc(&c->err, sizeof(unsigned))) != cudaSuccess) {
+        std::string m = std::string("device allocation: ") + cudaGetErrorString(e);
+        mpmgpu_destroy(c);
+        return set_err(nullptr, MPMGPU_ERR_OOM, m);
+    }
+    cudaMemcpy(c->grid_coords, coords.data(), ncoord * sizeof(double), cudaMemcpyHostToDevice);
+    g.xn = c->grid_coords;
+    g.yn = c->grid_coords + g.nx + 1;
+    g.zn = g.dim == 3 ? c->grid_coords + (g.nx + 1) + (g.ny + 1) : nullptr;
+    double *b = c->nblock;
+    DevNodes &nd = c->nd;
+    nd.mass = b;
+    nd.px = b + NN;
+    nd.py = b + 2 * NN;
+    nd.pz = b + 3 * NN;
+    nd.fx = b + 4 * NN;
+    nd.fy = b + 5 * NN;
+    nd.fz = b + 6 * NN;
+    nd.ux = b + 7 * NN;
+    nd.uy = b + 8 * NN;
+    nd.uz = b + 9 * NN;
+    nd.cx = b + 10 * NN;
+    nd.cy = b + 11 * NN;
+    nd.cz = b + 12 * NN;
+    nd.vx = b + 13 * NN;
+    nd.vy = b + 14 * NN;
+    nd.vz = b + 15 * NN;
+    nd.active = (unsigned char *)(b + 16 * NN);
+    c->nblock_zero_bytes = NN * ncleared * sizeof(double);
+    cudaMemset(c->nblock, 0, NN * (ncleared + nkept) * sizeof(double) + NN);
+    cudaMemset(c->bc_group, 0xFF, NN * sizeof(int));
+    cudaMemset(c->err, 0, sizeof(unsigned));
+    const char *names[] = {"p2g", "node_post", "strain_forces", "node_update", "g2p", "node_usl", "strain_last",
+                           "sort"};
+    for (const char *n : names) {
+        Profile pr{n, nullptr, nullptr, 0.};
+        cudaEventCreate(&pr.a);
+        cudaEventCreate(&pr.b);
+        c->prof.push_back(pr);
+    }
+    if ((e = cudaGetLastError()) != cudaSuccess) {
+        int st = cuda_fail(nullptr, e, "mpmgpu_create");
+        mpmgpu_destroy(c);
+        return st;
+    }
+    *out = c;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_set_materials(MpmGpuCtx *c, const MpmGpuMaterial *mats, int32_t nmat) {
+    if (!c || !mats || nmat <= 0) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_set_materials: bad argument");
+    std::vector<DevMat> h((size_t)nmat);
+    for (int i = 0; i < nmat; i++) {
+        std::string why;
+        int st = derive_material(mats[i], c->opts.np, h[i], why);
+        if (st != MPMGPU_OK) return set_err(c, st, "material " + std::to_string(i) + ": " + why);
+    }
+    if (c->mats) cudaFree(c->mats);
+    c->mats = nullptr;
+    CK(cudaMalloc(&c->mats, sizeof(DevMat) * nmat));
+    CK(cudaMemcpy(c->mats, h.data(), sizeof(DevMat) * nmat, cudaMemcpyHostToDevice));
+    c->hmats = h;
+    c->nmat = nmat;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_set_contact(MpmGpuCtx *c, const MpmGpuContact *contact) {
+    if (!c) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_set_contact: null context");
+    if (contact && contact->enabled)
+        return set_err(c, MPMGPU_ERR_UNSUPPORTED, "multimaterial contact is not implemented on the device");
+    return MPMGPU_OK;
+}
+
+int mpmgpu_set_velocity_bcs(MpmGpuCtx *c, const MpmGpuVelBC *bcs, int32_t nbc) {
+    if (!c || (nbc > 0 && !bcs) || nbc < 0) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_set_velocity_bcs: bad argument");
+    // group by node, keeping list order inside each node
+    std::map<int, std::vector<int>> by_node;
+    std::vector<int> order;
+    for (int k = 0; k < nbc; k++) {
+        const int nd = bcs[k].node - 1;
+        if (nd < 0 || nd >= c->g.nnodes) return set_err(c, MPMGPU_ERR_INVALID, "velocity BC node out of range");
+        const int dir = bcs[k].dir;
+        if (dir != 1 && dir != 2 && dir != 4) return set_err(c, MPMGPU_ERR_UNSUPPORTED, "velocity BC dir must be 1, 2 or 4");
+        if (dir == 4 && c->dim == 2) return set_err(c, MPMGPU_ERR_INVALID, "z velocity BC in 2D");
+        if (!by_node.count(nd)) order.push_back(nd);
+        by_node[nd].push_back(k);
+    }
+    const int ng = (int)order.size();
+    std::vector<int> gnode(ng), start(ng + 1), dir(nbc);
+    std::vector<double> val(nbc), ft(nbc);
+    std::vector<int> group(c->g.nnodes, -1);
+    int pos = 0;
+    for (int gi = 0; gi < ng; gi++) {
+        gnode[gi] = order[gi];
+        start[gi] = pos;
+        group[order[gi]] = gi;
+        for (int k : by_node[order[gi]]) {
+            dir[pos] = bcs[k].dir;
+            val[pos] = bcs[k].value;
+            ft[pos] = bcs[k].ftime;
+            pos++;
+        }
+    }
+    start[ng] = pos;
+    if (c->bc_block) cudaFree(c->bc_block);
+    c->bc_block = nullptr;
+    size_t bytes = sizeof(int) * (ng + ng + 1 + nbc) + sizeof(double) * (2 * nbc) + 64;
+    CK(cudaMalloc(&c->bc_block, bytes));
+    char *bb = (char *)c->bc_block;
+    double *dval = (double *)bb;
+    double *dft = dval + nbc;
+    int *dnode = (int *)(dft + nbc);
+    int *dstart = dnode + ng;
+    int *ddir = dstart + ng + 1;
+    CK(cudaMemcpy(dval, val.data(), sizeof(double) * nbc, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dft, ft.data(), sizeof(double) * nbc, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dnode, gnode.data(), sizeof(int) * ng, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(dstart, start.data(), sizeof(int) * (ng + 1), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(ddir, dir.data(), sizeof(int) * nbc, cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(c->bc_group, group.data(), sizeof(int) * c->g.nnodes, cudaMemcpyHostToDevice));
+    c->bcs.nnodes_bc = ng;
+    c->bcs.node = dnode;
+    c->bcs.start = dstart;
+    c->bcs.dir = ddir;
+    c->bcs.value = dval;
+    c->bcs.ftime = dft;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
+    if (!c || !h || h->n <= 0) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_upload_particles: bad argument");
+    if (h->n > (1LL << 31) - 1) return set_err(c, MPMGPU_ERR_INVALID, "too many particles for one context");
+    if (!c->mats) return set_err(c, MPMGPU_ERR_INVALID, "set materials before uploading particles");
+    const int n = (int)h->n;
+    // validate materials and elements on the host before anything reaches the device
+    for (int i = 0; i < n; i++) {
+        if (h->mat[i] < 0 || h->mat[i] >= c->nmat) return set_err(c, MPMGPU_ERR_INVALID, "particle material out of range");
+        const int ne = c->g.nx * c->g.ny * (c->dim == 3 ? c->g.nz : 1);
+        if (h->elem[i] < 0 || h->elem[i] >= ne) return set_err(c, MPMGPU_ERR_INVALID, "particle element out of range");
+    }
+    free_particles(c);
+    size_t bytes = (size_t)n * kParticleDoubles * sizeof(double);
+    cudaError_t e = cudaMalloc(&c->pblock, bytes + (size_t)n * sizeof(double));  // + zeta column
+    if (e != cudaSuccess) return set_err(c, MPMGPU_ERR_OOM, std::string("particle allocation: ") + cudaGetErrorString(e));
+    e = cudaMalloc(&c->iblock, (size_t)n * 3 * sizeof(int));
+    if (e != cudaSuccess) {
+        free_particles(c);
+        return set_err(c, MPMGPU_ERR_OOM, std::string("particle allocation: ") + cudaGetErrorString(e));
+    }
+    CK(cudaMemsetAsync(c->pblock, 0, bytes + (size_t)n * sizeof(double), c->stream));
+    c->p.n = n;
+    link_columns(c->p, c->pblock, c->iblock, &c->orig);
+    double *hc[kParticleDoubles];
+    hcols(h, hc);
+    for (int k = 0; k < kParticleDoubles; k++)
+        if (hc[k])
+            CK(cudaMemcpyAsync(c->pblock + (size_t)k * n, hc[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
+                               c->stream));
+    CK(cudaMemcpyAsync(c->p.mat, h->mat, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    CK(cudaMemcpyAsync(c->p.elem, h->elem, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    std::vector<int> idx(n);
+    for (int i = 0; i < n; i++) idx[i] = i;
+    CK(cudaMemcpyAsync(c->orig, idx.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
+    int st = sort_alloc(c->sort, n, c->g.nx * c->g.ny * (c->dim == 3 ? c->g.nz : 1), kParticleDoubles + 1);
+    if (st != 0) return set_err(c, MPMGPU_ERR_OOM, "sort workspace allocation failed");
+    CK(cudaStreamSynchronize(c->stream));
+    return MPMGPU_OK;
+}
+
+}  // extern "C"
+
+namespace {
+
+template <int DIM, int SHAPE>
+void enqueue_step(MpmGpuCtx *c, double t) {
+    const int n = c->p.n, NN = c->g.nnodes;
+    const int TB = 256;
+    const int pb = (n + TB - 1) / TB, nb = (NN + TB - 1) / TB;
+    const double dt = c->opts.timestep;
+    const int method = c->opts.method;
+    const double stFirst = method == MPMGPU_USAVG ? c->opts.fraction_usf * dt : dt;
+    const double stLast = method == MPMGPU_USAVG ? dt - stFirst : dt;
+    cudaStream_t s = c->stream;
+    auto mark = [&](int k, bool begin) {
+        if (c->profile) cudaEventRecord(begin ? c->prof[k].a : c->prof[k].b, s);
+    };
+    cudaMemsetAsync(c->nblock, 0, c->nblock_zero_bytes, s);
+    cudaMemsetAsync(c->nd.active, 0, (size_t)NN, s);
+    mark(0, true);
+    k_p2g<DIM, SHAPE><<<pb, TB, 0, s>>>(c->g, c->p, c->nd);
+    mark(0, false);
+    mark(1, true);
+    k_node_post<DIM><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL, t, dt);
+    mark(1, false);
+    mark(2, true);
+    if (method == MPMGPU_USL)
+        k_strain_forces<DIM, SHAPE, false><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stFirst);
+    else
+        k_strain_forces<DIM, SHAPE, true><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stFirst);
+    mark(2, false);
+    mark(3, true);
+    k_node_update<DIM><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, t, dt);
+    mark(3, false);
+    mark(4, true);
+    if (method == MPMGPU_USF) {
+        k_g2p<DIM, SHAPE, false><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, dt, c->err);
+        mark(4, false);
+        return;
+    }
+    k_g2p<DIM, SHAPE, true><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, dt, c->err);
+    mark(4, false);
+    mark(5, true);
+    k_node_usl<DIM><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, t, dt);
+    mark(5, false);
+    mark(6, true);
+    k_strain_last<DIM, SHAPE><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stLast, c->err);
+    mark(6, false);
+}
+
+void enqueue(MpmGpuCtx *c, double t) {
+    const bool d3 = c->dim == 3;
+    const bool lin = c->opts.shape == MPMGPU_SHAPE_LINEAR;
+    if (d3) {
+        if (lin) enqueue_step<3, SHAPE_LINEAR>(c, t);
+        else enqueue_step<3, SHAPE_UGIMP>(c, t);
+    } else {
+        if (lin) enqueue_step<2, SHAPE_LINEAR>(c, t);
+        else enqueue_step<2, SHAPE_UGIMP>(c, t);
+    }
+}
+
+int error_status(MpmGpuCtx *c, unsigned bits) {
+    if (bits & ERR_NAN) return set_err(c, MPMGPU_ERR_NAN, "a particle position became NaN");
+    if (bits & ERR_LEFT_GRID) return set_err(c, MPMGPU_ERR_LEFT_GRID, "a particle left the grid");
+    if (bits & ERR_EDGE) return set_err(c, MPMGPU_ERR_LEFT_GRID, "a particle moved into a grid edge element");
+    return MPMGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpmgpu_step(MpmGpuCtx *c, int32_t nsteps, double t0) {
+    if (!c || nsteps < 0) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step: bad argument");
+    if (c->p.n <= 0 || !c->mats) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step: no particles or materials");
+    for (auto &pr : c->prof) pr.ms = 0.;
+    double t = t0;
+    for (int s = 0; s < nsteps; s++) {
+        if (c->opts.sort_interval > 0 && c->steps_done % c->opts.sort_interval == 0) {
+            if (c->profile) cudaEventRecord(c->prof[7].a, c->stream);
+            int st = sort_particles(c->sort, c->p, c->pblock, c->iblock, c->orig, kParticleDoubles + 1, c->stream);
+            if (st != 0) return set_err(c, MPMGPU_ERR_CUDA, "particle sort failed");
+            if (c->profile) {
+                cudaEventRecord(c->prof[7].b, c->stream);
+                cudaEventSynchronize(c->prof[7].b);
+                float ms;
+                cudaEventElapsedTime(&ms, c->prof[7].a, c->prof[7].b);
+                c->prof[7].ms += ms;
+            }
+        }
+        enqueue(c, t);
+        if (c->profile) {
+            cudaStreamSynchronize(c->stream);
+            for (int k = 0; k < 7; k++) {
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, c->prof[k].a, c->prof[k].b) == cudaSuccess) c->prof[k].ms += ms;
+            }
+        }
+        c->steps_done++;
+        t += c->opts.timestep;
+    }
+    unsigned bits = 0;
+    CK(cudaMemcpyAsync(&bits, c->err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    if (bits) {
+        cudaMemsetAsync(c->err, 0, sizeof(unsigned), c->stream);
+        return error_status(c, bits);
+    }
+    return MPMGPU_OK;
+}
+
+int mpmgpu_download_particles(MpmGpuCtx *c, MpmGpuParticles *h) {
+    if (!c || !h) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_download_particles: null argument");
+    if (h->n != c->p.n) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_download_particles: particle count mismatch");
+    const int n = c->p.n;
+    // bring columns back in the host's original particle order
+    int st = unsort_to_scratch(c->sort, c->p, c->orig, c->pblock, kParticleDoubles + 1, c->stream);
+    if (st != 0) return set_err(c, MPMGPU_ERR_CUDA, "unsort failed");
+    double *hc[kParticleDoubles];
+    hcols(h, hc);
+    for (int k = 0; k < kParticleDoubles; k++)
+        if (hc[k]) CK(cudaMemcpyAsync(hc[k], c->sort.scratch + (size_t)k * n, (size_t)n * sizeof(double),
+                                      cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(h->mat, c->sort.iscratch, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaMemcpyAsync(h->elem, c->sort.iscratch + n, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    return MPMGPU_OK;
+}
+
+void mpmgpu_destroy(MpmGpuCtx *c) {
+    if (!c) return;
+    free_particles(c);
+    if (c->mats) cudaFree(c->mats);
+    if (c->grid_coords) cudaFree(c->grid_coords);
+    if (c->nblock) cudaFree(c->nblock);
+    if (c->bc_group) cudaFree(c->bc_group);
+    if (c->bc_block) cudaFree(c->bc_block);
+    if (c->err) cudaFree(c->err);
+    for (auto &pr : c->prof) {
+        if (pr.a) cudaEventDestroy(pr.a);
+        if (pr.b) cudaEventDestroy(pr.b);
+    }
+    if (c->stream) cudaStreamDestroy(c->stream);
+    delete c;
+}
+
+int mpmgpu_profile(const MpmGpuCtx *c, const char **names, double *ms, int32_t cap) {
+    if (!c) return 0;
+    int k = 0;
+    for (const auto &pr : c->prof) {
+        if (k >= cap) break;
+        if (names) names[k] = pr.name;
+        if (ms) ms[k] = pr.ms;
+        k++;
+    }
+    return k;
+}
+
+// Extension: enable per-kernel CUDA-event timing on the context stream (adds a
+// synchronisation per step; for profiling runs only).
+int mpmgpu_set_profiling(MpmGpuCtx *c, int32_t on) {
+    if (!c) return MPMGPU_ERR_INVALID;
+    c->profile = on != 0;
+    return MPMGPU_OK;
+}
+
+// Extension: the context's CUDA stream, for callers that time with their own events.
+void *mpmgpu_stream(MpmGpuCtx *c) { return c ? (void *)c->stream : nullptr; }
+
+}  // extern "C"

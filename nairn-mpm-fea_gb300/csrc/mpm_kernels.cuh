@@ -1,0 +1,463 @@
+// mpm_kernels.cuh -- kernels of one explicit MPM step (FP64 path).
+//
+// Step structure (the reference task chain, NairnMPM.cpp:870-1110, regrouped):
+//   k_p2g            InitializationTask + MassAndMomentumTask      (particles)
+//   k_node_post      PostExtrapolationTask + velocity BCs + v=p/m  (nodes)
+//   k_strain_forces  UpdateStrainsFirstTask fused with GridForcesTask (particles)
+//   k_node_update    PostForcesTask + UpdateMomentaTask + BCs + v  (nodes)
+//   k_g2p            UpdateParticlesTask fused with the momentum
+//                    re-extrapolation of UpdateStrainsLastContactTask (particles)
+//   k_node_usl       velocity BCs of the second extrapolation + v  (nodes)
+//   k_strain_last    second strain update fused with ResetElementsTask (particles)
+// Fusing is exact: each fused pair only uses the particle's own data between
+// the two halves, and the grid data both halves read is complete beforehand.
+#pragma once
+
+#include "mpm_device.cuh"
+
+namespace nmg {
+
+enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1 };
+
+// Visit the nodes of one particle in the reference's order, calling
+// f(node0based, N, dNdx, dNdy, dNdz).  ElementBase::GetShapeFunctions /
+// GetShapeGradients (NairnMPM/src/Elements/MoreMPMElementBase.cpp:120-284).
+template <int DIM, int SHAPE, bool GRAD, class F>
+__device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi, double eta, double zeta,
+                                              double lpx, double lpy, double lpz, F &&f) {
+    int col, row, zr;
+    elem_coords(g, e, col, row, zr);
+    const int n0 = zr * g.zplane + row * g.yplane + col;  // 0-based first node
+    const double DX = g.xn[col + 1] - g.xn[col];
+    const double DY = g.yn[row + 1] - g.yn[row];
+    const double DZ = DIM == 3 ? g.zn[zr + 1] - g.zn[zr] : 1.;
+    if (SHAPE == SHAPE_LINEAR) {
+        if (DIM == 2) {
+            // FourNodeIsoparam::ShapeFunction (6-argument form), FourNodeIsoparam.cpp:189-212
+            const int off[4] = {0, 1, 1 + g.yplane, g.yplane};
+            const double xs[4] = {-1., 1., 1., -1.}, es[4] = {-1., -1., 1., 1.};
+#pragma unroll
+            for (int i = 0; i < 4; i++) {
+                const double t1 = 1. + xs[i] * xi, t2 = 1. + es[i] * eta;
+                double dx = 0., dy = 0.;
+                if (GRAD) {
+                    dx = 0.5 * xs[i] * t2 / DX;
+                    dy = 0.5 * es[i] * t1 / DY;
+                }
+                f(n0 + off[i], 0.25 * t1 * t2, dx, dy, 0.);
+            }
+        } else {
+            // EightNodeIsoparamBrick::ShapeFunction (6-argument form), EightNodeIsoparamBrick.cpp:90-104
+            const double xs[8] = {-1., 1., 1., -1., -1., 1., 1., -1.};
+            const double es[8] = {-1., -1., 1., 1., -1., -1., 1., 1.};
+            const double zs[8] = {-1., -1., -1., -1., 1., 1., 1., 1.};
+#pragma unroll
+            for (int i = 0; i < 8; i++) {
+                const int off = (i == 1 || i == 5 ? 1 : 0) + (i == 2 || i == 6 ? 1 + g.yplane : 0) +
+                                (i == 3 || i == 7 ? g.yplane : 0) + (i >= 4 ? g.zplane : 0);
+                const double t1 = 1. + xs[i] * xi, t2 = 1. + es[i] * eta, t3 = 1. + zs[i] * zeta;
+                double dx = 0., dy = 0., dz = 0.;
+                if (GRAD) {
+                    dx = 0.25 * xs[i] * t2 * t3 / DX;
+                    dy = 0.25 * es[i] * t1 * t3 / DY;
+                    dz = 0.25 * zs[i] * t1 * t2 / DZ;
+                }
+                f(n0 + off, 0.125 * t1 * t2 * t3, dx, dy, dz);
+            }
+        }
+        return;
+    }
+    // uGIMP
+    Axis ax, ay, az;
+    gimp_axis<DIM == 3, GRAD>(xi, lpx, 1. / (4. * lpx), ax);
+    gimp_axis<DIM == 3, GRAD>(eta, lpy, 1. / (4. * lpy), ay);
+    const double idx = GRAD ? 2.0 / DX : 0., idy = GRAD ? 2.0 / DY : 0.;
+    if (DIM == 2) {
+#pragma unroll
+        for (int c = 0; c < 16; c++) {
+            const unsigned code = c_cand2d[c];
+            const int kx = code & 3, ky = (code >> 2) & 3;
+            if (!((ax.act >> kx) & (ay.act >> ky) & 1u)) continue;
+            const double Sx = ax.S[kx], Sy = ay.S[ky];
+            double dx = 0., dy = 0.;
+            if (GRAD) {
+                dx = ax.dS[kx] * Sy * idx;
+                dy = Sx * ay.dS[ky] * idy;
+            }
+            f(n0 + (kx - 1) + (ky - 1) * g.yplane, Sx * Sy, dx, dy, 0.);
+        }
+    } else {
+        gimp_axis<true, GRAD>(zeta, lpz, 1. / (4. * lpy), az);
+        const double idz = GRAD ? 2.0 / DZ : 0.;
+#pragma unroll 4
+        for (int c = 0; c < 64; c++) {
+            const unsigned code = c_cand3d[c];
+            const int kx = code & 3, ky = (code >> 2) & 3, kz = (code >> 4) & 3;
+            if (!((ax.act >> kx) & (ay.act >> ky) & (az.act >> kz) & 1u)) continue;
+            const double Sx = ax.S[kx], Sy = ay.S[ky], Sz = az.S[kz];
+            double dx = 0., dy = 0., dz = 0.;
+            if (GRAD) {
+                dx = ax.dS[kx] * Sy * Sz * idx;
+                dy = Sx * ay.dS[ky] * Sz * idy;
+                dz = Sx * Sy * az.dS[kz] * idz;
+            }
+            f(n0 + (kx - 1) + (ky - 1) * g.yplane + (kz - 1) * g.zplane, Sx * Sy * Sz, dx, dy, dz);
+        }
+    }
+}
+
+// ---------------------------------------------------------------------------
+// particle kernels
+// ---------------------------------------------------------------------------
+
+// InitializationTask::Execute (natural coordinates, InitializationTask.cpp:59-83)
+// and MassAndMomentumTask::Execute with NodalPoint::AddMassMomentum
+// (MassAndMomentumTask.cpp:48-127, NodalPointMPM.cpp:419-453).
+template <int DIM, int SHAPE>
+__global__ void __launch_bounds__(256) k_p2g(DevGrid g, DevParticles p, DevNodes nd) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const int e = p.elem[i];
+    const double x = p.x[i], y = p.y[i], z = DIM == 3 ? p.z[i] : 0.;
+    double xi, eta, zeta;
+    xi_position(g, e, x, y, z, xi, eta, zeta);
+    p.xi[i] = xi;
+    p.eta[i] = eta;
+    if (DIM == 3) p.zeta[i] = zeta;
+    const double mp = p.mass[i];
+    const double vx = p.vx[i], vy = p.vy[i], vz = DIM == 3 ? p.vz[i] : 0.;
+    for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1.,
+                                     [&](int n, double N, double, double, double) {
+                                         const double fnmp = N * mp;
+                                         atomicAdd(&nd.mass[n], fnmp);
+                                         atomicAdd(&nd.px[n], vx * fnmp);
+                                         atomicAdd(&nd.py[n], vy * fnmp);
+                                         if (DIM == 3) atomicAdd(&nd.pz[n], vz * fnmp);
+                                         nd.active[n] = 1;
+                                     });
+}
+
+template <int DIM>
+__device__ __forceinline__ void constitutive(const DevMat *mats, const DevParticles &p, int i, const double du[9]) {
+    const DevMat &m = mats[p.mat[i]];
+    if (DIM == 2) hypo_increment_F_2d(p, i, du);
+    else hypo_increment_F_3d(p, i, du);
+    if (m.type == 1) {
+        if (DIM == 2) iso_law_2d(m, p, i, du);
+        else iso_law_3d(m, p, i, du);
+    } else {
+        plastic_law<DIM == 3>(m, p, i, du);
+    }
+}
+
+// gather of ExtrapVelocityGradient (MatPoint2D.cpp:57-87, MatPoint3D.cpp:50-75)
+template <int DIM, int SHAPE>
+__device__ __forceinline__ void velocity_gradient(const DevGrid &g, const DevParticles &p, const DevNodes &nd, int i,
+                                                  double st, double du[9]) {
+    double d[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};
+    for_each_node<DIM, SHAPE, true>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
+                                    DIM == 3 ? p.lpz[i] : 1.,
+                                    [&](int n, double, double dx, double dy, double dz) {
+                                        const double vx = nd.vx[n], vy = nd.vy[n];
+                                        d[0] += vx * dx;
+                                        d[1] += vx * dy;
+                                        d[3] += vy * dx;
+                                        d[4] += vy * dy;
+                                        if (DIM == 3) {
+                                            const double vz = nd.vz[n];
+                                            d[2] += vx * dz;
+                                            d[5] += vy * dz;
+                                            d[6] += vz * dx;
+                                            d[7] += vz * dy;
+                                            d[8] += vz * dz;
+                                        }
+                                    });
+#pragma unroll
+    for (int k = 0; k < 9; k++) du[k] = d[k] * st;
+}
+
+// UpdateStrainsFirstTask::FullStrainUpdate (UpdateStrainsFirstTask.cpp:101-168)
+// fused with GridForcesTask::Execute and MatPoint2D/3D::GetFintPlusFext
+// (GridForcesTask.cpp:40-153, MatPoint2D.cpp:242-262, MatPoint3D.cpp:248-269).
+template <int DIM, int SHAPE, bool STRAIN>
+__global__ void __launch_bounds__(256) k_strain_forces(DevGrid g, DevParticles p, DevNodes nd, const DevMat *mats,
+                                                       double st) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    if (STRAIN) {
+        double du[9];
+        velocity_gradient<DIM, SHAPE>(g, p, nd, i, st, du);
+        constitutive<DIM>(mats, p, i, du);
+    }
+    const double mp = p.mass[i], P = p.pressure[i];
+    const double sxx = p.sxx[i] - P, syy = p.syy[i] - P, sxy = p.sxy[i];
+    const double szz = DIM == 3 ? p.szz[i] - P : 0., sxz = DIM == 3 ? p.sxz[i] : 0., syz = DIM == 3 ? p.syz[i] : 0.;
+    for_each_node<DIM, SHAPE, true>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
+                                    DIM == 3 ? p.lpz[i] : 1.,
+                                    [&](int n, double, double dx, double dy, double dz) {
+                                        if (DIM == 2) {
+                                            atomicAdd(&nd.fx[n], -mp * (sxx * dx + sxy * dy));
+                                            atomicAdd(&nd.fy[n], -mp * (sxy * dx + syy * dy));
+                                        } else {
+                                            atomicAdd(&nd.fx[n], -mp * (sxx * dx + sxy * dy + sxz * dz));
+                                            atomicAdd(&nd.fy[n], -mp * (sxy * dx + syy * dy + syz * dz));
+                                            atomicAdd(&nd.fz[n], -mp * (sxz * dx + syz * dy + szz * dz));
+                                        }
+                                    });
+}
+
+// ResetElementsTask::ResetElement with MeshInfo::FindElementFromPoint and
+// MeshInfo::EdgeElement2D/3D (ResetElementsTask.cpp:196-228,
+// MeshInfo.cpp:171-199, 593-633).
+template <int DIM>
+__device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
+    const double x = p.x[i], y = p.y[i], z = DIM == 3 ? p.z[i] : 0.;
+    if (x != x || y != y || z != z) {
+        atomicOr(err, ERR_NAN);
+        return;
+    }
+    const int e = p.elem[i];
+    int col, row, zr;
+    elem_coords(g, e, col, row, zr);
+    bool in = !(x < g.xn[col] || x >= g.xn[col + 1]) && !(y < g.yn[row] || y >= g.yn[row + 1]);
+    if (DIM == 3) in = in && !(z < g.zn[zr] || z >= g.zn[zr + 1]);
+    if (in) return;
+    int c = (int)((x - g.xmin) / g.gx);
+    bool bad = false;
+    if (c < 0 || c >= g.nx) {
+        if (x == g.xmin + g.nx * g.gx) c = g.nx - 1;
+        else bad = true;
+    }
+    int r = (int)((y - g.ymin) / g.gy);
+    if (r < 0 || r >= g.ny) {
+        if (y == g.ymin + g.ny * g.gy) r = g.ny - 1;
+        else bad = true;
+    }
+    int zz = 0;
+    if (DIM == 3) {
+        zz = (int)((z - g.zmin) / g.gz);
+        if (zz < 0 || zz >= g.nz) {
+            if (z == g.zmin + g.nz * g.gz) zz = g.nz - 1;
+            else bad = true;
+        }
+    }
+    if (bad) {
+        atomicOr(err, ERR_LEFT_GRID);
+        return;
+    }
+    const int num = DIM == 3 ? g.nx * (zz * g.ny + r) + c + 1 : r * g.nx + c + 1;
+    bool edge;
+    if (DIM == 2) {
+        const int total = g.nx * g.ny;
+        edge = num <= g.nx || num > total - g.nx || (num % g.nx) <= 1;
+    } else {
+        const int hv = g.nx * g.ny, total = hv * g.nz;
+        const int xz = num % hv;
+        edge = num <= hv || num > total - hv || (num % g.nx) <= 1 || xz <= g.nx || xz > g.nx * (g.ny - 1);
+    }
+    if (edge) {
+        atomicOr(err, ERR_EDGE);
+        return;
+    }
+    p.elem[i] = num - 1;
+}
+
+// UpdateParticlesTask::Execute, MatVelocityField::IncrementNodalVelAcc and
+// the FLIP branch of MatPoint2D/3D::MoveParticle without damping
+// (UpdateParticlesTask.cpp:75-178, MatVelocityField.cpp:410-426,
+// MatPoint2D.cpp:99-196), fused with the momentum re-extrapolation of
+// UpdateStrainsLastContactTask (UpdateStrainsLastContactTask.cpp:71-146,
+// NodalPoint::AddMassMomentumLast NodalPointMPM.cpp:470-486), which uses the
+// same natural coordinates of the step.
+template <int DIM, int SHAPE, bool USL>
+__global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes nd, double dt, unsigned *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    double Sv[3] = {0., 0., 0.}, Sa[3] = {0., 0., 0.};
+    const int e = p.elem[i];
+    const double xi = p.xi[i], eta = p.eta[i], zeta = DIM == 3 ? p.zeta[i] : 0.;
+    const double lx = p.lpx[i], ly = p.lpy[i], lz = DIM == 3 ? p.lpz[i] : 1.;
+    for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, double N, double, double, double) {
+        Sv[0] += nd.vx[n] * N;
+        Sv[1] += nd.vy[n] * N;
+        if (DIM == 3) Sv[2] += nd.vz[n] * N;
+        const double mnode = N / nd.mass[n];
+        Sa[0] += nd.fx[n] * mnode;
+        Sa[1] += nd.fy[n] * mnode;
+        if (DIM == 3) Sa[2] += nd.fz[n] * mnode;
+    });
+    double v[3] = {p.vx[i], p.vy[i], DIM == 3 ? p.vz[i] : 0.};
+    double xp[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
+#pragma unroll
+    for (int a = 0; a < DIM; a++) {
+        const double vm = Sv[a] - Sa[a] * dt;
+        const double dv = Sa[a] * dt;
+        v[a] += dv;
+        xp[a] += (vm + 0.5 * dv) * dt;
+    }
+    p.vx[i] = v[0];
+    p.vy[i] = v[1];
+    p.x[i] = xp[0];
+    p.y[i] = xp[1];
+    if (DIM == 3) {
+        p.vz[i] = v[2];
+        p.z[i] = xp[2];
+    }
+    if (USL) {
+        const double mp = p.mass[i];
+        for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, double N, double, double, double) {
+            const double fnmp = N * mp;
+            atomicAdd(&nd.ux[n], v[0] * fnmp);
+            atomicAdd(&nd.uy[n], v[1] * fnmp);
+            if (DIM == 3) atomicAdd(&nd.uz[n], v[2] * fnmp);
+        });
+    } else {
+        reset_element<DIM>(g, p, i, err);
+    }
+}
+
+// UpdateStrainsFirstTask::FullStrainUpdate called from
+// UpdateStrainsLastContactTask (:149), fused with ResetElementsTask.
+template <int DIM, int SHAPE>
+__global__ void __launch_bounds__(256) k_strain_last(DevGrid g, DevParticles p, DevNodes nd, const DevMat *mats,
+                                                     double st, unsigned *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    double du[9];
+    velocity_gradient<DIM, SHAPE>(g, p, nd, i, st, du);
+    constitutive<DIM>(mats, p, i, du);
+    reset_element<DIM>(g, p, i, err);
+}
+
+// ---------------------------------------------------------------------------
+// node kernels
+// ---------------------------------------------------------------------------
+enum { BC_MASS_MOMENTUM = 0, BC_UPDATE_MOMENTUM, BC_UPDATE_STRAINS_LAST, BC_GRID_FORCES };
+
+// NodalVelBC::VelocityBCLoop for one node: zero passes then add passes, in
+// list order (NodalVelBC.cpp:386-400; MatVelocityField::ZeroVelocityBC and
+// AddVelocityBC, MatVelocityField.cpp:490-575).
+__device__ __forceinline__ void node_bcs(const DevBCs &b, int grp, int pass, double mass, double t, double dt,
+                                         double p[3], double f[3]) {
+    const int s = b.start[grp], e = b.start[grp + 1];
+    for (int k = s; k < e; k++) {
+        if (t < b.ftime[k]) continue;
+        const int dir = b.dir[k];
+        const double n[3] = {dir == 1 ? 1. : 0., dir == 2 ? 1. : 0., dir == 4 ? 1. : 0.};
+        if (pass == BC_GRID_FORCES) {
+            const double dotf = f[0] * n[0] + f[1] * n[1] + f[2] * n[2];
+            const double dotp = p[0] * n[0] + p[1] * n[1] + p[2] * n[2];
+            const double sc = -dotf - dotp / dt;
+#pragma unroll
+            for (int a = 0; a < 3; a++) f[a] += n[a] * sc;
+        } else {
+            const double dotn = p[0] * n[0] + p[1] * n[1] + p[2] * n[2];
+#pragma unroll
+            for (int a = 0; a < 3; a++) p[a] += n[a] * (-dotn);
+            if (pass == BC_UPDATE_MOMENTUM) {
+#pragma unroll
+                for (int a = 0; a < 3; a++) f[a] += n[a] * (-dotn / dt);
+            }
+        }
+    }
+    for (int k = s; k < e; k++) {
+        if (t < b.ftime[k]) continue;
+        const int dir = b.dir[k];
+        const double n[3] = {dir == 1 ? 1. : 0., dir == 2 ? 1. : 0., dir == 4 ? 1. : 0.};
+        const double vel = b.value[k];
+        if (pass == BC_GRID_FORCES) {
+            const double sc = mass * vel / dt;
+#pragma unroll
+            for (int a = 0; a < 3; a++) f[a] += n[a] * sc;
+        } else {
+            const double pv = mass * vel;
+#pragma unroll
+            for (int a = 0; a < 3; a++) p[a] += n[a] * pv;
+            if (pass == BC_UPDATE_MOMENTUM) {
+                const double sc = pv / dt;
+#pragma unroll
+                for (int a = 0; a < 3; a++) f[a] += n[a] * sc;
+            }
+        }
+    }
+}
+
+// MatVelocityField::GridValueCalculation (MatVelocityField.cpp:239-251)
+__device__ __forceinline__ void node_velocity(const DevNodes &nd, int n, double mass, const double p[3]) {
+    if (mass == 0.) return;
+    const double r = 1. / mass;
+    nd.vx[n] = p[0] * r;
+    nd.vy[n] = p[1] * r;
+    nd.vz[n] = p[2] * r;
+}
+
+// PostExtrapolationTask::Execute (PostExtrapolationTask.cpp:46-165):
+// vk[pkCopy] = pk, velocity conditions of MASS_MOMENTUM_CALL, then grid velocity.
+template <int DIM>
+__global__ void k_node_post(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, int do_bcs, double t,
+                            double dt) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nnodes || !nd.active[n]) return;
+    double p[3] = {nd.px[n], nd.py[n], DIM == 3 ? nd.pz[n] : 0.};
+    nd.cx[n] = p[0];
+    nd.cy[n] = p[1];
+    if (DIM == 3) nd.cz[n] = p[2];
+    const double m = nd.mass[n];
+    const int grp = bc_group[n];
+    if (do_bcs && grp >= 0) {
+        double f[3] = {0., 0., 0.};
+        node_bcs(b, grp, BC_MASS_MOMENTUM, m, t, dt, p, f);
+        nd.px[n] = p[0];
+        nd.py[n] = p[1];
+        if (DIM == 3) nd.pz[n] = p[2];
+    }
+    node_velocity(nd, n, m, p);
+}
+
+// PostForcesTask::Execute (restore momenta, GRID_FORCES_CALL velocity
+// conditions; PostForcesTask.cpp:43-111) and UpdateMomentaTask::Execute
+// (p += f dt, UPDATE_MOMENTUM_CALL conditions; UpdateMomentaTask.cpp:44-94),
+// then grid velocity for the particle update.
+template <int DIM>
+__global__ void k_node_update(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, double t, double dt) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nnodes || !nd.active[n]) return;
+    double p[3] = {nd.cx[n], nd.cy[n], DIM == 3 ? nd.cz[n] : 0.};
+    double f[3] = {nd.fx[n], nd.fy[n], DIM == 3 ? nd.fz[n] : 0.};
+    const double m = nd.mass[n];
+    const int grp = bc_group[n];
+    if (grp >= 0) node_bcs(b, grp, BC_GRID_FORCES, m, t, dt, p, f);
+#pragma unroll
+    for (int a = 0; a < 3; a++) p[a] += f[a] * dt;
+    if (grp >= 0) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, f);
+    nd.px[n] = p[0];
+    nd.py[n] = p[1];
+    nd.fx[n] = f[0];
+    nd.fy[n] = f[1];
+    if (DIM == 3) {
+        nd.pz[n] = p[2];
+        nd.fz[n] = f[2];
+    }
+    node_velocity(nd, n, m, p);
+}
+
+// UpdateStrainsLastContactTask: p = second extrapolation, UPDATE_STRAINS_LAST_CALL
+// conditions, grid velocity (UpdateStrainsLastContactTask.cpp:60-152).
+template <int DIM>
+__global__ void k_node_usl(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, double t, double dt) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nnodes || !nd.active[n]) return;
+    double p[3] = {nd.ux[n], nd.uy[n], DIM == 3 ? nd.uz[n] : 0.};
+    const double m = nd.mass[n];
+    const int grp = bc_group[n];
+    if (grp >= 0) {
+        double f[3] = {0., 0., 0.};
+        node_bcs(b, grp, BC_UPDATE_STRAINS_LAST, m, t, dt, p, f);
+    }
+    nd.px[n] = p[0];
+    nd.py[n] = p[1];
+    if (DIM == 3) nd.pz[n] = p[2];
+    node_velocity(nd, n, m, p);
+}
+
+}  // namespace nmg

@@ -1,0 +1,230 @@
+// sort.cuh -- stable LSD radix sort of particles by element (cell) and the
+// permutation of every particle column.
+//
+// The reference keeps particles in mpm[] order and walks them per patch
+// (GridPatch, NairnMPM/src/Patches/GridPatch.cpp:256-278); on the GPU the
+// particles are re-ordered by cell so that the particles of a warp touch the
+// same grid nodes, which keeps the P2G atomics and G2P gathers in L2.  The sort
+// is stable and deterministic: equal keys keep their previous relative order,
+// so the permutation is a pure function of the element array.
+//
+// Each warp owns a tile of kTile keys.  Pass = histogram per tile, one
+// exclusive scan over (digit, tile), then a scatter in which each warp ranks
+// its keys round by round with __match_any_sync.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include "mpm_device.cuh"
+
+namespace nmg {
+
+constexpr int kSortWarpsPerBlock = 4;
+constexpr int kTile = 32 * 16;  // keys per warp tile
+
+struct SortWorkspace {
+    int n = 0, nelems = 0, ntiles = 0, bits = 0;
+    int *keys[2] = {nullptr, nullptr};
+    int *vals[2] = {nullptr, nullptr};
+    int *hist = nullptr;       // 256 * ntiles
+    double *scratch = nullptr; // ncols * n doubles (the other particle buffer)
+    int *iscratch = nullptr;   // 3 * n ints
+    size_t scratch_cols = 0;
+};
+
+__global__ void k_sort_init(const int *elem, int *k, int *v, int n) {
+    int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n) {
+        k[i] = elem[i];
+        v[i] = i;
+    }
+}
+
+__global__ void k_sort_hist(const int *keys, int n, int shift, int *hist, int ntiles) {
+    __shared__ int h[kSortWarpsPerBlock][256];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x * kSortWarpsPerBlock + w;
+    for (int d = lane; d < 256; d += 32) h[w][d] = 0;
+    __syncwarp();
+    if (tile < ntiles) {
+        const int base = tile * kTile;
+        for (int j = lane; j < kTile; j += 32) {
+            const int i = base + j;
+            if (i < n) atomicAdd(&h[w][(keys[i] >> shift) & 255], 1);
+        }
+    }
+    __syncwarp();
+    if (tile < ntiles)
+        for (int d = lane; d < 256; d += 32) hist[d * ntiles + tile] = h[w][d];
+}
+
+// exclusive scan of m ints in one block of 1024 threads
+__global__ void k_sort_scan(int *a, int m) {
+    __shared__ int part[1024];
+    const int t = threadIdx.x;
+    const int per = (m + 1023) / 1024;
+    const int lo = t * per, hi = min(lo + per, m);
+    int s = 0;
+    for (int i = lo; i < hi; i++) s += a[i];
+    part[t] = s;
+    __syncthreads();
+    for (int off = 1; off < 1024; off <<= 1) {
+        int v = t >= off ? part[t - off] : 0;
+        __syncthreads();
+        part[t] += v;
+        __syncthreads();
+    }
+    int run = part[t] - s;
+    for (int i = lo; i < hi; i++) {
+        int v = a[i];
+        a[i] = run;
+        run += v;
+    }
+}
+
+__global__ void k_sort_scatter(const int *kin, const int *vin, int *kout, int *vout, int n, int shift,
+                               const int *offs, int ntiles) {
+    __shared__ int run[kSortWarpsPerBlock][256];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int tile = blockIdx.x * kSortWarpsPerBlock + w;
+    if (tile >= ntiles) return;
+    for (int d = lane; d < 256; d += 32) run[w][d] = offs[d * ntiles + tile];
+    __syncwarp();
+    const int base = tile * kTile;
+    const unsigned lt = (1u << lane) - 1u;
+    for (int r = 0; r < kTile; r += 32) {
+        const int i = base + r + lane;
+        const bool ok = i < n;
+        const int key = ok ? kin[i] : 0;
+        const int d = ok ? (key >> shift) & 255 : 256 + lane;  // out-of-range lanes never match
+        const unsigned peers = __match_any_sync(0xffffffffu, d);
+        const int rank = __popc(peers & lt);
+        int dst = 0;
+        if (ok) dst = run[w][d] + rank;
+        __syncwarp();
+        if (ok && rank == 0) run[w][d] += __popc(peers);
+        __syncwarp();
+        if (ok) {
+            kout[dst] = key;
+            vout[dst] = vin[i];
+        }
+    }
+}
+
+// dst[k*n + j] = src[k*n + perm[j]] for every column k
+__global__ void k_gather_cols(const double *__restrict__ src, double *__restrict__ dst, const int *__restrict__ perm,
+                              int n, int ncols) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int s = perm[j];
+    for (int k = 0; k < ncols; k++) dst[(size_t)k * n + j] = src[(size_t)k * n + s];
+}
+
+__global__ void k_gather_ints(const int *__restrict__ src, int *__restrict__ dst, const int *__restrict__ perm, int n,
+                              int ncols) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int s = perm[j];
+    for (int k = 0; k < ncols; k++) dst[(size_t)k * n + j] = src[(size_t)k * n + s];
+}
+
+// dst[k*n + orig[j]] = src[k*n + j] (slot j holds host particle orig[j])
+__global__ void k_unsort_cols(const double *__restrict__ src, double *__restrict__ dst, const int *__restrict__ orig,
+                              int n, int ncols) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int o = orig[j];
+    for (int k = 0; k < ncols; k++) dst[(size_t)k * n + o] = src[(size_t)k * n + j];
+}
+
+__global__ void k_unsort_ints(const int *__restrict__ src, int *__restrict__ dst, const int *__restrict__ orig, int n,
+                              int ncols) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int o = orig[j];
+    for (int k = 0; k < ncols; k++) dst[(size_t)k * n + o] = src[(size_t)k * n + j];
+}
+
+inline void sort_free(SortWorkspace &w) {
+    for (int b = 0; b < 2; b++) {
+        if (w.keys[b]) cudaFree(w.keys[b]);
+        if (w.vals[b]) cudaFree(w.vals[b]);
+        w.keys[b] = w.vals[b] = nullptr;
+    }
+    if (w.hist) cudaFree(w.hist);
+    if (w.scratch) cudaFree(w.scratch);
+    if (w.iscratch) cudaFree(w.iscratch);
+    w.hist = nullptr;
+    w.scratch = nullptr;
+    w.iscratch = nullptr;
+    w.n = 0;
+}
+
+inline int sort_alloc(SortWorkspace &w, int n, int nelems, int ncols) {
+    sort_free(w);
+    w.n = n;
+    w.nelems = nelems;
+    w.ntiles = (n + kTile - 1) / kTile;
+    w.bits = 1;
+    while ((1LL << w.bits) < (long long)nelems) w.bits++;
+    w.scratch_cols = (size_t)ncols;
+    bool ok = true;
+    for (int b = 0; b < 2; b++) {
+        ok &= cudaMalloc(&w.keys[b], sizeof(int) * n) == cudaSuccess;
+        ok &= cudaMalloc(&w.vals[b], sizeof(int) * n) == cudaSuccess;
+    }
+    ok &= cudaMalloc(&w.hist, sizeof(int) * 256 * w.ntiles) == cudaSuccess;
+    ok &= cudaMalloc(&w.scratch, sizeof(double) * (size_t)ncols * n) == cudaSuccess;
+    ok &= cudaMalloc(&w.iscratch, sizeof(int) * 3 * (size_t)n) == cudaSuccess;
+    if (!ok) {
+        sort_free(w);
+        return 1;
+    }
+    return 0;
+}
+
+// Sort by element, permute every column into the scratch buffers and swap the
+// buffers with the live ones.  Column k of the double block holds
+// pblock + k*n; the int block holds mat, elem, orig.
+void relink_particles(DevParticles &p, double *pblock, int *iblock, int **orig);
+
+inline int sort_particles(SortWorkspace &w, DevParticles &p, double *&pblock, int *&iblock, int *&orig, int ncols,
+                          cudaStream_t s) {
+    const int n = p.n;
+    if (n <= 0) return 0;
+    const int TB = 256;
+    const int pb = (n + TB - 1) / TB;
+    k_sort_init<<<pb, TB, 0, s>>>(p.elem, w.keys[0], w.vals[0], n);
+    int cur = 0;
+    const int tb = (w.ntiles + kSortWarpsPerBlock - 1) / kSortWarpsPerBlock;
+    for (int shift = 0; shift < w.bits; shift += 8) {
+        k_sort_hist<<<tb, 32 * kSortWarpsPerBlock, 0, s>>>(w.keys[cur], n, shift, w.hist, w.ntiles);
+        k_sort_scan<<<1, 1024, 0, s>>>(w.hist, 256 * w.ntiles);
+        k_sort_scatter<<<tb, 32 * kSortWarpsPerBlock, 0, s>>>(w.keys[cur], w.vals[cur], w.keys[1 - cur],
+                                                              w.vals[1 - cur], n, shift, w.hist, w.ntiles);
+        cur = 1 - cur;
+    }
+    const int *perm = w.vals[cur];
+    k_gather_cols<<<pb, TB, 0, s>>>(pblock, w.scratch, perm, n, ncols);
+    k_gather_ints<<<pb, TB, 0, s>>>(iblock, w.iscratch, perm, n, 3);  // mat, elem, orig
+    if (cudaGetLastError() != cudaSuccess) return 1;
+    double *old = pblock;
+    pblock = w.scratch;
+    w.scratch = old;
+    int *oldi = iblock;
+    iblock = w.iscratch;
+    w.iscratch = oldi;
+    relink_particles(p, pblock, iblock, &orig);
+    return 0;
+}
+
+inline int unsort_to_scratch(SortWorkspace &w, const DevParticles &p, const int *orig, const double *pblock, int ncols,
+                             cudaStream_t s) {
+    const int n = p.n;
+    const int TB = 256, pb = (n + TB - 1) / TB;
+    k_unsort_cols<<<pb, TB, 0, s>>>(pblock, w.scratch, orig, n, ncols);
+    k_unsort_ints<<<pb, TB, 0, s>>>(p.mat, w.iscratch, orig, n, 2);
+    return cudaGetLastError() == cudaSuccess ? 0 : 1;
+}
+
+}  // namespace nmg

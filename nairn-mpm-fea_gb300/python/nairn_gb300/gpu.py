@@ -1,0 +1,128 @@
+"""Python binding of the C ABI in libnairn_mpm_gb300.so (include/nairn_mpm_gpu.h).
+
+The library is the product: CUDA kernels plus the C ABI a NairnMPM host task
+calls.  This module loads it in-tree (nairn-mpm-fea_gb300/lib/) and fails
+loudly when it is missing -- there is no CPU fallback.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+from .model import Model
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+PKG = os.path.dirname(os.path.dirname(HERE))
+LIBPATH = os.path.join(PKG, "lib", "libnairn_mpm_gb300.so")
+
+_lib = None
+
+
+class GpuError(RuntimeError):
+    def __init__(self, status: int, msg: str):
+        super().__init__(f"{abi.STATUS_NAMES.get(status, status)}: {msg}")
+        self.status = status
+
+
+def lib():
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(LIBPATH):
+        raise RuntimeError(f"{LIBPATH} is missing: build it with __graft_entry__.build()")
+    L = C.CDLL(LIBPATH)
+    P = C.POINTER
+    L.mpmgpu_abi_version.restype = C.c_int
+    L.mpmgpu_create.argtypes = [P(abi.MpmGpuGrid), P(abi.MpmGpuOptions), P(C.c_void_p)]
+    L.mpmgpu_set_materials.argtypes = [C.c_void_p, P(abi.MpmGpuMaterial), C.c_int32]
+    L.mpmgpu_set_contact.argtypes = [C.c_void_p, P(abi.MpmGpuContact)]
+    L.mpmgpu_set_velocity_bcs.argtypes = [C.c_void_p, P(abi.MpmGpuVelBC), C.c_int32]
+    L.mpmgpu_upload_particles.argtypes = [C.c_void_p, P(abi.MpmGpuParticles)]
+    L.mpmgpu_step.argtypes = [C.c_void_p, C.c_int32, C.c_double]
+    L.mpmgpu_download_particles.argtypes = [C.c_void_p, P(abi.MpmGpuParticles)]
+    L.mpmgpu_last_error.argtypes = [C.c_void_p]
+    L.mpmgpu_last_error.restype = C.c_char_p
+    L.mpmgpu_destroy.argtypes = [C.c_void_p]
+    L.mpmgpu_destroy.restype = None
+    L.mpmgpu_profile.argtypes = [C.c_void_p, P(C.c_char_p), P(C.c_double), C.c_int32]
+    L.mpmgpu_set_profiling.argtypes = [C.c_void_p, C.c_int32]
+    L.mpmgpu_stream.argtypes = [C.c_void_p]
+    L.mpmgpu_stream.restype = C.c_void_p
+    for f in ("mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact", "mpmgpu_set_velocity_bcs",
+              "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles", "mpmgpu_profile",
+              "mpmgpu_set_profiling"):
+        getattr(L, f).restype = C.c_int
+    _lib = L
+    return L
+
+
+# every symbol the header declares (checked by the CPU tests)
+EXPORTED = ("mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
+            "mpmgpu_set_velocity_bcs", "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles",
+            "mpmgpu_last_error", "mpmgpu_destroy", "mpmgpu_profile")
+
+
+class GpuRun:
+    """One MPM run resident on the current GPU."""
+
+    def __init__(self, model: Model, precision: int = 0, p2g: int = 0, sort_interval: int = 1):
+        L = lib()
+        self.model = model
+        self._b = abi.Bound()
+        g = abi.grid_struct(model, self._b)
+        o = abi.options_struct(model, precision=precision, p2g=p2g, sort_interval=sort_interval)
+        h = C.c_void_p()
+        st = L.mpmgpu_create(C.byref(g), C.byref(o), C.byref(h))
+        if st != 0:
+            raise GpuError(st, L.mpmgpu_last_error(None).decode())
+        self.h = h
+        self._check(L.mpmgpu_set_materials(self.h, abi.materials_array(model), len(model.materials)))
+        bcs, nbc = abi.bcs_array(model)
+        self._check(L.mpmgpu_set_velocity_bcs(self.h, bcs, nbc))
+        self.t = 0.0
+
+    def _check(self, st):
+        if st != 0:
+            raise GpuError(st, lib().mpmgpu_last_error(self.h).decode())
+
+    def upload(self, particles: dict):
+        b = abi.Bound()
+        ps = abi.particles_struct(particles, b)
+        self._check(lib().mpmgpu_upload_particles(self.h, C.byref(ps)))
+
+    def step(self, nsteps: int):
+        self._check(lib().mpmgpu_step(self.h, int(nsteps), float(self.t)))
+        self.t += nsteps * self.model.options["timestep"]
+
+    def download(self, like: dict) -> dict:
+        out = abi.empty_like_particles(like)
+        b = abi.Bound()
+        ps = abi.particles_struct(out, b)
+        self._check(lib().mpmgpu_download_particles(self.h, C.byref(ps)))
+        return out
+
+    def set_profiling(self, on: bool):
+        self._check(lib().mpmgpu_set_profiling(self.h, 1 if on else 0))
+
+    def profile(self) -> dict:
+        names = (C.c_char_p * 16)()
+        ms = (C.c_double * 16)()
+        k = lib().mpmgpu_profile(self.h, names, ms, 16)
+        return {names[i].decode(): ms[i] for i in range(k)}
+
+    def stream(self) -> int:
+        return lib().mpmgpu_stream(self.h)
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mpmgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass

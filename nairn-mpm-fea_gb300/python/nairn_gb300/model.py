@@ -205,10 +205,15 @@ def _new_particles(pos, elem, g: Grid, ppc_side: int, rho_gcc: float, thick: flo
     return p
 
 
+GIMP_NAMES = {"Classic": SHAPE_LINEAR, "Dirac": SHAPE_LINEAR, "uGIMP": SHAPE_UGIMP, "GIMP": SHAPE_UGIMP,
+              "lCPDI": SHAPE_LCPDI, "CPDI": SHAPE_LCPDI}
+
+
 def cantilever_2d(nx=100, ny=20, cell=1.0, ppc_side=2, E=1000., nu=0.33, rho=1.0, v0=1000.,
-                  steps=1000, cfl=0.4, shape=SHAPE_UGIMP, method=USAVG, margin_cells=4) -> Model:
+                  steps=1000, cfl=0.4, gimp="uGIMP", method=USAVG, margin_cells=4, **_ignored) -> Model:
     """Model of inputs.cantilever_2d (same arguments)."""
     from . import inputs
+    shape = GIMP_NAMES[gimp]
     L, H, m = nx * cell, ny * cell, margin_cells * cell
     g = make_grid(2, (-m, L + m), (-m, H + m), None, cell, 1.0)
     pos, elem = _element_points(g, ppc_side)
@@ -249,10 +254,11 @@ def _line_contains(x, y, x1, y1, x2, y2, tol):
 
 
 def taylor_3d(radius=5.0, length=25.0, cell=0.25, ppc_side=2, v0=-200000., E=200000., nu=0.3,
-              yield_=300., Ep=2000., rho=7.8, steps=2000, cfl=0.5, shape=SHAPE_UGIMP, method=USAVG,
-              lateral_margin=None) -> Model:
+              yield_=300., Ep=2000., rho=7.8, steps=2000, cfl=0.5, gimp="uGIMP", method=USAVG,
+              lateral_margin=None, **_ignored) -> Model:
     """Model of inputs.taylor_3d (same arguments)."""
     from . import inputs
+    shape = GIMP_NAMES[gimp]
     lm = lateral_margin if lateral_margin is not None else max(4 * cell, 0.8 * radius)
     xr = radius + lm
     g = make_grid(3, (-xr, xr), (-xr, xr), (-4 * cell, length + 4 * cell), cell)

@@ -1,0 +1,67 @@
+"""Shared test helpers.  GPU tests are marked ``gpu``; everything else runs on CPU."""
+import json
+import os
+import sys
+
+import numpy as np
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+sys.path.insert(0, os.path.join(ROOT, "nairn-mpm-fea_gb300", "python"))
+sys.path.insert(0, os.path.join(ROOT, "oracle"))
+GOLDEN = os.path.join(ROOT, "tests", "golden")
+
+
+def pytest_configure(config):
+    config.addinivalue_line("markers", "gpu: needs a CUDA GPU (GB300)")
+
+
+def golden_cases():
+    return sorted(f[:-4] for f in os.listdir(GOLDEN) if f.endswith(".npz"))
+
+
+def load_golden(name):
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    meta = json.loads(str(d["meta"]))
+    return meta, {k: d[k] for k in d.files if k != "meta"}
+
+
+def model_for(meta):
+    from nairn_gb300 import model
+    return getattr(model, meta["generator"])(**meta["kwargs"])
+
+
+def rel_l2(a, b):
+    a = np.asarray(a, dtype=np.float64)
+    b = np.asarray(b, dtype=np.float64)
+    nb = np.linalg.norm(b)
+    return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
+
+
+def archive_view(p, dim, rho_gcc):
+    """Particle dict -> the quantities a NairnMPM archive stores (ArchiveData.cpp:807-930)."""
+    P = p["pressure"]
+    rho = rho_gcc * 1e-3
+    if dim == 2:
+        pos = np.stack([p["x"], p["y"]], 1)
+        vel = np.stack([p["vx"], p["vy"]], 1)
+        st = np.stack([p["sxx"] - P, p["syy"] - P, p["szz"] - P, p["sxy"]], 1) * rho
+        ep = np.stack([p["exx"], p["eyy"], p["ezz"], p["exy"]], 1)
+        pl = np.stack([p["pxx"], p["pyy"], p["pzz"], p["pxy"]], 1)
+    else:
+        pos = np.stack([p["x"], p["y"], p["z"]], 1)
+        vel = np.stack([p["vx"], p["vy"], p["vz"]], 1)
+        st = np.stack([p["sxx"] - P, p["syy"] - P, p["szz"] - P, p["sxy"], p["sxz"], p["syz"]], 1) * rho
+        ep = np.stack([p["exx"], p["eyy"], p["ezz"], p["exy"], p["exz"], p["eyz"]], 1)
+        pl = np.stack([p["pxx"], p["pyy"], p["pzz"], p["pxy"], p["pxz"], p["pyz"]], 1)
+    return dict(pos=pos, vel=vel, stress=st, strain=ep, plastic=pl, hist1=p["hist0"], elem=p["elem"] + 1)
+
+
+@pytest.fixture(scope="session")
+def gpu_lib():
+    import __graft_entry__ as g  # noqa: F401
+    sys.path.insert(0, ROOT)
+    import __graft_entry__
+    __graft_entry__.build_library()
+    from nairn_gb300 import gpu
+    return gpu.lib()

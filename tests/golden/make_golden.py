@@ -1,0 +1,88 @@
+"""Generate the golden fixtures from the reference NairnMPM built from source.
+
+Run in a container that has the reference tree and the oracle build:
+
+    make -C oracle/ref -j8            # builds oracle/_ref/NairnMPM
+    python tests/golden/make_golden.py
+
+For every case it writes the synthetic XML (nairn_gb300.inputs), runs
+``NairnMPM -np 1`` (single patch, the reference's deterministic order), reads
+the t=0 and final binary archives, and stores both plus the generator
+arguments in tests/golden/<case>.npz.  The GPU parity tests and the oracle pin
+tests replay these files; nothing at test time runs the reference.
+"""
+from __future__ import annotations
+
+import json
+import os
+import shutil
+import subprocess
+import sys
+import tempfile
+
+import numpy as np
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(os.path.dirname(HERE))
+sys.path.insert(0, os.path.join(ROOT, "nairn-mpm-fea_gb300", "python"))
+from nairn_gb300 import inputs  # noqa: E402
+from nairn_gb300.archive import read_archive  # noqa: E402
+
+REF = os.path.join(ROOT, "oracle", "_ref", "NairnMPM")
+
+# name -> (generator, kwargs); kwargs are shared with nairn_gb300.model
+CASES = {
+    "cant2d_ugimp_usavg": ("cantilever_2d", dict(nx=10, ny=4, steps=60)),
+    "cant2d_ugimp_usavg_long": ("cantilever_2d", dict(nx=24, ny=6, steps=400)),
+    "cant2d_linear_usavg": ("cantilever_2d", dict(nx=10, ny=4, steps=60, gimp="Classic")),
+    "cant2d_ugimp_usf": ("cantilever_2d", dict(nx=10, ny=4, steps=60, method=0)),
+    "cant2d_ugimp_usl": ("cantilever_2d", dict(nx=10, ny=4, steps=60, method=3)),
+    "cant2d_ugimp_ppc3": ("cantilever_2d", dict(nx=8, ny=3, steps=40, ppc_side=3)),
+    "taylor3d_ugimp_usavg": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30)),
+    "taylor3d_ugimp_long": ("taylor_3d", dict(radius=1.5, length=3.0, cell=0.5, steps=120)),
+    "taylor3d_linear_usavg": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, gimp="Classic")),
+    "taylor3d_ugimp_usl": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, method=3)),
+}
+
+KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")
+
+
+def run_case(name, gen, kw, workdir):
+    xml, info = getattr(inputs, gen)(archive_root="Results/out.", **kw)
+    d = os.path.join(workdir, name)
+    os.makedirs(os.path.join(d, "Results"), exist_ok=True)
+    with open(os.path.join(d, "in.xml"), "w") as fh:
+        fh.write(xml)
+    out = subprocess.run([REF, "-np", "1", "in.xml"], cwd=d, capture_output=True, text=True)
+    if out.returncode != 0 or "RUN COMPLETED" not in out.stdout:
+        raise RuntimeError(f"{name}: reference failed\n{out.stdout[-2000:]}\n{out.stderr[-2000:]}")
+    steps = int(out.stdout.split("Calculation Steps:")[1].split()[0])
+    assert steps == kw["steps"], (name, steps)
+    a0 = read_archive(os.path.join(d, "Results", "out.0"))
+    a1 = read_archive(os.path.join(d, "Results", f"out.{steps}"))
+    arrays = {}
+    for k in KEEP:
+        if k in a0:
+            arrays["init_" + k] = a0[k]
+        if k in a1:
+            arrays["final_" + k] = a1[k]
+    meta = dict(generator=gen, kwargs=kw, steps=steps, three_d=bool(a0["three_d"]), order=a0["order"],
+                time_ms=a1["time_ms"])
+    np.savez_compressed(os.path.join(HERE, name + ".npz"), meta=json.dumps(meta), **arrays)
+    return steps, len(a0["mass"])
+
+
+def main():
+    if not os.path.exists(REF):
+        sys.exit(f"{REF} not built: make -C oracle/ref -j8")
+    work = tempfile.mkdtemp(prefix="nairn_golden_")
+    try:
+        for name, (gen, kw) in CASES.items():
+            steps, n = run_case(name, gen, kw, work)
+            print(f"{name}: {n} particles, {steps} steps")
+    finally:
+        shutil.rmtree(work)
+
+
+if __name__ == "__main__":
+    main()

@@ -1,0 +1,40 @@
+"""The C ABI library loads and exports every symbol include/nairn_mpm_gpu.h declares."""
+import ctypes
+import os
+import re
+
+from conftest import ROOT
+
+
+def header_symbols():
+    src = open(os.path.join(ROOT, "include", "nairn_mpm_gpu.h")).read()
+    return sorted(set(re.findall(r"\b(mpmgpu_[a-z_]+)\s*\(", src)))
+
+
+def test_header_lists_expected_entry_points():
+    syms = header_symbols()
+    for s in ("mpmgpu_create", "mpmgpu_step", "mpmgpu_upload_particles", "mpmgpu_download_particles",
+              "mpmgpu_destroy", "mpmgpu_last_error"):
+        assert s in syms
+
+
+def test_library_exports_header_symbols(gpu_lib):
+    lib = ctypes.CDLL(os.path.join(ROOT, "nairn-mpm-fea_gb300", "lib", "libnairn_mpm_gb300.so"))
+    for s in header_symbols():
+        assert hasattr(lib, s), s
+    assert lib.mpmgpu_abi_version() == 1
+
+
+def test_create_rejects_bad_options_without_gpu_work(gpu_lib):
+    """Argument validation happens on the host before any device call."""
+    import ctypes as C
+    from nairn_gb300 import abi, model
+    m = model.cantilever_2d(nx=6, ny=3, steps=5)
+    b = abi.Bound()
+    g = abi.grid_struct(m, b)
+    o = abi.options_struct(m)
+    o.shape = 11  # qCPDI is not implemented
+    h = C.c_void_p()
+    st = gpu_lib.mpmgpu_create(C.byref(g), C.byref(o), C.byref(h))
+    assert st == 2 and not h.value
+    assert b"shape" in gpu_lib.mpmgpu_last_error(None)

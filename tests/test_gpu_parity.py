@@ -1,0 +1,70 @@
+"""GPU path against the reference's golden vectors and the CPU oracle (FP64 mode)."""
+import numpy as np
+import pytest
+
+from conftest import archive_view, golden_cases, load_golden, model_for, rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10  # relative L2, all-FP64 GPU mode vs the reference's FP64 path
+
+
+def gpu_run(m, steps, **kw):
+    from nairn_gb300.gpu import GpuRun
+    r = GpuRun(m, **kw)
+    r.upload(m.particles)
+    r.step(steps)
+    out = r.download(m.particles)
+    r.close()
+    return out
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_gpu_matches_reference(case, gpu_lib):
+    meta, g = load_golden(case)
+    m = model_for(meta)
+    out = gpu_run(m, meta["steps"])
+    v = archive_view(out, 3 if meta["three_d"] else 2, m.materials[0]["rho"])
+    for k in ("pos", "vel", "stress", "strain"):
+        assert rel_l2(v[k], g["final_" + k]) <= TOL, (k, rel_l2(v[k], g["final_" + k]))
+    if g["final_hist1"].any():
+        assert rel_l2(v["hist1"], g["final_hist1"]) <= TOL
+    # cell indexing is bit-exact
+    assert np.array_equal(v["elem"], g["final_elem"])
+
+
+@pytest.mark.parametrize("sort_interval", [0, 1, 7])
+def test_sort_interval_does_not_change_results(sort_interval, gpu_lib):
+    import oracle_lib
+    from nairn_gb300 import model, abi
+    m = model.taylor_3d(radius=1.5, length=3.0, cell=0.5, steps=40)
+    ref = abi.copy_particles(m.particles)
+    oracle_lib.run(m, ref, m.nsteps)
+    out = gpu_run(m, m.nsteps, sort_interval=sort_interval)
+    for k in ("x", "y", "z", "vx", "vz", "szz", "sxy", "hist0"):
+        assert rel_l2(out[k], ref[k]) <= TOL, k
+    assert np.array_equal(out["elem"], ref["elem"])
+
+
+def test_larger_2d_against_oracle(gpu_lib):
+    import oracle_lib
+    from nairn_gb300 import model, abi
+    m = model.cantilever_2d(nx=100, ny=20, steps=200)
+    ref = abi.copy_particles(m.particles)
+    oracle_lib.run(m, ref, m.nsteps, nthreads=4)
+    out = gpu_run(m, m.nsteps)
+    for k in ("x", "y", "vx", "vy", "sxx", "syy", "sxy", "szz"):
+        assert rel_l2(out[k], ref[k]) <= TOL, k
+
+
+def test_left_grid_is_reported(gpu_lib):
+    from nairn_gb300 import model
+    from nairn_gb300.gpu import GpuRun, GpuError
+    m = model.cantilever_2d(nx=6, ny=3, steps=5)
+    p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
+    p["vx"][0] = -1.e9
+    r = GpuRun(m)
+    r.upload(p)
+    with pytest.raises(GpuError, match="LEFT_GRID"):
+        r.step(2)
+    r.close()
