@@ -1,0 +1,368 @@
+#!/usr/bin/env python3
+"""Throughput of NairnMPM's explicit time step on GB300, in particle-steps/s.
+
+Workload (default): the 3D elastic-plastic Taylor impact -- von Mises with
+linear hardening (E=200 GPa, nu=0.3, yield 300 MPa, Ep 2 GPa, rho 7.8 g/cm^3),
+cylinder r=5 mm, L=25 mm at 200 m/s onto a rigid wall (zero normal velocity on
+the wall node plane), 0.25 mm cells, 2x2x2 particles per cell (~1.0 M
+particles), uGIMP, USAVG, all-FP64 path.  Inputs are synthetic (seeded,
+deterministic), built exactly as the reference's XML generator builds them.
+
+One "step" = one explicit MPM step over all particles (P2G, grid update with
+velocity BCs, strain/constitutive update, internal forces, momentum update,
+G2P, second extrapolation and strain update, element reset).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+Under torchrun (N>1) every rank runs an independent replica of the workload
+(the runs do not exchange data), so scaling is weak.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import math
+import os
+import statistics
+import subprocess
+import sys
+import tempfile
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.join(ROOT, "nairn-mpm-fea_gb300", "python"))
+
+METRIC = "particle-steps/s"
+KERNEL_NAMES = ("p2g", "node_post", "strain_forces", "node_update", "g2p", "node_usl", "strain_last", "sort")
+
+
+def parse():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=200)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--radius", type=float, default=5.0)
+    ap.add_argument("--length", type=float, default=25.0)
+    ap.add_argument("--cell", type=float, default=0.25)
+    ap.add_argument("--sort-interval", type=int, default=1)
+    ap.add_argument("--e2e-steps", type=int, default=20)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup():
+    ws = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    return ws, rank, local
+
+
+class Dist:
+    """Barrier and max-reduction across ranks (torch.distributed when launched by torchrun)."""
+
+    def __init__(self, ws, rank, local, backend):
+        self.ws, self.rank = ws, rank
+        self.pg = None
+        if ws > 1:
+            import torch
+            import torch.distributed as dist
+            os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+            if backend == "nccl":
+                torch.cuda.set_device(local)
+            dist.init_process_group(backend=backend)
+            self.dist = dist
+            self.torch = torch
+            self.dev = torch.device("cuda", local) if backend == "nccl" else torch.device("cpu")
+
+    def barrier(self):
+        if self.ws > 1:
+            self.dist.barrier()
+
+    def max(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.MAX)
+        return float(t.item())
+
+    def sum(self, v: float) -> float:
+        if self.ws == 1:
+            return v
+        t = self.torch.tensor([v], dtype=self.torch.float64, device=self.dev)
+        self.dist.all_reduce(t, op=self.dist.ReduceOp.SUM)
+        return float(t.item())
+
+    def close(self):
+        if self.ws > 1:
+            self.dist.destroy_process_group()
+
+
+def workload(args):
+    from nairn_gb300 import model
+    return model.taylor_3d(radius=args.radius, length=args.length, cell=args.cell,
+                           steps=args.steps + args.warmup)
+
+
+def workload_config(args, m, extra=None):
+    cfg = {"workload": "3D elastic-plastic Taylor impact (von Mises, linear hardening), r=%g mm, L=%g mm, "
+                       "%g mm cells, 2x2x2 particles/cell, uGIMP, USAVG, FP64" % (args.radius, args.length, args.cell),
+           "particles": m.n, "grid_nodes": m.grid.nnodes, "material": "IsoPlasticity + LinearHardening",
+           "timestep_s": m.options["timestep"],
+           "l2": ("particle state %.0f MB vs 129 MB L2: inputs larger than L2, no flush needed"
+                  if m.n * 39 * 8 > 129e6 else "particle state %.0f MB fits in L2") % (m.n * 39 * 8 / 1e6),
+           "parallelism": "replicas" if int(os.environ.get("WORLD_SIZE", "1")) > 1 else "single GPU"}
+    if extra:
+        cfg.update(extra)
+    return cfg
+
+
+# ---------------------------------------------------------------------------
+# roofline byte model: algorithmic bytes per launch of each kernel (each
+# particle column touched once, each node column of the active grid once)
+# ---------------------------------------------------------------------------
+def algorithmic_bytes(m, nodes_active: int) -> dict:
+    dim = m.grid.dim
+    d = 8
+    vec = dim * d
+    plastic = any(mm["type"] == 9 for mm in m.materials)
+    ten = (6 if dim == 3 else 4) * d
+    F = (9 if dim == 3 else 5) * d
+    state = F + ten + (d + ten + d + d if plastic else 0) + d  # F, sigma, (P, eps_p, alpha, plastic E), work
+    elem, mat = 4, 4
+    xi = dim * d
+    lp = dim * d
+    n = m.n
+    per_particle = {
+        "p2g": elem + vec + d + vec + lp + xi,                 # read elem,x,m,v,lp; write xi
+        "strain_forces": elem + xi + lp + mat + d + 2 * state,  # read geometry + state, write state
+        "g2p": elem + xi + lp + 2 * vec + d + 2 * vec,          # read v,x,m; write v,x
+        "strain_last": elem + xi + lp + mat + vec + 2 * state + elem,
+        "node_post": 0, "node_update": 0, "node_usl": 0, "sort": 0,
+    }
+    per_node = {
+        "p2g": 2 * (d + vec),                 # mass, momentum accumulated (read-modify-write)
+        "node_post": 1 + 4 + (d + vec) + 2 * vec,
+        "strain_forces": vec + 2 * vec,       # velocity gather, force accumulation
+        "node_update": 1 + 4 + d + 2 * vec + 3 * vec,
+        "g2p": d + 2 * vec + 2 * vec,         # v, f, m gathered; second momentum accumulated
+        "node_usl": 1 + 4 + d + vec + 2 * vec,
+        "strain_last": vec,
+        "sort": 0,
+    }
+    return {k: n * per_particle[k] + nodes_active * per_node[k] for k in per_particle}
+
+
+def active_nodes(m) -> int:
+    """Nodes of the cells that hold particles (the extrapolation support at t=0)."""
+    import numpy as np
+    g = m.grid
+    e = np.unique(m.particles["elem"])
+    col = e % g.nx
+    row = (e // g.nx) % g.ny
+    zr = e // (g.nx * g.ny)
+    nodes = set()
+    for dz in (0, 1) if g.dim == 3 else (0,):
+        for dy in (0, 1):
+            for dx in (0, 1):
+                nodes.update((((zr + dz) * (g.ny + 1) + row + dy) * (g.nx + 1) + col + dx).tolist())
+    return len(nodes)
+
+
+def peaks():
+    p = os.path.join(ROOT, "MEASURED_PEAKS.json")
+    if os.path.exists(p):
+        with open(p) as fh:
+            d = json.load(fh)
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+def traffic_from_profiles(kernel: str, n_particles: int):
+    """Per-launch DRAM bytes from the committed ncu summary, scaled to this size."""
+    p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        d = json.load(fh)
+    k = d.get("kernels", {}).get(kernel)
+    if not k:
+        return None
+    return k["dram_bytes_per_launch"] * n_particles / d["particles"]
+
+
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons sampled during a timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.path = None
+
+    def start(self):
+        fd, self.path = tempfile.mkstemp(suffix=".csv")
+        os.close(fd)
+        q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=open(self.path, "w"), stderr=subprocess.DEVNULL)
+        except OSError:
+            self.proc = None
+
+    def stop(self) -> dict:
+        if self.proc is None:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["nvidia-smi unavailable"]}
+        self.proc.terminate()
+        try:
+            self.proc.wait(timeout=5)
+        except subprocess.TimeoutExpired:
+            self.proc.kill()
+        sm, smax, reasons = [], [], set()
+        names = ("hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap")
+        with open(self.path) as fh:
+            for line in fh:
+                f = [x.strip() for x in line.split(",")]
+                if len(f) < 9:
+                    continue
+                try:
+                    sm.append(float(f[1]))
+                    smax.append(float(f[2]))
+                except ValueError:
+                    continue
+                for nm, v in zip(names, f[5:9]):
+                    if v.lower() == "active":
+                        reasons.add(nm)
+        os.unlink(self.path)
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(smax) if smax else None,
+                "samples": len(sm), "reasons": sorted(reasons)}
+
+
+def cpu_baseline(m, seconds: float):
+    """The CPU restatement of the reference step (oracle port), all host threads,
+    on a bounded sample of the same workload (the first steps of the run)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_lib
+    from nairn_gb300 import abi
+    threads = os.cpu_count() or 1
+    p = abi.copy_particles(m.particles)
+    t0 = time.perf_counter()
+    oracle_lib.run(m, p, 1, 0.0, nthreads=threads)
+    t1 = time.perf_counter() - t0
+    steps = max(1, min(200, int(seconds / max(t1, 1e-6))))
+    t0 = time.perf_counter()
+    oracle_lib.run(m, p, steps, m.options["timestep"], nthreads=threads)
+    dt = time.perf_counter() - t0
+    return {"value": m.n * steps / dt, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"{steps} steps (after 1 untimed) of the same {m.n}-particle workload, "
+                      f"{threads} OpenMP threads, FP64"}
+
+
+def run_reference(args, ws, rank, local):
+    if rank != 0:
+        return 0
+    m = workload(args)
+    b = cpu_baseline(m, args.cpu_seconds * max(1, args.steps) / 200.0 + 5.0)
+    line = {"metric": METRIC, "value": b["value"], "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": 1e3 * m.n / b["value"], "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "impl": "reference", "config": workload_config(args, m),
+            "cpu_baseline": b, "e2e": {"value": b["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
+                                        "d2h_bytes_per_step": 0}}
+    print(json.dumps(line))
+    return 0
+
+
+def main():
+    args = parse()
+    ws, rank, local = dist_setup()
+    if args.impl == "reference":
+        return run_reference(args, ws, rank, local)
+    import __graft_entry__
+    __graft_entry__.build_library()
+    os.environ.setdefault("CUDA_VISIBLE_DEVICES", os.environ.get("CUDA_VISIBLE_DEVICES", ""))
+    dist = Dist(ws, rank, local, "nccl" if ws > 1 else "gloo")
+    from nairn_gb300 import abi, gpu
+    m = workload(args)
+    n = m.n
+    run = gpu.GpuRun(m, sort_interval=args.sort_interval)
+    run.upload(m.particles)
+    run.step(args.warmup)
+    run.set_profiling(True)
+    launches0 = run.launch_count()
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    ms = run.step_timed(args.steps)
+    dist.barrier()
+    clk = clocks.stop()
+    launches = run.launch_count() - launches0
+    prof = run.profile()
+    run.set_profiling(False)
+    ms_max = dist.max(ms)
+    total_particles = dist.sum(float(n))
+    value = total_particles * args.steps / (ms_max / 1e3)
+
+    # end to end through the C ABI with host-resident particle state: every
+    # step uploads the state from pinned host memory and downloads the result
+    host = abi.copy_particles(m.particles)
+    pinned = gpu.pin(host)
+    h2d = sum(a.nbytes for k, a in host.items() if k not in ("x0", "y0", "z0"))
+    d2h = h2d
+    ke = max(1, args.e2e_steps)
+    run.upload(host)
+    run.step(1)
+    run.download_into(host)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        run.upload(host)
+        run.step(1)
+        run.download_into(host)
+    t_e2e = time.perf_counter() - t0
+    dist.barrier()
+    gpu.unpin(pinned)
+    t_e2e = dist.max(t_e2e)
+    e2e_value = total_particles * ke / t_e2e
+    run.close()
+
+    # roofline of the dominant kernel (largest share of the timed region)
+    fams = {k: v for k, v in prof.items() if v > 0}
+    dom = max(fams, key=fams.get)
+    per_step_launch = 1.0
+    launches_dom = args.steps if dom != "sort" else max(1, args.steps // max(1, args.sort_interval))
+    avg_ms = fams[dom] / (launches_dom * per_step_launch)
+    nodes = active_nodes(m)
+    bytes_model = algorithmic_bytes(m, nodes)
+    peak, peak_kind = peaks()
+    achieved = bytes_model[dom] / (avg_ms / 1e3) / 1e9
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": traffic_from_profiles(dom, n), "algorithmic_bytes_per_launch": bytes_model[dom],
+            "avg_launch_ms": avg_ms}
+    kernels = {k: {"ms_per_step": v / args.steps, "share": v / sum(fams.values()),
+                   "algorithmic_GBps": (bytes_model.get(k, 0) / ((v / launches_dom) / 1e3) / 1e9)
+                   if v > 0 and bytes_model.get(k, 0) > 0 else None}
+               for k, v in fams.items()}
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": workload_config(args, m, {"sort_interval": args.sort_interval,
+                                                "active_nodes_t0": nodes}),
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d * ws,
+                    "d2h_bytes_per_step": d2h * ws, "steps": ke,
+                    "note": "per step: upload full particle state from pinned host memory, one step, download"},
+            "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk}
+    if rank == 0 and ws == 1 and not args.no_cpu_baseline:
+        line["cpu_baseline"] = cpu_baseline(workload(args), args.cpu_seconds)
+    dist.close()
+    if rank == 0:
+        print(json.dumps(line))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())

@@ -193,6 +193,28 @@ void mpmgpu_destroy(MpmGpuCtx *ctx);
  * profile NairnMPM prints (NairnMPM.cpp:246-275, MPMTask.cpp:57-72). */
 int mpmgpu_profile(const MpmGpuCtx *ctx, const char **names, double *ms, int32_t cap);
 
+/* ---- extensions without a counterpart in the reference ----------------------
+ * Host-integration and measurement helpers of this library; a NairnMPM
+ * integration does not need them. */
+
+/* mpmgpu_step plus the device time of the enqueued steps (CUDA events on the
+ * context stream), in milliseconds. */
+int mpmgpu_step_timed(MpmGpuCtx *ctx, int32_t nsteps, double t0, double *ms);
+
+/* Per-kernel event timing for later mpmgpu_step calls (read with mpmgpu_profile). */
+int mpmgpu_set_profiling(MpmGpuCtx *ctx, int32_t on);
+
+/* The context's cudaStream_t, as an opaque pointer. */
+void *mpmgpu_stream(MpmGpuCtx *ctx);
+
+/* Number of kernels the context has launched so far. */
+long long mpmgpu_launch_count(const MpmGpuCtx *ctx);
+
+/* Page-lock caller memory (cudaHostRegister) so uploads and downloads of
+ * particle columns run as asynchronous DMA; unregister before freeing. */
+int mpmgpu_host_register(void *ptr, uint64_t bytes);
+int mpmgpu_host_unregister(void *ptr);
+
 #ifdef __cplusplus
 }
 #endif

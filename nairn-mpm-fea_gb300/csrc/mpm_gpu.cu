@@ -27,11 +27,20 @@ const int kParticleDoubles = 38;  // double columns of DevParticles besides zeta
 
 struct Profile {
     const char *name;
-    cudaEvent_t a, b;
     double ms;
 };
 
 }  // namespace
+
+// slot order = host order after an upload; flags out-of-range indices
+__global__ void k_upload_check(const int *mat, const int *elem, int *orig, int n, int nmat, int nelems,
+                               unsigned *err) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    orig[i] = i;
+    const int m = mat[i], e = elem[i];
+    if (m < 0 || m >= nmat || e < 0 || e >= nelems) atomicOr(err, 8u);
+}
 
 struct MpmGpuCtx {
     MpmGpuOptions opts{};
@@ -59,6 +68,8 @@ struct MpmGpuCtx {
     std::string msg;
     std::vector<Profile> prof;
     bool profile = false;
+    std::vector<cudaEvent_t> ev;         // per-step kernel events when profiling
+    long long launches = 0;              // kernels launched by this context
 };
 
 namespace {
@@ -289,12 +300,7 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     cudaMemset(c->err, 0, sizeof(unsigned));
     const char *names[] = {"p2g", "node_post", "strain_forces", "node_update", "g2p", "node_usl", "strain_last",
                            "sort"};
-    for (const char *n : names) {
-        Profile pr{n, nullptr, nullptr, 0.};
-        cudaEventCreate(&pr.a);
-        cudaEventCreate(&pr.b);
-        c->prof.push_back(pr);
-    }
+    for (const char *n : names) c->prof.push_back(Profile{n, 0.});
     if ((e = cudaGetLastError()) != cudaSuccess) {
         int st = cuda_fail(nullptr, e, "mpmgpu_create");
         mpmgpu_destroy(c);
@@ -388,39 +394,54 @@ int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
     if (!c || !h || h->n <= 0) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_upload_particles: bad argument");
     if (h->n > (1LL << 31) - 1) return set_err(c, MPMGPU_ERR_INVALID, "too many particles for one context");
     if (!c->mats) return set_err(c, MPMGPU_ERR_INVALID, "set materials before uploading particles");
+    if (!h->x || !h->y || !h->vx || !h->vy || !h->mass || !h->mat || !h->elem || !h->lpx || !h->lpy ||
+        (c->dim == 3 && (!h->z || !h->vz || !h->lpz)))
+        return set_err(c, MPMGPU_ERR_INVALID,
+                       "mpmgpu_upload_particles: position, velocity, mass, size, material and element columns are required");
     const int n = (int)h->n;
-    // validate materials and elements on the host before anything reaches the device
-    for (int i = 0; i < n; i++) {
-        if (h->mat[i] < 0 || h->mat[i] >= c->nmat) return set_err(c, MPMGPU_ERR_INVALID, "particle material out of range");
-        const int ne = c->g.nx * c->g.ny * (c->dim == 3 ? c->g.nz : 1);
-        if (h->elem[i] < 0 || h->elem[i] >= ne) return set_err(c, MPMGPU_ERR_INVALID, "particle element out of range");
-    }
-    free_particles(c);
-    size_t bytes = (size_t)n * kParticleDoubles * sizeof(double);
-    cudaError_t e = cudaMalloc(&c->pblock, bytes + (size_t)n * sizeof(double));  // + zeta column
-    if (e != cudaSuccess) return set_err(c, MPMGPU_ERR_OOM, std::string("particle allocation: ") + cudaGetErrorString(e));
-    e = cudaMalloc(&c->iblock, (size_t)n * 3 * sizeof(int));
-    if (e != cudaSuccess) {
+    const int nelems = c->g.nx * c->g.ny * (c->dim == 3 ? c->g.nz : 1);
+    const size_t dbytes = (size_t)n * (kParticleDoubles + 1) * sizeof(double);
+    if (c->p.n != n || !c->pblock) {
         free_particles(c);
-        return set_err(c, MPMGPU_ERR_OOM, std::string("particle allocation: ") + cudaGetErrorString(e));
+        cudaError_t e = cudaMalloc(&c->pblock, dbytes);
+        if (e == cudaSuccess) e = cudaMalloc(&c->iblock, (size_t)n * 3 * sizeof(int));
+        if (e != cudaSuccess) {
+            free_particles(c);
+            return set_err(c, MPMGPU_ERR_OOM, std::string("particle allocation: ") + cudaGetErrorString(e));
+        }
+        if (sort_alloc(c->sort, n, nelems, kParticleDoubles + 1) != 0) {
+            free_particles(c);
+            return set_err(c, MPMGPU_ERR_OOM, "sort workspace allocation failed");
+        }
+        CK(cudaMemsetAsync(c->pblock, 0, dbytes, c->stream));
+        c->p.n = n;
     }
-    CK(cudaMemsetAsync(c->pblock, 0, bytes + (size_t)n * sizeof(double), c->stream));
-    c->p.n = n;
     link_columns(c->p, c->pblock, c->iblock, &c->orig);
     double *hc[kParticleDoubles];
     hcols(h, hc);
-    for (int k = 0; k < kParticleDoubles; k++)
+    for (int k = 0; k < kParticleDoubles; k++) {
+        double *dst = c->pblock + (size_t)k * n;
         if (hc[k])
-            CK(cudaMemcpyAsync(c->pblock + (size_t)k * n, hc[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice,
-                               c->stream));
+            CK(cudaMemcpyAsync(dst, hc[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
+        else
+            CK(cudaMemsetAsync(dst, 0, (size_t)n * sizeof(double), c->stream));
+    }
     CK(cudaMemcpyAsync(c->p.mat, h->mat, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->p.elem, h->elem, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    std::vector<int> idx(n);
-    for (int i = 0; i < n; i++) idx[i] = i;
-    CK(cudaMemcpyAsync(c->orig, idx.data(), (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
-    int st = sort_alloc(c->sort, n, c->g.nx * c->g.ny * (c->dim == 3 ? c->g.nz : 1), kParticleDoubles + 1);
-    if (st != 0) return set_err(c, MPMGPU_ERR_OOM, "sort workspace allocation failed");
+    // identity slot order and a range check of the indices the kernels use
+    CK(cudaMemsetAsync(c->err, 0, sizeof(unsigned), c->stream));
+    const int TB = 256;
+    k_upload_check<<<(n + TB - 1) / TB, TB, 0, c->stream>>>(c->p.mat, c->p.elem, c->orig, n, c->nmat, nelems, c->err);
+    c->launches++;
+    unsigned flags = 0;
+    CK(cudaMemcpyAsync(&flags, c->err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
+    if (flags) {
+        cudaMemsetAsync(c->err, 0, sizeof(unsigned), c->stream);
+        cudaStreamSynchronize(c->stream);
+        return set_err(c, MPMGPU_ERR_INVALID, "particle material or element index out of range");
+    }
+    c->steps_done = 0;
     return MPMGPU_OK;
 }
 
@@ -428,8 +449,15 @@ int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
 
 namespace {
 
+constexpr int kFamilies = 8;  // p2g, node_post, strain_forces, node_update, g2p, node_usl, strain_last, sort
+
+// event of kernel family k in step slot `slot` of the current call
+inline cudaEvent_t &event_at(MpmGpuCtx *c, int slot, int k, bool begin) {
+    return c->ev[((size_t)slot * kFamilies + k) * 2 + (begin ? 0 : 1)];
+}
+
 template <int DIM, int SHAPE>
-void enqueue_step(MpmGpuCtx *c, double t) {
+void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     const int n = c->p.n, NN = c->g.nnodes;
     const int TB = 256;
     const int pb = (n + TB - 1) / TB, nb = (NN + TB - 1) / TB;
@@ -439,7 +467,8 @@ void enqueue_step(MpmGpuCtx *c, double t) {
     const double stLast = method == MPMGPU_USAVG ? dt - stFirst : dt;
     cudaStream_t s = c->stream;
     auto mark = [&](int k, bool begin) {
-        if (c->profile) cudaEventRecord(begin ? c->prof[k].a : c->prof[k].b, s);
+        if (c->profile) cudaEventRecord(event_at(c, slot, k, begin), s);
+        if (!begin) c->launches++;
     };
     cudaMemsetAsync(c->nblock, 0, c->nblock_zero_bytes, s);
     cudaMemsetAsync(c->nd.active, 0, (size_t)NN, s);
@@ -474,16 +503,26 @@ void enqueue_step(MpmGpuCtx *c, double t) {
     mark(6, false);
 }
 
-void enqueue(MpmGpuCtx *c, double t) {
+void enqueue(MpmGpuCtx *c, double t, int slot) {
     const bool d3 = c->dim == 3;
     const bool lin = c->opts.shape == MPMGPU_SHAPE_LINEAR;
     if (d3) {
-        if (lin) enqueue_step<3, SHAPE_LINEAR>(c, t);
-        else enqueue_step<3, SHAPE_UGIMP>(c, t);
+        if (lin) enqueue_step<3, SHAPE_LINEAR>(c, t, slot);
+        else enqueue_step<3, SHAPE_UGIMP>(c, t, slot);
     } else {
-        if (lin) enqueue_step<2, SHAPE_LINEAR>(c, t);
-        else enqueue_step<2, SHAPE_UGIMP>(c, t);
+        if (lin) enqueue_step<2, SHAPE_LINEAR>(c, t, slot);
+        else enqueue_step<2, SHAPE_UGIMP>(c, t, slot);
     }
+}
+
+int ensure_events(MpmGpuCtx *c, int nsteps) {
+    const size_t need = (size_t)nsteps * kFamilies * 2;
+    while (c->ev.size() < need) {
+        cudaEvent_t e;
+        if (cudaEventCreate(&e) != cudaSuccess) return 1;
+        c->ev.push_back(e);
+    }
+    return 0;
 }
 
 int error_status(MpmGpuCtx *c, unsigned bits) {
@@ -497,44 +536,79 @@ int error_status(MpmGpuCtx *c, unsigned bits) {
 
 extern "C" {
 
-int mpmgpu_step(MpmGpuCtx *c, int32_t nsteps, double t0) {
+}  // extern "C"
+
+namespace {
+
+// Enqueue nsteps steps; when ms is given, CUDA events on the context stream
+// bracket the enqueued work and *ms receives its device time.
+int step_impl(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
     if (!c || nsteps < 0) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step: bad argument");
     if (c->p.n <= 0 || !c->mats) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step: no particles or materials");
     for (auto &pr : c->prof) pr.ms = 0.;
+    if (c->profile && ensure_events(c, nsteps) != 0) return set_err(c, MPMGPU_ERR_CUDA, "event creation failed");
+    std::vector<char> sorted((size_t)nsteps, 0);
+    cudaEvent_t w0 = nullptr, w1 = nullptr;
+    if (ms) {
+        CK(cudaEventCreate(&w0));
+        CK(cudaEventCreate(&w1));
+        CK(cudaEventRecord(w0, c->stream));
+    }
     double t = t0;
     for (int s = 0; s < nsteps; s++) {
         if (c->opts.sort_interval > 0 && c->steps_done % c->opts.sort_interval == 0) {
-            if (c->profile) cudaEventRecord(c->prof[7].a, c->stream);
+            if (c->profile) cudaEventRecord(event_at(c, s, 7, true), c->stream);
             int st = sort_particles(c->sort, c->p, c->pblock, c->iblock, c->orig, kParticleDoubles + 1, c->stream);
             if (st != 0) return set_err(c, MPMGPU_ERR_CUDA, "particle sort failed");
-            if (c->profile) {
-                cudaEventRecord(c->prof[7].b, c->stream);
-                cudaEventSynchronize(c->prof[7].b);
-                float ms;
-                cudaEventElapsedTime(&ms, c->prof[7].a, c->prof[7].b);
-                c->prof[7].ms += ms;
-            }
+            c->launches += sort_launches(c->sort);
+            if (c->profile) cudaEventRecord(event_at(c, s, 7, false), c->stream);
+            sorted[s] = 1;
         }
-        enqueue(c, t);
-        if (c->profile) {
-            cudaStreamSynchronize(c->stream);
-            for (int k = 0; k < 7; k++) {
-                float ms = 0.f;
-                if (cudaEventElapsedTime(&ms, c->prof[k].a, c->prof[k].b) == cudaSuccess) c->prof[k].ms += ms;
-            }
-        }
+        enqueue(c, t, s);
         c->steps_done++;
         t += c->opts.timestep;
     }
+    if (ms) CK(cudaEventRecord(w1, c->stream));
     unsigned bits = 0;
     CK(cudaMemcpyAsync(&bits, c->err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaGetLastError());
+    if (ms) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, w0, w1);
+        *ms = f;
+        cudaEventDestroy(w0);
+        cudaEventDestroy(w1);
+    }
+    if (c->profile) {
+        const bool usl = c->opts.method != MPMGPU_USF;
+        for (int s = 0; s < nsteps; s++)
+            for (int k = 0; k < kFamilies; k++) {
+                if (k == 7 && !sorted[s]) continue;
+                if (!usl && (k == 5 || k == 6)) continue;
+                float ms = 0.f;
+                if (cudaEventElapsedTime(&ms, event_at(c, s, k, true), event_at(c, s, k, false)) == cudaSuccess)
+                    c->prof[k].ms += ms;
+            }
+    }
     if (bits) {
         cudaMemsetAsync(c->err, 0, sizeof(unsigned), c->stream);
         return error_status(c, bits);
     }
     return MPMGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpmgpu_step(MpmGpuCtx *c, int32_t nsteps, double t0) { return step_impl(c, nsteps, t0, nullptr); }
+
+// Extension: mpmgpu_step that also returns the device time of the enqueued
+// steps in *ms (CUDA events recorded on the context stream).
+int mpmgpu_step_timed(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
+    if (!ms) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step_timed: null ms");
+    return step_impl(c, nsteps, t0, ms);
 }
 
 int mpmgpu_download_particles(MpmGpuCtx *c, MpmGpuParticles *h) {
@@ -564,10 +638,7 @@ void mpmgpu_destroy(MpmGpuCtx *c) {
     if (c->bc_group) cudaFree(c->bc_group);
     if (c->bc_block) cudaFree(c->bc_block);
     if (c->err) cudaFree(c->err);
-    for (auto &pr : c->prof) {
-        if (pr.a) cudaEventDestroy(pr.a);
-        if (pr.b) cudaEventDestroy(pr.b);
-    }
+    for (auto &e : c->ev) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -594,5 +665,21 @@ int mpmgpu_set_profiling(MpmGpuCtx *c, int32_t on) {
 
 // Extension: the context's CUDA stream, for callers that time with their own events.
 void *mpmgpu_stream(MpmGpuCtx *c) { return c ? (void *)c->stream : nullptr; }
+
+// Extension: number of kernels this context has launched so far.
+long long mpmgpu_launch_count(const MpmGpuCtx *c) { return c ? c->launches : 0; }
+
+// Extension: page-lock caller memory so uploads and downloads run as async DMA.
+int mpmgpu_host_register(void *ptr, uint64_t bytes) {
+    if (!ptr || !bytes) return MPMGPU_ERR_INVALID;
+    cudaError_t e = cudaHostRegister(ptr, (size_t)bytes, cudaHostRegisterDefault);
+    return e == cudaSuccess ? MPMGPU_OK : cuda_fail(nullptr, e, "cudaHostRegister");
+}
+
+int mpmgpu_host_unregister(void *ptr) {
+    if (!ptr) return MPMGPU_ERR_INVALID;
+    cudaError_t e = cudaHostUnregister(ptr);
+    return e == cudaSuccess ? MPMGPU_OK : cuda_fail(nullptr, e, "cudaHostUnregister");
+}
 
 }  // extern "C"

@@ -218,6 +218,9 @@ inline int sort_particles(SortWorkspace &w, DevParticles &p, double *&pblock, in
     return 0;
 }
 
+// kernels one sort_particles call launches
+inline int sort_launches(const SortWorkspace &w) { return 1 + 3 * ((w.bits + 7) / 8) + 2; }
+
 inline int unsort_to_scratch(SortWorkspace &w, const DevParticles &p, const int *orig, const double *pblock, int ncols,
                              cudaStream_t s) {
     const int n = p.n;

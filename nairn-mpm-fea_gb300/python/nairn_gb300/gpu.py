@@ -51,6 +51,14 @@ def lib():
     L.mpmgpu_set_profiling.argtypes = [C.c_void_p, C.c_int32]
     L.mpmgpu_stream.argtypes = [C.c_void_p]
     L.mpmgpu_stream.restype = C.c_void_p
+    L.mpmgpu_step_timed.argtypes = [C.c_void_p, C.c_int32, C.c_double, P(C.c_double)]
+    L.mpmgpu_step_timed.restype = C.c_int
+    L.mpmgpu_launch_count.argtypes = [C.c_void_p]
+    L.mpmgpu_launch_count.restype = C.c_longlong
+    L.mpmgpu_host_register.argtypes = [C.c_void_p, C.c_uint64]
+    L.mpmgpu_host_register.restype = C.c_int
+    L.mpmgpu_host_unregister.argtypes = [C.c_void_p]
+    L.mpmgpu_host_unregister.restype = C.c_int
     for f in ("mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact", "mpmgpu_set_velocity_bcs",
               "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles", "mpmgpu_profile",
               "mpmgpu_set_profiling"):
@@ -60,7 +68,8 @@ def lib():
 
 
 # every symbol the header declares (checked by the CPU tests)
-EXPORTED = ("mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
+EXPORTED = ("mpmgpu_step_timed", "mpmgpu_set_profiling", "mpmgpu_stream", "mpmgpu_launch_count",
+            "mpmgpu_host_register", "mpmgpu_host_unregister", "mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
             "mpmgpu_set_velocity_bcs", "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles",
             "mpmgpu_last_error", "mpmgpu_destroy", "mpmgpu_profile")
 
@@ -97,6 +106,21 @@ class GpuRun:
         self._check(lib().mpmgpu_step(self.h, int(nsteps), float(self.t)))
         self.t += nsteps * self.model.options["timestep"]
 
+    def step_timed(self, nsteps: int) -> float:
+        """Advance nsteps; return their device time in ms (CUDA events on the context stream)."""
+        ms = C.c_double()
+        self._check(lib().mpmgpu_step_timed(self.h, int(nsteps), float(self.t), C.byref(ms)))
+        self.t += nsteps * self.model.options["timestep"]
+        return ms.value
+
+    def launch_count(self) -> int:
+        return int(lib().mpmgpu_launch_count(self.h))
+
+    def download_into(self, out: dict):
+        b = abi.Bound()
+        ps = abi.particles_struct(out, b)
+        self._check(lib().mpmgpu_download_particles(self.h, C.byref(ps)))
+
     def download(self, like: dict) -> dict:
         out = abi.empty_like_particles(like)
         b = abi.Bound()
@@ -116,6 +140,7 @@ class GpuRun:
     def stream(self) -> int:
         return lib().mpmgpu_stream(self.h)
 
+
     def close(self):
         if getattr(self, "h", None):
             lib().mpmgpu_destroy(self.h)
@@ -126,3 +151,17 @@ class GpuRun:
             self.close()
         except Exception:
             pass
+
+
+def pin(arrays: dict) -> list:
+    """Page-lock numpy arrays for DMA transfers; returns the registered list."""
+    done = []
+    for a in arrays.values():
+        if a.nbytes and lib().mpmgpu_host_register(a.ctypes.data, a.nbytes) == 0:
+            done.append(a)
+    return done
+
+
+def unpin(done: list):
+    for a in done:
+        lib().mpmgpu_host_unregister(a.ctypes.data)
