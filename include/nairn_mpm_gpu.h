@@ -193,6 +193,19 @@ void mpmgpu_destroy(MpmGpuCtx *ctx);
  * profile NairnMPM prints (NairnMPM.cpp:246-275, MPMTask.cpp:57-72). */
 int mpmgpu_profile(const MpmGpuCtx *ctx, const char **names, double *ms, int32_t cap);
 
+/* Stable radix sort of n particles by element (cell) index, the ordering step
+ * of the GPU path.  The reference assigns the element in
+ * ResetElementsTask::ResetElement / MeshInfo::FindElementFromPoint
+ * (ResetElementsTask.cpp:196-228, MeshInfo.cpp:593-633) and keeps mpm[] order;
+ * the device re-orders particles by that element each step.  d_elem and
+ * d_perm are device pointers of n ints; each d_elem[i] must lie in
+ * [0, nelems).  On return d_perm[j] is the slot of the j-th particle in
+ * (element, slot) order -- equal elements keep their slot order, so the result
+ * is bit-for-bit a stable argsort.  stream is a cudaStream_t (NULL: legacy
+ * default stream); the call synchronizes it.  Allocates its scratch with
+ * cudaMalloc. */
+int mpmgpu_sort_by_cell(const int32_t *d_elem, int32_t n, int32_t nelems, int32_t *d_perm, void *stream);
+
 /* ---- extensions without a counterpart in the reference ----------------------
  * Host-integration and measurement helpers of this library; a NairnMPM
  * integration does not need them. */

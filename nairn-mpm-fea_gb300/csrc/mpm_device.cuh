@@ -141,15 +141,34 @@ __device__ __forceinline__ void gimp_axis(double xi, double lp, double inv_size,
     }
 }
 
-// candidate order of the reference tables, packed (k_x | k_y<<2 | k_z<<4)
-__constant__ unsigned char c_cand2d[16] = {
-    0x05, 0x06, 0x0A, 0x09, 0x00, 0x01, 0x02, 0x03, 0x07, 0x0B, 0x0F, 0x0E, 0x0D, 0x0C, 0x08, 0x04};
-__constant__ unsigned char c_cand3d[64] = {
-    0x15, 0x16, 0x1A, 0x19, 0x25, 0x26, 0x2A, 0x29,
-    0x10, 0x11, 0x12, 0x13, 0x17, 0x1B, 0x1F, 0x1E, 0x1D, 0x1C, 0x18, 0x14,
-    0x20, 0x21, 0x22, 0x23, 0x27, 0x2B, 0x2F, 0x2E, 0x2D, 0x2C, 0x28, 0x24,
-    0x05, 0x06, 0x0A, 0x09, 0x00, 0x01, 0x02, 0x03, 0x07, 0x0B, 0x0F, 0x0E, 0x0D, 0x0C, 0x08, 0x04,
-    0x35, 0x36, 0x3A, 0x39, 0x30, 0x31, 0x32, 0x33, 0x37, 0x3B, 0x3F, 0x3E, 0x3D, 0x3C, 0x38, 0x34};
+// candidate order of the reference tables, packed (k_x | k_y<<2 | k_z<<4):
+// FourNodeIsoparam.cpp:27-30 (gxii, geti) and EightNodeIsoparamBrick.cpp
+// (x3off, y3off, z3off) with k = offset + 1.  Written as constexpr functions so
+// that, with the candidate loops fully unrolled, every index is a constant and
+// the per-axis factors stay in registers.
+__host__ __device__ constexpr unsigned cand2d(int c) {
+    return
+            c == 0 ? 0x05u : c == 1 ? 0x06u : c == 2 ? 0x0Au : c == 3 ? 0x09u : c == 4 ? 0x00u :
+            c == 5 ? 0x01u : c == 6 ? 0x02u : c == 7 ? 0x03u : c == 8 ? 0x07u : c == 9 ? 0x0Bu :
+            c == 10 ? 0x0Fu : c == 11 ? 0x0Eu : c == 12 ? 0x0Du : c == 13 ? 0x0Cu : c == 14 ? 0x08u :
+            c == 15 ? 0x04u : 0u;
+}
+__host__ __device__ constexpr unsigned cand3d(int c) {
+    return
+            c == 0 ? 0x15u : c == 1 ? 0x16u : c == 2 ? 0x1Au : c == 3 ? 0x19u : c == 4 ? 0x25u :
+            c == 5 ? 0x26u : c == 6 ? 0x2Au : c == 7 ? 0x29u : c == 8 ? 0x10u : c == 9 ? 0x11u :
+            c == 10 ? 0x12u : c == 11 ? 0x13u : c == 12 ? 0x17u : c == 13 ? 0x1Bu : c == 14 ? 0x1Fu :
+            c == 15 ? 0x1Eu : c == 16 ? 0x1Du : c == 17 ? 0x1Cu : c == 18 ? 0x18u : c == 19 ? 0x14u :
+            c == 20 ? 0x20u : c == 21 ? 0x21u : c == 22 ? 0x22u : c == 23 ? 0x23u : c == 24 ? 0x27u :
+            c == 25 ? 0x2Bu : c == 26 ? 0x2Fu : c == 27 ? 0x2Eu : c == 28 ? 0x2Du : c == 29 ? 0x2Cu :
+            c == 30 ? 0x28u : c == 31 ? 0x24u : c == 32 ? 0x05u : c == 33 ? 0x06u : c == 34 ? 0x0Au :
+            c == 35 ? 0x09u : c == 36 ? 0x00u : c == 37 ? 0x01u : c == 38 ? 0x02u : c == 39 ? 0x03u :
+            c == 40 ? 0x07u : c == 41 ? 0x0Bu : c == 42 ? 0x0Fu : c == 43 ? 0x0Eu : c == 44 ? 0x0Du :
+            c == 45 ? 0x0Cu : c == 46 ? 0x08u : c == 47 ? 0x04u : c == 48 ? 0x35u : c == 49 ? 0x36u :
+            c == 50 ? 0x3Au : c == 51 ? 0x39u : c == 52 ? 0x30u : c == 53 ? 0x31u : c == 54 ? 0x32u :
+            c == 55 ? 0x33u : c == 56 ? 0x37u : c == 57 ? 0x3Bu : c == 58 ? 0x3Fu : c == 59 ? 0x3Eu :
+            c == 60 ? 0x3Du : c == 61 ? 0x3Cu : c == 62 ? 0x38u : c == 63 ? 0x34u : 0u;
+}
 
 // ---------------------------------------------------------------------------
 // Constitutive updates (FP64).  du is the velocity gradient times the strain

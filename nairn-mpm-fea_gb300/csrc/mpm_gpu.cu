@@ -666,6 +666,30 @@ int mpmgpu_set_profiling(MpmGpuCtx *c, int32_t on) {
 // Extension: the context's CUDA stream, for callers that time with their own events.
 void *mpmgpu_stream(MpmGpuCtx *c) { return c ? (void *)c->stream : nullptr; }
 
+// Stable sort of particles by element: see include/nairn_mpm_gpu.h.
+int mpmgpu_sort_by_cell(const int32_t *d_elem, int32_t n, int32_t nelems, int32_t *d_perm, void *stream) {
+    MpmGpuCtx *c = nullptr;  // for CK: errors go to the static message
+    if (!d_elem || !d_perm || n <= 0 || nelems <= 0)
+        return set_err(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_sort_by_cell: bad argument");
+    cudaStream_t s = (cudaStream_t)stream;
+    int bits = 1;
+    while ((1LL << bits) < (long long)nelems) bits++;
+    const int ntiles = (n + kTile - 1) / kTile;
+    const size_t nsums = (size_t)(256 * ntiles + kScanChunk - 1) / kScanChunk + 1;
+    int *buf = nullptr;
+    const size_t ints = 4 * (size_t)n + 256 * (size_t)ntiles + nsums;
+    cudaError_t e = cudaMalloc(&buf, ints * sizeof(int));
+    if (e != cudaSuccess) return set_err(nullptr, MPMGPU_ERR_OOM, std::string("sort scratch: ") + cudaGetErrorString(e));
+    int *keys[2] = {buf, buf + n}, *vals[2] = {buf + 2 * (size_t)n, buf + 3 * (size_t)n};
+    int *hist = buf + 4 * (size_t)n, *sums = hist + 256 * (size_t)ntiles;
+    const int cur = radix_sort_keys(d_elem, n, bits, keys, vals, hist, sums, s);
+    e = cudaMemcpyAsync(d_perm, vals[cur], sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    cudaFree(buf);
+    if (e != cudaSuccess) return cuda_fail(c, e, "mpmgpu_sort_by_cell");
+    return MPMGPU_OK;
+}
+
 // Extension: number of kernels this context has launched so far.
 long long mpmgpu_launch_count(const MpmGpuCtx *c) { return c ? c->launches : 0; }
 

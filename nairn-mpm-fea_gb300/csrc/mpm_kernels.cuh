@@ -75,7 +75,7 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi
     if (DIM == 2) {
 #pragma unroll
         for (int c = 0; c < 16; c++) {
-            const unsigned code = c_cand2d[c];
+            const unsigned code = cand2d(c);
             const int kx = code & 3, ky = (code >> 2) & 3;
             if (!((ax.act >> kx) & (ay.act >> ky) & 1u)) continue;
             const double Sx = ax.S[kx], Sy = ay.S[ky];
@@ -89,9 +89,9 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi
     } else {
         gimp_axis<true, GRAD>(zeta, lpz, 1. / (4. * lpy), az);
         const double idz = GRAD ? 2.0 / DZ : 0.;
-#pragma unroll 4
+#pragma unroll
         for (int c = 0; c < 64; c++) {
-            const unsigned code = c_cand3d[c];
+            const unsigned code = cand3d(c);
             const int kx = code & 3, ky = (code >> 2) & 3, kz = (code >> 4) & 3;
             if (!((ax.act >> kx) & (ay.act >> ky) & (az.act >> kz) & 1u)) continue;
             const double Sx = ax.S[kx], Sy = ay.S[ky], Sz = az.S[kz];

@@ -27,6 +27,7 @@ struct SortWorkspace {
     int *keys[2] = {nullptr, nullptr};
     int *vals[2] = {nullptr, nullptr};
     int *hist = nullptr;       // 256 * ntiles
+    int *sums = nullptr;       // scan block sums
     double *scratch = nullptr; // ncols * n doubles (the other particle buffer)
     int *iscratch = nullptr;   // 3 * n ints
     size_t scratch_cols = 0;
@@ -58,27 +59,79 @@ __global__ void k_sort_hist(const int *keys, int n, int shift, int *hist, int nt
         for (int d = lane; d < 256; d += 32) hist[d * ntiles + tile] = h[w][d];
 }
 
-// exclusive scan of m ints in one block of 1024 threads
-__global__ void k_sort_scan(int *a, int m) {
-    __shared__ int part[1024];
-    const int t = threadIdx.x;
-    const int per = (m + 1023) / 1024;
-    const int lo = t * per, hi = min(lo + per, m);
-    int s = 0;
-    for (int i = lo; i < hi; i++) s += a[i];
-    part[t] = s;
-    __syncthreads();
-    for (int off = 1; off < 1024; off <<= 1) {
-        int v = t >= off ? part[t - off] : 0;
-        __syncthreads();
-        part[t] += v;
-        __syncthreads();
+// Exclusive scan of m ints in three launches: per-block sums, a scan of the
+// block sums in one block, then a block-local scan plus the block offset.
+constexpr int kScanBlock = 1024;   // threads per scan block
+constexpr int kScanItems = 4;      // ints per thread
+constexpr int kScanChunk = kScanBlock * kScanItems;
+
+__device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int &total) {
+    const int t = threadIdx.x, lane = t & 31, w = t >> 5;
+    int x = v;
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+        int y = __shfl_up_sync(0xffffffffu, x, o);
+        if (lane >= o) x += y;
     }
-    int run = part[t] - s;
-    for (int i = lo; i < hi; i++) {
-        int v = a[i];
-        a[i] = run;
-        run += v;
+    if (lane == 31) sh[w] = x;
+    __syncthreads();
+    if (w == 0) {
+        int s = lane < (blockDim.x >> 5) ? sh[lane] : 0;
+#pragma unroll
+        for (int o = 1; o < 32; o <<= 1) {
+            int y = __shfl_up_sync(0xffffffffu, s, o);
+            if (lane >= o) s += y;
+        }
+        sh[lane] = s;
+    }
+    __syncthreads();
+    const int before = w > 0 ? sh[w - 1] : 0;
+    total = sh[(blockDim.x >> 5) - 1];
+    __syncthreads();
+    return before + x - v;
+}
+
+__global__ void k_scan_reduce(const int *a, int m, int *sums) {
+    __shared__ int sh[32];
+    const int base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++)
+        if (base + k < m) s += a[base + k];
+    int total;
+    block_exclusive_scan(s, sh, total);
+    if (threadIdx.x == 0) sums[blockIdx.x] = total;
+}
+
+__global__ void k_scan_sums(int *sums, int nb) {
+    __shared__ int sh[32];
+    int run = 0;
+    for (int base = 0; base < nb; base += kScanBlock) {
+        const int i = base + threadIdx.x;
+        const int v = i < nb ? sums[i] : 0;
+        int total;
+        const int ex = block_exclusive_scan(v, sh, total);
+        if (i < nb) sums[i] = run + ex;
+        run += total;
+    }
+}
+
+__global__ void k_scan_apply(int *a, int m, const int *sums) {
+    __shared__ int sh[32];
+    const int base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
+    int v[kScanItems];
+    int s = 0;
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        v[k] = base + k < m ? a[base + k] : 0;
+        s += v[k];
+    }
+    int total;
+    int run = block_exclusive_scan(s, sh, total) + sums[blockIdx.x];
+#pragma unroll
+    for (int k = 0; k < kScanItems; k++) {
+        if (base + k < m) a[base + k] = run;
+        run += v[k];
     }
 }
 
@@ -152,6 +205,8 @@ inline void sort_free(SortWorkspace &w) {
         w.keys[b] = w.vals[b] = nullptr;
     }
     if (w.hist) cudaFree(w.hist);
+    if (w.sums) cudaFree(w.sums);
+    w.sums = nullptr;
     if (w.scratch) cudaFree(w.scratch);
     if (w.iscratch) cudaFree(w.iscratch);
     w.hist = nullptr;
@@ -174,6 +229,7 @@ inline int sort_alloc(SortWorkspace &w, int n, int nelems, int ncols) {
         ok &= cudaMalloc(&w.vals[b], sizeof(int) * n) == cudaSuccess;
     }
     ok &= cudaMalloc(&w.hist, sizeof(int) * 256 * w.ntiles) == cudaSuccess;
+    ok &= cudaMalloc(&w.sums, sizeof(int) * ((256 * w.ntiles + kScanChunk - 1) / kScanChunk + 1)) == cudaSuccess;
     ok &= cudaMalloc(&w.scratch, sizeof(double) * (size_t)ncols * n) == cudaSuccess;
     ok &= cudaMalloc(&w.iscratch, sizeof(int) * 3 * (size_t)n) == cudaSuccess;
     if (!ok) {
@@ -188,22 +244,39 @@ inline int sort_alloc(SortWorkspace &w, int n, int nelems, int ncols) {
 // pblock + k*n; the int block holds mat, elem, orig.
 void relink_particles(DevParticles &p, double *pblock, int *iblock, int **orig);
 
+// Stable LSD radix sort of n keys (0 <= key < 2^bits) carrying their slot index.
+// keys/vals/hist/sums are caller-provided scratch: keys[2], vals[2] of n ints,
+// hist of 256*ntiles ints, sums of ceil(256*ntiles/kScanChunk) ints.  Returns
+// the buffer index (0 or 1) that holds the sorted keys and the permutation.
+inline int radix_sort_keys(const int *elem, int n, int bits, int *keys[2], int *vals[2], int *hist, int *sums,
+                           cudaStream_t s) {
+    const int TB = 256;
+    const int pb = (n + TB - 1) / TB;
+    const int ntiles = (n + kTile - 1) / kTile;
+    k_sort_init<<<pb, TB, 0, s>>>(elem, keys[0], vals[0], n);
+    int cur = 0;
+    const int tb = (ntiles + kSortWarpsPerBlock - 1) / kSortWarpsPerBlock;
+    const int m = 256 * ntiles;
+    const int nb = (m + kScanChunk - 1) / kScanChunk;
+    for (int shift = 0; shift < bits; shift += 8) {
+        k_sort_hist<<<tb, 32 * kSortWarpsPerBlock, 0, s>>>(keys[cur], n, shift, hist, ntiles);
+        k_scan_reduce<<<nb, kScanBlock, 0, s>>>(hist, m, sums);
+        k_scan_sums<<<1, kScanBlock, 0, s>>>(sums, nb);
+        k_scan_apply<<<nb, kScanBlock, 0, s>>>(hist, m, sums);
+        k_sort_scatter<<<tb, 32 * kSortWarpsPerBlock, 0, s>>>(keys[cur], vals[cur], keys[1 - cur], vals[1 - cur], n,
+                                                              shift, hist, ntiles);
+        cur = 1 - cur;
+    }
+    return cur;
+}
+
 inline int sort_particles(SortWorkspace &w, DevParticles &p, double *&pblock, int *&iblock, int *&orig, int ncols,
                           cudaStream_t s) {
     const int n = p.n;
     if (n <= 0) return 0;
     const int TB = 256;
     const int pb = (n + TB - 1) / TB;
-    k_sort_init<<<pb, TB, 0, s>>>(p.elem, w.keys[0], w.vals[0], n);
-    int cur = 0;
-    const int tb = (w.ntiles + kSortWarpsPerBlock - 1) / kSortWarpsPerBlock;
-    for (int shift = 0; shift < w.bits; shift += 8) {
-        k_sort_hist<<<tb, 32 * kSortWarpsPerBlock, 0, s>>>(w.keys[cur], n, shift, w.hist, w.ntiles);
-        k_sort_scan<<<1, 1024, 0, s>>>(w.hist, 256 * w.ntiles);
-        k_sort_scatter<<<tb, 32 * kSortWarpsPerBlock, 0, s>>>(w.keys[cur], w.vals[cur], w.keys[1 - cur],
-                                                              w.vals[1 - cur], n, shift, w.hist, w.ntiles);
-        cur = 1 - cur;
-    }
+    const int cur = radix_sort_keys(p.elem, n, w.bits, w.keys, w.vals, w.hist, w.sums, s);
     const int *perm = w.vals[cur];
     k_gather_cols<<<pb, TB, 0, s>>>(pblock, w.scratch, perm, n, ncols);
     k_gather_ints<<<pb, TB, 0, s>>>(iblock, w.iscratch, perm, n, 3);  // mat, elem, orig
@@ -219,7 +292,7 @@ inline int sort_particles(SortWorkspace &w, DevParticles &p, double *&pblock, in
 }
 
 // kernels one sort_particles call launches
-inline int sort_launches(const SortWorkspace &w) { return 1 + 3 * ((w.bits + 7) / 8) + 2; }
+inline int sort_launches(const SortWorkspace &w) { return 1 + 5 * ((w.bits + 7) / 8) + 2; }
 
 inline int unsort_to_scratch(SortWorkspace &w, const DevParticles &p, const int *orig, const double *pblock, int ncols,
                              cudaStream_t s) {

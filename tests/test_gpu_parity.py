@@ -68,3 +68,21 @@ def test_left_grid_is_reported(gpu_lib):
     with pytest.raises(GpuError, match="LEFT_GRID"):
         r.step(2)
     r.close()
+
+
+@pytest.mark.parametrize("n,nelems", [(1, 1), (1000, 37), (70000, 570000), (300001, 1 << 20)])
+def test_cell_sort_is_a_stable_argsort(n, nelems, gpu_lib):
+    """mpmgpu_sort_by_cell is bit-for-bit numpy's stable argsort."""
+    import ctypes as C
+    torch = pytest.importorskip("torch")
+    rng = np.random.default_rng(n)
+    # many repeated keys, as particles share cells
+    keys = rng.integers(0, nelems, size=n, dtype=np.int32)
+    if n > 10:
+        keys[: n // 3] = keys[n // 3]
+    d_keys = torch.from_numpy(keys).cuda()
+    d_perm = torch.empty(n, dtype=torch.int32, device="cuda")
+    torch.cuda.synchronize()
+    st = gpu_lib.mpmgpu_sort_by_cell(C.c_void_p(d_keys.data_ptr()), n, nelems, C.c_void_p(d_perm.data_ptr()), None)
+    assert st == 0
+    assert np.array_equal(d_perm.cpu().numpy(), np.argsort(keys, kind="stable").astype(np.int32))
