@@ -206,6 +206,26 @@ int mpmgpu_profile(const MpmGpuCtx *ctx, const char **names, double *ms, int32_t
  * cudaMalloc. */
 int mpmgpu_sort_by_cell(const int32_t *d_elem, int32_t n, int32_t nelems, int32_t *d_perm, void *stream);
 
+/* Largest particle count mpmgpu_sort_by_cell_noalloc accepts. */
+#define MPMGPU_NOALLOC_MAX_PARTICLES 131072
+
+/* Allocation-free variant of mpmgpu_sort_by_cell, for callers that cannot
+ * call cudaMalloc: a host integration whose device memory is reserved up front
+ * (for example a serving loop that budgets HBM per run and must not allocate
+ * while runs are in flight), or code where cudaMalloc's implicit device-wide
+ * synchronisation is not acceptable.  It has no counterpart in the reference.
+ * Same arguments and result as mpmgpu_sort_by_cell, for at most
+ * MPMGPU_NOALLOC_MAX_PARTICLES particles; larger n is rejected with
+ * MPMGPU_ERR_INVALID before any device work.  Its scratch is a fixed device
+ * array inside this library (2.25 MiB per GPU, held until the process
+ * exits), so it calls no cudaMalloc, cudaFree or allocating library routine.
+ * The first call on a device looks up that array's device address (once per
+ * device); make that first call before any stream capture.  All calls share
+ * the one array: calls whose work overlaps on a GPU (different streams or
+ * host threads without ordering) race and must be serialised by the caller.
+ * The call synchronizes `stream`. */
+int mpmgpu_sort_by_cell_noalloc(const int32_t *d_elem, int32_t n, int32_t nelems, int32_t *d_perm, void *stream);
+
 /* ---- extensions without a counterpart in the reference ----------------------
  * Host-integration and measurement helpers of this library; a NairnMPM
  * integration does not need them. */

@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <map>
+#include <mutex>
 #include <string>
 #include <vector>
 
@@ -687,6 +688,81 @@ int mpmgpu_sort_by_cell(const int32_t *d_elem, int32_t n, int32_t nelems, int32_
     if (e == cudaSuccess) e = cudaStreamSynchronize(s);
     cudaFree(buf);
     if (e != cudaSuccess) return cuda_fail(c, e, "mpmgpu_sort_by_cell");
+    return MPMGPU_OK;
+}
+
+}  // extern "C"
+
+// ---------------------------------------------------------------------------
+// Allocation-free cell sort.  Its scratch (two key and two value buffers, the
+// per-tile digit histogram and the scan block sums) lives in one file-scope
+// device array sized for MPMGPU_NOALLOC_MAX_PARTICLES particles (2.25 MiB),
+// which every GPU that loads this library holds until the process exits.
+// ---------------------------------------------------------------------------
+namespace {
+constexpr int kNoAllocTiles = (MPMGPU_NOALLOC_MAX_PARTICLES + kTile - 1) / kTile;
+constexpr size_t kNoAllocSums = (256 * (size_t)kNoAllocTiles + kScanChunk - 1) / kScanChunk + 1;
+constexpr size_t kNoAllocInts = 4 * (size_t)MPMGPU_NOALLOC_MAX_PARTICLES + 256 * (size_t)kNoAllocTiles + kNoAllocSums;
+constexpr int kNoAllocMaxDevices = 64;
+}  // namespace
+
+static __device__ __align__(256) int g_noalloc_sort_scratch[kNoAllocInts];
+
+namespace {
+// Device address of g_noalloc_sort_scratch per device ordinal.  In host code
+// the array's name only stands in for the symbol; the address must come from
+// cudaGetSymbolAddress with that device current.
+std::mutex g_noalloc_mutex;
+int *g_noalloc_base[kNoAllocMaxDevices] = {};
+
+int noalloc_scratch(int **base) {
+    int dev = -1;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpmgpu_sort_by_cell_noalloc: cudaGetDevice");
+    if (dev < 0 || dev >= kNoAllocMaxDevices)
+        return set_err(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_sort_by_cell_noalloc: device ordinal out of range");
+    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
+    if (!g_noalloc_base[dev]) {
+        int *p = nullptr;
+        e = cudaGetSymbolAddress((void **)&p, g_noalloc_sort_scratch);
+        if (e != cudaSuccess || !p)
+            return cuda_fail(nullptr, e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                             "mpmgpu_sort_by_cell_noalloc: cudaGetSymbolAddress");
+        g_noalloc_base[dev] = p;
+    }
+    *base = g_noalloc_base[dev];
+    return MPMGPU_OK;
+}
+}  // namespace
+
+extern "C" {
+
+int mpmgpu_sort_by_cell_noalloc(const int32_t *d_elem, int32_t n, int32_t nelems, int32_t *d_perm, void *stream) {
+    if (!d_elem || !d_perm || n <= 0 || nelems <= 0)
+        return set_err(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_sort_by_cell_noalloc: bad argument");
+    if (n > MPMGPU_NOALLOC_MAX_PARTICLES)
+        return set_err(nullptr, MPMGPU_ERR_INVALID,
+                       "mpmgpu_sort_by_cell_noalloc: n = " + std::to_string(n) + " exceeds the maximum of " +
+                           std::to_string(MPMGPU_NOALLOC_MAX_PARTICLES) +
+                           " particles this allocation-free variant supports; use mpmgpu_sort_by_cell");
+    int *base = nullptr;
+    int st = noalloc_scratch(&base);
+    if (st != MPMGPU_OK) return st;
+    cudaStream_t s = (cudaStream_t)stream;
+    int bits = 1;
+    while ((1LL << bits) < (long long)nelems) bits++;
+    const int ntiles = (n + kTile - 1) / kTile;
+    int *keys[2] = {base, base + n}, *vals[2] = {base + 2 * (size_t)n, base + 3 * (size_t)n};
+    int *hist = base + 4 * (size_t)n, *sums = hist + 256 * (size_t)ntiles;
+    // every scratch word the sort reads is written earlier in the same call
+    // (keys/vals by k_sort_init and each scatter, the histogram for all tiles
+    // and digits, the scan sums), so nothing needs clearing between calls
+    const int cur = radix_sort_keys(d_elem, n, bits, keys, vals, hist, sums, s);
+    cudaError_t e = cudaGetLastError();
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(d_perm, vals[cur], sizeof(int) * (size_t)n, cudaMemcpyDeviceToDevice, s);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(s);
+    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpmgpu_sort_by_cell_noalloc");
     return MPMGPU_OK;
 }
 

@@ -59,6 +59,8 @@ def lib():
     L.mpmgpu_host_register.restype = C.c_int
     L.mpmgpu_sort_by_cell.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
     L.mpmgpu_sort_by_cell.restype = C.c_int
+    L.mpmgpu_sort_by_cell_noalloc.argtypes = [C.c_void_p, C.c_int32, C.c_int32, C.c_void_p, C.c_void_p]
+    L.mpmgpu_sort_by_cell_noalloc.restype = C.c_int
     L.mpmgpu_host_unregister.argtypes = [C.c_void_p]
     L.mpmgpu_host_unregister.restype = C.c_int
     for f in ("mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact", "mpmgpu_set_velocity_bcs",
