@@ -51,6 +51,7 @@ struct DevNodes {
     double *cx, *cy, *cz;      // copy of extrapolated momentum (vk[pkCopy])
     double *vx, *vy, *vz;      // velocity p/m
     double *ux, *uy, *uz;      // second (update-strains-last) momentum extrapolation
+    double *ax, *ay, *az;      // acceleration f/m after the momentum update
     unsigned char *active;     // numberPoints > 0
 };
 
@@ -94,30 +95,33 @@ __device__ __forceinline__ void xi_position(const DevGrid &g, int e, double x, d
 }
 
 // ---------------------------------------------------------------------------
-// uGIMP, evaluated per axis.  Candidate k = 0..3 sits at natural coordinate
-// 2k-3 (i.e. -3,-1,1,3) and at node offset k-1 from the element's first node.
-// FourNodeIsoparam::GimpShapeFunction (FourNodeIsoparam.cpp:431-519) and
-// EightNodeIsoparamBrick::GimpShapeFunction (EightNodeIsoparamBrick.cpp:289-403)
-// compute the same 1D factors inline; the products below keep their order.
+// uGIMP factors.  FourNodeIsoparam::GimpShapeFunction (FourNodeIsoparam.cpp:431-519)
+// and EightNodeIsoparamBrick::GimpShapeFunction (EightNodeIsoparamBrick.cpp:289-403)
+// evaluate, for each candidate node at natural coordinate 2k-3 (k = 0..3, node
+// offset k-1 from the element's first node), a 1D factor per axis and take
+// their product.  The window below computes the same 1D factors.
 // ---------------------------------------------------------------------------
-struct Axis {
-    double S[4];
-    double dS[4];   // sign * dS
-    unsigned act;   // bit k set when candidate k is inside the support
+// Window form of the same factors.  For lp <= 1 the support of a particle
+// spans three candidates per axis: k = s..s+2 with s = 1 exactly when the
+// candidate at +3 passes the reference's test |xi-3| < 2+lp (then the one at -3
+// cannot), else s = 0 (the -3 candidate may still be outside the support and
+// gets a zero factor).  All lanes of a warp then run the same 27 (3D) or 9
+// (2D) node bodies.  dS already carries the sign and the 2/dx scale.
+struct Win {
+    double S[3], dS[3];
+    int s;
 };
 
-// inv_size is 1/(4*lp) of this axis (3D z uses lp.y, as the reference does)
 template <bool kThreeD, bool kGrad>
-__device__ __forceinline__ void gimp_axis(double xi, double lp, double inv_size, Axis &a) {
+__device__ __forceinline__ void gimp_window(double xi, double lp, double inv_size, double idx, Win &w) {
     const double q1 = 2. - lp, q2 = 2. + lp;
-    a.act = 0u;
+    w.s = fabs(xi - 3.) < q2 ? 1 : 0;
 #pragma unroll
-    for (int k = 0; k < 4; k++) {
-        const double gk = (double)(2 * k - 3);
+    for (int j = 0; j < 3; j++) {
+        const double gk = (double)(2 * (w.s + j) - 3);
         const double xp = fabs(xi - gk);
         double S = 0., dS = 0.;
         if (xp < q2) {
-            a.act |= 1u << k;
             double arg = 0.;
             if (xp < lp) {
                 S = ((4. - lp) * lp - xp * xp) * inv_size;
@@ -128,46 +132,16 @@ __device__ __forceinline__ void gimp_axis(double xi, double lp, double inv_size,
                 S = 2. * lp * arg * arg;
             }
             if (kGrad) {
-                const double sgn = xi > gk ? 1. : -1.;
                 double d;
                 if (xp < lp) d = kThreeD ? -xp / (2. * lp) : -xp * inv_size * 2.0;
                 else if (xp <= q1) d = -0.5;
                 else d = -arg;
-                dS = sgn * d;
+                dS = (xi > gk ? d : -d) * idx;
             }
         }
-        a.S[k] = S;
-        a.dS[k] = dS;
+        w.S[j] = S;
+        w.dS[j] = dS;
     }
-}
-
-// candidate order of the reference tables, packed (k_x | k_y<<2 | k_z<<4):
-// FourNodeIsoparam.cpp:27-30 (gxii, geti) and EightNodeIsoparamBrick.cpp
-// (x3off, y3off, z3off) with k = offset + 1.  Written as constexpr functions so
-// that, with the candidate loops fully unrolled, every index is a constant and
-// the per-axis factors stay in registers.
-__host__ __device__ constexpr unsigned cand2d(int c) {
-    return
-            c == 0 ? 0x05u : c == 1 ? 0x06u : c == 2 ? 0x0Au : c == 3 ? 0x09u : c == 4 ? 0x00u :
-            c == 5 ? 0x01u : c == 6 ? 0x02u : c == 7 ? 0x03u : c == 8 ? 0x07u : c == 9 ? 0x0Bu :
-            c == 10 ? 0x0Fu : c == 11 ? 0x0Eu : c == 12 ? 0x0Du : c == 13 ? 0x0Cu : c == 14 ? 0x08u :
-            c == 15 ? 0x04u : 0u;
-}
-__host__ __device__ constexpr unsigned cand3d(int c) {
-    return
-            c == 0 ? 0x15u : c == 1 ? 0x16u : c == 2 ? 0x1Au : c == 3 ? 0x19u : c == 4 ? 0x25u :
-            c == 5 ? 0x26u : c == 6 ? 0x2Au : c == 7 ? 0x29u : c == 8 ? 0x10u : c == 9 ? 0x11u :
-            c == 10 ? 0x12u : c == 11 ? 0x13u : c == 12 ? 0x17u : c == 13 ? 0x1Bu : c == 14 ? 0x1Fu :
-            c == 15 ? 0x1Eu : c == 16 ? 0x1Du : c == 17 ? 0x1Cu : c == 18 ? 0x18u : c == 19 ? 0x14u :
-            c == 20 ? 0x20u : c == 21 ? 0x21u : c == 22 ? 0x22u : c == 23 ? 0x23u : c == 24 ? 0x27u :
-            c == 25 ? 0x2Bu : c == 26 ? 0x2Fu : c == 27 ? 0x2Eu : c == 28 ? 0x2Du : c == 29 ? 0x2Cu :
-            c == 30 ? 0x28u : c == 31 ? 0x24u : c == 32 ? 0x05u : c == 33 ? 0x06u : c == 34 ? 0x0Au :
-            c == 35 ? 0x09u : c == 36 ? 0x00u : c == 37 ? 0x01u : c == 38 ? 0x02u : c == 39 ? 0x03u :
-            c == 40 ? 0x07u : c == 41 ? 0x0Bu : c == 42 ? 0x0Fu : c == 43 ? 0x0Eu : c == 44 ? 0x0Du :
-            c == 45 ? 0x0Cu : c == 46 ? 0x08u : c == 47 ? 0x04u : c == 48 ? 0x35u : c == 49 ? 0x36u :
-            c == 50 ? 0x3Au : c == 51 ? 0x39u : c == 52 ? 0x30u : c == 53 ? 0x31u : c == 54 ? 0x32u :
-            c == 55 ? 0x33u : c == 56 ? 0x37u : c == 57 ? 0x3Bu : c == 58 ? 0x3Fu : c == 59 ? 0x3Eu :
-            c == 60 ? 0x3Du : c == 61 ? 0x3Cu : c == 62 ? 0x38u : c == 63 ? 0x34u : 0u;
 }
 
 // ---------------------------------------------------------------------------

@@ -261,9 +261,9 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     coords.insert(coords.end(), grid->xnodes, grid->xnodes + g.nx + 1);
     coords.insert(coords.end(), grid->ynodes, grid->ynodes + g.ny + 1);
     if (g.dim == 3) coords.insert(coords.end(), grid->znodes, grid->znodes + g.nz + 1);
-    // node columns: mass, p(3), f(3), u(3) are cleared each step; c(3), v(3) are not
+    // node columns: mass, p(3), f(3), u(3) are cleared each step; c(3), v(3), a(3) are not
     const size_t NN = (size_t)g.nnodes;
-    const int ncleared = 10, nkept = 6;
+    const int ncleared = 10, nkept = 9;
     if ((e = cudaMalloc(&c->grid_coords, ncoord * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&c->nblock, NN * (ncleared + nkept) * sizeof(double) + NN)) != cudaSuccess ||
         (e = cudaMalloc(&c->bc_group, NN * sizeof(int))) != cudaSuccess ||
@@ -294,7 +294,10 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     nd.vx = b + 13 * NN;
     nd.vy = b + 14 * NN;
     nd.vz = b + 15 * NN;
-    nd.active = (unsigned char *)(b + 16 * NN);
+    nd.ax = b + 16 * NN;
+    nd.ay = b + 17 * NN;
+    nd.az = b + 18 * NN;
+    nd.active = (unsigned char *)(b + 19 * NN);
     c->nblock_zero_bytes = NN * ncleared * sizeof(double);
     cudaMemset(c->nblock, 0, NN * (ncleared + nkept) * sizeof(double) + NN);
     cudaMemset(c->bc_group, 0xFF, NN * sizeof(int));

@@ -67,41 +67,49 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi
         }
         return;
     }
-    // uGIMP
-    Axis ax, ay, az;
-    gimp_axis<DIM == 3, GRAD>(xi, lpx, 1. / (4. * lpx), ax);
-    gimp_axis<DIM == 3, GRAD>(eta, lpy, 1. / (4. * lpy), ay);
-    const double idx = GRAD ? 2.0 / DX : 0., idy = GRAD ? 2.0 / DY : 0.;
+    // uGIMP over the particle's window (see gimp_window); f is called for
+    // every window node, with N == 0 marking a node outside the support.
+    Win wx, wy;
+    gimp_window<DIM == 3, GRAD>(xi, lpx, 1. / (4. * lpx), GRAD ? 2.0 / DX : 0., wx);
+    gimp_window<DIM == 3, GRAD>(eta, lpy, 1. / (4. * lpy), GRAD ? 2.0 / DY : 0., wy);
+    const int base = n0 + (wx.s - 1) + (wy.s - 1) * g.yplane;
     if (DIM == 2) {
 #pragma unroll
-        for (int c = 0; c < 16; c++) {
-            const unsigned code = cand2d(c);
-            const int kx = code & 3, ky = (code >> 2) & 3;
-            if (!((ax.act >> kx) & (ay.act >> ky) & 1u)) continue;
-            const double Sx = ax.S[kx], Sy = ay.S[ky];
-            double dx = 0., dy = 0.;
-            if (GRAD) {
-                dx = ax.dS[kx] * Sy * idx;
-                dy = Sx * ay.dS[ky] * idy;
+        for (int jy = 0; jy < 3; jy++) {
+#pragma unroll
+            for (int jx = 0; jx < 3; jx++) {
+                const double Sx = wx.S[jx], Sy = wy.S[jy];
+                double dx = 0., dy = 0.;
+                if (GRAD) {
+                    dx = wx.dS[jx] * Sy;
+                    dy = Sx * wy.dS[jy];
+                }
+                f(base + jx + jy * g.yplane, Sx * Sy, dx, dy, 0.);
             }
-            f(n0 + (kx - 1) + (ky - 1) * g.yplane, Sx * Sy, dx, dy, 0.);
         }
     } else {
-        gimp_axis<true, GRAD>(zeta, lpz, 1. / (4. * lpy), az);
-        const double idz = GRAD ? 2.0 / DZ : 0.;
+        Win wz;
+        gimp_window<true, GRAD>(zeta, lpz, 1. / (4. * lpy), GRAD ? 2.0 / DZ : 0., wz);
+        const int base3 = base + (wz.s - 1) * g.zplane;
 #pragma unroll
-        for (int c = 0; c < 64; c++) {
-            const unsigned code = cand3d(c);
-            const int kx = code & 3, ky = (code >> 2) & 3, kz = (code >> 4) & 3;
-            if (!((ax.act >> kx) & (ay.act >> ky) & (az.act >> kz) & 1u)) continue;
-            const double Sx = ax.S[kx], Sy = ay.S[ky], Sz = az.S[kz];
-            double dx = 0., dy = 0., dz = 0.;
-            if (GRAD) {
-                dx = ax.dS[kx] * Sy * Sz * idx;
-                dy = Sx * ay.dS[ky] * Sz * idy;
-                dz = Sx * Sy * az.dS[kz] * idz;
+        for (int jz = 0; jz < 3; jz++) {
+#pragma unroll
+            for (int jy = 0; jy < 3; jy++) {
+                const double Syz = wy.S[jy] * wz.S[jz];
+                const double dySz = GRAD ? wy.dS[jy] * wz.S[jz] : 0.;
+                const double SydZ = GRAD ? wy.S[jy] * wz.dS[jz] : 0.;
+#pragma unroll
+                for (int jx = 0; jx < 3; jx++) {
+                    const double Sx = wx.S[jx];
+                    double dx = 0., dy = 0., dz = 0.;
+                    if (GRAD) {
+                        dx = wx.dS[jx] * Syz;
+                        dy = Sx * dySz;
+                        dz = Sx * SydZ;
+                    }
+                    f(base3 + jx + jy * g.yplane + jz * g.zplane, Sx * Syz, dx, dy, dz);
+                }
             }
-            f(n0 + (kx - 1) + (ky - 1) * g.yplane + (kz - 1) * g.zplane, Sx * Sy * Sz, dx, dy, dz);
         }
     }
 }
@@ -128,6 +136,7 @@ __global__ void __launch_bounds__(256) k_p2g(DevGrid g, DevParticles p, DevNodes
     const double vx = p.vx[i], vy = p.vy[i], vz = DIM == 3 ? p.vz[i] : 0.;
     for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1.,
                                      [&](int n, double N, double, double, double) {
+                                         if (N == 0.) return;
                                          const double fnmp = N * mp;
                                          atomicAdd(&nd.mass[n], fnmp);
                                          atomicAdd(&nd.px[n], vx * fnmp);
@@ -157,7 +166,8 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, const DevPar
     double d[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};
     for_each_node<DIM, SHAPE, true>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
                                     DIM == 3 ? p.lpz[i] : 1.,
-                                    [&](int n, double, double dx, double dy, double dz) {
+                                    [&](int n, double N, double dx, double dy, double dz) {
+                                        if (N == 0.) return;
                                         const double vx = nd.vx[n], vy = nd.vy[n];
                                         d[0] += vx * dx;
                                         d[1] += vx * dy;
@@ -189,19 +199,22 @@ __global__ void __launch_bounds__(256) k_strain_forces(DevGrid g, DevParticles p
         velocity_gradient<DIM, SHAPE>(g, p, nd, i, st, du);
         constitutive<DIM>(mats, p, i, du);
     }
+    // -mp * (sigma - P I): the internal force of GetFintPlusFext, scaled once
     const double mp = p.mass[i], P = p.pressure[i];
-    const double sxx = p.sxx[i] - P, syy = p.syy[i] - P, sxy = p.sxy[i];
-    const double szz = DIM == 3 ? p.szz[i] - P : 0., sxz = DIM == 3 ? p.sxz[i] : 0., syz = DIM == 3 ? p.syz[i] : 0.;
+    const double sxx = -mp * (p.sxx[i] - P), syy = -mp * (p.syy[i] - P), sxy = -mp * p.sxy[i];
+    const double szz = DIM == 3 ? -mp * (p.szz[i] - P) : 0., sxz = DIM == 3 ? -mp * p.sxz[i] : 0.,
+                 syz = DIM == 3 ? -mp * p.syz[i] : 0.;
     for_each_node<DIM, SHAPE, true>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
                                     DIM == 3 ? p.lpz[i] : 1.,
-                                    [&](int n, double, double dx, double dy, double dz) {
+                                    [&](int n, double N, double dx, double dy, double dz) {
+                                        if (N == 0.) return;
                                         if (DIM == 2) {
-                                            atomicAdd(&nd.fx[n], -mp * (sxx * dx + sxy * dy));
-                                            atomicAdd(&nd.fy[n], -mp * (sxy * dx + syy * dy));
+                                            atomicAdd(&nd.fx[n], sxx * dx + sxy * dy);
+                                            atomicAdd(&nd.fy[n], sxy * dx + syy * dy);
                                         } else {
-                                            atomicAdd(&nd.fx[n], -mp * (sxx * dx + sxy * dy + sxz * dz));
-                                            atomicAdd(&nd.fy[n], -mp * (sxy * dx + syy * dy + syz * dz));
-                                            atomicAdd(&nd.fz[n], -mp * (sxz * dx + syz * dy + szz * dz));
+                                            atomicAdd(&nd.fx[n], sxx * dx + sxy * dy + sxz * dz);
+                                            atomicAdd(&nd.fy[n], sxy * dx + syy * dy + syz * dz);
+                                            atomicAdd(&nd.fz[n], sxz * dx + syz * dy + szz * dz);
                                         }
                                     });
 }
@@ -278,13 +291,13 @@ __global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes
     const double xi = p.xi[i], eta = p.eta[i], zeta = DIM == 3 ? p.zeta[i] : 0.;
     const double lx = p.lpx[i], ly = p.lpy[i], lz = DIM == 3 ? p.lpz[i] : 1.;
     for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, double N, double, double, double) {
+        if (N == 0.) return;
         Sv[0] += nd.vx[n] * N;
         Sv[1] += nd.vy[n] * N;
         if (DIM == 3) Sv[2] += nd.vz[n] * N;
-        const double mnode = N / nd.mass[n];
-        Sa[0] += nd.fx[n] * mnode;
-        Sa[1] += nd.fy[n] * mnode;
-        if (DIM == 3) Sa[2] += nd.fz[n] * mnode;
+        Sa[0] += nd.ax[n] * N;   // f/m of the node (the reference forms f*(N/m))
+        Sa[1] += nd.ay[n] * N;
+        if (DIM == 3) Sa[2] += nd.az[n] * N;
     });
     double v[3] = {p.vx[i], p.vy[i], DIM == 3 ? p.vz[i] : 0.};
     double xp[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
@@ -306,6 +319,7 @@ __global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes
     if (USL) {
         const double mp = p.mass[i];
         for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, double N, double, double, double) {
+            if (N == 0.) return;
             const double fnmp = N * mp;
             atomicAdd(&nd.ux[n], v[0] * fnmp);
             atomicAdd(&nd.uy[n], v[1] * fnmp);
@@ -439,6 +453,11 @@ __global__ void k_node_update(DevNodes nd, int nnodes, DevBCs b, const int *bc_g
         nd.fz[n] = f[2];
     }
     node_velocity(nd, n, m, p);
+    // acceleration for the particle update (every active node has mass > 0)
+    const double r = 1. / m;
+    nd.ax[n] = f[0] * r;
+    nd.ay[n] = f[1] * r;
+    if (DIM == 3) nd.az[n] = f[2] * r;
 }
 
 // UpdateStrainsLastContactTask: p = second extrapolation, UPDATE_STRAINS_LAST_CALL
