@@ -53,6 +53,11 @@ struct DevNodes {
     double *ux, *uy, *uz;      // second (update-strains-last) momentum extrapolation
     double *ax, *ay, *az;      // acceleration f/m after the momentum update
     unsigned char *active;     // numberPoints > 0
+    // mixed-precision transfer mode only
+    float *vhx, *vhy, *vhz;    // velocity split v = hi + lo in FP32 pairs
+    float *vlx, *vly, *vlz;
+    float *gx, *gy, *gz;       // FP32 force accumulators
+    float *bx, *by, *bz;       // FP32 acceleration for the particle update
 };
 
 // Velocity conditions grouped by node, list order kept inside a node.
@@ -107,34 +112,36 @@ __device__ __forceinline__ void xi_position(const DevGrid &g, int e, double x, d
 // cannot), else s = 0 (the -3 candidate may still be outside the support and
 // gets a zero factor).  All lanes of a warp then run the same 27 (3D) or 9
 // (2D) node bodies.  dS already carries the sign and the 2/dx scale.
+template <typename T>
 struct Win {
-    double S[3], dS[3];
+    T S[3], dS[3];
     int s;
 };
 
-template <bool kThreeD, bool kGrad>
-__device__ __forceinline__ void gimp_window(double xi, double lp, double inv_size, double idx, Win &w) {
-    const double q1 = 2. - lp, q2 = 2. + lp;
-    w.s = fabs(xi - 3.) < q2 ? 1 : 0;
+// T = double in the FP64 path, float in the mixed-precision transfer mode
+template <typename T, bool kThreeD, bool kGrad>
+__device__ __forceinline__ void gimp_window(T xi, T lp, T inv_size, T idx, Win<T> &w) {
+    const T q1 = T(2) - lp, q2 = T(2) + lp;
+    w.s = fabs(xi - T(3)) < q2 ? 1 : 0;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-        const double gk = (double)(2 * (w.s + j) - 3);
-        const double xp = fabs(xi - gk);
-        double S = 0., dS = 0.;
+        const T gk = (T)(2 * (w.s + j) - 3);
+        const T xp = fabs(xi - gk);
+        T S = T(0), dS = T(0);
         if (xp < q2) {
-            double arg = 0.;
+            T arg = T(0);
             if (xp < lp) {
-                S = ((4. - lp) * lp - xp * xp) * inv_size;
+                S = ((T(4) - lp) * lp - xp * xp) * inv_size;
             } else if (xp <= q1) {
-                S = kThreeD ? 0.5 * (2. - xp) : (2. - xp) / 2.;
+                S = kThreeD ? T(0.5) * (T(2) - xp) : (T(2) - xp) / T(2);
             } else {
                 arg = (q2 - xp) * inv_size;
-                S = 2. * lp * arg * arg;
+                S = T(2) * lp * arg * arg;
             }
             if (kGrad) {
-                double d;
-                if (xp < lp) d = kThreeD ? -xp / (2. * lp) : -xp * inv_size * 2.0;
-                else if (xp <= q1) d = -0.5;
+                T d;
+                if (xp < lp) d = kThreeD ? -xp / (T(2) * lp) : -xp * inv_size * T(2);
+                else if (xp <= q1) d = T(-0.5);
                 else d = -arg;
                 dS = (xi > gk ? d : -d) * idx;
             }
@@ -142,6 +149,12 @@ __device__ __forceinline__ void gimp_window(double xi, double lp, double inv_siz
         w.S[j] = S;
         w.dS[j] = dS;
     }
+}
+
+// FP64 value as an FP32 pair hi + lo (hi = nearest float, lo = nearest float of the rest)
+__device__ __forceinline__ void split2(double v, float &hi, float &lo) {
+    hi = __double2float_rn(v);
+    lo = __double2float_rn(v - (double)hi);
 }
 
 // ---------------------------------------------------------------------------

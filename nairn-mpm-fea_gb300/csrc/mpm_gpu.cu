@@ -59,6 +59,8 @@ struct MpmGpuCtx {
     int *iblock = nullptr;               // mat, elem, original index
     int *orig = nullptr;                 // original (host) index of each slot
     double *nblock = nullptr;            // node double columns
+    float *fblock = nullptr;             // node float columns (mixed mode)
+    size_t fblock_zero_bytes = 0;
     size_t nblock_zero_bytes = 0;        // bytes cleared at each step start
     unsigned char *active = nullptr;
     unsigned *err = nullptr;
@@ -221,8 +223,8 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
     if (opts->method != MPMGPU_USF && opts->method != MPMGPU_USAVG && opts->method != MPMGPU_USL)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
-    if (opts->precision != MPMGPU_PREC_FP64)
-        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "only the FP64 transfer mode is built in this library");
+    if (opts->precision != MPMGPU_PREC_FP64 && opts->precision != MPMGPU_PREC_MIXED)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "precision must be MPMGPU_PREC_FP64 or MPMGPU_PREC_MIXED");
     if (opts->nfields > 1)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "multimaterial contact is not implemented on the device");
     if (!(opts->timestep > 0.)) return set_err(nullptr, MPMGPU_ERR_INVALID, "timestep must be > 0");
@@ -264,8 +266,12 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     // node columns: mass, p(3), f(3), u(3) are cleared each step; c(3), v(3), a(3) are not
     const size_t NN = (size_t)g.nnodes;
     const int ncleared = 10, nkept = 9;
+    // FP32 columns of the mixed mode: force accumulators (cleared), velocity
+    // hi/lo pairs and acceleration
+    const int fcleared = 3, fkept = 9;
     if ((e = cudaMalloc(&c->grid_coords, ncoord * sizeof(double))) != cudaSuccess ||
         (e = cudaMalloc(&c->nblock, NN * (ncleared + nkept) * sizeof(double) + NN)) != cudaSuccess ||
+        (e = cudaMalloc(&c->fblock, NN * (fcleared + fkept) * sizeof(float))) != cudaSuccess ||
         (e = cudaMalloc(&c->bc_group, NN * sizeof(int))) != cudaSuccess ||
         (e = cudaMalloc(&c->err, sizeof(unsigned))) != cudaSuccess) {
         std::string m = std::string("device allocation: ") + cudaGetErrorString(e);
@@ -300,6 +306,21 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     nd.active = (unsigned char *)(b + 19 * NN);
     c->nblock_zero_bytes = NN * ncleared * sizeof(double);
     cudaMemset(c->nblock, 0, NN * (ncleared + nkept) * sizeof(double) + NN);
+    float *fb = c->fblock;
+    nd.gx = fb;
+    nd.gy = fb + NN;
+    nd.gz = fb + 2 * NN;
+    nd.vhx = fb + 3 * NN;
+    nd.vhy = fb + 4 * NN;
+    nd.vhz = fb + 5 * NN;
+    nd.vlx = fb + 6 * NN;
+    nd.vly = fb + 7 * NN;
+    nd.vlz = fb + 8 * NN;
+    nd.bx = fb + 9 * NN;
+    nd.by = fb + 10 * NN;
+    nd.bz = fb + 11 * NN;
+    c->fblock_zero_bytes = NN * fcleared * sizeof(float);
+    cudaMemset(c->fblock, 0, NN * (fcleared + fkept) * sizeof(float));
     cudaMemset(c->bc_group, 0xFF, NN * sizeof(int));
     cudaMemset(c->err, 0, sizeof(unsigned));
     const char *names[] = {"p2g", "node_post", "strain_forces", "node_update", "g2p", "node_usl", "strain_last",
@@ -460,7 +481,7 @@ inline cudaEvent_t &event_at(MpmGpuCtx *c, int slot, int k, bool begin) {
     return c->ev[((size_t)slot * kFamilies + k) * 2 + (begin ? 0 : 1)];
 }
 
-template <int DIM, int SHAPE>
+template <int DIM, int SHAPE, bool MIX>
 void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     const int n = c->p.n, NN = c->g.nnodes;
     const int TB = 256;
@@ -476,47 +497,54 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     };
     cudaMemsetAsync(c->nblock, 0, c->nblock_zero_bytes, s);
     cudaMemsetAsync(c->nd.active, 0, (size_t)NN, s);
+    if (MIX) cudaMemsetAsync(c->fblock, 0, c->fblock_zero_bytes, s);
     mark(0, true);
-    k_p2g<DIM, SHAPE><<<pb, TB, 0, s>>>(c->g, c->p, c->nd);
+    k_p2g<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd);
     mark(0, false);
     mark(1, true);
-    k_node_post<DIM><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL, t, dt);
+    k_node_post<DIM, MIX><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL, t, dt);
     mark(1, false);
     mark(2, true);
     if (method == MPMGPU_USL)
-        k_strain_forces<DIM, SHAPE, false><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stFirst);
+        k_strain_forces<DIM, SHAPE, false, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stFirst);
     else
-        k_strain_forces<DIM, SHAPE, true><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stFirst);
+        k_strain_forces<DIM, SHAPE, true, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stFirst);
     mark(2, false);
     mark(3, true);
-    k_node_update<DIM><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, t, dt);
+    k_node_update<DIM, MIX><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, t, dt);
     mark(3, false);
     mark(4, true);
     if (method == MPMGPU_USF) {
-        k_g2p<DIM, SHAPE, false><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, dt, c->err);
+        k_g2p<DIM, SHAPE, false, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, dt, c->err);
         mark(4, false);
         return;
     }
-    k_g2p<DIM, SHAPE, true><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, dt, c->err);
+    k_g2p<DIM, SHAPE, true, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, dt, c->err);
     mark(4, false);
     mark(5, true);
-    k_node_usl<DIM><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, t, dt);
+    k_node_usl<DIM, MIX><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, t, dt);
     mark(5, false);
     mark(6, true);
-    k_strain_last<DIM, SHAPE><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stLast, c->err);
+    k_strain_last<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stLast, c->err);
     mark(6, false);
 }
 
-void enqueue(MpmGpuCtx *c, double t, int slot) {
+template <bool MIX>
+void enqueue_prec(MpmGpuCtx *c, double t, int slot) {
     const bool d3 = c->dim == 3;
     const bool lin = c->opts.shape == MPMGPU_SHAPE_LINEAR;
     if (d3) {
-        if (lin) enqueue_step<3, SHAPE_LINEAR>(c, t, slot);
-        else enqueue_step<3, SHAPE_UGIMP>(c, t, slot);
+        if (lin) enqueue_step<3, SHAPE_LINEAR, MIX>(c, t, slot);
+        else enqueue_step<3, SHAPE_UGIMP, MIX>(c, t, slot);
     } else {
-        if (lin) enqueue_step<2, SHAPE_LINEAR>(c, t, slot);
-        else enqueue_step<2, SHAPE_UGIMP>(c, t, slot);
+        if (lin) enqueue_step<2, SHAPE_LINEAR, MIX>(c, t, slot);
+        else enqueue_step<2, SHAPE_UGIMP, MIX>(c, t, slot);
     }
+}
+
+void enqueue(MpmGpuCtx *c, double t, int slot) {
+    if (c->opts.precision == MPMGPU_PREC_MIXED) enqueue_prec<true>(c, t, slot);
+    else enqueue_prec<false>(c, t, slot);
 }
 
 int ensure_events(MpmGpuCtx *c, int nsteps) {
@@ -639,6 +667,7 @@ void mpmgpu_destroy(MpmGpuCtx *c) {
     if (c->mats) cudaFree(c->mats);
     if (c->grid_coords) cudaFree(c->grid_coords);
     if (c->nblock) cudaFree(c->nblock);
+    if (c->fblock) cudaFree(c->fblock);
     if (c->bc_group) cudaFree(c->bc_group);
     if (c->bc_block) cudaFree(c->bc_block);
     if (c->err) cudaFree(c->err);

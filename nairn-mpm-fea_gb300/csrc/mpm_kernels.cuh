@@ -19,89 +19,93 @@ namespace nmg {
 
 enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1 };
 
-// Visit the nodes of one particle in the reference's order, calling
-// f(node0based, N, dNdx, dNdy, dNdz).  ElementBase::GetShapeFunctions /
-// GetShapeGradients (NairnMPM/src/Elements/MoreMPMElementBase.cpp:120-284).
-template <int DIM, int SHAPE, bool GRAD, class F>
-__device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi, double eta, double zeta,
-                                              double lpx, double lpy, double lpz, F &&f) {
+// Visit the nodes of one particle, calling f(node0based, N, dNdx, dNdy, dNdz).
+// ElementBase::GetShapeFunctions / GetShapeGradients
+// (NairnMPM/src/Elements/MoreMPMElementBase.cpp:120-284).  T is the arithmetic
+// of the weights: double in the FP64 path, float in the mixed-precision mode
+// (natural coordinates are formed in FP64 and rounded once).
+template <int DIM, int SHAPE, bool GRAD, typename T, class F>
+__device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi_d, double eta_d, double zeta_d,
+                                              double lpx_d, double lpy_d, double lpz_d, F &&f) {
     int col, row, zr;
     elem_coords(g, e, col, row, zr);
     const int n0 = zr * g.zplane + row * g.yplane + col;  // 0-based first node
-    const double DX = g.xn[col + 1] - g.xn[col];
-    const double DY = g.yn[row + 1] - g.yn[row];
-    const double DZ = DIM == 3 ? g.zn[zr + 1] - g.zn[zr] : 1.;
+    const T DX = (T)(g.xn[col + 1] - g.xn[col]);
+    const T DY = (T)(g.yn[row + 1] - g.yn[row]);
+    const T DZ = DIM == 3 ? (T)(g.zn[zr + 1] - g.zn[zr]) : T(1);
+    const T xi = (T)xi_d, eta = (T)eta_d, zeta = (T)zeta_d;
     if (SHAPE == SHAPE_LINEAR) {
         if (DIM == 2) {
             // FourNodeIsoparam::ShapeFunction (6-argument form), FourNodeIsoparam.cpp:189-212
             const int off[4] = {0, 1, 1 + g.yplane, g.yplane};
-            const double xs[4] = {-1., 1., 1., -1.}, es[4] = {-1., -1., 1., 1.};
+            const T xs[4] = {-1, 1, 1, -1}, es[4] = {-1, -1, 1, 1};
 #pragma unroll
             for (int i = 0; i < 4; i++) {
-                const double t1 = 1. + xs[i] * xi, t2 = 1. + es[i] * eta;
-                double dx = 0., dy = 0.;
+                const T t1 = T(1) + xs[i] * xi, t2 = T(1) + es[i] * eta;
+                T dx = 0, dy = 0;
                 if (GRAD) {
-                    dx = 0.5 * xs[i] * t2 / DX;
-                    dy = 0.5 * es[i] * t1 / DY;
+                    dx = T(0.5) * xs[i] * t2 / DX;
+                    dy = T(0.5) * es[i] * t1 / DY;
                 }
-                f(n0 + off[i], 0.25 * t1 * t2, dx, dy, 0.);
+                f(n0 + off[i], T(0.25) * t1 * t2, dx, dy, T(0));
             }
         } else {
             // EightNodeIsoparamBrick::ShapeFunction (6-argument form), EightNodeIsoparamBrick.cpp:90-104
-            const double xs[8] = {-1., 1., 1., -1., -1., 1., 1., -1.};
-            const double es[8] = {-1., -1., 1., 1., -1., -1., 1., 1.};
-            const double zs[8] = {-1., -1., -1., -1., 1., 1., 1., 1.};
+            const T xs[8] = {-1, 1, 1, -1, -1, 1, 1, -1};
+            const T es[8] = {-1, -1, 1, 1, -1, -1, 1, 1};
+            const T zs[8] = {-1, -1, -1, -1, 1, 1, 1, 1};
 #pragma unroll
             for (int i = 0; i < 8; i++) {
                 const int off = (i == 1 || i == 5 ? 1 : 0) + (i == 2 || i == 6 ? 1 + g.yplane : 0) +
                                 (i == 3 || i == 7 ? g.yplane : 0) + (i >= 4 ? g.zplane : 0);
-                const double t1 = 1. + xs[i] * xi, t2 = 1. + es[i] * eta, t3 = 1. + zs[i] * zeta;
-                double dx = 0., dy = 0., dz = 0.;
+                const T t1 = T(1) + xs[i] * xi, t2 = T(1) + es[i] * eta, t3 = T(1) + zs[i] * zeta;
+                T dx = 0, dy = 0, dz = 0;
                 if (GRAD) {
-                    dx = 0.25 * xs[i] * t2 * t3 / DX;
-                    dy = 0.25 * es[i] * t1 * t3 / DY;
-                    dz = 0.25 * zs[i] * t1 * t2 / DZ;
+                    dx = T(0.25) * xs[i] * t2 * t3 / DX;
+                    dy = T(0.25) * es[i] * t1 * t3 / DY;
+                    dz = T(0.25) * zs[i] * t1 * t2 / DZ;
                 }
-                f(n0 + off, 0.125 * t1 * t2 * t3, dx, dy, dz);
+                f(n0 + off, T(0.125) * t1 * t2 * t3, dx, dy, dz);
             }
         }
         return;
     }
     // uGIMP over the particle's window (see gimp_window); f is called for
     // every window node, with N == 0 marking a node outside the support.
-    Win wx, wy;
-    gimp_window<DIM == 3, GRAD>(xi, lpx, 1. / (4. * lpx), GRAD ? 2.0 / DX : 0., wx);
-    gimp_window<DIM == 3, GRAD>(eta, lpy, 1. / (4. * lpy), GRAD ? 2.0 / DY : 0., wy);
+    const T lpx = (T)lpx_d, lpy = (T)lpy_d, lpz = (T)lpz_d;
+    Win<T> wx, wy;
+    gimp_window<T, DIM == 3, GRAD>(xi, lpx, T(1) / (T(4) * lpx), GRAD ? T(2) / DX : T(0), wx);
+    gimp_window<T, DIM == 3, GRAD>(eta, lpy, T(1) / (T(4) * lpy), GRAD ? T(2) / DY : T(0), wy);
     const int base = n0 + (wx.s - 1) + (wy.s - 1) * g.yplane;
     if (DIM == 2) {
 #pragma unroll
         for (int jy = 0; jy < 3; jy++) {
 #pragma unroll
             for (int jx = 0; jx < 3; jx++) {
-                const double Sx = wx.S[jx], Sy = wy.S[jy];
-                double dx = 0., dy = 0.;
+                const T Sx = wx.S[jx], Sy = wy.S[jy];
+                T dx = 0, dy = 0;
                 if (GRAD) {
                     dx = wx.dS[jx] * Sy;
                     dy = Sx * wy.dS[jy];
                 }
-                f(base + jx + jy * g.yplane, Sx * Sy, dx, dy, 0.);
+                f(base + jx + jy * g.yplane, Sx * Sy, dx, dy, T(0));
             }
         }
     } else {
-        Win wz;
-        gimp_window<true, GRAD>(zeta, lpz, 1. / (4. * lpy), GRAD ? 2.0 / DZ : 0., wz);
+        Win<T> wz;
+        gimp_window<T, true, GRAD>(zeta, lpz, T(1) / (T(4) * lpy), GRAD ? T(2) / DZ : T(0), wz);
         const int base3 = base + (wz.s - 1) * g.zplane;
 #pragma unroll
         for (int jz = 0; jz < 3; jz++) {
 #pragma unroll
             for (int jy = 0; jy < 3; jy++) {
-                const double Syz = wy.S[jy] * wz.S[jz];
-                const double dySz = GRAD ? wy.dS[jy] * wz.S[jz] : 0.;
-                const double SydZ = GRAD ? wy.S[jy] * wz.dS[jz] : 0.;
+                const T Syz = wy.S[jy] * wz.S[jz];
+                const T dySz = GRAD ? wy.dS[jy] * wz.S[jz] : T(0);
+                const T SydZ = GRAD ? wy.S[jy] * wz.dS[jz] : T(0);
 #pragma unroll
                 for (int jx = 0; jx < 3; jx++) {
-                    const double Sx = wx.S[jx];
-                    double dx = 0., dy = 0., dz = 0.;
+                    const T Sx = wx.S[jx];
+                    T dx = 0, dy = 0, dz = 0;
                     if (GRAD) {
                         dx = wx.dS[jx] * Syz;
                         dy = Sx * dySz;
@@ -118,11 +122,24 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi
 // particle kernels
 // ---------------------------------------------------------------------------
 
+// Weight arithmetic of each transfer mode.
+template <bool MIX>
+struct Wt {
+    using T = double;
+};
+template <>
+struct Wt<true> {
+    using T = float;
+};
+
 // InitializationTask::Execute (natural coordinates, InitializationTask.cpp:59-83)
 // and MassAndMomentumTask::Execute with NodalPoint::AddMassMomentum
-// (MassAndMomentumTask.cpp:48-127, NodalPointMPM.cpp:419-453).
-template <int DIM, int SHAPE>
+// (MassAndMomentumTask.cpp:48-127, NodalPointMPM.cpp:419-453).  Momentum and
+// mass accumulate in FP64 in both modes: grid velocities carry the bulk motion
+// and their differences across a cell are the strain rate.
+template <int DIM, int SHAPE, bool MIX>
 __global__ void __launch_bounds__(256) k_p2g(DevGrid g, DevParticles p, DevNodes nd) {
+    using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     const int e = p.elem[i];
@@ -134,16 +151,16 @@ __global__ void __launch_bounds__(256) k_p2g(DevGrid g, DevParticles p, DevNodes
     if (DIM == 3) p.zeta[i] = zeta;
     const double mp = p.mass[i];
     const double vx = p.vx[i], vy = p.vy[i], vz = DIM == 3 ? p.vz[i] : 0.;
-    for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1.,
-                                     [&](int n, double N, double, double, double) {
-                                         if (N == 0.) return;
-                                         const double fnmp = N * mp;
-                                         atomicAdd(&nd.mass[n], fnmp);
-                                         atomicAdd(&nd.px[n], vx * fnmp);
-                                         atomicAdd(&nd.py[n], vy * fnmp);
-                                         if (DIM == 3) atomicAdd(&nd.pz[n], vz * fnmp);
-                                         nd.active[n] = 1;
-                                     });
+    for_each_node<DIM, SHAPE, false, T>(g, e, xi, eta, zeta, p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1.,
+                                        [&](int n, T N, T, T, T) {
+                                            if (N == T(0)) return;
+                                            const double fnmp = (double)N * mp;
+                                            atomicAdd(&nd.mass[n], fnmp);
+                                            atomicAdd(&nd.px[n], vx * fnmp);
+                                            atomicAdd(&nd.py[n], vy * fnmp);
+                                            if (DIM == 3) atomicAdd(&nd.pz[n], vz * fnmp);
+                                            nd.active[n] = 1;
+                                        });
 }
 
 template <int DIM>
@@ -159,64 +176,94 @@ __device__ __forceinline__ void constitutive(const DevMat *mats, const DevPartic
     }
 }
 
-// gather of ExtrapVelocityGradient (MatPoint2D.cpp:57-87, MatPoint3D.cpp:50-75)
-template <int DIM, int SHAPE>
+// gather of ExtrapVelocityGradient (MatPoint2D.cpp:57-87, MatPoint3D.cpp:50-75),
+// scaled by the strain time step.  Mixed mode: sum over nodes of
+// (v_node - v_particle) * grad N in FP32 -- the same value in exact arithmetic
+// because the gradients sum to zero -- where the velocity difference is formed
+// exactly from FP32 hi/lo pairs of both velocities, so the bulk motion cancels
+// before any rounding.
+template <int DIM, int SHAPE, bool MIX>
 __device__ __forceinline__ void velocity_gradient(const DevGrid &g, const DevParticles &p, const DevNodes &nd, int i,
                                                   double st, double du[9]) {
-    double d[9] = {0., 0., 0., 0., 0., 0., 0., 0., 0.};
-    for_each_node<DIM, SHAPE, true>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
-                                    DIM == 3 ? p.lpz[i] : 1.,
-                                    [&](int n, double N, double dx, double dy, double dz) {
-                                        if (N == 0.) return;
-                                        const double vx = nd.vx[n], vy = nd.vy[n];
-                                        d[0] += vx * dx;
-                                        d[1] += vx * dy;
-                                        d[3] += vy * dx;
-                                        d[4] += vy * dy;
-                                        if (DIM == 3) {
-                                            const double vz = nd.vz[n];
-                                            d[2] += vx * dz;
-                                            d[5] += vy * dz;
-                                            d[6] += vz * dx;
-                                            d[7] += vz * dy;
-                                            d[8] += vz * dz;
-                                        }
-                                    });
+    using T = typename Wt<MIX>::T;
+    T d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    float ph[3] = {0.f, 0.f, 0.f}, pl[3] = {0.f, 0.f, 0.f};
+    if (MIX) {
+        split2(p.vx[i], ph[0], pl[0]);
+        split2(p.vy[i], ph[1], pl[1]);
+        if (DIM == 3) split2(p.vz[i], ph[2], pl[2]);
+    }
+    for_each_node<DIM, SHAPE, true, T>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
+                                       DIM == 3 ? p.lpz[i] : 1., [&](int n, T N, T dx, T dy, T dz) {
+                                           if (N == T(0)) return;
+                                           T vx, vy, vz = 0;
+                                           if (MIX) {
+                                               vx = (T)((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0]));
+                                               vy = (T)((nd.vhy[n] - ph[1]) + (nd.vly[n] - pl[1]));
+                                               if (DIM == 3) vz = (T)((nd.vhz[n] - ph[2]) + (nd.vlz[n] - pl[2]));
+                                           } else {
+                                               vx = (T)nd.vx[n];
+                                               vy = (T)nd.vy[n];
+                                               if (DIM == 3) vz = (T)nd.vz[n];
+                                           }
+                                           d[0] += vx * dx;
+                                           d[1] += vx * dy;
+                                           d[3] += vy * dx;
+                                           d[4] += vy * dy;
+                                           if (DIM == 3) {
+                                               d[2] += vx * dz;
+                                               d[5] += vy * dz;
+                                               d[6] += vz * dx;
+                                               d[7] += vz * dy;
+                                               d[8] += vz * dz;
+                                           }
+                                       });
 #pragma unroll
-    for (int k = 0; k < 9; k++) du[k] = d[k] * st;
+    for (int k = 0; k < 9; k++) du[k] = (double)d[k] * st;
 }
 
 // UpdateStrainsFirstTask::FullStrainUpdate (UpdateStrainsFirstTask.cpp:101-168)
 // fused with GridForcesTask::Execute and MatPoint2D/3D::GetFintPlusFext
 // (GridForcesTask.cpp:40-153, MatPoint2D.cpp:242-262, MatPoint3D.cpp:248-269).
-template <int DIM, int SHAPE, bool STRAIN>
+// Mixed mode: internal-force products in FP32 into FP32 accumulators.
+template <int DIM, int SHAPE, bool STRAIN, bool MIX>
 __global__ void __launch_bounds__(256) k_strain_forces(DevGrid g, DevParticles p, DevNodes nd, const DevMat *mats,
                                                        double st) {
+    using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     if (STRAIN) {
         double du[9];
-        velocity_gradient<DIM, SHAPE>(g, p, nd, i, st, du);
+        velocity_gradient<DIM, SHAPE, MIX>(g, p, nd, i, st, du);
         constitutive<DIM>(mats, p, i, du);
     }
     // -mp * (sigma - P I): the internal force of GetFintPlusFext, scaled once
     const double mp = p.mass[i], P = p.pressure[i];
-    const double sxx = -mp * (p.sxx[i] - P), syy = -mp * (p.syy[i] - P), sxy = -mp * p.sxy[i];
-    const double szz = DIM == 3 ? -mp * (p.szz[i] - P) : 0., sxz = DIM == 3 ? -mp * p.sxz[i] : 0.,
-                 syz = DIM == 3 ? -mp * p.syz[i] : 0.;
-    for_each_node<DIM, SHAPE, true>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
-                                    DIM == 3 ? p.lpz[i] : 1.,
-                                    [&](int n, double N, double dx, double dy, double dz) {
-                                        if (N == 0.) return;
-                                        if (DIM == 2) {
-                                            atomicAdd(&nd.fx[n], sxx * dx + sxy * dy);
-                                            atomicAdd(&nd.fy[n], sxy * dx + syy * dy);
-                                        } else {
-                                            atomicAdd(&nd.fx[n], sxx * dx + sxy * dy + sxz * dz);
-                                            atomicAdd(&nd.fy[n], sxy * dx + syy * dy + syz * dz);
-                                            atomicAdd(&nd.fz[n], sxz * dx + syz * dy + szz * dz);
-                                        }
-                                    });
+    const T sxx = (T)(-mp * (p.sxx[i] - P)), syy = (T)(-mp * (p.syy[i] - P)), sxy = (T)(-mp * p.sxy[i]);
+    const T szz = DIM == 3 ? (T)(-mp * (p.szz[i] - P)) : T(0), sxz = DIM == 3 ? (T)(-mp * p.sxz[i]) : T(0),
+            syz = DIM == 3 ? (T)(-mp * p.syz[i]) : T(0);
+    for_each_node<DIM, SHAPE, true, T>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
+                                       DIM == 3 ? p.lpz[i] : 1., [&](int n, T N, T dx, T dy, T dz) {
+                                           if (N == T(0)) return;
+                                           T fx, fy, fz = 0;
+                                           if (DIM == 2) {
+                                               fx = sxx * dx + sxy * dy;
+                                               fy = sxy * dx + syy * dy;
+                                           } else {
+                                               fx = sxx * dx + sxy * dy + sxz * dz;
+                                               fy = sxy * dx + syy * dy + syz * dz;
+                                               fz = sxz * dx + syz * dy + szz * dz;
+                                           }
+                                           if (MIX) {
+                                               atomicAdd(&nd.gx[n], (float)fx);
+                                               atomicAdd(&nd.gy[n], (float)fy);
+                                               if (DIM == 3) atomicAdd(&nd.gz[n], (float)fz);
+                                           } else {
+                                               atomicAdd(&nd.fx[n], (double)fx);
+                                               atomicAdd(&nd.fy[n], (double)fy);
+                                               if (DIM == 3) atomicAdd(&nd.fz[n], (double)fz);
+                                           }
+                                       });
 }
 
 // ResetElementsTask::ResetElement with MeshInfo::FindElementFromPoint and
@@ -281,30 +328,49 @@ __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticl
 // MatPoint2D.cpp:99-196), fused with the momentum re-extrapolation of
 // UpdateStrainsLastContactTask (UpdateStrainsLastContactTask.cpp:71-146,
 // NodalPoint::AddMassMomentumLast NodalPointMPM.cpp:470-486), which uses the
-// same natural coordinates of the step.
-template <int DIM, int SHAPE, bool USL>
+// same natural coordinates of the step.  Mixed mode: S v is formed as
+// v_particle + sum N (v_node - v_particle) (the weights sum to one) with the
+// differences from FP32 pairs, S a in FP32; the update itself is FP64.
+template <int DIM, int SHAPE, bool USL, bool MIX>
 __global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes nd, double dt, unsigned *err) {
+    using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    double Sv[3] = {0., 0., 0.}, Sa[3] = {0., 0., 0.};
+    T Sv[3] = {0, 0, 0}, Sa[3] = {0, 0, 0};
     const int e = p.elem[i];
     const double xi = p.xi[i], eta = p.eta[i], zeta = DIM == 3 ? p.zeta[i] : 0.;
     const double lx = p.lpx[i], ly = p.lpy[i], lz = DIM == 3 ? p.lpz[i] : 1.;
-    for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, double N, double, double, double) {
-        if (N == 0.) return;
-        Sv[0] += nd.vx[n] * N;
-        Sv[1] += nd.vy[n] * N;
-        if (DIM == 3) Sv[2] += nd.vz[n] * N;
-        Sa[0] += nd.ax[n] * N;   // f/m of the node (the reference forms f*(N/m))
-        Sa[1] += nd.ay[n] * N;
-        if (DIM == 3) Sa[2] += nd.az[n] * N;
-    });
     double v[3] = {p.vx[i], p.vy[i], DIM == 3 ? p.vz[i] : 0.};
+    float ph[3] = {0.f, 0.f, 0.f}, pl[3] = {0.f, 0.f, 0.f};
+    if (MIX) {
+#pragma unroll
+        for (int a = 0; a < DIM; a++) split2(v[a], ph[a], pl[a]);
+    }
+    for_each_node<DIM, SHAPE, false, T>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, T N, T, T, T) {
+        if (N == T(0)) return;
+        if (MIX) {
+            Sv[0] += ((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0])) * N;
+            Sv[1] += ((nd.vhy[n] - ph[1]) + (nd.vly[n] - pl[1])) * N;
+            if (DIM == 3) Sv[2] += ((nd.vhz[n] - ph[2]) + (nd.vlz[n] - pl[2])) * N;
+            Sa[0] += nd.bx[n] * N;
+            Sa[1] += nd.by[n] * N;
+            if (DIM == 3) Sa[2] += nd.bz[n] * N;
+        } else {
+            Sv[0] += nd.vx[n] * N;
+            Sv[1] += nd.vy[n] * N;
+            if (DIM == 3) Sv[2] += nd.vz[n] * N;
+            Sa[0] += nd.ax[n] * N;  // f/m of the node (the reference forms f*(N/m))
+            Sa[1] += nd.ay[n] * N;
+            if (DIM == 3) Sa[2] += nd.az[n] * N;
+        }
+    });
     double xp[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
 #pragma unroll
     for (int a = 0; a < DIM; a++) {
-        const double vm = Sv[a] - Sa[a] * dt;
-        const double dv = Sa[a] * dt;
+        const double sv = MIX ? v[a] + (double)Sv[a] : (double)Sv[a];
+        const double sa = (double)Sa[a];
+        const double vm = sv - sa * dt;
+        const double dv = sa * dt;
         v[a] += dv;
         xp[a] += (vm + 0.5 * dv) * dt;
     }
@@ -318,9 +384,9 @@ __global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes
     }
     if (USL) {
         const double mp = p.mass[i];
-        for_each_node<DIM, SHAPE, false>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, double N, double, double, double) {
-            if (N == 0.) return;
-            const double fnmp = N * mp;
+        for_each_node<DIM, SHAPE, false, T>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, T N, T, T, T) {
+            if (N == T(0)) return;
+            const double fnmp = (double)N * mp;
             atomicAdd(&nd.ux[n], v[0] * fnmp);
             atomicAdd(&nd.uy[n], v[1] * fnmp);
             if (DIM == 3) atomicAdd(&nd.uz[n], v[2] * fnmp);
@@ -332,13 +398,13 @@ __global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes
 
 // UpdateStrainsFirstTask::FullStrainUpdate called from
 // UpdateStrainsLastContactTask (:149), fused with ResetElementsTask.
-template <int DIM, int SHAPE>
+template <int DIM, int SHAPE, bool MIX>
 __global__ void __launch_bounds__(256) k_strain_last(DevGrid g, DevParticles p, DevNodes nd, const DevMat *mats,
                                                      double st, unsigned *err) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     double du[9];
-    velocity_gradient<DIM, SHAPE>(g, p, nd, i, st, du);
+    velocity_gradient<DIM, SHAPE, MIX>(g, p, nd, i, st, du);
     constitutive<DIM>(mats, p, i, du);
     reset_element<DIM>(g, p, i, err);
 }
@@ -396,18 +462,26 @@ __device__ __forceinline__ void node_bcs(const DevBCs &b, int grp, int pass, dou
     }
 }
 
-// MatVelocityField::GridValueCalculation (MatVelocityField.cpp:239-251)
+// MatVelocityField::GridValueCalculation (MatVelocityField.cpp:239-251); the
+// mixed mode also keeps the velocity as FP32 hi/lo pairs.
+template <bool MIX>
 __device__ __forceinline__ void node_velocity(const DevNodes &nd, int n, double mass, const double p[3]) {
     if (mass == 0.) return;
     const double r = 1. / mass;
-    nd.vx[n] = p[0] * r;
-    nd.vy[n] = p[1] * r;
-    nd.vz[n] = p[2] * r;
+    const double vx = p[0] * r, vy = p[1] * r, vz = p[2] * r;
+    nd.vx[n] = vx;
+    nd.vy[n] = vy;
+    nd.vz[n] = vz;
+    if (MIX) {
+        split2(vx, nd.vhx[n], nd.vlx[n]);
+        split2(vy, nd.vhy[n], nd.vly[n]);
+        split2(vz, nd.vhz[n], nd.vlz[n]);
+    }
 }
 
 // PostExtrapolationTask::Execute (PostExtrapolationTask.cpp:46-165):
 // vk[pkCopy] = pk, velocity conditions of MASS_MOMENTUM_CALL, then grid velocity.
-template <int DIM>
+template <int DIM, bool MIX>
 __global__ void k_node_post(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, int do_bcs, double t,
                             double dt) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
@@ -425,19 +499,28 @@ __global__ void k_node_post(DevNodes nd, int nnodes, DevBCs b, const int *bc_gro
         nd.py[n] = p[1];
         if (DIM == 3) nd.pz[n] = p[2];
     }
-    node_velocity(nd, n, m, p);
+    node_velocity<MIX>(nd, n, m, p);
 }
 
 // PostForcesTask::Execute (restore momenta, GRID_FORCES_CALL velocity
 // conditions; PostForcesTask.cpp:43-111) and UpdateMomentaTask::Execute
 // (p += f dt, UPDATE_MOMENTUM_CALL conditions; UpdateMomentaTask.cpp:44-94),
 // then grid velocity for the particle update.
-template <int DIM>
+template <int DIM, bool MIX>
 __global__ void k_node_update(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, double t, double dt) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !nd.active[n]) return;
     double p[3] = {nd.cx[n], nd.cy[n], DIM == 3 ? nd.cz[n] : 0.};
-    double f[3] = {nd.fx[n], nd.fy[n], DIM == 3 ? nd.fz[n] : 0.};
+    double f[3];
+    if (MIX) {
+        f[0] = (double)nd.gx[n];
+        f[1] = (double)nd.gy[n];
+        f[2] = DIM == 3 ? (double)nd.gz[n] : 0.;
+    } else {
+        f[0] = nd.fx[n];
+        f[1] = nd.fy[n];
+        f[2] = DIM == 3 ? nd.fz[n] : 0.;
+    }
     const double m = nd.mass[n];
     const int grp = bc_group[n];
     if (grp >= 0) node_bcs(b, grp, BC_GRID_FORCES, m, t, dt, p, f);
@@ -452,17 +535,22 @@ __global__ void k_node_update(DevNodes nd, int nnodes, DevBCs b, const int *bc_g
         nd.pz[n] = p[2];
         nd.fz[n] = f[2];
     }
-    node_velocity(nd, n, m, p);
+    node_velocity<MIX>(nd, n, m, p);
     // acceleration for the particle update (every active node has mass > 0)
     const double r = 1. / m;
     nd.ax[n] = f[0] * r;
     nd.ay[n] = f[1] * r;
     if (DIM == 3) nd.az[n] = f[2] * r;
+    if (MIX) {
+        nd.bx[n] = (float)(f[0] * r);
+        nd.by[n] = (float)(f[1] * r);
+        if (DIM == 3) nd.bz[n] = (float)(f[2] * r);
+    }
 }
 
 // UpdateStrainsLastContactTask: p = second extrapolation, UPDATE_STRAINS_LAST_CALL
 // conditions, grid velocity (UpdateStrainsLastContactTask.cpp:60-152).
-template <int DIM>
+template <int DIM, bool MIX>
 __global__ void k_node_usl(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, double t, double dt) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !nd.active[n]) return;
@@ -476,7 +564,7 @@ __global__ void k_node_usl(DevNodes nd, int nnodes, DevBCs b, const int *bc_grou
     nd.px[n] = p[0];
     nd.py[n] = p[1];
     if (DIM == 3) nd.pz[n] = p[2];
-    node_velocity(nd, n, m, p);
+    node_velocity<MIX>(nd, n, m, p);
 }
 
 }  // namespace nmg

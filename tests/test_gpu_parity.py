@@ -86,3 +86,29 @@ def test_cell_sort_is_a_stable_argsort(n, nelems, gpu_lib):
     st = gpu_lib.mpmgpu_sort_by_cell(C.c_void_p(d_keys.data_ptr()), n, nelems, C.c_void_p(d_perm.data_ptr()), None)
     assert st == 0
     assert np.array_equal(d_perm.cpu().numpy(), np.argsort(keys, kind="stable").astype(np.int32))
+
+
+TOL_MIXED = 1e-5  # relative L2, FP32 transfers + FP64 constitutive vs the reference's FP64 path
+
+
+@pytest.mark.parametrize("case", golden_cases())
+def test_mixed_precision_matches_reference(case, gpu_lib):
+    meta, g = load_golden(case)
+    m = model_for(meta)
+    out = gpu_run(m, meta["steps"], precision=1)
+    v = archive_view(out, 3 if meta["three_d"] else 2, m.materials[0]["rho"])
+    for k in ("pos", "vel", "stress", "strain"):
+        assert rel_l2(v[k], g["final_" + k]) <= TOL_MIXED, (k, rel_l2(v[k], g["final_" + k]))
+    assert np.array_equal(v["elem"], g["final_elem"])
+
+
+def test_mixed_precision_taylor_against_oracle(gpu_lib):
+    """A longer 3D plastic run: stresses stay within 1e-5 of the FP64 path."""
+    import oracle_lib
+    from nairn_gb300 import model, abi
+    m = model.taylor_3d(radius=2.0, length=5.0, cell=0.25, steps=300)
+    ref = abi.copy_particles(m.particles)
+    oracle_lib.run(m, ref, m.nsteps, nthreads=8)
+    out = gpu_run(m, m.nsteps, precision=1)
+    for k in ("x", "y", "z", "vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "syz", "sxz", "hist0"):
+        assert rel_l2(out[k], ref[k]) <= TOL_MIXED, (k, rel_l2(out[k], ref[k]))
