@@ -248,6 +248,73 @@ long long mpmgpu_launch_count(const MpmGpuCtx *ctx);
 int mpmgpu_host_register(void *ptr, uint64_t bytes);
 int mpmgpu_host_unregister(void *ptr);
 
+/* ---- batch: many independent runs in one graph-captured step ----------------
+ * A batch holds the state of many runs on the device and advances all of them
+ * with one launch of each step kernel.  The runs share the batch's analysis
+ * options (dimension, method, shape functions, precision) and
+ * differ in grid, materials, velocity conditions, particles, time step and
+ * step count.  Each run is the same computation as a single-run context given
+ * the same input (mpmgpu_create ... mpmgpu_step): only the order of the atomic
+ * node sums differs.  It has no counterpart in the reference, which runs one
+ * analysis per process (NairnMPM::StartAnalysis, NairnMPM.cpp:91-218).  One
+ * host thread drives a batch. */
+typedef struct MpmGpuBatch MpmGpuBatch;
+
+typedef struct {
+    int32_t np;               /* MPMGPU_PLANE_STRAIN or MPMGPU_THREED        */
+    int32_t method;           /* MPMGPU_USF / _USAVG / _USL                  */
+    int32_t shape;            /* MPMGPU_SHAPE_LINEAR or _UGIMP               */
+    int32_t precision;        /* MPMGPU_PREC_*                               */
+    int32_t sort_interval;    /* cell sort every k steps (0: never)          */
+    int32_t block;            /* threads per block of particle kernels (0: 256) */
+    int32_t max_runs;         /* run slots                                   */
+    int32_t max_materials;    /* material slots (sum over resident runs)     */
+    int64_t max_particles;    /* particle slots (sum over resident runs)     */
+    int64_t max_nodes;        /* grid nodes (sum over resident runs)         */
+    double fraction_usf;      /* USAVG split (0 -> 0.5)                      */
+} MpmGpuBatchOptions;
+
+/* run states returned by mpmgpu_batch_run_state; a failed run reports the
+ * negated status (-MPMGPU_ERR_LEFT_GRID, -MPMGPU_ERR_NAN) and stops stepping */
+enum { MPMGPU_RUN_EMPTY = 0, MPMGPU_RUN_RUNNING = 1, MPMGPU_RUN_FINISHED = 2 };
+
+typedef struct {
+    int32_t runs, running;    /* resident runs, runs still stepping          */
+    int32_t block, sort_interval;
+    int64_t particles_used;   /* particle slots in use (including dead ones) */
+    int64_t particles_dead;   /* slots of removed runs, dropped at the next sort */
+    int64_t nodes_used;       /* extent of the node arena in use             */
+    int64_t steps;            /* batched steps taken                         */
+    int64_t launches;         /* kernels launched (graph nodes included)     */
+} MpmGpuBatchInfo;
+
+/* Device bytes mpmgpu_batch_create allocates for these capacities. */
+int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *opts);
+int mpmgpu_batch_create(const MpmGpuBatchOptions *opts, MpmGpuBatch **out);
+/* Admit one run; *run_id receives its slot.  MPMGPU_ERR_BUSY: not enough free
+ * run slots, particles, nodes or material slots now (retry after removals). */
+int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
+                         const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuParticles *p, double timestep,
+                         int32_t nsteps, int32_t *run_id);
+/* Advance every running run by nsteps steps (a run stops at its own count). */
+int mpmgpu_batch_step(MpmGpuBatch *b, int32_t nsteps);
+int mpmgpu_batch_step_timed(MpmGpuBatch *b, int32_t nsteps, double *ms);
+int mpmgpu_batch_run_state(const MpmGpuBatch *b, int32_t run_id, int32_t *state, int32_t *steps_done);
+/* Particle state of a run in its upload order (x0 columns are not kept). */
+int mpmgpu_batch_download_run(MpmGpuBatch *b, int32_t run_id, MpmGpuParticles *out);
+/* Remove a run (downloading it first when out is not NULL) and free its slots. */
+int mpmgpu_batch_remove_run(MpmGpuBatch *b, int32_t run_id, MpmGpuParticles *out);
+/* Particle-kernel block size (64, 128, 256) and sort interval. */
+int mpmgpu_batch_set_tuning(MpmGpuBatch *b, int32_t block, int32_t sort_interval);
+/* Time candidate block sizes and sort intervals on real steps of the resident
+ * runs (the trial steps count as steps of those runs) and keep the fastest. */
+int mpmgpu_batch_autotune(MpmGpuBatch *b, int32_t trial_steps, int32_t *block, int32_t *sort_interval,
+                          double *ms_per_step);
+int mpmgpu_batch_info(const MpmGpuBatch *b, MpmGpuBatchInfo *info);
+const char *mpmgpu_batch_last_error(const MpmGpuBatch *b);
+void *mpmgpu_batch_stream(MpmGpuBatch *b);
+void mpmgpu_batch_destroy(MpmGpuBatch *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -1,0 +1,905 @@
+// batch.cuh -- many independent MPM runs advanced together on one GPU.
+// Included by mpm_gpu.cu (one translation unit); implements the
+// mpmgpu_batch_* entry points of include/nairn_mpm_gpu.h.
+//
+// Runs share arenas: particle slots (structure of arrays, one run id per
+// slot), grid nodes (each run owns a contiguous node range), cells (the sort
+// key space) and material slots.  A batched step launches every step kernel
+// once over all slots and all used nodes; each thread finds its run in the
+// device run table (DevRun), so runs of different sizes, grids, materials and
+// time steps advance together and each stops after its own step count.  The
+// step (optionally preceded by the cell sort) is captured once in a CUDA graph
+// and replayed until the set of runs changes.  The particle arena has two
+// buffers that the sort ping-pongs between; one graph is kept per buffer.
+// Removed runs leave dead slots; the next sort puts them last and the slot
+// count shrinks, so the sort is also the compaction.
+#pragma once
+
+#include <map>
+
+namespace {
+
+// first-fit allocator of integer ranges in [0, cap)
+struct RangeAlloc {
+    long long cap = 0;
+    std::map<long long, long long> free;  // start -> length
+    void init(long long c) {
+        cap = c;
+        free.clear();
+        if (c > 0) free[0] = c;
+    }
+    long long alloc(long long n) {
+        if (n <= 0) return -1;
+        for (auto it = free.begin(); it != free.end(); ++it) {
+            if (it->second >= n) {
+                const long long s = it->first, len = it->second;
+                free.erase(it);
+                if (len > n) free[s + n] = len - n;
+                return s;
+            }
+        }
+        return -1;
+    }
+    void release(long long s, long long n) {
+        if (n <= 0) return;
+        auto it = free.emplace(s, n).first;
+        auto nx = std::next(it);
+        if (nx != free.end() && it->first + it->second == nx->first) {
+            it->second += nx->second;
+            free.erase(nx);
+        }
+        if (it != free.begin()) {
+            auto pv = std::prev(it);
+            if (pv->first + pv->second == it->first) {
+                pv->second += it->second;
+                free.erase(it);
+            }
+        }
+    }
+    // one past the highest used index
+    long long high_water() const {
+        if (free.empty()) return cap;
+        auto last = std::prev(free.end());
+        return last->first + last->second == cap ? last->first : cap;
+    }
+};
+
+struct BatchRun {
+    bool used = false;
+    int state = 0;  // MPMGPU_RUN_* (or the negated status of a failed run)
+    int np = 0;
+    long long node_base = 0, nnodes = 0, cell_base = 0, nelems = 0, mat_base = 0, nmat = 0;
+    int steps_total = 0, steps_done = 0;
+    std::vector<MpmGpuVelBC> bcs;  // batch-global 1-based node numbers
+};
+
+// admission of np particles at slots [start, start+np): slot order = host
+// order, run id, material index moved into the run's material slots
+__global__ void k_batch_admit(int *mat, const int *elem, int *orig, int *run, int start, int np, int r, int mat_base,
+                              int nmat, int nelems, unsigned *flag) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= np) return;
+    const int i = start + j;
+    orig[i] = j;
+    run[i] = r;
+    const int m = mat[i], e = elem[i];
+    if (m < 0 || m >= nmat || e < 0 || e >= nelems) atomicOr(flag, 8u);
+    mat[i] = m + mat_base;
+}
+
+__global__ void k_fill_int(int *a, long long start, long long n, int v) {
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j < n) a[start + j] = v;
+}
+
+// slots of run r -> packed columns of np values in the run's original order
+__global__ void k_batch_extract(const double *pblock, int cap, const int *mat, const int *elem, const int *orig,
+                                const int *run, int n, int r, int mat_base, double *out, int *iout, int np,
+                                int ncols) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n || run[i] != r) return;
+    const int o = orig[i];
+    for (int k = 0; k < ncols; k++) out[(size_t)k * np + o] = pblock[(size_t)k * cap + i];
+    iout[o] = mat[i] - mat_base;
+    iout[np + o] = elem[i];
+}
+
+// mark the slots of run r empty
+__global__ void k_batch_kill(int *run, int n, int r) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i < n && run[i] == r) run[i] = -1;
+}
+
+// sort keys of a batch: the run's cell base + element; empty slots last
+__global__ void k_batch_keys(const int *elem, const int *run, const DevRun *runs, int *keys, int *vals, int n,
+                             int dead_key) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= n) return;
+    const int r = run[i];
+    keys[i] = r < 0 ? dead_key : runs[r].cell_base + elem[i];
+    vals[i] = i;
+}
+
+// dst[k*cap + j] = src[k*cap + perm[j]] for the first n slots of every column
+template <typename T>
+__global__ void k_gather_cap(const T *__restrict__ src, T *__restrict__ dst, const int *__restrict__ perm, int n,
+                             int ncols, int cap) {
+    const int j = blockIdx.x * blockDim.x + threadIdx.x;
+    if (j >= n) return;
+    const int s = perm[j];
+    for (int k = 0; k < ncols; k++) dst[(size_t)k * cap + j] = src[(size_t)k * cap + s];
+}
+
+// step-start clear of the accumulated node columns of the used node range
+template <bool MIX>
+__global__ void k_clear_nodes(DevNodes nd, int nn) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    nd.mass[n] = 0.;
+    nd.px[n] = nd.py[n] = nd.pz[n] = 0.;
+    nd.fx[n] = nd.fy[n] = nd.fz[n] = 0.;
+    nd.ux[n] = nd.uy[n] = nd.uz[n] = 0.;
+    nd.active[n] = 0;
+    if (MIX) nd.gx[n] = nd.gy[n] = nd.gz[n] = 0.f;
+}
+
+constexpr int kBatchIntCols = 4;  // mat, elem, orig, run
+
+struct BatchGraph {
+    cudaGraphExec_t exec = nullptr;
+    long long key = -1;
+};
+
+}  // namespace
+
+struct MpmGpuBatch {
+    MpmGpuBatchOptions o{};
+    int dim = 2;
+    int pcap = 0, ncap = 0;
+    int tb = 256;  // threads per block of the particle kernels
+    // particle arena, two buffers: kParticleDoubles+1 double columns and
+    // kBatchIntCols int columns of capacity pcap each; buffer `par` is current
+    double *pbuf[2] = {nullptr, nullptr};
+    int *ibuf[2] = {nullptr, nullptr};
+    int par = 0;
+    DevParticles p{};
+    int *orig = nullptr;
+    int n_used = 0, n_dead = 0;
+    // node arena
+    DevNodes nd{};
+    double *nblock = nullptr;
+    float *fblock = nullptr;
+    double *coords = nullptr;  // node coordinates; a run's sit at its node base
+    int *nrun = nullptr, *bc_group = nullptr;
+    RangeAlloc nodes, cells, matslots;
+    int node_used = 0;
+    // sort scratch
+    int *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr}, *hist = nullptr, *sums = nullptr;
+    int sort_bits = 1;
+    long long since_sort = 1LL << 40;
+    // materials, runs, velocity conditions
+    DevMat *mats = nullptr;
+    DevRun *runs_dev = nullptr;
+    std::vector<DevRun> runs_host;
+    std::vector<BatchRun> runs;
+    void *bc_block = nullptr;
+    DevBCs bcs{};
+    bool bcs_dirty = true;
+    long long layout = 0;  // bumped whenever the captured launches would change
+    unsigned *flag = nullptr;
+    cudaStream_t stream = nullptr;
+    BatchGraph graphs[2][2];  // [arena buffer][with sort]
+    long long launches = 0;
+    long long steps = 0;
+    std::string msg;
+};
+
+namespace {
+
+int berr(MpmGpuBatch *b, int code, const std::string &m) {
+    if (b) b->msg = m;
+    else g_static_err = m;
+    return code;
+}
+
+#define BCK(call)                                                                                 \
+    do {                                                                                          \
+        cudaError_t e_ = (call);                                                                  \
+        if (e_ != cudaSuccess)                                                                    \
+            return berr(b, MPMGPU_ERR_CUDA, std::string(#call) + ": " + cudaGetErrorString(e_)); \
+    } while (0)
+
+void batch_link(MpmGpuBatch *b) {
+    DevParticles &p = b->p;
+    const size_t cap = (size_t)b->pcap;
+    double *pb = b->pbuf[b->par];
+    int *ib = b->ibuf[b->par];
+    double **cols[kParticleDoubles + 1] = {&p.x, &p.y, &p.z, &p.vx, &p.vy, &p.vz, &p.mass, &p.lpx, &p.lpy, &p.lpz,
+                                           &p.exx, &p.eyy, &p.ezz, &p.exy, &p.exz, &p.eyz, &p.wxy, &p.wxz, &p.wyz,
+                                           &p.sxx, &p.syy, &p.szz, &p.sxy, &p.sxz, &p.syz, &p.pressure,
+                                           &p.pxx, &p.pyy, &p.pzz, &p.pxy, &p.pxz, &p.pyz,
+                                           &p.hist0, &p.hist1, &p.work, &p.plast, &p.xi, &p.eta, &p.zeta};
+    for (int k = 0; k <= kParticleDoubles; k++) *cols[k] = pb + (size_t)k * cap;
+    p.mat = ib;
+    p.elem = ib + cap;
+    b->orig = ib + 2 * cap;
+    p.run = ib + 3 * cap;
+    p.n = b->n_used;
+}
+
+void batch_drop_graphs(MpmGpuBatch *b) {
+    for (auto &row : b->graphs)
+        for (auto &g : row) {
+            if (g.exec) cudaGraphExecDestroy(g.exec);
+            g = BatchGraph{};
+        }
+}
+
+void batch_free(MpmGpuBatch *b) {
+    batch_drop_graphs(b);
+    void *ptrs[] = {b->pbuf[0], b->pbuf[1], b->ibuf[0], b->ibuf[1], b->nblock, b->fblock, b->coords, b->nrun,
+                    b->bc_group, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->sums, b->mats,
+                    b->runs_dev, b->bc_block, b->flag};
+    for (void *q : ptrs)
+        if (q) cudaFree(q);
+    if (b->stream) cudaStreamDestroy(b->stream);
+}
+
+// rebuild the grouped velocity conditions of all runs (after runs come or go)
+int batch_rebuild_bcs(MpmGpuBatch *b) {
+    std::map<int, std::vector<const MpmGpuVelBC *>> by_node;
+    std::vector<int> order;
+    for (const auto &r : b->runs) {
+        if (!r.used) continue;
+        for (const auto &bc : r.bcs) {
+            const int nd = bc.node - 1;
+            if (!by_node.count(nd)) order.push_back(nd);
+            by_node[nd].push_back(&bc);
+        }
+    }
+    const int ng = (int)order.size();
+    int nbc = 0;
+    for (auto &kv : by_node) nbc += (int)kv.second.size();
+    std::vector<int> gnode(ng), start(ng + 1), dir(nbc);
+    std::vector<double> val(nbc), ft(nbc);
+    std::vector<int> group((size_t)std::max(b->node_used, 1), -1);
+    int pos = 0;
+    for (int gi = 0; gi < ng; gi++) {
+        gnode[gi] = order[gi];
+        start[gi] = pos;
+        group[order[gi]] = gi;
+        for (const MpmGpuVelBC *bc : by_node[order[gi]]) {
+            dir[pos] = bc->dir;
+            val[pos] = bc->value;
+            ft[pos] = bc->ftime;
+            pos++;
+        }
+    }
+    start[ng] = pos;
+    BCK(cudaStreamSynchronize(b->stream));
+    if (b->bc_block) cudaFree(b->bc_block);
+    b->bc_block = nullptr;
+    const size_t bytes = sizeof(int) * (ng + ng + 1 + nbc) + sizeof(double) * (2 * nbc) + 64;
+    BCK(cudaMalloc(&b->bc_block, bytes));
+    double *dval = (double *)b->bc_block;
+    double *dft = dval + nbc;
+    int *dnode = (int *)(dft + nbc);
+    int *dstart = dnode + ng;
+    int *ddir = dstart + ng + 1;
+    cudaStream_t s = b->stream;
+    if (nbc) {
+        BCK(cudaMemcpyAsync(dval, val.data(), sizeof(double) * nbc, cudaMemcpyHostToDevice, s));
+        BCK(cudaMemcpyAsync(dft, ft.data(), sizeof(double) * nbc, cudaMemcpyHostToDevice, s));
+        BCK(cudaMemcpyAsync(ddir, dir.data(), sizeof(int) * nbc, cudaMemcpyHostToDevice, s));
+    }
+    if (ng) BCK(cudaMemcpyAsync(dnode, gnode.data(), sizeof(int) * ng, cudaMemcpyHostToDevice, s));
+    BCK(cudaMemcpyAsync(dstart, start.data(), sizeof(int) * (ng + 1), cudaMemcpyHostToDevice, s));
+    if (b->node_used > 0)
+        BCK(cudaMemcpyAsync(b->bc_group, group.data(), sizeof(int) * b->node_used, cudaMemcpyHostToDevice, s));
+    BCK(cudaStreamSynchronize(s));
+    b->bcs.nnodes_bc = ng;
+    b->bcs.node = dnode;
+    b->bcs.start = dstart;
+    b->bcs.dir = ddir;
+    b->bcs.value = dval;
+    b->bcs.ftime = dft;
+    b->bcs_dirty = false;
+    b->layout++;
+    return MPMGPU_OK;
+}
+
+int batch_sort_launches(const MpmGpuBatch *b) { return 1 + 5 * ((b->sort_bits + 7) / 8) + 2; }
+
+// Enqueue the cell sort of the used slots into the other arena buffer and make
+// that buffer current.  Keys are (run cell base + element), so each run's
+// particles are contiguous and in cell order; empty slots sort last.
+void batch_enqueue_sort(MpmGpuBatch *b) {
+    const int n = b->n_used;
+    const int TB = 256, pb = (n + TB - 1) / TB;
+    cudaStream_t s = b->stream;
+    const int dead_key = (int)b->cells.cap;
+    k_batch_keys<<<pb, TB, 0, s>>>(b->p.elem, b->p.run, b->runs_dev, b->keys[0], b->vals[0], n, dead_key);
+    const int cur = radix_sort_passes(n, b->sort_bits, b->keys, b->vals, b->hist, b->sums, s);
+    const int *perm = b->vals[cur];
+    const int other = 1 - b->par;
+    k_gather_cap<double><<<pb, TB, 0, s>>>(b->pbuf[b->par], b->pbuf[other], perm, n, kParticleDoubles + 1, b->pcap);
+    k_gather_cap<int><<<pb, TB, 0, s>>>(b->ibuf[b->par], b->ibuf[other], perm, n, kBatchIntCols, b->pcap);
+    b->par = other;
+    batch_link(b);
+}
+
+// sort now (outside any graph) and drop the empty slots it moved to the end
+int batch_compact(MpmGpuBatch *b) {
+    if (b->n_used > 0) {
+        batch_enqueue_sort(b);
+        b->launches += batch_sort_launches(b);
+        BCK(cudaGetLastError());
+    }
+    b->n_used -= b->n_dead;
+    b->n_dead = 0;
+    b->p.n = b->n_used;
+    b->since_sort = 0;
+    b->layout++;
+    return MPMGPU_OK;
+}
+
+template <int DIM, int SHAPE, bool MIX>
+void batch_enqueue_step(MpmGpuBatch *b) {
+    const int n = b->n_used, NN = b->node_used;
+    const int TB = b->tb, NTB = 256;
+    const int pb = (n + TB - 1) / TB, nb = (NN + NTB - 1) / NTB;
+    cudaStream_t s = b->stream;
+    const int method = b->o.method;
+    StepParams sp{};
+    sp.runs = b->runs_dev;
+    sp.nrun = b->nrun;
+    k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN);
+    k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
+    k_node_post<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, method != MPMGPU_USL);
+    if (method == MPMGPU_USL)
+        k_strain_forces<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    else
+        k_strain_forces<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group);
+    if (method == MPMGPU_USF) {
+        k_g2p<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
+    } else {
+        k_g2p<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
+        k_node_usl<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group);
+        k_strain_last<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    }
+    k_advance_runs<<<(b->o.max_runs + 127) / 128, 128, 0, s>>>(b->runs_dev, b->o.max_runs);
+}
+
+void batch_enqueue_any(MpmGpuBatch *b) {
+    const bool mix = b->o.precision == MPMGPU_PREC_MIXED;
+    const bool lin = b->o.shape == MPMGPU_SHAPE_LINEAR;
+    if (b->dim == 3) {
+        if (mix) lin ? batch_enqueue_step<3, SHAPE_LINEAR, true>(b) : batch_enqueue_step<3, SHAPE_UGIMP, true>(b);
+        else lin ? batch_enqueue_step<3, SHAPE_LINEAR, false>(b) : batch_enqueue_step<3, SHAPE_UGIMP, false>(b);
+    } else {
+        if (mix) lin ? batch_enqueue_step<2, SHAPE_LINEAR, true>(b) : batch_enqueue_step<2, SHAPE_UGIMP, true>(b);
+        else lin ? batch_enqueue_step<2, SHAPE_LINEAR, false>(b) : batch_enqueue_step<2, SHAPE_UGIMP, false>(b);
+    }
+}
+
+int batch_step_launches(const MpmGpuBatch *b) { return b->o.method == MPMGPU_USF ? 7 : 9; }
+
+long long batch_graph_key(const MpmGpuBatch *b) {
+    return ((b->layout * 1000003LL + b->n_used) * 1000003LL + b->node_used) * 1031LL + b->tb;
+}
+
+// the graph of one step (with the sort before it when with_sort) for the
+// current arena buffer; captured when missing or stale
+int batch_graph(MpmGpuBatch *b, int with_sort, cudaGraphExec_t *out) {
+    BatchGraph &G = b->graphs[b->par][with_sort];
+    const long long key = batch_graph_key(b);
+    if (G.exec && G.key == key) {
+        *out = G.exec;
+        return MPMGPU_OK;
+    }
+    if (G.exec) cudaGraphExecDestroy(G.exec);
+    G = BatchGraph{};
+    const int par0 = b->par;
+    cudaGraph_t g = nullptr;
+    BCK(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+    if (with_sort) batch_enqueue_sort(b);
+    batch_enqueue_any(b);
+    cudaError_t e = cudaStreamEndCapture(b->stream, &g);
+    if (b->par != par0) {
+        b->par = par0;
+        batch_link(b);
+    }
+    if (e != cudaSuccess) return berr(b, MPMGPU_ERR_CUDA, std::string("graph capture: ") + cudaGetErrorString(e));
+    e = cudaGraphInstantiate(&G.exec, g, 0);
+    cudaGraphDestroy(g);
+    if (e != cudaSuccess) {
+        G = BatchGraph{};
+        return berr(b, MPMGPU_ERR_CUDA, std::string("graph instantiate: ") + cudaGetErrorString(e));
+    }
+    G.key = key;
+    *out = G.exec;
+    return MPMGPU_OK;
+}
+
+// the graphs of both arena buffers: with the sort when the batch sorts, and
+// without it unless it sorts every step
+int batch_prepare(MpmGpuBatch *b) {
+    const int si = b->o.sort_interval;
+    const int par0 = b->par;
+    int st = MPMGPU_OK;
+    cudaGraphExec_t gx = nullptr;
+    for (int q = 0; q < 2 && st == MPMGPU_OK; q++) {
+        b->par = q;
+        batch_link(b);
+        if (si > 0) st = batch_graph(b, 1, &gx);
+        if (st == MPMGPU_OK && si != 1) st = batch_graph(b, 0, &gx);
+    }
+    b->par = par0;
+    batch_link(b);
+    return st;
+}
+
+int batch_status(unsigned bits) {
+    if (bits & ERR_NAN) return MPMGPU_ERR_NAN;
+    if (bits & (ERR_LEFT_GRID | ERR_EDGE)) return MPMGPU_ERR_LEFT_GRID;
+    return MPMGPU_ERR_INVALID;
+}
+
+int batch_active_runs(const MpmGpuBatch *b) {
+    int k = 0;
+    for (const auto &r : b->runs) k += r.used && r.state == MPMGPU_RUN_RUNNING;
+    return k;
+}
+
+// one graph launch per step; run states are read back at the end
+int batch_steps(MpmGpuBatch *b, int nsteps, double *ms) {
+    if (b->bcs_dirty) {
+        int st = batch_rebuild_bcs(b);
+        if (st != MPMGPU_OK) return st;
+    }
+    if (ms) *ms = 0.;
+    if (b->n_dead > 0) {
+        int st = batch_compact(b);
+        if (st != MPMGPU_OK) return st;
+    }
+    if (!batch_active_runs(b) || b->n_used == 0 || nsteps == 0) return MPMGPU_OK;
+    // capture every graph the steps can use before the first launch, so no
+    // capture sits between launches (or inside the timed region)
+    int st = batch_prepare(b);
+    if (st != MPMGPU_OK) return st;
+    cudaGraphExec_t gx = nullptr;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ms) {
+        BCK(cudaEventCreate(&e0));
+        BCK(cudaEventCreate(&e1));
+        BCK(cudaEventRecord(e0, b->stream));
+    }
+    for (int s = 0; s < nsteps; s++) {
+        const int with_sort = b->o.sort_interval > 0 && b->since_sort >= b->o.sort_interval;
+        st = batch_graph(b, with_sort, &gx);
+        if (st != MPMGPU_OK) return st;
+        BCK(cudaGraphLaunch(gx, b->stream));
+        b->launches += batch_step_launches(b) + (with_sort ? batch_sort_launches(b) : 0);
+        if (with_sort) {
+            b->par = 1 - b->par;
+            batch_link(b);
+            b->since_sort = 0;
+        }
+        b->since_sort++;
+        b->steps++;
+    }
+    if (ms) BCK(cudaEventRecord(e1, b->stream));
+    BCK(cudaMemcpyAsync(b->runs_host.data(), b->runs_dev, sizeof(DevRun) * b->runs_host.size(),
+                        cudaMemcpyDeviceToHost, b->stream));
+    BCK(cudaStreamSynchronize(b->stream));
+    if (ms) {
+        float f = 0.f;
+        cudaEventElapsedTime(&f, e0, e1);
+        *ms = f;
+        cudaEventDestroy(e0);
+        cudaEventDestroy(e1);
+    }
+    for (size_t r = 0; r < b->runs.size(); r++) {
+        BatchRun &br = b->runs[r];
+        if (!br.used || br.state != MPMGPU_RUN_RUNNING) continue;
+        const DevRun &R = b->runs_host[r];
+        br.steps_done = br.steps_total - R.steps_left;
+        if (R.err) br.state = -batch_status(R.err);
+        else if (!R.active) br.state = MPMGPU_RUN_FINISHED;
+    }
+    return MPMGPU_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *o) {
+    if (!o || o->max_particles <= 0 || o->max_nodes <= 0) return -1;
+    const int64_t P = o->max_particles, N = o->max_nodes;
+    const int64_t ntiles = (P + kTile - 1) / kTile;
+    int64_t bytes = 2 * P * (int64_t)((kParticleDoubles + 1) * sizeof(double) + kBatchIntCols * sizeof(int));
+    bytes += 4 * P * (int64_t)sizeof(int) + 2 * 256 * ntiles * (int64_t)sizeof(int);  // sort keys, histograms
+    bytes += N * (int64_t)(19 * sizeof(double) + 12 * sizeof(float) + 1 + 2 * sizeof(int) + sizeof(double));
+    bytes += (int64_t)o->max_materials * (int64_t)sizeof(DevMat) + (int64_t)o->max_runs * (int64_t)sizeof(DevRun);
+    return bytes;
+}
+
+int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
+    if (!o || !out) return berr(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_batch_create: null argument");
+    *out = nullptr;
+    if (o->np != MPMGPU_PLANE_STRAIN && o->np != MPMGPU_THREED)
+        return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "batch analysis type must be 2D plane strain or 3D");
+    if (o->shape != MPMGPU_SHAPE_LINEAR && o->shape != MPMGPU_SHAPE_UGIMP)
+        return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
+    if (o->method != MPMGPU_USF && o->method != MPMGPU_USAVG && o->method != MPMGPU_USL)
+        return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
+    if (o->precision != MPMGPU_PREC_FP64 && o->precision != MPMGPU_PREC_MIXED)
+        return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "precision must be MPMGPU_PREC_FP64 or MPMGPU_PREC_MIXED");
+    if (o->max_particles <= 0 || o->max_particles > (1LL << 31) - 1 || o->max_nodes <= 0 ||
+        o->max_nodes > (1LL << 30) || o->max_runs <= 0 || o->max_runs > (1 << 20) || o->max_materials <= 0 ||
+        o->max_materials > (1 << 24))
+        return berr(nullptr, MPMGPU_ERR_INVALID, "batch capacities out of range");
+    if (o->block != 0 && o->block != 64 && o->block != 128 && o->block != 256)
+        return berr(nullptr, MPMGPU_ERR_INVALID, "block must be 0, 64, 128 or 256");
+    MpmGpuBatch *b = new MpmGpuBatch();
+    b->o = *o;
+    if (!(b->o.fraction_usf > 0.)) b->o.fraction_usf = 0.5;
+    if (b->o.sort_interval < 0) b->o.sort_interval = 0;
+    b->tb = o->block ? o->block : 256;
+    b->dim = o->np == MPMGPU_THREED ? 3 : 2;
+    b->pcap = (int)o->max_particles;
+    b->ncap = (int)o->max_nodes;
+    const size_t P = (size_t)b->pcap, N = (size_t)b->ncap;
+    const size_t ntiles = (P + kTile - 1) / kTile;
+    const size_t nsums = (256 * ntiles + kScanChunk - 1) / kScanChunk + 1;
+    cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
+    auto A = [&](void **q, size_t bytes) {
+        if (e == cudaSuccess) e = cudaMalloc(q, bytes);
+    };
+    for (int k = 0; k < 2; k++) {
+        A((void **)&b->pbuf[k], P * (kParticleDoubles + 1) * sizeof(double));
+        A((void **)&b->ibuf[k], P * kBatchIntCols * sizeof(int));
+        A((void **)&b->keys[k], P * sizeof(int));
+        A((void **)&b->vals[k], P * sizeof(int));
+    }
+    A((void **)&b->nblock, N * 19 * sizeof(double) + N);
+    A((void **)&b->fblock, N * 12 * sizeof(float));
+    A((void **)&b->coords, N * sizeof(double));
+    A((void **)&b->nrun, N * sizeof(int));
+    A((void **)&b->bc_group, N * sizeof(int));
+    A((void **)&b->hist, 256 * ntiles * sizeof(int));
+    A((void **)&b->sums, nsums * sizeof(int));
+    A((void **)&b->mats, (size_t)o->max_materials * sizeof(DevMat));
+    A((void **)&b->runs_dev, (size_t)o->max_runs * sizeof(DevRun));
+    A((void **)&b->flag, sizeof(unsigned));
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->nblock, 0, N * 19 * sizeof(double) + N, b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->fblock, 0, N * 12 * sizeof(float), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->nrun, 0xFF, N * sizeof(int), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->bc_group, 0xFF, N * sizeof(int), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->runs_dev, 0, (size_t)o->max_runs * sizeof(DevRun), b->stream);
+    for (int k = 0; k < 2 && e == cudaSuccess; k++)
+        e = cudaMemsetAsync(b->pbuf[k], 0, P * (kParticleDoubles + 1) * sizeof(double), b->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+    if (e != cudaSuccess) {
+        std::string m = std::string("batch allocation: ") + cudaGetErrorString(e);
+        batch_free(b);
+        delete b;
+        return berr(nullptr, MPMGPU_ERR_OOM, m);
+    }
+    double *nb = b->nblock;
+    DevNodes &nd = b->nd;
+    double **dc[19] = {&nd.mass, &nd.px, &nd.py, &nd.pz, &nd.fx, &nd.fy, &nd.fz, &nd.ux, &nd.uy, &nd.uz,
+                       &nd.cx, &nd.cy, &nd.cz, &nd.vx, &nd.vy, &nd.vz, &nd.ax, &nd.ay, &nd.az};
+    for (int k = 0; k < 19; k++) *dc[k] = nb + (size_t)k * N;
+    nd.active = (unsigned char *)(nb + 19 * N);
+    float *fb = b->fblock;
+    float **fc[12] = {&nd.gx, &nd.gy, &nd.gz, &nd.vhx, &nd.vhy, &nd.vhz,
+                      &nd.vlx, &nd.vly, &nd.vlz, &nd.bx, &nd.by, &nd.bz};
+    for (int k = 0; k < 12; k++) *fc[k] = fb + (size_t)k * N;
+    batch_link(b);
+    b->nodes.init(b->ncap);
+    b->cells.init(b->ncap);  // every run has fewer cells than nodes
+    b->matslots.init(o->max_materials);
+    while ((1LL << b->sort_bits) <= (long long)b->ncap) b->sort_bits++;
+    b->runs.resize((size_t)o->max_runs);
+    b->runs_host.assign((size_t)o->max_runs, DevRun{});
+    *out = b;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
+                         const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuParticles *h, double timestep,
+                         int32_t nsteps, int32_t *run_id) {
+    if (!b || !grid || !mats || nmat <= 0 || !h || h->n <= 0 || (nbc > 0 && !bcs) || nbc < 0 || !run_id ||
+        nsteps <= 0 || !(timestep > 0.))
+        return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_add_run: bad argument");
+    if (grid->dim != b->dim) return berr(b, MPMGPU_ERR_INVALID, "run dimension differs from the batch");
+    if (grid->nx < 3 || grid->ny < 3 || (grid->dim == 3 && grid->nz < 3) || !grid->xnodes || !grid->ynodes ||
+        (grid->dim == 3 && !grid->znodes))
+        return berr(b, MPMGPU_ERR_INVALID, "grid needs >= 3 elements per axis and node coordinates");
+    if (!h->x || !h->y || !h->vx || !h->vy || !h->mass || !h->mat || !h->elem || !h->lpx || !h->lpy ||
+        (b->dim == 3 && (!h->z || !h->vz || !h->lpz)))
+        return berr(b, MPMGPU_ERR_INVALID,
+                    "position, velocity, mass, size, material and element columns are required");
+    const long long nnodes = (long long)(grid->nx + 1) * (grid->ny + 1) * (b->dim == 3 ? grid->nz + 1 : 1);
+    const long long nelems = (long long)grid->nx * grid->ny * (b->dim == 3 ? grid->nz : 1);
+    if (h->n > b->pcap) return berr(b, MPMGPU_ERR_INVALID, "run has more particles than the batch capacity");
+    if (nnodes > b->ncap) return berr(b, MPMGPU_ERR_INVALID, "run has more nodes than the batch capacity");
+    const int np = (int)h->n;
+    for (int k = 0; k < nbc; k++) {
+        if (bcs[k].node < 1 || bcs[k].node > nnodes)
+            return berr(b, MPMGPU_ERR_INVALID, "velocity BC node out of range");
+        if (bcs[k].dir != 1 && bcs[k].dir != 2 && bcs[k].dir != 4)
+            return berr(b, MPMGPU_ERR_UNSUPPORTED, "velocity BC dir must be 1, 2 or 4");
+        if (bcs[k].dir == 4 && b->dim == 2) return berr(b, MPMGPU_ERR_INVALID, "z velocity BC in 2D");
+    }
+    std::vector<DevMat> dm((size_t)nmat);
+    for (int i = 0; i < nmat; i++) {
+        std::string why;
+        const int st = derive_material(mats[i], b->o.np, dm[i], why);
+        if (st != MPMGPU_OK) return berr(b, st, "material " + std::to_string(i) + ": " + why);
+    }
+    int r = -1;
+    for (int k = 0; k < (int)b->runs.size() && r < 0; k++)
+        if (!b->runs[k].used) r = k;
+    if (r < 0) return berr(b, MPMGPU_ERR_BUSY, "no free run slot");
+    if ((long long)b->n_used + np > b->pcap && b->n_dead > 0) {
+        const int st = batch_compact(b);
+        if (st != MPMGPU_OK) return st;
+    }
+    if ((long long)b->n_used + np > b->pcap) return berr(b, MPMGPU_ERR_BUSY, "particle capacity is in use");
+    const long long nbase = b->nodes.alloc(nnodes);
+    if (nbase < 0) return berr(b, MPMGPU_ERR_BUSY, "node capacity is in use");
+    const long long cbase = b->cells.alloc(nelems);
+    const long long mbase = cbase >= 0 ? b->matslots.alloc(nmat) : -1;
+    if (cbase < 0 || mbase < 0) {
+        b->nodes.release(nbase, nnodes);
+        if (cbase >= 0) b->cells.release(cbase, nelems);
+        return berr(b, MPMGPU_ERR_BUSY, "cell or material capacity is in use");
+    }
+    cudaStream_t s = b->stream;
+    // node coordinates at the run's node base (a run has more nodes than coordinates)
+    double *xn = b->coords + nbase, *yn = xn + grid->nx + 1, *zn = yn + grid->ny + 1;
+    BCK(cudaMemcpyAsync(xn, grid->xnodes, sizeof(double) * (grid->nx + 1), cudaMemcpyHostToDevice, s));
+    BCK(cudaMemcpyAsync(yn, grid->ynodes, sizeof(double) * (grid->ny + 1), cudaMemcpyHostToDevice, s));
+    if (b->dim == 3)
+        BCK(cudaMemcpyAsync(zn, grid->znodes, sizeof(double) * (grid->nz + 1), cudaMemcpyHostToDevice, s));
+    BCK(cudaMemcpyAsync(b->mats + mbase, dm.data(), sizeof(DevMat) * nmat, cudaMemcpyHostToDevice, s));
+    // particles after the used slots
+    const int start = b->n_used;
+    double *hc[kParticleDoubles];
+    hcols(h, hc);
+    double *pb = b->pbuf[b->par];
+    for (int k = 0; k < kParticleDoubles; k++) {
+        double *dst = pb + (size_t)k * b->pcap + start;
+        if (hc[k]) BCK(cudaMemcpyAsync(dst, hc[k], sizeof(double) * np, cudaMemcpyHostToDevice, s));
+        else BCK(cudaMemsetAsync(dst, 0, sizeof(double) * np, s));
+    }
+    BCK(cudaMemcpyAsync(b->p.mat + start, h->mat, sizeof(int) * np, cudaMemcpyHostToDevice, s));
+    BCK(cudaMemcpyAsync(b->p.elem + start, h->elem, sizeof(int) * np, cudaMemcpyHostToDevice, s));
+    BCK(cudaMemsetAsync(b->flag, 0, sizeof(unsigned), s));
+    const int TB = 256;
+    k_batch_admit<<<(np + TB - 1) / TB, TB, 0, s>>>(b->p.mat, b->p.elem, b->orig, b->p.run, start, np, r,
+                                                    (int)mbase, nmat, (int)nelems, b->flag);
+    k_fill_int<<<(int)((nnodes + TB - 1) / TB), TB, 0, s>>>(b->nrun, nbase, nnodes, r);
+    b->launches += 2;
+    BCK(cudaGetLastError());
+    DevRun R{};
+    R.g.dim = b->dim;
+    R.g.nx = grid->nx;
+    R.g.ny = grid->ny;
+    R.g.nz = b->dim == 3 ? grid->nz : 0;
+    R.g.xplane = 1;
+    R.g.yplane = grid->nx + 1;
+    R.g.zplane = (grid->nx + 1) * (grid->ny + 1);
+    R.g.nnodes = (int)nnodes;
+    R.g.xmin = grid->xmin;
+    R.g.ymin = grid->ymin;
+    R.g.zmin = grid->zmin;
+    R.g.gx = grid->dx;
+    R.g.gy = grid->dy;
+    R.g.gz = grid->dz;
+    R.g.xn = xn;
+    R.g.yn = yn;
+    R.g.zn = b->dim == 3 ? zn : nullptr;
+    R.node_base = (int)nbase;
+    R.cell_base = (int)cbase;
+    R.active = 1;
+    R.steps_left = nsteps;
+    R.dt = timestep;
+    R.st_first = b->o.method == MPMGPU_USAVG ? b->o.fraction_usf * timestep : timestep;
+    R.st_last = b->o.method == MPMGPU_USAVG ? timestep - R.st_first : timestep;
+    R.t = 0.;
+    R.err = 0;
+    BCK(cudaMemcpyAsync(b->runs_dev + r, &R, sizeof(DevRun), cudaMemcpyHostToDevice, s));
+    unsigned bad = 0;
+    BCK(cudaMemcpyAsync(&bad, b->flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));
+    BCK(cudaStreamSynchronize(s));
+    BatchRun &br = b->runs[r];
+    br = BatchRun{};
+    br.used = true;
+    br.np = np;
+    br.node_base = nbase;
+    br.nnodes = nnodes;
+    br.cell_base = cbase;
+    br.nelems = nelems;
+    br.mat_base = mbase;
+    br.nmat = nmat;
+    br.steps_total = nsteps;
+    br.state = MPMGPU_RUN_RUNNING;
+    br.bcs.reserve((size_t)nbc);
+    for (int k = 0; k < nbc; k++) {
+        MpmGpuVelBC bc = bcs[k];
+        bc.node += (int)nbase;
+        br.bcs.push_back(bc);
+    }
+    b->runs_host[r] = R;
+    b->n_used += np;
+    b->p.n = b->n_used;
+    b->node_used = (int)b->nodes.high_water();
+    b->bcs_dirty = true;
+    b->layout++;
+    b->since_sort = 1LL << 40;  // new slots are unsorted
+    if (bad) {
+        mpmgpu_batch_remove_run(b, r, nullptr);
+        return berr(b, MPMGPU_ERR_INVALID, "particle material or element index out of range");
+    }
+    *run_id = r;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_batch_step(MpmGpuBatch *b, int32_t nsteps) {
+    if (!b || nsteps < 0) return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_step: bad argument");
+    return batch_steps(b, nsteps, nullptr);
+}
+
+int mpmgpu_batch_step_timed(MpmGpuBatch *b, int32_t nsteps, double *ms) {
+    if (!b || nsteps < 0 || !ms) return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_step_timed: bad argument");
+    return batch_steps(b, nsteps, ms);
+}
+
+int mpmgpu_batch_run_state(const MpmGpuBatch *b, int32_t run_id, int32_t *state, int32_t *steps_done) {
+    if (!b || run_id < 0 || run_id >= (int)b->runs.size()) return MPMGPU_ERR_INVALID;
+    const BatchRun &br = b->runs[run_id];
+    if (state) *state = br.used ? br.state : MPMGPU_RUN_EMPTY;
+    if (steps_done) *steps_done = br.used ? br.steps_done : 0;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_batch_download_run(MpmGpuBatch *b, int32_t run_id, MpmGpuParticles *out) {
+    if (!b || !out || run_id < 0 || run_id >= (int)b->runs.size() || !b->runs[run_id].used)
+        return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_download_run: bad run");
+    const BatchRun &br = b->runs[run_id];
+    if (out->n != br.np) return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_download_run: particle count mismatch");
+    cudaStream_t s = b->stream;
+    const int TB = 256, n = b->n_used;
+    // the other arena buffer is free between steps: pack the run there
+    double *packed = b->pbuf[1 - b->par];
+    int *ipacked = b->ibuf[1 - b->par];
+    if (n > 0) {
+        k_batch_extract<<<(n + TB - 1) / TB, TB, 0, s>>>(b->pbuf[b->par], b->pcap, b->p.mat, b->p.elem, b->orig,
+                                                         b->p.run, n, run_id, (int)br.mat_base, packed, ipacked,
+                                                         br.np, kParticleDoubles);
+        b->launches++;
+        BCK(cudaGetLastError());
+    }
+    double *hc[kParticleDoubles];
+    hcols(out, hc);
+    for (int k = 0; k < kParticleDoubles; k++)
+        if (hc[k])
+            BCK(cudaMemcpyAsync(hc[k], packed + (size_t)k * br.np, sizeof(double) * br.np, cudaMemcpyDeviceToHost,
+                                s));
+    if (out->mat) BCK(cudaMemcpyAsync(out->mat, ipacked, sizeof(int) * br.np, cudaMemcpyDeviceToHost, s));
+    if (out->elem) BCK(cudaMemcpyAsync(out->elem, ipacked + br.np, sizeof(int) * br.np, cudaMemcpyDeviceToHost, s));
+    BCK(cudaStreamSynchronize(s));
+    return MPMGPU_OK;
+}
+
+int mpmgpu_batch_remove_run(MpmGpuBatch *b, int32_t run_id, MpmGpuParticles *out) {
+    if (!b || run_id < 0 || run_id >= (int)b->runs.size() || !b->runs[run_id].used)
+        return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_remove_run: bad run");
+    BatchRun &br = b->runs[run_id];
+    if (out) {
+        const int st = mpmgpu_batch_download_run(b, run_id, out);
+        if (st != MPMGPU_OK) return st;
+    }
+    cudaStream_t s = b->stream;
+    const int TB = 256, n = b->n_used;
+    if (n > 0) k_batch_kill<<<(n + TB - 1) / TB, TB, 0, s>>>(b->p.run, n, run_id);
+    k_fill_int<<<(int)((br.nnodes + TB - 1) / TB), TB, 0, s>>>(b->nrun, br.node_base, br.nnodes, -1);
+    b->launches += 2;
+    BCK(cudaGetLastError());
+    DevRun R{};
+    b->runs_host[run_id] = R;
+    BCK(cudaMemcpyAsync(b->runs_dev + run_id, &R, sizeof(DevRun), cudaMemcpyHostToDevice, s));
+    BCK(cudaStreamSynchronize(s));
+    b->n_dead += br.np;
+    b->nodes.release(br.node_base, br.nnodes);
+    b->cells.release(br.cell_base, br.nelems);
+    b->matslots.release(br.mat_base, br.nmat);
+    b->node_used = (int)b->nodes.high_water();
+    br = BatchRun{};
+    b->bcs_dirty = true;
+    b->layout++;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_batch_set_tuning(MpmGpuBatch *b, int32_t block, int32_t sort_interval) {
+    if (!b || (block != 64 && block != 128 && block != 256) || sort_interval < 0)
+        return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_set_tuning: block must be 64, 128 or 256");
+    b->tb = block;
+    b->o.sort_interval = sort_interval;
+    return MPMGPU_OK;
+}
+
+// Pick the particle-kernel block size and the sort interval by timing real
+// steps of the current runs: each candidate runs `trial_steps` steps (rounded
+// up to a multiple of 8, starting from a fresh sort) after one untimed step
+// that captures its graphs.  The trial steps advance the runs like any other
+// steps.  Results: the chosen block and interval (also set on the batch).
+int mpmgpu_batch_autotune(MpmGpuBatch *b, int32_t trial_steps, int32_t *block, int32_t *sort_interval,
+                          double *ms_per_step) {
+    if (!b || trial_steps <= 0) return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_autotune: bad argument");
+    const int steps = (trial_steps + 7) / 8 * 8;
+    const int blocks[] = {128, 256};
+    const int intervals[] = {1, 2, 4, 8};
+    double best = 1e300;
+    int best_tb = b->tb, best_si = b->o.sort_interval;
+    for (int tb : blocks)
+        for (int si : intervals) {
+            if (!batch_active_runs(b)) break;
+            b->tb = tb;
+            b->o.sort_interval = si;
+            b->since_sort = 1LL << 40;
+            int st = batch_steps(b, 1, nullptr);  // captures the graphs of this candidate
+            if (st != MPMGPU_OK) return st;
+            b->since_sort = 1LL << 40;
+            double ms = 0.;
+            st = batch_steps(b, steps, &ms);
+            if (st != MPMGPU_OK) return st;
+            if (ms > 0. && ms / steps < best) {
+                best = ms / steps;
+                best_tb = tb;
+                best_si = si;
+            }
+        }
+    b->tb = best_tb;
+    b->o.sort_interval = best_si;
+    if (block) *block = best_tb;
+    if (sort_interval) *sort_interval = best_si;
+    if (ms_per_step) *ms_per_step = best < 1e300 ? best : 0.;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_batch_info(const MpmGpuBatch *b, MpmGpuBatchInfo *info) {
+    if (!b || !info) return MPMGPU_ERR_INVALID;
+    info->runs = 0;
+    info->running = 0;
+    for (const auto &r : b->runs) {
+        info->runs += r.used;
+        info->running += r.used && r.state == MPMGPU_RUN_RUNNING;
+    }
+    info->particles_used = b->n_used;
+    info->particles_dead = b->n_dead;
+    info->nodes_used = b->node_used;
+    info->block = b->tb;
+    info->sort_interval = b->o.sort_interval;
+    info->steps = b->steps;
+    info->launches = b->launches;
+    return MPMGPU_OK;
+}
+
+const char *mpmgpu_batch_last_error(const MpmGpuBatch *b) { return b ? b->msg.c_str() : g_static_err.c_str(); }
+
+void *mpmgpu_batch_stream(MpmGpuBatch *b) { return b ? (void *)b->stream : nullptr; }
+
+void mpmgpu_batch_destroy(MpmGpuBatch *b) {
+    if (!b) return;
+    cudaStreamSynchronize(b->stream);
+    batch_free(b);
+    delete b;
+}
+
+}  // extern "C"

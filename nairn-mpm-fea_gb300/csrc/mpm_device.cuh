@@ -42,6 +42,7 @@ struct DevParticles {
     double *pxx, *pyy, *pzz, *pxy, *pxz, *pyz;
     double *hist0, *hist1, *work, *plast;
     double *xi, *eta, *zeta;   // natural coordinates of the step (ncpos)
+    int *run;                  // run of each slot in a batch (-1: empty); unused for one run
 };
 
 struct DevNodes {
@@ -58,6 +59,29 @@ struct DevNodes {
     float *vlx, *vly, *vlz;
     float *gx, *gy, *gz;       // FP32 force accumulators
     float *bx, *by, *bz;       // FP32 acceleration for the particle update
+};
+
+// One run of a batch: its grid, where its nodes and cells start in the
+// batch's node and cell arenas, and its own time stepping.
+struct DevRun {
+    DevGrid g;
+    int node_base;     // first global node of the run
+    int cell_base;     // first global cell (offset of the run's sort keys)
+    int active;        // the run advances while active
+    int steps_left;    // steps still to take (the run deactivates at zero)
+    double dt, st_first, st_last, t;
+    unsigned err;      // error bits of this run
+};
+
+// Per-launch step parameters.  A single-run context uses g, dt, st_first,
+// st_last, t and err directly; a batch (BATCH = true in the kernels) reads the
+// run of each particle (DevParticles::run) or node (nrun) from `runs`.
+struct StepParams {
+    DevGrid g;
+    double dt, st_first, st_last, t;
+    unsigned *err;
+    DevRun *runs;
+    const int *nrun;   // run of each node (-1: unused)
 };
 
 // Velocity conditions grouped by node, list order kept inside a node.

@@ -498,34 +498,43 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     cudaMemsetAsync(c->nblock, 0, c->nblock_zero_bytes, s);
     cudaMemsetAsync(c->nd.active, 0, (size_t)NN, s);
     if (MIX) cudaMemsetAsync(c->fblock, 0, c->fblock_zero_bytes, s);
+    StepParams sp;
+    sp.g = c->g;
+    sp.dt = dt;
+    sp.st_first = stFirst;
+    sp.st_last = stLast;
+    sp.t = t;
+    sp.err = c->err;
+    sp.runs = nullptr;
+    sp.nrun = nullptr;
     mark(0, true);
-    k_p2g<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd);
+    k_p2g<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
     mark(0, false);
     mark(1, true);
-    k_node_post<DIM, MIX><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL, t, dt);
+    k_node_post<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL);
     mark(1, false);
     mark(2, true);
     if (method == MPMGPU_USL)
-        k_strain_forces<DIM, SHAPE, false, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stFirst);
+        k_strain_forces<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     else
-        k_strain_forces<DIM, SHAPE, true, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stFirst);
+        k_strain_forces<DIM, SHAPE, true, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     mark(2, false);
     mark(3, true);
-    k_node_update<DIM, MIX><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, t, dt);
+    k_node_update<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
     mark(3, false);
     mark(4, true);
     if (method == MPMGPU_USF) {
-        k_g2p<DIM, SHAPE, false, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, dt, c->err);
+        k_g2p<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
         mark(4, false);
         return;
     }
-    k_g2p<DIM, SHAPE, true, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, dt, c->err);
+    k_g2p<DIM, SHAPE, true, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
     mark(4, false);
     mark(5, true);
-    k_node_usl<DIM, MIX><<<nb, TB, 0, s>>>(c->nd, NN, c->bcs, c->bc_group, t, dt);
+    k_node_usl<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
     mark(5, false);
     mark(6, true);
-    k_strain_last<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(c->g, c->p, c->nd, c->mats, stLast, c->err);
+    k_strain_last<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     mark(6, false);
 }
 
@@ -815,3 +824,5 @@ int mpmgpu_host_unregister(void *ptr) {
 }
 
 }  // extern "C"
+
+#include "batch.cuh"

@@ -25,11 +25,11 @@ enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1 };
 // of the weights: double in the FP64 path, float in the mixed-precision mode
 // (natural coordinates are formed in FP64 and rounded once).
 template <int DIM, int SHAPE, bool GRAD, typename T, class F>
-__device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi_d, double eta_d, double zeta_d,
-                                              double lpx_d, double lpy_d, double lpz_d, F &&f) {
+__device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, double xi_d, double eta_d,
+                                              double zeta_d, double lpx_d, double lpy_d, double lpz_d, F &&f) {
     int col, row, zr;
     elem_coords(g, e, col, row, zr);
-    const int n0 = zr * g.zplane + row * g.yplane + col;  // 0-based first node
+    const int n0 = nb + zr * g.zplane + row * g.yplane + col;  // first node (global index)
     const T DX = (T)(g.xn[col + 1] - g.xn[col]);
     const T DY = (T)(g.yn[row + 1] - g.yn[row]);
     const T DZ = DIM == 3 ? (T)(g.zn[zr + 1] - g.zn[zr]) : T(1);
@@ -122,6 +122,38 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int e, double xi
 // particle kernels
 // ---------------------------------------------------------------------------
 
+// The run a particle belongs to: its grid, node base and time stepping.
+struct RunView {
+    DevGrid g;
+    int nb;
+    double dt, st_first, st_last;
+    unsigned *err;
+};
+
+template <bool BATCH>
+__device__ __forceinline__ bool particle_run(const StepParams &sp, const DevParticles &p, int i, RunView &rv) {
+    if (!BATCH) {
+        rv.g = sp.g;
+        rv.nb = 0;
+        rv.dt = sp.dt;
+        rv.st_first = sp.st_first;
+        rv.st_last = sp.st_last;
+        rv.err = sp.err;
+        return true;
+    }
+    const int r = p.run[i];
+    if (r < 0) return false;
+    DevRun &R = sp.runs[r];
+    if (!R.active) return false;
+    rv.g = R.g;
+    rv.nb = R.node_base;
+    rv.dt = R.dt;
+    rv.st_first = R.st_first;
+    rv.st_last = R.st_last;
+    rv.err = &R.err;
+    return true;
+}
+
 // Weight arithmetic of each transfer mode.
 template <bool MIX>
 struct Wt {
@@ -137,11 +169,14 @@ struct Wt<true> {
 // (MassAndMomentumTask.cpp:48-127, NodalPointMPM.cpp:419-453).  Momentum and
 // mass accumulate in FP64 in both modes: grid velocities carry the bulk motion
 // and their differences across a cell are the strain rate.
-template <int DIM, int SHAPE, bool MIX>
-__global__ void __launch_bounds__(256) k_p2g(DevGrid g, DevParticles p, DevNodes nd) {
+template <int DIM, int SHAPE, bool MIX, bool BATCH>
+__global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevNodes nd) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    RunView rv;
+    if (!particle_run<BATCH>(sp, p, i, rv)) return;
+    const DevGrid &g = rv.g;
     const int e = p.elem[i];
     const double x = p.x[i], y = p.y[i], z = DIM == 3 ? p.z[i] : 0.;
     double xi, eta, zeta;
@@ -151,7 +186,7 @@ __global__ void __launch_bounds__(256) k_p2g(DevGrid g, DevParticles p, DevNodes
     if (DIM == 3) p.zeta[i] = zeta;
     const double mp = p.mass[i];
     const double vx = p.vx[i], vy = p.vy[i], vz = DIM == 3 ? p.vz[i] : 0.;
-    for_each_node<DIM, SHAPE, false, T>(g, e, xi, eta, zeta, p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1.,
+    for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1.,
                                         [&](int n, T N, T, T, T) {
                                             if (N == T(0)) return;
                                             const double fnmp = (double)N * mp;
@@ -183,8 +218,8 @@ __device__ __forceinline__ void constitutive(const DevMat *mats, const DevPartic
 // exactly from FP32 hi/lo pairs of both velocities, so the bulk motion cancels
 // before any rounding.
 template <int DIM, int SHAPE, bool MIX>
-__device__ __forceinline__ void velocity_gradient(const DevGrid &g, const DevParticles &p, const DevNodes &nd, int i,
-                                                  double st, double du[9]) {
+__device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, const DevParticles &p, const DevNodes &nd,
+                                                  int i, double st, double du[9]) {
     using T = typename Wt<MIX>::T;
     T d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float ph[3] = {0.f, 0.f, 0.f}, pl[3] = {0.f, 0.f, 0.f};
@@ -193,8 +228,8 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, const DevPar
         split2(p.vy[i], ph[1], pl[1]);
         if (DIM == 3) split2(p.vz[i], ph[2], pl[2]);
     }
-    for_each_node<DIM, SHAPE, true, T>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
-                                       DIM == 3 ? p.lpz[i] : 1., [&](int n, T N, T dx, T dy, T dz) {
+    for_each_node<DIM, SHAPE, true, T>(g, nb, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
+                                       p.lpy[i], DIM == 3 ? p.lpz[i] : 1., [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
                                            T vx, vy, vz = 0;
                                            if (MIX) {
@@ -226,15 +261,17 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, const DevPar
 // fused with GridForcesTask::Execute and MatPoint2D/3D::GetFintPlusFext
 // (GridForcesTask.cpp:40-153, MatPoint2D.cpp:242-262, MatPoint3D.cpp:248-269).
 // Mixed mode: internal-force products in FP32 into FP32 accumulators.
-template <int DIM, int SHAPE, bool STRAIN, bool MIX>
-__global__ void __launch_bounds__(256) k_strain_forces(DevGrid g, DevParticles p, DevNodes nd, const DevMat *mats,
-                                                       double st) {
+template <int DIM, int SHAPE, bool STRAIN, bool MIX, bool BATCH>
+__global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    RunView rv;
+    if (!particle_run<BATCH>(sp, p, i, rv)) return;
+    const DevGrid &g = rv.g;
     if (STRAIN) {
         double du[9];
-        velocity_gradient<DIM, SHAPE, MIX>(g, p, nd, i, st, du);
+        velocity_gradient<DIM, SHAPE, MIX>(g, rv.nb, p, nd, i, rv.st_first, du);
         constitutive<DIM>(mats, p, i, du);
     }
     // -mp * (sigma - P I): the internal force of GetFintPlusFext, scaled once
@@ -242,8 +279,8 @@ __global__ void __launch_bounds__(256) k_strain_forces(DevGrid g, DevParticles p
     const T sxx = (T)(-mp * (p.sxx[i] - P)), syy = (T)(-mp * (p.syy[i] - P)), sxy = (T)(-mp * p.sxy[i]);
     const T szz = DIM == 3 ? (T)(-mp * (p.szz[i] - P)) : T(0), sxz = DIM == 3 ? (T)(-mp * p.sxz[i]) : T(0),
             syz = DIM == 3 ? (T)(-mp * p.syz[i]) : T(0);
-    for_each_node<DIM, SHAPE, true, T>(g, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
-                                       DIM == 3 ? p.lpz[i] : 1., [&](int n, T N, T dx, T dy, T dz) {
+    for_each_node<DIM, SHAPE, true, T>(g, rv.nb, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
+                                       p.lpy[i], DIM == 3 ? p.lpz[i] : 1., [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
                                            T fx, fy, fz = 0;
                                            if (DIM == 2) {
@@ -331,11 +368,15 @@ __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticl
 // same natural coordinates of the step.  Mixed mode: S v is formed as
 // v_particle + sum N (v_node - v_particle) (the weights sum to one) with the
 // differences from FP32 pairs, S a in FP32; the update itself is FP64.
-template <int DIM, int SHAPE, bool USL, bool MIX>
-__global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes nd, double dt, unsigned *err) {
+template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH>
+__global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevNodes nd) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    RunView rv;
+    if (!particle_run<BATCH>(sp, p, i, rv)) return;
+    const DevGrid &g = rv.g;
+    const double dt = rv.dt;
     T Sv[3] = {0, 0, 0}, Sa[3] = {0, 0, 0};
     const int e = p.elem[i];
     const double xi = p.xi[i], eta = p.eta[i], zeta = DIM == 3 ? p.zeta[i] : 0.;
@@ -346,7 +387,7 @@ __global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes
 #pragma unroll
         for (int a = 0; a < DIM; a++) split2(v[a], ph[a], pl[a]);
     }
-    for_each_node<DIM, SHAPE, false, T>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, T N, T, T, T) {
+    for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, [&](int n, T N, T, T, T) {
         if (N == T(0)) return;
         if (MIX) {
             Sv[0] += ((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0])) * N;
@@ -384,7 +425,7 @@ __global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes
     }
     if (USL) {
         const double mp = p.mass[i];
-        for_each_node<DIM, SHAPE, false, T>(g, e, xi, eta, zeta, lx, ly, lz, [&](int n, T N, T, T, T) {
+        for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, [&](int n, T N, T, T, T) {
             if (N == T(0)) return;
             const double fnmp = (double)N * mp;
             atomicAdd(&nd.ux[n], v[0] * fnmp);
@@ -392,21 +433,22 @@ __global__ void __launch_bounds__(256) k_g2p(DevGrid g, DevParticles p, DevNodes
             if (DIM == 3) atomicAdd(&nd.uz[n], v[2] * fnmp);
         });
     } else {
-        reset_element<DIM>(g, p, i, err);
+        reset_element<DIM>(g, p, i, rv.err);
     }
 }
 
 // UpdateStrainsFirstTask::FullStrainUpdate called from
 // UpdateStrainsLastContactTask (:149), fused with ResetElementsTask.
-template <int DIM, int SHAPE, bool MIX>
-__global__ void __launch_bounds__(256) k_strain_last(DevGrid g, DevParticles p, DevNodes nd, const DevMat *mats,
-                                                     double st, unsigned *err) {
+template <int DIM, int SHAPE, bool MIX, bool BATCH>
+__global__ void __launch_bounds__(256) k_strain_last(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    RunView rv;
+    if (!particle_run<BATCH>(sp, p, i, rv)) return;
     double du[9];
-    velocity_gradient<DIM, SHAPE, MIX>(g, p, nd, i, st, du);
+    velocity_gradient<DIM, SHAPE, MIX>(rv.g, rv.nb, p, nd, i, rv.st_last, du);
     constitutive<DIM>(mats, p, i, du);
-    reset_element<DIM>(g, p, i, err);
+    reset_element<DIM>(rv.g, p, i, rv.err);
 }
 
 // ---------------------------------------------------------------------------
@@ -481,11 +523,29 @@ __device__ __forceinline__ void node_velocity(const DevNodes &nd, int n, double 
 
 // PostExtrapolationTask::Execute (PostExtrapolationTask.cpp:46-165):
 // vk[pkCopy] = pk, velocity conditions of MASS_MOMENTUM_CALL, then grid velocity.
-template <int DIM, bool MIX>
-__global__ void k_node_post(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, int do_bcs, double t,
-                            double dt) {
+// time and time step of the run a node belongs to
+template <bool BATCH>
+__device__ __forceinline__ bool node_run(const StepParams &sp, int n, double &t, double &dt) {
+    if (!BATCH) {
+        t = sp.t;
+        dt = sp.dt;
+        return true;
+    }
+    const int r = sp.nrun[n];
+    if (r < 0) return false;
+    const DevRun &R = sp.runs[r];
+    if (!R.active) return false;
+    t = R.t;
+    dt = R.dt;
+    return true;
+}
+
+template <int DIM, bool MIX, bool BATCH>
+__global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group, int do_bcs) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !nd.active[n]) return;
+    double t, dt;
+    if (!node_run<BATCH>(sp, n, t, dt)) return;
     double p[3] = {nd.px[n], nd.py[n], DIM == 3 ? nd.pz[n] : 0.};
     nd.cx[n] = p[0];
     nd.cy[n] = p[1];
@@ -506,10 +566,12 @@ __global__ void k_node_post(DevNodes nd, int nnodes, DevBCs b, const int *bc_gro
 // conditions; PostForcesTask.cpp:43-111) and UpdateMomentaTask::Execute
 // (p += f dt, UPDATE_MOMENTUM_CALL conditions; UpdateMomentaTask.cpp:44-94),
 // then grid velocity for the particle update.
-template <int DIM, bool MIX>
-__global__ void k_node_update(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, double t, double dt) {
+template <int DIM, bool MIX, bool BATCH>
+__global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !nd.active[n]) return;
+    double t, dt;
+    if (!node_run<BATCH>(sp, n, t, dt)) return;
     double p[3] = {nd.cx[n], nd.cy[n], DIM == 3 ? nd.cz[n] : 0.};
     double f[3];
     if (MIX) {
@@ -550,10 +612,12 @@ __global__ void k_node_update(DevNodes nd, int nnodes, DevBCs b, const int *bc_g
 
 // UpdateStrainsLastContactTask: p = second extrapolation, UPDATE_STRAINS_LAST_CALL
 // conditions, grid velocity (UpdateStrainsLastContactTask.cpp:60-152).
-template <int DIM, bool MIX>
-__global__ void k_node_usl(DevNodes nd, int nnodes, DevBCs b, const int *bc_group, double t, double dt) {
+template <int DIM, bool MIX, bool BATCH>
+__global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !nd.active[n]) return;
+    double t, dt;
+    if (!node_run<BATCH>(sp, n, t, dt)) return;
     double p[3] = {nd.ux[n], nd.uy[n], DIM == 3 ? nd.uz[n] : 0.};
     const double m = nd.mass[n];
     const int grp = bc_group[n];
@@ -565,6 +629,22 @@ __global__ void k_node_usl(DevNodes nd, int nnodes, DevBCs b, const int *bc_grou
     nd.py[n] = p[1];
     if (DIM == 3) nd.pz[n] = p[2];
     node_velocity<MIX>(nd, n, m, p);
+}
+
+// End of a batched step: advance the time of every active run and retire
+// runs that have taken all their steps.  A run that raised an error stops
+// here, so the error stays confined to its own particles and nodes.
+__global__ void k_advance_runs(DevRun *runs, int nruns) {
+    const int r = blockIdx.x * blockDim.x + threadIdx.x;
+    if (r >= nruns) return;
+    DevRun &R = runs[r];
+    if (!R.active) return;
+    if (R.err) {
+        R.active = 0;
+        return;
+    }
+    R.t += R.dt;
+    if (--R.steps_left <= 0) R.active = 0;
 }
 
 }  // namespace nmg

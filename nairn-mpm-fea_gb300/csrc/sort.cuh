@@ -248,12 +248,10 @@ void relink_particles(DevParticles &p, double *pblock, int *iblock, int **orig);
 // keys/vals/hist/sums are caller-provided scratch: keys[2], vals[2] of n ints,
 // hist of 256*ntiles ints, sums of ceil(256*ntiles/kScanChunk) ints.  Returns
 // the buffer index (0 or 1) that holds the sorted keys and the permutation.
-inline int radix_sort_keys(const int *elem, int n, int bits, int *keys[2], int *vals[2], int *hist, int *sums,
-                           cudaStream_t s) {
-    const int TB = 256;
-    const int pb = (n + TB - 1) / TB;
+// LSD passes over keys[0]/vals[0] already filled; returns the buffer index
+// (0 or 1) that holds the sorted keys and the permutation.
+inline int radix_sort_passes(int n, int bits, int *keys[2], int *vals[2], int *hist, int *sums, cudaStream_t s) {
     const int ntiles = (n + kTile - 1) / kTile;
-    k_sort_init<<<pb, TB, 0, s>>>(elem, keys[0], vals[0], n);
     int cur = 0;
     const int tb = (ntiles + kSortWarpsPerBlock - 1) / kSortWarpsPerBlock;
     const int m = 256 * ntiles;
@@ -268,6 +266,17 @@ inline int radix_sort_keys(const int *elem, int n, int bits, int *keys[2], int *
         cur = 1 - cur;
     }
     return cur;
+}
+
+// Stable LSD radix sort of n keys (0 <= key < 2^bits) carrying their slot index.
+// keys/vals/hist/sums are caller-provided scratch: keys[2], vals[2] of n ints,
+// hist of 256*ntiles ints, sums of ceil(256*ntiles/kScanChunk) ints.  Returns
+// the buffer index (0 or 1) that holds the sorted keys and the permutation.
+inline int radix_sort_keys(const int *elem, int n, int bits, int *keys[2], int *vals[2], int *hist, int *sums,
+                           cudaStream_t s) {
+    const int TB = 256;
+    k_sort_init<<<(n + TB - 1) / TB, TB, 0, s>>>(elem, keys[0], vals[0], n);
+    return radix_sort_passes(n, bits, keys, vals, hist, sums, s);
 }
 
 inline int sort_particles(SortWorkspace &w, DevParticles &p, double *&pblock, int *&iblock, int *&orig, int ncols,

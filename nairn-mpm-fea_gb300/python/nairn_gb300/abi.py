@@ -129,3 +129,19 @@ def copy_particles(p: dict) -> dict:
 
 def empty_like_particles(p: dict) -> dict:
     return {k: np.zeros_like(v) for k, v in p.items()}
+
+
+class MpmGpuBatchOptions(C.Structure):
+    _fields_ = [("np", C.c_int32), ("method", C.c_int32), ("shape", C.c_int32), ("precision", C.c_int32),
+                ("sort_interval", C.c_int32), ("block", C.c_int32), ("max_runs", C.c_int32),
+                ("max_materials", C.c_int32), ("max_particles", C.c_int64), ("max_nodes", C.c_int64),
+                ("fraction_usf", C.c_double)]
+
+
+class MpmGpuBatchInfo(C.Structure):
+    _fields_ = [("runs", C.c_int32), ("running", C.c_int32), ("block", C.c_int32), ("sort_interval", C.c_int32),
+                ("particles_used", C.c_int64), ("particles_dead", C.c_int64), ("nodes_used", C.c_int64),
+                ("steps", C.c_int64), ("launches", C.c_int64)]
+
+
+RUN_EMPTY, RUN_RUNNING, RUN_FINISHED = 0, 1, 2

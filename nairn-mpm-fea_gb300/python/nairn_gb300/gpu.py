@@ -63,6 +63,27 @@ def lib():
     L.mpmgpu_sort_by_cell_noalloc.restype = C.c_int
     L.mpmgpu_host_unregister.argtypes = [C.c_void_p]
     L.mpmgpu_host_unregister.restype = C.c_int
+    VP = C.c_void_p
+    batch_sigs = {
+        "mpmgpu_batch_bytes": ([P(abi.MpmGpuBatchOptions)], C.c_int64),
+        "mpmgpu_batch_create": ([P(abi.MpmGpuBatchOptions), P(VP)], C.c_int),
+        "mpmgpu_batch_add_run": ([VP, P(abi.MpmGpuGrid), P(abi.MpmGpuMaterial), C.c_int32, P(abi.MpmGpuVelBC),
+                                  C.c_int32, P(abi.MpmGpuParticles), C.c_double, C.c_int32, P(C.c_int32)], C.c_int),
+        "mpmgpu_batch_step": ([VP, C.c_int32], C.c_int),
+        "mpmgpu_batch_step_timed": ([VP, C.c_int32, P(C.c_double)], C.c_int),
+        "mpmgpu_batch_run_state": ([VP, C.c_int32, P(C.c_int32), P(C.c_int32)], C.c_int),
+        "mpmgpu_batch_download_run": ([VP, C.c_int32, P(abi.MpmGpuParticles)], C.c_int),
+        "mpmgpu_batch_remove_run": ([VP, C.c_int32, P(abi.MpmGpuParticles)], C.c_int),
+        "mpmgpu_batch_set_tuning": ([VP, C.c_int32, C.c_int32], C.c_int),
+        "mpmgpu_batch_autotune": ([VP, C.c_int32, P(C.c_int32), P(C.c_int32), P(C.c_double)], C.c_int),
+        "mpmgpu_batch_info": ([VP, P(abi.MpmGpuBatchInfo)], C.c_int),
+        "mpmgpu_batch_last_error": ([VP], C.c_char_p),
+        "mpmgpu_batch_stream": ([VP], VP),
+        "mpmgpu_batch_destroy": ([VP], None),
+    }
+    for f, (args, res) in batch_sigs.items():
+        getattr(L, f).argtypes = args
+        getattr(L, f).restype = res
     for f in ("mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact", "mpmgpu_set_velocity_bcs",
               "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles", "mpmgpu_profile",
               "mpmgpu_set_profiling"):
@@ -148,6 +169,119 @@ class GpuRun:
     def close(self):
         if getattr(self, "h", None):
             lib().mpmgpu_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuBatch:
+    """Many independent runs resident on the current GPU, advanced together by
+    one graph-captured batched step (mpmgpu_batch_* in the C ABI).  All runs
+    share the analysis options (dimension, method, shape functions,
+    precision); grids, materials, velocity conditions, particles, time steps
+    and step counts are per run."""
+
+    def __init__(self, np_: int, method: int, shape: int, precision: int = 0, *, max_runs: int,
+                 max_particles: int, max_nodes: int, max_materials: int | None = None, sort_interval: int = 1,
+                 block: int = 0, fraction_usf: float = 0.5):
+        L = lib()
+        self.opts = abi.MpmGpuBatchOptions(np_, method, shape, precision, sort_interval, block, max_runs,
+                                           max_materials or max_runs, max_particles, max_nodes, fraction_usf)
+        self.bytes = int(L.mpmgpu_batch_bytes(C.byref(self.opts)))
+        h = C.c_void_p()
+        st = L.mpmgpu_batch_create(C.byref(self.opts), C.byref(h))
+        if st != 0:
+            raise GpuError(st, L.mpmgpu_batch_last_error(None).decode())
+        self.h = h
+        self.models = {}
+
+    @classmethod
+    def for_models(cls, models, precision: int = 0, slack: float = 1.0, **kw) -> "GpuBatch":
+        """A batch sized to hold all `models` at once (times `slack`)."""
+        o = models[0].options
+        return cls(o["np"], o["method"], o["shape"], precision, max_runs=kw.pop("max_runs", len(models)),
+                   max_particles=int(slack * sum(m.n for m in models)),
+                   max_nodes=int(slack * sum(m.grid.nnodes for m in models)),
+                   max_materials=int(slack * sum(len(m.materials) for m in models)) + 1,
+                   fraction_usf=o.get("fraction_usf", 0.5), **kw)
+
+    @staticmethod
+    def bytes_for(models, precision: int = 0) -> int:
+        o = models[0].options
+        opts = abi.MpmGpuBatchOptions(o["np"], o["method"], o["shape"], precision, 1, 0, len(models),
+                                      sum(len(m.materials) for m in models) + 1, sum(m.n for m in models),
+                                      sum(m.grid.nnodes for m in models), 0.5)
+        return int(lib().mpmgpu_batch_bytes(C.byref(opts)))
+
+    def _check(self, st):
+        if st != 0:
+            raise GpuError(st, lib().mpmgpu_batch_last_error(self.h).decode())
+
+    def add(self, model: Model, nsteps: int | None = None, particles: dict | None = None) -> int:
+        """Admit a run; returns its run id (GpuError BUSY when it does not fit now)."""
+        b = abi.Bound()
+        g = abi.grid_struct(model, b)
+        bcs, nbc = abi.bcs_array(model)
+        ps = abi.particles_struct(particles if particles is not None else model.particles, b)
+        rid = C.c_int32(-1)
+        self._check(lib().mpmgpu_batch_add_run(self.h, C.byref(g), abi.materials_array(model), len(model.materials),
+                                               bcs, nbc, C.byref(ps), float(model.options["timestep"]),
+                                               int(nsteps if nsteps is not None else model.nsteps), C.byref(rid)))
+        self.models[rid.value] = model
+        return rid.value
+
+    def step(self, nsteps: int = 1):
+        self._check(lib().mpmgpu_batch_step(self.h, int(nsteps)))
+
+    def step_timed(self, nsteps: int) -> float:
+        ms = C.c_double()
+        self._check(lib().mpmgpu_batch_step_timed(self.h, int(nsteps), C.byref(ms)))
+        return ms.value
+
+    def state(self, rid: int):
+        s, d = C.c_int32(), C.c_int32()
+        self._check(lib().mpmgpu_batch_run_state(self.h, rid, C.byref(s), C.byref(d)))
+        return s.value, d.value
+
+    def download(self, rid: int, like: dict | None = None) -> dict:
+        out = abi.empty_like_particles(like if like is not None else self.models[rid].particles)
+        b = abi.Bound()
+        ps = abi.particles_struct(out, b)
+        self._check(lib().mpmgpu_batch_download_run(self.h, rid, C.byref(ps)))
+        return out
+
+    def remove(self, rid: int, download: bool = True):
+        out = None
+        if download:
+            out = abi.empty_like_particles(self.models[rid].particles)
+            b = abi.Bound()
+            ps = abi.particles_struct(out, b)
+            self._check(lib().mpmgpu_batch_remove_run(self.h, rid, C.byref(ps)))
+        else:
+            self._check(lib().mpmgpu_batch_remove_run(self.h, rid, None))
+        self.models.pop(rid, None)
+        return out
+
+    def set_tuning(self, block: int, sort_interval: int):
+        self._check(lib().mpmgpu_batch_set_tuning(self.h, block, sort_interval))
+
+    def autotune(self, trial_steps: int = 8):
+        blk, si, ms = C.c_int32(), C.c_int32(), C.c_double()
+        self._check(lib().mpmgpu_batch_autotune(self.h, trial_steps, C.byref(blk), C.byref(si), C.byref(ms)))
+        return blk.value, si.value, ms.value
+
+    def info(self) -> dict:
+        i = abi.MpmGpuBatchInfo()
+        self._check(lib().mpmgpu_batch_info(self.h, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in abi.MpmGpuBatchInfo._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mpmgpu_batch_destroy(self.h)
             self.h = None
 
     def __del__(self):

@@ -294,3 +294,88 @@ def taylor_3d(radius=5.0, length=25.0, cell=0.25, ppc_side=2, v0=-200000., E=200
     opts = dict(np=THREED, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
                 inc_defgrad_terms=1, nfields=1)
     return Model(g, p, mats, bcs, opts, steps, name=f"taylor_3d_r{radius}_c{cell}")
+
+
+def block_2d(ncx=40, ncy=20, cell=1.0, ppc_side=2, mat=None, vel=(1000., 0., 0., 0., 0., 0.),
+             fixed_left=False, steps=500, cfl=0.4, gimp="uGIMP", method=USAVG, margin_cells=4,
+             name="block_2d", **_ignored) -> Model:
+    """2D plane-strain rectangle of ncx x ncy cells (ppc_side^2 points per cell)
+    with the initial velocity field
+
+        vx = a0 + a1*sin(pi*x/L + phx),   vy = b0 + b1*sin(pi*y/H + phy)
+
+    given as vel = (a0, a1, phx, b0, b1, phy) in mm/s and radians; optionally the
+    left edge (x = 0) held at zero velocity in x and y, as in cantilever_2d.
+    `mat` is one material dict (default: the cantilever's elastic material)."""
+    from . import inputs
+    shape = GIMP_NAMES[gimp]
+    L, H, m = ncx * cell, ncy * cell, margin_cells * cell
+    g = make_grid(2, (-m, L + m), (-m, H + m), None, cell, 1.0)
+    pos, elem = _element_points(g, ppc_side)
+    inside = (pos[:, 0] <= L) & (pos[:, 0] >= 0.) & (pos[:, 1] <= H) & (pos[:, 1] >= 0.)
+    mat = dict(mat) if mat is not None else dict(type=MAT_ISO, field=0, rho=1.0, E=1000., nu=0.33, yield_=0.,
+                                                 Ep=0., G=0., K=0., UJOption=0)
+    p = _new_particles(pos[inside], elem[inside], g, ppc_side, mat["rho"], 1.0)
+    a0, a1, phx, b0, b1, phy = vel
+    p["vx"][:] = a0 + a1 * np.sin(math.pi * p["x"] / L + phx)
+    p["vy"][:] = b0 + b1 * np.sin(math.pi * p["y"] / H + phy)
+    bcs = np.zeros(0, dtype=BC_DTYPE)
+    if fixed_left:
+        nn = g.nnodes
+        ids = np.arange(1, nn + 1)
+        ndx = g.xnodes[(ids - 1) % (g.nx + 1)]
+        ndy = g.ynodes[(ids - 1) // (g.nx + 1)]
+        nodes = ids[_line_contains(ndx, ndy, 0., -0.5 * cell, 0., H + 0.5 * cell, 0.01)]
+        bcs = np.zeros(2 * nodes.size, dtype=BC_DTYPE)
+        bcs["node"][:nodes.size] = nodes
+        bcs["dir"][:nodes.size] = 1
+        bcs["node"][nodes.size:] = nodes
+        bcs["dir"][nodes.size:] = 2
+    c = inputs.iso_wave_speed(mat["E"], mat["nu"], mat["rho"])
+    dt = inputs.cfl_timestep(g.dx, c, cfl)
+    opts = dict(np=PLANE_STRAIN, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
+                inc_defgrad_terms=2, nfields=1)
+    return Model(g, p, [mat], bcs, opts, steps, name=name)
+
+
+def batch_run_params(count=512, seed=2024, nmin=2000, nmax=200000, steps=500, cell=1.0, ppc_side=2, cfl=0.4):
+    """Seeded parameters of a batch of independent 2D runs (keyword dicts for
+    block_2d): particle counts log-uniform in [nmin, nmax]; block aspect
+    log-uniform in [1, 4]; 50/50 linear elastic (type 1) or von Mises with
+    linear hardening (type 9), E log-uniform 0.1-200 GPa, nu uniform 0.2-0.45,
+    yield uniform 0.1-1 % of E, tangent modulus uniform 0.1-5 % of E, density
+    uniform 1-8 g/cm^3; velocity field amplitude uniform 0.1-10 m/s; every
+    other run with its left edge held.  The grid margin covers the largest
+    displacement the amplitude allows over the run's steps."""
+    from . import inputs
+    rng = np.random.default_rng(seed)
+    out = []
+    ppc = ppc_side * ppc_side
+    for k in range(count):
+        n = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        aspect = math.exp(rng.uniform(0., math.log(4.)))
+        cells = max(n / ppc, 9.)
+        ncy = max(3, int(round(math.sqrt(cells / aspect))))
+        ncx = max(3, int(round(cells / ncy)))
+        E = math.exp(rng.uniform(math.log(100.), math.log(200000.)))  # MPa: 0.1-200 GPa
+        nu = rng.uniform(0.2, 0.45)
+        rho = rng.uniform(1., 8.)
+        plastic = rng.uniform() < 0.5
+        mat = dict(type=MAT_PLASTIC if plastic else MAT_ISO, field=0, rho=rho, E=E, nu=nu,
+                   yield_=rng.uniform(0.001, 0.01) * E if plastic else 0., Ep=rng.uniform(0.001, 0.05) * E if plastic else 0.,
+                   G=0., K=0., UJOption=0)
+        amp = 1000. * rng.uniform(0.1, 10.)  # mm/s
+        w = rng.uniform(-1., 1., 4)
+        w = w / np.abs(w).sum()
+        vel = (amp * w[0], amp * w[1], rng.uniform(0., 2. * math.pi), amp * w[2], amp * w[3],
+               rng.uniform(0., 2. * math.pi))
+        dt = inputs.cfl_timestep(cell, inputs.iso_wave_speed(E, nu, rho), cfl)
+        travel = amp * dt * steps / cell
+        out.append(dict(ncx=ncx, ncy=ncy, cell=cell, ppc_side=ppc_side, mat=mat, vel=vel, fixed_left=(k % 2 == 1),
+                        steps=steps, cfl=cfl, margin_cells=3 + int(math.ceil(travel)), name=f"batch{seed}_{k}"))
+    return out
+
+
+def batch_models(count=512, seed=2024, **kw) -> list:
+    """The Models of batch_run_params (same arguments)."""
+    return [block_2d(**p) for p in batch_run_params(count=count, seed=seed, **kw)]

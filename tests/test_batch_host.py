@@ -1,0 +1,63 @@
+"""Host side of the batch API (no GPU): argument checks made before any device
+call, the memory estimate the serving admission uses, and the seeded run
+population of the 512-run batch."""
+import ctypes as C
+
+import numpy as np
+
+
+def test_batch_create_rejects_bad_options_without_gpu_work(gpu_lib):
+    from nairn_gb300 import abi, model
+    base = dict(np=model.PLANE_STRAIN, method=model.USAVG, shape=model.SHAPE_UGIMP, precision=1, sort_interval=1,
+                block=0, max_runs=4, max_materials=4, max_particles=1000, max_nodes=1000, fraction_usf=0.5)
+    for bad, status in ((dict(shape=model.SHAPE_LCPDI), 2), (dict(np=11), 2), (dict(precision=3), 2),
+                        (dict(max_runs=0), 1), (dict(max_particles=-5), 1), (dict(block=96), 1)):
+        o = abi.MpmGpuBatchOptions(**{**base, **bad})
+        h = C.c_void_p()
+        assert gpu_lib.mpmgpu_batch_create(C.byref(o), C.byref(h)) == status, bad
+        assert not h.value
+        assert gpu_lib.mpmgpu_batch_last_error(None)
+
+
+def test_batch_bytes_grows_with_capacity(gpu_lib):
+    from nairn_gb300 import abi, model
+    o = abi.MpmGpuBatchOptions(model.PLANE_STRAIN, model.USAVG, model.SHAPE_UGIMP, 1, 1, 0, 512, 512,
+                               1_000_000, 500_000, 0.5)
+    b1 = gpu_lib.mpmgpu_batch_bytes(C.byref(o))
+    o.max_particles = 2_000_000
+    b2 = gpu_lib.mpmgpu_batch_bytes(C.byref(o))
+    # two arena buffers of 39 doubles + 4 ints per particle, plus sort keys
+    assert b2 - b1 >= 1_000_000 * 2 * (39 * 8 + 4 * 4)
+    assert b1 < 1_000_000 * 700 + 500_000 * 250  # about 680 B per particle slot, 217 B per node
+
+
+def test_batch_population_is_seeded_and_matches_the_spec():
+    from nairn_gb300 import model
+    a = model.batch_run_params(512, seed=2024)
+    b = model.batch_run_params(512, seed=2024)
+    assert a == b
+    n = np.array([p["ncx"] * p["ncy"] * p["ppc_side"] ** 2 for p in a])
+    assert n.min() >= 1800 and n.max() <= 210000
+    assert 15e6 < n.sum() < 30e6  # log-uniform 2k-200k: mean about 43k
+    types = [p["mat"]["type"] for p in a]
+    assert 200 < types.count(model.MAT_PLASTIC) < 312
+    E = np.array([p["mat"]["E"] for p in a])
+    assert E.min() >= 100. and E.max() <= 200000.
+    for p in a:
+        if p["mat"]["type"] == model.MAT_PLASTIC:
+            assert 0.001 * p["mat"]["E"] <= p["mat"]["yield_"] <= 0.01 * p["mat"]["E"]
+        amp = np.abs(np.array(p["vel"])[[0, 1, 3, 4]]).sum()
+        assert 99. <= amp <= 10001.
+
+
+def test_block_model_is_consistent():
+    from nairn_gb300 import model
+    m = model.block_2d(ncx=10, ncy=4, fixed_left=True, vel=(100., 50., 0.3, -20., 10., 1.0))
+    assert m.n == 10 * 4 * 4
+    g = m.grid
+    # every particle lies in its element
+    col = m.particles["elem"] % g.nx
+    row = m.particles["elem"] // g.nx
+    assert np.all((g.xnodes[col] <= m.particles["x"]) & (m.particles["x"] < g.xnodes[col + 1]))
+    assert np.all((g.ynodes[row] <= m.particles["y"]) & (m.particles["y"] < g.ynodes[row + 1]))
+    assert len(m.bcs) == 2 * 5 and set(m.bcs["dir"]) == {1, 2}

@@ -1,0 +1,171 @@
+"""Batched runs (mpmgpu_batch_*): every run of a batch gives the result it
+gives alone -- against the CPU oracle at the FP64 tolerance, and in the mixed
+mode at the mixed tolerance -- whatever else shares the batch, including runs
+that finish early, leave, fail or arrive later."""
+import numpy as np
+import pytest
+
+from conftest import rel_l2
+
+pytestmark = pytest.mark.gpu
+
+TOL = 1e-10
+TOL_MIXED = 1e-5
+FIELDS = ("x", "y", "vx", "vy", "sxx", "syy", "sxy", "szz", "exx", "exy", "hist0", "work")
+
+
+def small_models(count=6, seed=11, steps=40, nmin=300, nmax=3000):
+    from nairn_gb300 import model
+    return model.batch_models(count, seed=seed, nmin=nmin, nmax=nmax, steps=steps)
+
+
+def oracle(m, steps):
+    import oracle_lib
+    from nairn_gb300 import abi
+    ref = abi.copy_particles(m.particles)
+    oracle_lib.run(m, ref, steps, nthreads=4)
+    return ref
+
+
+def assert_close(out, ref, tol, what=""):
+    for k in FIELDS:
+        if np.abs(ref[k]).max() == 0. and np.abs(out[k]).max() == 0.:
+            continue
+        e = rel_l2(out[k], ref[k])
+        assert e <= tol, (what, k, e)
+    assert np.array_equal(out["elem"], ref["elem"]), what
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
+def test_batch_runs_match_oracle(precision, tol, gpu_lib):
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import abi
+    ms = small_models()
+    b = GpuBatch.for_models(ms, precision=precision)
+    ids = [b.add(m) for m in ms]
+    b.step(ms[0].nsteps)
+    for rid, m in zip(ids, ms):
+        st, done = b.state(rid)
+        assert (st, done) == (abi.RUN_FINISHED, m.nsteps)
+        assert_close(b.download(rid), oracle(m, m.nsteps), tol, m.name)
+    info = b.info()
+    assert info["runs"] == len(ms) and info["running"] == 0
+    b.close()
+
+
+def test_batch_matches_single_run_path(gpu_lib):
+    """The batch and the single-run context compute the same step."""
+    from nairn_gb300.gpu import GpuBatch, GpuRun
+    ms = small_models(count=3, seed=5, steps=25)
+    b = GpuBatch.for_models(ms)
+    ids = [b.add(m) for m in ms]
+    b.step(25)
+    for rid, m in zip(ids, ms):
+        r = GpuRun(m)
+        r.upload(m.particles)
+        r.step(25)
+        alone = r.download(m.particles)
+        r.close()
+        assert_close(b.download(rid), alone, TOL, m.name)
+    b.close()
+
+
+def test_runs_stop_at_their_own_step_counts(gpu_lib):
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import abi
+    ms = small_models(count=4, seed=3, steps=30)
+    counts = [7, 30, 18, 1]
+    b = GpuBatch.for_models(ms)
+    ids = [b.add(m, nsteps=c) for m, c in zip(ms, counts)]
+    b.step(10)
+    assert [b.state(r) for r in ids] == [(abi.RUN_FINISHED, 7), (abi.RUN_RUNNING, 10), (abi.RUN_RUNNING, 10),
+                                         (abi.RUN_FINISHED, 1)]
+    b.step(25)
+    for rid, m, c in zip(ids, ms, counts):
+        assert b.state(rid) == (abi.RUN_FINISHED, c)
+        assert_close(b.download(rid), oracle(m, c), TOL, m.name)
+    b.close()
+
+
+def test_removal_compaction_and_late_admission(gpu_lib):
+    """A run removed mid-way leaves the others untouched; its slots are
+    compacted away and a run admitted later starts from its own t = 0."""
+    from nairn_gb300.gpu import GpuBatch
+    ms = small_models(count=5, seed=9, steps=30)
+    first, late = ms[:4], ms[4]
+    b = GpuBatch.for_models(ms)
+    ids = [b.add(m) for m in first]
+    b.step(12)
+    mid = b.remove(ids[1])
+    assert_close(mid, oracle(first[1], 12), TOL, "removed run")
+    rid_late = b.add(late)
+    b.step(30)
+    info = b.info()
+    assert info["particles_dead"] == 0
+    assert info["particles_used"] == sum(m.n for m in ms) - first[1].n
+    for k in (0, 2, 3):
+        assert_close(b.download(ids[k]), oracle(first[k], 30), TOL, first[k].name)
+    assert_close(b.download(rid_late), oracle(late, 30), TOL, "late run")
+    b.close()
+
+
+def test_a_failing_run_is_confined(gpu_lib):
+    """A run whose particle leaves its grid reports LEFT_GRID and stops; the
+    other runs of the batch are unaffected."""
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import abi
+    ms = small_models(count=3, seed=21, steps=20)
+    bad = {k: np.array(v, copy=True) for k, v in ms[1].particles.items()}
+    bad["vx"][0] = -1.e9
+    b = GpuBatch.for_models(ms)
+    ids = [b.add(ms[0]), b.add(ms[1], particles=bad), b.add(ms[2])]
+    b.step(20)
+    st, done = b.state(ids[1])
+    assert st == -6 and done < 20  # -MPMGPU_ERR_LEFT_GRID
+    for k in (0, 2):
+        assert b.state(ids[k]) == (abi.RUN_FINISHED, 20)
+        assert_close(b.download(ids[k]), oracle(ms[k], 20), TOL, ms[k].name)
+    b.close()
+
+
+def test_admission_rejects_bad_indices_and_full_batch(gpu_lib):
+    from nairn_gb300.gpu import GpuBatch, GpuError
+    ms = small_models(count=2, seed=4, steps=5)
+    b = GpuBatch.for_models(ms[:1])
+    bad = {k: np.array(v, copy=True) for k, v in ms[0].particles.items()}
+    bad["elem"][3] = ms[0].grid.nelems
+    with pytest.raises(GpuError, match="INVALID"):
+        b.add(ms[0], particles=bad)
+    rid = b.add(ms[0])  # the rejected run's slots are reused
+    with pytest.raises(GpuError, match="BUSY"):
+        b.add(ms[1])
+    b.step(5)
+    assert_close(b.download(rid), oracle(ms[0], 5), TOL, "after rejection")
+    b.close()
+
+
+@pytest.mark.parametrize("sort_interval", [0, 3])
+def test_sort_interval_and_block_do_not_change_results(sort_interval, gpu_lib):
+    from nairn_gb300.gpu import GpuBatch
+    ms = small_models(count=3, seed=13, steps=20)
+    b = GpuBatch.for_models(ms, sort_interval=sort_interval, block=128)
+    ids = [b.add(m) for m in ms]
+    b.step(20)
+    for rid, m in zip(ids, ms):
+        assert_close(b.download(rid), oracle(m, 20), TOL, m.name)
+    b.close()
+
+
+def test_autotune_steps_count_and_results_hold(gpu_lib):
+    from nairn_gb300.gpu import GpuBatch
+    ms = small_models(count=4, seed=17, steps=200)
+    b = GpuBatch.for_models(ms, precision=1)
+    ids = [b.add(m) for m in ms]
+    blk, si, ms_step = b.autotune(trial_steps=8)
+    assert blk in (128, 256) and si in (1, 2, 4, 8) and ms_step > 0.
+    done = b.state(ids[0])[1]
+    assert done == 8 * (8 + 1)  # 8 candidates x (1 capture step + 8 timed steps)
+    b.step(200 - done)
+    for rid, m in zip(ids, ms):
+        assert_close(b.download(rid), oracle(m, 200), TOL_MIXED, m.name)
+    b.close()
