@@ -14,6 +14,11 @@ G2P, second extrapolation and strain update, element reset).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+The line also carries "batched": 512 independent seeded 2D runs (2k-200k
+particles each) advanced by one graph-captured batched step in mixed
+precision, against the same runs on the plain single-run FP64 path, with the
+error of the batched results against that path.
+
 Under torchrun (N>1) every rank runs an independent replica of the workload
 (the runs do not exchange data), so scaling is weak.
 """
@@ -51,6 +56,9 @@ def parse():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--precision", choices=("mixed", "fp64"), default="mixed",
                     help="transfer arithmetic of the headline run (the FP64 path is always measured too)")
+    ap.add_argument("--batch-runs", type=int, default=512,
+                    help="runs of the batched measurement (0: skip it)")
+    ap.add_argument("--batch-steps", type=int, default=100, help="timed steps of the batched measurement")
     return ap.parse_args()
 
 
@@ -316,6 +324,75 @@ def state_error(a: dict, b: dict, dim: int) -> dict:
     return {"pos": rel(ax), "vel": rel(vx), "stress": rel(sx)}
 
 
+def batched_measurement(args, dist, local):
+    """The batched form: `batch_runs` independent seeded 2D plane-strain runs
+    (2k-200k particles log-uniform, 50/50 elastic / von Mises, E 0.1-200 GPa,
+    velocity fields 0.1-10 m/s, 500 steps each, uGIMP, USAVG) resident together
+    and advanced by one graph-captured batched step in mixed precision, block
+    size and sort interval picked by the autotuner.  Beside it: the same runs
+    on the plain single-run FP64 path (every 16th run, the same steps) and the
+    error of each sampled batched result against that path."""
+    import numpy as np
+    from nairn_gb300 import gpu, model
+    ms = model.batch_models(args.batch_runs, seed=2024)
+    n = sum(m.n for m in ms)
+    b = gpu.GpuBatch.for_models(ms, precision=1)
+    ids = [b.add(m) for m in ms]
+    b.step(max(3, args.warmup))
+    blk, si, _ = b.autotune(8)
+    k = args.batch_steps
+    l0 = b.info()["launches"]
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    ms_b = b.step_timed(k)
+    dist.barrier()
+    clk = clocks.stop()
+    info = b.info()
+    done = b.state(ids[0])[1]
+    value = dist.sum(float(n)) * k / (dist.max(ms_b) / 1e3)
+    # the plain single-run FP64 path on a sample of the same runs, same steps
+    sample = list(range(0, len(ms), 16))
+    plain_ms, plain_ps, errs = 0.0, 0, []
+    for j in sample:
+        m = ms[j]
+        r = gpu.GpuRun(m)
+        r.upload(m.particles)
+        r.step(done - k)
+        plain_ms += r.step_timed(k)
+        plain_ps += m.n * k
+        alone = r.download(m.particles)
+        r.close()
+        errs.append(state_error(b.download(ids[j]), alone, 2))
+    b.close()
+    plain_value = plain_ps / (plain_ms / 1e3)
+    # the same batch in FP64 (separates the batching gain from the precision gain)
+    b64 = gpu.GpuBatch.for_models(ms, precision=0)
+    for m in ms:
+        b64.add(m)
+    b64.step(max(3, args.warmup))
+    k64 = max(1, k // 4)
+    ms64 = b64.step_timed(k64)
+    b64.close()
+    emax = {q: max(e[q] for e in errs) for q in ("pos", "vel", "stress")}
+    return {"value": value, "unit": METRIC, "ms_per_step": ms_b / k, "steps": k, "dtype": "mixed",
+            "config": {"workload": "%d independent 2D plane-strain runs, 2k-200k particles each (log-uniform, "
+                                   "seed 2024), 50/50 elastic / von Mises + linear hardening, uGIMP, USAVG, "
+                                   "500 steps each; one graph-captured batched step" % len(ms),
+                       "particles": n, "grid_nodes": info["nodes_used"], "runs": len(ms),
+                       "autotuned": {"block": blk, "sort_interval": si},
+                       "timed_window": "steps %d-%d of each run" % (done - k + 1, done),
+                       "l2": "batch state %.1f GB vs 129 MB L2: no flush needed" % (n * 39 * 8 / 1e9)},
+            "gpu_launches": info["launches"] - l0, "clocks": clk,
+            "plain_fp64_same_runs": {"value": plain_value, "unit": METRIC, "runs": len(sample),
+                                     "sample": "every 16th run alone on the single-run FP64 path, "
+                                               "same %d steps (small runs fit in L2: favours this path)" % k},
+            "speedup_vs_plain_fp64": value / plain_value,
+            "fp64_batch": {"value": dist.sum(float(n)) * k64 / (dist.max(ms64) / 1e3), "steps": k64},
+            "error_vs_plain_fp64": dict(emax, statistic="max over the %d sampled runs" % len(sample),
+                                        target="<= 1e-5 relative L2")}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
@@ -399,6 +476,8 @@ def main():
                     "d2h_bytes_per_step": d2h * ws, "steps": ke,
                     "note": "per step: upload full particle state from pinned host memory, one step, download"},
             "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk}
+    if args.batch_runs > 0:
+        line["batched"] = batched_measurement(args, dist, local)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(workload(args), args.cpu_seconds)
     dist.close()
