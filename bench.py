@@ -59,6 +59,9 @@ def parse():
     ap.add_argument("--batch-runs", type=int, default=512,
                     help="runs of the batched measurement (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=100, help="timed steps of the batched measurement")
+    ap.add_argument("--serve-requests", type=int, default=40,
+                    help="requests of the served measurement, a prefix of the seeded 200-request stream (0: skip)")
+    ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM admission budget of the server")
     return ap.parse_args()
 
 
@@ -393,6 +396,66 @@ def batched_measurement(args, dist, local):
                                         target="<= 1e-5 relative L2")}
 
 
+def served_measurement(args, dist):
+    """The served form: a seeded Poisson stream (20 requests/s) of independent
+    2D/3D elastic-plastic runs, 10k-2M particles (log-uniform), 200-2,000 steps,
+    submitted at their arrival times to the C++ serving loop (continuous
+    batching, HBM admission budget, mixed precision).  Reports throughput and
+    p50/p99 completion latency, beside every 5th request run alone on the plain
+    single-run FP64 path (20 timed steps, scaled to its step count)."""
+    import numpy as np
+    from nairn_gb300 import gpu, model
+    params = model.serve_request_params(200, seed=77)[:args.serve_requests]
+    ms = model.serve_models(params)
+    srv = gpu.GpuServer(model.USAVG, model.SHAPE_UGIMP, 1, hbm_budget_bytes=int(args.serve_budget_gb * 1e9),
+                        max_runs=256, steps_per_round=10, frac_3d=0.5)
+    dist.barrier()
+    t0 = time.perf_counter()
+    ids = []
+    for (t_arr, _, _), m in zip(params, ms):
+        delay = t_arr - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(m))
+    srv.drain(3600)
+    wall = time.perf_counter() - t0
+    infos = [srv.poll(r) for r in ids]
+    st = srv.stats()
+    srv.close()
+    lat = np.array([i["total_ms"] for i in infos])
+    qms = np.array([i["queue_ms"] for i in infos])
+    work = float(sum(m.n * m.nsteps for m in ms))
+    # each sampled request alone on the plain single-run FP64 path
+    alone, ratio, alone_ps, alone_s = [], [], 0.0, 0.0
+    for j in range(0, len(ms), 5):
+        m = ms[j]
+        t1 = time.perf_counter()
+        r = gpu.GpuRun(m)
+        r.upload(m.particles)
+        r.step(2)
+        k = 20
+        step_ms = r.step_timed(k) / k
+        r.close()
+        setup_ms = 1e3 * (time.perf_counter() - t1) - step_ms * (k + 2)
+        a = max(setup_ms, 0.0) + step_ms * m.nsteps
+        alone.append(a)
+        ratio.append(infos[j]["total_ms"] / a)
+        alone_ps += m.n * m.nsteps
+        alone_s += a / 1e3
+    return {"value": work / wall, "unit": METRIC, "requests": len(ms), "completed": st["completed"],
+            "failed": st["failed"], "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "queue_p50_ms": float(np.percentile(qms, 50)), "wall_s": wall, "particle_steps": work, "dtype": "mixed",
+            "config": {"workload": "seeded Poisson(20/s) stream, 2D/3D elastic-plastic blocks, 10k-2M particles "
+                                   "(log-uniform), 200-2000 steps, uGIMP, USAVG; first %d of 200 requests" % len(ms),
+                       "hbm_budget_gb": args.serve_budget_gb, "reserved_gb": st["reserved_bytes"] / 1e9,
+                       "steps_per_round": 10, "rounds": st["rounds"]},
+            "alone_plain_fp64": {"p50_ms": float(np.percentile(alone, 50)), "p99_ms": float(np.percentile(alone, 99)),
+                                 "throughput": alone_ps / alone_s, "unit": METRIC, "requests": len(alone),
+                                 "served_over_alone_latency_p50": float(np.percentile(ratio, 50)),
+                                 "sample": "every 5th request alone: setup + 20 timed steps scaled to its steps"},
+            "speedup_vs_plain_fp64": (work / wall) / (alone_ps / alone_s)}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
@@ -478,6 +541,8 @@ def main():
             "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk}
     if args.batch_runs > 0:
         line["batched"] = batched_measurement(args, dist, local)
+    if args.serve_requests > 0:
+        line["served"] = served_measurement(args, dist)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(workload(args), args.cpu_seconds)
     dist.close()

@@ -315,6 +315,72 @@ const char *mpmgpu_batch_last_error(const MpmGpuBatch *b);
 void *mpmgpu_batch_stream(MpmGpuBatch *b);
 void mpmgpu_batch_destroy(MpmGpuBatch *b);
 
+/* ---- server: continuous batching of independent requests ------------------
+ * A server keeps one batch per dimension (2D plane strain, 3D) sized within
+ * an HBM budget and runs a host thread that admits queued requests as run
+ * slots and memory free up, advances all admitted runs together in rounds of
+ * steps_per_round batched steps (2D and 3D batches overlap on the device) and
+ * retires finished runs.  Each result equals the run computed alone (within
+ * the mode's tolerance; only the order of atomic node sums differs).  No
+ * counterpart in the reference.  submit/poll/wait/drain/release/stats may be
+ * called from any host thread. */
+typedef struct MpmGpuServer MpmGpuServer;
+
+typedef struct {
+    int32_t method;             /* MPMGPU_USF / _USAVG / _USL                  */
+    int32_t shape;              /* MPMGPU_SHAPE_LINEAR or _UGIMP               */
+    int32_t precision;          /* MPMGPU_PREC_*                               */
+    int32_t max_runs;           /* run slots per dimension                     */
+    int32_t steps_per_round;    /* steps between admissions/retirements (0: 10) */
+    int32_t backfill;           /* 1: a later request that fits may pass one that does not */
+    int32_t sort_interval;      /* cell sort every k steps (0: 1)              */
+    int32_t block;              /* particle-kernel block size (0: 256)         */
+    int64_t hbm_budget_bytes;   /* device memory the server holds (both batches) */
+    double frac_3d;             /* share of the budget for 3D runs (0..1)      */
+    double nodes_per_particle;  /* node slots per particle slot (0: 0.5)       */
+    double fraction_usf;        /* USAVG split (0 -> 0.5)                      */
+} MpmGpuServerOptions;
+
+enum { MPMGPU_REQ_QUEUED = 1, MPMGPU_REQ_RUNNING = 2, MPMGPU_REQ_DONE = 3, MPMGPU_REQ_FAILED = 4 };
+
+typedef struct {
+    int32_t state;              /* MPMGPU_REQ_*                                */
+    int32_t status;             /* MPMGPU_OK, or why a request failed          */
+    int32_t steps_done, pad;
+    double queue_ms;            /* submit -> admission (or now)                */
+    double run_ms;              /* admission -> completion (or now)            */
+    double total_ms;            /* submit -> completion (or now)               */
+} MpmGpuRequestInfo;
+
+typedef struct {
+    int64_t submitted, completed, failed, queued, running;
+    int64_t particle_steps;     /* sum of particles x steps of completed requests */
+    int64_t rounds;             /* stepping rounds                             */
+    int64_t reserved_bytes;     /* device bytes held by the server's batches   */
+    double busy_ms;             /* wall time of the rounds that stepped        */
+} MpmGpuServerStats;
+
+int mpmgpu_server_create(const MpmGpuServerOptions *opts, MpmGpuServer **out);
+/* Queue one run.  The particle arrays of p are borrowed: they must stay valid
+ * and unchanged until the request is done or failed; they are read at
+ * admission and receive the final state (upload order) at completion.  Grid
+ * coordinates, materials and velocity conditions are copied. */
+int mpmgpu_server_submit(MpmGpuServer *s, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
+                         const MpmGpuVelBC *bcs, int32_t nbc, MpmGpuParticles *p, double timestep,
+                         int32_t nsteps, int64_t *request_id);
+int mpmgpu_server_poll(MpmGpuServer *s, int64_t request_id, MpmGpuRequestInfo *info);
+/* Block until the request is done or failed; MPMGPU_ERR_TIMEOUT after timeout_s. */
+int mpmgpu_server_wait(MpmGpuServer *s, int64_t request_id, double timeout_s);
+/* Block until no request is queued or running; MPMGPU_ERR_TIMEOUT after timeout_s. */
+int mpmgpu_server_drain(MpmGpuServer *s, double timeout_s);
+/* Forget a finished request (its record and timings). */
+int mpmgpu_server_release(MpmGpuServer *s, int64_t request_id);
+int mpmgpu_server_stats(MpmGpuServer *s, MpmGpuServerStats *stats);
+const char *mpmgpu_server_last_error(const MpmGpuServer *s);
+/* Stop the loop (queued and running requests are abandoned) and free the
+ * device memory; no other call may be waiting on the server. */
+void mpmgpu_server_destroy(MpmGpuServer *s);
+
 #ifdef __cplusplus
 }
 #endif

@@ -452,29 +452,26 @@ int batch_active_runs(const MpmGpuBatch *b) {
     return k;
 }
 
-// one graph launch per step; run states are read back at the end
-int batch_steps(MpmGpuBatch *b, int nsteps, double *ms) {
+// Enqueue nsteps batched steps (one graph launch each) without waiting for
+// them; `mark`, when given, is recorded just before the first launch.  Sets
+// *launched to whether any step was enqueued.
+int batch_launch(MpmGpuBatch *b, int nsteps, cudaEvent_t mark, bool *launched) {
+    *launched = false;
     if (b->bcs_dirty) {
         int st = batch_rebuild_bcs(b);
         if (st != MPMGPU_OK) return st;
     }
-    if (ms) *ms = 0.;
     if (b->n_dead > 0) {
         int st = batch_compact(b);
         if (st != MPMGPU_OK) return st;
     }
     if (!batch_active_runs(b) || b->n_used == 0 || nsteps == 0) return MPMGPU_OK;
     // capture every graph the steps can use before the first launch, so no
-    // capture sits between launches (or inside the timed region)
+    // capture sits between launches (or inside a timed region)
     int st = batch_prepare(b);
     if (st != MPMGPU_OK) return st;
+    if (mark) BCK(cudaEventRecord(mark, b->stream));
     cudaGraphExec_t gx = nullptr;
-    cudaEvent_t e0 = nullptr, e1 = nullptr;
-    if (ms) {
-        BCK(cudaEventCreate(&e0));
-        BCK(cudaEventCreate(&e1));
-        BCK(cudaEventRecord(e0, b->stream));
-    }
     for (int s = 0; s < nsteps; s++) {
         const int with_sort = b->o.sort_interval > 0 && b->since_sort >= b->o.sort_interval;
         st = batch_graph(b, with_sort, &gx);
@@ -489,17 +486,16 @@ int batch_steps(MpmGpuBatch *b, int nsteps, double *ms) {
         b->since_sort++;
         b->steps++;
     }
-    if (ms) BCK(cudaEventRecord(e1, b->stream));
+    *launched = true;
+    return MPMGPU_OK;
+}
+
+// Wait for the enqueued steps and read the run table back: steps taken,
+// finished runs, failed runs (with their error status).
+int batch_collect(MpmGpuBatch *b) {
     BCK(cudaMemcpyAsync(b->runs_host.data(), b->runs_dev, sizeof(DevRun) * b->runs_host.size(),
                         cudaMemcpyDeviceToHost, b->stream));
     BCK(cudaStreamSynchronize(b->stream));
-    if (ms) {
-        float f = 0.f;
-        cudaEventElapsedTime(&f, e0, e1);
-        *ms = f;
-        cudaEventDestroy(e0);
-        cudaEventDestroy(e1);
-    }
     for (size_t r = 0; r < b->runs.size(); r++) {
         BatchRun &br = b->runs[r];
         if (!br.used || br.state != MPMGPU_RUN_RUNNING) continue;
@@ -509,6 +505,30 @@ int batch_steps(MpmGpuBatch *b, int nsteps, double *ms) {
         else if (!R.active) br.state = MPMGPU_RUN_FINISHED;
     }
     return MPMGPU_OK;
+}
+
+// nsteps steps, then the run states; *ms (when given) receives their device time
+int batch_steps(MpmGpuBatch *b, int nsteps, double *ms) {
+    if (ms) *ms = 0.;
+    cudaEvent_t e0 = nullptr, e1 = nullptr;
+    if (ms) {
+        BCK(cudaEventCreate(&e0));
+        BCK(cudaEventCreate(&e1));
+    }
+    bool launched = false;
+    int st = batch_launch(b, nsteps, e0, &launched);
+    if (st == MPMGPU_OK && launched) {
+        if (ms) BCK(cudaEventRecord(e1, b->stream));
+        st = batch_collect(b);
+        if (st == MPMGPU_OK && ms) {
+            float f = 0.f;
+            cudaEventElapsedTime(&f, e0, e1);
+            *ms = f;
+        }
+    }
+    if (e0) cudaEventDestroy(e0);
+    if (e1) cudaEventDestroy(e1);
+    return st;
 }
 
 }  // namespace

@@ -826,3 +826,4 @@ int mpmgpu_host_unregister(void *ptr) {
 }  // extern "C"
 
 #include "batch.cuh"
+#include "server.cuh"

@@ -1,0 +1,416 @@
+// server.cuh -- continuous-batching request loop over the batch engine.
+// Included by mpm_gpu.cu after batch.cuh; implements the mpmgpu_server_*
+// entry points of include/nairn_mpm_gpu.h.
+//
+// A server owns one batch per dimension (2D plane strain and 3D), sized at
+// creation so that both together stay within the HBM budget, and one host
+// thread that runs the loop
+//
+//     admit queued requests that fit (FIFO; optionally backfilling)
+//     enqueue `steps_per_round` batched steps on every batch with running runs
+//     wait for them, retire finished and failed runs (results written back)
+//
+// The batches step on their own streams, so 2D and 3D work overlaps on the
+// device.  Requests that arrive while others run join at the next round; a
+// finished run's slots are compacted away by the next sort.  Each request's
+// particle arrays are borrowed: they are read at admission and receive the
+// results when the request completes.
+#pragma once
+
+#include <chrono>
+#include <condition_variable>
+#include <deque>
+#include <memory>
+#include <thread>
+#include <unordered_map>
+
+namespace {
+
+using ServerClock = std::chrono::steady_clock;
+
+struct ServerRequest {
+    int64_t id = 0;
+    int dim = 2;
+    MpmGpuGrid grid{};
+    std::vector<double> xn, yn, zn;
+    std::vector<MpmGpuMaterial> mats;
+    std::vector<MpmGpuVelBC> bcs;
+    MpmGpuParticles p{};  // borrowed caller arrays
+    double dt = 0.;
+    int nsteps = 0;
+    int state = MPMGPU_REQ_QUEUED;
+    int status = MPMGPU_OK;
+    int run_id = -1;
+    int steps_done = 0;
+    std::string msg;
+    ServerClock::time_point t_submit, t_admit, t_done;
+};
+
+double ms_between(ServerClock::time_point a, ServerClock::time_point b) {
+    return std::chrono::duration<double, std::milli>(b - a).count();
+}
+
+}  // namespace
+
+struct MpmGpuServer {
+    MpmGpuServerOptions o{};
+    int device = 0;
+    MpmGpuBatch *batch[2] = {nullptr, nullptr};  // [0] 2D, [1] 3D
+    int64_t reserved = 0;
+    std::mutex mu;
+    std::condition_variable wake, done;
+    std::deque<ServerRequest *> queue;                                    // admission order
+    std::unordered_map<int64_t, std::unique_ptr<ServerRequest>> reqs;   // every unreleased request
+    std::vector<ServerRequest *> running[2];
+    int64_t next_id = 1;
+    bool stop = false;
+    std::thread worker;
+    MpmGpuServerStats stats{};
+    std::string msg;
+    std::string loop_error;
+};
+
+namespace {
+
+int serr(MpmGpuServer *s, int code, const std::string &m) {
+    if (s) s->msg = m;
+    else g_static_err = m;
+    return code;
+}
+
+// largest particle capacity whose batch fits in `bytes`
+int64_t server_capacity(MpmGpuBatchOptions o, int64_t bytes, double nodes_per_particle) {
+    int64_t lo = 0, hi = (1LL << 31) - 1;
+    while (lo < hi) {
+        const int64_t mid = lo + (hi - lo + 1) / 2;
+        o.max_particles = mid;
+        o.max_nodes = std::max<int64_t>(1, (int64_t)(nodes_per_particle * (double)mid));
+        if (o.max_nodes > (1LL << 30)) {
+            hi = mid - 1;
+            continue;
+        }
+        const int64_t need = mpmgpu_batch_bytes(&o);
+        if (need >= 0 && need <= bytes) lo = mid;
+        else hi = mid - 1;
+    }
+    return lo;
+}
+
+// admission: FIFO per dimension; with backfill a request that does not fit
+// now is passed by later ones of its dimension
+void server_admit(MpmGpuServer *s, std::vector<ServerRequest *> &admitted, std::vector<ServerRequest *> &failed) {
+    std::vector<ServerRequest *> cand;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        cand.assign(s->queue.begin(), s->queue.end());
+    }
+    bool blocked[2] = {false, false};
+    for (ServerRequest *q : cand) {
+        const int d = q->dim == 3 ? 1 : 0;
+        MpmGpuBatch *b = s->batch[d];
+        if (blocked[d]) continue;
+        int32_t rid = -1;
+        const int st = mpmgpu_batch_add_run(b, &q->grid, q->mats.data(), (int32_t)q->mats.size(),
+                                            q->bcs.empty() ? nullptr : q->bcs.data(), (int32_t)q->bcs.size(), &q->p,
+                                            q->dt, q->nsteps, &rid);
+        if (st == MPMGPU_OK) {
+            q->run_id = rid;
+            q->t_admit = ServerClock::now();
+            admitted.push_back(q);
+        } else if (st == MPMGPU_ERR_BUSY) {
+            MpmGpuBatchInfo bi{};
+            mpmgpu_batch_info(b, &bi);
+            if (bi.runs == 0) {
+                // the batch is empty and the request still does not fit
+                q->status = MPMGPU_ERR_OOM;
+                q->msg = "request needs more device memory than its share of the HBM budget";
+                failed.push_back(q);
+            } else if (!s->o.backfill) {
+                blocked[d] = true;
+            }
+        } else {
+            q->status = st;
+            q->msg = mpmgpu_batch_last_error(b);
+            failed.push_back(q);
+        }
+    }
+}
+
+void server_loop(MpmGpuServer *s) {
+    cudaSetDevice(s->device);
+    const int chunk = s->o.steps_per_round > 0 ? s->o.steps_per_round : 10;
+    while (true) {
+        {
+            std::unique_lock<std::mutex> lk(s->mu);
+            if (s->stop) break;
+            if (s->queue.empty() && s->running[0].empty() && s->running[1].empty()) {
+                s->wake.wait_for(lk, std::chrono::milliseconds(50));
+                continue;
+            }
+        }
+        std::vector<ServerRequest *> admitted, failed;
+        server_admit(s, admitted, failed);
+        {
+            std::lock_guard<std::mutex> lk(s->mu);
+            auto drop = [&](ServerRequest *q) {
+                for (auto it = s->queue.begin(); it != s->queue.end(); ++it)
+                    if (*it == q) {
+                        s->queue.erase(it);
+                        break;
+                    }
+            };
+            for (ServerRequest *q : admitted) {
+                drop(q);
+                q->state = MPMGPU_REQ_RUNNING;
+                s->running[q->dim == 3 ? 1 : 0].push_back(q);
+            }
+            for (ServerRequest *q : failed) {
+                drop(q);
+                q->state = MPMGPU_REQ_FAILED;
+                q->t_done = ServerClock::now();
+                s->stats.failed++;
+            }
+            if (!failed.empty()) s->done.notify_all();
+        }
+        bool any = false;
+        const auto t0 = ServerClock::now();
+        bool launched[2] = {false, false};
+        int status[2] = {MPMGPU_OK, MPMGPU_OK};
+        // enqueue on both batches first, then wait for both: their steps overlap
+        for (int d = 0; d < 2; d++)
+            if (!s->running[d].empty()) status[d] = batch_launch(s->batch[d], chunk, nullptr, &launched[d]);
+        for (int d = 0; d < 2; d++)
+            if (status[d] == MPMGPU_OK && launched[d]) status[d] = batch_collect(s->batch[d]);
+        for (int d = 0; d < 2; d++) {
+            if (status[d] != MPMGPU_OK) {
+                // a CUDA error on this batch: its running requests fail
+                std::lock_guard<std::mutex> lk(s->mu);
+                s->loop_error = mpmgpu_batch_last_error(s->batch[d]);
+                for (ServerRequest *q : s->running[d]) {
+                    q->state = MPMGPU_REQ_FAILED;
+                    q->status = status[d];
+                    q->msg = s->loop_error;
+                    q->t_done = ServerClock::now();
+                    s->stats.failed++;
+                }
+                s->running[d].clear();
+                launched[d] = false;
+                s->done.notify_all();
+            }
+            any = any || launched[d];
+        }
+        // retire finished and failed runs: results go back into the caller's arrays
+        for (int d = 0; d < 2; d++) {
+            std::vector<ServerRequest *> keep;
+            for (ServerRequest *q : s->running[d]) {
+                int32_t st = 0, steps = 0;
+                mpmgpu_batch_run_state(s->batch[d], q->run_id, &st, &steps);
+                {
+                    std::lock_guard<std::mutex> lk(s->mu);
+                    q->steps_done = steps;
+                }
+                if (st == MPMGPU_RUN_RUNNING) {
+                    keep.push_back(q);
+                    continue;
+                }
+                const int rs = mpmgpu_batch_remove_run(s->batch[d], q->run_id, &q->p);
+                std::lock_guard<std::mutex> lk(s->mu);
+                q->t_done = ServerClock::now();
+                if (st == MPMGPU_RUN_FINISHED && rs == MPMGPU_OK) {
+                    q->state = MPMGPU_REQ_DONE;
+                    s->stats.completed++;
+                    s->stats.particle_steps += q->p.n * (int64_t)q->steps_done;
+                } else {
+                    q->state = MPMGPU_REQ_FAILED;
+                    q->status = rs != MPMGPU_OK ? rs : -st;
+                    q->msg = rs != MPMGPU_OK ? mpmgpu_batch_last_error(s->batch[d]) : "run failed on the device";
+                    s->stats.failed++;
+                }
+                s->done.notify_all();
+            }
+            std::lock_guard<std::mutex> lk(s->mu);
+            s->running[d].swap(keep);
+        }
+        std::lock_guard<std::mutex> lk(s->mu);
+        if (any) {
+            s->stats.rounds++;
+            s->stats.busy_ms += ms_between(t0, ServerClock::now());
+        }
+    }
+}
+
+}  // namespace
+
+extern "C" {
+
+int mpmgpu_server_create(const MpmGpuServerOptions *o, MpmGpuServer **out) {
+    if (!o || !out) return serr(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_server_create: null argument");
+    *out = nullptr;
+    if (o->hbm_budget_bytes <= 0 || o->max_runs <= 0 || !(o->frac_3d >= 0. && o->frac_3d <= 1.))
+        return serr(nullptr, MPMGPU_ERR_INVALID, "server needs a positive HBM budget, run slots and 0 <= frac_3d <= 1");
+    auto s = std::make_unique<MpmGpuServer>();
+    s->o = *o;
+    if (!(s->o.nodes_per_particle > 0.)) s->o.nodes_per_particle = 0.5;
+    cudaGetDevice(&s->device);
+    const double frac[2] = {1. - o->frac_3d, o->frac_3d};
+    const int np[2] = {MPMGPU_PLANE_STRAIN, MPMGPU_THREED};
+    for (int d = 0; d < 2; d++) {
+        const int64_t bytes = (int64_t)(frac[d] * (double)o->hbm_budget_bytes);
+        if (frac[d] <= 0.) continue;
+        MpmGpuBatchOptions bo{};
+        bo.np = np[d];
+        bo.method = o->method;
+        bo.shape = o->shape;
+        bo.precision = o->precision;
+        bo.sort_interval = o->sort_interval > 0 ? o->sort_interval : 1;
+        bo.block = o->block;
+        bo.max_runs = o->max_runs;
+        bo.max_materials = 4 * o->max_runs;
+        bo.fraction_usf = o->fraction_usf;
+        const int64_t P = server_capacity(bo, bytes, s->o.nodes_per_particle);
+        if (P < 1000) {
+            for (auto *b : s->batch) mpmgpu_batch_destroy(b);
+            return serr(nullptr, MPMGPU_ERR_INVALID, "HBM budget too small for a batch");
+        }
+        bo.max_particles = P;
+        bo.max_nodes = std::max<int64_t>(1, (int64_t)(s->o.nodes_per_particle * (double)P));
+        const int st = mpmgpu_batch_create(&bo, &s->batch[d]);
+        if (st != MPMGPU_OK) {
+            std::string m = mpmgpu_batch_last_error(nullptr);
+            for (auto *b : s->batch) mpmgpu_batch_destroy(b);
+            return serr(nullptr, st, "server batch: " + m);
+        }
+        s->reserved += mpmgpu_batch_bytes(&bo);
+    }
+    s->stats.reserved_bytes = s->reserved;
+    MpmGpuServer *raw = s.release();
+    raw->worker = std::thread(server_loop, raw);
+    *out = raw;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_server_submit(MpmGpuServer *s, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
+                         const MpmGpuVelBC *bcs, int32_t nbc, MpmGpuParticles *p, double timestep, int32_t nsteps,
+                         int64_t *request_id) {
+    if (!s || !grid || !mats || nmat <= 0 || !p || p->n <= 0 || nbc < 0 || (nbc > 0 && !bcs) || !request_id ||
+        nsteps <= 0 || !(timestep > 0.))
+        return serr(s, MPMGPU_ERR_INVALID, "mpmgpu_server_submit: bad argument");
+    if (grid->dim != 2 && grid->dim != 3) return serr(s, MPMGPU_ERR_INVALID, "grid dim must be 2 or 3");
+    if (!s->batch[grid->dim == 3 ? 1 : 0])
+        return serr(s, MPMGPU_ERR_UNSUPPORTED, "the server holds no batch for this dimension");
+    if (grid->nx < 1 || grid->ny < 1 || (grid->dim == 3 && grid->nz < 1) || !grid->xnodes || !grid->ynodes ||
+        (grid->dim == 3 && !grid->znodes))
+        return serr(s, MPMGPU_ERR_INVALID, "grid needs element counts and node coordinates");
+    auto q = std::make_unique<ServerRequest>();
+    q->dim = grid->dim;
+    q->grid = *grid;
+    q->xn.assign(grid->xnodes, grid->xnodes + grid->nx + 1);
+    q->yn.assign(grid->ynodes, grid->ynodes + grid->ny + 1);
+    if (grid->dim == 3) q->zn.assign(grid->znodes, grid->znodes + grid->nz + 1);
+    q->grid.xnodes = q->xn.data();
+    q->grid.ynodes = q->yn.data();
+    q->grid.znodes = grid->dim == 3 ? q->zn.data() : nullptr;
+    q->mats.assign(mats, mats + nmat);
+    if (nbc) q->bcs.assign(bcs, bcs + nbc);
+    q->p = *p;
+    q->dt = timestep;
+    q->nsteps = nsteps;
+    q->t_submit = ServerClock::now();
+    std::lock_guard<std::mutex> lk(s->mu);
+    q->id = s->next_id++;
+    *request_id = q->id;
+    s->queue.push_back(q.get());
+    s->reqs[q->id] = std::move(q);
+    s->stats.submitted++;
+    s->wake.notify_all();
+    return MPMGPU_OK;
+}
+
+int mpmgpu_server_poll(MpmGpuServer *s, int64_t id, MpmGpuRequestInfo *info) {
+    if (!s || !info) return MPMGPU_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return serr(s, MPMGPU_ERR_INVALID, "unknown request");
+    const ServerRequest &q = *it->second;
+    const auto now = ServerClock::now();
+    const bool ended = q.state == MPMGPU_REQ_DONE || q.state == MPMGPU_REQ_FAILED;
+    const auto end = ended ? q.t_done : now;
+    info->state = q.state;
+    info->status = q.status;
+    info->steps_done = q.steps_done;
+    info->pad = 0;
+    info->queue_ms = q.state == MPMGPU_REQ_QUEUED || q.run_id < 0 ? ms_between(q.t_submit, end)
+                                                                  : ms_between(q.t_submit, q.t_admit);
+    info->run_ms = q.run_id >= 0 ? ms_between(q.t_admit, end) : 0.;
+    info->total_ms = ms_between(q.t_submit, end);
+    return MPMGPU_OK;
+}
+
+int mpmgpu_server_wait(MpmGpuServer *s, int64_t id, double timeout_s) {
+    if (!s) return MPMGPU_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return serr(s, MPMGPU_ERR_INVALID, "unknown request");
+    ServerRequest *q = it->second.get();
+    const auto limit = ServerClock::now() + std::chrono::duration_cast<ServerClock::duration>(
+                                                std::chrono::duration<double>(std::max(0., timeout_s)));
+    const bool ok = s->done.wait_until(lk, limit, [&] {
+        return q->state == MPMGPU_REQ_DONE || q->state == MPMGPU_REQ_FAILED;
+    });
+    if (!ok) return serr(s, MPMGPU_ERR_TIMEOUT, "request not finished within the timeout");
+    if (q->state == MPMGPU_REQ_FAILED) {
+        s->msg = q->msg;
+        return q->status != MPMGPU_OK ? q->status : MPMGPU_ERR_INVALID;
+    }
+    return MPMGPU_OK;
+}
+
+int mpmgpu_server_drain(MpmGpuServer *s, double timeout_s) {
+    if (!s) return MPMGPU_ERR_INVALID;
+    std::unique_lock<std::mutex> lk(s->mu);
+    const auto limit = ServerClock::now() + std::chrono::duration_cast<ServerClock::duration>(
+                                                std::chrono::duration<double>(std::max(0., timeout_s)));
+    const bool ok = s->done.wait_until(lk, limit, [&] {
+        return s->queue.empty() && s->running[0].empty() && s->running[1].empty();
+    });
+    return ok ? MPMGPU_OK : serr(s, MPMGPU_ERR_TIMEOUT, "requests still pending after the timeout");
+}
+
+int mpmgpu_server_release(MpmGpuServer *s, int64_t id) {
+    if (!s) return MPMGPU_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto it = s->reqs.find(id);
+    if (it == s->reqs.end()) return serr(s, MPMGPU_ERR_INVALID, "unknown request");
+    if (it->second->state != MPMGPU_REQ_DONE && it->second->state != MPMGPU_REQ_FAILED)
+        return serr(s, MPMGPU_ERR_BUSY, "request still queued or running");
+    s->reqs.erase(it);
+    return MPMGPU_OK;
+}
+
+int mpmgpu_server_stats(MpmGpuServer *s, MpmGpuServerStats *out) {
+    if (!s || !out) return MPMGPU_ERR_INVALID;
+    std::lock_guard<std::mutex> lk(s->mu);
+    *out = s->stats;
+    out->queued = (int64_t)s->queue.size();
+    out->running = (int64_t)(s->running[0].size() + s->running[1].size());
+    return MPMGPU_OK;
+}
+
+const char *mpmgpu_server_last_error(const MpmGpuServer *s) {
+    if (!s) return g_static_err.c_str();
+    return !s->loop_error.empty() && s->msg.empty() ? s->loop_error.c_str() : s->msg.c_str();
+}
+
+void mpmgpu_server_destroy(MpmGpuServer *s) {
+    if (!s) return;
+    {
+        std::lock_guard<std::mutex> lk(s->mu);
+        s->stop = true;
+        s->wake.notify_all();
+    }
+    if (s->worker.joinable()) s->worker.join();
+    for (auto *b : s->batch) mpmgpu_batch_destroy(b);
+    delete s;
+}
+
+}  // extern "C"

@@ -145,3 +145,24 @@ class MpmGpuBatchInfo(C.Structure):
 
 
 RUN_EMPTY, RUN_RUNNING, RUN_FINISHED = 0, 1, 2
+
+
+class MpmGpuServerOptions(C.Structure):
+    _fields_ = [("method", C.c_int32), ("shape", C.c_int32), ("precision", C.c_int32), ("max_runs", C.c_int32),
+                ("steps_per_round", C.c_int32), ("backfill", C.c_int32), ("sort_interval", C.c_int32),
+                ("block", C.c_int32), ("hbm_budget_bytes", C.c_int64), ("frac_3d", C.c_double),
+                ("nodes_per_particle", C.c_double), ("fraction_usf", C.c_double)]
+
+
+class MpmGpuRequestInfo(C.Structure):
+    _fields_ = [("state", C.c_int32), ("status", C.c_int32), ("steps_done", C.c_int32), ("pad", C.c_int32),
+                ("queue_ms", C.c_double), ("run_ms", C.c_double), ("total_ms", C.c_double)]
+
+
+class MpmGpuServerStats(C.Structure):
+    _fields_ = [("submitted", C.c_int64), ("completed", C.c_int64), ("failed", C.c_int64), ("queued", C.c_int64),
+                ("running", C.c_int64), ("particle_steps", C.c_int64), ("rounds", C.c_int64),
+                ("reserved_bytes", C.c_int64), ("busy_ms", C.c_double)]
+
+
+REQ_QUEUED, REQ_RUNNING, REQ_DONE, REQ_FAILED = 1, 2, 3, 4

@@ -80,6 +80,16 @@ def lib():
         "mpmgpu_batch_last_error": ([VP], C.c_char_p),
         "mpmgpu_batch_stream": ([VP], VP),
         "mpmgpu_batch_destroy": ([VP], None),
+        "mpmgpu_server_create": ([P(abi.MpmGpuServerOptions), P(VP)], C.c_int),
+        "mpmgpu_server_submit": ([VP, P(abi.MpmGpuGrid), P(abi.MpmGpuMaterial), C.c_int32, P(abi.MpmGpuVelBC),
+                                  C.c_int32, P(abi.MpmGpuParticles), C.c_double, C.c_int32, P(C.c_int64)], C.c_int),
+        "mpmgpu_server_poll": ([VP, C.c_int64, P(abi.MpmGpuRequestInfo)], C.c_int),
+        "mpmgpu_server_wait": ([VP, C.c_int64, C.c_double], C.c_int),
+        "mpmgpu_server_drain": ([VP, C.c_double], C.c_int),
+        "mpmgpu_server_release": ([VP, C.c_int64], C.c_int),
+        "mpmgpu_server_stats": ([VP, P(abi.MpmGpuServerStats)], C.c_int),
+        "mpmgpu_server_last_error": ([VP], C.c_char_p),
+        "mpmgpu_server_destroy": ([VP], None),
     }
     for f, (args, res) in batch_sigs.items():
         getattr(L, f).argtypes = args
@@ -282,6 +292,79 @@ class GpuBatch:
     def close(self):
         if getattr(self, "h", None):
             lib().mpmgpu_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+class GpuServer:
+    """Continuous-batching request loop on the current GPU (mpmgpu_server_*):
+    a C++ thread admits submitted runs against the HBM budget, advances all
+    admitted runs together and retires them as they finish.  Each request's
+    particle state is a private copy that receives the result."""
+
+    def __init__(self, method: int, shape: int, precision: int = 1, *, hbm_budget_bytes: int,
+                 max_runs: int = 256, steps_per_round: int = 10, backfill: bool = True, sort_interval: int = 1,
+                 block: int = 0, frac_3d: float = 0.5, nodes_per_particle: float = 0.5, fraction_usf: float = 0.5):
+        L = lib()
+        o = abi.MpmGpuServerOptions(method, shape, precision, max_runs, steps_per_round, 1 if backfill else 0,
+                                    sort_interval, block, int(hbm_budget_bytes), frac_3d, nodes_per_particle,
+                                    fraction_usf)
+        h = C.c_void_p()
+        st = L.mpmgpu_server_create(C.byref(o), C.byref(h))
+        if st != 0:
+            raise GpuError(st, L.mpmgpu_server_last_error(None).decode())
+        self.h = h
+        self._held = {}
+
+    def _check(self, st):
+        if st != 0:
+            raise GpuError(st, lib().mpmgpu_server_last_error(self.h).decode())
+
+    def submit(self, model: Model, particles: dict | None = None, nsteps: int | None = None) -> int:
+        b = abi.Bound()
+        g = abi.grid_struct(model, b)
+        bcs, nbc = abi.bcs_array(model)
+        state = abi.copy_particles(particles if particles is not None else model.particles)
+        ps = abi.particles_struct(state, b)
+        rid = C.c_int64(-1)
+        self._check(lib().mpmgpu_server_submit(self.h, C.byref(g), abi.materials_array(model), len(model.materials),
+                                               bcs, nbc, C.byref(ps), float(model.options["timestep"]),
+                                               int(nsteps if nsteps is not None else model.nsteps), C.byref(rid)))
+        self._held[rid.value] = (state, b, ps)
+        return rid.value
+
+    def poll(self, rid: int) -> dict:
+        i = abi.MpmGpuRequestInfo()
+        self._check(lib().mpmgpu_server_poll(self.h, rid, C.byref(i)))
+        return {f: getattr(i, f) for f, _ in abi.MpmGpuRequestInfo._fields_ if f != "pad"}
+
+    def wait(self, rid: int, timeout: float = 600.0) -> int:
+        """Status of the request once done or failed (TIMEOUT after `timeout` s)."""
+        return lib().mpmgpu_server_wait(self.h, rid, float(timeout))
+
+    def drain(self, timeout: float = 3600.0):
+        self._check(lib().mpmgpu_server_drain(self.h, float(timeout)))
+
+    def result(self, rid: int) -> dict:
+        return self._held[rid][0]
+
+    def release(self, rid: int):
+        self._check(lib().mpmgpu_server_release(self.h, rid))
+        self._held.pop(rid, None)
+
+    def stats(self) -> dict:
+        s = abi.MpmGpuServerStats()
+        self._check(lib().mpmgpu_server_stats(self.h, C.byref(s)))
+        return {f: getattr(s, f) for f, _ in abi.MpmGpuServerStats._fields_}
+
+    def close(self):
+        if getattr(self, "h", None):
+            lib().mpmgpu_server_destroy(self.h)
             self.h = None
 
     def __del__(self):

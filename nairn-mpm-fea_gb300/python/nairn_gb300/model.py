@@ -379,3 +379,108 @@ def batch_run_params(count=512, seed=2024, nmin=2000, nmax=200000, steps=500, ce
 def batch_models(count=512, seed=2024, **kw) -> list:
     """The Models of batch_run_params (same arguments)."""
     return [block_2d(**p) for p in batch_run_params(count=count, seed=seed, **kw)]
+
+
+def block_3d(ncx=8, ncy=8, ncz=8, cell=1.0, ppc_side=2, mat=None, vel=(0., 0., 0., 0., -1000., 0., 0., 0., 0.),
+             fixed_base=False, steps=500, cfl=0.5, gimp="uGIMP", method=USAVG, margin_cells=4,
+             name="block_3d", **_ignored) -> Model:
+    """3D box of ncx x ncy x ncz cells (ppc_side^3 points per cell) with the
+    initial velocity field
+
+        vx = a0 + a1*sin(pi*z/Lz + pa),  vy = b0 + b1*sin(pi*x/Lx + pb),  vz = c0 + c1*sin(pi*y/Ly + pc)
+
+    given as vel = (a0, a1, pa, b0, b1, pb, c0, c1, pc); optionally the base
+    plane z = 0 held at zero z velocity (a rigid wall, as in taylor_3d)."""
+    from . import inputs
+    shape = GIMP_NAMES[gimp]
+    Lx, Ly, Lz, m = ncx * cell, ncy * cell, ncz * cell, margin_cells * cell
+    g = make_grid(3, (-m, Lx + m), (-m, Ly + m), (-m, Lz + m), cell)
+    pos, elem = _element_points(g, ppc_side)
+    inside = ((pos[:, 0] <= Lx) & (pos[:, 0] >= 0.) & (pos[:, 1] <= Ly) & (pos[:, 1] >= 0.)
+              & (pos[:, 2] <= Lz) & (pos[:, 2] >= 0.))
+    mat = dict(mat) if mat is not None else dict(type=MAT_ISO, field=0, rho=1.0, E=1000., nu=0.33, yield_=0.,
+                                                 Ep=0., G=0., K=0., UJOption=0)
+    p = _new_particles(pos[inside], elem[inside], g, ppc_side, mat["rho"], 1.0)
+    a0, a1, pa, b0, b1, pb, c0, c1, pc = vel
+    p["vx"][:] = a0 + a1 * np.sin(math.pi * p["z"] / Lz + pa)
+    p["vy"][:] = b0 + b1 * np.sin(math.pi * p["x"] / Lx + pb)
+    p["vz"][:] = c0 + c1 * np.sin(math.pi * p["y"] / Ly + pc)
+    bcs = np.zeros(0, dtype=BC_DTYPE)
+    if fixed_base:
+        ids = np.arange(1, g.nnodes + 1)
+        plane = (g.nx + 1) * (g.ny + 1)
+        ndz = g.znodes[(ids - 1) // plane]
+        nodes = ids[(ndz <= 0.01 * cell) & (ndz >= -0.01 * cell)]
+        bcs = np.zeros(nodes.size, dtype=BC_DTYPE)
+        bcs["node"] = nodes
+        bcs["dir"] = 4
+    c = inputs.iso_wave_speed(mat["E"], mat["nu"], mat["rho"])
+    dt = inputs.cfl_timestep(g.dx, c, cfl)
+    opts = dict(np=THREED, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
+                inc_defgrad_terms=1, nfields=1)
+    return Model(g, p, [mat], bcs, opts, steps, name=name)
+
+
+def _random_material(rng):
+    """Material of the batched and served populations: 50/50 linear elastic or
+    von Mises with linear hardening, E log-uniform 0.1-200 GPa, nu 0.2-0.45,
+    yield 0.1-1 % of E, tangent modulus 0.1-5 % of E, density 1-8 g/cm^3."""
+    E = math.exp(rng.uniform(math.log(100.), math.log(200000.)))
+    nu = rng.uniform(0.2, 0.45)
+    rho = rng.uniform(1., 8.)
+    plastic = rng.uniform() < 0.5
+    return dict(type=MAT_PLASTIC if plastic else MAT_ISO, field=0, rho=rho, E=E, nu=nu,
+                yield_=rng.uniform(0.001, 0.01) * E if plastic else 0.,
+                Ep=rng.uniform(0.001, 0.05) * E if plastic else 0., G=0., K=0., UJOption=0)
+
+
+def serve_request_params(count=200, seed=77, rate=20.0, nmin=10000, nmax=2000000, smin=200, smax=2000,
+                         cell=1.0, ppc_side=2):
+    """Seeded request stream of independent runs: Poisson arrivals at `rate`
+    per second, 50/50 2D plane strain or 3D, particle counts log-uniform in
+    [nmin, nmax], step counts uniform in [smin, smax], materials as the batched
+    population, velocity amplitude 0.1-10 m/s.  Returns (arrival_s, dim,
+    kwargs of block_2d / block_3d) per request."""
+    from . import inputs
+    rng = np.random.default_rng(seed)
+    t = 0.
+    out = []
+    for k in range(count):
+        t += rng.exponential(1. / rate)
+        dim = 3 if rng.uniform() < 0.5 else 2
+        n = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        steps = int(rng.integers(smin, smax + 1))
+        mat = _random_material(rng)
+        amp = 1000. * rng.uniform(0.1, 10.)
+        dt = inputs.cfl_timestep(cell, inputs.iso_wave_speed(mat["E"], mat["nu"], mat["rho"]), 0.4 if dim == 2 else 0.5)
+        margin = 3 + int(math.ceil(amp * dt * steps / cell))
+        if dim == 2:
+            cells = max(n / ppc_side ** 2, 9.)
+            aspect = math.exp(rng.uniform(0., math.log(4.)))
+            ncy = max(3, int(round(math.sqrt(cells / aspect))))
+            ncx = max(3, int(round(cells / ncy)))
+            w = rng.uniform(-1., 1., 4)
+            w = w / np.abs(w).sum()
+            vel = (amp * w[0], amp * w[1], rng.uniform(0., 2. * math.pi), amp * w[2], amp * w[3],
+                   rng.uniform(0., 2. * math.pi))
+            kw = dict(ncx=ncx, ncy=ncy, cell=cell, ppc_side=ppc_side, mat=mat, vel=vel, fixed_left=(k % 2 == 1),
+                      steps=steps, cfl=0.4, margin_cells=margin, name=f"req{seed}_{k}_2d")
+        else:
+            cells = max(n / ppc_side ** 3, 27.)
+            side = cells ** (1. / 3.)
+            ncx = max(3, int(round(side * math.exp(rng.uniform(-0.3, 0.3)))))
+            ncy = max(3, int(round(side * math.exp(rng.uniform(-0.3, 0.3)))))
+            ncz = max(3, int(round(cells / (ncx * ncy))))
+            w = rng.uniform(-1., 1., 6)
+            w = w / np.abs(w).sum()
+            vel = (amp * w[0], amp * w[1], rng.uniform(0., 2. * math.pi), amp * w[2], amp * w[3],
+                   rng.uniform(0., 2. * math.pi), amp * w[4], amp * w[5], rng.uniform(0., 2. * math.pi))
+            kw = dict(ncx=ncx, ncy=ncy, ncz=ncz, cell=cell, ppc_side=ppc_side, mat=mat, vel=vel,
+                      fixed_base=(k % 2 == 1), steps=steps, cfl=0.5, margin_cells=margin, name=f"req{seed}_{k}_3d")
+        out.append((t, dim, kw))
+    return out
+
+
+def serve_models(params) -> list:
+    """Models of serve_request_params entries."""
+    return [block_3d(**kw) if dim == 3 else block_2d(**kw) for _, dim, kw in params]

@@ -61,3 +61,38 @@ def test_block_model_is_consistent():
     assert np.all((g.xnodes[col] <= m.particles["x"]) & (m.particles["x"] < g.xnodes[col + 1]))
     assert np.all((g.ynodes[row] <= m.particles["y"]) & (m.particles["y"] < g.ynodes[row + 1]))
     assert len(m.bcs) == 2 * 5 and set(m.bcs["dir"]) == {1, 2}
+
+
+def test_server_create_rejects_bad_options_without_gpu_work(gpu_lib):
+    from nairn_gb300 import abi, model
+    for budget, runs, frac in ((0, 8, 0.5), (1 << 30, 0, 0.5), (1 << 30, 8, 1.5)):
+        o = abi.MpmGpuServerOptions(model.USAVG, model.SHAPE_UGIMP, 1, runs, 10, 1, 1, 0, budget, frac, 0.5, 0.5)
+        h = C.c_void_p()
+        assert gpu_lib.mpmgpu_server_create(C.byref(o), C.byref(h)) == 1
+        assert not h.value and gpu_lib.mpmgpu_server_last_error(None)
+
+
+def test_served_stream_is_seeded_and_matches_the_spec():
+    from nairn_gb300 import model
+    ps = model.serve_request_params(200, seed=77)
+    assert ps == model.serve_request_params(200, seed=77)
+    t = np.array([p[0] for p in ps])
+    assert np.all(np.diff(t) > 0) and 6. < t[-1] < 14.  # Poisson, 20 per second
+    dims = [p[1] for p in ps]
+    assert 70 < dims.count(3) < 130
+    n = np.array([kw["ncx"] * kw["ncy"] * (kw["ncz"] * 8 if d == 3 else 4) for _, d, kw in ps])
+    assert n.min() >= 9000 and n.max() <= 2.2e6 and 2e5 < n.mean() < 6e5
+    steps = np.array([kw["steps"] for _, _, kw in ps])
+    assert steps.min() >= 200 and steps.max() <= 2000
+
+
+def test_block_3d_model_is_consistent():
+    from nairn_gb300 import model
+    m = model.block_3d(ncx=4, ncy=3, ncz=5, fixed_base=True)
+    assert m.n == 4 * 3 * 5 * 8
+    g = m.grid
+    e = m.particles["elem"]
+    col, row, lay = e % g.nx, (e // g.nx) % g.ny, e // (g.nx * g.ny)
+    for c, ax, nodes in ((col, "x", g.xnodes), (row, "y", g.ynodes), (lay, "z", g.znodes)):
+        assert np.all((nodes[c] <= m.particles[ax]) & (m.particles[ax] < nodes[c + 1]))
+    assert len(m.bcs) == (g.nx + 1) * (g.ny + 1) and set(m.bcs["dir"]) == {4}
