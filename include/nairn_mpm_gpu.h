@@ -292,7 +292,8 @@ typedef struct {
 int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *opts);
 int mpmgpu_batch_create(const MpmGpuBatchOptions *opts, MpmGpuBatch **out);
 /* Admit one run; *run_id receives its slot.  MPMGPU_ERR_BUSY: not enough free
- * run slots, particles, nodes or material slots now (retry after removals). */
+ * run slots, particles, nodes or material slots now (retry after removals);
+ * MPMGPU_ERR_OOM: the run is larger than the batch's capacities. */
 int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
                          const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuParticles *p, double timestep,
                          int32_t nsteps, int32_t *run_id);
@@ -339,6 +340,12 @@ typedef struct {
     double frac_3d;             /* share of the budget for 3D runs (0..1)      */
     double nodes_per_particle;  /* node slots per particle slot (0: 0.5)       */
     double fraction_usf;        /* USAVG split (0 -> 0.5)                      */
+    int64_t max_resident_particles; /* admit while the running runs hold fewer
+                                   particles than this (0: no cap); a request
+                                   is always admitted when nothing runs      */
+    int32_t order;              /* admission order: 0 arrival (FIFO), 1 least
+                                   work first (particles x steps)            */
+    int32_t pad;
 } MpmGpuServerOptions;
 
 enum { MPMGPU_REQ_QUEUED = 1, MPMGPU_REQ_RUNNING = 2, MPMGPU_REQ_DONE = 3, MPMGPU_REQ_FAILED = 4 };

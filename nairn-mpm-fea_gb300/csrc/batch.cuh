@@ -645,8 +645,8 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
                     "position, velocity, mass, size, material and element columns are required");
     const long long nnodes = (long long)(grid->nx + 1) * (grid->ny + 1) * (b->dim == 3 ? grid->nz + 1 : 1);
     const long long nelems = (long long)grid->nx * grid->ny * (b->dim == 3 ? grid->nz : 1);
-    if (h->n > b->pcap) return berr(b, MPMGPU_ERR_INVALID, "run has more particles than the batch capacity");
-    if (nnodes > b->ncap) return berr(b, MPMGPU_ERR_INVALID, "run has more nodes than the batch capacity");
+    if (h->n > b->pcap) return berr(b, MPMGPU_ERR_OOM, "run has more particles than the batch capacity");
+    if (nnodes > b->ncap) return berr(b, MPMGPU_ERR_OOM, "run has more nodes than the batch capacity");
     const int np = (int)h->n;
     for (int k = 0; k < nbc; k++) {
         if (bcs[k].node < 1 || bcs[k].node > nnodes)

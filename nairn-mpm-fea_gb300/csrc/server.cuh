@@ -104,11 +104,25 @@ void server_admit(MpmGpuServer *s, std::vector<ServerRequest *> &admitted, std::
         std::lock_guard<std::mutex> lk(s->mu);
         cand.assign(s->queue.begin(), s->queue.end());
     }
+    if (s->o.order == 1)
+        std::stable_sort(cand.begin(), cand.end(), [](const ServerRequest *a, const ServerRequest *b) {
+            return (double)a->p.n * a->nsteps < (double)b->p.n * b->nsteps;
+        });
+    int64_t resident = 0;
+    for (int d = 0; d < 2; d++)
+        for (const ServerRequest *q : s->running[d]) resident += q->p.n;
     bool blocked[2] = {false, false};
+    bool capped = false;
     for (ServerRequest *q : cand) {
         const int d = q->dim == 3 ? 1 : 0;
         MpmGpuBatch *b = s->batch[d];
         if (blocked[d]) continue;
+        if (s->o.max_resident_particles > 0 && resident > 0 && resident + q->p.n > s->o.max_resident_particles) {
+            // over the resident cap: wait (or let a smaller later request pass)
+            if (!s->o.backfill) capped = true;
+            if (capped) break;
+            continue;
+        }
         int32_t rid = -1;
         const int st = mpmgpu_batch_add_run(b, &q->grid, q->mats.data(), (int32_t)q->mats.size(),
                                             q->bcs.empty() ? nullptr : q->bcs.data(), (int32_t)q->bcs.size(), &q->p,
@@ -117,6 +131,7 @@ void server_admit(MpmGpuServer *s, std::vector<ServerRequest *> &admitted, std::
             q->run_id = rid;
             q->t_admit = ServerClock::now();
             admitted.push_back(q);
+            resident += q->p.n;
         } else if (st == MPMGPU_ERR_BUSY) {
             MpmGpuBatchInfo bi{};
             mpmgpu_batch_info(b, &bi);

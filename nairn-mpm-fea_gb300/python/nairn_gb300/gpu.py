@@ -309,11 +309,13 @@ class GpuServer:
 
     def __init__(self, method: int, shape: int, precision: int = 1, *, hbm_budget_bytes: int,
                  max_runs: int = 256, steps_per_round: int = 10, backfill: bool = True, sort_interval: int = 1,
-                 block: int = 0, frac_3d: float = 0.5, nodes_per_particle: float = 0.5, fraction_usf: float = 0.5):
+                 block: int = 0, frac_3d: float = 0.5, nodes_per_particle: float = 0.5, fraction_usf: float = 0.5,
+                 max_resident_particles: int = 0, order: str = "fifo"):
         L = lib()
         o = abi.MpmGpuServerOptions(method, shape, precision, max_runs, steps_per_round, 1 if backfill else 0,
                                     sort_interval, block, int(hbm_budget_bytes), frac_3d, nodes_per_particle,
-                                    fraction_usf)
+                                    fraction_usf, int(max_resident_particles),
+                                    {"fifo": 0, "least_work": 1}[order], 0)
         h = C.c_void_p()
         st = L.mpmgpu_server_create(C.byref(o), C.byref(h))
         if st != 0:

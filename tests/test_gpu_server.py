@@ -117,3 +117,27 @@ def test_wait_times_out_and_release_needs_completion(gpu_lib):
     assert s.wait(rid, 600) == 0
     s.release(rid)
     s.close()
+
+
+def test_resident_cap_serialises_runs(gpu_lib):
+    """With a resident-particle cap below any request, runs go one at a time
+    (least work first once queued); results are unchanged."""
+    from nairn_gb300 import abi
+    ms = requests(5, seed=31, smin=10, smax=20)
+    s = server(0, max_resident_particles=1, order="least_work")
+    t0 = time.perf_counter()
+    ids, sub = [], []
+    for m in ms:
+        sub.append(1e3 * (time.perf_counter() - t0))
+        ids.append(s.submit(m))
+    s.drain(600)
+    spans = []
+    for rid, m, ts in zip(ids, ms, sub):
+        info = s.poll(rid)
+        assert info["state"] == abi.REQ_DONE
+        spans.append((ts + info["queue_ms"], ts + info["total_ms"]))
+        check(s.result(rid), oracle(m), m.grid.dim, TOL, m.name)
+    spans.sort()
+    for (a0, a1), (b0, b1) in zip(spans, spans[1:]):
+        assert b0 >= a1 - 1.0, spans  # no two runs resident at once (1 ms clock slack)
+    s.close()
