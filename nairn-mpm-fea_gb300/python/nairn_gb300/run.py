@@ -1,0 +1,75 @@
+"""Run one synthetic workload on the GPU through the C ABI and print its timing.
+
+    python -m nairn_gb300.run taylor --precision mixed --steps 4
+    python -m nairn_gb300.run cantilever --nx 100 --ny 20 --steps 200
+    python -m nairn_gb300.run batch --runs 64 --steps 20
+
+Workloads: `cantilever` (2D elastic beam), `taylor` (3D elastic-plastic
+Taylor impact), `block2d` / `block3d` (one block of the batched population's
+form), `batch` (the first --runs runs of the seeded 512-run 2D population in
+one batch).  Used for profiling single kernels and for quick checks; the
+measurement of record is bench.py.
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import sys
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, os.path.dirname(HERE))
+
+
+def main(argv=None):
+    ap = argparse.ArgumentParser(prog="python -m nairn_gb300.run")
+    ap.add_argument("workload", choices=("cantilever", "taylor", "block2d", "block3d", "batch"))
+    ap.add_argument("--precision", choices=("fp64", "mixed"), default="fp64")
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=2)
+    ap.add_argument("--sort-interval", type=int, default=1)
+    ap.add_argument("--nx", type=int, default=100)
+    ap.add_argument("--ny", type=int, default=20)
+    ap.add_argument("--radius", type=float, default=5.0)
+    ap.add_argument("--length", type=float, default=25.0)
+    ap.add_argument("--cell", type=float, default=0.25)
+    ap.add_argument("--cells", type=int, default=64, help="block edge in cells (block2d/block3d)")
+    ap.add_argument("--runs", type=int, default=64, help="runs of the batch workload")
+    a = ap.parse_args(argv)
+    from nairn_gb300 import gpu, model
+    prec = 1 if a.precision == "mixed" else 0
+    total = a.steps + a.warmup
+    if a.workload == "batch":
+        ms = model.batch_models(512, seed=2024)[:a.runs]
+        b = gpu.GpuBatch.for_models(ms, precision=prec, sort_interval=a.sort_interval)
+        for m in ms:
+            b.add(m)
+        b.step(a.warmup)
+        t = b.step_timed(a.steps)
+        n = sum(m.n for m in ms)
+        out = {"workload": "batch", "runs": len(ms), "particles": n, "ms_per_step": t / a.steps,
+               "particle_steps_per_s": n * a.steps / (t / 1e3), "info": b.info()}
+        b.close()
+    else:
+        if a.workload == "cantilever":
+            m = model.cantilever_2d(nx=a.nx, ny=a.ny, steps=total)
+        elif a.workload == "taylor":
+            m = model.taylor_3d(radius=a.radius, length=a.length, cell=a.cell, steps=total)
+        elif a.workload == "block2d":
+            m = model.block_2d(ncx=a.cells, ncy=a.cells, steps=total)
+        else:
+            m = model.block_3d(ncx=a.cells, ncy=a.cells, ncz=a.cells, steps=total)
+        r = gpu.GpuRun(m, precision=prec, sort_interval=a.sort_interval)
+        r.upload(m.particles)
+        r.step(a.warmup)
+        t = r.step_timed(a.steps)
+        out = {"workload": m.name, "particles": m.n, "ms_per_step": t / a.steps,
+               "particle_steps_per_s": m.n * a.steps / (t / 1e3), "launches": r.launch_count()}
+        r.close()
+    out["precision"] = a.precision
+    print(json.dumps(out))
+    return 0
+
+
+if __name__ == "__main__":
+    sys.exit(main())
