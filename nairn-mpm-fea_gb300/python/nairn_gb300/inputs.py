@@ -24,6 +24,30 @@ def iso_wave_speed(E_mpa: float, nu: float, rho_gcc: float) -> float:
     return math.sqrt(2. * G * (1. - nu) / (rho * (1. - 2. * nu)))
 
 
+def neo_wave_speed(G_mpa: float, K_mpa: float, rho_gcc: float) -> float:
+    """Neohookean::WaveSpeed (NairnMPM/src/Materials/Neohookean.cpp:359), mm/s."""
+    return math.sqrt((K_mpa * 1.e6 + 4. * G_mpa * 1.e6 / 3.) / (rho_gcc * 0.001))
+
+
+def wave_speed(mat_type: int, rho: float, E: float = 0., nu: float = 0., G: float = 0., K: float = 0.) -> float:
+    return neo_wave_speed(G, K, rho) if mat_type == 28 else iso_wave_speed(E, nu, rho)
+
+
+def material_xml(mat_type: int, name: str, rho: float, E: float = 0., nu: float = 0., yield_: float = 0.,
+                 Ep: float = 0., G: float = 0., K: float = 0., uj: int = 0) -> str:
+    """<Material> block of type 1 (IsotropicMat), 9 (IsoPlasticity with linear
+    hardening) or 28 (Neohookean, G and K input, U(J) option uj)."""
+    body = f"    <rho>{_fmt(rho)}</rho>\n"
+    if mat_type == 28:
+        body += f"    <G>{_fmt(G)}</G>\n    <K>{_fmt(K)}</K>\n    <UJOption>{int(uj)}</UJOption>\n"
+    else:
+        body += f"    <E>{_fmt(E)}</E>\n    <nu>{_fmt(nu)}</nu>\n"
+    body += "    <alpha>0</alpha>\n"
+    if mat_type == 9:
+        body += f"    <yield>{_fmt(yield_)}</yield>\n    <Ep>{_fmt(Ep)}</Ep>\n"
+    return f'  <Material Type="{mat_type}" Name="{name}">\n{body}  </Material>\n'
+
+
 def cfl_timestep(cell_mm: float, wave_speed: float, cfl: float) -> float:
     """Time step of NairnMPM::CFLTimeStep (NairnMPM.cpp:1207-1240), seconds."""
     return cfl * (cell_mm / wave_speed)
@@ -34,7 +58,9 @@ def _fmt(v: float) -> str:
 
 
 def _header(analysis: int, method: int, gimp: str, maxtime_s: float, cfl: float,
-            archive_root: str, ppe: int, order: str) -> str:
+            archive_root: str, ppe: int, order: str, inc_terms: int = 0) -> str:
+    # <DefGradTerms> sets MaterialBase::incrementalDefGradTerms (MPMReadHandler.cpp:492-495)
+    terms = f"    <DefGradTerms>{int(inc_terms)}</DefGradTerms>\n" if inc_terms > 0 else ""
     return f"""<?xml version='1.0'?>
 <!DOCTYPE JANFEAInput SYSTEM "NairnMPM.dtd">
 <JANFEAInput version='3'>
@@ -51,7 +77,7 @@ def _header(analysis: int, method: int, gimp: str, maxtime_s: float, cfl: float,
     <ArchiveTime units="ms">{_fmt(maxtime_s * 1.e3 * 10.)}</ArchiveTime>
     <ArchiveRoot>{archive_root}</ArchiveRoot>
     <MPMArchiveOrder>{order}</MPMArchiveOrder>
-  </MPMHeader>
+{terms}  </MPMHeader>
 """
 
 
@@ -63,16 +89,18 @@ ARCHIVE_ORDER = "iYYYYYNYNYNNNYNNNN"
 def cantilever_2d(nx: int = 100, ny: int = 20, cell: float = 1.0, ppc_side: int = 2,
                   E: float = 1000., nu: float = 0.33, rho: float = 1.0, v0: float = 1000.,
                   steps: int = 1000, cfl: float = 0.4, gimp: str = "uGIMP", method: int = 2,
-                  margin_cells: int = 4, archive_root: str = "Results/cant.") -> tuple[str, dict]:
+                  margin_cells: int = 4, archive_root: str = "Results/cant.", mat_type: int = 1,
+                  G: float = 0., K: float = 0., uj: int = 0, inc_terms: int = 0) -> tuple[str, dict]:
     """2D plane-strain cantilever of nx*ny cells, left edge fixed, initial
-    v_y = v0*sin(pi*x/(2L)) (mm/s).  Returns (xml, info)."""
+    v_y = v0*sin(pi*x/(2L)) (mm/s); elastic (mat_type 1, E and nu) or
+    Neo-Hookean (mat_type 28, G and K).  Returns (xml, info)."""
     L = nx * cell
     H = ny * cell
-    c = iso_wave_speed(E, nu, rho)
+    c = wave_speed(mat_type, rho, E=E, nu=nu, G=G, K=K)
     dt = cfl_timestep(cell, c, cfl)
     maxtime = (steps - 0.5) * dt
     m = margin_cells * cell
-    xml = _header(10, method, gimp, maxtime, cfl, archive_root, ppc_side * ppc_side, ARCHIVE_ORDER)
+    xml = _header(10, method, gimp, maxtime, cfl, archive_root, ppc_side * ppc_side, ARCHIVE_ORDER, inc_terms)
     xml += f"""  <Mesh output="file">
     <Grid xmin="{_fmt(-m)}" xmax="{_fmt(L + m)}" ymin="{_fmt(-m)}" ymax="{_fmt(H + m)}" thickness="1">
       <Horiz cellsize="{_fmt(cell)}"/>
@@ -86,13 +114,7 @@ def cantilever_2d(nx: int = 100, ny: int = 20, cell: float = 1.0, ppc_side: int 
       <Rect xmin="0" xmax="{_fmt(L)}" ymin="0" ymax="{_fmt(H)}"/>
     </Body>
   </MaterialPoints>
-  <Material Type="1" Name="beam">
-    <rho>{_fmt(rho)}</rho>
-    <E>{_fmt(E)}</E>
-    <nu>{_fmt(nu)}</nu>
-    <alpha>0</alpha>
-  </Material>
-  <GridBCs>
+{material_xml(mat_type, "beam", rho, E=E, nu=nu, G=G, K=K, uj=uj)}  <GridBCs>
     <BCLine x1="0" y1="{_fmt(-0.5 * cell)}" x2="0" y2="{_fmt(H + 0.5 * cell)}" tolerance="{_fmt(0.01)}">
       <DisBC dir="1" disp="0"/>
       <DisBC dir="2" disp="0"/>
@@ -107,15 +129,17 @@ def taylor_3d(radius: float = 5.0, length: float = 25.0, cell: float = 0.25, ppc
               v0: float = -200000., E: float = 200000., nu: float = 0.3, yield_: float = 300.,
               Ep: float = 2000., rho: float = 7.8, steps: int = 2000, cfl: float = 0.5,
               gimp: str = "uGIMP", method: int = 2, lateral_margin: float | None = None,
-              archive_root: str = "Results/taylor.") -> tuple[str, dict]:
+              archive_root: str = "Results/taylor.", mat_type: int = 9, G: float = 0., K: float = 0.,
+              uj: int = 0, inc_terms: int = 0) -> tuple[str, dict]:
     """3D Taylor impact: cylinder along z from z=0 to z=length moving at v0
-    (mm/s) onto a rigid wall at z=0 (zero z-velocity on the z=0 node plane)."""
-    c = iso_wave_speed(E, nu, rho)
+    (mm/s) onto a rigid wall at z=0 (zero z-velocity on the z=0 node plane);
+    von Mises (mat_type 9), elastic (1) or Neo-Hookean (28)."""
+    c = wave_speed(mat_type, rho, E=E, nu=nu, G=G, K=K)
     dt = cfl_timestep(cell, c, cfl)
     maxtime = (steps - 0.5) * dt
     lm = lateral_margin if lateral_margin is not None else max(4 * cell, 0.8 * radius)
     xr = radius + lm
-    xml = _header(12, method, gimp, maxtime, cfl, archive_root, ppc_side ** 3, ARCHIVE_ORDER)
+    xml = _header(12, method, gimp, maxtime, cfl, archive_root, ppc_side ** 3, ARCHIVE_ORDER, inc_terms)
     xml += f"""  <Mesh output="file">
     <Grid xmin="{_fmt(-xr)}" xmax="{_fmt(xr)}" ymin="{_fmt(-xr)}" ymax="{_fmt(xr)}" zmin="{_fmt(-4 * cell)}" zmax="{_fmt(length + 4 * cell)}">
       <Horiz cellsize="{_fmt(cell)}"/>
@@ -128,15 +152,7 @@ def taylor_3d(radius: float = 5.0, length: float = 25.0, cell: float = 0.25, ppc
       <Cylinder xmin="{_fmt(-radius)}" xmax="{_fmt(radius)}" ymin="{_fmt(-radius)}" ymax="{_fmt(radius)}" zmin="0" zmax="{_fmt(length)}" axis="z"/>
     </Body>
   </MaterialPoints>
-  <Material Type="9" Name="steel">
-    <rho>{_fmt(rho)}</rho>
-    <E>{_fmt(E)}</E>
-    <nu>{_fmt(nu)}</nu>
-    <alpha>0</alpha>
-    <yield>{_fmt(yield_)}</yield>
-    <Ep>{_fmt(Ep)}</Ep>
-  </Material>
-  <GridBCs>
+{material_xml(mat_type, "bar", rho, E=E, nu=nu, yield_=yield_, Ep=Ep, G=G, K=K, uj=uj)}  <GridBCs>
     <BCBox xmin="{_fmt(-xr - cell)}" xmax="{_fmt(xr + cell)}" ymin="{_fmt(-xr - cell)}" ymax="{_fmt(xr + cell)}" zmin="{_fmt(-0.01 * cell)}" zmax="{_fmt(0.01 * cell)}">
       <DisBC dir="3" disp="0"/>
     </BCBox>

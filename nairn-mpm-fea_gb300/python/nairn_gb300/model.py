@@ -209,8 +209,26 @@ GIMP_NAMES = {"Classic": SHAPE_LINEAR, "Dirac": SHAPE_LINEAR, "uGIMP": SHAPE_UGI
               "lCPDI": SHAPE_LCPDI, "CPDI": SHAPE_LCPDI}
 
 
+def _material(mat_type, rho, E=0., nu=0., yield_=0., Ep=0., G=0., K=0., uj=0):
+    return dict(type=mat_type, field=0, rho=rho, E=E if mat_type != MAT_NEOHOOKEAN else 0.,
+                nu=nu if mat_type != MAT_NEOHOOKEAN else 0., yield_=yield_ if mat_type == MAT_PLASTIC else 0.,
+                Ep=Ep if mat_type == MAT_PLASTIC else 0., G=G if mat_type == MAT_NEOHOOKEAN else 0.,
+                K=K if mat_type == MAT_NEOHOOKEAN else 0., UJOption=uj if mat_type == MAT_NEOHOOKEAN else 0)
+
+
+def _initial_material_state(p, mat):
+    """MaterialBase::SetInitialParticleState / InitHistoryData of the material:
+    hyperelastic B = I in the plastic-strain slot (HyperElastic.cpp:45-53),
+    Neohookean history J = Jres = 1 (Neohookean.cpp:151-156)."""
+    if mat["type"] == MAT_NEOHOOKEAN:
+        sel = p["mat"] == 0 if "mat" in p else slice(None)
+        for k in ("pxx", "pyy", "pzz", "hist0", "hist1"):
+            p[k][sel] = 1.
+
+
 def cantilever_2d(nx=100, ny=20, cell=1.0, ppc_side=2, E=1000., nu=0.33, rho=1.0, v0=1000.,
-                  steps=1000, cfl=0.4, gimp="uGIMP", method=USAVG, margin_cells=4, **_ignored) -> Model:
+                  steps=1000, cfl=0.4, gimp="uGIMP", method=USAVG, margin_cells=4, mat_type=MAT_ISO,
+                  G=0., K=0., uj=0, inc_terms=0, **_ignored) -> Model:
     """Model of inputs.cantilever_2d (same arguments)."""
     from . import inputs
     shape = GIMP_NAMES[gimp]
@@ -221,7 +239,8 @@ def cantilever_2d(nx=100, ny=20, cell=1.0, ppc_side=2, E=1000., nu=0.33, rho=1.0
     p = _new_particles(pos[inside], elem[inside], g, ppc_side, rho, 1.0)
     # <vel0Y> expression v0*sin(pi*x/(2*L)) (Expression.cpp evaluates left to right)
     p["vy"][:] = v0 * np.sin(math.pi * p["x"] / (2. * L))
-    mats = [dict(type=MAT_ISO, field=0, rho=rho, E=E, nu=nu, yield_=0., Ep=0., G=0., K=0., UJOption=0)]
+    mats = [_material(mat_type, rho, E=E, nu=nu, G=G, K=K, uj=uj)]
+    _initial_material_state(p, mats[0])
     # BCLine x=0 from y=-cell/2 to H+cell/2 (LineController::ContainsPoint with the
     # 2D tolerance test); node order is increasing node number, one DisBC at a time
     nn = g.nnodes
@@ -235,10 +254,10 @@ def cantilever_2d(nx=100, ny=20, cell=1.0, ppc_side=2, E=1000., nu=0.33, rho=1.0
     bcs["dir"][:nodes.size] = 1
     bcs["node"][nodes.size:] = nodes
     bcs["dir"][nodes.size:] = 2
-    c = inputs.iso_wave_speed(E, nu, rho)
+    c = inputs.wave_speed(mat_type, rho, E=E, nu=nu, G=G, K=K)
     dt = inputs.cfl_timestep(g.dx, c, cfl)  # MeshInfo::GetMinCellDimension: grid.x for square grids
     opts = dict(np=PLANE_STRAIN, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
-                inc_defgrad_terms=2, nfields=1)
+                inc_defgrad_terms=inc_terms if inc_terms > 0 else 2, nfields=1)
     return Model(g, p, mats, bcs, opts, steps, name=f"cantilever_2d_{nx}x{ny}")
 
 
@@ -255,7 +274,7 @@ def _line_contains(x, y, x1, y1, x2, y2, tol):
 
 def taylor_3d(radius=5.0, length=25.0, cell=0.25, ppc_side=2, v0=-200000., E=200000., nu=0.3,
               yield_=300., Ep=2000., rho=7.8, steps=2000, cfl=0.5, gimp="uGIMP", method=USAVG,
-              lateral_margin=None, **_ignored) -> Model:
+              lateral_margin=None, mat_type=MAT_PLASTIC, G=0., K=0., uj=0, inc_terms=0, **_ignored) -> Model:
     """Model of inputs.taylor_3d (same arguments)."""
     from . import inputs
     shape = GIMP_NAMES[gimp]
@@ -276,7 +295,8 @@ def taylor_3d(radius=5.0, length=25.0, cell=0.25, ppc_side=2, v0=-200000., E=200
     inside = (z <= zmax) & (z >= zmin) & ((ddx * ddx / a2 + ddy * ddy / b2) <= R * R)
     p = _new_particles(pos[inside], elem[inside], g, ppc_side, rho, 1.0)
     p["vz"][:] = v0
-    mats = [dict(type=MAT_PLASTIC, field=0, rho=rho, E=E, nu=nu, yield_=yield_, Ep=Ep, G=0., K=0., UJOption=0)]
+    mats = [_material(mat_type, rho, E=E, nu=nu, yield_=yield_, Ep=Ep, G=G, K=K, uj=uj)]
+    _initial_material_state(p, mats[0])
     nn = g.nnodes
     ids = np.arange(1, nn + 1)
     plane = (g.nx + 1) * (g.ny + 1)
@@ -289,10 +309,10 @@ def taylor_3d(radius=5.0, length=25.0, cell=0.25, ppc_side=2, v0=-200000., E=200
     bcs = np.zeros(nodes.size, dtype=BC_DTYPE)
     bcs["node"] = nodes
     bcs["dir"] = 4
-    c = inputs.iso_wave_speed(E, nu, rho)
+    c = inputs.wave_speed(mat_type, rho, E=E, nu=nu, G=G, K=K)
     dt = inputs.cfl_timestep(g.dx, c, cfl)  # cubic grid: grid.x
     opts = dict(np=THREED, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
-                inc_defgrad_terms=1, nfields=1)
+                inc_defgrad_terms=inc_terms if inc_terms > 0 else 1, nfields=1)
     return Model(g, p, mats, bcs, opts, steps, name=f"taylor_3d_r{radius}_c{cell}")
 
 

@@ -42,6 +42,9 @@ typedef struct {
     double C3[6][6];            /* 3D specific stiffness                       */
     double Gred, Kred;          /* IsoPlasticity specific moduli               */
     double yldred, Epred, alphaMax, yldredMin;  /* LinearHardening             */
+    double Gpa, Kpa;            /* Neohookean moduli (Pa)                      */
+    double Gsp, Lamesp, Ksp;    /* Neohookean specific moduli (pr.Gsp, ...)    */
+    int uj;                     /* Neohookean UofJOption                       */
 } OMat;
 
 /* Elastic::SetAnalysisProps (Common/Materials/Elastic.cpp:194-330) for an
@@ -114,6 +117,18 @@ static int load_materials(const MpmGpuMaterial *in, int nmat, int np, OMat *out)
                 m->alphaMax = 1.e50;
                 if (beta < 0.) m->alphaMax = ((m->yldredMin / m->yldred) - 1.) / beta;
             }
+        } else if (m->type == MPMGPU_MAT_NEOHOOKEAN) {
+            /* Neohookean::VerifyAndLoadProperties, G and K branch (Neohookean.cpp:88-141);
+             * G and K inputs are MPa (Neohookean.cpp:67, HyperElastic.cpp:33) */
+            if (in[i].UJOption < 0 || in[i].UJOption > 2)
+                return fail(MPMGPU_ERR_INVALID, "oracle: Neohookean UJOption must be 0, 1 or 2");
+            m->Gpa = in[i].G * 1.e6;
+            m->Kpa = in[i].K * 1.e6;
+            double Lame = m->Kpa - 2. * m->Gpa / 3.;
+            m->Gsp = m->Gpa / m->rho;
+            m->Lamesp = Lame / m->rho;
+            m->Ksp = m->Lamesp + 2. * m->Gsp / 3.;
+            m->uj = in[i].UJOption;
         } else {
             return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: material type not implemented");
         }
@@ -121,8 +136,10 @@ static int load_materials(const MpmGpuMaterial *in, int nmat, int np, OMat *out)
     return MPMGPU_OK;
 }
 
-/* IsotropicMat::WaveSpeed (MoreIsotropicMat.cpp:388-395) */
+/* IsotropicMat::WaveSpeed (MoreIsotropicMat.cpp:388-395);
+ * Neohookean::WaveSpeed (Neohookean.cpp:359) */
 static double wave_speed(const OMat *m) {
+    if (m->type == MPMGPU_MAT_NEOHOOKEAN) return sqrt((m->Kpa + 4. * m->Gpa / 3.) / m->rho);
     return sqrt(2. * m->G * (1. - m->nu) / (m->rho * (1. - 2. * m->nu)));
 }
 
@@ -617,6 +634,179 @@ static void isoplastic(const OMat *m, MpmGpuParticles *p, long i, const M3 *de, 
     p->hist0[i] = alpnew;
 }
 
+/* Matrix3::Exponential (Common/System/Matrix3.cpp:312-364): dF = exp(du)
+ * truncated after kmax terms.  2D: the 2x2 Cayley-Hamilton recursion with
+ * the zz term separate; 3D: kmax 1 or 2. */
+static void mat_exp(const M3 *a, int kmax, int is3d, M3 *out) {
+    memset(out, 0, sizeof(*out));
+    const double (*m)[3] = a->m;
+    if (!is3d) {
+        if (kmax == 1) {
+            out->m[0][0] = 1. + m[0][0]; out->m[0][1] = m[0][1];
+            out->m[1][0] = m[1][0]; out->m[1][1] = 1. + m[1][1];
+            out->m[2][2] = 1. + m[2][2];
+            return;
+        }
+        double c0 = m[0][1] * m[1][0] - m[0][0] * m[1][1];
+        double c1 = m[0][0] + m[1][1];
+        double beta0 = 0., beta1 = 1., alpha0 = 1., alpha1 = 1.;
+        double betaz = m[2][2], ezz = 1. + betaz;
+        for (int k = 2; k <= kmax; k++) {
+            double factor = 1 / (double)k;
+            double temp = beta1;
+            beta1 = factor * (c1 * temp + beta0);
+            beta0 = factor * c0 * temp;
+            betaz *= factor * m[2][2];
+            alpha0 += beta0;
+            alpha1 += beta1;
+            ezz += betaz;
+        }
+        out->m[0][0] = alpha0 + alpha1 * m[0][0]; out->m[0][1] = alpha1 * m[0][1];
+        out->m[1][0] = alpha1 * m[1][0]; out->m[1][1] = alpha0 + alpha1 * m[1][1];
+        out->m[2][2] = ezz;
+        return;
+    }
+    if (kmax == 1) {
+        for (int r = 0; r < 3; r++)
+            for (int c = 0; c < 3; c++) out->m[r][c] = m[r][c] + (r == c ? 1. : 0.);
+        return;
+    }
+    double m2[3][3];
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++) {
+            m2[r][c] = 0.;
+            for (int k = 0; k < 3; k++) m2[r][c] += m[r][k] * m[k][c];
+        }
+    /* 1. + m + 0.5*m2 on the diagonal, m + 0.5*m2 off it */
+    for (int r = 0; r < 3; r++)
+        for (int c = 0; c < 3; c++)
+            out->m[r][c] = r == c ? 1. + m[r][c] + 0.5 * m2[r][c] : m[r][c] + 0.5 * m2[r][c];
+}
+
+/* product of two matrices the way Matrix3::operator*= forms it
+ * (Matrix3.cpp:920-966): the 2D formula when both are 2D, else the triple loop */
+static void mat_mul(const M3 *a, const M3 *b, int is3d, M3 *out) {
+    memset(out, 0, sizeof(*out));
+    if (!is3d) {
+        out->m[0][0] = a->m[0][0] * b->m[0][0] + a->m[0][1] * b->m[1][0];
+        out->m[0][1] = a->m[0][0] * b->m[0][1] + a->m[0][1] * b->m[1][1];
+        out->m[1][0] = a->m[1][0] * b->m[0][0] + a->m[1][1] * b->m[1][0];
+        out->m[1][1] = a->m[1][0] * b->m[0][1] + a->m[1][1] * b->m[1][1];
+        out->m[2][2] = a->m[2][2] * b->m[2][2];
+        return;
+    }
+    for (int i = 0; i < 3; i++)
+        for (int j = 0; j < 3; j++) {
+            double v = 0.;
+            for (int k = 0; k < 3; k++) v += a->m[i][k] * b->m[k][j];
+            out->m[i][j] = v;
+        }
+}
+
+/* HyperElastic::GetVolumetricTerms (HyperElastic.cpp:171-204) */
+static double volumetric_terms(int uj, double J, double Kred) {
+    if (uj == 1) return Kred * (J - 1.);
+    if (uj == 2) {
+        double Kterm = Kred * log(J);
+        return Kterm / J;
+    }
+    return 0.5 * Kred * (J - 1. / J);
+}
+
+/* Neohookean::MPMConstitutiveLaw without residual strains, thermal terms or
+ * artificial viscosity (Neohookean.cpp:177-331) with
+ * HyperElastic::IncrementDeformation (HyperElastic.cpp:104-139): F and the
+ * elastic left Cauchy-Green tensor B (held in the plastic-strain slot) are
+ * pushed forward by dF = exp(du); J and Jres are history doubles 0 and 1;
+ * the particle stress is the deviatoric Kirchhoff stress per unit initial
+ * density and the pressure is carried separately. */
+static void neohookean(const OMat *m, MpmGpuParticles *p, long i, const M3 *du, int is3d, int kterms) {
+    M3 dF, pF, F, Bold, dFB;
+    mat_exp(du, kterms, is3d, &dF);
+    memset(&pF, 0, sizeof(pF));
+    memset(&Bold, 0, sizeof(Bold));
+    pF.m[0][0] = 1. + p->exx[i];
+    pF.m[0][1] = 0.5 * (p->exy[i] - p->wxy[i]);
+    pF.m[1][0] = 0.5 * (p->exy[i] + p->wxy[i]);
+    pF.m[1][1] = 1. + p->eyy[i];
+    pF.m[2][2] = 1. + p->ezz[i];
+    Bold.m[0][0] = p->pxx[i]; Bold.m[0][1] = p->pxy[i];
+    Bold.m[1][0] = p->pxy[i]; Bold.m[1][1] = p->pyy[i];
+    Bold.m[2][2] = p->pzz[i];
+    if (is3d) {
+        pF.m[0][2] = 0.5 * (p->exz[i] - p->wxz[i]);
+        pF.m[2][0] = 0.5 * (p->exz[i] + p->wxz[i]);
+        pF.m[1][2] = 0.5 * (p->eyz[i] - p->wyz[i]);
+        pF.m[2][1] = 0.5 * (p->eyz[i] + p->wyz[i]);
+        Bold.m[0][2] = Bold.m[2][0] = p->pxz[i];
+        Bold.m[1][2] = Bold.m[2][1] = p->pyz[i];
+    }
+    mat_mul(&dF, &pF, is3d, &F);
+    /* SetDeformationGradientMatrix (MatPoint2D.cpp:310-322, MatPoint3D) */
+    p->exx[i] = F.m[0][0] - 1.;
+    p->eyy[i] = F.m[1][1] - 1.;
+    p->ezz[i] = F.m[2][2] - 1.;
+    p->exy[i] = F.m[1][0] + F.m[0][1];
+    p->wxy[i] = F.m[1][0] - F.m[0][1];
+    if (is3d) {
+        p->exz[i] = F.m[2][0] + F.m[0][2];
+        p->eyz[i] = F.m[2][1] + F.m[1][2];
+        p->wxz[i] = F.m[2][0] - F.m[0][2];
+        p->wyz[i] = F.m[2][1] - F.m[1][2];
+    }
+    mat_mul(&dF, &Bold, is3d, &dFB);
+    const double (*a)[3] = dFB.m, (*d)[3] = dF.m;
+    double Bxx = a[0][0] * d[0][0] + a[0][1] * d[0][1] + a[0][2] * d[0][2];
+    double Bxy = a[0][0] * d[1][0] + a[0][1] * d[1][1] + a[0][2] * d[1][2];
+    double Byy = a[1][0] * d[1][0] + a[1][1] * d[1][1] + a[1][2] * d[1][2];
+    double Bzz = a[2][0] * d[2][0] + a[2][1] * d[2][1] + a[2][2] * d[2][2];
+    double Bxz = 0., Byz = 0.;
+    p->pxx[i] = Bxx; p->pxy[i] = Bxy; p->pyy[i] = Byy; p->pzz[i] = Bzz;
+    if (is3d) {
+        Bxz = a[0][0] * d[2][0] + a[0][1] * d[2][1] + a[0][2] * d[2][2];
+        Byz = a[1][0] * d[2][0] + a[1][1] * d[2][1] + a[1][2] * d[2][2];
+        p->pxz[i] = Bxz; p->pyz[i] = Byz;
+    }
+    /* Matrix3::determinant (Matrix3.cpp:1195-1202) */
+    double detDf;
+    if (!is3d) detDf = d[2][2] * (d[0][0] * d[1][1] - d[1][0] * d[0][1]);
+    else
+        detDf = d[0][0] * (d[1][1] * d[2][2] - d[2][1] * d[1][2]) - d[1][0] * (d[0][1] * d[2][2] - d[2][1] * d[0][2]) +
+                d[2][0] * (d[0][1] * d[1][2] - d[1][1] * d[0][2]);
+    /* residual terms with Jres = 1: resStretch = Jres23 = 1 */
+    double Jres = p->hist1[i];
+    double resStretch = pow(Jres, 1. / 3.);
+    double Jres23 = resStretch * resStretch;
+    double J = detDf * p->hist0[i];
+    p->hist0[i] = J;
+    double st0xx = p->sxx[i], st0yy = p->syy[i], st0zz = p->szz[i], st0xy = p->sxy[i];
+    double st0xz = is3d ? p->sxz[i] : 0., st0yz = is3d ? p->syz[i] : 0.;
+    double Jeff = J / Jres;
+    double p0 = p->pressure[i];
+    double Pterm = J * volumetric_terms(m->uj, Jeff, m->Lamesp) + Jres * m->Gsp * ((Bxx + Byy + Bzz) / (3. * Jres23) - 1.);
+    double delV = 1. - 1. / detDf;
+    double Pfinal = -Pterm + 0.;
+    p->pressure[i] = Pfinal;
+    double avgP = 0.5 * (p0 + Pfinal);
+    double dilEnergy = -avgP * delV;
+    double GJeff = resStretch * m->Gsp;
+    double I1third = (Bxx + Byy + Bzz) / 3.;
+    double sxx = GJeff * (Bxx - I1third), syy = GJeff * (Byy - I1third), szz = GJeff * (Bzz - I1third);
+    double sxy = GJeff * Bxy;
+    p->sxx[i] = sxx; p->syy[i] = syy; p->szz[i] = szz; p->sxy[i] = sxy;
+    double sxz = 0., syz = 0.;
+    if (is3d) {
+        sxz = GJeff * Bxz;
+        syz = GJeff * Byz;
+        p->sxz[i] = sxz; p->syz[i] = syz;
+    }
+    double shearEnergy = 0.5 * ((sxx + st0xx) * du->m[0][0] + (syy + st0yy) * du->m[1][1] + (szz + st0zz) * du->m[2][2] +
+                                (sxy + st0xy) * (du->m[0][1] + du->m[1][0]));
+    if (is3d)
+        shearEnergy += 0.5 * ((sxz + st0xz) * (du->m[0][2] + du->m[2][0]) + (syz + st0yz) * (du->m[1][2] + du->m[2][1]));
+    if (p->work) p->work[i] += dilEnergy + shearEnergy;
+}
+
 /* ------------------------------------------------------------------------ */
 /* Step                                                                      */
 /* ------------------------------------------------------------------------ */
@@ -633,6 +823,7 @@ typedef struct {
     double *xi;             /* 3 per particle: natural coordinates (ncpos) */
     double dt, mtime;
     int nthreads;
+    int kterms;             /* MaterialBase::incrementalDefGradTerms */
 } OCtx;
 
 static void bc_norm(int dir, double *n) {
@@ -799,6 +990,10 @@ static void strain_update(OCtx *c, double strainTime) {
         for (int r = 0; r < 3; r++)
             for (int cc = 0; cc < 3; cc++) dv.m[r][cc] *= strainTime;
         const OMat *m = &c->mats[p->mat[q]];
+        if (m->type == MPMGPU_MAT_NEOHOOKEAN) {
+            neohookean(m, p, q, &dv, is3d, c->kterms);
+            continue;
+        }
         hypo_increment_F(p, q, &dv, is3d);
         if (m->type == MPMGPU_MAT_ISOTROPIC) {
             if (is3d) iso_3d(m, p, q, &dv);
@@ -1036,6 +1231,10 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     c.p = p;
     c.dt = opts->timestep;
     c.nthreads = nthreads < 1 ? 1 : nthreads;
+    /* StartOutput.cpp:116-119: the default (negative) becomes 2, or 1 in 3D */
+    c.kterms = opts->inc_defgrad_terms > 0 ? opts->inc_defgrad_terms : (grid->dim == 3 ? 1 : 2);
+    if (grid->dim == 3 && c.kterms > 2)
+        return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: 3D incremental F with more than 2 terms not implemented");
     c.mats = (OMat *)calloc((size_t)nmat, sizeof(OMat));
     int np = grid->dim == 3 ? MPMGPU_THREED : MPMGPU_PLANE_STRAIN;
     int st = load_materials(mats, nmat, np, c.mats);

@@ -38,10 +38,14 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
 
 
-def archive_view(p, dim, rho_gcc):
-    """Particle dict -> the quantities a NairnMPM archive stores (ArchiveData.cpp:807-930)."""
+def archive_view(p, dim, rho_gcc, mat_type=1):
+    """Particle dict -> the quantities a NairnMPM archive stores (ArchiveData.cpp:807-930).
+    The stress is (s - P) rho0 / J, with J the relative volume: 1 for the
+    small-strain materials, history 0 for Neohookean (type 28)."""
     P = p["pressure"]
     rho = rho_gcc * 1e-3
+    if mat_type == 28:
+        rho = rho / p["hist0"][:, None]
     if dim == 2:
         pos = np.stack([p["x"], p["y"]], 1)
         vel = np.stack([p["vx"], p["vy"]], 1)

@@ -42,6 +42,17 @@ CASES = {
     "taylor3d_ugimp_long": ("taylor_3d", dict(radius=1.5, length=3.0, cell=0.5, steps=120)),
     "taylor3d_linear_usavg": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, gimp="Classic")),
     "taylor3d_ugimp_usl": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, method=3)),
+    # Neohookean (type 28): soft rubber, large deformation
+    "cant2d_neo_usavg": ("cantilever_2d", dict(nx=10, ny=4, steps=150, mat_type=28, G=3., K=30., rho=1.1,
+                                               v0=20000., margin_cells=8)),
+    "cant2d_neo_uj1_usl": ("cantilever_2d", dict(nx=10, ny=4, steps=100, mat_type=28, G=3., K=30., rho=1.1,
+                                                 v0=20000., uj=1, method=3, margin_cells=8)),
+    "cant2d_neo_uj2_terms3": ("cantilever_2d", dict(nx=10, ny=4, steps=100, mat_type=28, G=3., K=30.,
+                                                    rho=1.1, v0=20000., uj=2, inc_terms=3, margin_cells=8)),
+    "taylor3d_neo_usavg": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=80, mat_type=28, G=10.,
+                                             K=50., rho=1.1, v0=-30000.)),
+    "taylor3d_neo_terms2_usl": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=60, mat_type=28,
+                                                  G=10., K=50., rho=1.1, v0=-30000., inc_terms=2, method=3)),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")
@@ -77,7 +88,10 @@ def main():
         sys.exit(f"{REF} not built: make -C oracle/ref -j8")
     work = tempfile.mkdtemp(prefix="nairn_golden_")
     try:
+        only = sys.argv[1:]
         for name, (gen, kw) in CASES.items():
+            if only and name not in only:
+                continue
             steps, n = run_case(name, gen, kw, work)
             print(f"{name}: {n} particles, {steps} steps")
     finally:
