@@ -272,6 +272,8 @@ typedef struct {
     int64_t max_particles;    /* particle slots (sum over resident runs)     */
     int64_t max_nodes;        /* grid nodes (sum over resident runs)         */
     double fraction_usf;      /* USAVG split (0 -> 0.5)                      */
+    int32_t inc_defgrad_terms;/* Exponential() terms of hyperelastic F (0: 2 in 2D, 1 in 3D) */
+    int32_t pad;
 } MpmGpuBatchOptions;
 
 /* run states returned by mpmgpu_batch_run_state; a failed run reports the

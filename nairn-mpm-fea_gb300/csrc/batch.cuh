@@ -658,7 +658,7 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     std::vector<DevMat> dm((size_t)nmat);
     for (int i = 0; i < nmat; i++) {
         std::string why;
-        const int st = derive_material(mats[i], b->o.np, dm[i], why);
+        const int st = derive_material(mats[i], b->o.np, dm[i], why, b->o.inc_defgrad_terms);
         if (st != MPMGPU_OK) return berr(b, st, "material " + std::to_string(i) + ": " + why);
     }
     int r = -1;

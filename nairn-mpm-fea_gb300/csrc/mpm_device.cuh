@@ -13,6 +13,9 @@ constexpr double kSqrtTwoThirds = 0.8164965809277260;  // sqrt(2/3)
 // error bits raised by kernels (reported through the C ABI status)
 enum : unsigned { ERR_NAN = 1u, ERR_LEFT_GRID = 2u, ERR_EDGE = 4u };
 
+// material type ids (MaterialController.cpp:105-231)
+constexpr int kMatIsotropic = 1, kMatIsoPlasticity = 9, kMatNeohookean = 28;
+
 struct DevGrid {
     int dim, nx, ny, nz;
     int xplane, yplane, zplane, nnodes;  // node-number strides, node count
@@ -29,6 +32,9 @@ struct DevMat {
     double C00, C01, C02, C11, C12, C22, C33, C44, C55;  // 3D specific stiffness
     double Gred, Kred;                           // IsoPlasticity specific moduli
     double yldred, Epred, alphaMax, yldredMin;   // LinearHardening
+    double Gsp, Lamesp;                          // Neohookean specific moduli (pr.Gsp, pr.Lamesp)
+    int uj;                                      // Neohookean U(J) option
+    int kterms;                                  // terms of the incremental F exponential
 };
 
 struct DevParticles {
@@ -350,7 +356,7 @@ __device__ __forceinline__ void plastic_law(const DevMat &m, const DevParticles 
         s0xy = spxy + 0.5 * (dwxy * (spxx - spyy) - dwyz * spxz - dwxz * spyz);
     }
     // trial deviatoric stress
-    const double third = delV / 3.;
+    const double third = delV * (1. / 3.);
     const double G = m.Gred;
     const double trxx = s0xx + 2. * G * (dexx - third);
     const double tryy = s0yy + 2. * G * (deyy - third);
@@ -388,10 +394,13 @@ __device__ __forceinline__ void plastic_law(const DevMat &m, const DevParticles 
     double lam = (smag - kSqrtTwoThirds * (m.yldred + m.Epred * alpint)) / (2. * (G + m.Epred / 3.));
     if (alpint + kSqrtTwoThirds * lam > m.alphaMax) lam = (smag - kSqrtTwoThirds * m.yldredMin) / (2. * G);
     const double alpnew = alpint + kSqrtTwoThirds * lam;
-    const double dpxx = lam * (trxx / smag), dpyy = lam * (tryy / smag), dpzz = lam * (trzz / smag);
-    const double dpxy = 2. * lam * (trxy / smag);
-    const double dpxz = kThreeD ? 2. * lam * (trxz / smag) : 0.;
-    const double dpyz = kThreeD ? 2. * lam * (tryz / smag) : 0.;
+    // lam * (tr / smag) with one FP64 division (the reference divides each
+    // component; the products differ from it by rounding only)
+    const double ls = lam / smag;
+    const double dpxx = ls * trxx, dpyy = ls * tryy, dpzz = ls * trzz;
+    const double dpxy = 2. * ls * trxy;
+    const double dpxz = kThreeD ? 2. * ls * trxz : 0.;
+    const double dpyz = kThreeD ? 2. * ls * tryz : 0.;
     const double sxx = trxx - 2. * G * dpxx, syy = tryy - 2. * G * dpyy, szz = trzz - 2. * G * dpzz;
     const double sxy = trxy - G * dpxy;
     p.sxx[i] = sxx;
@@ -418,6 +427,191 @@ __device__ __forceinline__ void plastic_law(const DevMat &m, const DevParticles 
     const double qdalpha = lam * kSqrtTwoThirds * fmax(m.Epred * alpnew, m.yldredMin - m.yldred);
     p.plast[i] += pe - qdalpha;
     p.hist0[i] = alpnew;
+}
+
+
+// ---------------------------------------------------------------------------
+// Neohookean (type 28)
+// ---------------------------------------------------------------------------
+
+// Matrix3::Exponential (Common/System/Matrix3.cpp:312-364): dF = exp(du) with
+// kmax terms; 2D uses the 2x2 Cayley-Hamilton recursion with zz separate, 3D
+// takes 1 or 2 terms.  Row-major 3x3.
+template <bool kThreeD>
+__device__ __forceinline__ void exp_increment(const double du[9], int kmax, double dF[9]) {
+    if (!kThreeD) {
+        dF[2] = dF[5] = dF[6] = dF[7] = 0.;
+        if (kmax == 1) {
+            dF[0] = 1. + du[0];
+            dF[1] = du[1];
+            dF[3] = du[3];
+            dF[4] = 1. + du[4];
+            dF[8] = 1. + du[8];
+            return;
+        }
+        const double c0 = du[1] * du[3] - du[0] * du[4];
+        const double c1 = du[0] + du[4];
+        double beta0 = 0., beta1 = 1., alpha0 = 1., alpha1 = 1.;
+        double betaz = du[8], ezz = 1. + betaz;
+        for (int k = 2; k <= kmax; k++) {
+            const double factor = 1 / (double)k;
+            const double temp = beta1;
+            beta1 = factor * (c1 * temp + beta0);
+            beta0 = factor * c0 * temp;
+            betaz *= factor * du[8];
+            alpha0 += beta0;
+            alpha1 += beta1;
+            ezz += betaz;
+        }
+        dF[0] = alpha0 + alpha1 * du[0];
+        dF[1] = alpha1 * du[1];
+        dF[3] = alpha1 * du[3];
+        dF[4] = alpha0 + alpha1 * du[4];
+        dF[8] = ezz;
+        return;
+    }
+    if (kmax == 1) {
+#pragma unroll
+        for (int k = 0; k < 9; k++) dF[k] = du[k] + (k % 4 == 0 ? 1. : 0.);
+        return;
+    }
+#pragma unroll
+    for (int r = 0; r < 3; r++)
+#pragma unroll
+        for (int c = 0; c < 3; c++) {
+            double m2 = 0.;
+#pragma unroll
+            for (int k = 0; k < 3; k++) m2 += du[3 * r + k] * du[3 * k + c];
+            dF[3 * r + c] = r == c ? 1. + du[3 * r + c] + 0.5 * m2 : du[3 * r + c] + 0.5 * m2;
+        }
+}
+
+// a * b as Matrix3::operator*= forms it (Matrix3.cpp:920-966)
+template <bool kThreeD>
+__device__ __forceinline__ void mat_mul(const double a[9], const double b[9], double o[9]) {
+    if constexpr (!kThreeD) {
+        o[0] = a[0] * b[0] + a[1] * b[3];
+        o[1] = a[0] * b[1] + a[1] * b[4];
+        o[3] = a[3] * b[0] + a[4] * b[3];
+        o[4] = a[3] * b[1] + a[4] * b[4];
+        o[2] = o[5] = o[6] = o[7] = 0.;
+        o[8] = a[8] * b[8];
+    } else {
+#pragma unroll
+        for (int i = 0; i < 3; i++)
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                double v = 0.;
+#pragma unroll
+                for (int k = 0; k < 3; k++) v += a[3 * i + k] * b[3 * k + j];
+                o[3 * i + j] = v;
+            }
+    }
+}
+
+// HyperElastic::GetVolumetricTerms (NairnMPM/src/Materials/HyperElastic.cpp:171-204)
+__device__ __forceinline__ double volumetric_terms(int uj, double J, double Kred) {
+    if (uj == 1) return Kred * (J - 1.);
+    if (uj == 2) return Kred * log(J) / J;
+    return 0.5 * Kred * (J - 1. / J);
+}
+
+// Neohookean::MPMConstitutiveLaw without residual strains, thermal terms or
+// artificial viscosity (NairnMPM/src/Materials/Neohookean.cpp:177-331) and
+// HyperElastic::IncrementDeformation (HyperElastic.cpp:104-139).  F (ep/wrot)
+// and the left Cauchy-Green tensor B (plastic-strain columns) are pushed
+// forward by dF = exp(du); J and Jres are history doubles 0 and 1; the stress
+// is the deviatoric Kirchhoff stress per initial density, pressure separate.
+template <bool kThreeD>
+__device__ __forceinline__ void neo_law(const DevMat &m, const DevParticles &p, int i, const double du[9]) {
+    double dF[9], pF[9], F[9], B[9], dFB[9];
+    exp_increment<kThreeD>(du, m.kterms, dF);
+    pF[0] = 1. + p.exx[i];
+    pF[1] = 0.5 * (p.exy[i] - p.wxy[i]);
+    pF[3] = 0.5 * (p.exy[i] + p.wxy[i]);
+    pF[4] = 1. + p.eyy[i];
+    pF[8] = 1. + p.ezz[i];
+    B[0] = p.pxx[i];
+    B[1] = B[3] = p.pxy[i];
+    B[4] = p.pyy[i];
+    B[8] = p.pzz[i];
+    if (kThreeD) {
+        pF[2] = 0.5 * (p.exz[i] - p.wxz[i]);
+        pF[6] = 0.5 * (p.exz[i] + p.wxz[i]);
+        pF[5] = 0.5 * (p.eyz[i] - p.wyz[i]);
+        pF[7] = 0.5 * (p.eyz[i] + p.wyz[i]);
+        B[2] = B[6] = p.pxz[i];
+        B[5] = B[7] = p.pyz[i];
+    } else {
+        pF[2] = pF[5] = pF[6] = pF[7] = 0.;
+        B[2] = B[5] = B[6] = B[7] = 0.;
+    }
+    mat_mul<kThreeD>(dF, pF, F);
+    p.exx[i] = F[0] - 1.;
+    p.eyy[i] = F[4] - 1.;
+    p.ezz[i] = F[8] - 1.;
+    p.exy[i] = F[3] + F[1];
+    p.wxy[i] = F[3] - F[1];
+    if (kThreeD) {
+        p.exz[i] = F[6] + F[2];
+        p.eyz[i] = F[7] + F[5];
+        p.wxz[i] = F[6] - F[2];
+        p.wyz[i] = F[7] - F[5];
+    }
+    mat_mul<kThreeD>(dF, B, dFB);
+    // B = dF.Bold.dF^T, component sums in the reference's order
+    const double Bxx = dFB[0] * dF[0] + dFB[1] * dF[1] + dFB[2] * dF[2];
+    const double Bxy = dFB[0] * dF[3] + dFB[1] * dF[4] + dFB[2] * dF[5];
+    const double Byy = dFB[3] * dF[3] + dFB[4] * dF[4] + dFB[5] * dF[5];
+    const double Bzz = dFB[6] * dF[6] + dFB[7] * dF[7] + dFB[8] * dF[8];
+    double Bxz = 0., Byz = 0.;
+    p.pxx[i] = Bxx;
+    p.pxy[i] = Bxy;
+    p.pyy[i] = Byy;
+    p.pzz[i] = Bzz;
+    if (kThreeD) {
+        Bxz = dFB[0] * dF[6] + dFB[1] * dF[7] + dFB[2] * dF[8];
+        Byz = dFB[3] * dF[6] + dFB[4] * dF[7] + dFB[5] * dF[8];
+        p.pxz[i] = Bxz;
+        p.pyz[i] = Byz;
+    }
+    // Matrix3::determinant (Matrix3.cpp:1195-1202)
+    const double detDf = kThreeD ? dF[0] * (dF[4] * dF[8] - dF[7] * dF[5]) - dF[3] * (dF[1] * dF[8] - dF[7] * dF[2]) +
+                                       dF[6] * (dF[1] * dF[5] - dF[4] * dF[2])
+                                 : dF[8] * (dF[0] * dF[4] - dF[3] * dF[1]);
+    // no residual strains: Jres stays 1, so its cube root and square are 1
+    const double Jres = p.hist1[i];
+    const double resStretch = Jres == 1. ? 1. : cbrt(Jres);
+    const double Jres23 = resStretch * resStretch;
+    const double J = detDf * p.hist0[i];
+    p.hist0[i] = J;
+    const double st0xx = p.sxx[i], st0yy = p.syy[i], st0zz = p.szz[i], st0xy = p.sxy[i];
+    const double st0xz = kThreeD ? p.sxz[i] : 0., st0yz = kThreeD ? p.syz[i] : 0.;
+    const double Jeff = J / Jres;
+    const double p0 = p.pressure[i];
+    const double trB = Bxx + Byy + Bzz;
+    const double Pterm = J * volumetric_terms(m.uj, Jeff, m.Lamesp) + Jres * m.Gsp * (trB / (3. * Jres23) - 1.);
+    const double delV = 1. - 1. / detDf;
+    const double Pfinal = -Pterm + 0.;
+    p.pressure[i] = Pfinal;
+    const double dilEnergy = -(0.5 * (p0 + Pfinal)) * delV;
+    const double GJeff = resStretch * m.Gsp;
+    const double I1third = trB / 3.;
+    const double sxx = GJeff * (Bxx - I1third), syy = GJeff * (Byy - I1third), szz = GJeff * (Bzz - I1third);
+    const double sxy = GJeff * Bxy;
+    p.sxx[i] = sxx;
+    p.syy[i] = syy;
+    p.szz[i] = szz;
+    p.sxy[i] = sxy;
+    double shear = 0.5 * ((sxx + st0xx) * du[0] + (syy + st0yy) * du[4] + (szz + st0zz) * du[8] +
+                          (sxy + st0xy) * (du[1] + du[3]));
+    if (kThreeD) {
+        const double sxz = GJeff * Bxz, syz = GJeff * Byz;
+        p.sxz[i] = sxz;
+        p.syz[i] = syz;
+        shear += 0.5 * ((sxz + st0xz) * (du[2] + du[6]) + (syz + st0yz) * (du[5] + du[7]));
+    }
+    p.work[i] += dilEnergy + shear;
 }
 
 }  // namespace nmg

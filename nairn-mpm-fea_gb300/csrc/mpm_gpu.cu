@@ -99,10 +99,35 @@ int cuda_fail(MpmGpuCtx *c, cudaError_t e, const char *where) {
 // material (Common/Materials/Elastic.cpp:43-160, 194-330), IsotropicMat
 // (Common/Materials/IsotropicMat.cpp:93-170), IsoPlasticity (IsoPlasticity.cpp:58-65),
 // HardeningLawBase/LinearHardening::VerifyAndLoadProperties (LinearHardening.cpp:45-58).
-int derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::string &why) {
+// Neohookean::VerifyAndLoadProperties, G and K input (Neohookean.cpp:88-141).
+// kterms: MaterialBase::incrementalDefGradTerms (<= 0: 2 in 2D, 1 in 3D, as
+// StartOutput.cpp:116-119 resolves the default).
+int derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::string &why, int kterms) {
     std::memset(&m, 0, sizeof(m));
     m.type = in.type;
     m.field = in.field;
+    m.kterms = kterms > 0 ? kterms : (np == MPMGPU_THREED ? 1 : 2);
+    if (in.type == MPMGPU_MAT_NEOHOOKEAN) {
+        const double rho = in.rho * 0.001;
+        const double G = in.G * 1.e6, K = in.K * 1.e6;
+        if (!(rho > 0.) || !(G > 0.) || !(K > 0.)) {
+            why = "Neohookean needs rho > 0, G > 0 and K > 0";
+            return MPMGPU_ERR_INVALID;
+        }
+        if (in.UJOption < 0 || in.UJOption > 2) {
+            why = "Neohookean dilational energy (UJOption) must be 0, 1, or 2";
+            return MPMGPU_ERR_INVALID;
+        }
+        if (np == MPMGPU_THREED && m.kterms > 2) {
+            why = "3D incremental deformation gradient with more than 2 terms is not implemented on the device";
+            return MPMGPU_ERR_UNSUPPORTED;
+        }
+        const double Lame = K - 2. * G / 3.;
+        m.Gsp = G / rho;
+        m.Lamesp = Lame / rho;
+        m.uj = in.UJOption;
+        return MPMGPU_OK;
+    }
     if (in.type != MPMGPU_MAT_ISOTROPIC && in.type != MPMGPU_MAT_ISOPLASTICITY) {
         why = "material type " + std::to_string(in.type) + " is not implemented on the device";
         return MPMGPU_ERR_UNSUPPORTED;
@@ -340,7 +365,7 @@ int mpmgpu_set_materials(MpmGpuCtx *c, const MpmGpuMaterial *mats, int32_t nmat)
     std::vector<DevMat> h((size_t)nmat);
     for (int i = 0; i < nmat; i++) {
         std::string why;
-        int st = derive_material(mats[i], c->opts.np, h[i], why);
+        int st = derive_material(mats[i], c->opts.np, h[i], why, c->opts.inc_defgrad_terms);
         if (st != MPMGPU_OK) return set_err(c, st, "material " + std::to_string(i) + ": " + why);
     }
     if (c->mats) cudaFree(c->mats);

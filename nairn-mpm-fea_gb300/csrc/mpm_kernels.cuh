@@ -201,9 +201,13 @@ __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevN
 template <int DIM>
 __device__ __forceinline__ void constitutive(const DevMat *mats, const DevParticles &p, int i, const double du[9]) {
     const DevMat &m = mats[p.mat[i]];
+    if (m.type == kMatNeohookean) {
+        neo_law<DIM == 3>(m, p, i, du);
+        return;
+    }
     if (DIM == 2) hypo_increment_F_2d(p, i, du);
     else hypo_increment_F_3d(p, i, du);
-    if (m.type == 1) {
+    if (m.type == kMatIsotropic) {
         if (DIM == 2) iso_law_2d(m, p, i, du);
         else iso_law_3d(m, p, i, du);
     } else {

@@ -135,7 +135,7 @@ class MpmGpuBatchOptions(C.Structure):
     _fields_ = [("np", C.c_int32), ("method", C.c_int32), ("shape", C.c_int32), ("precision", C.c_int32),
                 ("sort_interval", C.c_int32), ("block", C.c_int32), ("max_runs", C.c_int32),
                 ("max_materials", C.c_int32), ("max_particles", C.c_int64), ("max_nodes", C.c_int64),
-                ("fraction_usf", C.c_double)]
+                ("fraction_usf", C.c_double), ("inc_defgrad_terms", C.c_int32), ("pad", C.c_int32)]
 
 
 class MpmGpuBatchInfo(C.Structure):

@@ -112,3 +112,18 @@ def test_mixed_precision_taylor_against_oracle(gpu_lib):
     out = gpu_run(m, m.nsteps, precision=1)
     for k in ("x", "y", "z", "vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "syz", "sxz", "hist0"):
         assert rel_l2(out[k], ref[k]) <= TOL_MIXED, (k, rel_l2(out[k], ref[k]))
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
+def test_neohookean_3d_against_oracle(precision, tol, gpu_lib):
+    """Neo-Hookean rubber bar impact (large strains), FP64 and mixed modes."""
+    import oracle_lib
+    from nairn_gb300 import model, abi
+    m = model.taylor_3d(radius=2.0, length=5.0, cell=0.25, steps=200, mat_type=28, G=10., K=50., rho=1.1,
+                        v0=-30000.)
+    ref = abi.copy_particles(m.particles)
+    oracle_lib.run(m, ref, m.nsteps, nthreads=8)
+    out = gpu_run(m, m.nsteps, precision=precision)
+    for k in ("x", "y", "z", "vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "syz", "sxz", "pressure", "pxx", "pzz",
+              "hist0"):
+        assert rel_l2(out[k], ref[k]) <= tol, (k, rel_l2(out[k], ref[k]))
