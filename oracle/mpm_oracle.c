@@ -400,6 +400,178 @@ static void shape_eval(const OGrid *g, int shape, int e, const double *xi, const
 }
 
 /* ------------------------------------------------------------------------ */
+/* Linear CPDI (lCPDI)                                                       */
+/* ------------------------------------------------------------------------ */
+typedef struct {            /* CPDIDomain of each corner, found once per step */
+    int elem[8];
+    double xi[8][3];
+    double wg[8][3];
+} OCpdi;
+
+static const double r1s[8] = {-1., 1., 1., -1., -1., 1., 1., -1.};
+static const double r2s[8] = {-1., -1., 1., 1., -1., -1., 1., 1.};
+static const double r3s[8] = {-1., -1., -1., -1., 1., 1., 1., 1.};
+
+/* MeshInfo::FindElementFromPoint, equal element sizes (MeshInfo.cpp:593-633);
+ * returns the 0-based element or -1 when the point is off the grid */
+static int find_element(const OGrid *g, double x, double y, double z) {
+    int col = (int)((x - g->xmin) / g->gx);
+    if (col < 0 || col >= g->nx) {
+        if (x == g->xmin + g->nx * g->gx) col = g->nx - 1;
+        else return -1;
+    }
+    int row = (int)((y - g->ymin) / g->gy);
+    if (row < 0 || row >= g->ny) {
+        if (y == g->ymin + g->ny * g->gy) row = g->ny - 1;
+        else return -1;
+    }
+    if (g->dim == 3) {
+        int zr = (int)((z - g->zmin) / g->gz);
+        if (zr < 0 || zr >= g->nz) {
+            if (z == g->zmin + g->nz * g->gz) zr = g->nz - 1;
+            else return -1;
+        }
+        return g->nx * (zr * g->ny + row) + col;
+    }
+    return row * g->nx + col;
+}
+
+/* MatPoint2D::GetCPDINodesAndWeights (MatPoint2D.cpp:519-571) and
+ * MatPoint3D::GetCPDINodesAndWeights (MatPoint3D.cpp:538-601) with
+ * GetSemiSideVectors (MatPoint2D.cpp:423-439, MatPoint3D.cpp:413-433) and
+ * GetParticleSize (MPMBase.cpp:519-524, MatPoint3D.cpp:227-233); no rcrit
+ * rescaling (ElementBase::rcrit < 0 by default).  Returns 0, or -1 when a
+ * corner is off the grid. */
+static int cpdi_setup(const OGrid *g, const MpmGpuParticles *p, long q, OCpdi *cp) {
+    int is3d = g->dim == 3;
+    double ex0, ex1, ey0, ey1, ez0, ez1;
+    elem_extent(g, p->elem[q], &ex0, &ex1, &ey0, &ey1, &ez0, &ez1);
+    double pszx = ex1 - ex0, pszy = ey1 - ey0, pszz = ez1 - ez0;
+    pszx *= 0.5 * p->lpx[q];
+    pszy *= 0.5 * p->lpy[q];
+    double F00 = 1. + p->exx[q], F01 = 0.5 * (p->exy[q] - p->wxy[q]), F10 = 0.5 * (p->exy[q] + p->wxy[q]),
+           F11 = 1. + p->eyy[q], F22 = 1. + p->ezz[q];
+    if (!is3d) {
+        double r1x = F00 * pszx, r1y = F10 * pszx;
+        double r2x = F01 * pszy, r2y = F11 * pszy;
+        double Ap = 4. * (r1x * r2y - r1y * r2x);
+        double px = p->x[q], py = p->y[q];
+        double cx[4] = {px - r1x - r2x, px + r1x - r2x, px + r1x + r2x, px - r1x + r2x};
+        double cy[4] = {py - r1y - r2y, py + r1y - r2y, py + r1y + r2y, py - r1y + r2y};
+        for (int i = 0; i < 4; i++) {
+            int e = find_element(g, cx[i], cy[i], 0.);
+            if (e < 0) return -1;
+            cp->elem[i] = e;
+            xi_pos(g, e, cx[i], cy[i], 0., cp->xi[i]);
+        }
+        Ap = 1. / Ap;
+        cp->wg[0][0] = (r1y - r2y) * Ap;
+        cp->wg[1][0] = (r1y + r2y) * Ap;
+        cp->wg[2][0] = (-r1y + r2y) * Ap;
+        cp->wg[3][0] = (-r1y - r2y) * Ap;
+        cp->wg[0][1] = (-r1x + r2x) * Ap;
+        cp->wg[1][1] = (-r1x - r2x) * Ap;
+        cp->wg[2][1] = (r1x - r2x) * Ap;
+        cp->wg[3][1] = (r1x + r2x) * Ap;
+        for (int i = 0; i < 4; i++) cp->wg[i][2] = 0.;
+        return 0;
+    }
+    pszz *= 0.5 * p->lpz[q];
+    double F02 = 0.5 * (p->exz[q] - p->wxz[q]), F20 = 0.5 * (p->exz[q] + p->wxz[q]);
+    double F12 = 0.5 * (p->eyz[q] - p->wyz[q]), F21 = 0.5 * (p->eyz[q] + p->wyz[q]);
+    double r1[3] = {F00 * pszx, F10 * pszx, F20 * pszx};
+    double r2[3] = {F01 * pszy, F11 * pszy, F21 * pszy};
+    double r3[3] = {F02 * pszz, F12 * pszz, F22 * pszz};
+    double Vp = 8. * (r1[0] * (r2[1] * r3[2] - r2[2] * r3[1]) + r1[1] * (r2[2] * r3[0] - r2[0] * r3[2]) +
+                      r1[2] * (r2[0] * r3[1] - r2[1] * r3[0]));
+    for (int i = 0; i < 8; i++) {
+        double cx = p->x[q] + r1s[i] * r1[0] + r2s[i] * r2[0] + r3s[i] * r3[0];
+        double cy = p->y[q] + r1s[i] * r1[1] + r2s[i] * r2[1] + r3s[i] * r3[1];
+        double cz = p->z[q] + r1s[i] * r1[2] + r2s[i] * r2[2] + r3s[i] * r3[2];
+        int e = find_element(g, cx, cy, cz);
+        if (e < 0) return -1;
+        cp->elem[i] = e;
+        xi_pos(g, e, cx, cy, cz, cp->xi[i]);
+    }
+    Vp = 1. / Vp;
+    double r1x = r1[0], r1y = r1[1], r1z = r1[2], r2x = r2[0], r2y = r2[1], r2z = r2[2];
+    double r3x = r3[0], r3y = r3[1], r3z = r3[2];
+    /* gradient weights, term for term as MatPoint3D.cpp:571-594 writes them */
+    cp->wg[0][0] = (r1z*r2y - r1y*r2z - r1z*r3y + r2z*r3y + r1y*r3z - r2y*r3z)*Vp;
+    cp->wg[0][1] = (-(r1z*r2x) + r1x*r2z + r1z*r3x - r2z*r3x - r1x*r3z + r2x*r3z)*Vp;
+    cp->wg[0][2] = (r1y*r2x - r1x*r2y - r1y*r3x + r2y*r3x + r1x*r3y - r2x*r3y)*Vp;
+    cp->wg[1][0] = (r1z*r2y - r1y*r2z - r1z*r3y - r2z*r3y + r1y*r3z + r2y*r3z)*Vp;
+    cp->wg[1][1] = (-(r1z*r2x) + r1x*r2z + r1z*r3x + r2z*r3x - r1x*r3z - r2x*r3z)*Vp;
+    cp->wg[1][2] = (r1y*r2x - r1x*r2y - r1y*r3x - r2y*r3x + r1x*r3y + r2x*r3y)*Vp;
+    cp->wg[2][0] = (r1z*r2y - r1y*r2z + r1z*r3y - r2z*r3y - r1y*r3z + r2y*r3z)*Vp;
+    cp->wg[2][1] = (-(r1z*r2x) + r1x*r2z - r1z*r3x + r2z*r3x + r1x*r3z - r2x*r3z)*Vp;
+    cp->wg[2][2] = (r1y*r2x - r1x*r2y + r1y*r3x - r2y*r3x - r1x*r3y + r2x*r3y)*Vp;
+    cp->wg[3][0] = (r1z*r2y - r1y*r2z + r1z*r3y + r2z*r3y - r1y*r3z - r2y*r3z)*Vp;
+    cp->wg[3][1] = (-(r1z*r2x) + r1x*r2z - r1z*r3x - r2z*r3x + r1x*r3z + r2x*r3z)*Vp;
+    cp->wg[3][2] = (r1y*r2x - r1x*r2y + r1y*r3x + r2y*r3x - r1x*r3y - r2x*r3y)*Vp;
+    cp->wg[4][0] = (-(r1z*r2y) + r1y*r2z - r1z*r3y + r2z*r3y + r1y*r3z - r2y*r3z)*Vp;
+    cp->wg[4][1] = (r1z*r2x - r1x*r2z + r1z*r3x - r2z*r3x - r1x*r3z + r2x*r3z)*Vp;
+    cp->wg[4][2] = (-(r1y*r2x) + r1x*r2y - r1y*r3x + r2y*r3x + r1x*r3y - r2x*r3y)*Vp;
+    cp->wg[5][0] = (-(r1z*r2y) + r1y*r2z - r1z*r3y - r2z*r3y + r1y*r3z + r2y*r3z)*Vp;
+    cp->wg[5][1] = (r1z*r2x - r1x*r2z + r1z*r3x + r2z*r3x - r1x*r3z - r2x*r3z)*Vp;
+    cp->wg[5][2] = (-(r1y*r2x) + r1x*r2y - r1y*r3x - r2y*r3x + r1x*r3y + r2x*r3y)*Vp;
+    cp->wg[6][0] = (-(r1z*r2y) + r1y*r2z + r1z*r3y - r2z*r3y - r1y*r3z + r2y*r3z)*Vp;
+    cp->wg[6][1] = (r1z*r2x - r1x*r2z - r1z*r3x + r2z*r3x + r1x*r3z - r2x*r3z)*Vp;
+    cp->wg[6][2] = (-(r1y*r2x) + r1x*r2y + r1y*r3x - r2y*r3x - r1x*r3y + r2x*r3y)*Vp;
+    cp->wg[7][0] = (-(r1z*r2y) + r1y*r2z + r1z*r3y + r2z*r3y - r1y*r3z - r2y*r3z)*Vp;
+    cp->wg[7][1] = (r1z*r2x - r1x*r2z - r1z*r3x - r2z*r3x + r1x*r3z + r2x*r3z)*Vp;
+    cp->wg[7][2] = (-(r1y*r2x) + r1x*r2y + r1y*r3x + r2y*r3x - r1x*r3y - r2x*r3y)*Vp;
+    return 0;
+}
+
+/* ElementBase::GetCPDIFunctions, FAST_CPDI branch (MoreMPMElementBase.cpp:581-656):
+ * corners in order, the corner element's linear shape functions
+ * (GetShapeFunctionsForTractions), contributions below 1e-15 skipped, nodes
+ * merged in order of first appearance.  Returns 0, or -1 when the particle
+ * needs more than maxShapeNodes-1 nodes (17 in 2D, 50 in 3D,
+ * MPMReadHandler.cpp:558-562). */
+static int shape_cpdi(const OGrid *g, const OCpdi *cp, int grad, OShape *s) {
+    int is3d = g->dim == 3;
+    int ncorner = is3d ? 8 : 4;
+    int maxnodes = is3d ? 50 : 17;
+    double ws = is3d ? 0.125 : 0.25;
+    double lp1[3] = {1., 1., 1.};
+    int ind = 0;
+    for (int i = 0; i < ncorner; i++) {
+        OShape cs;
+        shape_eval(g, MPMGPU_SHAPE_LINEAR, cp->elem[i], cp->xi[i], lp1, 0, &cs);
+        for (int j = 0; j < cs.n; j++) {
+            double cfn = cs.fn[j];
+            if (cfn < 1e-15) continue;
+            long node = cs.nds[j];
+            int found = -1;
+            for (int look = ind - 1; look >= 0; look--)
+                if (s->nds[look] == node) { found = look; break; }
+            if (found >= 0) {
+                s->fn[found] += ws * cfn;
+                if (grad) {
+                    s->dx[found] += cp->wg[i][0] * cfn;
+                    s->dy[found] += cp->wg[i][1] * cfn;
+                    s->dz[found] += cp->wg[i][2] * cfn;
+                }
+                continue;
+            }
+            if (ind + 1 >= maxnodes) return -1;
+            s->nds[ind] = node;
+            s->fn[ind] = ws * cfn;
+            if (grad) {
+                s->dx[ind] = cp->wg[i][0] * cfn;
+                s->dy[ind] = cp->wg[i][1] * cfn;
+                s->dz[ind] = cp->wg[i][2] * cfn;
+            }
+            ind++;
+        }
+    }
+    s->n = ind;
+    return 0;
+}
+
+/* ------------------------------------------------------------------------ */
 /* Constitutive laws                                                         */
 /* ------------------------------------------------------------------------ */
 typedef struct {
@@ -824,7 +996,25 @@ typedef struct {
     double dt, mtime;
     int nthreads;
     int kterms;             /* MaterialBase::incrementalDefGradTerms */
+    OCpdi *cpdi;            /* lCPDI corners of each particle (this step) */
+    int cpdi_err;           /* a particle needed more CPDI nodes than allowed */
 } OCtx;
+
+/* shape functions of particle q for this step (GetShapeFunctions/GetShapeGradients) */
+static void particle_shape(OCtx *c, long q, int grad, OShape *s) {
+    if (c->o->shape == MPMGPU_SHAPE_LCPDI) {
+        if (shape_cpdi(&c->g, &c->cpdi[q], grad, s) != 0) {
+#pragma omp atomic write
+            c->cpdi_err = 1;
+            s->n = 0;
+        }
+        return;
+    }
+    MpmGpuParticles *p = c->p;
+    int is3d = c->g.dim == 3;
+    double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
+    shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, grad, s);
+}
 
 static void bc_norm(int dir, double *n) {
     n[0] = dir == 1 ? 1. : 0.;
@@ -912,8 +1102,7 @@ static void p2g_mass_momentum(OCtx *c, int last) {
     for (long k = 0; k < p->n; k++) {
         long q = particle_order(c, k);
         OShape s;
-        double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
-        shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, 0, &s);
+        particle_shape(c, q, 0, &s);
         double mp = p->mass[q];
         double vx = p->vx[q], vy = p->vy[q], vz = is3d ? p->vz[q] : 0.;
         for (int j = 0; j < s.n; j++) {
@@ -969,8 +1158,7 @@ static void strain_update(OCtx *c, double strainTime) {
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
     for (long q = 0; q < p->n; q++) {
         OShape s;
-        double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
-        shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, 1, &s);
+        particle_shape(c, q, 1, &s);
         M3 dv;
         memset(&dv, 0, sizeof(dv));
         for (int j = 0; j < s.n; j++) {
@@ -1014,8 +1202,7 @@ static void p2g_forces(OCtx *c) {
     for (long k = 0; k < p->n; k++) {
         long q = particle_order(c, k);
         OShape s;
-        double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
-        shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, 1, &s);
+        particle_shape(c, q, 1, &s);
         double mp = p->mass[q], P = p->pressure ? p->pressure[q] : 0.;
         double sxx = p->sxx[q], syy = p->syy[q], sxy = p->sxy[q];
         double szz = is3d ? p->szz[q] : 0., sxz = is3d ? p->sxz[q] : 0., syz = is3d ? p->syz[q] : 0.;
@@ -1059,8 +1246,7 @@ static void g2p_move(OCtx *c) {
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
     for (long q = 0; q < p->n; q++) {
         OShape s;
-        double lp[3] = {p->lpx[q], p->lpy[q], is3d ? p->lpz[q] : 1.};
-        shape_eval(&c->g, c->o->shape, p->elem[q], &c->xi[3 * q], lp, 0, &s);
+        particle_shape(c, q, 0, &s);
         double Svx = 0., Svy = 0., Svz = 0., Sax = 0., Say = 0., Saz = 0.;
         for (int j = 0; j < s.n; j++) {
             long nd = s.nds[j];
@@ -1152,13 +1338,18 @@ static int one_step(OCtx *c) {
     double stLast = method == MPMGPU_USAVG ? dt - stFirst : dt;
     int is3d = c->g.dim == 3;
 
-    /* InitializationTask: zero nodes, natural coordinates */
+    /* InitializationTask: zero nodes; ElementBase::GetShapeFunctionData: CPDI
+     * corners (lCPDI) and natural coordinates (MoreMPMElementBase.cpp:50-57) */
     zero_field(f, nn);
-    for (long q = 0; q < p->n; q++)
+    for (long q = 0; q < p->n; q++) {
+        if (c->o->shape == MPMGPU_SHAPE_LCPDI && cpdi_setup(&c->g, p, q, &c->cpdi[q]) != 0)
+            return fail(MPMGPU_ERR_LEFT_GRID, "oracle: a CPDI particle domain node has left the grid");
         xi_pos(&c->g, p->elem[q], p->x[q], p->y[q], is3d ? p->z[q] : 0., &c->xi[3 * q]);
+    }
 
     /* MassAndMomentumTask */
     p2g_mass_momentum(c, 0);
+    if (c->cpdi_err) return fail(MPMGPU_ERR_CPDI_NODES, "oracle: too many CPDI nodes found");
 
     /* PostExtrapolationTask: copy momenta, BCs (MASS_MOMENTUM_CALL) */
     for (long i = 1; i < nn; i++) {
@@ -1210,7 +1401,7 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
                    int nsteps, double t0, int nthreads) {
     g_err[0] = 0;
     if (!grid || !opts || !mats || !p) return fail(MPMGPU_ERR_INVALID, "oracle: null argument");
-    if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP)
+    if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI)
         return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: shape function not implemented");
     if (contact && contact->enabled) return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: contact not implemented");
     OCtx c;
@@ -1245,6 +1436,7 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     for (unsigned k = 0; k < sizeof(fl) / sizeof(fl[0]); k++) *fl[k] = (double *)calloc((size_t)nn, sizeof(double));
     c.f.npts = (int *)calloc((size_t)nn, sizeof(int));
     c.xi = (double *)calloc((size_t)(3 * (p->n > 0 ? p->n : 1)), sizeof(double));
+    if (opts->shape == MPMGPU_SHAPE_LCPDI) c.cpdi = (OCpdi *)calloc((size_t)(p->n > 0 ? p->n : 1), sizeof(OCpdi));
     c.mtime = t0;
     for (int s = 0; s < nsteps && st == MPMGPU_OK; s++) {
         st = one_step(&c);
@@ -1253,6 +1445,7 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     for (unsigned k = 0; k < sizeof(fl) / sizeof(fl[0]); k++) free(*fl[k]);
     free(c.f.npts);
     free(c.xi);
+    free(c.cpdi);
     free(c.mats);
     return st;
 }

@@ -53,6 +53,14 @@ CASES = {
                                              K=50., rho=1.1, v0=-30000.)),
     "taylor3d_neo_terms2_usl": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=60, mat_type=28,
                                                   G=10., K=50., rho=1.1, v0=-30000., inc_terms=2, method=3)),
+    # linear CPDI shape functions (lCPDI)
+    "cant2d_cpdi_usavg": ("cantilever_2d", dict(nx=10, ny=4, steps=60, gimp="lCPDI")),
+    "cant2d_cpdi_usl_ppc3": ("cantilever_2d", dict(nx=8, ny=3, steps=40, ppc_side=3, gimp="lCPDI", method=3)),
+    "cant2d_cpdi_neo": ("cantilever_2d", dict(nx=10, ny=4, steps=150, mat_type=28, G=3., K=30., rho=1.1,
+                                              v0=20000., margin_cells=8, gimp="lCPDI")),
+    "taylor3d_cpdi_usavg": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, gimp="lCPDI")),
+    "taylor3d_cpdi_neo_usf": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=80, mat_type=28, G=10.,
+                                                K=50., rho=1.1, v0=-30000., gimp="lCPDI", method=0)),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")
