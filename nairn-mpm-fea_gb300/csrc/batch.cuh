@@ -443,6 +443,7 @@ int batch_prepare(MpmGpuBatch *b) {
 int batch_status(unsigned bits) {
     if (bits & ERR_NAN) return MPMGPU_ERR_NAN;
     if (bits & (ERR_LEFT_GRID | ERR_EDGE)) return MPMGPU_ERR_LEFT_GRID;
+    if (bits & ERR_CPDI_NODES) return MPMGPU_ERR_CPDI_NODES;
     return MPMGPU_ERR_INVALID;
 }
 

@@ -11,7 +11,7 @@ namespace nmg {
 constexpr double kSqrtTwoThirds = 0.8164965809277260;  // sqrt(2/3)
 
 // error bits raised by kernels (reported through the C ABI status)
-enum : unsigned { ERR_NAN = 1u, ERR_LEFT_GRID = 2u, ERR_EDGE = 4u };
+enum : unsigned { ERR_NAN = 1u, ERR_LEFT_GRID = 2u, ERR_EDGE = 4u, ERR_CPDI_NODES = 16u };
 
 // material type ids (MaterialController.cpp:105-231)
 constexpr int kMatIsotropic = 1, kMatIsoPlasticity = 9, kMatNeohookean = 28;
@@ -49,6 +49,11 @@ struct DevParticles {
     double *hist0, *hist1, *work, *plast;
     double *xi, *eta, *zeta;   // natural coordinates of the step (ncpos)
     int *run;                  // run of each slot in a batch (-1: empty); unused for one run
+    // lCPDI only, rebuilt at every step start (CPDIDomain): per corner c the
+    // element ce[c*n+i], natural coordinates cxi[(3c+a)*n+i] and gradient
+    // weights cwg[(3c+a)*n+i]
+    int *ce;
+    double *cxi, *cwg;
 };
 
 struct DevNodes {

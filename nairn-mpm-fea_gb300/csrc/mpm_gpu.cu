@@ -73,6 +73,7 @@ struct MpmGpuCtx {
     bool profile = false;
     std::vector<cudaEvent_t> ev;         // per-step kernel events when profiling
     long long launches = 0;              // kernels launched by this context
+    void *cpdi = nullptr;                // lCPDI corner scratch (ints then doubles)
 };
 
 namespace {
@@ -218,8 +219,10 @@ void hcols(const MpmGpuParticles *h, double *out[kParticleDoubles]) {
 void free_particles(MpmGpuCtx *c) {
     if (c->pblock) cudaFree(c->pblock);
     if (c->iblock) cudaFree(c->iblock);
+    if (c->cpdi) cudaFree(c->cpdi);
     c->pblock = nullptr;
     c->iblock = nullptr;
+    c->cpdi = nullptr;
     sort_free(c->sort);
     c->p.n = 0;
 }
@@ -244,7 +247,7 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     if ((grid->dim == 3) != (opts->np == MPMGPU_THREED) ||
         (grid->dim == 2 && opts->np != MPMGPU_PLANE_STRAIN))
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "analysis type must be 2D plane strain or 3D");
-    if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP)
+    if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
     if (opts->method != MPMGPU_USF && opts->method != MPMGPU_USAVG && opts->method != MPMGPU_USL)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
@@ -463,10 +466,30 @@ int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
             free_particles(c);
             return set_err(c, MPMGPU_ERR_OOM, "sort workspace allocation failed");
         }
+        if (c->opts.shape == MPMGPU_SHAPE_LCPDI) {
+            // per corner: element (int), natural coordinates and gradient weights (3 doubles each)
+            const size_t nc = c->dim == 3 ? 8 : 4;
+            const size_t bytes = (size_t)n * nc * (sizeof(int) + 6 * sizeof(double)) + 256;
+            e = cudaMalloc(&c->cpdi, bytes);
+            if (e != cudaSuccess) {
+                free_particles(c);
+                return set_err(c, MPMGPU_ERR_OOM, "CPDI corner allocation failed");
+            }
+        }
         CK(cudaMemsetAsync(c->pblock, 0, dbytes, c->stream));
         c->p.n = n;
     }
     link_columns(c->p, c->pblock, c->iblock, &c->orig);
+    if (c->cpdi) {
+        // doubles first (8-byte aligned), then the corner elements
+        const size_t nc = c->dim == 3 ? 8 : 4;
+        c->p.cxi = (double *)c->cpdi;
+        c->p.cwg = c->p.cxi + 3 * nc * (size_t)n;
+        c->p.ce = (int *)(c->p.cwg + 3 * nc * (size_t)n);
+    } else {
+        c->p.cxi = c->p.cwg = nullptr;
+        c->p.ce = nullptr;
+    }
     double *hc[kParticleDoubles];
     hcols(h, hc);
     for (int k = 0; k < kParticleDoubles; k++) {
@@ -566,12 +589,14 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
 template <bool MIX>
 void enqueue_prec(MpmGpuCtx *c, double t, int slot) {
     const bool d3 = c->dim == 3;
-    const bool lin = c->opts.shape == MPMGPU_SHAPE_LINEAR;
+    const int shape = c->opts.shape;
     if (d3) {
-        if (lin) enqueue_step<3, SHAPE_LINEAR, MIX>(c, t, slot);
+        if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<3, SHAPE_LINEAR, MIX>(c, t, slot);
+        else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<3, SHAPE_LCPDI, MIX>(c, t, slot);
         else enqueue_step<3, SHAPE_UGIMP, MIX>(c, t, slot);
     } else {
-        if (lin) enqueue_step<2, SHAPE_LINEAR, MIX>(c, t, slot);
+        if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<2, SHAPE_LINEAR, MIX>(c, t, slot);
+        else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<2, SHAPE_LCPDI, MIX>(c, t, slot);
         else enqueue_step<2, SHAPE_UGIMP, MIX>(c, t, slot);
     }
 }
@@ -595,6 +620,8 @@ int error_status(MpmGpuCtx *c, unsigned bits) {
     if (bits & ERR_NAN) return set_err(c, MPMGPU_ERR_NAN, "a particle position became NaN");
     if (bits & ERR_LEFT_GRID) return set_err(c, MPMGPU_ERR_LEFT_GRID, "a particle left the grid");
     if (bits & ERR_EDGE) return set_err(c, MPMGPU_ERR_LEFT_GRID, "a particle moved into a grid edge element");
+    if (bits & ERR_CPDI_NODES)
+        return set_err(c, MPMGPU_ERR_CPDI_NODES, "a CPDI particle domain touches more nodes than the reference allows");
     return MPMGPU_OK;
 }
 

@@ -17,7 +17,7 @@
 
 namespace nmg {
 
-enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1 };
+enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2 };
 
 // Visit the nodes of one particle, calling f(node0based, N, dNdx, dNdy, dNdz).
 // ElementBase::GetShapeFunctions / GetShapeGradients
@@ -119,6 +119,205 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
 }
 
 // ---------------------------------------------------------------------------
+// linear CPDI
+// ---------------------------------------------------------------------------
+
+// MeshInfo::FindElementFromPoint for equal element sizes (MeshInfo.cpp:593-633):
+// truncated cell index, the grid's far edge clamped; -1 when off the grid.
+__device__ __forceinline__ int find_cell(double x, double xmin, double gx, int n) {
+    int c = (int)((x - xmin) / gx);
+    if (c < 0 || c >= n) {
+        if (x == xmin + n * gx) c = n - 1;
+        else c = -1;
+    }
+    return c;
+}
+
+// MatPoint2D/3D::GetCPDINodesAndWeights (MatPoint2D.cpp:519-571,
+// MatPoint3D.cpp:538-601): semi-side vectors r = F * (cell * lp / 2) of the
+// particle (GetSemiSideVectors, GetParticleSize), corners x +- r1 +- r2 (+- r3)
+// in the reference's order, their elements and natural coordinates, and the
+// gradient weights.  The reference throws when a corner is off the grid or the
+// particle touches more than 16 (2D) / 49 (3D) nodes (GetCPDIFunctions); here
+// those set ERR_LEFT_GRID / ERR_CPDI_NODES.  Returns false on an error.
+template <int DIM>
+__device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
+    constexpr int NC = DIM == 3 ? 8 : 4;
+    const size_t n = (size_t)p.n;
+    int col, row, zr;
+    elem_coords(g, p.elem[i], col, row, zr);
+    double pszx = g.xn[col + 1] - g.xn[col], pszy = g.yn[row + 1] - g.yn[row];
+    pszx *= 0.5 * p.lpx[i];
+    pszy *= 0.5 * p.lpy[i];
+    const double F00 = 1. + p.exx[i], F01 = 0.5 * (p.exy[i] - p.wxy[i]), F10 = 0.5 * (p.exy[i] + p.wxy[i]);
+    const double F11 = 1. + p.eyy[i];
+    double r1[3], r2[3], r3[3] = {0., 0., 0.};
+    r1[0] = F00 * pszx;
+    r1[1] = F10 * pszx;
+    r2[0] = F01 * pszy;
+    r2[1] = F11 * pszy;
+    if (DIM == 3) {
+        double pszz = g.zn[zr + 1] - g.zn[zr];
+        pszz *= 0.5 * p.lpz[i];
+        const double F02 = 0.5 * (p.exz[i] - p.wxz[i]), F20 = 0.5 * (p.exz[i] + p.wxz[i]);
+        const double F12 = 0.5 * (p.eyz[i] - p.wyz[i]), F21 = 0.5 * (p.eyz[i] + p.wyz[i]);
+        r1[2] = F20 * pszx;
+        r2[2] = F21 * pszy;
+        r3[0] = F02 * pszz;
+        r3[1] = F12 * pszz;
+        r3[2] = (1. + p.ezz[i]) * pszz;
+    } else {
+        r1[2] = r2[2] = 0.;
+    }
+    const double pos[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
+    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const double s1 = (c == 1 || c == 2 || c == 5 || c == 6) ? 1. : -1.;
+        const double s2 = (c == 2 || c == 3 || c == 6 || c == 7) ? 1. : -1.;
+        const double s3 = c >= 4 ? 1. : -1.;
+        double cp[3];
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            cp[a] = pos[a] + s1 * r1[a] + s2 * r2[a];
+            if (DIM == 3) cp[a] += s3 * r3[a];
+        }
+        const int cc = find_cell(cp[0], g.xmin, g.gx, g.nx);
+        const int cr = find_cell(cp[1], g.ymin, g.gy, g.ny);
+        const int cz = DIM == 3 ? find_cell(cp[2], g.zmin, g.gz, g.nz) : 0;
+        if (cc < 0 || cr < 0 || cz < 0) {
+            atomicOr(err, ERR_LEFT_GRID);
+            return false;
+        }
+        p.ce[c * n + i] = DIM == 3 ? g.nx * (cz * g.ny + cr) + cc : cr * g.nx + cc;
+        p.cxi[(3 * c + 0) * n + i] = (2. * cp[0] - g.xn[cc] - g.xn[cc + 1]) / (g.xn[cc + 1] - g.xn[cc]);
+        p.cxi[(3 * c + 1) * n + i] = (2. * cp[1] - g.yn[cr] - g.yn[cr + 1]) / (g.yn[cr + 1] - g.yn[cr]);
+        if (DIM == 3) p.cxi[(3 * c + 2) * n + i] = (2. * cp[2] - g.zn[cz] - g.zn[cz + 1]) / (g.zn[cz + 1] - g.zn[cz]);
+        const int cell[3] = {cc, cr, cz};
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            lo[a] = min(lo[a], cell[a]);
+            hi[a] = max(hi[a], cell[a]);
+        }
+    }
+    // gradient weights
+    if (DIM == 2) {
+        const double Ap = 1. / (4. * (r1[0] * r2[1] - r1[1] * r2[0]));
+        const double wx[4] = {r1[1] - r2[1], r1[1] + r2[1], -r1[1] + r2[1], -r1[1] - r2[1]};
+        const double wy[4] = {-r1[0] + r2[0], -r1[0] - r2[0], r1[0] - r2[0], r1[0] + r2[0]};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            p.cwg[(3 * c + 0) * n + i] = wx[c] * Ap;
+            p.cwg[(3 * c + 1) * n + i] = wy[c] * Ap;
+        }
+    } else {
+        // the reference's per-corner expressions are signed sums of the cross
+        // products r1 x r2, r1 x r3 and r2 x r3 divided by the volume
+        const double a12[3] = {r1[1] * r2[2] - r1[2] * r2[1], r1[2] * r2[0] - r1[0] * r2[2], r1[0] * r2[1] - r1[1] * r2[0]};
+        const double a13[3] = {r1[1] * r3[2] - r1[2] * r3[1], r1[2] * r3[0] - r1[0] * r3[2], r1[0] * r3[1] - r1[1] * r3[0]};
+        const double a23[3] = {r2[1] * r3[2] - r2[2] * r3[1], r2[2] * r3[0] - r2[0] * r3[2], r2[0] * r3[1] - r2[1] * r3[0]};
+        const double Vp = 1. / (8. * (r1[0] * a23[0] + r1[1] * a23[1] + r1[2] * a23[2]));
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const double s1 = (c == 1 || c == 2 || c == 5 || c == 6) ? 1. : -1.;
+            const double s2 = (c == 2 || c == 3 || c == 6 || c == 7) ? 1. : -1.;
+            const double s3 = c >= 4 ? 1. : -1.;
+            // wg = (s1 r2 x r3 - s2 r1 x r3 + s3 r1 x r2) / V (MatPoint3D.cpp:571-594)
+#pragma unroll
+            for (int a = 0; a < 3; a++) p.cwg[(3 * c + a) * n + i] = (s1 * a23[a] - s2 * a13[a] + s3 * a12[a]) * Vp;
+        }
+    }
+    // node count check (3D only: four 2D corner elements touch at most the 16
+    // nodes the 2D limit allows); spans of up to 2 cells per axis touch at
+    // most 27 nodes
+    bool small = true;
+#pragma unroll
+    for (int a = 0; a < DIM; a++) small = small && hi[a] - lo[a] <= 1;
+    if (DIM == 3 && !small) {
+        // distinct nodes with a weight of at least 1e-15, counted on a bit
+        // mask of the corner cells' bounding box (wide domains are rare)
+        const int wx = hi[0] - lo[0] + 2, wy = hi[1] - lo[1] + 2, wz = DIM == 3 ? hi[2] - lo[2] + 2 : 1;
+        if ((long long)wx * wy * wz > 512) {
+            atomicOr(err, ERR_CPDI_NODES);
+            return false;
+        }
+        unsigned mask[16] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        for (int c = 0; c < NC; c++) {
+            const int e = p.ce[c * n + i];
+            int ec, er, ez;
+            elem_coords(g, e, ec, er, ez);
+            const double xi = p.cxi[(3 * c) * n + i], eta = p.cxi[(3 * c + 1) * n + i];
+            const double zeta = DIM == 3 ? p.cxi[(3 * c + 2) * n + i] : 0.;
+            for (int k = 0; k < (DIM == 3 ? 8 : 4); k++) {
+                const int dx = (k == 1 || k == 2 || k == 5 || k == 6) ? 1 : 0;
+                const int dy = (k == 2 || k == 3 || k == 6 || k == 7) ? 1 : 0;
+                const int dz = k >= 4 ? 1 : 0;
+                const double t1 = 1. + (dx ? 1. : -1.) * xi, t2 = 1. + (dy ? 1. : -1.) * eta;
+                const double cfn = DIM == 3 ? 0.125 * t1 * t2 * (1. + (dz ? 1. : -1.) * zeta) : 0.25 * t1 * t2;
+                if (cfn < 1e-15) continue;
+                const int oz = DIM == 3 ? ez + dz - lo[2] : 0;
+                const int bit = (oz * wy + (er + dy - lo[1])) * wx + (ec + dx - lo[0]);
+                mask[bit >> 5] |= 1u << (bit & 31);
+            }
+        }
+        int count = 0;
+#pragma unroll
+        for (int w = 0; w < 16; w++) count += __popc(mask[w]);
+        if (count > 49) {
+            atomicOr(err, ERR_CPDI_NODES);
+            return false;
+        }
+    }
+    return true;
+}
+
+// GetCPDIFunctions (MoreMPMElementBase.cpp:581-656) without the node merge:
+// f is called for every (corner, element node) pair with weight ws * N and
+// gradient wg * N (N the corner element's linear shape function, pairs with
+// N < 1e-15 skipped); the sums over pairs equal the merged node values.
+template <int DIM, bool GRAD, typename T, class F>
+__device__ __forceinline__ void cpdi_nodes(const DevGrid &g, int nb, const DevParticles &p, int i, F &&f) {
+    constexpr int NC = DIM == 3 ? 8 : 4;
+    const size_t n = (size_t)p.n;
+    const T ws = DIM == 3 ? T(0.125) : T(0.25);
+#pragma unroll 1
+    for (int c = 0; c < NC; c++) {
+        int col, row, zr;
+        elem_coords(g, p.ce[c * n + i], col, row, zr);
+        const int n0 = nb + zr * g.zplane + row * g.yplane + col;
+        const T xi = (T)p.cxi[(3 * c) * n + i], eta = (T)p.cxi[(3 * c + 1) * n + i];
+        const T zeta = DIM == 3 ? (T)p.cxi[(3 * c + 2) * n + i] : T(0);
+        T gx = 0, gy = 0, gz = 0;
+        if (GRAD) {
+            gx = (T)p.cwg[(3 * c) * n + i];
+            gy = (T)p.cwg[(3 * c + 1) * n + i];
+            if (DIM == 3) gz = (T)p.cwg[(3 * c + 2) * n + i];
+        }
+#pragma unroll
+        for (int k = 0; k < (DIM == 3 ? 8 : 4); k++) {
+            const int dx = (k == 1 || k == 2 || k == 5 || k == 6) ? 1 : 0;
+            const int dy = (k == 2 || k == 3 || k == 6 || k == 7) ? 1 : 0;
+            const int dz = k >= 4 ? 1 : 0;
+            const T t1 = T(1) + (dx ? T(1) : T(-1)) * xi, t2 = T(1) + (dy ? T(1) : T(-1)) * eta;
+            const T cfn = DIM == 3 ? T(0.125) * t1 * t2 * (T(1) + (dz ? T(1) : T(-1)) * zeta) : T(0.25) * t1 * t2;
+            if (cfn < T(1e-15)) continue;
+            f(n0 + dx + dy * g.yplane + dz * g.zplane, ws * cfn, gx * cfn, gy * cfn, gz * cfn);
+        }
+    }
+}
+
+// the nodes of particle i for this step, whatever the shape-function option
+template <int DIM, int SHAPE, bool GRAD, typename T, class F>
+__device__ __forceinline__ void visit_nodes(const DevGrid &g, int nb, const DevParticles &p, int i, F &&f) {
+    if constexpr (SHAPE == SHAPE_LCPDI) {
+        cpdi_nodes<DIM, GRAD, T>(g, nb, p, i, f);
+    } else {
+        for_each_node<DIM, SHAPE, GRAD, T>(g, nb, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
+                                           p.lpy[i], DIM == 3 ? p.lpz[i] : 1., f);
+    }
+}
+
+// ---------------------------------------------------------------------------
 // particle kernels
 // ---------------------------------------------------------------------------
 
@@ -186,16 +385,23 @@ __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevN
     if (DIM == 3) p.zeta[i] = zeta;
     const double mp = p.mass[i];
     const double vx = p.vx[i], vy = p.vy[i], vz = DIM == 3 ? p.vz[i] : 0.;
-    for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1.,
-                                        [&](int n, T N, T, T, T) {
-                                            if (N == T(0)) return;
-                                            const double fnmp = (double)N * mp;
-                                            atomicAdd(&nd.mass[n], fnmp);
-                                            atomicAdd(&nd.px[n], vx * fnmp);
-                                            atomicAdd(&nd.py[n], vy * fnmp);
-                                            if (DIM == 3) atomicAdd(&nd.pz[n], vz * fnmp);
-                                            nd.active[n] = 1;
-                                        });
+    auto scatter = [&](int n, T N, T, T, T) {
+        if (N == T(0)) return;
+        const double fnmp = (double)N * mp;
+        atomicAdd(&nd.mass[n], fnmp);
+        atomicAdd(&nd.px[n], vx * fnmp);
+        atomicAdd(&nd.py[n], vy * fnmp);
+        if (DIM == 3) atomicAdd(&nd.pz[n], vz * fnmp);
+        nd.active[n] = 1;
+    };
+    if constexpr (SHAPE == SHAPE_LCPDI) {
+        // ElementBase::GetShapeFunctionData: the particle's CPDI corners for this step
+        if (!cpdi_setup<DIM>(g, p, i, rv.err)) return;
+        cpdi_nodes<DIM, false, T>(g, rv.nb, p, i, scatter);
+    } else {
+        for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, p.lpx[i], p.lpy[i],
+                                            DIM == 3 ? p.lpz[i] : 1., scatter);
+    }
 }
 
 template <int DIM>
@@ -232,8 +438,7 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, cons
         split2(p.vy[i], ph[1], pl[1]);
         if (DIM == 3) split2(p.vz[i], ph[2], pl[2]);
     }
-    for_each_node<DIM, SHAPE, true, T>(g, nb, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
-                                       p.lpy[i], DIM == 3 ? p.lpz[i] : 1., [&](int n, T N, T dx, T dy, T dz) {
+    visit_nodes<DIM, SHAPE, true, T>(g, nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
                                            T vx, vy, vz = 0;
                                            if (MIX) {
@@ -283,8 +488,7 @@ __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticl
     const T sxx = (T)(-mp * (p.sxx[i] - P)), syy = (T)(-mp * (p.syy[i] - P)), sxy = (T)(-mp * p.sxy[i]);
     const T szz = DIM == 3 ? (T)(-mp * (p.szz[i] - P)) : T(0), sxz = DIM == 3 ? (T)(-mp * p.sxz[i]) : T(0),
             syz = DIM == 3 ? (T)(-mp * p.syz[i]) : T(0);
-    for_each_node<DIM, SHAPE, true, T>(g, rv.nb, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
-                                       p.lpy[i], DIM == 3 ? p.lpz[i] : 1., [&](int n, T N, T dx, T dy, T dz) {
+    visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
                                            T fx, fy, fz = 0;
                                            if (DIM == 2) {
@@ -391,7 +595,12 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
 #pragma unroll
         for (int a = 0; a < DIM; a++) split2(v[a], ph[a], pl[a]);
     }
-    for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, [&](int n, T N, T, T, T) {
+    // the particle's nodes for this step (CPDI corners or the element window)
+    auto visit = [&](auto &&fn) {
+        if constexpr (SHAPE == SHAPE_LCPDI) cpdi_nodes<DIM, false, T>(g, rv.nb, p, i, fn);
+        else for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, fn);
+    };
+    visit([&](int n, T N, T, T, T) {
         if (N == T(0)) return;
         if (MIX) {
             Sv[0] += ((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0])) * N;
@@ -429,7 +638,7 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
     }
     if (USL) {
         const double mp = p.mass[i];
-        for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, [&](int n, T N, T, T, T) {
+        visit([&](int n, T N, T, T, T) {
             if (N == T(0)) return;
             const double fnmp = (double)N * mp;
             atomicAdd(&nd.ux[n], v[0] * fnmp);

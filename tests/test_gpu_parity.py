@@ -127,3 +127,31 @@ def test_neohookean_3d_against_oracle(precision, tol, gpu_lib):
     for k in ("x", "y", "z", "vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "syz", "sxz", "pressure", "pxx", "pzz",
               "hist0"):
         assert rel_l2(out[k], ref[k]) <= tol, (k, rel_l2(out[k], ref[k]))
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
+def test_cpdi_3d_neohookean_against_oracle(precision, tol, gpu_lib):
+    """lCPDI shape functions on a larger 3D Neo-Hookean impact, FP64 and mixed."""
+    import oracle_lib
+    from nairn_gb300 import model, abi
+    m = model.taylor_3d(radius=2.0, length=4.0, cell=0.25, steps=120, mat_type=28, G=10., K=50., rho=1.1,
+                        v0=-30000., gimp="lCPDI")
+    ref = abi.copy_particles(m.particles)
+    oracle_lib.run(m, ref, m.nsteps, nthreads=8)
+    out = gpu_run(m, m.nsteps, precision=precision)
+    for k in ("x", "y", "z", "vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "syz", "sxz", "pressure", "hist0"):
+        assert rel_l2(out[k], ref[k]) <= tol, (k, rel_l2(out[k], ref[k]))
+    assert np.array_equal(out["elem"], ref["elem"])
+
+
+def test_cpdi_node_limit_is_reported(gpu_lib):
+    from nairn_gb300 import model
+    from nairn_gb300.gpu import GpuRun, GpuError
+    m = model.taylor_3d(radius=1.0, length=2.0, cell=0.5, steps=3, gimp="lCPDI")
+    p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
+    p["exx"][5] = p["eyy"][5] = p["ezz"][5] = 5.0  # eight corner cells apart: 64 nodes > 49
+    r = GpuRun(m)
+    r.upload(p)
+    with pytest.raises(GpuError, match="CPDI_NODES"):
+        r.step(1)
+    r.close()

@@ -59,3 +59,17 @@ def test_oracle_reports_left_grid():
     p["vx"][0] = -1.e9
     with pytest.raises(RuntimeError, match="LEFT_GRID"):
         oracle_lib.run(m, p, 2)
+
+
+def test_oracle_cpdi_node_limit():
+    """A CPDI domain touching more than 49 nodes (3D) stops the run, as
+    GetCPDIFunctions throws 'Too many CPDI nodes found' (in 2D four corner
+    elements touch at most 16 nodes, the 2D limit)."""
+    import oracle_lib
+    from nairn_gb300 import model
+    m = model.taylor_3d(radius=1.0, length=2.0, cell=0.5, steps=3, gimp="lCPDI")
+    p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
+    # F = 6 I: the eight corners fall in eight separate cells, 64 nodes > 49
+    p["exx"][5] = p["eyy"][5] = p["ezz"][5] = 5.0
+    with pytest.raises(RuntimeError, match="CPDI_NODES"):
+        oracle_lib.run(m, p, 1)
