@@ -97,6 +97,15 @@ def materials_array(m: Model):
     return arr
 
 
+def contact_struct(m: Model) -> MpmGpuContact:
+    """Multimaterial contact settings of a model (disabled when it has none)."""
+    c = m.extra.get("contact") if m.extra else None
+    if not c:
+        return MpmGpuContact()
+    return MpmGpuContact(int(c["enabled"]), int(c["normals"]), float(c["friction"]), float(c["contact_cutoff"]),
+                         float(c["rigid_gradient_bias"]))
+
+
 def bcs_array(m: Model):
     n = len(m.bcs)
     arr = (MpmGpuVelBC * max(n, 1))()

@@ -124,6 +124,9 @@ class GpuRun:
             raise GpuError(st, L.mpmgpu_last_error(None).decode())
         self.h = h
         self._check(L.mpmgpu_set_materials(self.h, abi.materials_array(model), len(model.materials)))
+        ct = abi.contact_struct(model)
+        if ct.enabled:
+            self._check(L.mpmgpu_set_contact(self.h, C.byref(ct)))
         bcs, nbc = abi.bcs_array(model)
         self._check(L.mpmgpu_set_velocity_bcs(self.h, bcs, nbc))
         self.t = 0.0

@@ -160,3 +160,103 @@ def taylor_3d(radius: float = 5.0, length: float = 25.0, cell: float = 0.25, ppc
 </JANFEAInput>
 """
     return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 3}
+
+
+def _mm_mode(normals: int, friction: float) -> str:
+    """<MultiMaterialMode> with the normal method and a Coulomb friction law
+    (<Friction>: < 0 stick, 0 frictionless; ContactLaw::ConvertOldStyleToContactLaw)."""
+    return (f'    <MultiMaterialMode Normals="{int(normals)}">\n'
+            f'      <Friction>{_fmt(friction)}</Friction>\n'
+            f'    </MultiMaterialMode>\n')
+
+
+def contact_2d(plate=(20, 4), block=(6, 4), block_x0=5.0, gap=0.0, cell=1.0, ppc_side=2, v=(2000., -2000.),
+               plate_mat=None, block_mat=None, friction=0.3, normals=2, steps=200, cfl=0.4, gimp="uGIMP",
+               method=2, margin_cells=4, archive_root: str = "Results/contact.", inc_terms: int = 0) -> tuple[str, dict]:
+    """2D plane-strain multimaterial contact: a block (plate=(nx, ny) and
+    block=(nx, ny) in cells) moving at v onto an elastic plate whose base is
+    held; materials (type, properties) as dicts for material_xml."""
+    pm = dict(mat_type=1, rho=2.7, E=70000., nu=0.33) if plate_mat is None else dict(plate_mat)
+    bm = dict(mat_type=28, rho=1.1, G=10., K=50.) if block_mat is None else dict(block_mat)
+    Lp, Hp = plate[0] * cell, plate[1] * cell
+    Lb, Hb = block[0] * cell, block[1] * cell
+    y0 = Hp + gap
+    c = max(wave_speed(pm["mat_type"], pm["rho"], E=pm.get("E", 0.), nu=pm.get("nu", 0.), G=pm.get("G", 0.),
+                       K=pm.get("K", 0.)),
+            wave_speed(bm["mat_type"], bm["rho"], E=bm.get("E", 0.), nu=bm.get("nu", 0.), G=bm.get("G", 0.),
+                       K=bm.get("K", 0.)))
+    dt = cfl_timestep(cell, c, cfl)
+    maxtime = (steps - 0.5) * dt
+    m = margin_cells * cell
+    xml = _header(10, method, gimp, maxtime, cfl, archive_root, ppc_side * ppc_side, ARCHIVE_ORDER, inc_terms)
+    xml = xml.replace("  </MPMHeader>\n", _mm_mode(normals, friction) + "  </MPMHeader>\n")
+    xml += f"""  <Mesh output="file">
+    <Grid xmin="{_fmt(-m)}" xmax="{_fmt(Lp + m)}" ymin="{_fmt(-m)}" ymax="{_fmt(y0 + Hb + m)}" thickness="1">
+      <Horiz cellsize="{_fmt(cell)}"/>
+      <Vert cellsize="{_fmt(cell)}"/>
+    </Grid>
+  </Mesh>
+  <MaterialPoints>
+    <Body mat="1" angle="0" thick="1" vx="0" vy="0">
+      <Rect xmin="0" xmax="{_fmt(Lp)}" ymin="0" ymax="{_fmt(Hp)}"/>
+    </Body>
+    <Body mat="2" angle="0" thick="1" vx="{_fmt(v[0])}" vy="{_fmt(v[1])}">
+      <Rect xmin="{_fmt(block_x0)}" xmax="{_fmt(block_x0 + Lb)}" ymin="{_fmt(y0)}" ymax="{_fmt(y0 + Hb)}"/>
+    </Body>
+  </MaterialPoints>
+{material_xml(pm.pop("mat_type"), "plate", **pm)}{material_xml(bm.pop("mat_type"), "block", **bm)}  <GridBCs>
+    <BCLine x1="{_fmt(-0.5 * cell)}" y1="0" x2="{_fmt(Lp + 0.5 * cell)}" y2="0" tolerance="{_fmt(0.01)}">
+      <DisBC dir="1" disp="0"/>
+      <DisBC dir="2" disp="0"/>
+    </BCLine>
+  </GridBCs>
+</JANFEAInput>
+"""
+    return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 2}
+
+
+def contact_3d(plate=(12, 12, 3), block=(4, 4, 3), block_x0=4.0, block_y0=4.0, gap=0.0, cell=0.5, ppc_side=2,
+               v=(4000., 0., -4000.), plate_mat=None, block_mat=None, friction=0.3, normals=2, steps=100, cfl=0.5,
+               gimp="lCPDI", method=2, margin_cells=4, archive_root: str = "Results/contact3.",
+               inc_terms: int = 0) -> tuple[str, dict]:
+    """3D multimaterial contact (the config-3 form): a Neo-Hookean block
+    pressed and sliding on an elastic plate whose base plane is held."""
+    pm = dict(mat_type=1, rho=2.7, E=70000., nu=0.33) if plate_mat is None else dict(plate_mat)
+    bm = dict(mat_type=28, rho=1.1, G=10., K=50.) if block_mat is None else dict(block_mat)
+    Lx, Ly, Hp = plate[0] * cell, plate[1] * cell, plate[2] * cell
+    bx, by, bz = block[0] * cell, block[1] * cell, block[2] * cell
+    z0 = Hp + gap
+    c = max(wave_speed(pm["mat_type"], pm["rho"], E=pm.get("E", 0.), nu=pm.get("nu", 0.), G=pm.get("G", 0.),
+                       K=pm.get("K", 0.)),
+            wave_speed(bm["mat_type"], bm["rho"], E=bm.get("E", 0.), nu=bm.get("nu", 0.), G=bm.get("G", 0.),
+                       K=bm.get("K", 0.)))
+    dt = cfl_timestep(cell, c, cfl)
+    maxtime = (steps - 0.5) * dt
+    m = margin_cells * cell
+    xml = _header(12, method, gimp, maxtime, cfl, archive_root, ppc_side ** 3, ARCHIVE_ORDER, inc_terms)
+    xml = xml.replace("  </MPMHeader>\n", _mm_mode(normals, friction) + "  </MPMHeader>\n")
+    xml += f"""  <Mesh output="file">
+    <Grid xmin="{_fmt(-m)}" xmax="{_fmt(Lx + m)}" ymin="{_fmt(-m)}" ymax="{_fmt(Ly + m)}" zmin="{_fmt(-m)}" zmax="{_fmt(z0 + bz + m)}">
+      <Horiz cellsize="{_fmt(cell)}"/>
+      <Vert cellsize="{_fmt(cell)}"/>
+      <Depth cellsize="{_fmt(cell)}"/>
+    </Grid>
+  </Mesh>
+  <MaterialPoints>
+    <Body mat="1" angle="0" vx="0" vy="0" vz="0">
+      <Box xmin="0" xmax="{_fmt(Lx)}" ymin="0" ymax="{_fmt(Ly)}" zmin="0" zmax="{_fmt(Hp)}"/>
+    </Body>
+    <Body mat="2" angle="0" vx="{_fmt(v[0])}" vy="{_fmt(v[1])}" vz="{_fmt(v[2])}">
+      <Box xmin="{_fmt(block_x0)}" xmax="{_fmt(block_x0 + bx)}" ymin="{_fmt(block_y0)}" ymax="{_fmt(block_y0 + by)}" zmin="{_fmt(z0)}" zmax="{_fmt(z0 + bz)}"/>
+    </Body>
+  </MaterialPoints>
+{material_xml(pm.pop("mat_type"), "plate", **pm)}{material_xml(bm.pop("mat_type"), "block", **bm)}  <GridBCs>
+    <BCBox xmin="{_fmt(-m - cell)}" xmax="{_fmt(Lx + m + cell)}" ymin="{_fmt(-m - cell)}" ymax="{_fmt(Ly + m + cell)}" zmin="{_fmt(-0.01 * cell)}" zmax="{_fmt(0.01 * cell)}">
+      <DisBC dir="1" disp="0"/>
+      <DisBC dir="2" disp="0"/>
+      <DisBC dir="3" disp="0"/>
+    </BCBox>
+  </GridBCs>
+</JANFEAInput>
+"""
+    return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 3}

@@ -217,13 +217,13 @@ def _material(mat_type, rho, E=0., nu=0., yield_=0., Ep=0., G=0., K=0., uj=0):
 
 
 def _initial_material_state(p, mat):
-    """MaterialBase::SetInitialParticleState / InitHistoryData of the material:
-    hyperelastic B = I in the plastic-strain slot (HyperElastic.cpp:45-53),
-    Neohookean history J = Jres = 1 (Neohookean.cpp:151-156)."""
+    """MaterialBase::SetInitialParticleState / InitHistoryData of the material
+    for all particles of p (one body): hyperelastic B = I in the plastic-strain
+    slot (HyperElastic.cpp:45-53), Neohookean history J = Jres = 1
+    (Neohookean.cpp:151-156)."""
     if mat["type"] == MAT_NEOHOOKEAN:
-        sel = p["mat"] == 0 if "mat" in p else slice(None)
         for k in ("pxx", "pyy", "pzz", "hist0", "hist1"):
-            p[k][sel] = 1.
+            p[k][:] = 1.
 
 
 def cantilever_2d(nx=100, ny=20, cell=1.0, ppc_side=2, E=1000., nu=0.33, rho=1.0, v0=1000.,
@@ -504,3 +504,109 @@ def serve_request_params(count=200, seed=77, rate=20.0, nmin=10000, nmax=2000000
 def serve_models(params) -> list:
     """Models of serve_request_params entries."""
     return [block_3d(**kw) if dim == 3 else block_2d(**kw) for _, dim, kw in params]
+
+
+def _body_particles(g, pos, elem, inside, ppc_side, mat, mat_index, vel, thick=1.0):
+    """Particles of one <Body> (MPMReadHandler::MPMPts): the candidate points
+    inside its shape, in element order, with the body's material and velocity."""
+    p = _new_particles(pos[inside], elem[inside], g, ppc_side, mat["rho"], thick)
+    p["mat"][:] = mat_index
+    for k, v in zip(("vx", "vy", "vz"), vel):
+        p[k][:] = v
+    _initial_material_state(p, mat)
+    return p
+
+
+def _concat(parts):
+    return {k: np.concatenate([q[k] for q in parts]) for k in parts[0]}
+
+
+def _contact_options(normals, friction):
+    # MpmGpuContact: displacement-based separation (contact_cutoff < 0)
+    return dict(enabled=1, normals=int(normals), friction=float(friction), contact_cutoff=-1., rigid_gradient_bias=1.)
+
+
+def _mat_from(d, default):
+    d = dict(default if d is None else d)
+    t = d.pop("mat_type")
+    return _material(t, d["rho"], E=d.get("E", 0.), nu=d.get("nu", 0.), yield_=d.get("yield_", 0.),
+                     Ep=d.get("Ep", 0.), G=d.get("G", 0.), K=d.get("K", 0.), uj=d.get("uj", 0))
+
+
+def contact_2d(plate=(20, 4), block=(6, 4), block_x0=5.0, gap=0.0, cell=1.0, ppc_side=2, v=(2000., -2000.),
+               plate_mat=None, block_mat=None, friction=0.3, normals=2, steps=200, cfl=0.4, gimp="uGIMP",
+               method=USAVG, margin_cells=4, inc_terms=0, **_ignored) -> Model:
+    """Model of inputs.contact_2d (same arguments): plate in material field 0,
+    block in field 1, multimaterial contact on."""
+    from . import inputs
+    shape = GIMP_NAMES[gimp]
+    pm = _mat_from(plate_mat, dict(mat_type=MAT_ISO, rho=2.7, E=70000., nu=0.33))
+    bm = _mat_from(block_mat, dict(mat_type=MAT_NEOHOOKEAN, rho=1.1, G=10., K=50.))
+    pm["field"], bm["field"] = 0, 1
+    Lp, Hp = plate[0] * cell, plate[1] * cell
+    Lb, Hb = block[0] * cell, block[1] * cell
+    y0 = Hp + gap
+    m = margin_cells * cell
+    g = make_grid(2, (-m, Lp + m), (-m, y0 + Hb + m), None, cell, 1.0)
+    pos, elem = _element_points(g, ppc_side)
+    x, y = pos[:, 0], pos[:, 1]
+    in_p = (x <= Lp) & (x >= 0.) & (y <= Hp) & (y >= 0.)
+    in_b = (x <= block_x0 + Lb) & (x >= block_x0) & (y <= y0 + Hb) & (y >= y0) & ~in_p
+    p = _concat([_body_particles(g, pos, elem, in_p, ppc_side, pm, 0, (0., 0., 0.)),
+                 _body_particles(g, pos, elem, in_b, ppc_side, bm, 1, (v[0], v[1], 0.))])
+    ids = np.arange(1, g.nnodes + 1)
+    ndx = g.xnodes[(ids - 1) % (g.nx + 1)]
+    ndy = g.ynodes[(ids - 1) // (g.nx + 1)]
+    nodes = ids[_line_contains(ndx, ndy, -0.5 * cell, 0., Lp + 0.5 * cell, 0., 0.01)]
+    bcs = np.zeros(2 * nodes.size, dtype=BC_DTYPE)
+    bcs["node"][:nodes.size] = nodes
+    bcs["dir"][:nodes.size] = 1
+    bcs["node"][nodes.size:] = nodes
+    bcs["dir"][nodes.size:] = 2
+    c = max(inputs.wave_speed(q["type"], q["rho"], E=q["E"], nu=q["nu"], G=q["G"], K=q["K"]) for q in (pm, bm))
+    dt = inputs.cfl_timestep(g.dx, c, cfl)
+    opts = dict(np=PLANE_STRAIN, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
+                inc_defgrad_terms=inc_terms if inc_terms > 0 else 2, nfields=2)
+    return Model(g, p, [pm, bm], bcs, opts, steps, name="contact_2d",
+                 extra={"contact": _contact_options(normals, friction)})
+
+
+def contact_3d(plate=(12, 12, 3), block=(4, 4, 3), block_x0=4.0, block_y0=4.0, gap=0.0, cell=0.5, ppc_side=2,
+               v=(4000., 0., -4000.), plate_mat=None, block_mat=None, friction=0.3, normals=2, steps=100, cfl=0.5,
+               gimp="lCPDI", method=USAVG, margin_cells=4, inc_terms=0, **_ignored) -> Model:
+    """Model of inputs.contact_3d (same arguments)."""
+    from . import inputs
+    shape = GIMP_NAMES[gimp]
+    pm = _mat_from(plate_mat, dict(mat_type=MAT_ISO, rho=2.7, E=70000., nu=0.33))
+    bm = _mat_from(block_mat, dict(mat_type=MAT_NEOHOOKEAN, rho=1.1, G=10., K=50.))
+    pm["field"], bm["field"] = 0, 1
+    Lx, Ly, Hp = plate[0] * cell, plate[1] * cell, plate[2] * cell
+    bx, by, bz = block[0] * cell, block[1] * cell, block[2] * cell
+    z0 = Hp + gap
+    m = margin_cells * cell
+    g = make_grid(3, (-m, Lx + m), (-m, Ly + m), (-m, z0 + bz + m), cell)
+    pos, elem = _element_points(g, ppc_side)
+    x, y, z = pos[:, 0], pos[:, 1], pos[:, 2]
+    in_p = (x <= Lx) & (x >= 0.) & (y <= Ly) & (y >= 0.) & (z <= Hp) & (z >= 0.)
+    in_b = ((x <= block_x0 + bx) & (x >= block_x0) & (y <= block_y0 + by) & (y >= block_y0) & (z <= z0 + bz)
+            & (z >= z0) & ~in_p)
+    p = _concat([_body_particles(g, pos, elem, in_p, ppc_side, pm, 0, (0., 0., 0.)),
+                 _body_particles(g, pos, elem, in_b, ppc_side, bm, 1, v)])
+    ids = np.arange(1, g.nnodes + 1)
+    plane = (g.nx + 1) * (g.ny + 1)
+    ndx = g.xnodes[(ids - 1) % (g.nx + 1)]
+    ndy = g.ynodes[((ids - 1) % plane) // (g.nx + 1)]
+    ndz = g.znodes[(ids - 1) // plane]
+    bx0, bx1, by0, by1 = -m - cell, Lx + m + cell, -m - cell, Ly + m + cell
+    on = (ndx <= bx1) & (ndx >= bx0) & (ndy <= by1) & (ndy >= by0) & (ndz <= 0.01 * cell) & (ndz >= -0.01 * cell)
+    nodes = ids[on]
+    bcs = np.zeros(3 * nodes.size, dtype=BC_DTYPE)
+    for k, d in enumerate((1, 2, 4)):
+        bcs["node"][k * nodes.size:(k + 1) * nodes.size] = nodes
+        bcs["dir"][k * nodes.size:(k + 1) * nodes.size] = d
+    c = max(inputs.wave_speed(q["type"], q["rho"], E=q["E"], nu=q["nu"], G=q["G"], K=q["K"]) for q in (pm, bm))
+    dt = inputs.cfl_timestep(g.dx, c, cfl)
+    opts = dict(np=THREED, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
+                inc_defgrad_terms=inc_terms if inc_terms > 0 else 1, nfields=2)
+    return Model(g, p, [pm, bm], bcs, opts, steps, name="contact_3d",
+                 extra={"contact": _contact_options(normals, friction)})

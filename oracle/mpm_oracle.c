@@ -174,9 +174,12 @@ typedef struct {
     double xmin, ymin, zmin, gx, gy, gz;
 } OGrid;
 
-typedef struct {            /* one material velocity field on every node */
+typedef struct {            /* material velocity fields: field f of node n at f*(nnodes+1)+n */
     double *mass, *px, *py, *pz, *fx, *fy, *fz, *vx, *vy, *vz, *cx, *cy, *cz;
     int *npts;
+    /* multimaterial contact terms (ContactTerms): volume, displacement and
+     * volume gradient extrapolations */
+    double *vol, *ux, *uy, *uz, *gvx, *gvy, *gvz;
 } OField;
 
 static void elem_extent(const OGrid *g, int e, double *x0, double *x1, double *y0, double *y1,
@@ -998,7 +1001,19 @@ typedef struct {
     int kterms;             /* MaterialBase::incrementalDefGradTerms */
     OCpdi *cpdi;            /* lCPDI corners of each particle (this step) */
     int cpdi_err;           /* a particle needed more CPDI nodes than allowed */
+    int nf;                 /* material velocity fields */
+    long nn;                /* nodes + 1: stride between fields */
+    long nfn;               /* nf * nn */
+    int mm;                 /* multimaterial mode: contact terms and contact */
+    int normals;            /* MeshInfo::materialNormalMethod (0, 1 or 2) */
+    int friction_style;     /* CoulombFriction: 0 stick, 1 frictionless, 2 frictional */
+    double friction;        /* Coulomb coefficient */
 } OCtx;
+
+/* field of particle q (MaterialBase::GetField) */
+static int particle_field(const OCtx *c, long q) {
+    return c->nf > 1 ? c->mats[c->p->mat[q]].field : 0;
+}
 
 /* shape functions of particle q for this step (GetShapeFunctions/GetShapeGradients) */
 static void particle_shape(OCtx *c, long q, int grad, OShape *s) {
@@ -1023,14 +1038,16 @@ static void bc_norm(int dir, double *n) {
 }
 
 /* NodalVelBC::VelocityBCLoop (NodalVelBC.cpp:386-400) with
- * MatVelocityField::ZeroVelocityBC / AddVelocityBC (MatVelocityField.cpp:490-575). */
-static void velocity_bc_loop(OCtx *c, int pass) {
+ * MatVelocityField::ZeroVelocityBC / AddVelocityBC (MatVelocityField.cpp:490-575),
+ * on one material field (every nonrigid field gets the same conditions,
+ * CrackVelocityFieldMulti::ZeroVelocityBC / AddVelocityBC). */
+static void velocity_bc_field(OCtx *c, int pass, int fld) {
     OField *f = &c->f;
     double dt = c->dt;
     for (int b = 0; b < c->nbc; b++) {
         const MpmGpuVelBC *bc = &c->bcs[b];
         if (c->mtime < bc->ftime) continue;
-        long i = bc->node;
+        long i = (long)fld * c->nn + bc->node;
         if (f->npts[i] <= 0) continue;
         double n[3];
         bc_norm(bc->dir, n);
@@ -1058,7 +1075,7 @@ static void velocity_bc_loop(OCtx *c, int pass) {
     for (int b = 0; b < c->nbc; b++) {
         const MpmGpuVelBC *bc = &c->bcs[b];
         if (c->mtime < bc->ftime) continue;
-        long i = bc->node;
+        long i = (long)fld * c->nn + bc->node;
         if (f->npts[i] <= 0) continue;
         double n[3], vel = bc->value;
         bc_norm(bc->dir, n);
@@ -1086,6 +1103,10 @@ static void velocity_bc_loop(OCtx *c, int pass) {
     }
 }
 
+static void velocity_bc_loop(OCtx *c, int pass) {
+    for (int fld = 0; fld < c->nf; fld++) velocity_bc_field(c, pass, fld);
+}
+
 static long particle_order(const OCtx *c, long k) {
     /* reverse order of the patch list when single-threaded */
     return c->p->n - 1 - k;
@@ -1094,6 +1115,27 @@ static long particle_order(const OCtx *c, long k) {
 /* MassAndMomentumTask::Execute (MassAndMomentumTask.cpp:48-127) and
  * NodalPoint::AddMassMomentum (NodalPointMPM.cpp:419-453); when last is set,
  * UpdateStrainsLastContactTask's AddMassMomentumLast (NodalPointMPM.cpp:470-486). */
+/* particle volume for contact (MatPoint2D/3D::GetVolume with DEFORMED_AREA or
+ * DEFORMED_AREA_FOR_GRADIENT, MatPoint2D.cpp:407-417, MatPoint3D.cpp:395-408) */
+static double contact_volume(const OCtx *c, long q) {
+    const MpmGpuParticles *p = c->p;
+    double rho = c->mats[p->mat[q]].rho;
+    double F00 = 1. + p->exx[q], F01 = 0.5 * (p->exy[q] - p->wxy[q]), F10 = 0.5 * (p->exy[q] + p->wxy[q]);
+    double F11 = 1. + p->eyy[q];
+    if (c->g.dim != 3) return (F00 * F11 - F10 * F01) * p->mass[q] / rho;
+    double F22 = 1. + p->ezz[q];
+    double F02 = 0.5 * (p->exz[q] - p->wxz[q]), F20 = 0.5 * (p->exz[q] + p->wxz[q]);
+    double F12 = 0.5 * (p->eyz[q] - p->wyz[q]), F21 = 0.5 * (p->eyz[q] + p->wyz[q]);
+    double J = F00 * (F11 * F22 - F21 * F12) - F01 * (F10 * F22 - F20 * F12) + F02 * (F10 * F21 - F20 * F11);
+    return J * p->mass[q] / rho;
+}
+
+/* MassAndMomentumTask / UpdateStrainsLastContactTask extrapolations with
+ * NodalPoint::AddMassMomentum / AddMassMomentumLast (NodalPointMPM.cpp:419-486):
+ * momentum (and mass and point counts on the first pass) of the particle's
+ * material field; in multimaterial mode also the contact volume, displacement
+ * and volume gradient (CrackVelocityField::AddVolumeDisplacement :395-401,
+ * CrackVelocityFieldMulti::AddVolumeGradient :108-112). */
 static void p2g_mass_momentum(OCtx *c, int last) {
     MpmGpuParticles *p = c->p;
     OField *f = &c->f;
@@ -1102,11 +1144,19 @@ static void p2g_mass_momentum(OCtx *c, int last) {
     for (long k = 0; k < p->n; k++) {
         long q = particle_order(c, k);
         OShape s;
-        particle_shape(c, q, 0, &s);
+        particle_shape(c, q, c->mm, &s);
+        long off = (long)particle_field(c, q) * c->nn;
         double mp = p->mass[q];
         double vx = p->vx[q], vy = p->vy[q], vz = is3d ? p->vz[q] : 0.;
+        double Vp = 0., dx = 0., dy = 0., dz = 0.;
+        if (c->mm) {
+            Vp = contact_volume(c, q);
+            dx = p->x[q] - p->x0[q];
+            dy = p->y[q] - p->y0[q];
+            dz = is3d ? p->z[q] - p->z0[q] : 0.;
+        }
         for (int j = 0; j < s.n; j++) {
-            long nd = s.nds[j];
+            long nd = off + s.nds[j];
             double fnmp = s.fn[j] * mp;
             double ax = vx * fnmp, ay = vy * fnmp, az = vz * fnmp;
             if (c->nthreads > 1) {
@@ -1122,10 +1172,37 @@ static void p2g_mass_momentum(OCtx *c, int last) {
 #pragma omp atomic
                     f->mass[nd] += fnmp;
                 }
+                if (c->mm) {
+                    double wv = s.fn[j] * Vp, gx = s.dx[j] * Vp, gy = s.dy[j] * Vp, gz = s.dz[j] * Vp;
+                    double ux = dx * fnmp, uy = dy * fnmp, uz = dz * fnmp;
+#pragma omp atomic
+                    f->vol[nd] += wv;
+#pragma omp atomic
+                    f->ux[nd] += ux;
+#pragma omp atomic
+                    f->uy[nd] += uy;
+#pragma omp atomic
+                    f->uz[nd] += uz;
+#pragma omp atomic
+                    f->gvx[nd] += gx;
+#pragma omp atomic
+                    f->gvy[nd] += gy;
+#pragma omp atomic
+                    f->gvz[nd] += gz;
+                }
             } else {
                 f->px[nd] += ax;
                 f->py[nd] += ay;
                 f->pz[nd] += az;
+                if (c->mm) {
+                    f->vol[nd] += s.fn[j] * Vp;
+                    f->ux[nd] += dx * fnmp;
+                    f->uy[nd] += dy * fnmp;
+                    f->uz[nd] += dz * fnmp;
+                    f->gvx[nd] += s.dx[j] * Vp;
+                    f->gvy[nd] += s.dy[j] * Vp;
+                    f->gvz[nd] += s.dz[j] * Vp;
+                }
                 if (!last) {
                     f->npts[nd] += 1;
                     f->mass[nd] += fnmp;
@@ -1138,7 +1215,7 @@ static void p2g_mass_momentum(OCtx *c, int last) {
 /* MatVelocityField::GridValueCalculation (MatVelocityField.cpp:239-251) */
 static void grid_velocity(OCtx *c) {
     OField *f = &c->f;
-    for (long i = 1; i <= c->g.nnodes; i++) {
+    for (long i = 1; i < c->nfn; i++) {
         if (f->npts[i] <= 0 || f->mass[i] == 0.) continue;
         double r = 1. / f->mass[i];
         f->vx[i] = f->px[i] * r;
@@ -1159,10 +1236,11 @@ static void strain_update(OCtx *c, double strainTime) {
     for (long q = 0; q < p->n; q++) {
         OShape s;
         particle_shape(c, q, 1, &s);
+        long off = (long)particle_field(c, q) * c->nn;
         M3 dv;
         memset(&dv, 0, sizeof(dv));
         for (int j = 0; j < s.n; j++) {
-            long nd = s.nds[j];
+            long nd = off + s.nds[j];
             double vx = f->vx[nd], vy = f->vy[nd], vz = f->vz[nd];
             if (!is3d) {
                 dv.m[0][0] += vx * s.dx[j];
@@ -1203,11 +1281,12 @@ static void p2g_forces(OCtx *c) {
         long q = particle_order(c, k);
         OShape s;
         particle_shape(c, q, 1, &s);
+        long off = (long)particle_field(c, q) * c->nn;
         double mp = p->mass[q], P = p->pressure ? p->pressure[q] : 0.;
         double sxx = p->sxx[q], syy = p->syy[q], sxy = p->sxy[q];
         double szz = is3d ? p->szz[q] : 0., sxz = is3d ? p->sxz[q] : 0., syz = is3d ? p->syz[q] : 0.;
         for (int j = 0; j < s.n; j++) {
-            long nd = s.nds[j];
+            long nd = off + s.nds[j];
             double fx, fy, fz;
             if (!is3d) {
                 fx = -mp * ((sxx - P) * s.dx[j] + sxy * s.dy[j]) + s.fn[j] * 0.;
@@ -1247,9 +1326,10 @@ static void g2p_move(OCtx *c) {
     for (long q = 0; q < p->n; q++) {
         OShape s;
         particle_shape(c, q, 0, &s);
+        long off = (long)particle_field(c, q) * c->nn;
         double Svx = 0., Svy = 0., Svz = 0., Sax = 0., Say = 0., Saz = 0.;
         for (int j = 0; j < s.n; j++) {
-            long nd = s.nds[j];
+            long nd = off + s.nds[j];
             double fi = s.fn[j];
             Svx += f->vx[nd] * fi;
             Svy += f->vy[nd] * fi;
@@ -1317,12 +1397,195 @@ static int reset_elements(OCtx *c) {
 }
 
 static void zero_field(OField *f, long nn) {
-    memset(f->mass, 0, nn * sizeof(double));
-    memset(f->px, 0, nn * sizeof(double)); memset(f->py, 0, nn * sizeof(double)); memset(f->pz, 0, nn * sizeof(double));
-    memset(f->fx, 0, nn * sizeof(double)); memset(f->fy, 0, nn * sizeof(double)); memset(f->fz, 0, nn * sizeof(double));
-    memset(f->vx, 0, nn * sizeof(double)); memset(f->vy, 0, nn * sizeof(double)); memset(f->vz, 0, nn * sizeof(double));
-    memset(f->cx, 0, nn * sizeof(double)); memset(f->cy, 0, nn * sizeof(double)); memset(f->cz, 0, nn * sizeof(double));
+    double *cols[] = {f->mass, f->px, f->py, f->pz, f->fx, f->fy, f->fz, f->vx, f->vy, f->vz, f->cx, f->cy, f->cz,
+                      f->vol, f->ux, f->uy, f->uz, f->gvx, f->gvy, f->gvz};
+    for (unsigned k = 0; k < sizeof(cols) / sizeof(cols[0]); k++)
+        if (cols[k]) memset(cols[k], 0, nn * sizeof(double));
     memset(f->npts, 0, nn * sizeof(int));
+}
+
+/* ------------------------------------------------------------------------ */
+/* Multimaterial contact                                                     */
+/* ------------------------------------------------------------------------ */
+static double dot3(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+
+/* MatVelocityField::ChangeMatMomentum (MatVelocityField.cpp:197-228) */
+static void change_momentum(OCtx *c, long k, const double *d, int callType) {
+    OField *f = &c->f;
+    f->px[k] += d[0];
+    f->py[k] += d[1];
+    f->pz[k] += d[2];
+    if (callType == UPDATE_MOMENTUM_CALL) {
+        double s = 1. / c->dt;
+        f->fx[k] += d[0] * s;
+        f->fy[k] += d[1] * s;
+        f->fz[k] += d[2] * s;
+    } else if (callType == MASS_MOMENTUM_CALL) {
+        f->cx[k] = f->px[k];
+        f->cy[k] = f->py[k];
+        f->cz[k] = f->pz[k];
+    }
+}
+
+/* CoulombFriction::GetFrictionalDeltaMomentum (CoulombFriction.cpp:146-262)
+ * with GetSslideAcDt (:266-285), no static coefficient.  Returns 0 when the
+ * law leaves the momenta alone (not in contact). */
+static int coulomb_delta(const OCtx *c, double *delPi, const double *norm, double dotn, double deln, double mred,
+                         const double *delFi) {
+    if (c->friction_style == 0) return 1;
+    if (delFi) {
+        double fn = dot3(delFi, norm);
+        deln += c->dt * (dotn - 0.5 * fn * c->dt) / mred;
+    }
+    int inContact = deln < 0. && dotn < 0.;
+    if (c->friction_style == 1) {
+        if (inContact) {
+            for (int a = 0; a < 3; a++) delPi[a] = norm[a] * dotn;
+            return 1;
+        }
+        return 0;
+    }
+    if (!inContact) return 0;
+    double dott = 0., tang[3];
+    for (int a = 0; a < 3; a++) tang[a] = delPi[a];
+    for (int a = 0; a < 3; a++) tang[a] += norm[a] * (-dotn);
+    double tangMag = sqrt(dot3(tang, tang));
+    if (tangMag > 0.) {
+        double s = 1. / tangMag;
+        for (int a = 0; a < 3; a++) tang[a] *= s;
+        dott = dot3(delPi, tang);
+        if (dott < 0.) {
+            for (int a = 0; a < 3; a++) tang[a] *= -1.;
+            dott = -dott;
+        }
+    }
+    double SslideAcDt = c->friction * (-dotn);
+    if (SslideAcDt <= 0.) {
+        for (int a = 0; a < 3; a++) delPi[a] = norm[a] * dotn;
+    } else if (dott > SslideAcDt) {
+        for (int a = 0; a < 3; a++) delPi[a] = norm[a] * dotn;
+        for (int a = 0; a < 3; a++) delPi[a] += tang[a] * SslideAcDt;
+    }
+    return 1;
+}
+
+/* MaterialContactNode::ContactOnKnownNodes -> NodalPoint::MaterialContactOnNode ->
+ * CrackVelocityFieldMulti::MaterialContactOnCVF / MaterialContactOnCVFLumped
+ * (CrackVelocityFieldMulti.cpp:302-671) for nonrigid materials: each material
+ * against the others lumped (two materials: one pair, equal and opposite
+ * momentum changes), normals from volume gradients (GetNormalVector, :960-1069,
+ * methods 0-2), separation from extrapolated displacements
+ * (CrackSurfaceContact::MaterialSeparation), Coulomb friction. */
+static void material_contact(OCtx *c, int callType) {
+    OField *f = &c->f;
+    int nf = c->nf;
+    int act[64];
+    int postUpdate = callType == UPDATE_MOMENTUM_CALL;
+    for (long n = 1; n <= c->g.nnodes; n++) {
+        int nm = 0;
+        double Pc[3] = {0., 0., 0.}, Mc = 0.;
+        for (int fl = 0; fl < nf; fl++) {
+            long k = fl * c->nn + n;
+            if (f->npts[k] <= 0) continue;
+            Pc[0] += f->px[k];
+            Pc[1] += f->py[k];
+            Pc[2] += f->pz[k];
+            Mc += f->mass[k];
+            act[nm++] = fl;
+        }
+        if (nm <= 1) continue;
+        int doingPairs = nm == 2;
+        int miMax = doingPairs ? nm - 1 : nm;
+        double dispc[3] = {0., 0., 0.};
+        for (int fl = 0; fl < nf; fl++) {
+            long k = fl * c->nn + n;
+            if (f->npts[k] <= 0) continue;
+            dispc[0] += f->ux[k];
+            dispc[1] += f->uy[k];
+            dispc[2] += f->uz[k];
+        }
+        double rMc = 1. / Mc;
+        for (int a = 0; a < 3; a++) dispc[a] *= rMc;
+        for (int mi = 0; mi < miMax; mi++) {
+            long ki = act[mi] * c->nn + n;
+            double massi = f->mass[ki];
+            double voli = f->vol[ki];
+            double voltot = 0.;
+            for (int fl = 0; fl < nf; fl++) {
+                long k = fl * c->nn + n;
+                if (f->npts[k] > 0) voltot += f->vol[k];
+            }
+            double volj = voltot - voli;
+            int j = -1;
+            double gradj[3] = {0., 0., 0.}, maxOther = 0.;
+            for (int kj = 0; kj < nm; kj++) {
+                if (kj == mi) continue;
+                long kk = act[kj] * c->nn + n;
+                if (f->vol[kk] > maxOther) {
+                    maxOther = f->vol[kk];
+                    j = act[kj];
+                }
+                gradj[0] += f->gvx[kk] * -1.;
+                gradj[1] += f->gvy[kk] * -1.;
+                gradj[2] += f->gvz[kk] * -1.;
+            }
+            if (j < 0) continue;
+            double massRatio = massi / Mc;
+            double mred = 1. - massRatio;
+            double delPi[3] = {f->px[ki] * -1., f->py[ki] * -1., f->pz[ki] * -1.};
+            delPi[0] += Pc[0] * massRatio;
+            delPi[1] += Pc[1] * massRatio;
+            delPi[2] += Pc[2] * massRatio;
+            double normi[3] = {f->gvx[ki] * 1., f->gvy[ki] * 1., f->gvz[ki] * 1.}, norm[3];
+            if (c->normals == 0) {
+                double magi = sqrt(dot3(normi, normi)), magj = sqrt(dot3(gradj, gradj));
+                if (magi >= 1. * magj) for (int a = 0; a < 3; a++) norm[a] = normi[a] * (1. / magi);
+                else for (int a = 0; a < 3; a++) norm[a] = gradj[a] * (1. / magj);
+            } else if (c->normals == 1) {
+                if (voli >= volj) for (int a = 0; a < 3; a++) norm[a] = normi[a];
+                else for (int a = 0; a < 3; a++) norm[a] = gradj[a];
+                double s = 1. / sqrt(dot3(norm, norm));
+                for (int a = 0; a < 3; a++) norm[a] = norm[a] * s;
+            } else {
+                for (int a = 0; a < 3; a++) norm[a] = normi[a] + gradj[a];
+                double magi = dot3(norm, norm);
+                double s = 1. / sqrt(magi);
+                for (int a = 0; a < 3; a++) norm[a] *= s;
+            }
+            if (norm[0] != norm[0] || norm[1] != norm[1] || norm[2] != norm[2]) continue;
+            double dotn = dot3(delPi, norm);
+            double rmi = 1. / massi;
+            double dispa[3] = {f->ux[ki] * rmi, f->uy[ki] * rmi, f->uz[ki] * rmi};
+            double delta[3] = {dispc[0] - dispa[0], dispc[1] - dispa[1], dispc[2] - dispa[2]};
+            double rmred = 1. / mred;
+            for (int a = 0; a < 3; a++) delta[a] *= rmred;
+            double dispb[3] = {delta[0] + dispa[0], delta[1] + dispa[1], delta[2] + dispa[2]};
+            double deln = dot3(dispb, norm) - dot3(dispa, norm);
+            mred *= massi;
+            double delFi[3], *dfp = NULL;
+            if (postUpdate) {
+                double Fc[3] = {0., 0., 0.};
+                for (int fl = 0; fl < nf; fl++) {
+                    long k = fl * c->nn + n;
+                    if (f->npts[k] <= 0) continue;
+                    Fc[0] += f->fx[k];
+                    Fc[1] += f->fy[k];
+                    Fc[2] += f->fz[k];
+                }
+                double r = massi / Mc;
+                delFi[0] = Fc[0] * r + f->fx[ki] * -1.;
+                delFi[1] = Fc[1] * r + f->fy[ki] * -1.;
+                delFi[2] = Fc[2] * r + f->fz[ki] * -1.;
+                dfp = delFi;
+            }
+            if (!coulomb_delta(c, delPi, norm, dotn, deln, mred, dfp)) continue;
+            change_momentum(c, ki, delPi, callType);
+            if (doingPairs) {
+                for (int a = 0; a < 3; a++) delPi[a] *= -1.;
+                change_momentum(c, (long)j * c->nn + n, delPi, callType);
+            }
+        }
+    }
 }
 
 /* One NairnMPM::MPMStep with the task chain of NairnMPM::CreateTasks
@@ -1330,7 +1593,7 @@ static void zero_field(OField *f, long nn) {
 static int one_step(OCtx *c) {
     MpmGpuParticles *p = c->p;
     OField *f = &c->f;
-    long nn = c->g.nnodes + 1;
+    long nn = c->nfn;   /* every field of every node */
     int method = c->o->method;
     double dt = c->dt;
     double fusf = c->o->fraction_usf;
@@ -1355,6 +1618,7 @@ static int one_step(OCtx *c) {
     for (long i = 1; i < nn; i++) {
         if (f->npts[i] > 0) { f->cx[i] = f->px[i]; f->cy[i] = f->py[i]; f->cz[i] = f->pz[i]; }
     }
+    if (c->mm) material_contact(c, MASS_MOMENTUM_CALL);
     if (method == MPMGPU_USF || method == MPMGPU_USAVG) velocity_bc_loop(c, MASS_MOMENTUM_CALL);
 
     /* UpdateStrainsFirstTask */
@@ -1377,6 +1641,7 @@ static int one_step(OCtx *c) {
             f->pz[i] += f->fz[i] * dt;
         }
     }
+    if (c->mm) material_contact(c, UPDATE_MOMENTUM_CALL);
     velocity_bc_loop(c, UPDATE_MOMENTUM_CALL);
 
     /* UpdateParticlesTask */
@@ -1384,10 +1649,19 @@ static int one_step(OCtx *c) {
 
     /* UpdateStrainsLastContactTask */
     if (method == MPMGPU_USL || method == MPMGPU_USAVG) {
+        /* RezeroNodeTask6: momenta and contact terms */
         for (long i = 1; i < nn; i++) {
-            if (f->npts[i] > 0) { f->px[i] = 0.; f->py[i] = 0.; f->pz[i] = 0.; }
+            if (f->npts[i] > 0) {
+                f->px[i] = 0.; f->py[i] = 0.; f->pz[i] = 0.;
+                if (c->mm) {
+                    f->vol[i] = 0.;
+                    f->ux[i] = 0.; f->uy[i] = 0.; f->uz[i] = 0.;
+                    f->gvx[i] = 0.; f->gvy[i] = 0.; f->gvz[i] = 0.;
+                }
+            }
         }
         p2g_mass_momentum(c, 1);
+        if (c->mm) material_contact(c, UPDATE_STRAINS_LAST_CALL);
         velocity_bc_loop(c, UPDATE_STRAINS_LAST_CALL);
         strain_update(c, stLast);
     }
@@ -1403,7 +1677,12 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     if (!grid || !opts || !mats || !p) return fail(MPMGPU_ERR_INVALID, "oracle: null argument");
     if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI)
         return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: shape function not implemented");
-    if (contact && contact->enabled) return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: contact not implemented");
+    if (contact && contact->enabled) {
+        if (contact->normals < 0 || contact->normals > 2)
+            return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: contact normals must be method 0, 1 or 2");
+        if (contact->contact_cutoff > 0.)
+            return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: position-based contact not implemented");
+    }
     OCtx c;
     memset(&c, 0, sizeof(c));
     c.g.dim = grid->dim;
@@ -1430,9 +1709,25 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     int np = grid->dim == 3 ? MPMGPU_THREED : MPMGPU_PLANE_STRAIN;
     int st = load_materials(mats, nmat, np, c.mats);
     if (st != MPMGPU_OK) { free(c.mats); return st; }
-    long nn = c.g.nnodes + 1;
+    /* material velocity fields: one, or one per field in multimaterial mode */
+    c.nf = 1;
+    for (int i = 0; i < nmat; i++)
+        if (mats[i].field + 1 > c.nf) c.nf = mats[i].field + 1;
+    if (c.nf > 64) { free(c.mats); return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: more than 64 material fields"); }
+    c.mm = c.nf > 1 && contact && contact->enabled;
+    if (c.nf > 1 && !c.mm) { free(c.mats); return fail(MPMGPU_ERR_INVALID, "oracle: several material fields need contact"); }
+    if (c.mm) {
+        c.normals = contact->normals;
+        c.friction = contact->friction;
+        /* CoulombFriction::VerifyAndLoadProperties: <0 stick, 0 frictionless */
+        c.friction_style = contact->friction < 0. ? 0 : (contact->friction == 0. ? 1 : 2);
+    }
+    c.nn = c.g.nnodes + 1;
+    c.nfn = c.nn * c.nf;
+    long nn = c.nfn;
     double **fl[] = {&c.f.mass, &c.f.px, &c.f.py, &c.f.pz, &c.f.fx, &c.f.fy, &c.f.fz,
-                     &c.f.vx, &c.f.vy, &c.f.vz, &c.f.cx, &c.f.cy, &c.f.cz};
+                     &c.f.vx, &c.f.vy, &c.f.vz, &c.f.cx, &c.f.cy, &c.f.cz,
+                     &c.f.vol, &c.f.ux, &c.f.uy, &c.f.uz, &c.f.gvx, &c.f.gvy, &c.f.gvz};
     for (unsigned k = 0; k < sizeof(fl) / sizeof(fl[0]); k++) *fl[k] = (double *)calloc((size_t)nn, sizeof(double));
     c.f.npts = (int *)calloc((size_t)nn, sizeof(int));
     c.xi = (double *)calloc((size_t)(3 * (p->n > 0 ? p->n : 1)), sizeof(double));

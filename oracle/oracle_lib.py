@@ -58,7 +58,9 @@ def run(model, particles: dict, nsteps: int, t0: float = 0.0, nthreads: int = 1,
     mats = abi.materials_array(model)
     bcs, nbc = abi.bcs_array(model)
     ps = abi.particles_struct(particles, b)
-    ct = contact if contact is not None else abi.MpmGpuContact()
+    if contact is None:
+        contact = abi.contact_struct(model)
+    ct = contact
     st = L.mpm_oracle_run(C.byref(g), C.byref(o), mats, len(model.materials), bcs, nbc, C.byref(ct),
                           C.byref(ps), int(nsteps), float(t0), int(nthreads))
     if st != 0:

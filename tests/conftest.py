@@ -26,6 +26,13 @@ def load_golden(name):
     return meta, {k: d[k] for k in d.files if k != "meta"}
 
 
+def view_for(p, m):
+    """archive_view with each particle's material density and type."""
+    rho = np.array([q["rho"] for q in m.materials])[p["mat"]]
+    typ = np.array([q["type"] for q in m.materials])[p["mat"]]
+    return archive_view(p, m.grid.dim, rho, typ)
+
+
 def model_for(meta):
     from nairn_gb300 import model
     return getattr(model, meta["generator"])(**meta["kwargs"])
@@ -41,10 +48,14 @@ def rel_l2(a, b):
 def archive_view(p, dim, rho_gcc, mat_type=1):
     """Particle dict -> the quantities a NairnMPM archive stores (ArchiveData.cpp:807-930).
     The stress is (s - P) rho0 / J, with J the relative volume: 1 for the
-    small-strain materials, history 0 for Neohookean (type 28)."""
+    small-strain materials, history 0 for Neohookean (type 28).  rho_gcc and
+    mat_type may be per-particle arrays (several materials)."""
     P = p["pressure"]
-    rho = rho_gcc * 1e-3
-    if mat_type == 28:
+    rho = np.asarray(rho_gcc, dtype=np.float64) * 1e-3
+    neo = np.asarray(mat_type) == 28
+    if rho.ndim:
+        rho = (rho / np.where(neo, p["hist0"], 1.0))[:, None]
+    elif neo.any():
         rho = rho / p["hist0"][:, None]
     if dim == 2:
         pos = np.stack([p["x"], p["y"]], 1)

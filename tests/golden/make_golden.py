@@ -61,6 +61,13 @@ CASES = {
     "taylor3d_cpdi_usavg": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, gimp="lCPDI")),
     "taylor3d_cpdi_neo_usf": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=80, mat_type=28, G=10.,
                                                 K=50., rho=1.1, v0=-30000., gimp="lCPDI", method=0)),
+    # multimaterial contact: Neo-Hookean block onto an elastic plate whose base is held
+    "contact2d_fric_avgg": ("contact_2d", dict(steps=200, friction=0.3, normals=2)),
+    "contact2d_frictionless_maxg": ("contact_2d", dict(steps=150, friction=0.0, normals=0)),
+    "contact2d_stick_maxv_usl": ("contact_2d", dict(steps=150, friction=-1.0, normals=1, method=3)),
+    "contact2d_fric_cpdi_usf": ("contact_2d", dict(steps=150, friction=0.3, normals=2, gimp="lCPDI", method=0)),
+    "contact3d_fric_cpdi": ("contact_3d", dict(steps=60, friction=0.3, normals=2)),
+    "contact3d_fric_ugimp_maxg": ("contact_3d", dict(steps=60, friction=0.5, normals=0, gimp="uGIMP")),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")

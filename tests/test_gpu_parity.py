@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import archive_view, golden_cases, load_golden, model_for, rel_l2
+from conftest import golden_cases, load_golden, model_for, rel_l2, view_for
 
 pytestmark = pytest.mark.gpu
 
@@ -24,7 +24,7 @@ def test_gpu_matches_reference(case, gpu_lib):
     meta, g = load_golden(case)
     m = model_for(meta)
     out = gpu_run(m, meta["steps"])
-    v = archive_view(out, 3 if meta["three_d"] else 2, m.materials[0]["rho"], m.materials[0]["type"])
+    v = view_for(out, m)
     for k in ("pos", "vel", "stress", "strain"):
         assert rel_l2(v[k], g["final_" + k]) <= TOL, (k, rel_l2(v[k], g["final_" + k]))
     if g["final_hist1"].any():
@@ -96,7 +96,7 @@ def test_mixed_precision_matches_reference(case, gpu_lib):
     meta, g = load_golden(case)
     m = model_for(meta)
     out = gpu_run(m, meta["steps"], precision=1)
-    v = archive_view(out, 3 if meta["three_d"] else 2, m.materials[0]["rho"], m.materials[0]["type"])
+    v = view_for(out, m)
     for k in ("pos", "vel", "stress", "strain"):
         assert rel_l2(v[k], g["final_" + k]) <= TOL_MIXED, (k, rel_l2(v[k], g["final_" + k]))
     assert np.array_equal(v["elem"], g["final_elem"])

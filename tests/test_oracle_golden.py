@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import archive_view, golden_cases, load_golden, model_for, rel_l2
+from conftest import golden_cases, load_golden, model_for, rel_l2, view_for
 
 
 @pytest.mark.parametrize("case", golden_cases())
@@ -28,7 +28,7 @@ def test_oracle_matches_reference(case):
     m = model_for(meta)
     p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
     oracle_lib.run(m, p, meta["steps"], nthreads=1)
-    v = archive_view(p, 3 if meta["three_d"] else 2, m.materials[0]["rho"], m.materials[0]["type"])
+    v = view_for(p, m)
     for k in ("pos", "vel", "stress", "strain"):
         assert rel_l2(v[k], g["final_" + k]) <= 1e-13, k
     if g["final_hist1"].any():
