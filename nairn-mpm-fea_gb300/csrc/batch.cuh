@@ -218,7 +218,7 @@ void batch_link(MpmGpuBatch *b) {
                                            &p.exx, &p.eyy, &p.ezz, &p.exy, &p.exz, &p.eyz, &p.wxy, &p.wxz, &p.wyz,
                                            &p.sxx, &p.syy, &p.szz, &p.sxy, &p.sxz, &p.syz, &p.pressure,
                                            &p.pxx, &p.pyy, &p.pzz, &p.pxy, &p.pxz, &p.pyz,
-                                           &p.hist0, &p.hist1, &p.work, &p.plast, &p.xi, &p.eta, &p.zeta};
+                                           &p.hist0, &p.hist1, &p.work, &p.plast, &p.x0, &p.y0, &p.z0, &p.xi, &p.eta, &p.zeta};
     for (int k = 0; k <= kParticleDoubles; k++) *cols[k] = pb + (size_t)k * cap;
     p.mat = ib;
     p.elem = ib + cap;
@@ -353,18 +353,19 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     StepParams sp{};
     sp.runs = b->runs_dev;
     sp.nrun = b->nrun;
+    sp.ct.nf = 1;
     k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN);
-    k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
+    k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     k_node_post<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, method != MPMGPU_USL);
     if (method == MPMGPU_USL)
         k_strain_forces<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     else
         k_strain_forces<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
-    k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group);
+    k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, 0);
     if (method == MPMGPU_USF) {
-        k_g2p<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
+        k_g2p<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     } else {
-        k_g2p<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
+        k_g2p<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
         k_node_usl<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group);
         k_strain_last<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     }

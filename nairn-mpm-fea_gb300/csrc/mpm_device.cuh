@@ -27,7 +27,8 @@ struct DevGrid {
 // VerifyAndLoadProperties does.
 struct DevMat {
     int type;
-    int field;
+    int field;                                   // material velocity field (multimaterial mode)
+    double rho;                                  // density, g/mm^3 (contact volumes)
     double c11, c12, c22, c33, c41, c42, c44;    // 2D: Elastic::FillUnrotatedElasticProperties
     double C00, C01, C02, C11, C12, C22, C33, C44, C55;  // 3D specific stiffness
     double Gred, Kred;                           // IsoPlasticity specific moduli
@@ -40,6 +41,7 @@ struct DevMat {
 struct DevParticles {
     int n;
     double *x, *y, *z, *vx, *vy, *vz;
+    double *x0, *y0, *z0;      // original position (multimaterial contact displacement)
     double *mass;
     int *mat, *elem;
     double *lpx, *lpy, *lpz;
@@ -70,6 +72,18 @@ struct DevNodes {
     float *vlx, *vly, *vlz;
     float *gx, *gy, *gz;       // FP32 force accumulators
     float *bx, *by, *bz;       // FP32 acceleration for the particle update
+    // multimaterial contact terms (ContactTerms): volume, displacement and
+    // volume gradient extrapolations of each material field
+    double *vol, *dsx, *dsy, *dsz, *gvx, *gvy, *gvz;
+};
+
+// Multimaterial contact settings (MeshInfo and the Coulomb friction law).
+struct DevContact {
+    int nf;          // material velocity fields (1: single material mode)
+    int fstride;     // node-index offset between fields
+    int normals;     // MeshInfo::materialNormalMethod 0, 1 or 2
+    int style;       // CoulombFriction: 0 stick, 1 frictionless, 2 frictional
+    double friction; // Coulomb coefficient
 };
 
 // One run of a batch: its grid, where its nodes and cells start in the
@@ -93,6 +107,7 @@ struct StepParams {
     unsigned *err;
     DevRun *runs;
     const int *nrun;   // run of each node (-1: unused)
+    DevContact ct;     // one field unless multimaterial mode
 };
 
 // Velocity conditions grouped by node, list order kept inside a node.

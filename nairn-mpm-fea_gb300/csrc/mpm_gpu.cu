@@ -24,7 +24,7 @@ using namespace nmg;
 
 namespace {
 
-const int kParticleDoubles = 38;  // double columns of DevParticles besides zeta
+const int kParticleDoubles = 41;  // double columns of DevParticles besides zeta
 
 struct Profile {
     const char *name;
@@ -74,6 +74,8 @@ struct MpmGpuCtx {
     std::vector<cudaEvent_t> ev;         // per-step kernel events when profiling
     long long launches = 0;              // kernels launched by this context
     void *cpdi = nullptr;                // lCPDI corner scratch (ints then doubles)
+    DevContact ct{1, 0, 2, 2, 0.};       // material fields and multimaterial contact
+    bool contact_on = false;
 };
 
 namespace {
@@ -107,6 +109,7 @@ int derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::string &wh
     std::memset(&m, 0, sizeof(m));
     m.type = in.type;
     m.field = in.field;
+    m.rho = in.rho * 0.001;
     m.kterms = kterms > 0 ? kterms : (np == MPMGPU_THREED ? 1 : 2);
     if (in.type == MPMGPU_MAT_NEOHOOKEAN) {
         const double rho = in.rho * 0.001;
@@ -199,7 +202,7 @@ void link_columns(DevParticles &p, double *pb, int *ib, int **orig) {
                                            &p.exx, &p.eyy, &p.ezz, &p.exy, &p.exz, &p.eyz, &p.wxy, &p.wxz, &p.wyz,
                                            &p.sxx, &p.syy, &p.szz, &p.sxy, &p.sxz, &p.syz, &p.pressure,
                                            &p.pxx, &p.pyy, &p.pzz, &p.pxy, &p.pxz, &p.pyz,
-                                           &p.hist0, &p.hist1, &p.work, &p.plast, &p.xi, &p.eta, &p.zeta};
+                                           &p.hist0, &p.hist1, &p.work, &p.plast, &p.x0, &p.y0, &p.z0, &p.xi, &p.eta, &p.zeta};
     for (int k = 0; k <= kParticleDoubles; k++) *cols[k] = pb + (size_t)k * n;
     p.mat = ib;
     p.elem = ib + n;
@@ -212,7 +215,7 @@ void hcols(const MpmGpuParticles *h, double *out[kParticleDoubles]) {
                                      h->exx, h->eyy, h->ezz, h->exy, h->exz, h->eyz, h->wxy, h->wxz, h->wyz,
                                      h->sxx, h->syy, h->szz, h->sxy, h->sxz, h->syz, h->pressure,
                                      h->pxx, h->pyy, h->pzz, h->pxy, h->pxz, h->pyz,
-                                     h->hist0, h->hist1, h->work, h->plast, nullptr, nullptr};
+                                     h->hist0, h->hist1, h->work, h->plast, h->x0, h->y0, h->z0, nullptr, nullptr};
     std::memcpy(out, tmp, sizeof(tmp));
 }
 
@@ -253,8 +256,6 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
     if (opts->precision != MPMGPU_PREC_FP64 && opts->precision != MPMGPU_PREC_MIXED)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "precision must be MPMGPU_PREC_FP64 or MPMGPU_PREC_MIXED");
-    if (opts->nfields > 1)
-        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "multimaterial contact is not implemented on the device");
     if (!(opts->timestep > 0.)) return set_err(nullptr, MPMGPU_ERR_INVALID, "timestep must be > 0");
     if (grid->nx < 3 || grid->ny < 3 || (grid->dim == 3 && grid->nz < 3) || !grid->xnodes || !grid->ynodes ||
         (grid->dim == 3 && !grid->znodes))
@@ -291,9 +292,19 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     coords.insert(coords.end(), grid->xnodes, grid->xnodes + g.nx + 1);
     coords.insert(coords.end(), grid->ynodes, grid->ynodes + g.ny + 1);
     if (g.dim == 3) coords.insert(coords.end(), grid->znodes, grid->znodes + g.nz + 1);
-    // node columns: mass, p(3), f(3), u(3) are cleared each step; c(3), v(3), a(3) are not
-    const size_t NN = (size_t)g.nnodes;
-    const int ncleared = 10, nkept = 9;
+    // node columns, one entry per material field of each node (field f of
+    // node n at f*nnodes+n): mass, p(3), f(3), u(3) and, with several fields,
+    // the contact terms vol, ds(3), gv(3) are cleared each step; c(3), v(3),
+    // a(3) are not
+    const int nf = opts->nfields > 1 ? opts->nfields : 1;
+    if (nf > kMaxFields) {
+        mpmgpu_destroy(c);
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "more material velocity fields than the device supports (8)");
+    }
+    c->ct.nf = nf;
+    c->ct.fstride = g.nnodes;
+    const size_t NN = (size_t)g.nnodes * nf;
+    const int ncleared = nf > 1 ? 17 : 10, nkept = 9;
     // FP32 columns of the mixed mode: force accumulators (cleared), velocity
     // hi/lo pairs and acceleration
     const int fcleared = 3, fkept = 9;
@@ -322,16 +333,26 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     nd.ux = b + 7 * NN;
     nd.uy = b + 8 * NN;
     nd.uz = b + 9 * NN;
-    nd.cx = b + 10 * NN;
-    nd.cy = b + 11 * NN;
-    nd.cz = b + 12 * NN;
-    nd.vx = b + 13 * NN;
-    nd.vy = b + 14 * NN;
-    nd.vz = b + 15 * NN;
-    nd.ax = b + 16 * NN;
-    nd.ay = b + 17 * NN;
-    nd.az = b + 18 * NN;
-    nd.active = (unsigned char *)(b + 19 * NN);
+    if (nf > 1) {
+        nd.vol = b + 10 * NN;
+        nd.dsx = b + 11 * NN;
+        nd.dsy = b + 12 * NN;
+        nd.dsz = b + 13 * NN;
+        nd.gvx = b + 14 * NN;
+        nd.gvy = b + 15 * NN;
+        nd.gvz = b + 16 * NN;
+    }
+    double *kb = b + ncleared * NN;
+    nd.cx = kb;
+    nd.cy = kb + NN;
+    nd.cz = kb + 2 * NN;
+    nd.vx = kb + 3 * NN;
+    nd.vy = kb + 4 * NN;
+    nd.vz = kb + 5 * NN;
+    nd.ax = kb + 6 * NN;
+    nd.ay = kb + 7 * NN;
+    nd.az = kb + 8 * NN;
+    nd.active = (unsigned char *)(b + (ncleared + nkept) * NN);
     c->nblock_zero_bytes = NN * ncleared * sizeof(double);
     cudaMemset(c->nblock, 0, NN * (ncleared + nkept) * sizeof(double) + NN);
     float *fb = c->fblock;
@@ -370,6 +391,8 @@ int mpmgpu_set_materials(MpmGpuCtx *c, const MpmGpuMaterial *mats, int32_t nmat)
         std::string why;
         int st = derive_material(mats[i], c->opts.np, h[i], why, c->opts.inc_defgrad_terms);
         if (st != MPMGPU_OK) return set_err(c, st, "material " + std::to_string(i) + ": " + why);
+        if (mats[i].field < 0 || mats[i].field >= c->ct.nf)
+            return set_err(c, MPMGPU_ERR_INVALID, "material " + std::to_string(i) + ": field outside 0 .. nfields-1");
     }
     if (c->mats) cudaFree(c->mats);
     c->mats = nullptr;
@@ -380,10 +403,25 @@ int mpmgpu_set_materials(MpmGpuCtx *c, const MpmGpuMaterial *mats, int32_t nmat)
     return MPMGPU_OK;
 }
 
+// MeshInfo::MaterialOutput / CoulombFriction::VerifyAndLoadProperties
+// (MeshInfo.cpp:1128-1190, CoulombFriction.cpp:80-104): normal method and the
+// friction style (coefficient < 0 stick, 0 frictionless, > 0 Coulomb).
 int mpmgpu_set_contact(MpmGpuCtx *c, const MpmGpuContact *contact) {
     if (!c) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_set_contact: null context");
-    if (contact && contact->enabled)
-        return set_err(c, MPMGPU_ERR_UNSUPPORTED, "multimaterial contact is not implemented on the device");
+    if (!contact || !contact->enabled) {
+        c->contact_on = false;
+        return MPMGPU_OK;
+    }
+    if (contact->normals < 0 || contact->normals > 2)
+        return set_err(c, MPMGPU_ERR_UNSUPPORTED,
+                       "contact normals: only volume-gradient methods 0 (max gradient), 1 (max volume) and 2 "
+                       "(average gradient) are implemented on the device");
+    if (contact->contact_cutoff > 0.)
+        return set_err(c, MPMGPU_ERR_UNSUPPORTED, "position-based contact is not implemented on the device");
+    c->ct.normals = contact->normals;
+    c->ct.friction = contact->friction;
+    c->ct.style = contact->friction < 0. ? 0 : (contact->friction == 0. ? 1 : 2);
+    c->contact_on = true;
     return MPMGPU_OK;
 }
 
@@ -544,9 +582,10 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
         if (!begin) c->launches++;
     };
     cudaMemsetAsync(c->nblock, 0, c->nblock_zero_bytes, s);
-    cudaMemsetAsync(c->nd.active, 0, (size_t)NN, s);
+    cudaMemsetAsync(c->nd.active, 0, (size_t)NN * c->ct.nf, s);
     if (MIX) cudaMemsetAsync(c->fblock, 0, c->fblock_zero_bytes, s);
     StepParams sp;
+    sp.ct = c->ct;
     sp.g = c->g;
     sp.dt = dt;
     sp.st_first = stFirst;
@@ -556,7 +595,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     sp.runs = nullptr;
     sp.nrun = nullptr;
     mark(0, true);
-    k_p2g<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
+    k_p2g<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     mark(0, false);
     mark(1, true);
     k_node_post<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL);
@@ -568,15 +607,16 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
         k_strain_forces<DIM, SHAPE, true, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     mark(2, false);
     mark(3, true);
-    k_node_update<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
+    k_node_update<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group,
+                                                     c->ct.nf > 1 && method != MPMGPU_USF);
     mark(3, false);
     mark(4, true);
     if (method == MPMGPU_USF) {
-        k_g2p<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
+        k_g2p<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
         mark(4, false);
         return;
     }
-    k_g2p<DIM, SHAPE, true, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
+    k_g2p<DIM, SHAPE, true, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     mark(4, false);
     mark(5, true);
     k_node_usl<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
@@ -638,6 +678,8 @@ namespace {
 int step_impl(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
     if (!c || nsteps < 0) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step: bad argument");
     if (c->p.n <= 0 || !c->mats) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step: no particles or materials");
+    if (c->ct.nf > 1 && !c->contact_on)
+        return set_err(c, MPMGPU_ERR_INVALID, "several material fields need multimaterial contact (mpmgpu_set_contact)");
     for (auto &pr : c->prof) pr.ms = 0.;
     if (c->profile && ensure_events(c, nsteps) != 0) return set_err(c, MPMGPU_ERR_CUDA, "event creation failed");
     std::vector<char> sorted((size_t)nsteps, 0);

@@ -363,13 +363,50 @@ struct Wt<true> {
     using T = float;
 };
 
+// node-index offset of the particle's material velocity field
+__device__ __forceinline__ int field_offset(const StepParams &sp, const DevMat *mats, const DevParticles &p, int i) {
+    return sp.ct.nf > 1 ? mats[p.mat[i]].field * sp.ct.fstride : 0;
+}
+
+// particle volume for contact (MatPoint2D/3D::GetVolume with DEFORMED_AREA,
+// MatPoint2D.cpp:407-417, MatPoint3D.cpp:395-408): det F * mp / rho, the 2D
+// form without F_zz
+template <int DIM>
+__device__ __forceinline__ double contact_volume(const DevParticles &p, int i, double rho) {
+    const double F00 = 1. + p.exx[i], F01 = 0.5 * (p.exy[i] - p.wxy[i]), F10 = 0.5 * (p.exy[i] + p.wxy[i]);
+    const double F11 = 1. + p.eyy[i];
+    if (DIM == 2) return (F00 * F11 - F10 * F01) * p.mass[i] / rho;
+    const double F22 = 1. + p.ezz[i];
+    const double F02 = 0.5 * (p.exz[i] - p.wxz[i]), F20 = 0.5 * (p.exz[i] + p.wxz[i]);
+    const double F12 = 0.5 * (p.eyz[i] - p.wyz[i]), F21 = 0.5 * (p.eyz[i] + p.wyz[i]);
+    const double J = F00 * (F11 * F22 - F21 * F12) - F01 * (F10 * F22 - F20 * F12) + F02 * (F10 * F21 - F20 * F11);
+    return J * p.mass[i] / rho;
+}
+
+// multimaterial contact terms of one particle at node k: volume, mass-weighted
+// displacement and volume gradient (CrackVelocityField::AddVolumeDisplacement,
+// CrackVelocityFieldMulti::AddVolumeGradient)
+template <int DIM>
+__device__ __forceinline__ void add_contact_terms(const DevNodes &nd, int k, double N, double fnmp, double Vp,
+                                                  const double d[3], double gx, double gy, double gz) {
+    atomicAdd(&nd.vol[k], N * Vp);
+    atomicAdd(&nd.dsx[k], d[0] * fnmp);
+    atomicAdd(&nd.dsy[k], d[1] * fnmp);
+    atomicAdd(&nd.gvx[k], gx * Vp);
+    atomicAdd(&nd.gvy[k], gy * Vp);
+    if (DIM == 3) {
+        atomicAdd(&nd.dsz[k], d[2] * fnmp);
+        atomicAdd(&nd.gvz[k], gz * Vp);
+    }
+}
+
 // InitializationTask::Execute (natural coordinates, InitializationTask.cpp:59-83)
 // and MassAndMomentumTask::Execute with NodalPoint::AddMassMomentum
 // (MassAndMomentumTask.cpp:48-127, NodalPointMPM.cpp:419-453).  Momentum and
 // mass accumulate in FP64 in both modes: grid velocities carry the bulk motion
 // and their differences across a cell are the strain rate.
 template <int DIM, int SHAPE, bool MIX, bool BATCH>
-__global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevNodes nd) {
+__global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -385,22 +422,38 @@ __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevN
     if (DIM == 3) p.zeta[i] = zeta;
     const double mp = p.mass[i];
     const double vx = p.vx[i], vy = p.vy[i], vz = DIM == 3 ? p.vz[i] : 0.;
-    auto scatter = [&](int n, T N, T, T, T) {
+    const int off = field_offset(sp, mats, p, i);
+    const bool mm = sp.ct.nf > 1;
+    double Vp = 0., d[3] = {0., 0., 0.};
+    if (mm) {
+        Vp = contact_volume<DIM>(p, i, mats[p.mat[i]].rho);
+        d[0] = p.x[i] - p.x0[i];
+        d[1] = p.y[i] - p.y0[i];
+        if (DIM == 3) d[2] = p.z[i] - p.z0[i];
+    }
+    auto scatter = [&](int n, T N, T gx, T gy, T gz) {
         if (N == T(0)) return;
+        n += off;
         const double fnmp = (double)N * mp;
         atomicAdd(&nd.mass[n], fnmp);
         atomicAdd(&nd.px[n], vx * fnmp);
         atomicAdd(&nd.py[n], vy * fnmp);
         if (DIM == 3) atomicAdd(&nd.pz[n], vz * fnmp);
         nd.active[n] = 1;
+        if (mm) add_contact_terms<DIM>(nd, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz);
     };
     if constexpr (SHAPE == SHAPE_LCPDI) {
         // ElementBase::GetShapeFunctionData: the particle's CPDI corners for this step
         if (!cpdi_setup<DIM>(g, p, i, rv.err)) return;
-        cpdi_nodes<DIM, false, T>(g, rv.nb, p, i, scatter);
+        if (mm) cpdi_nodes<DIM, true, T>(g, rv.nb, p, i, scatter);
+        else cpdi_nodes<DIM, false, T>(g, rv.nb, p, i, scatter);
     } else {
-        for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, p.lpx[i], p.lpy[i],
-                                            DIM == 3 ? p.lpz[i] : 1., scatter);
+        if (mm)
+            for_each_node<DIM, SHAPE, true, T>(g, rv.nb, e, xi, eta, zeta, p.lpx[i], p.lpy[i],
+                                               DIM == 3 ? p.lpz[i] : 1., scatter);
+        else
+            for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, p.lpx[i], p.lpy[i],
+                                                DIM == 3 ? p.lpz[i] : 1., scatter);
     }
 }
 
@@ -429,7 +482,7 @@ __device__ __forceinline__ void constitutive(const DevMat *mats, const DevPartic
 // before any rounding.
 template <int DIM, int SHAPE, bool MIX>
 __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, const DevParticles &p, const DevNodes &nd,
-                                                  int i, double st, double du[9]) {
+                                                  int i, double st, double du[9], int off) {
     using T = typename Wt<MIX>::T;
     T d[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     float ph[3] = {0.f, 0.f, 0.f}, pl[3] = {0.f, 0.f, 0.f};
@@ -440,6 +493,7 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, cons
     }
     visit_nodes<DIM, SHAPE, true, T>(g, nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
+                                           n += off;
                                            T vx, vy, vz = 0;
                                            if (MIX) {
                                                vx = (T)((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0]));
@@ -478,9 +532,10 @@ __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticl
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
     const DevGrid &g = rv.g;
+    const int off = field_offset(sp, mats, p, i);
     if (STRAIN) {
         double du[9];
-        velocity_gradient<DIM, SHAPE, MIX>(g, rv.nb, p, nd, i, rv.st_first, du);
+        velocity_gradient<DIM, SHAPE, MIX>(g, rv.nb, p, nd, i, rv.st_first, du, off);
         constitutive<DIM>(mats, p, i, du);
     }
     // -mp * (sigma - P I): the internal force of GetFintPlusFext, scaled once
@@ -490,6 +545,7 @@ __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticl
             syz = DIM == 3 ? (T)(-mp * p.syz[i]) : T(0);
     visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
+                                           n += off;
                                            T fx, fy, fz = 0;
                                            if (DIM == 2) {
                                                fx = sxx * dx + sxy * dy;
@@ -577,7 +633,7 @@ __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticl
 // v_particle + sum N (v_node - v_particle) (the weights sum to one) with the
 // differences from FP32 pairs, S a in FP32; the update itself is FP64.
 template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH>
-__global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevNodes nd) {
+__global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -595,6 +651,7 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
 #pragma unroll
         for (int a = 0; a < DIM; a++) split2(v[a], ph[a], pl[a]);
     }
+    const int off = field_offset(sp, mats, p, i);
     // the particle's nodes for this step (CPDI corners or the element window)
     auto visit = [&](auto &&fn) {
         if constexpr (SHAPE == SHAPE_LCPDI) cpdi_nodes<DIM, false, T>(g, rv.nb, p, i, fn);
@@ -602,6 +659,7 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
     };
     visit([&](int n, T N, T, T, T) {
         if (N == T(0)) return;
+        n += off;
         if (MIX) {
             Sv[0] += ((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0])) * N;
             Sv[1] += ((nd.vhy[n] - ph[1]) + (nd.vly[n] - pl[1])) * N;
@@ -637,14 +695,31 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
         p.z[i] = xp[2];
     }
     if (USL) {
+        // second extrapolation (NodalPoint::AddMassMomentumLast), with the
+        // contact terms at the moved positions in multimaterial mode
         const double mp = p.mass[i];
-        visit([&](int n, T N, T, T, T) {
+        double Vp = 0., d[3] = {0., 0., 0.};
+        if (sp.ct.nf > 1) {
+            Vp = contact_volume<DIM>(p, i, mats[p.mat[i]].rho);
+            d[0] = xp[0] - p.x0[i];
+            d[1] = xp[1] - p.y0[i];
+            if (DIM == 3) d[2] = xp[2] - p.z0[i];
+        }
+        auto scatter = [&](int n, T N, T gx, T gy, T gz) {
             if (N == T(0)) return;
+            n += off;
             const double fnmp = (double)N * mp;
             atomicAdd(&nd.ux[n], v[0] * fnmp);
             atomicAdd(&nd.uy[n], v[1] * fnmp);
             if (DIM == 3) atomicAdd(&nd.uz[n], v[2] * fnmp);
-        });
+            if (sp.ct.nf > 1) add_contact_terms<DIM>(nd, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz);
+        };
+        if (sp.ct.nf > 1) {
+            if constexpr (SHAPE == SHAPE_LCPDI) cpdi_nodes<DIM, true, T>(g, rv.nb, p, i, scatter);
+            else for_each_node<DIM, SHAPE, true, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, scatter);
+        } else {
+            visit(scatter);
+        }
     } else {
         reset_element<DIM>(g, p, i, rv.err);
     }
@@ -659,7 +734,7 @@ __global__ void __launch_bounds__(256) k_strain_last(StepParams sp, DevParticles
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
     double du[9];
-    velocity_gradient<DIM, SHAPE, MIX>(rv.g, rv.nb, p, nd, i, rv.st_last, du);
+    velocity_gradient<DIM, SHAPE, MIX>(rv.g, rv.nb, p, nd, i, rv.st_last, du, field_offset(sp, mats, p, i));
     constitutive<DIM>(mats, p, i, du);
     reset_element<DIM>(rv.g, p, i, rv.err);
 }
@@ -753,95 +828,350 @@ __device__ __forceinline__ bool node_run(const StepParams &sp, int n, double &t,
     return true;
 }
 
+// ---------------------------------------------------------------------------
+// multimaterial contact
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ double dot3(const double a[3], const double b[3]) {
+    return a[0] * b[0] + a[1] * b[1] + a[2] * b[2];
+}
+
+// MatVelocityField::ChangeMatMomentum (MatVelocityField.cpp:197-228)
+__device__ __forceinline__ void change_momentum(const DevNodes &nd, int k, const double d[3], int pass, double dt) {
+    nd.px[k] += d[0];
+    nd.py[k] += d[1];
+    nd.pz[k] += d[2];
+    if (pass == BC_UPDATE_MOMENTUM) {
+        const double s = 1. / dt;
+        nd.fx[k] += d[0] * s;
+        nd.fy[k] += d[1] * s;
+        nd.fz[k] += d[2] * s;
+    } else if (pass == BC_MASS_MOMENTUM) {
+        nd.cx[k] = nd.px[k];
+        nd.cy[k] = nd.py[k];
+        nd.cz[k] = nd.pz[k];
+    }
+}
+
+// CoulombFriction::GetFrictionalDeltaMomentum (CoulombFriction.cpp:146-262)
+// without a static coefficient; false: the law leaves the momenta alone
+__device__ __forceinline__ bool coulomb_delta(const DevContact &ct, double delPi[3], const double norm[3],
+                                              double dotn, double deln, double mred, const double *delFi,
+                                              double dt) {
+    if (ct.style == 0) return true;
+    if (delFi) deln += dt * (dotn - 0.5 * dot3(delFi, norm) * dt) / mred;
+    const bool inContact = deln < 0. && dotn < 0.;
+    if (ct.style == 1) {
+        if (!inContact) return false;
+#pragma unroll
+        for (int a = 0; a < 3; a++) delPi[a] = norm[a] * dotn;
+        return true;
+    }
+    if (!inContact) return false;
+    double dott = 0., tang[3];
+#pragma unroll
+    for (int a = 0; a < 3; a++) tang[a] = delPi[a] + norm[a] * (-dotn);
+    const double tangMag = sqrt(dot3(tang, tang));
+    if (tangMag > 0.) {
+        const double s = 1. / tangMag;
+#pragma unroll
+        for (int a = 0; a < 3; a++) tang[a] *= s;
+        dott = dot3(delPi, tang);
+        if (dott < 0.) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) tang[a] = -tang[a];
+            dott = -dott;
+        }
+    }
+    const double slide = ct.friction * (-dotn);
+    if (slide <= 0.) {
+#pragma unroll
+        for (int a = 0; a < 3; a++) delPi[a] = norm[a] * dotn;
+    } else if (dott > slide) {
+#pragma unroll
+        for (int a = 0; a < 3; a++) delPi[a] = norm[a] * dotn + tang[a] * slide;
+    }
+    return true;
+}
+
+// CrackVelocityFieldMulti::MaterialContactOnCVF / MaterialContactOnCVFLumped
+// (CrackVelocityFieldMulti.cpp:302-671) at node n for nonrigid materials:
+// each material against the others lumped (two materials: one pair with
+// equal and opposite momentum changes), normal from volume gradients
+// (GetNormalVector :960-1069, methods 0-2), separation from the extrapolated
+// displacements (CrackSurfaceContact::MaterialSeparation), Coulomb friction.
+constexpr int kMaxFields = 8;
+__device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, int pass, double dt) {
+    const int S = ct.fstride;
+    int act[kMaxFields], nm = 0;
+    double Pc[3] = {0., 0., 0.}, Mc = 0., dispc[3] = {0., 0., 0.}, voltot = 0.;
+    for (int f = 0; f < ct.nf; f++) {
+        const int k = f * S + n;
+        if (!nd.active[k]) continue;
+        Pc[0] += nd.px[k];
+        Pc[1] += nd.py[k];
+        Pc[2] += nd.pz[k];
+        Mc += nd.mass[k];
+        dispc[0] += nd.dsx[k];
+        dispc[1] += nd.dsy[k];
+        dispc[2] += nd.dsz[k];
+        voltot += nd.vol[k];
+        act[nm++] = f;
+    }
+    if (nm <= 1) return;
+    const bool pairs = nm == 2;
+    const int miMax = pairs ? 1 : nm;
+    const double rMc = 1. / Mc;
+#pragma unroll
+    for (int a = 0; a < 3; a++) dispc[a] *= rMc;
+    for (int mi = 0; mi < miMax; mi++) {
+        const int ki = act[mi] * S + n;
+        const double massi = nd.mass[ki], voli = nd.vol[ki];
+        const double volj = voltot - voli;
+        int j = -1;
+        double gradj[3] = {0., 0., 0.}, maxOther = 0.;
+        for (int kj = 0; kj < nm; kj++) {
+            if (kj == mi) continue;
+            const int kk = act[kj] * S + n;
+            if (nd.vol[kk] > maxOther) {
+                maxOther = nd.vol[kk];
+                j = act[kj];
+            }
+            gradj[0] -= nd.gvx[kk];
+            gradj[1] -= nd.gvy[kk];
+            gradj[2] -= nd.gvz[kk];
+        }
+        if (j < 0) continue;
+        const double massRatio = massi / Mc;
+        double mred = 1. - massRatio;
+        double delPi[3] = {Pc[0] * massRatio - nd.px[ki], Pc[1] * massRatio - nd.py[ki],
+                           Pc[2] * massRatio - nd.pz[ki]};
+        const double normi[3] = {nd.gvx[ki], nd.gvy[ki], nd.gvz[ki]};
+        double norm[3];
+        if (ct.normals == 0) {
+            const double magi = sqrt(dot3(normi, normi)), magj = sqrt(dot3(gradj, gradj));
+            const bool useI = magi >= magj;
+            const double s = 1. / (useI ? magi : magj);
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] = (useI ? normi[a] : gradj[a]) * s;
+        } else if (ct.normals == 1) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] = voli >= volj ? normi[a] : gradj[a];
+            const double s = 1. / sqrt(dot3(norm, norm));
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] *= s;
+        } else {
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] = normi[a] + gradj[a];
+            const double s = 1. / sqrt(dot3(norm, norm));
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] *= s;
+        }
+        if (norm[0] != norm[0] || norm[1] != norm[1] || norm[2] != norm[2]) continue;
+        const double dotn = dot3(delPi, norm);
+        const double rmi = 1. / massi, rmred = 1. / mred;
+        const double dispa[3] = {nd.dsx[ki] * rmi, nd.dsy[ki] * rmi, nd.dsz[ki] * rmi};
+        double dispb[3];
+#pragma unroll
+        for (int a = 0; a < 3; a++) dispb[a] = (dispc[a] - dispa[a]) * rmred + dispa[a];
+        const double deln = dot3(dispb, norm) - dot3(dispa, norm);
+        mred *= massi;
+        double delFi[3];
+        const double *dfp = nullptr;
+        if (pass == BC_UPDATE_MOMENTUM) {
+            double Fc[3] = {0., 0., 0.};
+            for (int q = 0; q < nm; q++) {
+                const int k = act[q] * S + n;
+                Fc[0] += nd.fx[k];
+                Fc[1] += nd.fy[k];
+                Fc[2] += nd.fz[k];
+            }
+            delFi[0] = Fc[0] * massRatio - nd.fx[ki];
+            delFi[1] = Fc[1] * massRatio - nd.fy[ki];
+            delFi[2] = Fc[2] * massRatio - nd.fz[ki];
+            dfp = delFi;
+        }
+        if (!coulomb_delta(ct, delPi, norm, dotn, deln, mred, dfp, dt)) continue;
+        change_momentum(nd, ki, delPi, pass, dt);
+        if (pairs) {
+            const double neg[3] = {-delPi[0], -delPi[1], -delPi[2]};
+            change_momentum(nd, j * S + n, neg, pass, dt);
+        }
+    }
+}
+
+// store the updated momentum and force, grid velocity, and the acceleration
+// f/m for the particle update (every active node has mass > 0)
+template <int DIM, bool MIX>
+__device__ __forceinline__ void node_finish_update(const DevNodes &nd, int k, double m, const double p[3],
+                                                   const double fr[3]) {
+    nd.px[k] = p[0];
+    nd.py[k] = p[1];
+    nd.fx[k] = fr[0];
+    nd.fy[k] = fr[1];
+    if (DIM == 3) {
+        nd.pz[k] = p[2];
+        nd.fz[k] = fr[2];
+    }
+    node_velocity<MIX>(nd, k, m, p);
+    const double r = 1. / m;
+    nd.ax[k] = fr[0] * r;
+    nd.ay[k] = fr[1] * r;
+    if (DIM == 3) nd.az[k] = fr[2] * r;
+    if (MIX) {
+        nd.bx[k] = (float)(fr[0] * r);
+        nd.by[k] = (float)(fr[1] * r);
+        if (DIM == 3) nd.bz[k] = (float)(fr[2] * r);
+    }
+}
+
+// true when any material field of node n has particles
+__device__ __forceinline__ bool node_active(const StepParams &sp, const DevNodes &nd, int n) {
+    for (int f = 0; f < sp.ct.nf; f++)
+        if (nd.active[f * sp.ct.fstride + n]) return true;
+    return false;
+}
+
+// PostExtrapolationTask::Execute (PostExtrapolationTask.cpp:46-165):
+// vk[pkCopy] = pk, contact (MASS_MOMENTUM_CALL), velocity conditions, grid
+// velocity, on every material field of the node.
 template <int DIM, bool MIX, bool BATCH>
 __global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group, int do_bcs) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nnodes || !nd.active[n]) return;
+    if (n >= nnodes || !node_active(sp, nd, n)) return;
     double t, dt;
     if (!node_run<BATCH>(sp, n, t, dt)) return;
-    double p[3] = {nd.px[n], nd.py[n], DIM == 3 ? nd.pz[n] : 0.};
-    nd.cx[n] = p[0];
-    nd.cy[n] = p[1];
-    if (DIM == 3) nd.cz[n] = p[2];
-    const double m = nd.mass[n];
     const int grp = bc_group[n];
-    if (do_bcs && grp >= 0) {
-        double f[3] = {0., 0., 0.};
-        node_bcs(b, grp, BC_MASS_MOMENTUM, m, t, dt, p, f);
-        nd.px[n] = p[0];
-        nd.py[n] = p[1];
-        if (DIM == 3) nd.pz[n] = p[2];
+    for (int f = 0; f < sp.ct.nf; f++) {
+        const int k = f * sp.ct.fstride + n;
+        if (!nd.active[k]) continue;
+        nd.cx[k] = nd.px[k];
+        nd.cy[k] = nd.py[k];
+        if (DIM == 3) nd.cz[k] = nd.pz[k];
     }
-    node_velocity<MIX>(nd, n, m, p);
+    if (sp.ct.nf > 1) node_contact(sp.ct, nd, n, BC_MASS_MOMENTUM, dt);
+    for (int f = 0; f < sp.ct.nf; f++) {
+        const int k = f * sp.ct.fstride + n;
+        if (!nd.active[k]) continue;
+        double p[3] = {nd.px[k], nd.py[k], DIM == 3 ? nd.pz[k] : 0.};
+        const double m = nd.mass[k];
+        if (do_bcs && grp >= 0) {
+            double fz[3] = {0., 0., 0.};
+            node_bcs(b, grp, BC_MASS_MOMENTUM, m, t, dt, p, fz);
+            nd.px[k] = p[0];
+            nd.py[k] = p[1];
+            if (DIM == 3) nd.pz[k] = p[2];
+        }
+        node_velocity<MIX>(nd, k, m, p);
+    }
 }
 
 // PostForcesTask::Execute (restore momenta, GRID_FORCES_CALL velocity
 // conditions; PostForcesTask.cpp:43-111) and UpdateMomentaTask::Execute
-// (p += f dt, UPDATE_MOMENTUM_CALL conditions; UpdateMomentaTask.cpp:44-94),
-// then grid velocity for the particle update.
+// (p += f dt, contact and UPDATE_MOMENTUM_CALL conditions;
+// UpdateMomentaTask.cpp:44-94), then grid velocity and acceleration for the
+// particle update.  zero_contact: clear the contact terms for the second
+// extrapolation.
 template <int DIM, bool MIX, bool BATCH>
-__global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group) {
+__global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group,
+                              int zero_contact) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nnodes || !nd.active[n]) return;
+    if (n >= nnodes || !node_active(sp, nd, n)) return;
     double t, dt;
     if (!node_run<BATCH>(sp, n, t, dt)) return;
-    double p[3] = {nd.cx[n], nd.cy[n], DIM == 3 ? nd.cz[n] : 0.};
-    double f[3];
-    if (MIX) {
-        f[0] = (double)nd.gx[n];
-        f[1] = (double)nd.gy[n];
-        f[2] = DIM == 3 ? (double)nd.gz[n] : 0.;
-    } else {
-        f[0] = nd.fx[n];
-        f[1] = nd.fy[n];
-        f[2] = DIM == 3 ? nd.fz[n] : 0.;
-    }
-    const double m = nd.mass[n];
     const int grp = bc_group[n];
-    if (grp >= 0) node_bcs(b, grp, BC_GRID_FORCES, m, t, dt, p, f);
+    const bool mm = sp.ct.nf > 1;
+    for (int f = 0; f < sp.ct.nf; f++) {
+        const int k = f * sp.ct.fstride + n;
+        if (!nd.active[k]) continue;
+        double p[3] = {nd.cx[k], nd.cy[k], DIM == 3 ? nd.cz[k] : 0.};
+        double fr[3];
+        if (MIX) {
+            fr[0] = (double)nd.gx[k];
+            fr[1] = (double)nd.gy[k];
+            fr[2] = DIM == 3 ? (double)nd.gz[k] : 0.;
+        } else {
+            fr[0] = nd.fx[k];
+            fr[1] = nd.fy[k];
+            fr[2] = DIM == 3 ? nd.fz[k] : 0.;
+        }
+        const double m = nd.mass[k];
+        if (grp >= 0) node_bcs(b, grp, BC_GRID_FORCES, m, t, dt, p, fr);
 #pragma unroll
-    for (int a = 0; a < 3; a++) p[a] += f[a] * dt;
-    if (grp >= 0) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, f);
-    nd.px[n] = p[0];
-    nd.py[n] = p[1];
-    nd.fx[n] = f[0];
-    nd.fy[n] = f[1];
-    if (DIM == 3) {
-        nd.pz[n] = p[2];
-        nd.fz[n] = f[2];
+        for (int a = 0; a < 3; a++) p[a] += fr[a] * dt;
+        if (mm) {
+            // staged for the contact of all the node's fields
+            nd.px[k] = p[0];
+            nd.py[k] = p[1];
+            nd.pz[k] = p[2];
+            nd.fx[k] = fr[0];
+            nd.fy[k] = fr[1];
+            nd.fz[k] = fr[2];
+            continue;
+        }
+        if (grp >= 0) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, fr);
+        node_finish_update<DIM, MIX>(nd, k, m, p, fr);
     }
-    node_velocity<MIX>(nd, n, m, p);
-    // acceleration for the particle update (every active node has mass > 0)
-    const double r = 1. / m;
-    nd.ax[n] = f[0] * r;
-    nd.ay[n] = f[1] * r;
-    if (DIM == 3) nd.az[n] = f[2] * r;
-    if (MIX) {
-        nd.bx[n] = (float)(f[0] * r);
-        nd.by[n] = (float)(f[1] * r);
-        if (DIM == 3) nd.bz[n] = (float)(f[2] * r);
+    if (!mm) return;
+    node_contact(sp.ct, nd, n, BC_UPDATE_MOMENTUM, dt);
+    for (int f = 0; f < sp.ct.nf; f++) {
+        const int k = f * sp.ct.fstride + n;
+        if (!nd.active[k]) continue;
+        double p[3] = {nd.px[k], nd.py[k], nd.pz[k]}, fr[3] = {nd.fx[k], nd.fy[k], nd.fz[k]};
+        const double m = nd.mass[k];
+        if (grp >= 0) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, fr);
+        node_finish_update<DIM, MIX>(nd, k, m, p, fr);
+        if (zero_contact) {
+            nd.vol[k] = 0.;
+            nd.dsx[k] = nd.dsy[k] = nd.dsz[k] = 0.;
+            nd.gvx[k] = nd.gvy[k] = nd.gvz[k] = 0.;
+        }
     }
 }
 
-// UpdateStrainsLastContactTask: p = second extrapolation, UPDATE_STRAINS_LAST_CALL
-// conditions, grid velocity (UpdateStrainsLastContactTask.cpp:60-152).
+// UpdateStrainsLastContactTask: p = second extrapolation, contact and
+// UPDATE_STRAINS_LAST_CALL conditions, grid velocity
+// (UpdateStrainsLastContactTask.cpp:60-152).
 template <int DIM, bool MIX, bool BATCH>
 __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nnodes || !nd.active[n]) return;
+    if (n >= nnodes || !node_active(sp, nd, n)) return;
     double t, dt;
     if (!node_run<BATCH>(sp, n, t, dt)) return;
-    double p[3] = {nd.ux[n], nd.uy[n], DIM == 3 ? nd.uz[n] : 0.};
-    const double m = nd.mass[n];
     const int grp = bc_group[n];
-    if (grp >= 0) {
-        double f[3] = {0., 0., 0.};
-        node_bcs(b, grp, BC_UPDATE_STRAINS_LAST, m, t, dt, p, f);
+    const bool mm = sp.ct.nf > 1;
+    if (mm) {
+        for (int f = 0; f < sp.ct.nf; f++) {
+            const int k = f * sp.ct.fstride + n;
+            if (!nd.active[k]) continue;
+            nd.px[k] = nd.ux[k];
+            nd.py[k] = nd.uy[k];
+            nd.pz[k] = nd.uz[k];
+        }
+        node_contact(sp.ct, nd, n, BC_UPDATE_STRAINS_LAST, dt);
     }
-    nd.px[n] = p[0];
-    nd.py[n] = p[1];
-    if (DIM == 3) nd.pz[n] = p[2];
-    node_velocity<MIX>(nd, n, m, p);
+    for (int f = 0; f < sp.ct.nf; f++) {
+        const int k = f * sp.ct.fstride + n;
+        if (!nd.active[k]) continue;
+        double p[3];
+        if (mm) {
+            p[0] = nd.px[k];
+            p[1] = nd.py[k];
+            p[2] = nd.pz[k];
+        } else {
+            p[0] = nd.ux[k];
+            p[1] = nd.uy[k];
+            p[2] = DIM == 3 ? nd.uz[k] : 0.;
+        }
+        const double m = nd.mass[k];
+        if (grp >= 0) {
+            double fz[3] = {0., 0., 0.};
+            node_bcs(b, grp, BC_UPDATE_STRAINS_LAST, m, t, dt, p, fz);
+        }
+        nd.px[k] = p[0];
+        nd.py[k] = p[1];
+        if (DIM == 3) nd.pz[k] = p[2];
+        node_velocity<MIX>(nd, k, m, p);
+    }
 }
 
 // End of a batched step: advance the time of every active run and retire
