@@ -26,9 +26,9 @@ def test_batch_bytes_grows_with_capacity(gpu_lib):
     b1 = gpu_lib.mpmgpu_batch_bytes(C.byref(o))
     o.max_particles = 2_000_000
     b2 = gpu_lib.mpmgpu_batch_bytes(C.byref(o))
-    # two arena buffers of 39 doubles + 4 ints per particle, plus sort keys
-    assert b2 - b1 >= 1_000_000 * 2 * (39 * 8 + 4 * 4)
-    assert b1 < 1_000_000 * 700 + 500_000 * 250  # about 680 B per particle slot, 217 B per node
+    # two arena buffers of 42 doubles + 4 ints per particle, plus sort keys
+    assert b2 - b1 >= 1_000_000 * 2 * (42 * 8 + 4 * 4)
+    assert b1 < 1_000_000 * 750 + 500_000 * 250  # about 730 B per particle slot, 217 B per node
 
 
 def test_batch_population_is_seeded_and_matches_the_spec():
