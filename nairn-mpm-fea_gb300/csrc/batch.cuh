@@ -723,6 +723,9 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     R.g.gx = grid->dx;
     R.g.gy = grid->dy;
     R.g.gz = grid->dz;
+    R.g.igx = 1. / grid->dx;
+    R.g.igy = 1. / grid->dy;
+    R.g.igz = b->dim == 3 ? 1. / grid->dz : 0.;
     R.g.xn = xn;
     R.g.yn = yn;
     R.g.zn = b->dim == 3 ? zn : nullptr;

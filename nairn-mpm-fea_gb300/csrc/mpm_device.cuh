@@ -20,6 +20,7 @@ struct DevGrid {
     int dim, nx, ny, nz;
     int xplane, yplane, zplane, nnodes;  // node-number strides, node count
     double xmin, ymin, zmin, gx, gy, gz;  // origin and cell size (MeshInfo)
+    double igx, igy, igz;                 // 1 / cell size
     const double *xn, *yn, *zn;           // node coordinates per axis
 };
 

@@ -281,6 +281,9 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     g.gx = grid->dx;
     g.gy = grid->dy;
     g.gz = grid->dz;
+    g.igx = 1. / grid->dx;
+    g.igy = 1. / grid->dy;
+    g.igz = grid->dim == 3 ? 1. / grid->dz : 0.;
     cudaError_t e;
     if ((e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking)) != cudaSuccess) {
         int st = cuda_fail(nullptr, e, "cudaStreamCreate");

@@ -13,6 +13,8 @@
 // the two halves, and the grid data both halves read is complete beforehand.
 #pragma once
 
+#include <type_traits>
+
 #include "mpm_device.cuh"
 
 namespace nmg {
@@ -124,8 +126,12 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
 
 // MeshInfo::FindElementFromPoint for equal element sizes (MeshInfo.cpp:593-633):
 // truncated cell index, the grid's far edge clamped; -1 when off the grid.
-__device__ __forceinline__ int find_cell(double x, double xmin, double gx, int n) {
-    int c = (int)((x - xmin) / gx);
+__device__ __forceinline__ int find_cell(double x, double xmin, double gx, double igx, int n) {
+    // (x - xmin) * (1/gx) can differ from the quotient by an ulp, which moves a
+    // point lying on a cell boundary to the neighbouring cell; the linear
+    // shape functions of both cells agree on their shared face, so the CPDI
+    // weights do not change
+    int c = (int)((x - xmin) * igx);
     if (c < 0 || c >= n) {
         if (x == xmin + n * gx) c = n - 1;
         else c = -1;
@@ -182,17 +188,19 @@ __device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i, unsig
             cp[a] = pos[a] + s1 * r1[a] + s2 * r2[a];
             if (DIM == 3) cp[a] += s3 * r3[a];
         }
-        const int cc = find_cell(cp[0], g.xmin, g.gx, g.nx);
-        const int cr = find_cell(cp[1], g.ymin, g.gy, g.ny);
-        const int cz = DIM == 3 ? find_cell(cp[2], g.zmin, g.gz, g.nz) : 0;
+        const int cc = find_cell(cp[0], g.xmin, g.gx, g.igx, g.nx);
+        const int cr = find_cell(cp[1], g.ymin, g.gy, g.igy, g.ny);
+        const int cz = DIM == 3 ? find_cell(cp[2], g.zmin, g.gz, g.igz, g.nz) : 0;
         if (cc < 0 || cr < 0 || cz < 0) {
             atomicOr(err, ERR_LEFT_GRID);
             return false;
         }
         p.ce[c * n + i] = DIM == 3 ? g.nx * (cz * g.ny + cr) + cc : cr * g.nx + cc;
-        p.cxi[(3 * c + 0) * n + i] = (2. * cp[0] - g.xn[cc] - g.xn[cc + 1]) / (g.xn[cc + 1] - g.xn[cc]);
-        p.cxi[(3 * c + 1) * n + i] = (2. * cp[1] - g.yn[cr] - g.yn[cr + 1]) / (g.yn[cr + 1] - g.yn[cr]);
-        if (DIM == 3) p.cxi[(3 * c + 2) * n + i] = (2. * cp[2] - g.zn[cz] - g.zn[cz + 1]) / (g.zn[cz + 1] - g.zn[cz]);
+        // GetXiPos (2x - xmin - xmax) / dx with the equal cell size of a
+        // regular grid (the element extents differ from it by rounding only)
+        p.cxi[(3 * c + 0) * n + i] = (2. * cp[0] - g.xn[cc] - g.xn[cc + 1]) * g.igx;
+        p.cxi[(3 * c + 1) * n + i] = (2. * cp[1] - g.yn[cr] - g.yn[cr + 1]) * g.igy;
+        if (DIM == 3) p.cxi[(3 * c + 2) * n + i] = (2. * cp[2] - g.zn[cz] - g.zn[cz + 1]) * g.igz;
         const int cell[3] = {cc, cr, cz};
 #pragma unroll
         for (int a = 0; a < DIM; a++) {
@@ -306,11 +314,99 @@ __device__ __forceinline__ void cpdi_nodes(const DevGrid &g, int nb, const DevPa
     }
 }
 
+// Mixed mode: the same pairs merged per node before anything touches memory.
+// When every corner lies in the 2x2(x2) cells from the lowest corner cell lo
+// (the usual case: a particle domain no wider than a cell), the weights of the
+// 3x3(x3) nodes from lo are sums over corners of separable products
+//   N = ws * Wx[a] Wy[b] Wz[c],  grad N = wg * Wx[a] Wy[b] Wz[c]
+// with W the corner element's 1D linear weights placed at the corner's cell
+// offset, accumulated in registers; f is then called once per node with a
+// nonzero weight (at most 27 calls instead of 64 pair calls).  Wider domains
+// fall back to the pair visits.  Returns false when it fell back.
+template <int DIM, bool GRAD, class F>
+__device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevParticles &p, int i, F &&f) {
+    constexpr int NC = DIM == 3 ? 8 : 4;
+    constexpr int W = DIM == 3 ? 27 : 9;
+    const size_t n = (size_t)p.n;
+    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
+    int cell[NC][3];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        elem_coords(g, p.ce[c * n + i], cell[c][0], cell[c][1], cell[c][2]);
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            lo[a] = min(lo[a], cell[c][a]);
+            hi[a] = max(hi[a], cell[c][a]);
+        }
+    }
+    bool fits = true;
+#pragma unroll
+    for (int a = 0; a < DIM; a++) fits = fits && hi[a] - lo[a] <= 1;
+    if (!fits) {
+        cpdi_nodes<DIM, GRAD, float>(g, nb, p, i, f);
+        return;
+    }
+    const float ws = DIM == 3 ? 0.125f : 0.25f;
+    float N[W], GX[W], GY[W], GZ[W];
+#pragma unroll
+    for (int w = 0; w < W; w++) N[w] = GX[w] = GY[w] = GZ[w] = 0.f;
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        float wt[3][3];
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            const float xi = (float)p.cxi[(3 * c + a) * n + i];
+            const int o = cell[c][a] - lo[a];
+            const float w0 = 0.5f * (1.f - xi), w1 = 0.5f * (1.f + xi);
+            wt[a][0] = o == 0 ? w0 : 0.f;
+            wt[a][1] = o == 0 ? w1 : w0;
+            wt[a][2] = o == 0 ? 0.f : w1;
+        }
+        float gxc = 0.f, gyc = 0.f, gzc = 0.f;
+        if (GRAD) {
+            gxc = (float)p.cwg[(3 * c) * n + i];
+            gyc = (float)p.cwg[(3 * c + 1) * n + i];
+            if (DIM == 3) gzc = (float)p.cwg[(3 * c + 2) * n + i];
+        }
+        // the corner element's linear shape function is the product of the
+        // factors 0.5 (1 +- xi): 0.25 (1+-xi)(1+-eta) in 2D, 0.125 (...) in 3D
+#pragma unroll
+        for (int cz = 0; cz < (DIM == 3 ? 3 : 1); cz++)
+#pragma unroll
+            for (int cy = 0; cy < 3; cy++)
+#pragma unroll
+                for (int cx = 0; cx < 3; cx++) {
+                    const int w = (cz * 3 + cy) * 3 + cx;
+                    float sfn = wt[0][cx] * wt[1][cy];
+                    if (DIM == 3) sfn *= wt[2][cz];
+                    if (sfn < 1e-15f) continue;
+                    N[w] += ws * sfn;
+                    if (GRAD) {
+                        GX[w] += gxc * sfn;
+                        GY[w] += gyc * sfn;
+                        if (DIM == 3) GZ[w] += gzc * sfn;
+                    }
+                }
+    }
+    const int base = nb + (DIM == 3 ? lo[2] * g.zplane : 0) + lo[1] * g.yplane + lo[0];
+#pragma unroll
+    for (int cz = 0; cz < (DIM == 3 ? 3 : 1); cz++)
+#pragma unroll
+        for (int cy = 0; cy < 3; cy++)
+#pragma unroll
+            for (int cx = 0; cx < 3; cx++) {
+                const int w = (cz * 3 + cy) * 3 + cx;
+                if (N[w] == 0.f) continue;
+                f(base + cx + cy * g.yplane + cz * g.zplane, N[w], GX[w], GY[w], GZ[w]);
+            }
+}
+
 // the nodes of particle i for this step, whatever the shape-function option
 template <int DIM, int SHAPE, bool GRAD, typename T, class F>
 __device__ __forceinline__ void visit_nodes(const DevGrid &g, int nb, const DevParticles &p, int i, F &&f) {
     if constexpr (SHAPE == SHAPE_LCPDI) {
-        cpdi_nodes<DIM, GRAD, T>(g, nb, p, i, f);
+        if constexpr (std::is_same<T, float>::value) cpdi_window<DIM, GRAD>(g, nb, p, i, f);
+        else cpdi_nodes<DIM, GRAD, T>(g, nb, p, i, f);
     } else {
         for_each_node<DIM, SHAPE, GRAD, T>(g, nb, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
                                            p.lpy[i], DIM == 3 ? p.lpz[i] : 1., f);
@@ -445,8 +541,8 @@ __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevN
     if constexpr (SHAPE == SHAPE_LCPDI) {
         // ElementBase::GetShapeFunctionData: the particle's CPDI corners for this step
         if (!cpdi_setup<DIM>(g, p, i, rv.err)) return;
-        if (mm) cpdi_nodes<DIM, true, T>(g, rv.nb, p, i, scatter);
-        else cpdi_nodes<DIM, false, T>(g, rv.nb, p, i, scatter);
+        if (mm) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
+        else visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, scatter);
     } else {
         if (mm)
             for_each_node<DIM, SHAPE, true, T>(g, rv.nb, e, xi, eta, zeta, p.lpx[i], p.lpy[i],
@@ -654,7 +750,7 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
     const int off = field_offset(sp, mats, p, i);
     // the particle's nodes for this step (CPDI corners or the element window)
     auto visit = [&](auto &&fn) {
-        if constexpr (SHAPE == SHAPE_LCPDI) cpdi_nodes<DIM, false, T>(g, rv.nb, p, i, fn);
+        if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
         else for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, fn);
     };
     visit([&](int n, T N, T, T, T) {
@@ -715,7 +811,7 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
             if (sp.ct.nf > 1) add_contact_terms<DIM>(nd, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz);
         };
         if (sp.ct.nf > 1) {
-            if constexpr (SHAPE == SHAPE_LCPDI) cpdi_nodes<DIM, true, T>(g, rv.nb, p, i, scatter);
+            if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
             else for_each_node<DIM, SHAPE, true, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, scatter);
         } else {
             visit(scatter);
