@@ -62,6 +62,8 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=40,
                     help="requests of the served measurement, a prefix of the seeded 200-request stream (0: skip)")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM admission budget of the server")
+    ap.add_argument("--config3-steps", type=int, default=10,
+                    help="timed steps of the 3D contact (config 3) measurement (0: skip)")
     return ap.parse_args()
 
 
@@ -469,6 +471,44 @@ def served_measurement(args, dist):
                                "policy": "admit while fewer than 3 M particles are resident, least work first"}}
 
 
+def config3_measurement(args, dist, local):
+    """The 3D two-material contact form: a Neo-Hookean block (G 10 MPa, K 50 MPa,
+    rho 1.1) pressed and sliding (4 m/s down, 4 m/s along) on an elastic plate
+    (70 GPa, 0.33, 2.7) whose base is held, Coulomb friction 0.3, lCPDI, 0.5 mm
+    cells, 2x2x2 particles per cell (4,136,960 particles), USAVG; plain FP64
+    and mixed precision on the same steps, with the mixed state's error."""
+    from nairn_gb300 import gpu, model
+    m = model.contact_3d(plate=(128, 128, 30), block=(40, 40, 16), block_x0=22.0, block_y0=22.0, cell=0.5,
+                         v=(4000., 0., -4000.), steps=1500, gimp="lCPDI", friction=0.3, normals=2)
+    k = args.config3_steps
+    out, finals = {}, {}
+    for prec in (0, 1):
+        r = gpu.GpuRun(m, precision=prec, sort_interval=args.sort_interval)
+        r.upload(m.particles)
+        r.step(3)
+        l0 = r.launch_count()
+        clocks = ClockSampler(local)
+        clocks.start()
+        dist.barrier()
+        ms = r.step_timed(k)
+        dist.barrier()
+        clk = clocks.stop()
+        out[prec] = {"value": dist.sum(float(m.n)) * k / (dist.max(ms) / 1e3), "ms_per_step": ms / k,
+                     "gpu_launches": r.launch_count() - l0, "clocks": clk}
+        finals[prec] = r.download(m.particles)
+        r.close()
+    err = state_error(finals[1], finals[0], 3)
+    return {"value": out[1]["value"], "unit": METRIC, "ms_per_step": out[1]["ms_per_step"], "dtype": "mixed",
+            "steps": k, "gpu_launches": out[1]["gpu_launches"], "clocks": out[1]["clocks"],
+            "config": {"workload": "3D multimaterial contact: Neo-Hookean block pressed and sliding on an elastic "
+                                   "plate, Coulomb friction 0.3, lCPDI, 0.5 mm cells, 2x2x2 particles/cell, USAVG",
+                       "particles": m.n, "grid_nodes": m.grid.nnodes, "material_fields": 2,
+                       "l2": "particle state %.2f GB vs 129 MB L2: no flush needed" % (m.n * 42 * 8 / 1e9)},
+            "plain_fp64": {"value": out[0]["value"], "ms_per_step": out[0]["ms_per_step"]},
+            "speedup_vs_plain_fp64": out[1]["value"] / out[0]["value"],
+            "error_vs_fp64_path": dict(err, steps=3 + k, target="<= 1e-5 relative L2")}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
@@ -552,6 +592,8 @@ def main():
                     "d2h_bytes_per_step": d2h * ws, "steps": ke,
                     "note": "per step: upload full particle state from pinned host memory, one step, download"},
             "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk}
+    if args.config3_steps > 0:
+        line["contact3d"] = config3_measurement(args, dist, local)
     if args.batch_runs > 0:
         line["batched"] = batched_measurement(args, dist, local)
     if args.serve_requests > 0:
