@@ -17,7 +17,11 @@ G2P, second extrapolation and strain update, element reset).
 The line also carries "batched": 512 independent seeded 2D runs (2k-200k
 particles each) advanced by one graph-captured batched step in mixed
 precision, against the same runs on the plain single-run FP64 path, with the
-error of the batched results against that path.
+error of the batched results against that path; "contact3d": the 3D
+two-material contact problem (4.1 M particles, lCPDI) in FP64 and mixed
+precision; "contact3d_batched": 48 seeded contact runs of 20k-500k particles
+in one batched mixed step against each run alone on the plain FP64 path; and
+"served": a seeded request stream through the continuous-batching server.
 
 Under torchrun (N>1) every rank runs an independent replica of the workload
 (the runs do not exchange data), so scaling is weak.
@@ -62,6 +66,9 @@ def parse():
     ap.add_argument("--serve-requests", type=int, default=40,
                     help="requests of the served measurement, a prefix of the seeded 200-request stream (0: skip)")
     ap.add_argument("--serve-budget-gb", type=float, default=150.0, help="HBM admission budget of the server")
+    ap.add_argument("--contact-runs", type=int, default=48,
+                    help="runs of the batched 3D contact instance mix (0: skip)")
+    ap.add_argument("--contact-steps", type=int, default=40, help="timed steps of the batched contact measurement")
     ap.add_argument("--config3-steps", type=int, default=10,
                     help="timed steps of the 3D contact (config 3) measurement (0: skip)")
     return ap.parse_args()
@@ -509,6 +516,62 @@ def config3_measurement(args, dist, local):
             "error_vs_fp64_path": dict(err, steps=3 + k, target="<= 1e-5 relative L2")}
 
 
+def contact_batched_measurement(args, dist, local):
+    """The batched form on the 3D contact instance mix: `contact_runs` seeded
+    two-material contact runs of the contact_3d form (Neo-Hookean block pressed
+    and sliding on an elastic plate, Coulomb friction 0.3, lCPDI, 0.5 mm cells,
+    8 particles per cell), 20k-500k particles each (log-uniform), resident
+    together and advanced by one graph-captured batched step in mixed
+    precision, autotuned.  Beside it: every run alone on the plain single-run
+    FP64 path (the same steps) and each batched result's error against it."""
+    from nairn_gb300 import gpu, model
+    ms = model.contact_models(args.contact_runs, seed=303, steps=1500)
+    n = sum(m.n for m in ms)
+    b = gpu.GpuBatch.for_models(ms, precision=1)
+    ids = [b.add(m) for m in ms]
+    b.step(max(3, args.warmup))
+    blk, si, _ = b.autotune(4)
+    k = args.contact_steps
+    l0 = b.info()["launches"]
+    clocks = ClockSampler(local)
+    clocks.start()
+    dist.barrier()
+    ms_b = b.step_timed(k)
+    dist.barrier()
+    clk = clocks.stop()
+    info = b.info()
+    done = b.state(ids[0])[1]
+    value = dist.sum(float(n)) * k / (dist.max(ms_b) / 1e3)
+    plain_ms, plain_ps, errs = 0.0, 0, []
+    for j, m in enumerate(ms):
+        r = gpu.GpuRun(m)
+        r.upload(m.particles)
+        r.step(done - k)
+        plain_ms += r.step_timed(k)
+        plain_ps += m.n * k
+        alone = r.download(m.particles)
+        r.close()
+        errs.append(state_error(b.download(ids[j]), alone, 3))
+    b.close()
+    plain_value = plain_ps / (plain_ms / 1e3)
+    emax = {q: max(e[q] for e in errs) for q in ("pos", "vel", "stress")}
+    return {"value": value, "unit": METRIC, "ms_per_step": ms_b / k, "steps": k, "dtype": "mixed",
+            "config": {"workload": "%d independent 3D two-material contact runs (Neo-Hookean block on elastic "
+                                   "plate, Coulomb 0.3, lCPDI, 0.5 mm cells, 8 particles/cell, USAVG), "
+                                   "20k-500k particles each (log-uniform, seed 303); one graph-captured "
+                                   "batched step" % len(ms),
+                       "particles": n, "grid_nodes": info["nodes_used"], "runs": len(ms), "material_fields": 2,
+                       "autotuned": {"block": blk, "sort_interval": si},
+                       "timed_window": "steps %d-%d of each run" % (done - k + 1, done),
+                       "l2": "batch state %.1f GB vs 129 MB L2: no flush needed" % (n * 42 * 8 / 1e9)},
+            "gpu_launches": info["launches"] - l0, "clocks": clk,
+            "plain_fp64_same_runs": {"value": plain_value, "unit": METRIC, "runs": len(ms),
+                                     "sample": "every run alone on the single-run FP64 path, same %d steps" % k},
+            "speedup_vs_plain_fp64": value / plain_value,
+            "error_vs_plain_fp64": dict(emax, statistic="max over the %d runs" % len(ms),
+                                        target="<= 1e-5 relative L2")}
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
@@ -594,6 +657,8 @@ def main():
             "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk}
     if args.config3_steps > 0:
         line["contact3d"] = config3_measurement(args, dist, local)
+    if args.contact_runs > 0:
+        line["contact3d_batched"] = contact_batched_measurement(args, dist, local)
     if args.batch_runs > 0:
         line["batched"] = batched_measurement(args, dist, local)
     if args.serve_requests > 0:

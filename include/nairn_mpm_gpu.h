@@ -263,7 +263,7 @@ typedef struct MpmGpuBatch MpmGpuBatch;
 typedef struct {
     int32_t np;               /* MPMGPU_PLANE_STRAIN or MPMGPU_THREED        */
     int32_t method;           /* MPMGPU_USF / _USAVG / _USL                  */
-    int32_t shape;            /* MPMGPU_SHAPE_LINEAR or _UGIMP               */
+    int32_t shape;            /* MPMGPU_SHAPE_LINEAR, _UGIMP or _LCPDI       */
     int32_t precision;        /* MPMGPU_PREC_*                               */
     int32_t sort_interval;    /* cell sort every k steps (0: never)          */
     int32_t block;            /* threads per block of particle kernels (0: 256) */
@@ -273,7 +273,8 @@ typedef struct {
     int64_t max_nodes;        /* grid nodes (sum over resident runs)         */
     double fraction_usf;      /* USAVG split (0 -> 0.5)                      */
     int32_t inc_defgrad_terms;/* Exponential() terms of hyperelastic F (0: 2 in 2D, 1 in 3D) */
-    int32_t pad;
+    int32_t max_fields;       /* material velocity fields per run (0, 1: single
+                                 material mode; up to 8 for multimaterial contact) */
 } MpmGpuBatchOptions;
 
 /* run states returned by mpmgpu_batch_run_state; a failed run reports the
@@ -293,12 +294,14 @@ typedef struct {
 /* Device bytes mpmgpu_batch_create allocates for these capacities. */
 int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *opts);
 int mpmgpu_batch_create(const MpmGpuBatchOptions *opts, MpmGpuBatch **out);
-/* Admit one run; *run_id receives its slot.  MPMGPU_ERR_BUSY: not enough free
+/* Admit one run; *run_id receives its slot.  contact (may be NULL) enables
+ * multimaterial contact for the run; its materials' field numbers must be
+ * below the batch's max_fields.  MPMGPU_ERR_BUSY: not enough free
  * run slots, particles, nodes or material slots now (retry after removals);
  * MPMGPU_ERR_OOM: the run is larger than the batch's capacities. */
 int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
-                         const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuParticles *p, double timestep,
-                         int32_t nsteps, int32_t *run_id);
+                         const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuContact *contact,
+                         const MpmGpuParticles *p, double timestep, int32_t nsteps, int32_t *run_id);
 /* Advance every running run by nsteps steps (a run stops at its own count). */
 int mpmgpu_batch_step(MpmGpuBatch *b, int32_t nsteps);
 int mpmgpu_batch_step_timed(MpmGpuBatch *b, int32_t nsteps, double *ms);
@@ -331,7 +334,7 @@ typedef struct MpmGpuServer MpmGpuServer;
 
 typedef struct {
     int32_t method;             /* MPMGPU_USF / _USAVG / _USL                  */
-    int32_t shape;              /* MPMGPU_SHAPE_LINEAR or _UGIMP               */
+    int32_t shape;              /* MPMGPU_SHAPE_LINEAR, _UGIMP or _LCPDI       */
     int32_t precision;          /* MPMGPU_PREC_*                               */
     int32_t max_runs;           /* run slots per dimension                     */
     int32_t steps_per_round;    /* steps between admissions/retirements (0: 10) */
@@ -347,7 +350,7 @@ typedef struct {
                                    is always admitted when nothing runs      */
     int32_t order;              /* admission order: 0 arrival (FIFO), 1 least
                                    work first (particles x steps)            */
-    int32_t pad;
+    int32_t max_fields;         /* material velocity fields per run (0: 1)     */
 } MpmGpuServerOptions;
 
 enum { MPMGPU_REQ_QUEUED = 1, MPMGPU_REQ_RUNNING = 2, MPMGPU_REQ_DONE = 3, MPMGPU_REQ_FAILED = 4 };
@@ -375,8 +378,8 @@ int mpmgpu_server_create(const MpmGpuServerOptions *opts, MpmGpuServer **out);
  * admission and receive the final state (upload order) at completion.  Grid
  * coordinates, materials and velocity conditions are copied. */
 int mpmgpu_server_submit(MpmGpuServer *s, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
-                         const MpmGpuVelBC *bcs, int32_t nbc, MpmGpuParticles *p, double timestep,
-                         int32_t nsteps, int64_t *request_id);
+                         const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuContact *contact, MpmGpuParticles *p,
+                         double timestep, int32_t nsteps, int64_t *request_id);
 int mpmgpu_server_poll(MpmGpuServer *s, int64_t request_id, MpmGpuRequestInfo *info);
 /* Block until the request is done or failed; MPMGPU_ERR_TIMEOUT after timeout_s. */
 int mpmgpu_server_wait(MpmGpuServer *s, int64_t request_id, double timeout_s);

@@ -131,16 +131,25 @@ __global__ void k_gather_cap(const T *__restrict__ src, T *__restrict__ dst, con
 }
 
 // step-start clear of the accumulated node columns of the used node range
+// (every material field, and the contact terms when there are several)
 template <bool MIX>
-__global__ void k_clear_nodes(DevNodes nd, int nn) {
+__global__ void k_clear_nodes(DevNodes nd, int nn, int nf, int fstride) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nn) return;
-    nd.mass[n] = 0.;
-    nd.px[n] = nd.py[n] = nd.pz[n] = 0.;
-    nd.fx[n] = nd.fy[n] = nd.fz[n] = 0.;
-    nd.ux[n] = nd.uy[n] = nd.uz[n] = 0.;
-    nd.active[n] = 0;
-    if (MIX) nd.gx[n] = nd.gy[n] = nd.gz[n] = 0.f;
+    for (int f = 0; f < nf; f++) {
+        const int k = f * fstride + n;
+        nd.mass[k] = 0.;
+        nd.px[k] = nd.py[k] = nd.pz[k] = 0.;
+        nd.fx[k] = nd.fy[k] = nd.fz[k] = 0.;
+        nd.ux[k] = nd.uy[k] = nd.uz[k] = 0.;
+        nd.active[k] = 0;
+        if (MIX) nd.gx[k] = nd.gy[k] = nd.gz[k] = 0.f;
+        if (nf > 1) {
+            nd.vol[k] = 0.;
+            nd.dsx[k] = nd.dsy[k] = nd.dsz[k] = 0.;
+            nd.gvx[k] = nd.gvy[k] = nd.gvz[k] = 0.;
+        }
+    }
 }
 
 constexpr int kBatchIntCols = 4;  // mat, elem, orig, run
@@ -156,7 +165,9 @@ struct MpmGpuBatch {
     MpmGpuBatchOptions o{};
     int dim = 2;
     int pcap = 0, ncap = 0;
+    int nf = 1;    // material velocity fields per node (node columns are nf * ncap long)
     int tb = 256;  // threads per block of the particle kernels
+    void *cpdi = nullptr;  // lCPDI corner scratch for pcap slots
     // particle arena, two buffers: kParticleDoubles+1 double columns and
     // kBatchIntCols int columns of capacity pcap each; buffer `par` is current
     double *pbuf[2] = {nullptr, nullptr};
@@ -225,6 +236,13 @@ void batch_link(MpmGpuBatch *b) {
     b->orig = ib + 2 * cap;
     p.run = ib + 3 * cap;
     p.n = b->n_used;
+    if (b->cpdi) {
+        // corner scratch, rebuilt at every step start with stride n_used
+        const size_t nc = b->dim == 3 ? 8 : 4;
+        p.cxi = (double *)b->cpdi;
+        p.cwg = p.cxi + 3 * nc * cap;
+        p.ce = (int *)(p.cwg + 3 * nc * cap);
+    }
 }
 
 void batch_drop_graphs(MpmGpuBatch *b) {
@@ -239,7 +257,7 @@ void batch_free(MpmGpuBatch *b) {
     batch_drop_graphs(b);
     void *ptrs[] = {b->pbuf[0], b->pbuf[1], b->ibuf[0], b->ibuf[1], b->nblock, b->fblock, b->coords, b->nrun,
                     b->bc_group, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->sums, b->mats,
-                    b->runs_dev, b->bc_block, b->flag};
+                    b->runs_dev, b->bc_block, b->flag, b->cpdi};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -353,15 +371,17 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     StepParams sp{};
     sp.runs = b->runs_dev;
     sp.nrun = b->nrun;
-    sp.ct.nf = 1;
-    k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN);
+    sp.ct.nf = b->nf;
+    sp.ct.fstride = b->ncap;
+    k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN, b->nf, b->ncap);
     k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     k_node_post<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, method != MPMGPU_USL);
     if (method == MPMGPU_USL)
         k_strain_forces<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     else
         k_strain_forces<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
-    k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, 0);
+    k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group,
+                                                    b->nf > 1 && method != MPMGPU_USF);
     if (method == MPMGPU_USF) {
         k_g2p<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     } else {
@@ -372,16 +392,17 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     k_advance_runs<<<(b->o.max_runs + 127) / 128, 128, 0, s>>>(b->runs_dev, b->o.max_runs);
 }
 
+template <int DIM, bool MIX>
+void batch_enqueue_shape(MpmGpuBatch *b) {
+    if (b->o.shape == MPMGPU_SHAPE_LINEAR) batch_enqueue_step<DIM, SHAPE_LINEAR, MIX>(b);
+    else if (b->o.shape == MPMGPU_SHAPE_LCPDI) batch_enqueue_step<DIM, SHAPE_LCPDI, MIX>(b);
+    else batch_enqueue_step<DIM, SHAPE_UGIMP, MIX>(b);
+}
+
 void batch_enqueue_any(MpmGpuBatch *b) {
     const bool mix = b->o.precision == MPMGPU_PREC_MIXED;
-    const bool lin = b->o.shape == MPMGPU_SHAPE_LINEAR;
-    if (b->dim == 3) {
-        if (mix) lin ? batch_enqueue_step<3, SHAPE_LINEAR, true>(b) : batch_enqueue_step<3, SHAPE_UGIMP, true>(b);
-        else lin ? batch_enqueue_step<3, SHAPE_LINEAR, false>(b) : batch_enqueue_step<3, SHAPE_UGIMP, false>(b);
-    } else {
-        if (mix) lin ? batch_enqueue_step<2, SHAPE_LINEAR, true>(b) : batch_enqueue_step<2, SHAPE_UGIMP, true>(b);
-        else lin ? batch_enqueue_step<2, SHAPE_LINEAR, false>(b) : batch_enqueue_step<2, SHAPE_UGIMP, false>(b);
-    }
+    if (b->dim == 3) mix ? batch_enqueue_shape<3, true>(b) : batch_enqueue_shape<3, false>(b);
+    else mix ? batch_enqueue_shape<2, true>(b) : batch_enqueue_shape<2, false>(b);
 }
 
 int batch_step_launches(const MpmGpuBatch *b) { return b->o.method == MPMGPU_USF ? 7 : 9; }
@@ -541,9 +562,13 @@ int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *o) {
     if (!o || o->max_particles <= 0 || o->max_nodes <= 0) return -1;
     const int64_t P = o->max_particles, N = o->max_nodes;
     const int64_t ntiles = (P + kTile - 1) / kTile;
+    const int64_t nf = o->max_fields > 1 ? o->max_fields : 1;
+    const int64_t nc = o->np == MPMGPU_THREED ? 8 : 4;
     int64_t bytes = 2 * P * (int64_t)((kParticleDoubles + 1) * sizeof(double) + kBatchIntCols * sizeof(int));
     bytes += 4 * P * (int64_t)sizeof(int) + 2 * 256 * ntiles * (int64_t)sizeof(int);  // sort keys, histograms
-    bytes += N * (int64_t)(19 * sizeof(double) + 12 * sizeof(float) + 1 + 2 * sizeof(int) + sizeof(double));
+    if (o->shape == MPMGPU_SHAPE_LCPDI) bytes += P * nc * (int64_t)(sizeof(int) + 6 * sizeof(double));
+    bytes += N * nf * (int64_t)((nf > 1 ? 26 : 19) * sizeof(double) + 12 * sizeof(float) + 1);
+    bytes += N * (int64_t)(2 * sizeof(int) + sizeof(double));
     bytes += (int64_t)o->max_materials * (int64_t)sizeof(DevMat) + (int64_t)o->max_runs * (int64_t)sizeof(DevRun);
     return bytes;
 }
@@ -553,12 +578,14 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     *out = nullptr;
     if (o->np != MPMGPU_PLANE_STRAIN && o->np != MPMGPU_THREED)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "batch analysis type must be 2D plane strain or 3D");
-    if (o->shape != MPMGPU_SHAPE_LINEAR && o->shape != MPMGPU_SHAPE_UGIMP)
+    if (o->shape != MPMGPU_SHAPE_LINEAR && o->shape != MPMGPU_SHAPE_UGIMP && o->shape != MPMGPU_SHAPE_LCPDI)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
     if (o->method != MPMGPU_USF && o->method != MPMGPU_USAVG && o->method != MPMGPU_USL)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
     if (o->precision != MPMGPU_PREC_FP64 && o->precision != MPMGPU_PREC_MIXED)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "precision must be MPMGPU_PREC_FP64 or MPMGPU_PREC_MIXED");
+    if (o->max_fields < 0 || o->max_fields > kMaxFields)
+        return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "max_fields must be 0 to 8");
     if (o->max_particles <= 0 || o->max_particles > (1LL << 31) - 1 || o->max_nodes <= 0 ||
         o->max_nodes > (1LL << 30) || o->max_runs <= 0 || o->max_runs > (1 << 20) || o->max_materials <= 0 ||
         o->max_materials > (1 << 24))
@@ -573,7 +600,9 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     b->dim = o->np == MPMGPU_THREED ? 3 : 2;
     b->pcap = (int)o->max_particles;
     b->ncap = (int)o->max_nodes;
-    const size_t P = (size_t)b->pcap, N = (size_t)b->ncap;
+    b->nf = o->max_fields > 1 ? o->max_fields : 1;
+    const size_t P = (size_t)b->pcap, N = (size_t)b->ncap, NT = N * b->nf;
+    const int ncleared = b->nf > 1 ? 17 : 10, ncols = ncleared + 9;
     const size_t ntiles = (P + kTile - 1) / kTile;
     const size_t nsums = (256 * ntiles + kScanChunk - 1) / kScanChunk + 1;
     cudaError_t e = cudaStreamCreateWithFlags(&b->stream, cudaStreamNonBlocking);
@@ -586,8 +615,9 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
         A((void **)&b->keys[k], P * sizeof(int));
         A((void **)&b->vals[k], P * sizeof(int));
     }
-    A((void **)&b->nblock, N * 19 * sizeof(double) + N);
-    A((void **)&b->fblock, N * 12 * sizeof(float));
+    A((void **)&b->nblock, NT * ncols * sizeof(double) + NT);
+    A((void **)&b->fblock, NT * 12 * sizeof(float));
+    if (o->shape == MPMGPU_SHAPE_LCPDI) A(&b->cpdi, P * (b->dim == 3 ? 8 : 4) * (sizeof(int) + 6 * sizeof(double)));
     A((void **)&b->coords, N * sizeof(double));
     A((void **)&b->nrun, N * sizeof(int));
     A((void **)&b->bc_group, N * sizeof(int));
@@ -596,8 +626,8 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     A((void **)&b->mats, (size_t)o->max_materials * sizeof(DevMat));
     A((void **)&b->runs_dev, (size_t)o->max_runs * sizeof(DevRun));
     A((void **)&b->flag, sizeof(unsigned));
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->nblock, 0, N * 19 * sizeof(double) + N, b->stream);
-    if (e == cudaSuccess) e = cudaMemsetAsync(b->fblock, 0, N * 12 * sizeof(float), b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->nblock, 0, NT * ncols * sizeof(double) + NT, b->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(b->fblock, 0, NT * 12 * sizeof(float), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->nrun, 0xFF, N * sizeof(int), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->bc_group, 0xFF, N * sizeof(int), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->runs_dev, 0, (size_t)o->max_runs * sizeof(DevRun), b->stream);
@@ -612,14 +642,18 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     }
     double *nb = b->nblock;
     DevNodes &nd = b->nd;
-    double **dc[19] = {&nd.mass, &nd.px, &nd.py, &nd.pz, &nd.fx, &nd.fy, &nd.fz, &nd.ux, &nd.uy, &nd.uz,
-                       &nd.cx, &nd.cy, &nd.cz, &nd.vx, &nd.vy, &nd.vz, &nd.ax, &nd.ay, &nd.az};
-    for (int k = 0; k < 19; k++) *dc[k] = nb + (size_t)k * N;
-    nd.active = (unsigned char *)(nb + 19 * N);
+    // field f of node n at f * ncap + n in every column
+    double **dc[26] = {&nd.mass, &nd.px, &nd.py, &nd.pz, &nd.fx, &nd.fy, &nd.fz, &nd.ux, &nd.uy, &nd.uz,
+                       &nd.cx, &nd.cy, &nd.cz, &nd.vx, &nd.vy, &nd.vz, &nd.ax, &nd.ay, &nd.az,
+                       &nd.vol, &nd.dsx, &nd.dsy, &nd.dsz, &nd.gvx, &nd.gvy, &nd.gvz};
+    for (int k = 0; k < 19; k++) *dc[k] = nb + (size_t)k * NT;
+    if (b->nf > 1)
+        for (int k = 19; k < 26; k++) *dc[k] = nb + (size_t)k * NT;
+    nd.active = (unsigned char *)(nb + (size_t)ncols * NT);
     float *fb = b->fblock;
     float **fc[12] = {&nd.gx, &nd.gy, &nd.gz, &nd.vhx, &nd.vhy, &nd.vhz,
                       &nd.vlx, &nd.vly, &nd.vlz, &nd.bx, &nd.by, &nd.bz};
-    for (int k = 0; k < 12; k++) *fc[k] = fb + (size_t)k * N;
+    for (int k = 0; k < 12; k++) *fc[k] = fb + (size_t)k * NT;
     batch_link(b);
     b->nodes.init(b->ncap);
     b->cells.init(b->ncap);  // every run has fewer cells than nodes
@@ -632,8 +666,8 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
 }
 
 int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
-                         const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuParticles *h, double timestep,
-                         int32_t nsteps, int32_t *run_id) {
+                         const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuContact *contact,
+                         const MpmGpuParticles *h, double timestep, int32_t nsteps, int32_t *run_id) {
     if (!b || !grid || !mats || nmat <= 0 || !h || h->n <= 0 || (nbc > 0 && !bcs) || nbc < 0 || !run_id ||
         nsteps <= 0 || !(timestep > 0.))
         return berr(b, MPMGPU_ERR_INVALID, "mpmgpu_batch_add_run: bad argument");
@@ -658,10 +692,24 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
         if (bcs[k].dir == 4 && b->dim == 2) return berr(b, MPMGPU_ERR_INVALID, "z velocity BC in 2D");
     }
     std::vector<DevMat> dm((size_t)nmat);
+    int maxfield = 0;
     for (int i = 0; i < nmat; i++) {
         std::string why;
         const int st = derive_material(mats[i], b->o.np, dm[i], why, b->o.inc_defgrad_terms);
         if (st != MPMGPU_OK) return berr(b, st, "material " + std::to_string(i) + ": " + why);
+        if (mats[i].field < 0 || mats[i].field >= b->nf)
+            return berr(b, MPMGPU_ERR_INVALID, "material " + std::to_string(i) + ": field outside 0 .. max_fields-1");
+        maxfield = std::max(maxfield, mats[i].field);
+    }
+    const bool mm = contact && contact->enabled;
+    if (maxfield > 0 && !mm)
+        return berr(b, MPMGPU_ERR_INVALID, "a run with several material fields needs multimaterial contact");
+    if (mm) {
+        if (b->nf < 2) return berr(b, MPMGPU_ERR_INVALID, "contact needs a batch with max_fields >= 2");
+        if (contact->normals < 0 || contact->normals > 2)
+            return berr(b, MPMGPU_ERR_UNSUPPORTED, "contact normals: methods 0, 1 and 2 are implemented");
+        if (contact->contact_cutoff > 0.)
+            return berr(b, MPMGPU_ERR_UNSUPPORTED, "position-based contact is not implemented on the device");
     }
     int r = -1;
     for (int k = 0; k < (int)b->runs.size() && r < 0; k++)
@@ -738,6 +786,10 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     R.st_last = b->o.method == MPMGPU_USAVG ? timestep - R.st_first : timestep;
     R.t = 0.;
     R.err = 0;
+    R.mm = mm ? 1 : 0;
+    R.normals = mm ? contact->normals : 2;
+    R.friction = mm ? contact->friction : 0.;
+    R.style = !mm ? 2 : (contact->friction < 0. ? 0 : (contact->friction == 0. ? 1 : 2));
     BCK(cudaMemcpyAsync(b->runs_dev + r, &R, sizeof(DevRun), cudaMemcpyHostToDevice, s));
     unsigned bad = 0;
     BCK(cudaMemcpyAsync(&bad, b->flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));

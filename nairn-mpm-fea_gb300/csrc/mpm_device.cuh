@@ -97,6 +97,9 @@ struct DevRun {
     int steps_left;    // steps still to take (the run deactivates at zero)
     double dt, st_first, st_last, t;
     unsigned err;      // error bits of this run
+    int mm;            // multimaterial contact on for this run
+    int normals, style;
+    double friction;   // the run's contact law (DevContact fields)
 };
 
 // Per-launch step parameters.  A single-run context uses g, dt, st_first,

@@ -423,6 +423,7 @@ struct RunView {
     int nb;
     double dt, st_first, st_last;
     unsigned *err;
+    bool mm;           // multimaterial contact (contact terms are extrapolated)
 };
 
 template <bool BATCH>
@@ -434,6 +435,7 @@ __device__ __forceinline__ bool particle_run(const StepParams &sp, const DevPart
         rv.st_first = sp.st_first;
         rv.st_last = sp.st_last;
         rv.err = sp.err;
+        rv.mm = sp.ct.nf > 1;
         return true;
     }
     const int r = p.run[i];
@@ -446,6 +448,7 @@ __device__ __forceinline__ bool particle_run(const StepParams &sp, const DevPart
     rv.st_first = R.st_first;
     rv.st_last = R.st_last;
     rv.err = &R.err;
+    rv.mm = R.mm != 0;
     return true;
 }
 
@@ -519,7 +522,7 @@ __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevN
     const double mp = p.mass[i];
     const double vx = p.vx[i], vy = p.vy[i], vz = DIM == 3 ? p.vz[i] : 0.;
     const int off = field_offset(sp, mats, p, i);
-    const bool mm = sp.ct.nf > 1;
+    const bool mm = rv.mm;
     double Vp = 0., d[3] = {0., 0., 0.};
     if (mm) {
         Vp = contact_volume<DIM>(p, i, mats[p.mat[i]].rho);
@@ -795,7 +798,7 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
         // contact terms at the moved positions in multimaterial mode
         const double mp = p.mass[i];
         double Vp = 0., d[3] = {0., 0., 0.};
-        if (sp.ct.nf > 1) {
+        if (rv.mm) {
             Vp = contact_volume<DIM>(p, i, mats[p.mat[i]].rho);
             d[0] = xp[0] - p.x0[i];
             d[1] = xp[1] - p.y0[i];
@@ -808,9 +811,9 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
             atomicAdd(&nd.ux[n], v[0] * fnmp);
             atomicAdd(&nd.uy[n], v[1] * fnmp);
             if (DIM == 3) atomicAdd(&nd.uz[n], v[2] * fnmp);
-            if (sp.ct.nf > 1) add_contact_terms<DIM>(nd, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz);
+            if (rv.mm) add_contact_terms<DIM>(nd, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz);
         };
-        if (sp.ct.nf > 1) {
+        if (rv.mm) {
             if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
             else for_each_node<DIM, SHAPE, true, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, scatter);
         } else {
@@ -922,6 +925,21 @@ __device__ __forceinline__ bool node_run(const StepParams &sp, int n, double &t,
     t = R.t;
     dt = R.dt;
     return true;
+}
+
+// the contact settings that apply at node n (a batch run carries its own law);
+// nf == 1 means no contact at this node
+template <bool BATCH>
+__device__ __forceinline__ DevContact node_contact_params(const StepParams &sp, int n) {
+    DevContact ct = sp.ct;
+    if (BATCH && ct.nf > 1) {
+        const DevRun &R = sp.runs[sp.nrun[n]];
+        if (!R.mm) ct.nf = 1;
+        ct.normals = R.normals;
+        ct.style = R.style;
+        ct.friction = R.friction;
+    }
+    return ct;
 }
 
 // ---------------------------------------------------------------------------
@@ -1144,7 +1162,10 @@ __global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBCs b, co
         nd.cy[k] = nd.py[k];
         if (DIM == 3) nd.cz[k] = nd.pz[k];
     }
-    if (sp.ct.nf > 1) node_contact(sp.ct, nd, n, BC_MASS_MOMENTUM, dt);
+    {
+        const DevContact ct = node_contact_params<BATCH>(sp, n);
+        if (ct.nf > 1) node_contact(ct, nd, n, BC_MASS_MOMENTUM, dt);
+    }
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;
         if (!nd.active[k]) continue;
@@ -1175,7 +1196,8 @@ __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, 
     double t, dt;
     if (!node_run<BATCH>(sp, n, t, dt)) return;
     const int grp = bc_group[n];
-    const bool mm = sp.ct.nf > 1;
+    const DevContact ct = node_contact_params<BATCH>(sp, n);
+    const bool mm = ct.nf > 1;
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;
         if (!nd.active[k]) continue;
@@ -1208,7 +1230,7 @@ __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, 
         node_finish_update<DIM, MIX>(nd, k, m, p, fr);
     }
     if (!mm) return;
-    node_contact(sp.ct, nd, n, BC_UPDATE_MOMENTUM, dt);
+    node_contact(ct, nd, n, BC_UPDATE_MOMENTUM, dt);
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;
         if (!nd.active[k]) continue;
@@ -1234,7 +1256,8 @@ __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs b, con
     double t, dt;
     if (!node_run<BATCH>(sp, n, t, dt)) return;
     const int grp = bc_group[n];
-    const bool mm = sp.ct.nf > 1;
+    const DevContact ct = node_contact_params<BATCH>(sp, n);
+    const bool mm = ct.nf > 1;
     if (mm) {
         for (int f = 0; f < sp.ct.nf; f++) {
             const int k = f * sp.ct.fstride + n;
@@ -1243,7 +1266,7 @@ __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs b, con
             nd.py[k] = nd.uy[k];
             nd.pz[k] = nd.uz[k];
         }
-        node_contact(sp.ct, nd, n, BC_UPDATE_STRAINS_LAST, dt);
+        node_contact(ct, nd, n, BC_UPDATE_STRAINS_LAST, dt);
     }
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;

@@ -35,6 +35,7 @@ struct ServerRequest {
     std::vector<double> xn, yn, zn;
     std::vector<MpmGpuMaterial> mats;
     std::vector<MpmGpuVelBC> bcs;
+    MpmGpuContact contact{};
     MpmGpuParticles p{};  // borrowed caller arrays
     double dt = 0.;
     int nsteps = 0;
@@ -125,8 +126,9 @@ void server_admit(MpmGpuServer *s, std::vector<ServerRequest *> &admitted, std::
         }
         int32_t rid = -1;
         const int st = mpmgpu_batch_add_run(b, &q->grid, q->mats.data(), (int32_t)q->mats.size(),
-                                            q->bcs.empty() ? nullptr : q->bcs.data(), (int32_t)q->bcs.size(), &q->p,
-                                            q->dt, q->nsteps, &rid);
+                                            q->bcs.empty() ? nullptr : q->bcs.data(), (int32_t)q->bcs.size(),
+                                            q->contact.enabled ? &q->contact : nullptr, &q->p, q->dt, q->nsteps,
+                                            &rid);
         if (st == MPMGPU_OK) {
             q->run_id = rid;
             q->t_admit = ServerClock::now();
@@ -281,6 +283,7 @@ int mpmgpu_server_create(const MpmGpuServerOptions *o, MpmGpuServer **out) {
         bo.block = o->block;
         bo.max_runs = o->max_runs;
         bo.max_materials = 4 * o->max_runs;
+        bo.max_fields = o->max_fields;
         bo.fraction_usf = o->fraction_usf;
         const int64_t P = server_capacity(bo, bytes, s->o.nodes_per_particle);
         if (P < 1000) {
@@ -305,8 +308,8 @@ int mpmgpu_server_create(const MpmGpuServerOptions *o, MpmGpuServer **out) {
 }
 
 int mpmgpu_server_submit(MpmGpuServer *s, const MpmGpuGrid *grid, const MpmGpuMaterial *mats, int32_t nmat,
-                         const MpmGpuVelBC *bcs, int32_t nbc, MpmGpuParticles *p, double timestep, int32_t nsteps,
-                         int64_t *request_id) {
+                         const MpmGpuVelBC *bcs, int32_t nbc, const MpmGpuContact *contact, MpmGpuParticles *p,
+                         double timestep, int32_t nsteps, int64_t *request_id) {
     if (!s || !grid || !mats || nmat <= 0 || !p || p->n <= 0 || nbc < 0 || (nbc > 0 && !bcs) || !request_id ||
         nsteps <= 0 || !(timestep > 0.))
         return serr(s, MPMGPU_ERR_INVALID, "mpmgpu_server_submit: bad argument");
@@ -327,6 +330,7 @@ int mpmgpu_server_submit(MpmGpuServer *s, const MpmGpuGrid *grid, const MpmGpuMa
     q->grid.znodes = grid->dim == 3 ? q->zn.data() : nullptr;
     q->mats.assign(mats, mats + nmat);
     if (nbc) q->bcs.assign(bcs, bcs + nbc);
+    if (contact) q->contact = *contact;
     q->p = *p;
     q->dt = timestep;
     q->nsteps = nsteps;

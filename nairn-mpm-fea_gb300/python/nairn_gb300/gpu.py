@@ -68,7 +68,8 @@ def lib():
         "mpmgpu_batch_bytes": ([P(abi.MpmGpuBatchOptions)], C.c_int64),
         "mpmgpu_batch_create": ([P(abi.MpmGpuBatchOptions), P(VP)], C.c_int),
         "mpmgpu_batch_add_run": ([VP, P(abi.MpmGpuGrid), P(abi.MpmGpuMaterial), C.c_int32, P(abi.MpmGpuVelBC),
-                                  C.c_int32, P(abi.MpmGpuParticles), C.c_double, C.c_int32, P(C.c_int32)], C.c_int),
+                                  C.c_int32, P(abi.MpmGpuContact), P(abi.MpmGpuParticles), C.c_double, C.c_int32,
+                                  P(C.c_int32)], C.c_int),
         "mpmgpu_batch_step": ([VP, C.c_int32], C.c_int),
         "mpmgpu_batch_step_timed": ([VP, C.c_int32, P(C.c_double)], C.c_int),
         "mpmgpu_batch_run_state": ([VP, C.c_int32, P(C.c_int32), P(C.c_int32)], C.c_int),
@@ -82,7 +83,8 @@ def lib():
         "mpmgpu_batch_destroy": ([VP], None),
         "mpmgpu_server_create": ([P(abi.MpmGpuServerOptions), P(VP)], C.c_int),
         "mpmgpu_server_submit": ([VP, P(abi.MpmGpuGrid), P(abi.MpmGpuMaterial), C.c_int32, P(abi.MpmGpuVelBC),
-                                  C.c_int32, P(abi.MpmGpuParticles), C.c_double, C.c_int32, P(C.c_int64)], C.c_int),
+                                  C.c_int32, P(abi.MpmGpuContact), P(abi.MpmGpuParticles), C.c_double, C.c_int32,
+                                  P(C.c_int64)], C.c_int),
         "mpmgpu_server_poll": ([VP, C.c_int64, P(abi.MpmGpuRequestInfo)], C.c_int),
         "mpmgpu_server_wait": ([VP, C.c_int64, C.c_double], C.c_int),
         "mpmgpu_server_drain": ([VP, C.c_double], C.c_int),
@@ -200,10 +202,11 @@ class GpuBatch:
 
     def __init__(self, np_: int, method: int, shape: int, precision: int = 0, *, max_runs: int,
                  max_particles: int, max_nodes: int, max_materials: int | None = None, sort_interval: int = 1,
-                 block: int = 0, fraction_usf: float = 0.5):
+                 block: int = 0, fraction_usf: float = 0.5, inc_defgrad_terms: int = 0, max_fields: int = 1):
         L = lib()
         self.opts = abi.MpmGpuBatchOptions(np_, method, shape, precision, sort_interval, block, max_runs,
-                                           max_materials or max_runs, max_particles, max_nodes, fraction_usf)
+                                           max_materials or max_runs, max_particles, max_nodes, fraction_usf,
+                                           inc_defgrad_terms, max_fields)
         self.bytes = int(L.mpmgpu_batch_bytes(C.byref(self.opts)))
         h = C.c_void_p()
         st = L.mpmgpu_batch_create(C.byref(self.opts), C.byref(h))
@@ -220,14 +223,16 @@ class GpuBatch:
                    max_particles=int(slack * sum(m.n for m in models)),
                    max_nodes=int(slack * sum(m.grid.nnodes for m in models)),
                    max_materials=int(slack * sum(len(m.materials) for m in models)) + 1,
-                   fraction_usf=o.get("fraction_usf", 0.5), **kw)
+                   fraction_usf=o.get("fraction_usf", 0.5), inc_defgrad_terms=o.get("inc_defgrad_terms", 0),
+                   max_fields=kw.pop("max_fields", max(m.options.get("nfields", 1) for m in models)), **kw)
 
     @staticmethod
     def bytes_for(models, precision: int = 0) -> int:
         o = models[0].options
         opts = abi.MpmGpuBatchOptions(o["np"], o["method"], o["shape"], precision, 1, 0, len(models),
                                       sum(len(m.materials) for m in models) + 1, sum(m.n for m in models),
-                                      sum(m.grid.nnodes for m in models), 0.5)
+                                      sum(m.grid.nnodes for m in models), 0.5, o.get("inc_defgrad_terms", 0),
+                                      max(m.options.get("nfields", 1) for m in models))
         return int(lib().mpmgpu_batch_bytes(C.byref(opts)))
 
     def _check(self, st):
@@ -241,8 +246,9 @@ class GpuBatch:
         bcs, nbc = abi.bcs_array(model)
         ps = abi.particles_struct(particles if particles is not None else model.particles, b)
         rid = C.c_int32(-1)
+        ct = abi.contact_struct(model)
         self._check(lib().mpmgpu_batch_add_run(self.h, C.byref(g), abi.materials_array(model), len(model.materials),
-                                               bcs, nbc, C.byref(ps), float(model.options["timestep"]),
+                                               bcs, nbc, C.byref(ct), C.byref(ps), float(model.options["timestep"]),
                                                int(nsteps if nsteps is not None else model.nsteps), C.byref(rid)))
         self.models[rid.value] = model
         return rid.value
@@ -313,12 +319,12 @@ class GpuServer:
     def __init__(self, method: int, shape: int, precision: int = 1, *, hbm_budget_bytes: int,
                  max_runs: int = 256, steps_per_round: int = 10, backfill: bool = True, sort_interval: int = 1,
                  block: int = 0, frac_3d: float = 0.5, nodes_per_particle: float = 0.5, fraction_usf: float = 0.5,
-                 max_resident_particles: int = 0, order: str = "fifo"):
+                 max_resident_particles: int = 0, order: str = "fifo", max_fields: int = 1):
         L = lib()
         o = abi.MpmGpuServerOptions(method, shape, precision, max_runs, steps_per_round, 1 if backfill else 0,
                                     sort_interval, block, int(hbm_budget_bytes), frac_3d, nodes_per_particle,
                                     fraction_usf, int(max_resident_particles),
-                                    {"fifo": 0, "least_work": 1}[order], 0)
+                                    {"fifo": 0, "least_work": 1}[order], int(max_fields))
         h = C.c_void_p()
         st = L.mpmgpu_server_create(C.byref(o), C.byref(h))
         if st != 0:
@@ -337,8 +343,9 @@ class GpuServer:
         state = abi.copy_particles(particles if particles is not None else model.particles)
         ps = abi.particles_struct(state, b)
         rid = C.c_int64(-1)
+        ct = abi.contact_struct(model)
         self._check(lib().mpmgpu_server_submit(self.h, C.byref(g), abi.materials_array(model), len(model.materials),
-                                               bcs, nbc, C.byref(ps), float(model.options["timestep"]),
+                                               bcs, nbc, C.byref(ct), C.byref(ps), float(model.options["timestep"]),
                                                int(nsteps if nsteps is not None else model.nsteps), C.byref(rid)))
         self._held[rid.value] = (state, b, ps)
         return rid.value

@@ -610,3 +610,48 @@ def contact_3d(plate=(12, 12, 3), block=(4, 4, 3), block_x0=4.0, block_y0=4.0, g
                 inc_defgrad_terms=inc_terms if inc_terms > 0 else 1, nfields=2)
     return Model(g, p, [pm, bm], bcs, opts, steps, name="contact_3d",
                  extra={"contact": _contact_options(normals, friction)})
+
+
+def contact_run_params(count=64, seed=303, nmin=20000, nmax=500000, steps=100, cell=0.5, ppc_side=2,
+                       friction=0.3, normals=2, gimp="lCPDI"):
+    """Seeded population of independent 3D two-material contact runs of the
+    contact_3d form (Neo-Hookean block G 10 MPa, K 50 MPa, rho 1.1 pressed and
+    sliding on a linear elastic plate 70 GPa, 0.33, rho 2.7, Coulomb friction,
+    lCPDI, 0.5 mm cells, 8 points per cell): particle counts log-uniform in
+    [nmin, nmax]; plate aspect log-uniform in [0.7, 1.4]; plate 3-6 cells
+    thick; block a third of the plate's width and depth, 2-4 cells tall,
+    placed at a random in-plate position; pressing speed uniform 2-6 m/s,
+    sliding speed uniform 0-6 m/s in a random direction."""
+    rng = np.random.default_rng(seed)
+    per_cell = ppc_side ** 3
+    out = []
+    for k in range(count):
+        n = math.exp(rng.uniform(math.log(nmin), math.log(nmax)))
+        pz = int(rng.integers(3, 7))
+        bzc = int(rng.integers(2, 5))
+        aspect = math.exp(rng.uniform(math.log(0.7), math.log(1.4)))
+        # plate cells px*py*pz plus block cells (px/3)(py/3)bzc make n / per_cell
+        area = max(n / per_cell / (pz + bzc / 9.), 36.)
+        px = max(6, int(round(math.sqrt(area * aspect))))
+        py = max(6, int(round(area / px)))
+        bxc, byc = max(2, px // 3), max(2, py // 3)
+        bx0 = cell * int(rng.integers(0, px - bxc + 1))
+        by0 = cell * int(rng.integers(0, py - byc + 1))
+        press = 1000. * rng.uniform(2., 6.)
+        slide = 1000. * rng.uniform(0., 6.)
+        ang = rng.uniform(0., 2. * math.pi)
+        out.append(dict(plate=(px, py, pz), block=(bxc, byc, bzc), block_x0=bx0, block_y0=by0, cell=cell,
+                        ppc_side=ppc_side, v=(slide * math.cos(ang), slide * math.sin(ang), -press),
+                        friction=friction, normals=normals, steps=steps, gimp=gimp, name=f"contact{seed}_{k}"))
+    return out
+
+
+def contact_models(count=64, seed=303, **kw) -> list:
+    """The Models of contact_run_params (same arguments)."""
+    out = []
+    for p in contact_run_params(count=count, seed=seed, **kw):
+        name = p.pop("name")
+        m = contact_3d(**p)
+        m.name = name
+        out.append(m)
+    return out

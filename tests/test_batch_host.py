@@ -10,7 +10,7 @@ def test_batch_create_rejects_bad_options_without_gpu_work(gpu_lib):
     from nairn_gb300 import abi, model
     base = dict(np=model.PLANE_STRAIN, method=model.USAVG, shape=model.SHAPE_UGIMP, precision=1, sort_interval=1,
                 block=0, max_runs=4, max_materials=4, max_particles=1000, max_nodes=1000, fraction_usf=0.5)
-    for bad, status in ((dict(shape=model.SHAPE_LCPDI), 2), (dict(np=11), 2), (dict(precision=3), 2),
+    for bad, status in ((dict(shape=7), 2), (dict(max_fields=9), 2), (dict(np=11), 2), (dict(precision=3), 2),
                         (dict(max_runs=0), 1), (dict(max_particles=-5), 1), (dict(block=96), 1)):
         o = abi.MpmGpuBatchOptions(**{**base, **bad})
         h = C.c_void_p()
@@ -29,6 +29,13 @@ def test_batch_bytes_grows_with_capacity(gpu_lib):
     # two arena buffers of 42 doubles + 4 ints per particle, plus sort keys
     assert b2 - b1 >= 1_000_000 * 2 * (42 * 8 + 4 * 4)
     assert b1 < 1_000_000 * 750 + 500_000 * 250  # about 730 B per particle slot, 217 B per node
+    # two material fields: 26 double and 12 float columns per node and field
+    o.max_particles, o.max_fields = 1_000_000, 2
+    b3 = gpu_lib.mpmgpu_batch_bytes(C.byref(o))
+    assert b3 - b1 == 500_000 * (2 * (26 * 8 + 12 * 4 + 1) - (19 * 8 + 12 * 4 + 1))
+    # lCPDI corner scratch: 4 corners x (element + 6 doubles) per particle in 2D
+    o.shape = model.SHAPE_LCPDI
+    assert gpu_lib.mpmgpu_batch_bytes(C.byref(o)) - b3 == 1_000_000 * 4 * (4 + 6 * 8)
 
 
 def test_batch_population_is_seeded_and_matches_the_spec():
@@ -96,3 +103,22 @@ def test_block_3d_model_is_consistent():
     for c, ax, nodes in ((col, "x", g.xnodes), (row, "y", g.ynodes), (lay, "z", g.znodes)):
         assert np.all((nodes[c] <= m.particles[ax]) & (m.particles[ax] < nodes[c + 1]))
     assert len(m.bcs) == (g.nx + 1) * (g.ny + 1) and set(m.bcs["dir"]) == {4}
+
+
+def test_contact_population_is_seeded_and_matches_the_spec():
+    from nairn_gb300 import model
+    a = model.contact_run_params(64, seed=303)
+    assert a == model.contact_run_params(64, seed=303)
+    ms = model.contact_models(6, seed=303, nmin=20000, nmax=60000)
+    for m in ms:
+        assert m.options["shape"] == model.SHAPE_LCPDI and m.options["nfields"] == 2
+        assert 15000 < m.n < 75000
+        mats = m.materials
+        assert mats[0]["type"] == model.MAT_ISO and mats[1]["type"] == model.MAT_NEOHOOKEAN
+        assert m.extra["contact"]["friction"] == 0.3
+        # the block lies on the plate, inside it in x and y
+        blk = m.particles["mat"] == 1
+        plate = ~blk
+        assert blk.any() and plate.any()
+        assert m.particles["x"][blk].max() <= m.particles["x"][plate].max()
+        assert m.particles["z"][blk].min() >= m.particles["z"][plate].max()

@@ -169,3 +169,76 @@ def test_autotune_steps_count_and_results_hold(gpu_lib):
     for rid, m in zip(ids, ms):
         assert_close(b.download(rid), oracle(m, 200), TOL_MIXED, m.name)
     b.close()
+
+
+FIELDS_3D = ("x", "y", "z", "vx", "vy", "vz", "sxx", "syy", "szz", "sxy", "syz", "sxz", "pressure", "hist0")
+
+
+def assert_close_3d(out, ref, tol, what=""):
+    for k in FIELDS_3D:
+        if np.abs(ref[k]).max() == 0. and np.abs(out[k]).max() == 0.:
+            continue
+        e = rel_l2(out[k], ref[k])
+        assert e <= tol, (what, k, e)
+    assert np.array_equal(out["elem"], ref["elem"]), what
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
+def test_batched_contact_cpdi_runs_match_oracle(precision, tol, gpu_lib):
+    """3D two-material contact runs (lCPDI, Neo-Hookean on elastic, Coulomb
+    friction) of uneven sizes in one batch, each against the oracle."""
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import model, abi
+    ms = model.contact_models(4, seed=5, nmin=1500, nmax=8000, steps=25)
+    b = GpuBatch.for_models(ms, precision=precision)
+    assert b.opts.max_fields == 2
+    ids = [b.add(m) for m in ms]
+    b.step(25)
+    for rid, m in zip(ids, ms):
+        assert b.state(rid) == (abi.RUN_FINISHED, 25)
+        assert_close_3d(b.download(rid), oracle(m, 25), tol, m.name)
+    b.close()
+
+
+def test_contact_and_single_field_runs_share_a_batch(gpu_lib):
+    """A single-field run (no contact) in a two-field batch computes what it
+    computes alone; contact runs beside it are unaffected, including ones
+    with other normals and friction laws."""
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import model
+    plain = model.block_3d(ncx=6, ncy=5, ncz=4, steps=20, gimp="lCPDI")
+    c1 = model.contact_3d(plate=(8, 8, 3), block=(3, 3, 2), block_x0=1.0, block_y0=1.0, steps=20, normals=0,
+                          friction=0.)
+    c2 = model.contact_3d(plate=(7, 9, 3), block=(3, 3, 2), block_x0=1.5, block_y0=0.5, steps=20, normals=1,
+                          friction=-1.)
+    ms = [c1, plain, c2]
+    b = GpuBatch.for_models(ms)
+    ids = [b.add(m) for m in ms]
+    b.step(20)
+    for rid, m in zip(ids, ms):
+        assert_close_3d(b.download(rid), oracle(m, 20), TOL, m.name)
+    b.close()
+
+
+def test_batched_contact_2d_ugimp(gpu_lib):
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import model
+    ms = [model.contact_2d(plate=(16, 4), block=(5, 3), block_x0=3.0 + k, friction=0.3 * k, normals=k % 3,
+                           steps=30) for k in range(3)]
+    b = GpuBatch.for_models(ms, precision=1)
+    ids = [b.add(m) for m in ms]
+    b.step(30)
+    for rid, m in zip(ids, ms):
+        assert_close(b.download(rid), oracle(m, 30), TOL_MIXED, m.name)
+    b.close()
+
+
+def test_contact_run_needs_a_multifield_batch(gpu_lib):
+    from nairn_gb300.gpu import GpuBatch, GpuError
+    from nairn_gb300 import model
+    c = model.contact_3d(plate=(6, 6, 3), block=(2, 2, 2), steps=5)
+    plain = model.block_3d(ncx=4, ncy=4, ncz=4, steps=5, gimp="lCPDI")
+    b = GpuBatch.for_models([c, plain], max_fields=1)
+    with pytest.raises(GpuError, match="INVALID"):
+        b.add(c)
+    b.close()

@@ -141,3 +141,25 @@ def test_resident_cap_serialises_runs(gpu_lib):
     for (a0, a1), (b0, b1) in zip(spans, spans[1:]):
         assert b0 >= a1 - 1.0, spans  # no two runs resident at once (1 ms clock slack)
     s.close()
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
+def test_served_contact_runs(precision, tol, gpu_lib):
+    """3D two-material contact requests (lCPDI, Coulomb friction) served
+    together, arriving in two waves; each result is the oracle's."""
+    from nairn_gb300 import model, abi
+    from nairn_gb300.gpu import GpuServer
+    ms = model.contact_models(6, seed=9, nmin=1500, nmax=6000, steps=20)
+    for k, m in enumerate(ms):
+        m.nsteps = 12 + 4 * k
+    s = GpuServer(model.USAVG, model.SHAPE_LCPDI, precision, hbm_budget_bytes=512 << 20, frac_3d=1.0,
+                  steps_per_round=5, max_fields=2, nodes_per_particle=3.0)
+    ids = [s.submit(m) for m in ms[:3]]
+    time.sleep(0.05)
+    ids += [s.submit(m) for m in ms[3:]]
+    s.drain(600)
+    for rid, m in zip(ids, ms):
+        info = s.poll(rid)
+        assert info["state"] == abi.REQ_DONE and info["steps_done"] == m.nsteps, info
+        check(s.result(rid), oracle(m), 3, tol, m.name)
+    s.close()
