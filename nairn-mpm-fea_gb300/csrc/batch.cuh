@@ -1,5 +1,5 @@
 // batch.cuh -- many independent MPM runs advanced together on one GPU.
-// Included by mpm_gpu.cu (one translation unit); implements the
+// Included by batch.cu; implements the
 // mpmgpu_batch_* entry points of include/nairn_mpm_gpu.h.
 //
 // Runs share arenas: particle slots (structure of arrays, one run id per

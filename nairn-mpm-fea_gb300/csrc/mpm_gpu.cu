@@ -16,6 +16,7 @@
 #include <string>
 #include <vector>
 
+#include "host_common.cuh"
 #include "mpm_kernels.cuh"
 #include "nairn_mpm_gpu.h"
 #include "sort.cuh"
@@ -23,8 +24,6 @@
 using namespace nmg;
 
 namespace {
-
-const int kParticleDoubles = 41;  // double columns of DevParticles besides zeta
 
 struct Profile {
     const char *name;
@@ -105,7 +104,9 @@ int cuda_fail(MpmGpuCtx *c, cudaError_t e, const char *where) {
 // Neohookean::VerifyAndLoadProperties, G and K input (Neohookean.cpp:88-141).
 // kterms: MaterialBase::incrementalDefGradTerms (<= 0: 2 in 2D, 1 in 3D, as
 // StartOutput.cpp:116-119 resolves the default).
-int derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::string &why, int kterms) {
+}  // namespace
+
+int nmg::derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::string &why, int kterms) {
     std::memset(&m, 0, sizeof(m));
     m.type = in.type;
     m.field = in.field;
@@ -194,6 +195,8 @@ int derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::string &wh
     return MPMGPU_OK;
 }
 
+namespace {
+
 // Point the particle columns at a block of kParticleDoubles+1 double columns
 // (the last three are the step's natural coordinates) and 3 int columns.
 void link_columns(DevParticles &p, double *pb, int *ib, int **orig) {
@@ -209,8 +212,10 @@ void link_columns(DevParticles &p, double *pb, int *ib, int **orig) {
     *orig = ib + 2 * n;
 }
 
+}  // namespace
+
 // the matching host columns of MpmGpuParticles (nullptr for the natural coordinates)
-void hcols(const MpmGpuParticles *h, double *out[kParticleDoubles]) {
+void nmg::hcols(const MpmGpuParticles *h, double *out[kParticleDoubles]) {
     double *tmp[kParticleDoubles] = {h->x, h->y, h->z, h->vx, h->vy, h->vz, h->mass, h->lpx, h->lpy, h->lpz,
                                      h->exx, h->eyy, h->ezz, h->exy, h->exz, h->eyz, h->wxy, h->wxz, h->wyz,
                                      h->sxx, h->syy, h->szz, h->sxy, h->sxz, h->syz, h->pressure,
@@ -218,6 +223,8 @@ void hcols(const MpmGpuParticles *h, double *out[kParticleDoubles]) {
                                      h->hist0, h->hist1, h->work, h->plast, h->x0, h->y0, h->z0, nullptr, nullptr};
     std::memcpy(out, tmp, sizeof(tmp));
 }
+
+namespace {
 
 void free_particles(MpmGpuCtx *c) {
     if (c->pblock) cudaFree(c->pblock);
@@ -921,6 +928,3 @@ int mpmgpu_host_unregister(void *ptr) {
 }
 
 }  // extern "C"
-
-#include "batch.cuh"
-#include "server.cuh"

@@ -147,7 +147,7 @@ __device__ __forceinline__ int find_cell(double x, double xmin, double gx, doubl
 // particle touches more than 16 (2D) / 49 (3D) nodes (GetCPDIFunctions); here
 // those set ERR_LEFT_GRID / ERR_CPDI_NODES.  Returns false on an error.
 template <int DIM>
-__device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
+static __device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
     constexpr int NC = DIM == 3 ? 8 : 4;
     const size_t n = (size_t)p.n;
     int col, row, zr;
@@ -505,7 +505,7 @@ __device__ __forceinline__ void add_contact_terms(const DevNodes &nd, int k, dou
 // mass accumulate in FP64 in both modes: grid velocities carry the bulk motion
 // and their differences across a cell are the strain rate.
 template <int DIM, int SHAPE, bool MIX, bool BATCH>
-__global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -624,7 +624,7 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, cons
 // (GridForcesTask.cpp:40-153, MatPoint2D.cpp:242-262, MatPoint3D.cpp:248-269).
 // Mixed mode: internal-force products in FP32 into FP32 accumulators.
 template <int DIM, int SHAPE, bool STRAIN, bool MIX, bool BATCH>
-__global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -732,7 +732,7 @@ __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticl
 // v_particle + sum N (v_node - v_particle) (the weights sum to one) with the
 // differences from FP32 pairs, S a in FP32; the update itself is FP64.
 template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH>
-__global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -827,7 +827,7 @@ __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevN
 // UpdateStrainsFirstTask::FullStrainUpdate called from
 // UpdateStrainsLastContactTask (:149), fused with ResetElementsTask.
 template <int DIM, int SHAPE, bool MIX, bool BATCH>
-__global__ void __launch_bounds__(256) k_strain_last(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256) k_strain_last(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     RunView rv;
@@ -1014,7 +1014,7 @@ __device__ __forceinline__ bool coulomb_delta(const DevContact &ct, double delPi
 // (GetNormalVector :960-1069, methods 0-2), separation from the extrapolated
 // displacements (CrackSurfaceContact::MaterialSeparation), Coulomb friction.
 constexpr int kMaxFields = 8;
-__device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, int pass, double dt) {
+static __device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, int pass, double dt) {
     const int S = ct.fstride;
     int act[kMaxFields], nm = 0;
     double Pc[3] = {0., 0., 0.}, Mc = 0., dispc[3] = {0., 0., 0.}, voltot = 0.;
@@ -1149,7 +1149,7 @@ __device__ __forceinline__ bool node_active(const StepParams &sp, const DevNodes
 // vk[pkCopy] = pk, contact (MASS_MOMENTUM_CALL), velocity conditions, grid
 // velocity, on every material field of the node.
 template <int DIM, bool MIX, bool BATCH>
-__global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group, int do_bcs) {
+static __global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group, int do_bcs) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !node_active(sp, nd, n)) return;
     double t, dt;
@@ -1189,7 +1189,7 @@ __global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBCs b, co
 // particle update.  zero_contact: clear the contact terms for the second
 // extrapolation.
 template <int DIM, bool MIX, bool BATCH>
-__global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group,
+static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group,
                               int zero_contact) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !node_active(sp, nd, n)) return;
@@ -1250,7 +1250,7 @@ __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, 
 // UPDATE_STRAINS_LAST_CALL conditions, grid velocity
 // (UpdateStrainsLastContactTask.cpp:60-152).
 template <int DIM, bool MIX, bool BATCH>
-__global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group) {
+static __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !node_active(sp, nd, n)) return;
     double t, dt;
@@ -1296,7 +1296,7 @@ __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs b, con
 // End of a batched step: advance the time of every active run and retire
 // runs that have taken all their steps.  A run that raised an error stops
 // here, so the error stays confined to its own particles and nodes.
-__global__ void k_advance_runs(DevRun *runs, int nruns) {
+static __global__ void k_advance_runs(DevRun *runs, int nruns) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nruns) return;
     DevRun &R = runs[r];

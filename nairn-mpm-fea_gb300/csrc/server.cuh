@@ -1,5 +1,5 @@
 // server.cuh -- continuous-batching request loop over the batch engine.
-// Included by mpm_gpu.cu after batch.cuh; implements the mpmgpu_server_*
+// Included by batch.cu after batch.cuh; implements the mpmgpu_server_*
 // entry points of include/nairn_mpm_gpu.h.
 //
 // A server owns one batch per dimension (2D plane strain and 3D), sized at

@@ -33,7 +33,7 @@ struct SortWorkspace {
     size_t scratch_cols = 0;
 };
 
-__global__ void k_sort_init(const int *elem, int *k, int *v, int n) {
+static __global__ void k_sort_init(const int *elem, int *k, int *v, int n) {
     int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i < n) {
         k[i] = elem[i];
@@ -41,7 +41,7 @@ __global__ void k_sort_init(const int *elem, int *k, int *v, int n) {
     }
 }
 
-__global__ void k_sort_hist(const int *keys, int n, int shift, int *hist, int ntiles) {
+static __global__ void k_sort_hist(const int *keys, int n, int shift, int *hist, int ntiles) {
     __shared__ int h[kSortWarpsPerBlock][256];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
     const int tile = blockIdx.x * kSortWarpsPerBlock + w;
@@ -91,7 +91,7 @@ __device__ __forceinline__ int block_exclusive_scan(int v, int *sh, int &total) 
     return before + x - v;
 }
 
-__global__ void k_scan_reduce(const int *a, int m, int *sums) {
+static __global__ void k_scan_reduce(const int *a, int m, int *sums) {
     __shared__ int sh[32];
     const int base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
     int s = 0;
@@ -103,7 +103,7 @@ __global__ void k_scan_reduce(const int *a, int m, int *sums) {
     if (threadIdx.x == 0) sums[blockIdx.x] = total;
 }
 
-__global__ void k_scan_sums(int *sums, int nb) {
+static __global__ void k_scan_sums(int *sums, int nb) {
     __shared__ int sh[32];
     int run = 0;
     for (int base = 0; base < nb; base += kScanBlock) {
@@ -116,7 +116,7 @@ __global__ void k_scan_sums(int *sums, int nb) {
     }
 }
 
-__global__ void k_scan_apply(int *a, int m, const int *sums) {
+static __global__ void k_scan_apply(int *a, int m, const int *sums) {
     __shared__ int sh[32];
     const int base = blockIdx.x * kScanChunk + threadIdx.x * kScanItems;
     int v[kScanItems];
@@ -135,7 +135,7 @@ __global__ void k_scan_apply(int *a, int m, const int *sums) {
     }
 }
 
-__global__ void k_sort_scatter(const int *kin, const int *vin, int *kout, int *vout, int n, int shift,
+static __global__ void k_sort_scatter(const int *kin, const int *vin, int *kout, int *vout, int n, int shift,
                                const int *offs, int ntiles) {
     __shared__ int run[kSortWarpsPerBlock][256];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -165,7 +165,7 @@ __global__ void k_sort_scatter(const int *kin, const int *vin, int *kout, int *v
 }
 
 // dst[k*n + j] = src[k*n + perm[j]] for every column k
-__global__ void k_gather_cols(const double *__restrict__ src, double *__restrict__ dst, const int *__restrict__ perm,
+static __global__ void k_gather_cols(const double *__restrict__ src, double *__restrict__ dst, const int *__restrict__ perm,
                               int n, int ncols) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
@@ -173,7 +173,7 @@ __global__ void k_gather_cols(const double *__restrict__ src, double *__restrict
     for (int k = 0; k < ncols; k++) dst[(size_t)k * n + j] = src[(size_t)k * n + s];
 }
 
-__global__ void k_gather_ints(const int *__restrict__ src, int *__restrict__ dst, const int *__restrict__ perm, int n,
+static __global__ void k_gather_ints(const int *__restrict__ src, int *__restrict__ dst, const int *__restrict__ perm, int n,
                               int ncols) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
@@ -182,7 +182,7 @@ __global__ void k_gather_ints(const int *__restrict__ src, int *__restrict__ dst
 }
 
 // dst[k*n + orig[j]] = src[k*n + j] (slot j holds host particle orig[j])
-__global__ void k_unsort_cols(const double *__restrict__ src, double *__restrict__ dst, const int *__restrict__ orig,
+static __global__ void k_unsort_cols(const double *__restrict__ src, double *__restrict__ dst, const int *__restrict__ orig,
                               int n, int ncols) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
@@ -190,7 +190,7 @@ __global__ void k_unsort_cols(const double *__restrict__ src, double *__restrict
     for (int k = 0; k < ncols; k++) dst[(size_t)k * n + o] = src[(size_t)k * n + j];
 }
 
-__global__ void k_unsort_ints(const int *__restrict__ src, int *__restrict__ dst, const int *__restrict__ orig, int n,
+static __global__ void k_unsort_ints(const int *__restrict__ src, int *__restrict__ dst, const int *__restrict__ orig, int n,
                               int ncols) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
