@@ -47,7 +47,9 @@ enum {
     MPMGPU_ERR_LEFT_GRID = 6,    /* a particle left the grid (LEFT_GRID)        */
     MPMGPU_ERR_CPDI_NODES = 7,   /* CPDI domain needs more nodes than allowed   */
     MPMGPU_ERR_TIMEOUT = 8,      /* a bounded device wait gave up               */
-    MPMGPU_ERR_BUSY = 9          /* request still running (serving API)        */
+    MPMGPU_ERR_BUSY = 9,         /* request still running (serving API)        */
+    MPMGPU_ERR_RANGE = 10        /* a deterministic node sum met a contribution
+                                    beyond its bound (NaN or infinite values)  */
 };
 
 /* ---- analysis options (values follow the reference's constants) -------- */
@@ -60,7 +62,13 @@ enum { MPMGPU_PLANE_STRAIN = 10, MPMGPU_THREED = 12 };
 /* Arithmetic of the transfers (P2G/G2P and grid); the constitutive update,
  * deformation gradient and particle displacement are FP64 in both modes. */
 enum { MPMGPU_PREC_FP64 = 0, MPMGPU_PREC_MIXED = 1 };
-/* P2G accumulation: hardware FP64/FP32 atomics, or a fixed-order gather */
+/* Node sums (P2G mass and momentum, internal forces, the second extrapolation,
+ * contact terms): hardware FP64/FP32 atomics, whose summation order -- and so
+ * the last bits of a result -- varies from run to run; or exact integer sums
+ * (each contribution rounded once to a multiple of 2^-102 of the step's bound
+ * on it, then added as 64-bit integer limbs), which give the same bits in every
+ * run whatever the thread scheduling, launch shape or particle order.
+ * Single-run contexts only. */
 enum { MPMGPU_P2G_ATOMIC = 0, MPMGPU_P2G_DETERMINISTIC = 1 };
 /* Material types: Common/Read_XML/MaterialController.cpp:105-231 */
 enum { MPMGPU_MAT_ISOTROPIC = 1, MPMGPU_MAT_ISOPLASTICITY = 9, MPMGPU_MAT_NEOHOOKEAN = 28 };

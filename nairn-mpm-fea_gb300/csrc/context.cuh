@@ -1,0 +1,74 @@
+// context.cuh -- the single-run context (MpmGpuCtx of include/nairn_mpm_gpu.h),
+// shared by the C ABI (mpm_gpu.cu) and the step translation units
+// (step_fp64.cu, step_mixed.cu), which instantiate the step kernels of one
+// transfer precision each so the library builds in parallel.
+#pragma once
+
+#include <cuda_runtime.h>
+
+#include <string>
+#include <vector>
+
+#include "mpm_kernels.cuh"
+#include "nairn_mpm_gpu.h"
+#include "sort.cuh"
+
+namespace nmg {
+
+struct Profile {
+    const char *name;
+    double ms;
+};
+
+constexpr int kFamilies = 8;  // p2g, node_post, strain_forces, node_update, g2p, node_usl, strain_last, sort
+
+}  // namespace nmg
+
+struct MpmGpuCtx {
+    MpmGpuOptions opts{};
+    int dim = 2;
+    nmg::DevGrid g{};
+    nmg::DevParticles p{};
+    nmg::DevNodes nd{};
+    nmg::DevBCs bcs{};
+    int *bc_group = nullptr;
+    nmg::DevMat *mats = nullptr;
+    int nmat = 0;
+    std::vector<nmg::DevMat> hmats;
+    double *grid_coords = nullptr;
+    double *pblock = nullptr;            // particle double columns
+    int *iblock = nullptr;               // mat, elem, original index
+    int *orig = nullptr;                 // original (host) index of each slot
+    double *nblock = nullptr;            // node double columns
+    float *fblock = nullptr;             // node float columns (mixed mode)
+    size_t fblock_zero_bytes = 0;
+    size_t nblock_zero_bytes = 0;        // bytes cleared at each step start
+    unsigned char *active = nullptr;
+    unsigned *err = nullptr;
+    void *bc_block = nullptr;
+    cudaStream_t stream = nullptr;
+    nmg::SortWorkspace sort{};
+    long long steps_done = 0;
+    std::string msg;
+    std::vector<nmg::Profile> prof;
+    bool profile = false;
+    std::vector<cudaEvent_t> ev;         // per-step kernel events when profiling
+    long long launches = 0;              // kernels launched by this context
+    void *cpdi = nullptr;                // lCPDI corner scratch (ints then doubles)
+    nmg::DevContact ct{1, 0, 2, 2, 0.};       // material fields and multimaterial contact
+    bool contact_on = false;
+    nmg::DevDet det{nullptr, 0, nullptr, nullptr};     // deterministic node sums (p2g option 1)
+};
+
+namespace nmg {
+
+// event of kernel family k in step slot `slot` of the current call
+inline cudaEvent_t &event_at(MpmGpuCtx *c, int slot, int k, bool begin) {
+    return c->ev[((size_t)slot * kFamilies + k) * 2 + (begin ? 0 : 1)];
+}
+
+// enqueue one step of a context (FP64 / mixed transfers; deterministic node sums)
+void enqueue_fp64(MpmGpuCtx *c, double t, int slot, bool det);
+void enqueue_mixed(MpmGpuCtx *c, double t, int slot, bool det);
+
+}  // namespace nmg

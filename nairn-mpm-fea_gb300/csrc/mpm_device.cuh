@@ -11,7 +11,7 @@ namespace nmg {
 constexpr double kSqrtTwoThirds = 0.8164965809277260;  // sqrt(2/3)
 
 // error bits raised by kernels (reported through the C ABI status)
-enum : unsigned { ERR_NAN = 1u, ERR_LEFT_GRID = 2u, ERR_EDGE = 4u, ERR_CPDI_NODES = 16u };
+enum : unsigned { ERR_NAN = 1u, ERR_LEFT_GRID = 2u, ERR_EDGE = 4u, ERR_CPDI_NODES = 16u, ERR_RANGE = 32u };
 
 // material type ids (MaterialController.cpp:105-231)
 constexpr int kMatIsotropic = 1, kMatIsoPlasticity = 9, kMatNeohookean = 28;
@@ -87,6 +87,19 @@ struct DevContact {
     double friction; // Coulomb coefficient
 };
 
+// Deterministic node sums (MPMGPU_P2G_DETERMINISTIC): three 64-bit integer
+// limbs per accumulated node quantity -- limb l of quantity q at node n is
+// lim[(3 q + l) stride + n] -- and the step's magnitude bounds, step-wide per
+// bound slot and per node, as the bit patterns of non-negative doubles
+// (atomicMax on the bits orders them as numbers).  lim == nullptr: hardware
+// float atomics.
+struct DevDet {
+    long long *lim;
+    size_t stride;
+    unsigned long long *bnd;
+    unsigned long long *nbnd;  // each node's largest mass contribution (bits)
+};
+
 // One run of a batch: its grid, where its nodes and cells start in the
 // batch's node and cell arenas, and its own time stepping.
 struct DevRun {
@@ -112,6 +125,7 @@ struct StepParams {
     DevRun *runs;
     const int *nrun;   // run of each node (-1: unused)
     DevContact ct;     // one field unless multimaterial mode
+    DevDet det;        // deterministic node sums (single-run contexts only)
 };
 
 // Velocity conditions grouped by node, list order kept inside a node.

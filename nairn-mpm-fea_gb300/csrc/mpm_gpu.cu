@@ -16,21 +16,10 @@
 #include <string>
 #include <vector>
 
+#include "context.cuh"
 #include "host_common.cuh"
-#include "mpm_kernels.cuh"
-#include "nairn_mpm_gpu.h"
-#include "sort.cuh"
 
 using namespace nmg;
-
-namespace {
-
-struct Profile {
-    const char *name;
-    double ms;
-};
-
-}  // namespace
 
 // slot order = host order after an upload; flags out-of-range indices
 __global__ void k_upload_check(const int *mat, const int *elem, int *orig, int n, int nmat, int nelems,
@@ -41,41 +30,6 @@ __global__ void k_upload_check(const int *mat, const int *elem, int *orig, int n
     const int m = mat[i], e = elem[i];
     if (m < 0 || m >= nmat || e < 0 || e >= nelems) atomicOr(err, 8u);
 }
-
-struct MpmGpuCtx {
-    MpmGpuOptions opts{};
-    int dim = 2;
-    DevGrid g{};
-    DevParticles p{};
-    DevNodes nd{};
-    DevBCs bcs{};
-    int *bc_group = nullptr;
-    DevMat *mats = nullptr;
-    int nmat = 0;
-    std::vector<DevMat> hmats;
-    double *grid_coords = nullptr;
-    double *pblock = nullptr;            // particle double columns
-    int *iblock = nullptr;               // mat, elem, original index
-    int *orig = nullptr;                 // original (host) index of each slot
-    double *nblock = nullptr;            // node double columns
-    float *fblock = nullptr;             // node float columns (mixed mode)
-    size_t fblock_zero_bytes = 0;
-    size_t nblock_zero_bytes = 0;        // bytes cleared at each step start
-    unsigned char *active = nullptr;
-    unsigned *err = nullptr;
-    void *bc_block = nullptr;
-    cudaStream_t stream = nullptr;
-    SortWorkspace sort{};
-    long long steps_done = 0;
-    std::string msg;
-    std::vector<Profile> prof;
-    bool profile = false;
-    std::vector<cudaEvent_t> ev;         // per-step kernel events when profiling
-    long long launches = 0;              // kernels launched by this context
-    void *cpdi = nullptr;                // lCPDI corner scratch (ints then doubles)
-    DevContact ct{1, 0, 2, 2, 0.};       // material fields and multimaterial contact
-    bool contact_on = false;
-};
 
 namespace {
 
@@ -263,6 +217,8 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
     if (opts->precision != MPMGPU_PREC_FP64 && opts->precision != MPMGPU_PREC_MIXED)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "precision must be MPMGPU_PREC_FP64 or MPMGPU_PREC_MIXED");
+    if (opts->p2g != MPMGPU_P2G_ATOMIC && opts->p2g != MPMGPU_P2G_DETERMINISTIC)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "p2g must be MPMGPU_P2G_ATOMIC or MPMGPU_P2G_DETERMINISTIC");
     if (!(opts->timestep > 0.)) return set_err(nullptr, MPMGPU_ERR_INVALID, "timestep must be > 0");
     if (grid->nx < 3 || grid->ny < 3 || (grid->dim == 3 && grid->nz < 3) || !grid->xnodes || !grid->ynodes ||
         (grid->dim == 3 && !grid->znodes))
@@ -382,6 +338,20 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     cudaMemset(c->fblock, 0, NN * (fcleared + fkept) * sizeof(float));
     cudaMemset(c->bc_group, 0xFF, NN * sizeof(int));
     cudaMemset(c->err, 0, sizeof(unsigned));
+    if (opts->p2g == MPMGPU_P2G_DETERMINISTIC) {
+        // three limbs per accumulated quantity (the contact terms only with
+        // several fields), zero between uses; the step's bounds
+        const size_t nq = nf > 1 ? kDetQuantities : DQ_VOL;
+        if ((e = cudaMalloc(&c->det.lim, nq * 3 * NN * sizeof(long long))) != cudaSuccess ||
+            (e = cudaMalloc(&c->det.bnd, kDetBounds * sizeof(unsigned long long))) != cudaSuccess ||
+            (e = cudaMalloc(&c->det.nbnd, NN * sizeof(unsigned long long))) != cudaSuccess) {
+            std::string m = std::string("device allocation: ") + cudaGetErrorString(e);
+            mpmgpu_destroy(c);
+            return set_err(nullptr, MPMGPU_ERR_OOM, m);
+        }
+        c->det.stride = NN;
+        cudaMemset(c->det.lim, 0, nq * 3 * NN * sizeof(long long));
+    }
     const char *names[] = {"p2g", "node_post", "strain_forces", "node_update", "g2p", "node_usl", "strain_last",
                            "sort"};
     for (const char *n : names) c->prof.push_back(Profile{n, 0.});
@@ -570,90 +540,10 @@ int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
 
 namespace {
 
-constexpr int kFamilies = 8;  // p2g, node_post, strain_forces, node_update, g2p, node_usl, strain_last, sort
-
-// event of kernel family k in step slot `slot` of the current call
-inline cudaEvent_t &event_at(MpmGpuCtx *c, int slot, int k, bool begin) {
-    return c->ev[((size_t)slot * kFamilies + k) * 2 + (begin ? 0 : 1)];
-}
-
-template <int DIM, int SHAPE, bool MIX>
-void enqueue_step(MpmGpuCtx *c, double t, int slot) {
-    const int n = c->p.n, NN = c->g.nnodes;
-    const int TB = 256;
-    const int pb = (n + TB - 1) / TB, nb = (NN + TB - 1) / TB;
-    const double dt = c->opts.timestep;
-    const int method = c->opts.method;
-    const double stFirst = method == MPMGPU_USAVG ? c->opts.fraction_usf * dt : dt;
-    const double stLast = method == MPMGPU_USAVG ? dt - stFirst : dt;
-    cudaStream_t s = c->stream;
-    auto mark = [&](int k, bool begin) {
-        if (c->profile) cudaEventRecord(event_at(c, slot, k, begin), s);
-        if (!begin) c->launches++;
-    };
-    cudaMemsetAsync(c->nblock, 0, c->nblock_zero_bytes, s);
-    cudaMemsetAsync(c->nd.active, 0, (size_t)NN * c->ct.nf, s);
-    if (MIX) cudaMemsetAsync(c->fblock, 0, c->fblock_zero_bytes, s);
-    StepParams sp;
-    sp.ct = c->ct;
-    sp.g = c->g;
-    sp.dt = dt;
-    sp.st_first = stFirst;
-    sp.st_last = stLast;
-    sp.t = t;
-    sp.err = c->err;
-    sp.runs = nullptr;
-    sp.nrun = nullptr;
-    mark(0, true);
-    k_p2g<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
-    mark(0, false);
-    mark(1, true);
-    k_node_post<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL);
-    mark(1, false);
-    mark(2, true);
-    if (method == MPMGPU_USL)
-        k_strain_forces<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
-    else
-        k_strain_forces<DIM, SHAPE, true, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
-    mark(2, false);
-    mark(3, true);
-    k_node_update<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group,
-                                                     c->ct.nf > 1 && method != MPMGPU_USF);
-    mark(3, false);
-    mark(4, true);
-    if (method == MPMGPU_USF) {
-        k_g2p<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
-        mark(4, false);
-        return;
-    }
-    k_g2p<DIM, SHAPE, true, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
-    mark(4, false);
-    mark(5, true);
-    k_node_usl<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
-    mark(5, false);
-    mark(6, true);
-    k_strain_last<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
-    mark(6, false);
-}
-
-template <bool MIX>
-void enqueue_prec(MpmGpuCtx *c, double t, int slot) {
-    const bool d3 = c->dim == 3;
-    const int shape = c->opts.shape;
-    if (d3) {
-        if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<3, SHAPE_LINEAR, MIX>(c, t, slot);
-        else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<3, SHAPE_LCPDI, MIX>(c, t, slot);
-        else enqueue_step<3, SHAPE_UGIMP, MIX>(c, t, slot);
-    } else {
-        if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<2, SHAPE_LINEAR, MIX>(c, t, slot);
-        else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<2, SHAPE_LCPDI, MIX>(c, t, slot);
-        else enqueue_step<2, SHAPE_UGIMP, MIX>(c, t, slot);
-    }
-}
-
 void enqueue(MpmGpuCtx *c, double t, int slot) {
-    if (c->opts.precision == MPMGPU_PREC_MIXED) enqueue_prec<true>(c, t, slot);
-    else enqueue_prec<false>(c, t, slot);
+    const bool det = c->det.lim != nullptr;
+    if (c->opts.precision == MPMGPU_PREC_MIXED) enqueue_mixed(c, t, slot, det);
+    else enqueue_fp64(c, t, slot, det);
 }
 
 int ensure_events(MpmGpuCtx *c, int nsteps) {
@@ -672,6 +562,8 @@ int error_status(MpmGpuCtx *c, unsigned bits) {
     if (bits & ERR_EDGE) return set_err(c, MPMGPU_ERR_LEFT_GRID, "a particle moved into a grid edge element");
     if (bits & ERR_CPDI_NODES)
         return set_err(c, MPMGPU_ERR_CPDI_NODES, "a CPDI particle domain touches more nodes than the reference allows");
+    if (bits & ERR_RANGE)
+        return set_err(c, MPMGPU_ERR_RANGE, "a deterministic node sum met a NaN, infinite or out-of-bound value");
     return MPMGPU_OK;
 }
 
@@ -784,6 +676,9 @@ void mpmgpu_destroy(MpmGpuCtx *c) {
     if (c->bc_group) cudaFree(c->bc_group);
     if (c->bc_block) cudaFree(c->bc_block);
     if (c->err) cudaFree(c->err);
+    if (c->det.lim) cudaFree(c->det.lim);
+    if (c->det.bnd) cudaFree(c->det.bnd);
+    if (c->det.nbnd) cudaFree(c->det.nbnd);
     for (auto &e : c->ev) cudaEventDestroy(e);
     if (c->stream) cudaStreamDestroy(c->stream);
     delete c;

@@ -21,6 +21,124 @@ namespace nmg {
 
 enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2 };
 
+// ---------------------------------------------------------------------------
+// deterministic node sums (MPMGPU_P2G_DETERMINISTIC)
+// ---------------------------------------------------------------------------
+// Every contribution v to a node quantity is rounded once to an integer
+// multiple of 2^-k, where a bound B on |v| fixes k so that |v| 2^k < 2^103,
+// and that integer is added as three limbs of 42 bits (v 2^k = l0 + l1 2^42 +
+// l2 2^84, each limb a signed 64-bit sum).  Integer addition is associative,
+// so a node sum -- and all that is computed from it -- is the same bit for bit
+// whatever order threads add in, whatever the particle order and launch shape.
+// A limb holds 2^20 contributions before it could overflow.
+//
+// Mass-like quantities are scaled per node: B is the node's largest mass
+// contribution N mp (found by k_det_bounds), times a step-wide bound on the
+// ratio to mass for momentum (|v|), contact volume (V/m) and mass-weighted
+// displacement (|x - x0|).  So a node touched only by the far edge of a
+// particle's support (N ~ 1e-30 in uGIMP) keeps 2^-102 relative resolution:
+// its velocity p/m and acceleration f/m are then as accurate as the FP64
+// sums', which matters because such a node's velocity enters the particle's
+// velocity gradient through grad N ~ sqrt(N).  Forces and volume gradients,
+// which scale with grad N, use a step-wide B.
+enum { DQ_MASS = 0, DQ_PX, DQ_PY, DQ_PZ, DQ_FX, DQ_FY, DQ_FZ, DQ_UX, DQ_UY, DQ_UZ,
+       DQ_VOL, DQ_DSX, DQ_DSY, DQ_DSZ, DQ_GVX, DQ_GVY, DQ_GVZ, kDetQuantities };
+// step-wide bound slots: largest |v|, internal force, |v| after the particle
+// update, and for contact V/m, |x - x0| and the volume-gradient terms of the
+// first (P2G) and second (USL) extrapolations
+enum { DB_MOM = 0, DB_FORCE, DB_UMOM, DB_VOL, DB_DS, DB_GV, DB_UVOL, DB_UDS, DB_UGV, kDetBounds };
+
+// exponent e of a bound (the bits of a non-negative double) with B < 2^(e+1)
+__device__ __forceinline__ int det_exp(unsigned long long bits) {
+    const int ex = (int)(bits >> 52);
+    return ex ? ex - 1023 : -1023;
+}
+
+__device__ __forceinline__ int det_clamp(int k) { return k > 1000 ? 1000 : (k < -1000 ? -1000 : k); }
+
+// k for contributions bounded by B: 2^(e+1) 2^k = 2^103
+__device__ __forceinline__ int det_shift(unsigned long long bits) {
+    return bits == 0ull ? 0 : det_clamp(102 - det_exp(bits));
+}
+
+// k for contributions bounded by the product of two bounds
+__device__ __forceinline__ int det_shift2(unsigned long long a, unsigned long long b) {
+    return (a == 0ull || b == 0ull) ? 0 : det_clamp(101 - det_exp(a) - det_exp(b));
+}
+
+// 2^k as a double, -1022 <= k <= 1023
+__device__ __forceinline__ double pow2(int k) { return __longlong_as_double((long long)(k + 1023) << 52); }
+
+// add v 2^k, rounded to the nearest integer (ties away from zero), to the
+// limbs of quantity q at node n
+__device__ __forceinline__ void det_add(const DevDet &d, int q, int n, double v, double scale, unsigned *err) {
+    const double t = v * scale;
+    const unsigned long long b = (unsigned long long)__double_as_longlong(t);
+    const int ex = (int)((b >> 52) & 0x7ffull);
+    if (ex == 0x7ff || ex > 1075 + 51) {  // NaN, infinite or beyond 2^104: the bound did not hold
+        atomicOr(err, ERR_RANGE);
+        return;
+    }
+    const unsigned long long m = (b & 0xFFFFFFFFFFFFFull) | (ex ? (1ull << 52) : 0ull);
+    const int sh = (ex ? ex : 1) - 1075;  // |t| = m 2^sh
+    constexpr unsigned long long M42 = (1ull << 42) - 1;
+    unsigned long long l0, l1, l2;
+    if (sh >= 0) {
+        const unsigned __int128 X = (unsigned __int128)m << sh;
+        l0 = (unsigned long long)X & M42;
+        l1 = (unsigned long long)(X >> 42) & M42;
+        l2 = (unsigned long long)(X >> 84);
+    } else if (sh > -54) {
+        const unsigned long long X = (m + (1ull << (-sh - 1))) >> (-sh);
+        l0 = X & M42;
+        l1 = X >> 42;
+        l2 = 0ull;
+    } else {
+        return;  // |t| < 1/2 rounds to zero
+    }
+    if (b >> 63) {
+        l0 = 0ull - l0;
+        l1 = 0ull - l1;
+        l2 = 0ull - l2;
+    }
+    unsigned long long *L = (unsigned long long *)d.lim + (size_t)(3 * q) * d.stride + n;
+    if (l0) atomicAdd(L, l0);
+    if (l1) atomicAdd(L + d.stride, l1);
+    if (l2) atomicAdd(L + 2 * d.stride, l2);
+}
+
+// the node sum of quantity q as a double (times 2^-k via inv_scale); the
+// limbs are cleared for the next accumulation
+__device__ __forceinline__ double det_take(const DevDet &d, int q, int n, double inv_scale) {
+    long long *L = d.lim + (size_t)(3 * q) * d.stride + n;
+    long long a0 = L[0], a1 = L[d.stride], a2 = L[2 * d.stride];
+    if ((a0 | a1 | a2) == 0) return 0.;
+    L[0] = 0;
+    L[d.stride] = 0;
+    L[2 * d.stride] = 0;
+    // carry into normalised limbs r0, r1 in [0, 2^42)
+    const long long c0 = a0 >> 42;
+    const long long r0 = a0 - c0 * (1ll << 42);
+    a1 += c0;
+    const long long c1 = a1 >> 42;
+    const long long r1 = a1 - c1 * (1ll << 42);
+    a2 += c1;
+    const double lowpart = (double)r1 * 4398046511104.0 + (double)r0;  // r1 2^42 + r0, one rounding
+    return ((double)a2 * 19342813113834066795298816.0 + lowpart) * inv_scale;  // a2 2^84 + ...
+}
+
+// raise bound slot `slot` to at least v (v >= 0) -- one atomic per warp
+__device__ __forceinline__ void det_bound(const DevDet &d, int slot, double v) {
+    const unsigned long long bits = (unsigned long long)__double_as_longlong(v);
+    const unsigned mask = __activemask();
+    const unsigned hi = __reduce_max_sync(mask, (unsigned)(bits >> 32));
+    const unsigned lo = __reduce_max_sync(mask, (unsigned)(bits >> 32) == hi ? (unsigned)bits : 0u);
+    if ((threadIdx.x & 31) == (unsigned)(__ffs(mask) - 1)) {
+        const unsigned long long w = ((unsigned long long)hi << 32) | lo;
+        if (w > d.bnd[slot]) atomicMax(d.bnd + slot, w);
+    }
+}
+
 // Visit the nodes of one particle, calling f(node0based, N, dNdx, dNdy, dNdz).
 // ElementBase::GetShapeFunctions / GetShapeGradients
 // (NairnMPM/src/Elements/MoreMPMElementBase.cpp:120-284).  T is the arithmetic
@@ -499,12 +617,106 @@ __device__ __forceinline__ void add_contact_terms(const DevNodes &nd, int k, dou
     }
 }
 
+// the same terms as deterministic node sums (scales: volume, displacement, gradient)
+template <int DIM>
+__device__ __forceinline__ void det_contact_terms(const DevDet &dd, int k, double N, double fnmp, double Vp,
+                                                  const double d[3], double gx, double gy, double gz,
+                                                  const double sc[3], unsigned *err) {
+    det_add(dd, DQ_VOL, k, N * Vp, sc[0], err);
+    det_add(dd, DQ_DSX, k, d[0] * fnmp, sc[1], err);
+    det_add(dd, DQ_DSY, k, d[1] * fnmp, sc[1], err);
+    det_add(dd, DQ_GVX, k, gx * Vp, sc[2], err);
+    det_add(dd, DQ_GVY, k, gy * Vp, sc[2], err);
+    if (DIM == 3) {
+        det_add(dd, DQ_DSZ, k, d[2] * fnmp, sc[1], err);
+        det_add(dd, DQ_GVZ, k, gz * Vp, sc[2], err);
+    }
+}
+
+// A bound on every shape-function gradient component of particle i, twice
+// the analytic one: 1 / cell size for linear and uGIMP weights (a GIMP weight
+// changes by at most the particle width over the cell size across the particle
+// width); for lCPDI the sum over corners of the largest gradient weight, as
+// each node gradient is sum_c wg_c N_c(node) with 0 <= N_c <= 1.
+template <int DIM, int SHAPE>
+__device__ __forceinline__ double grad_bound(const DevGrid &g, const DevParticles &p, int i) {
+    if constexpr (SHAPE == SHAPE_LCPDI) {
+        constexpr int NC = DIM == 3 ? 8 : 4;
+        const size_t n = (size_t)p.n;
+        double s = 0.;
+#pragma unroll
+        for (int c = 0; c < NC; c++) {
+            double w = fmax(fabs(p.cwg[(3 * c) * n + i]), fabs(p.cwg[(3 * c + 1) * n + i]));
+            if (DIM == 3) w = fmax(w, fabs(p.cwg[(3 * c + 2) * n + i]));
+            s += w;
+        }
+        return 2. * s;
+    } else {
+        double m = fmax(g.igx, g.igy);
+        if (DIM == 3) m = fmax(m, g.igz);
+        return 2. * m;
+    }
+}
+
+// largest |x - x0| component of particle i at position xp
+template <int DIM>
+__device__ __forceinline__ double displacement_bound(const DevParticles &p, int i, const double xp[3]) {
+    double m = fmax(fabs(xp[0] - p.x0[i]), fabs(xp[1] - p.y0[i]));
+    if (DIM == 3) m = fmax(m, fabs(xp[2] - p.z0[i]));
+    return m;
+}
+
+// Bounds of the first extrapolation's contributions, before k_p2g in the
+// deterministic mode: each node's largest N mp (the visit and arithmetic of
+// k_p2g, so every node k_p2g adds to has one), and the step-wide ratio bounds.
+// The lCPDI corners of the step are set here (k_p2g then uses them).
+template <int DIM, int SHAPE, bool MIX>
+static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevParticles p, const DevMat *mats) {
+    using T = typename Wt<MIX>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const DevGrid &g = sp.g;
+    bool ok = true;
+    if constexpr (SHAPE == SHAPE_LCPDI) ok = cpdi_setup<DIM>(g, p, i, sp.err);
+    const double mp = p.mass[i];
+    const int off = sp.ct.nf > 1 ? sp.ct.fstride * mats[p.mat[i]].field : 0;
+    const bool mm = sp.ct.nf > 1;
+    unsigned long long *nb = sp.det.nbnd;
+    auto node = [&](int n, T N, T, T, T) {
+        if (N == T(0)) return;
+        atomicMax(nb + n + off, (unsigned long long)__double_as_longlong((double)N * mp));
+    };
+    if (ok) {
+        if constexpr (SHAPE == SHAPE_LCPDI) {
+            if (mm) visit_nodes<DIM, SHAPE, true, T>(g, 0, p, i, node);
+            else visit_nodes<DIM, SHAPE, false, T>(g, 0, p, i, node);
+        } else {
+            const int e = p.elem[i];
+            double xi, eta, zeta;
+            xi_position(g, e, p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0., xi, eta, zeta);
+            const double lz = DIM == 3 ? p.lpz[i] : 1.;
+            if (mm) for_each_node<DIM, SHAPE, true, T>(g, 0, e, xi, eta, zeta, p.lpx[i], p.lpy[i], lz, node);
+            else for_each_node<DIM, SHAPE, false, T>(g, 0, e, xi, eta, zeta, p.lpx[i], p.lpy[i], lz, node);
+        }
+    }
+    double vm = fmax(fabs(p.vx[i]), fabs(p.vy[i]));
+    if (DIM == 3) vm = fmax(vm, fabs(p.vz[i]));
+    det_bound(sp.det, DB_MOM, vm);
+    if (mm) {
+        const double Vp = fabs(contact_volume<DIM>(p, i, mats[p.mat[i]].rho));
+        const double xp[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
+        det_bound(sp.det, DB_VOL, Vp / mp);
+        det_bound(sp.det, DB_DS, displacement_bound<DIM>(p, i, xp));
+        det_bound(sp.det, DB_GV, Vp * grad_bound<DIM, SHAPE>(g, p, i));
+    }
+}
+
 // InitializationTask::Execute (natural coordinates, InitializationTask.cpp:59-83)
 // and MassAndMomentumTask::Execute with NodalPoint::AddMassMomentum
 // (MassAndMomentumTask.cpp:48-127, NodalPointMPM.cpp:419-453).  Momentum and
 // mass accumulate in FP64 in both modes: grid velocities carry the bulk motion
 // and their differences across a cell are the strain rate.
-template <int DIM, int SHAPE, bool MIX, bool BATCH>
+template <int DIM, int SHAPE, bool MIX, bool BATCH, bool DET = false>
 static __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -530,10 +742,33 @@ static __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles 
         d[1] = p.y[i] - p.y0[i];
         if (DIM == 3) d[2] = p.z[i] - p.z0[i];
     }
+    unsigned long long bM = 0, bV = 0, bD = 0;
+    double sG = 1.;
+    if constexpr (DET) {
+        bM = sp.det.bnd[DB_MOM];
+        bV = sp.det.bnd[DB_VOL];
+        bD = sp.det.bnd[DB_DS];
+        sG = pow2(det_shift(sp.det.bnd[DB_GV]));
+    }
     auto scatter = [&](int n, T N, T gx, T gy, T gz) {
         if (N == T(0)) return;
         n += off;
         const double fnmp = (double)N * mp;
+        if constexpr (DET) {
+            const unsigned long long nb = sp.det.nbnd[n];
+            const double sP = pow2(det_shift2(nb, bM));
+            det_add(sp.det, DQ_MASS, n, fnmp, pow2(det_shift(nb)), rv.err);
+            det_add(sp.det, DQ_PX, n, vx * fnmp, sP, rv.err);
+            det_add(sp.det, DQ_PY, n, vy * fnmp, sP, rv.err);
+            if (DIM == 3) det_add(sp.det, DQ_PZ, n, vz * fnmp, sP, rv.err);
+            nd.active[n] = 1;
+            if (mm) {
+                const double sc[3] = {pow2(det_shift2(nb, bV)), pow2(det_shift2(nb, bD)), sG};
+                det_contact_terms<DIM>(sp.det, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz, sc,
+                                       rv.err);
+            }
+            return;
+        }
         atomicAdd(&nd.mass[n], fnmp);
         atomicAdd(&nd.px[n], vx * fnmp);
         atomicAdd(&nd.py[n], vy * fnmp);
@@ -542,8 +777,9 @@ static __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles 
         if (mm) add_contact_terms<DIM>(nd, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz);
     };
     if constexpr (SHAPE == SHAPE_LCPDI) {
-        // ElementBase::GetShapeFunctionData: the particle's CPDI corners for this step
-        if (!cpdi_setup<DIM>(g, p, i, rv.err)) return;
+        // ElementBase::GetShapeFunctionData: the particle's CPDI corners for
+        // this step (set by k_det_bounds in the deterministic mode)
+        if (!DET && !cpdi_setup<DIM>(g, p, i, rv.err)) return;
         if (mm) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
         else visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, scatter);
     } else {
@@ -619,30 +855,21 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, cons
     for (int k = 0; k < 9; k++) du[k] = (double)d[k] * st;
 }
 
-// UpdateStrainsFirstTask::FullStrainUpdate (UpdateStrainsFirstTask.cpp:101-168)
-// fused with GridForcesTask::Execute and MatPoint2D/3D::GetFintPlusFext
-// (GridForcesTask.cpp:40-153, MatPoint2D.cpp:242-262, MatPoint3D.cpp:248-269).
-// Mixed mode: internal-force products in FP32 into FP32 accumulators.
-template <int DIM, int SHAPE, bool STRAIN, bool MIX, bool BATCH>
-static __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+// GetFintPlusFext scatter of particle i: -mp (sigma - P I) . grad N to its
+// nodes (FP32 products and atomics in the mixed mode; deterministic node sums
+// with DET)
+template <int DIM, int SHAPE, bool MIX, bool DET>
+__device__ __forceinline__ void forces_scatter(const StepParams &sp, const DevParticles &p, const DevNodes &nd,
+                                                 int i, const DevGrid &g, int nb, int off) {
     using T = typename Wt<MIX>::T;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    RunView rv;
-    if (!particle_run<BATCH>(sp, p, i, rv)) return;
-    const DevGrid &g = rv.g;
-    const int off = field_offset(sp, mats, p, i);
-    if (STRAIN) {
-        double du[9];
-        velocity_gradient<DIM, SHAPE, MIX>(g, rv.nb, p, nd, i, rv.st_first, du, off);
-        constitutive<DIM>(mats, p, i, du);
-    }
+    double sF = 1.;
+    if constexpr (DET) sF = pow2(det_shift(sp.det.bnd[DB_FORCE]));
     // -mp * (sigma - P I): the internal force of GetFintPlusFext, scaled once
     const double mp = p.mass[i], P = p.pressure[i];
     const T sxx = (T)(-mp * (p.sxx[i] - P)), syy = (T)(-mp * (p.syy[i] - P)), sxy = (T)(-mp * p.sxy[i]);
     const T szz = DIM == 3 ? (T)(-mp * (p.szz[i] - P)) : T(0), sxz = DIM == 3 ? (T)(-mp * p.sxz[i]) : T(0),
             syz = DIM == 3 ? (T)(-mp * p.syz[i]) : T(0);
-    visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
+    visit_nodes<DIM, SHAPE, true, T>(g, nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
                                            n += off;
                                            T fx, fy, fz = 0;
@@ -654,7 +881,11 @@ static __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, Dev
                                                fy = sxy * dx + syy * dy + syz * dz;
                                                fz = sxz * dx + syz * dy + szz * dz;
                                            }
-                                           if (MIX) {
+                                           if constexpr (DET) {
+                                               det_add(sp.det, DQ_FX, n, (double)fx, sF, sp.err);
+                                               det_add(sp.det, DQ_FY, n, (double)fy, sF, sp.err);
+                                               if (DIM == 3) det_add(sp.det, DQ_FZ, n, (double)fz, sF, sp.err);
+                                           } else if (MIX) {
                                                atomicAdd(&nd.gx[n], (float)fx);
                                                atomicAdd(&nd.gy[n], (float)fy);
                                                if (DIM == 3) atomicAdd(&nd.gz[n], (float)fz);
@@ -664,6 +895,48 @@ static __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, Dev
                                                if (DIM == 3) atomicAdd(&nd.fz[n], (double)fz);
                                            }
                                        });
+}
+
+
+// UpdateStrainsFirstTask::FullStrainUpdate (UpdateStrainsFirstTask.cpp:101-168)
+// fused with GridForcesTask::Execute and MatPoint2D/3D::GetFintPlusFext
+// (GridForcesTask.cpp:40-153, MatPoint2D.cpp:242-262, MatPoint3D.cpp:248-269).
+// Mixed mode: internal-force products in FP32 into FP32 accumulators.
+template <int DIM, int SHAPE, bool STRAIN, bool MIX, bool BATCH, bool DET = false>
+static __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    RunView rv;
+    if (!particle_run<BATCH>(sp, p, i, rv)) return;
+    const DevGrid &g = rv.g;
+    const int off = field_offset(sp, mats, p, i);
+    if (STRAIN) {
+        double du[9];
+        velocity_gradient<DIM, SHAPE, MIX>(g, rv.nb, p, nd, i, rv.st_first, du, off);
+        constitutive<DIM>(mats, p, i, du);
+    }
+    if constexpr (DET) {
+        // the forces are summed by k_det_forces once the bound of all of them is known
+        const double mp = p.mass[i], P = p.pressure[i];
+        const double a = fabs(p.sxx[i] - P), b = fabs(p.syy[i] - P), c = fabs(p.sxy[i]);
+        double r = fmax(a + c, c + b);
+        if (DIM == 3) {
+            const double zz = fabs(p.szz[i] - P), xz = fabs(p.sxz[i]), yz = fabs(p.syz[i]);
+            r = fmax(fmax(a + c + xz, c + b + yz), xz + yz + zz);
+        }
+        det_bound(sp.det, DB_FORCE, mp * r * grad_bound<DIM, SHAPE>(g, p, i));
+        return;
+    }
+    forces_scatter<DIM, SHAPE, MIX, false>(sp, p, nd, i, g, rv.nb, off);
+}
+
+// Deterministic mode: the internal-force scatter of k_strain_forces as its own
+// pass, once k_strain_forces has bounded every particle's forces.
+template <int DIM, int SHAPE, bool MIX>
+static __global__ void __launch_bounds__(256) k_det_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    forces_scatter<DIM, SHAPE, MIX, true>(sp, p, nd, i, sp.g, 0, field_offset(sp, mats, p, i));
 }
 
 // ResetElementsTask::ResetElement with MeshInfo::FindElementFromPoint and
@@ -731,7 +1004,7 @@ __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticl
 // same natural coordinates of the step.  Mixed mode: S v is formed as
 // v_particle + sum N (v_node - v_particle) (the weights sum to one) with the
 // differences from FP32 pairs, S a in FP32; the update itself is FP64.
-template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH>
+template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH, bool DET = false>
 static __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
@@ -793,7 +1066,19 @@ static __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles 
         p.vz[i] = v[2];
         p.z[i] = xp[2];
     }
-    if (USL) {
+    if (USL && DET) {
+        // bounds of the second extrapolation, which k_det_usl then sums
+        const double mp = p.mass[i];
+        double vm = fmax(fabs(v[0]), fabs(v[1]));
+        if (DIM == 3) vm = fmax(vm, fabs(v[2]));
+        det_bound(sp.det, DB_UMOM, vm);
+        if (rv.mm) {
+            const double Vp = fabs(contact_volume<DIM>(p, i, mats[p.mat[i]].rho));
+            det_bound(sp.det, DB_UVOL, Vp / mp);
+            det_bound(sp.det, DB_UDS, displacement_bound<DIM>(p, i, xp));
+            det_bound(sp.det, DB_UGV, Vp * grad_bound<DIM, SHAPE>(g, p, i));
+        }
+    } else if (USL) {
         // second extrapolation (NodalPoint::AddMassMomentumLast), with the
         // contact terms at the moved positions in multimaterial mode
         const double mp = p.mass[i];
@@ -821,6 +1106,55 @@ static __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles 
         }
     } else {
         reset_element<DIM>(g, p, i, rv.err);
+    }
+}
+
+// Deterministic mode: the second extrapolation of k_g2p (momentum at the
+// updated velocities, contact terms at the moved positions, the step's
+// natural coordinates) as its own pass, once k_g2p has bounded it.
+template <int DIM, int SHAPE, bool MIX>
+static __global__ void __launch_bounds__(256) k_det_usl(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+    using T = typename Wt<MIX>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    const DevGrid &g = sp.g;
+    const int off = field_offset(sp, mats, p, i);
+    const bool mm = sp.ct.nf > 1;
+    const double mp = p.mass[i];
+    const double v[3] = {p.vx[i], p.vy[i], DIM == 3 ? p.vz[i] : 0.};
+    const unsigned long long bU = sp.det.bnd[DB_UMOM], bV = sp.det.bnd[DB_UVOL], bD = sp.det.bnd[DB_UDS];
+    const double sG = pow2(det_shift(sp.det.bnd[DB_UGV]));
+    double Vp = 0., d[3] = {0., 0., 0.};
+    if (mm) {
+        Vp = contact_volume<DIM>(p, i, mats[p.mat[i]].rho);
+        d[0] = p.x[i] - p.x0[i];
+        d[1] = p.y[i] - p.y0[i];
+        if (DIM == 3) d[2] = p.z[i] - p.z0[i];
+    }
+    auto scatter = [&](int n, T N, T gx, T gy, T gz) {
+        if (N == T(0)) return;
+        n += off;
+        const double fnmp = (double)N * mp;
+        const unsigned long long nb = sp.det.nbnd[n];
+        const double sU = pow2(det_shift2(nb, bU));
+        det_add(sp.det, DQ_UX, n, v[0] * fnmp, sU, sp.err);
+        det_add(sp.det, DQ_UY, n, v[1] * fnmp, sU, sp.err);
+        if (DIM == 3) det_add(sp.det, DQ_UZ, n, v[2] * fnmp, sU, sp.err);
+        if (mm) {
+            const double sc[3] = {pow2(det_shift2(nb, bV)), pow2(det_shift2(nb, bD)), sG};
+            det_contact_terms<DIM>(sp.det, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz, sc,
+                                   sp.err);
+        }
+    };
+    if constexpr (SHAPE == SHAPE_LCPDI) {
+        if (mm) visit_nodes<DIM, SHAPE, true, T>(g, 0, p, i, scatter);
+        else visit_nodes<DIM, SHAPE, false, T>(g, 0, p, i, scatter);
+    } else {
+        const int e = p.elem[i];
+        const double xi = p.xi[i], eta = p.eta[i], zeta = DIM == 3 ? p.zeta[i] : 0.;
+        const double lx = p.lpx[i], ly = p.lpy[i], lz = DIM == 3 ? p.lpz[i] : 1.;
+        if (mm) for_each_node<DIM, SHAPE, true, T>(g, 0, e, xi, eta, zeta, lx, ly, lz, scatter);
+        else for_each_node<DIM, SHAPE, false, T>(g, 0, e, xi, eta, zeta, lx, ly, lz, scatter);
     }
 }
 
@@ -1290,6 +1624,58 @@ static __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs
         nd.py[k] = p[1];
         if (DIM == 3) nd.pz[k] = p[2];
         node_velocity<MIX>(nd, k, m, p);
+    }
+}
+
+// Deterministic mode: the node sums of one extrapolation written over the
+// node columns the node kernels read, the limbs cleared for the next one.
+// Phase 0: mass and momentum (and contact terms) after k_p2g; 1: internal
+// forces after k_det_forces; 2: momentum (and contact terms) after k_det_usl.
+// nn counts every field of every node.
+template <int DIM, bool MIX>
+static __global__ void k_det_resolve(StepParams sp, DevNodes nd, int nn, int phase) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nn) return;
+    const DevDet &d = sp.det;
+    auto take = [&](int q, int slot) { return det_take(d, q, n, pow2(-det_shift(d.bnd[slot]))); };
+    const unsigned long long nb = d.nbnd[n];  // the node's largest mass contribution
+    auto take2 = [&](int q, int slot) { return det_take(d, q, n, pow2(-det_shift2(nb, d.bnd[slot]))); };
+    if (phase == 1) {
+        const double fx = take(DQ_FX, DB_FORCE), fy = take(DQ_FY, DB_FORCE);
+        const double fz = DIM == 3 ? take(DQ_FZ, DB_FORCE) : 0.;
+        if (MIX) {
+            nd.gx[n] = (float)fx;
+            nd.gy[n] = (float)fy;
+            if (DIM == 3) nd.gz[n] = (float)fz;
+        } else {
+            nd.fx[n] = fx;
+            nd.fy[n] = fy;
+            if (DIM == 3) nd.fz[n] = fz;
+        }
+        return;
+    }
+    const bool usl = phase == 2;
+    if (usl) {
+        nd.ux[n] = take2(DQ_UX, DB_UMOM);
+        nd.uy[n] = take2(DQ_UY, DB_UMOM);
+        if (DIM == 3) nd.uz[n] = take2(DQ_UZ, DB_UMOM);
+    } else {
+        nd.mass[n] = det_take(d, DQ_MASS, n, pow2(-det_shift(nb)));
+        nd.px[n] = take2(DQ_PX, DB_MOM);
+        nd.py[n] = take2(DQ_PY, DB_MOM);
+        if (DIM == 3) nd.pz[n] = take2(DQ_PZ, DB_MOM);
+    }
+    if (sp.ct.nf > 1) {
+        const int bv = usl ? DB_UVOL : DB_VOL, bd = usl ? DB_UDS : DB_DS, bg = usl ? DB_UGV : DB_GV;
+        nd.vol[n] = take2(DQ_VOL, bv);
+        nd.dsx[n] = take2(DQ_DSX, bd);
+        nd.dsy[n] = take2(DQ_DSY, bd);
+        nd.gvx[n] = take(DQ_GVX, bg);
+        nd.gvy[n] = take(DQ_GVY, bg);
+        if (DIM == 3) {
+            nd.dsz[n] = take2(DQ_DSZ, bd);
+            nd.gvz[n] = take(DQ_GVZ, bg);
+        }
     }
 }
 

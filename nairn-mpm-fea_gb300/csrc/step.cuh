@@ -1,0 +1,110 @@
+// step.cuh -- the kernel sequence of one explicit step of a single-run
+// context, included by step_fp64.cu and step_mixed.cu.
+#pragma once
+
+#include "context.cuh"
+
+namespace nmg {
+namespace {
+
+// One step on the context stream.  DET: deterministic node sums -- each
+// scatter is preceded by a pass that bounds its contributions (k_det_bounds,
+// k_strain_forces and k_g2p in their DET forms) and followed by k_det_resolve,
+// which writes the sums into the node columns.
+template <int DIM, int SHAPE, bool MIX, bool DET>
+void enqueue_step(MpmGpuCtx *c, double t, int slot) {
+    const int n = c->p.n, NN = c->g.nnodes;
+    const int TB = 256;
+    const int pb = (n + TB - 1) / TB, nb = (NN + TB - 1) / TB;
+    const double dt = c->opts.timestep;
+    const int method = c->opts.method;
+    const double stFirst = method == MPMGPU_USAVG ? c->opts.fraction_usf * dt : dt;
+    const double stLast = method == MPMGPU_USAVG ? dt - stFirst : dt;
+    cudaStream_t s = c->stream;
+    auto mark = [&](int k, bool begin) {
+        if (c->profile) cudaEventRecord(event_at(c, slot, k, begin), s);
+        if (!begin) c->launches++;
+    };
+    cudaMemsetAsync(c->nblock, 0, c->nblock_zero_bytes, s);
+    cudaMemsetAsync(c->nd.active, 0, (size_t)NN * c->ct.nf, s);
+    if (MIX) cudaMemsetAsync(c->fblock, 0, c->fblock_zero_bytes, s);
+    StepParams sp;
+    sp.ct = c->ct;
+    sp.g = c->g;
+    sp.dt = dt;
+    sp.st_first = stFirst;
+    sp.st_last = stLast;
+    sp.t = t;
+    sp.err = c->err;
+    sp.runs = nullptr;
+    sp.nrun = nullptr;
+    sp.det = c->det;
+    const int NT = NN * c->ct.nf, ntb = (NT + TB - 1) / TB;
+    mark(0, true);
+    if (DET) {
+        cudaMemsetAsync(c->det.bnd, 0, kDetBounds * sizeof(unsigned long long), s);
+        cudaMemsetAsync(c->det.nbnd, 0, (size_t)NT * sizeof(unsigned long long), s);
+        k_det_bounds<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, c->mats);
+    }
+    k_p2g<DIM, SHAPE, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    if (DET) {
+        k_det_resolve<DIM, MIX><<<ntb, TB, 0, s>>>(sp, c->nd, NT, 0);
+        c->launches += 2;
+    }
+    mark(0, false);
+    mark(1, true);
+    k_node_post<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL);
+    mark(1, false);
+    mark(2, true);
+    if (method == MPMGPU_USL)
+        k_strain_forces<DIM, SHAPE, false, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    else
+        k_strain_forces<DIM, SHAPE, true, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    if (DET) {
+        k_det_forces<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+        k_det_resolve<DIM, MIX><<<ntb, TB, 0, s>>>(sp, c->nd, NT, 1);
+        c->launches += 2;
+    }
+    mark(2, false);
+    mark(3, true);
+    k_node_update<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group,
+                                                     c->ct.nf > 1 && method != MPMGPU_USF);
+    mark(3, false);
+    mark(4, true);
+    if (method == MPMGPU_USF) {
+        k_g2p<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+        mark(4, false);
+        return;
+    }
+    k_g2p<DIM, SHAPE, true, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    if (DET) {
+        k_det_usl<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+        k_det_resolve<DIM, MIX><<<ntb, TB, 0, s>>>(sp, c->nd, NT, 2);
+        c->launches += 2;
+    }
+    mark(4, false);
+    mark(5, true);
+    k_node_usl<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
+    mark(5, false);
+    mark(6, true);
+    k_strain_last<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    mark(6, false);
+}
+
+template <bool MIX, bool DET>
+void enqueue_prec(MpmGpuCtx *c, double t, int slot) {
+    const bool d3 = c->dim == 3;
+    const int shape = c->opts.shape;
+    if (d3) {
+        if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<3, SHAPE_LINEAR, MIX, DET>(c, t, slot);
+        else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<3, SHAPE_LCPDI, MIX, DET>(c, t, slot);
+        else enqueue_step<3, SHAPE_UGIMP, MIX, DET>(c, t, slot);
+    } else {
+        if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<2, SHAPE_LINEAR, MIX, DET>(c, t, slot);
+        else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<2, SHAPE_LCPDI, MIX, DET>(c, t, slot);
+        else enqueue_step<2, SHAPE_UGIMP, MIX, DET>(c, t, slot);
+    }
+}
+
+}  // namespace
+}  // namespace nmg

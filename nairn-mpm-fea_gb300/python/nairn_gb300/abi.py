@@ -16,7 +16,7 @@ c_int32_p = C.POINTER(C.c_int32)
 
 MPMGPU_OK = 0
 STATUS_NAMES = {0: "OK", 1: "INVALID", 2: "UNSUPPORTED", 3: "CUDA", 4: "OOM", 5: "NAN",
-                6: "LEFT_GRID", 7: "CPDI_NODES", 8: "TIMEOUT", 9: "BUSY"}
+                6: "LEFT_GRID", 7: "CPDI_NODES", 8: "TIMEOUT", 9: "BUSY", 10: "RANGE"}
 
 
 class MpmGpuGrid(C.Structure):
