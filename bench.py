@@ -54,7 +54,8 @@ def parse():
     ap.add_argument("--radius", type=float, default=5.0)
     ap.add_argument("--length", type=float, default=25.0)
     ap.add_argument("--cell", type=float, default=0.25)
-    ap.add_argument("--sort-interval", type=int, default=1)
+    ap.add_argument("--sort-interval", type=int, default=0,
+                    help="cell-sort interval of the single-run measurements (0: autotuned over 1, 2, 4, 8)")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
@@ -303,9 +304,13 @@ def timed_run(args, m, dist, precision: int, local: int):
     stream (per-kernel event pairs in the same region).  Returns the run
     (still open), its timings and the state after W+K steps."""
     from nairn_gb300 import gpu
-    run = gpu.GpuRun(m, sort_interval=args.sort_interval, precision=precision)
+    run = gpu.GpuRun(m, sort_interval=max(1, args.sort_interval), precision=precision)
     run.upload(m.particles)
     run.step(args.warmup)
+    si, tuned = args.sort_interval, 0
+    if si <= 0:
+        si, _ = run.autotune_sort(16)  # 64 real steps
+        tuned = 64
     run.set_profiling(True)
     launches0 = run.launch_count()
     clocks = ClockSampler(local)
@@ -318,7 +323,8 @@ def timed_run(args, m, dist, precision: int, local: int):
     prof = run.profile()
     run.set_profiling(False)
     final = run.download(m.particles)
-    return run, {"ms": ms, "prof": prof, "launches": launches, "clocks": clk}, final
+    return run, {"ms": ms, "prof": prof, "launches": launches, "clocks": clk, "sort_interval": si,
+                 "tuning_steps": tuned}, final
 
 
 def state_error(a: dict, b: dict, dim: int) -> dict:
@@ -490,9 +496,12 @@ def config3_measurement(args, dist, local):
     k = args.config3_steps
     out, finals = {}, {}
     for prec in (0, 1):
-        r = gpu.GpuRun(m, precision=prec, sort_interval=args.sort_interval)
+        r = gpu.GpuRun(m, precision=prec, sort_interval=max(1, args.sort_interval))
         r.upload(m.particles)
         r.step(3)
+        si = args.sort_interval
+        if si <= 0:
+            si, _ = r.autotune_sort(8)  # 32 real steps
         l0 = r.launch_count()
         clocks = ClockSampler(local)
         clocks.start()
@@ -501,7 +510,7 @@ def config3_measurement(args, dist, local):
         dist.barrier()
         clk = clocks.stop()
         out[prec] = {"value": dist.sum(float(m.n)) * k / (dist.max(ms) / 1e3), "ms_per_step": ms / k,
-                     "gpu_launches": r.launch_count() - l0, "clocks": clk}
+                     "gpu_launches": r.launch_count() - l0, "clocks": clk, "sort_interval": si}
         finals[prec] = r.download(m.particles)
         r.close()
     err = state_error(finals[1], finals[0], 3)
@@ -510,10 +519,13 @@ def config3_measurement(args, dist, local):
             "config": {"workload": "3D multimaterial contact: Neo-Hookean block pressed and sliding on an elastic "
                                    "plate, Coulomb friction 0.3, lCPDI, 0.5 mm cells, 2x2x2 particles/cell, USAVG",
                        "particles": m.n, "grid_nodes": m.grid.nnodes, "material_fields": 2,
+                       "sort_interval": out[1]["sort_interval"],
                        "l2": "particle state %.2f GB vs 129 MB L2: no flush needed" % (m.n * 42 * 8 / 1e9)},
-            "plain_fp64": {"value": out[0]["value"], "ms_per_step": out[0]["ms_per_step"]},
+            "plain_fp64": {"value": out[0]["value"], "ms_per_step": out[0]["ms_per_step"],
+                           "sort_interval": out[0]["sort_interval"]},
             "speedup_vs_plain_fp64": out[1]["value"] / out[0]["value"],
-            "error_vs_fp64_path": dict(err, steps=3 + k, target="<= 1e-5 relative L2")}
+            "error_vs_fp64_path": dict(err, steps=3 + (32 if args.sort_interval <= 0 else 0) + k,
+                                       target="<= 1e-5 relative L2")}
 
 
 def contact_batched_measurement(args, dist, local):
@@ -625,7 +637,7 @@ def main():
     # roofline of the dominant kernel (largest share of the timed region)
     fams = {k: v for k, v in prof.items() if v > 0}
     dom = max(fams, key=fams.get)
-    launches_dom = args.steps if dom != "sort" else max(1, args.steps // max(1, args.sort_interval))
+    launches_dom = args.steps if dom != "sort" else max(1, args.steps // head["sort_interval"])
     avg_ms = fams[dom] / launches_dom
     nodes = active_nodes(m)
     bytes_model = algorithmic_bytes(m, nodes)
@@ -644,11 +656,13 @@ def main():
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
-            "config": workload_config(args, m, {"sort_interval": args.sort_interval,
+            "config": workload_config(args, m, {"sort_interval": head["sort_interval"],
+                                                "sort_interval_autotuned": args.sort_interval <= 0,
                                                 "active_nodes_t0": nodes, "precision": args.precision}),
             "plain_fp64": {"value": plain_value, "ms_per_step": dist.max(plain["ms"]) / args.steps,
+                           "sort_interval": plain["sort_interval"],
                            "kernels_ms_per_step": {k: v / args.steps for k, v in plain["prof"].items() if v > 0}},
-            "error_vs_fp64_path": dict(err, steps=args.warmup + args.steps,
+            "error_vs_fp64_path": dict(err, steps=args.warmup + head["tuning_steps"] + args.steps,
                                        note="relative L2 of the headline run against the all-FP64 GPU path, "
                                             "which matches the reference within 1e-10"),
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d * ws,

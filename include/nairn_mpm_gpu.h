@@ -245,6 +245,15 @@ int mpmgpu_step_timed(MpmGpuCtx *ctx, int32_t nsteps, double t0, double *ms);
 /* Per-kernel event timing for later mpmgpu_step calls (read with mpmgpu_profile). */
 int mpmgpu_set_profiling(MpmGpuCtx *ctx, int32_t on);
 
+/* Pick the cell-sort interval of this context by timing: about trial_steps
+ * real steps (from time t0, as mpmgpu_step; whole chunks of 8, the candidates
+ * taking turns) at each interval 1, 2, 4 and 8; the fastest is kept.  Results
+ * do not depend on the interval beyond the order of atomic sums.
+ * *steps_taken (a multiple of 32) is how far the simulation advanced;
+ * *best_interval and *ms_per_step describe the choice. */
+int mpmgpu_autotune_sort(MpmGpuCtx *ctx, int32_t trial_steps, double t0, int32_t *best_interval,
+                         double *ms_per_step, int32_t *steps_taken);
+
 /* The context's cudaStream_t, as an opaque pointer. */
 void *mpmgpu_stream(MpmGpuCtx *ctx);
 

@@ -641,6 +641,45 @@ extern "C" {
 
 int mpmgpu_step(MpmGpuCtx *c, int32_t nsteps, double t0) { return step_impl(c, nsteps, t0, nullptr); }
 
+// Extension: the sort interval with the shortest step, by timing trial steps
+// at each candidate (the steps are real; the caller's clock advances).  The
+// candidates take turns in chunks of 8 steps, each chunk starting with a sort,
+// in alternating order, so that a step cost that drifts as the run evolves
+// (plastic zones growing) favours none of them.
+int mpmgpu_autotune_sort(MpmGpuCtx *c, int32_t trial_steps, double t0, int32_t *best_interval,
+                         double *ms_per_step, int32_t *steps_taken) {
+    if (!c || trial_steps < 1 || !best_interval || !ms_per_step || !steps_taken)
+        return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_autotune_sort: bad argument");
+    const int cand[4] = {1, 2, 4, 8};
+    const int chunk = 8, rounds = trial_steps > chunk ? trial_steps / chunk : 1;
+    const int keep = c->opts.sort_interval;
+    double total[4] = {0., 0., 0., 0.};
+    double t = t0;
+    *steps_taken = 0;
+    for (int r = 0; r < rounds; r++)
+        for (int j = 0; j < 4; j++) {
+            const int k = (r & 1) ? 3 - j : j;
+            c->opts.sort_interval = cand[k];
+            c->steps_done = 0;  // the chunk starts with a sort
+            double ms = 0.;
+            const int st = step_impl(c, chunk, t, &ms);
+            *steps_taken += chunk;
+            t += chunk * c->opts.timestep;
+            if (st != MPMGPU_OK) {
+                c->opts.sort_interval = keep;
+                return st;
+            }
+            total[k] += ms;
+        }
+    int best = 0;
+    for (int k = 1; k < 4; k++)
+        if (total[k] < total[best]) best = k;
+    c->opts.sort_interval = cand[best];
+    *best_interval = cand[best];
+    *ms_per_step = total[best] / (rounds * chunk);
+    return MPMGPU_OK;
+}
+
 // Extension: mpmgpu_step that also returns the device time of the enqueued
 // steps in *ms (CUDA events recorded on the context stream).
 int mpmgpu_step_timed(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {

@@ -52,6 +52,9 @@ def lib():
     L.mpmgpu_stream.argtypes = [C.c_void_p]
     L.mpmgpu_stream.restype = C.c_void_p
     L.mpmgpu_step_timed.argtypes = [C.c_void_p, C.c_int32, C.c_double, P(C.c_double)]
+    L.mpmgpu_autotune_sort.argtypes = [C.c_void_p, C.c_int32, C.c_double, P(C.c_int32), P(C.c_double),
+                                       P(C.c_int32)]
+    L.mpmgpu_autotune_sort.restype = C.c_int
     L.mpmgpu_step_timed.restype = C.c_int
     L.mpmgpu_launch_count.argtypes = [C.c_void_p]
     L.mpmgpu_launch_count.restype = C.c_longlong
@@ -105,7 +108,7 @@ def lib():
 
 
 # every symbol the header declares (checked by the CPU tests)
-EXPORTED = ("mpmgpu_step_timed", "mpmgpu_set_profiling", "mpmgpu_stream", "mpmgpu_launch_count",
+EXPORTED = ("mpmgpu_step_timed", "mpmgpu_autotune_sort", "mpmgpu_set_profiling", "mpmgpu_stream", "mpmgpu_launch_count",
             "mpmgpu_host_register", "mpmgpu_host_unregister", "mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
             "mpmgpu_set_velocity_bcs", "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles",
             "mpmgpu_last_error", "mpmgpu_destroy", "mpmgpu_profile")
@@ -152,6 +155,16 @@ class GpuRun:
         self._check(lib().mpmgpu_step_timed(self.h, int(nsteps), float(self.t), C.byref(ms)))
         self.t += nsteps * self.model.options["timestep"]
         return ms.value
+
+    def autotune_sort(self, trial_steps: int = 16):
+        """Keep the fastest cell-sort interval of 1, 2, 4, 8 (about 4 x
+        trial_steps real steps are taken); returns (interval, ms per step)."""
+        si, ms, taken = C.c_int32(), C.c_double(), C.c_int32()
+        st = lib().mpmgpu_autotune_sort(self.h, int(trial_steps), float(self.t), C.byref(si), C.byref(ms),
+                                        C.byref(taken))
+        self.t += taken.value * self.model.options["timestep"]
+        self._check(st)
+        return si.value, ms.value
 
     def launch_count(self) -> int:
         return int(lib().mpmgpu_launch_count(self.h))

@@ -155,3 +155,24 @@ def test_cpdi_node_limit_is_reported(gpu_lib):
     with pytest.raises(GpuError, match="CPDI_NODES"):
         r.step(1)
     r.close()
+
+
+def test_sort_autotune_keeps_results(gpu_lib):
+    """The single-run sort autotuner takes real steps (a multiple of 32) and
+    leaves the results those of the oracle over the same step count."""
+    import oracle_lib
+    from nairn_gb300 import model, abi
+    from nairn_gb300.gpu import GpuRun
+    m = model.taylor_3d(radius=1.5, length=3.0, cell=0.5, steps=40)
+    r = GpuRun(m, precision=0)
+    r.upload(m.particles)
+    r.step(4)
+    si, ms = r.autotune_sort(16)
+    assert si in (1, 2, 4, 8) and ms > 0.
+    r.step(4)
+    out = r.download(m.particles)
+    r.close()
+    ref = abi.copy_particles(m.particles)
+    oracle_lib.run(m, ref, 4 + 64 + 4)
+    for k in ("x", "y", "z", "vx", "vz", "szz", "sxy", "hist0"):
+        assert rel_l2(out[k], ref[k]) <= TOL, k
