@@ -257,6 +257,20 @@ __device__ __forceinline__ int find_cell(double x, double xmin, double gx, doubl
     return c;
 }
 
+// Corner data of the step: the FP64 path keeps natural coordinates and
+// gradient weights as doubles; the mixed mode keeps them as floats in the same
+// scratch (index k = (3 c + a) n + i either way).
+template <typename T>
+__device__ __forceinline__ T cpdi_xi(const DevParticles &p, size_t k) {
+    if constexpr (std::is_same<T, float>::value) return reinterpret_cast<const float *>(p.cxi)[k];
+    else return p.cxi[k];
+}
+template <typename T>
+__device__ __forceinline__ T cpdi_wg(const DevParticles &p, size_t k) {
+    if constexpr (std::is_same<T, float>::value) return reinterpret_cast<const float *>(p.cwg)[k];
+    else return p.cwg[k];
+}
+
 // MatPoint2D/3D::GetCPDINodesAndWeights (MatPoint2D.cpp:519-571,
 // MatPoint3D.cpp:538-601): semi-side vectors r = F * (cell * lp / 2) of the
 // particle (GetSemiSideVectors, GetParticleSize), corners x +- r1 +- r2 (+- r3)
@@ -397,6 +411,132 @@ static __device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i
     return true;
 }
 
+// cpdi_setup in the mixed mode: the same corners, elements, natural
+// coordinates and gradient weights formed in FP32 from the particle position
+// relative to its own cell origin (one FP64 difference per axis), the corner's
+// cell found as the particle's cell plus a floored offset; results stored as
+// floats.  A corner within float rounding of a cell face may land in the
+// neighbouring cell; the linear shape functions of the two cells agree on the
+// face, so the weights change by rounding only.
+template <int DIM>
+static __device__ bool cpdi_setup_f32(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
+    constexpr int NC = DIM == 3 ? 8 : 4;
+    const size_t n = (size_t)p.n;
+    float *cxf = reinterpret_cast<float *>(p.cxi), *cwf = reinterpret_cast<float *>(p.cwg);
+    int col, row, zr;
+    elem_coords(g, p.elem[i], col, row, zr);
+    const float dx = (float)g.gx, dy = (float)g.gy, dz = DIM == 3 ? (float)g.gz : 1.f;
+    const float idx = (float)g.igx, idy = (float)g.igy, idz = DIM == 3 ? (float)g.igz : 0.f;
+    const float rel[3] = {(float)(p.x[i] - g.xn[col]), (float)(p.y[i] - g.yn[row]),
+                          DIM == 3 ? (float)(p.z[i] - g.zn[zr]) : 0.f};
+    const float pszx = 0.5f * dx * (float)p.lpx[i], pszy = 0.5f * dy * (float)p.lpy[i];
+    const float F00 = 1.f + (float)p.exx[i], F11 = 1.f + (float)p.eyy[i];
+    const float exy = (float)p.exy[i], wxy = (float)p.wxy[i];
+    const float F01 = 0.5f * (exy - wxy), F10 = 0.5f * (exy + wxy);
+    float r1[3] = {F00 * pszx, F10 * pszx, 0.f}, r2[3] = {F01 * pszy, F11 * pszy, 0.f}, r3[3] = {0.f, 0.f, 0.f};
+    if (DIM == 3) {
+        const float pszz = 0.5f * dz * (float)p.lpz[i];
+        const float exz = (float)p.exz[i], wxz = (float)p.wxz[i], eyz = (float)p.eyz[i], wyz = (float)p.wyz[i];
+        r1[2] = 0.5f * (exz + wxz) * pszx;
+        r2[2] = 0.5f * (eyz + wyz) * pszy;
+        r3[0] = 0.5f * (exz - wxz) * pszz;
+        r3[1] = 0.5f * (eyz - wyz) * pszz;
+        r3[2] = (1.f + (float)p.ezz[i]) * pszz;
+    }
+    const int base[3] = {col, row, zr}, ncell[3] = {g.nx, g.ny, g.nz};
+    const float ics[3] = {idx, idy, idz};
+    int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
+    float xiv[NC][3];
+    int cel[NC][3];
+#pragma unroll
+    for (int c = 0; c < NC; c++) {
+        const float s1 = (c == 1 || c == 2 || c == 5 || c == 6) ? 1.f : -1.f;
+        const float s2 = (c == 2 || c == 3 || c == 6 || c == 7) ? 1.f : -1.f;
+        const float s3 = c >= 4 ? 1.f : -1.f;
+        int ce[3] = {0, 0, 0};
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            float cp = rel[a] + s1 * r1[a] + s2 * r2[a];
+            if (DIM == 3) cp += s3 * r3[a];
+            const float q = cp * ics[a];
+            const int o = __float2int_rd(q);
+            ce[a] = base[a] + o;
+            if (ce[a] < 0 || ce[a] >= ncell[a]) {
+                atomicOr(err, ERR_LEFT_GRID);
+                return false;
+            }
+            // 2 (cp - (o + 1/2) cell) / cell
+            xiv[c][a] = 2.f * (q - (float)o) - 1.f;
+            cel[c][a] = ce[a];
+            lo[a] = min(lo[a], ce[a]);
+            hi[a] = max(hi[a], ce[a]);
+            cxf[(3 * c + a) * n + i] = xiv[c][a];
+        }
+        p.ce[c * n + i] = DIM == 3 ? g.nx * (ce[2] * g.ny + ce[1]) + ce[0] : ce[1] * g.nx + ce[0];
+    }
+    if (DIM == 2) {
+        const float Ap = 1.f / (4.f * (r1[0] * r2[1] - r1[1] * r2[0]));
+        const float wx[4] = {r1[1] - r2[1], r1[1] + r2[1], -r1[1] + r2[1], -r1[1] - r2[1]};
+        const float wy[4] = {-r1[0] + r2[0], -r1[0] - r2[0], r1[0] - r2[0], r1[0] + r2[0]};
+#pragma unroll
+        for (int c = 0; c < 4; c++) {
+            cwf[(3 * c + 0) * n + i] = wx[c] * Ap;
+            cwf[(3 * c + 1) * n + i] = wy[c] * Ap;
+        }
+    } else {
+        const float a12[3] = {r1[1] * r2[2] - r1[2] * r2[1], r1[2] * r2[0] - r1[0] * r2[2], r1[0] * r2[1] - r1[1] * r2[0]};
+        const float a13[3] = {r1[1] * r3[2] - r1[2] * r3[1], r1[2] * r3[0] - r1[0] * r3[2], r1[0] * r3[1] - r1[1] * r3[0]};
+        const float a23[3] = {r2[1] * r3[2] - r2[2] * r3[1], r2[2] * r3[0] - r2[0] * r3[2], r2[0] * r3[1] - r2[1] * r3[0]};
+        const float Vp = 1.f / (8.f * (r1[0] * a23[0] + r1[1] * a23[1] + r1[2] * a23[2]));
+#pragma unroll
+        for (int c = 0; c < 8; c++) {
+            const float s1 = (c == 1 || c == 2 || c == 5 || c == 6) ? 1.f : -1.f;
+            const float s2 = (c == 2 || c == 3 || c == 6 || c == 7) ? 1.f : -1.f;
+            const float s3 = c >= 4 ? 1.f : -1.f;
+#pragma unroll
+            for (int a = 0; a < 3; a++) cwf[(3 * c + a) * n + i] = (s1 * a23[a] - s2 * a13[a] + s3 * a12[a]) * Vp;
+        }
+    }
+    bool small = true;
+#pragma unroll
+    for (int a = 0; a < DIM; a++) small = small && hi[a] - lo[a] <= 1;
+    if (DIM == 3 && !small) {
+        // the node count check of cpdi_setup on the float corner data
+        const int wx = hi[0] - lo[0] + 2, wy = hi[1] - lo[1] + 2, wz = hi[2] - lo[2] + 2;
+        if ((long long)wx * wy * wz > 512) {
+            atomicOr(err, ERR_CPDI_NODES);
+            return false;
+        }
+        unsigned mask[16] = {0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u, 0u};
+        for (int c = 0; c < NC; c++)
+            for (int k = 0; k < 8; k++) {
+                const int ddx = (k == 1 || k == 2 || k == 5 || k == 6) ? 1 : 0;
+                const int ddy = (k == 2 || k == 3 || k == 6 || k == 7) ? 1 : 0;
+                const int ddz = k >= 4 ? 1 : 0;
+                const float t1 = 1.f + (ddx ? 1.f : -1.f) * xiv[c][0], t2 = 1.f + (ddy ? 1.f : -1.f) * xiv[c][1];
+                const float cfn = 0.125f * t1 * t2 * (1.f + (ddz ? 1.f : -1.f) * xiv[c][2]);
+                if (cfn < 1e-15f) continue;
+                const int bit = ((cel[c][2] + ddz - lo[2]) * wy + (cel[c][1] + ddy - lo[1])) * wx + (cel[c][0] + ddx - lo[0]);
+                mask[bit >> 5] |= 1u << (bit & 31);
+            }
+        int count = 0;
+#pragma unroll
+        for (int w = 0; w < 16; w++) count += __popc(mask[w]);
+        if (count > 49) {
+            atomicOr(err, ERR_CPDI_NODES);
+            return false;
+        }
+    }
+    return true;
+}
+
+// the corner setup of the step in the transfer arithmetic of the mode
+template <int DIM, bool MIX>
+__device__ __forceinline__ bool cpdi_setup_for(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
+    if constexpr (MIX) return cpdi_setup_f32<DIM>(g, p, i, err);
+    else return cpdi_setup<DIM>(g, p, i, err);
+}
+
 // GetCPDIFunctions (MoreMPMElementBase.cpp:581-656) without the node merge:
 // f is called for every (corner, element node) pair with weight ws * N and
 // gradient wg * N (N the corner element's linear shape function, pairs with
@@ -411,13 +551,13 @@ __device__ __forceinline__ void cpdi_nodes(const DevGrid &g, int nb, const DevPa
         int col, row, zr;
         elem_coords(g, p.ce[c * n + i], col, row, zr);
         const int n0 = nb + zr * g.zplane + row * g.yplane + col;
-        const T xi = (T)p.cxi[(3 * c) * n + i], eta = (T)p.cxi[(3 * c + 1) * n + i];
-        const T zeta = DIM == 3 ? (T)p.cxi[(3 * c + 2) * n + i] : T(0);
+        const T xi = cpdi_xi<T>(p, (3 * c) * n + i), eta = cpdi_xi<T>(p, (3 * c + 1) * n + i);
+        const T zeta = DIM == 3 ? cpdi_xi<T>(p, (3 * c + 2) * n + i) : T(0);
         T gx = 0, gy = 0, gz = 0;
         if (GRAD) {
-            gx = (T)p.cwg[(3 * c) * n + i];
-            gy = (T)p.cwg[(3 * c + 1) * n + i];
-            if (DIM == 3) gz = (T)p.cwg[(3 * c + 2) * n + i];
+            gx = cpdi_wg<T>(p, (3 * c) * n + i);
+            gy = cpdi_wg<T>(p, (3 * c + 1) * n + i);
+            if (DIM == 3) gz = cpdi_wg<T>(p, (3 * c + 2) * n + i);
         }
 #pragma unroll
         for (int k = 0; k < (DIM == 3 ? 8 : 4); k++) {
@@ -473,7 +613,7 @@ __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevP
         float wt[3][3];
 #pragma unroll
         for (int a = 0; a < DIM; a++) {
-            const float xi = (float)p.cxi[(3 * c + a) * n + i];
+            const float xi = cpdi_xi<float>(p, (3 * c + a) * n + i);
             const int o = cell[c][a] - lo[a];
             const float w0 = 0.5f * (1.f - xi), w1 = 0.5f * (1.f + xi);
             wt[a][0] = o == 0 ? w0 : 0.f;
@@ -482,9 +622,9 @@ __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevP
         }
         float gxc = 0.f, gyc = 0.f, gzc = 0.f;
         if (GRAD) {
-            gxc = (float)p.cwg[(3 * c) * n + i];
-            gyc = (float)p.cwg[(3 * c + 1) * n + i];
-            if (DIM == 3) gzc = (float)p.cwg[(3 * c + 2) * n + i];
+            gxc = cpdi_wg<float>(p, (3 * c) * n + i);
+            gyc = cpdi_wg<float>(p, (3 * c + 1) * n + i);
+            if (DIM == 3) gzc = cpdi_wg<float>(p, (3 * c + 2) * n + i);
         }
         // the corner element's linear shape function is the product of the
         // factors 0.5 (1 +- xi): 0.25 (1+-xi)(1+-eta) in 2D, 0.125 (...) in 3D
@@ -638,16 +778,17 @@ __device__ __forceinline__ void det_contact_terms(const DevDet &dd, int k, doubl
 // changes by at most the particle width over the cell size across the particle
 // width); for lCPDI the sum over corners of the largest gradient weight, as
 // each node gradient is sum_c wg_c N_c(node) with 0 <= N_c <= 1.
-template <int DIM, int SHAPE>
+template <int DIM, int SHAPE, bool MIX>
 __device__ __forceinline__ double grad_bound(const DevGrid &g, const DevParticles &p, int i) {
     if constexpr (SHAPE == SHAPE_LCPDI) {
+        using T = typename Wt<MIX>::T;
         constexpr int NC = DIM == 3 ? 8 : 4;
         const size_t n = (size_t)p.n;
         double s = 0.;
 #pragma unroll
         for (int c = 0; c < NC; c++) {
-            double w = fmax(fabs(p.cwg[(3 * c) * n + i]), fabs(p.cwg[(3 * c + 1) * n + i]));
-            if (DIM == 3) w = fmax(w, fabs(p.cwg[(3 * c + 2) * n + i]));
+            double w = fmax(fabs((double)cpdi_wg<T>(p, (3 * c) * n + i)), fabs((double)cpdi_wg<T>(p, (3 * c + 1) * n + i)));
+            if (DIM == 3) w = fmax(w, fabs((double)cpdi_wg<T>(p, (3 * c + 2) * n + i)));
             s += w;
         }
         return 2. * s;
@@ -677,7 +818,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
     if (i >= p.n) return;
     const DevGrid &g = sp.g;
     bool ok = true;
-    if constexpr (SHAPE == SHAPE_LCPDI) ok = cpdi_setup<DIM>(g, p, i, sp.err);
+    if constexpr (SHAPE == SHAPE_LCPDI) ok = cpdi_setup_for<DIM, MIX>(g, p, i, sp.err);
     const double mp = p.mass[i];
     const int off = sp.ct.nf > 1 ? sp.ct.fstride * mats[p.mat[i]].field : 0;
     const bool mm = sp.ct.nf > 1;
@@ -707,7 +848,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
         const double xp[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
         det_bound(sp.det, DB_VOL, Vp / mp);
         det_bound(sp.det, DB_DS, displacement_bound<DIM>(p, i, xp));
-        det_bound(sp.det, DB_GV, Vp * grad_bound<DIM, SHAPE>(g, p, i));
+        det_bound(sp.det, DB_GV, Vp * grad_bound<DIM, SHAPE, MIX>(g, p, i));
     }
 }
 
@@ -779,7 +920,7 @@ static __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles 
     if constexpr (SHAPE == SHAPE_LCPDI) {
         // ElementBase::GetShapeFunctionData: the particle's CPDI corners for
         // this step (set by k_det_bounds in the deterministic mode)
-        if (!DET && !cpdi_setup<DIM>(g, p, i, rv.err)) return;
+        if (!DET && !cpdi_setup_for<DIM, MIX>(g, p, i, rv.err)) return;
         if (mm) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
         else visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, scatter);
     } else {
@@ -924,7 +1065,7 @@ static __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, Dev
             const double zz = fabs(p.szz[i] - P), xz = fabs(p.sxz[i]), yz = fabs(p.syz[i]);
             r = fmax(fmax(a + c + xz, c + b + yz), xz + yz + zz);
         }
-        det_bound(sp.det, DB_FORCE, mp * r * grad_bound<DIM, SHAPE>(g, p, i));
+        det_bound(sp.det, DB_FORCE, mp * r * grad_bound<DIM, SHAPE, MIX>(g, p, i));
         return;
     }
     forces_scatter<DIM, SHAPE, MIX, false>(sp, p, nd, i, g, rv.nb, off);
@@ -1076,7 +1217,7 @@ static __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles 
             const double Vp = fabs(contact_volume<DIM>(p, i, mats[p.mat[i]].rho));
             det_bound(sp.det, DB_UVOL, Vp / mp);
             det_bound(sp.det, DB_UDS, displacement_bound<DIM>(p, i, xp));
-            det_bound(sp.det, DB_UGV, Vp * grad_bound<DIM, SHAPE>(g, p, i));
+            det_bound(sp.det, DB_UGV, Vp * grad_bound<DIM, SHAPE, MIX>(g, p, i));
         }
     } else if (USL) {
         // second extrapolation (NodalPoint::AddMassMomentumLast), with the
