@@ -145,9 +145,12 @@ __global__ void k_clear_nodes(DevNodes nd, int nn, int nf, int fstride) {
         nd.active[k] = 0;
         if (MIX) nd.gx[k] = nd.gy[k] = nd.gz[k] = 0.f;
         if (nf > 1) {
-            nd.vol[k] = 0.;
+            // the volume and volume-gradient terms are floats in the mixed mode
+            cterm_set<MIX>(nd.vol, k, 0.);
             nd.dsx[k] = nd.dsy[k] = nd.dsz[k] = 0.;
-            nd.gvx[k] = nd.gvy[k] = nd.gvz[k] = 0.;
+            cterm_set<MIX>(nd.gvx, k, 0.);
+            cterm_set<MIX>(nd.gvy, k, 0.);
+            cterm_set<MIX>(nd.gvz, k, 0.);
         }
     }
 }

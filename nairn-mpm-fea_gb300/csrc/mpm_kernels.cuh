@@ -740,21 +740,42 @@ __device__ __forceinline__ double contact_volume(const DevParticles &p, int i, d
     return J * p.mass[i] / rho;
 }
 
+// Contact volume and volume-gradient node terms (vol, gvx, gvy, gvz): FP64
+// columns in the FP64 path; in the mixed mode FP32 values, k-th float of the
+// same columns -- they only set the contact normal and which material is
+// larger.  The mass-weighted displacement, which decides separation, stays FP64.
+template <bool MIX>
+__device__ __forceinline__ double cterm(const double *col, int k) {
+    if constexpr (MIX) return (double)reinterpret_cast<const float *>(col)[k];
+    else return col[k];
+}
+template <bool MIX>
+__device__ __forceinline__ void cterm_set(double *col, int k, double v) {
+    if constexpr (MIX) reinterpret_cast<float *>(col)[k] = (float)v;
+    else col[k] = v;
+}
+
 // multimaterial contact terms of one particle at node k: volume, mass-weighted
 // displacement and volume gradient (CrackVelocityField::AddVolumeDisplacement,
-// CrackVelocityFieldMulti::AddVolumeGradient)
-template <int DIM>
-__device__ __forceinline__ void add_contact_terms(const DevNodes &nd, int k, double N, double fnmp, double Vp,
-                                                  const double d[3], double gx, double gy, double gz) {
-    atomicAdd(&nd.vol[k], N * Vp);
+// CrackVelocityFieldMulti::AddVolumeGradient); T the weight arithmetic
+template <int DIM, bool MIX, typename T>
+__device__ __forceinline__ void add_contact_terms(const DevNodes &nd, int k, T N, double fnmp, double Vp,
+                                                  const double d[3], T gx, T gy, T gz) {
+    if constexpr (MIX) {
+        const float V = (float)Vp;
+        atomicAdd(reinterpret_cast<float *>(nd.vol) + k, (float)N * V);
+        atomicAdd(reinterpret_cast<float *>(nd.gvx) + k, (float)gx * V);
+        atomicAdd(reinterpret_cast<float *>(nd.gvy) + k, (float)gy * V);
+        if (DIM == 3) atomicAdd(reinterpret_cast<float *>(nd.gvz) + k, (float)gz * V);
+    } else {
+        atomicAdd(&nd.vol[k], (double)N * Vp);
+        atomicAdd(&nd.gvx[k], (double)gx * Vp);
+        atomicAdd(&nd.gvy[k], (double)gy * Vp);
+        if (DIM == 3) atomicAdd(&nd.gvz[k], (double)gz * Vp);
+    }
     atomicAdd(&nd.dsx[k], d[0] * fnmp);
     atomicAdd(&nd.dsy[k], d[1] * fnmp);
-    atomicAdd(&nd.gvx[k], gx * Vp);
-    atomicAdd(&nd.gvy[k], gy * Vp);
-    if (DIM == 3) {
-        atomicAdd(&nd.dsz[k], d[2] * fnmp);
-        atomicAdd(&nd.gvz[k], gz * Vp);
-    }
+    if (DIM == 3) atomicAdd(&nd.dsz[k], d[2] * fnmp);
 }
 
 // the same terms as deterministic node sums (scales: volume, displacement, gradient)
@@ -915,7 +936,7 @@ static __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles 
         atomicAdd(&nd.py[n], vy * fnmp);
         if (DIM == 3) atomicAdd(&nd.pz[n], vz * fnmp);
         nd.active[n] = 1;
-        if (mm) add_contact_terms<DIM>(nd, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz);
+        if (mm) add_contact_terms<DIM, MIX>(nd, n, N, fnmp, Vp, d, gx, gy, gz);
     };
     if constexpr (SHAPE == SHAPE_LCPDI) {
         // ElementBase::GetShapeFunctionData: the particle's CPDI corners for
@@ -1237,7 +1258,7 @@ static __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles 
             atomicAdd(&nd.ux[n], v[0] * fnmp);
             atomicAdd(&nd.uy[n], v[1] * fnmp);
             if (DIM == 3) atomicAdd(&nd.uz[n], v[2] * fnmp);
-            if (rv.mm) add_contact_terms<DIM>(nd, n, (double)N, fnmp, Vp, d, (double)gx, (double)gy, (double)gz);
+            if (rv.mm) add_contact_terms<DIM, MIX>(nd, n, N, fnmp, Vp, d, gx, gy, gz);
         };
         if (rv.mm) {
             if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
@@ -1489,7 +1510,8 @@ __device__ __forceinline__ bool coulomb_delta(const DevContact &ct, double delPi
 // (GetNormalVector :960-1069, methods 0-2), separation from the extrapolated
 // displacements (CrackSurfaceContact::MaterialSeparation), Coulomb friction.
 constexpr int kMaxFields = 8;
-static __device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, int pass, double dt) {
+template <bool MIX>
+__device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, int pass, double dt) {
     const int S = ct.fstride;
     int act[kMaxFields], nm = 0;
     double Pc[3] = {0., 0., 0.}, Mc = 0., dispc[3] = {0., 0., 0.}, voltot = 0.;
@@ -1503,7 +1525,7 @@ static __device__ void node_contact(const DevContact &ct, const DevNodes &nd, in
         dispc[0] += nd.dsx[k];
         dispc[1] += nd.dsy[k];
         dispc[2] += nd.dsz[k];
-        voltot += nd.vol[k];
+        voltot += cterm<MIX>(nd.vol, k);
         act[nm++] = f;
     }
     if (nm <= 1) return;
@@ -1514,27 +1536,28 @@ static __device__ void node_contact(const DevContact &ct, const DevNodes &nd, in
     for (int a = 0; a < 3; a++) dispc[a] *= rMc;
     for (int mi = 0; mi < miMax; mi++) {
         const int ki = act[mi] * S + n;
-        const double massi = nd.mass[ki], voli = nd.vol[ki];
+        const double massi = nd.mass[ki], voli = cterm<MIX>(nd.vol, ki);
         const double volj = voltot - voli;
         int j = -1;
         double gradj[3] = {0., 0., 0.}, maxOther = 0.;
         for (int kj = 0; kj < nm; kj++) {
             if (kj == mi) continue;
             const int kk = act[kj] * S + n;
-            if (nd.vol[kk] > maxOther) {
-                maxOther = nd.vol[kk];
+            const double vk = cterm<MIX>(nd.vol, kk);
+            if (vk > maxOther) {
+                maxOther = vk;
                 j = act[kj];
             }
-            gradj[0] -= nd.gvx[kk];
-            gradj[1] -= nd.gvy[kk];
-            gradj[2] -= nd.gvz[kk];
+            gradj[0] -= cterm<MIX>(nd.gvx, kk);
+            gradj[1] -= cterm<MIX>(nd.gvy, kk);
+            gradj[2] -= cterm<MIX>(nd.gvz, kk);
         }
         if (j < 0) continue;
         const double massRatio = massi / Mc;
         double mred = 1. - massRatio;
         double delPi[3] = {Pc[0] * massRatio - nd.px[ki], Pc[1] * massRatio - nd.py[ki],
                            Pc[2] * massRatio - nd.pz[ki]};
-        const double normi[3] = {nd.gvx[ki], nd.gvy[ki], nd.gvz[ki]};
+        const double normi[3] = {cterm<MIX>(nd.gvx, ki), cterm<MIX>(nd.gvy, ki), cterm<MIX>(nd.gvz, ki)};
         double norm[3];
         if (ct.normals == 0) {
             const double magi = sqrt(dot3(normi, normi)), magj = sqrt(dot3(gradj, gradj));
@@ -1639,7 +1662,7 @@ static __global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBC
     }
     {
         const DevContact ct = node_contact_params<BATCH>(sp, n);
-        if (ct.nf > 1) node_contact(ct, nd, n, BC_MASS_MOMENTUM, dt);
+        if (ct.nf > 1) node_contact<MIX>(ct, nd, n, BC_MASS_MOMENTUM, dt);
     }
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;
@@ -1705,7 +1728,7 @@ static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, Dev
         node_finish_update<DIM, MIX>(nd, k, m, p, fr);
     }
     if (!mm) return;
-    node_contact(ct, nd, n, BC_UPDATE_MOMENTUM, dt);
+    node_contact<MIX>(ct, nd, n, BC_UPDATE_MOMENTUM, dt);
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;
         if (!nd.active[k]) continue;
@@ -1714,9 +1737,11 @@ static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, Dev
         if (grp >= 0) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, fr);
         node_finish_update<DIM, MIX>(nd, k, m, p, fr);
         if (zero_contact) {
-            nd.vol[k] = 0.;
+            cterm_set<MIX>(nd.vol, k, 0.);
             nd.dsx[k] = nd.dsy[k] = nd.dsz[k] = 0.;
-            nd.gvx[k] = nd.gvy[k] = nd.gvz[k] = 0.;
+            cterm_set<MIX>(nd.gvx, k, 0.);
+            cterm_set<MIX>(nd.gvy, k, 0.);
+            cterm_set<MIX>(nd.gvz, k, 0.);
         }
     }
 }
@@ -1741,7 +1766,7 @@ static __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs
             nd.py[k] = nd.uy[k];
             nd.pz[k] = nd.uz[k];
         }
-        node_contact(ct, nd, n, BC_UPDATE_STRAINS_LAST, dt);
+        node_contact<MIX>(ct, nd, n, BC_UPDATE_STRAINS_LAST, dt);
     }
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;
@@ -1808,14 +1833,14 @@ static __global__ void k_det_resolve(StepParams sp, DevNodes nd, int nn, int pha
     }
     if (sp.ct.nf > 1) {
         const int bv = usl ? DB_UVOL : DB_VOL, bd = usl ? DB_UDS : DB_DS, bg = usl ? DB_UGV : DB_GV;
-        nd.vol[n] = take2(DQ_VOL, bv);
+        cterm_set<MIX>(nd.vol, n, take2(DQ_VOL, bv));
         nd.dsx[n] = take2(DQ_DSX, bd);
         nd.dsy[n] = take2(DQ_DSY, bd);
-        nd.gvx[n] = take(DQ_GVX, bg);
-        nd.gvy[n] = take(DQ_GVY, bg);
+        cterm_set<MIX>(nd.gvx, n, take(DQ_GVX, bg));
+        cterm_set<MIX>(nd.gvy, n, take(DQ_GVY, bg));
         if (DIM == 3) {
             nd.dsz[n] = take2(DQ_DSZ, bd);
-            nd.gvz[n] = take(DQ_GVZ, bg);
+            cterm_set<MIX>(nd.gvz, n, take(DQ_GVZ, bg));
         }
     }
 }
