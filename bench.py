@@ -304,13 +304,19 @@ def timed_run(args, m, dist, precision: int, local: int):
     stream (per-kernel event pairs in the same region).  Returns the run
     (still open), its timings and the state after W+K steps."""
     from nairn_gb300 import gpu
-    run = gpu.GpuRun(m, sort_interval=max(1, args.sort_interval), precision=precision)
+    si = args.sort_interval
+    if si <= 0:
+        # the sort interval, tuned on a separate context over the same early
+        # steps, so the measured run covers steps W+1 .. W+K like any other
+        tune = gpu.GpuRun(m, precision=precision)
+        tune.upload(m.particles)
+        tune.step(args.warmup)
+        si, _ = tune.autotune_sort(16)
+        tune.close()
+    run = gpu.GpuRun(m, sort_interval=si, precision=precision)
     run.upload(m.particles)
     run.step(args.warmup)
-    si, tuned = args.sort_interval, 0
-    if si <= 0:
-        si, _ = run.autotune_sort(16)  # 64 real steps
-        tuned = 64
+    tuned = 0
     run.set_profiling(True)
     launches0 = run.launch_count()
     clocks = ClockSampler(local)

@@ -42,6 +42,7 @@ def main(argv=None):
     ap.add_argument("--plate", type=int, nargs=3, default=(64, 64, 16), help="plate cells (contact3d)")
     ap.add_argument("--block", type=int, nargs=3, default=(20, 20, 8), help="block cells (contact3d)")
     ap.add_argument("--p2g", choices=("atomic", "deterministic"), default="atomic")
+    ap.add_argument("--profile", action="store_true", help="per-kernel ms of the timed steps (single runs)")
     a = ap.parse_args(argv)
     from nairn_gb300 import gpu, model
     prec = 1 if a.precision == "mixed" else 0
@@ -77,9 +78,13 @@ def main(argv=None):
         r = gpu.GpuRun(m, precision=prec, sort_interval=a.sort_interval, p2g=1 if a.p2g == "deterministic" else 0)
         r.upload(m.particles)
         r.step(a.warmup)
+        if a.profile:
+            r.set_profiling(True)
         t = r.step_timed(a.steps)
         out = {"workload": m.name, "particles": m.n, "ms_per_step": t / a.steps,
                "particle_steps_per_s": m.n * a.steps / (t / 1e3), "launches": r.launch_count()}
+        if a.profile:
+            out["kernels_ms_per_step"] = {k: round(v / a.steps, 4) for k, v in r.profile().items() if v > 0}
         r.close()
     out["precision"] = a.precision
     out["sort_interval"] = a.sort_interval
