@@ -21,6 +21,13 @@ namespace nmg {
 
 enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2 };
 
+// Resident 256-thread blocks per SM the strain kernels are compiled for (this
+// caps their registers at 80): their FP64 constitutive updates are latency
+// bound at the two blocks the uncapped register count allows.  lCPDI kernels
+// keep their registers (the 27-node window); capping them spills.
+template <int SHAPE>
+constexpr int kStrainBlocks = SHAPE == SHAPE_LCPDI ? 1 : 3;
+
 // ---------------------------------------------------------------------------
 // deterministic node sums (MPMGPU_P2G_DETERMINISTIC)
 // ---------------------------------------------------------------------------
@@ -1065,7 +1072,7 @@ __device__ __forceinline__ void forces_scatter(const StepParams &sp, const DevPa
 // (GridForcesTask.cpp:40-153, MatPoint2D.cpp:242-262, MatPoint3D.cpp:248-269).
 // Mixed mode: internal-force products in FP32 into FP32 accumulators.
 template <int DIM, int SHAPE, bool STRAIN, bool MIX, bool BATCH, bool DET = false>
-static __global__ void __launch_bounds__(256) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     RunView rv;
@@ -1323,7 +1330,7 @@ static __global__ void __launch_bounds__(256) k_det_usl(StepParams sp, DevPartic
 // UpdateStrainsFirstTask::FullStrainUpdate called from
 // UpdateStrainsLastContactTask (:149), fused with ResetElementsTask.
 template <int DIM, int SHAPE, bool MIX, bool BATCH>
-static __global__ void __launch_bounds__(256) k_strain_last(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_last(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
     RunView rv;
