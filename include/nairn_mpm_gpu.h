@@ -106,7 +106,9 @@ typedef struct {
  * friction law CoulombFriction (NairnMPM/src/Materials/CoulombFriction.cpp). */
 typedef struct {
     int32_t enabled;
-    int32_t normals;          /* MeshInfo materialNormalMethod 0..4 (volume gradients) */
+    int32_t normals;          /* MeshInfo materialNormalMethod (MeshInfo.hpp:31):
+                                 0 MAXIMUM_VOLUME_GRADIENT, 1 MAXIMUM_VOLUME,
+                                 2 AVERAGE_MAT_VOLUME_GRADIENTS; others refused */
     double friction;          /* Coulomb coefficient; <0 stick; 0 frictionless */
     double contact_cutoff;    /* position-based contact cutoff (cells); <0 displacement based */
     double rigid_gradient_bias;
