@@ -26,7 +26,7 @@ enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2 };
 // bound at the two blocks the uncapped register count allows.  lCPDI kernels
 // keep their registers (the 27-node window); capping them spills.
 template <int SHAPE>
-constexpr int kStrainBlocks = SHAPE == SHAPE_LCPDI ? 1 : 3;
+constexpr int kStrainBlocks = SHAPE == SHAPE_LCPDI ? 2 : 3;
 
 // ---------------------------------------------------------------------------
 // deterministic node sums (MPMGPU_P2G_DETERMINISTIC)
@@ -591,7 +591,6 @@ __device__ __forceinline__ void cpdi_nodes(const DevGrid &g, int nb, const DevPa
 template <int DIM, bool GRAD, class F>
 __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevParticles &p, int i, F &&f) {
     constexpr int NC = DIM == 3 ? 8 : 4;
-    constexpr int W = DIM == 3 ? 27 : 9;
     const size_t n = (size_t)p.n;
     int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
     int cell[NC][3];
@@ -611,59 +610,55 @@ __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevP
         cpdi_nodes<DIM, GRAD, float>(g, nb, p, i, f);
         return;
     }
-    const float ws = DIM == 3 ? 0.125f : 0.25f;
-    float N[W], GX[W], GY[W], GZ[W];
-#pragma unroll
-    for (int w = 0; w < W; w++) N[w] = GX[w] = GY[w] = GZ[w] = 0.f;
+    // per corner: natural coordinates, the corner cell's offset in the window
+    // (bit a set: one cell up along axis a) and gradient weights
+    float xi[NC][3], wg[NC][3];
+    unsigned off = 0u;
 #pragma unroll
     for (int c = 0; c < NC; c++) {
-        float wt[3][3];
 #pragma unroll
-        for (int a = 0; a < DIM; a++) {
-            const float xi = cpdi_xi<float>(p, (3 * c + a) * n + i);
-            const int o = cell[c][a] - lo[a];
-            const float w0 = 0.5f * (1.f - xi), w1 = 0.5f * (1.f + xi);
-            wt[a][0] = o == 0 ? w0 : 0.f;
-            wt[a][1] = o == 0 ? w1 : w0;
-            wt[a][2] = o == 0 ? 0.f : w1;
+        for (int a = 0; a < 3; a++) {
+            xi[c][a] = a < DIM ? cpdi_xi<float>(p, (3 * c + a) * n + i) : 0.f;
+            wg[c][a] = GRAD && a < DIM ? cpdi_wg<float>(p, (3 * c + a) * n + i) : 0.f;
+            if (a < DIM && cell[c][a] != lo[a]) off |= 1u << (3 * c + a);
         }
-        float gxc = 0.f, gyc = 0.f, gzc = 0.f;
-        if (GRAD) {
-            gxc = cpdi_wg<float>(p, (3 * c) * n + i);
-            gyc = cpdi_wg<float>(p, (3 * c + 1) * n + i);
-            if (DIM == 3) gzc = cpdi_wg<float>(p, (3 * c + 2) * n + i);
-        }
-        // the corner element's linear shape function is the product of the
-        // factors 0.5 (1 +- xi): 0.25 (1+-xi)(1+-eta) in 2D, 0.125 (...) in 3D
-#pragma unroll
-        for (int cz = 0; cz < (DIM == 3 ? 3 : 1); cz++)
-#pragma unroll
-            for (int cy = 0; cy < 3; cy++)
-#pragma unroll
-                for (int cx = 0; cx < 3; cx++) {
-                    const int w = (cz * 3 + cy) * 3 + cx;
-                    float sfn = wt[0][cx] * wt[1][cy];
-                    if (DIM == 3) sfn *= wt[2][cz];
-                    if (sfn < 1e-15f) continue;
-                    N[w] += ws * sfn;
-                    if (GRAD) {
-                        GX[w] += gxc * sfn;
-                        GY[w] += gyc * sfn;
-                        if (DIM == 3) GZ[w] += gzc * sfn;
-                    }
-                }
     }
+    // factor 0.5 (1 -+ xi) of window position j (0..2) along axis a for corner c
+    auto wt = [&](int c, int a, int j) -> float {
+        const bool up = (off >> (3 * c + a)) & 1u;
+        const float w0 = 0.5f * (1.f - xi[c][a]), w1 = 0.5f * (1.f + xi[c][a]);
+        return j == 0 ? (up ? 0.f : w0) : (j == 1 ? (up ? w0 : w1) : (up ? w1 : 0.f));
+    };
+    const float ws = DIM == 3 ? 0.125f : 0.25f;
     const int base = nb + (DIM == 3 ? lo[2] * g.zplane : 0) + lo[1] * g.yplane + lo[0];
+    // one window row (cy, cz) at a time: sums over the corners in corner order,
+    // as the merged node list of the reference accumulates them
+#pragma unroll 1
+    for (int row = 0; row < (DIM == 3 ? 9 : 3); row++) {
+        const int cy = row % 3, cz = row / 3;
+        float N[3] = {0.f, 0.f, 0.f}, GX[3] = {0.f, 0.f, 0.f}, GY[3] = {0.f, 0.f, 0.f}, GZ[3] = {0.f, 0.f, 0.f};
 #pragma unroll
-    for (int cz = 0; cz < (DIM == 3 ? 3 : 1); cz++)
-#pragma unroll
-        for (int cy = 0; cy < 3; cy++)
+        for (int c = 0; c < NC; c++) {
+            const float wy = wt(c, 1, cy), wz = DIM == 3 ? wt(c, 2, cz) : 1.f;
 #pragma unroll
             for (int cx = 0; cx < 3; cx++) {
-                const int w = (cz * 3 + cy) * 3 + cx;
-                if (N[w] == 0.f) continue;
-                f(base + cx + cy * g.yplane + cz * g.zplane, N[w], GX[w], GY[w], GZ[w]);
+                float sfn = wt(c, 0, cx) * wy;
+                if (DIM == 3) sfn *= wz;
+                if (sfn < 1e-15f) continue;
+                N[cx] += ws * sfn;
+                if (GRAD) {
+                    GX[cx] += wg[c][0] * sfn;
+                    GY[cx] += wg[c][1] * sfn;
+                    if (DIM == 3) GZ[cx] += wg[c][2] * sfn;
+                }
             }
+        }
+#pragma unroll
+        for (int cx = 0; cx < 3; cx++) {
+            if (N[cx] == 0.f) continue;
+            f(base + cx + cy * g.yplane + cz * g.zplane, N[cx], GX[cx], GY[cx], GZ[cx]);
+        }
+    }
 }
 
 // the nodes of particle i for this step, whatever the shape-function option
@@ -886,7 +881,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
 // mass accumulate in FP64 in both modes: grid velocities carry the bulk motion
 // and their differences across a cell are the strain rate.
 template <int DIM, int SHAPE, bool MIX, bool BATCH, bool DET = false>
-static __global__ void __launch_bounds__(256) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -1174,7 +1169,7 @@ __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticl
 // v_particle + sum N (v_node - v_particle) (the weights sum to one) with the
 // differences from FP32 pairs, S a in FP32; the update itself is FP64.
 template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH, bool DET = false>
-static __global__ void __launch_bounds__(256) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
