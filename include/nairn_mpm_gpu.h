@@ -236,6 +236,27 @@ int mpmgpu_sort_by_cell(const int32_t *d_elem, int32_t n, int32_t nelems, int32_
  * The call synchronizes `stream`. */
 int mpmgpu_sort_by_cell_noalloc(const int32_t *d_elem, int32_t n, int32_t nelems, int32_t *d_perm, void *stream);
 
+/* ---- archive output ----------------------------------------------------------
+ * The particle records of a NairnMPM archive file (ArchiveData::ArchiveResults,
+ * NairnMPM/src/System/ArchiveData.cpp:807-1100), packed on the device from the
+ * current particle state and copied to the host in the host's particle order,
+ * so the host writes its 64-byte header (ArchiveData::SetArchiveHeader) and
+ * then the buffer -- without downloading the particle state into mpm[].
+ * mpm_order is the MPMArchiveOrder string; it is padded and its forced items
+ * set as ArchiveData::CalcArchiveSize does.  Items the device does not hold
+ * (temperature, heat energy, element crossings, damage normals, spin, history
+ * values beyond the first, particle size) and big-endian ('m') archives are
+ * refused with MPMGPU_ERR_UNSUPPORTED.  Initial material angles are zero. */
+
+/* Bytes of one particle record for a dimension (2 or 3) and order string, or
+ * the negated status when the order cannot be packed. */
+int64_t mpmgpu_archive_record_size(int32_t dim, const char *mpm_order);
+
+/* Pack the records of all particles into host_records (capacity bytes, at
+ * least n * record size); thickness is the 2D particles' thickness (mm). */
+int mpmgpu_archive_records(MpmGpuCtx *ctx, const char *mpm_order, double thickness, void *host_records,
+                           int64_t capacity);
+
 /* ---- extensions without a counterpart in the reference ----------------------
  * Host-integration and measurement helpers of this library; a NairnMPM
  * integration does not need them. */

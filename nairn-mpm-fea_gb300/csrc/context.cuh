@@ -58,6 +58,8 @@ struct MpmGpuCtx {
     nmg::DevContact ct{1, 0, 2, 2, 0.};       // material fields and multimaterial contact
     bool contact_on = false;
     nmg::DevDet det{nullptr, 0, nullptr, nullptr};     // deterministic node sums (p2g option 1)
+    void *archive_buf = nullptr;         // device staging of archive records
+    size_t archive_cap = 0;
 };
 
 namespace nmg {

@@ -18,6 +18,7 @@
 
 #include "context.cuh"
 #include "host_common.cuh"
+#include "archive.cuh"
 
 using namespace nmg;
 
@@ -705,6 +706,48 @@ int mpmgpu_download_particles(MpmGpuCtx *c, MpmGpuParticles *h) {
     return MPMGPU_OK;
 }
 
+int64_t mpmgpu_archive_record_size(int32_t dim, const char *mpm_order) {
+    ArchiveLayout L{};
+    std::string why;
+    const int st = archive_layout(dim, mpm_order, L, why);
+    if (st != MPMGPU_OK) {
+        set_err(nullptr, st, "mpmgpu_archive_record_size: " + why);
+        return -st;
+    }
+    return L.rec;
+}
+
+int mpmgpu_archive_records(MpmGpuCtx *c, const char *mpm_order, double thickness, void *host_records,
+                           int64_t capacity) {
+    if (!c || !host_records) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_archive_records: null argument");
+    if (c->p.n <= 0 || !c->mats) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_archive_records: no particles");
+    ArchiveLayout L{};
+    std::string why;
+    const int st = archive_layout(c->dim, mpm_order, L, why);
+    if (st != MPMGPU_OK) return set_err(c, st, "mpmgpu_archive_records: " + why);
+    L.thickness = thickness;
+    const size_t bytes = (size_t)c->p.n * L.rec;
+    if (capacity < (int64_t)bytes) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_archive_records: buffer too small");
+    if (c->archive_cap < bytes) {
+        if (c->archive_buf) cudaFree(c->archive_buf);
+        c->archive_buf = nullptr;
+        c->archive_cap = 0;
+        cudaError_t e = cudaMalloc(&c->archive_buf, bytes);
+        if (e != cudaSuccess) return set_err(c, MPMGPU_ERR_OOM, "archive staging buffer");
+        c->archive_cap = bytes;
+    }
+    const int TB = 256, nb = (c->p.n + TB - 1) / TB;
+    if (c->dim == 3)
+        k_archive_pack<3><<<nb, TB, 0, c->stream>>>(L, c->p, c->orig, c->mats, (char *)c->archive_buf);
+    else
+        k_archive_pack<2><<<nb, TB, 0, c->stream>>>(L, c->p, c->orig, c->mats, (char *)c->archive_buf);
+    c->launches++;
+    CK(cudaMemcpyAsync(host_records, c->archive_buf, bytes, cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    CK(cudaGetLastError());
+    return MPMGPU_OK;
+}
+
 void mpmgpu_destroy(MpmGpuCtx *c) {
     if (!c) return;
     free_particles(c);
@@ -715,6 +758,7 @@ void mpmgpu_destroy(MpmGpuCtx *c) {
     if (c->bc_group) cudaFree(c->bc_group);
     if (c->bc_block) cudaFree(c->bc_block);
     if (c->err) cudaFree(c->err);
+    if (c->archive_buf) cudaFree(c->archive_buf);
     if (c->det.lim) cudaFree(c->det.lim);
     if (c->det.bnd) cudaFree(c->det.bnd);
     if (c->det.nbnd) cudaFree(c->det.nbnd);

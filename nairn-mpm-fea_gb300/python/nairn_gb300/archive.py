@@ -94,3 +94,97 @@ def read_archive(path: str) -> dict:
     out["three_d"] = three_d
     out["order"] = order
     return out
+
+
+ARCH_MAXMPMITEMS = 25
+
+
+def normalize_order(order: str) -> str:
+    """ArchiveData::CalcArchiveSize (ArchiveData.cpp:266-283): pad to the
+    known items with 'N', defaults on, retired items off, RotStrain = Strain."""
+    o = list(order if len(order) >= 2 else "mY")
+    o += ["N"] * (ARCH_MAXMPMITEMS - len(o))
+    o = o[:ARCH_MAXMPMITEMS]
+    o[ARCH_Defaults] = "Y"
+    o[ARCH_OldOrigPosition] = "N"
+    o[ARCH_ver2Empty] = "N"
+    o[ARCH_RotStrain] = o[ARCH_Strain]
+    return "".join(o)
+
+
+def record_dtype(order: str, three_d: bool) -> np.dtype:
+    """The particle record of an (unnormalized) MPMArchiveOrder string."""
+    return _dtype(normalize_order(order), three_d)
+
+
+def write_archive(path: str, order: str, three_d: bool, time_ms: float, records: bytes,
+                  crack_order: str = "iYNNNNN", structured: bool = True) -> None:
+    """A ver6 archive: the 64-byte header of ArchiveData::SetArchiveHeader
+    (ArchiveData.cpp:464-486) followed by the particle records."""
+    mo = normalize_order(order)
+    hdr = bytearray(HEADER_LENGTH)
+    k = 0
+    for chunk in (b"ver6", bytes([len(mo)]), mo.encode("ascii"), bytes([len(crack_order)]),
+                  crack_order.encode("ascii"), b"3" if three_d else b"2", b"1" if structured else b"0"):
+        hdr[k:k + len(chunk)] = chunk
+        k += len(chunk)
+    hdr[k:k + 4] = np.float32(time_ms).tobytes()
+    with open(path, "wb") as fh:
+        fh.write(bytes(hdr))
+        fh.write(records)
+
+
+def pack_records(p: dict, materials, order: str, three_d: bool, thickness: float = 1.0) -> bytes:
+    """CPU restatement of ArchiveData::ArchiveResults' particle records
+    (ArchiveData.cpp:807-1100) from a particle-state dict: the checker of the
+    device packer (mpmgpu_archive_records), same arithmetic in the same order."""
+    mo = normalize_order(order)
+    dt = _dtype(mo, three_d)
+    n = p["x"].shape[0]
+    rec = np.zeros(n, dtype=dt)
+    mat = p["mat"]
+    rho0 = np.array([m["rho"] * 0.001 for m in materials])[mat]
+    mtype = np.array([m["type"] for m in materials])[mat]
+    rec["elem"] = p["elem"] + 1
+    rec["mass"] = p["mass"]
+    rec["mat"] = mat + 1
+    # GetRotationZ/Y/XInDegrees with zero initial angles (MPMBase.cpp:601-622)
+    rec["anglez"] = 180. * (0. - 0.5 * p["wxy"]) / np.pi
+    if three_d:
+        rec["angley"] = 180. * (0. + 0.5 * p["wxz"]) / np.pi
+        rec["anglex"] = 180. * (0. - 0.5 * p["wyz"]) / np.pi
+        axes = ("x", "y", "z")
+    else:
+        rec["thick"] = thickness
+        axes = ("x", "y")
+    rec["pos"] = np.stack([p[a] for a in axes], 1)
+    rec["origpos"] = np.stack([p[a + "0"] for a in axes], 1)
+
+    def on(i):
+        return mo[i] == "Y"
+
+    if on(ARCH_Velocity):
+        rec["vel"] = np.stack([p["v" + a] for a in axes], 1)
+    if on(ARCH_Stress):
+        rho = rho0 / np.where(mtype == 28, p["hist0"], 1.)
+        P = np.where(mtype == 1, 0., p["pressure"])
+        cols = [rho * (p["sxx"] - P), rho * (p["syy"] - P), rho * (p["szz"] - P), rho * p["sxy"]]
+        if three_d:
+            cols += [rho * p["sxz"], rho * p["syz"]]
+        rec["stress"] = np.stack(cols, 1)
+    tens = ("xx", "yy", "zz", "xy", "xz", "yz") if three_d else ("xx", "yy", "zz", "xy")
+    if on(ARCH_Strain):
+        rec["strain"] = np.stack([p["e" + t] for t in tens], 1)
+    if on(ARCH_PlasticStrain):
+        rec["plastic"] = np.stack([p["p" + t] for t in tens], 1)
+    if on(ARCH_WorkEnergy):
+        rec["work"] = 1.e-9 * p["mass"] * p["work"]
+    if on(ARCH_PlasticEnergy):
+        rec["plastE"] = 1.e-9 * p["mass"] * p["plast"]
+    if on(ARCH_ShearComponents):
+        rec["shear"] = np.stack([0.5 * (p["exy"] - p["wxy"]), 0.5 * (p["exy"] + p["wxy"])], 1)
+    if on(ARCH_StrainEnergy):
+        rec["strainE"] = 1.e-9 * p["mass"] * p["work"]
+    if on(ARCH_History):
+        rec["hist1"] = p["hist0"]
+    return rec.tobytes()

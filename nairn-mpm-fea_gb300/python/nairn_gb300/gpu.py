@@ -55,6 +55,10 @@ def lib():
     L.mpmgpu_autotune_sort.argtypes = [C.c_void_p, C.c_int32, C.c_double, P(C.c_int32), P(C.c_double),
                                        P(C.c_int32)]
     L.mpmgpu_autotune_sort.restype = C.c_int
+    L.mpmgpu_archive_record_size.argtypes = [C.c_int32, C.c_char_p]
+    L.mpmgpu_archive_record_size.restype = C.c_int64
+    L.mpmgpu_archive_records.argtypes = [C.c_void_p, C.c_char_p, C.c_double, C.c_void_p, C.c_int64]
+    L.mpmgpu_archive_records.restype = C.c_int
     L.mpmgpu_step_timed.restype = C.c_int
     L.mpmgpu_launch_count.argtypes = [C.c_void_p]
     L.mpmgpu_launch_count.restype = C.c_longlong
@@ -108,7 +112,8 @@ def lib():
 
 
 # every symbol the header declares (checked by the CPU tests)
-EXPORTED = ("mpmgpu_step_timed", "mpmgpu_autotune_sort", "mpmgpu_set_profiling", "mpmgpu_stream", "mpmgpu_launch_count",
+EXPORTED = ("mpmgpu_step_timed", "mpmgpu_autotune_sort", "mpmgpu_archive_record_size", "mpmgpu_archive_records",
+            "mpmgpu_set_profiling", "mpmgpu_stream", "mpmgpu_launch_count",
             "mpmgpu_host_register", "mpmgpu_host_unregister", "mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
             "mpmgpu_set_velocity_bcs", "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles",
             "mpmgpu_last_error", "mpmgpu_destroy", "mpmgpu_profile")
@@ -165,6 +170,18 @@ class GpuRun:
         self.t += taken.value * self.model.options["timestep"]
         self._check(st)
         return si.value, ms.value
+
+    def archive_records(self, order: str, thickness: float = 1.0) -> bytes:
+        """The particle records of a NairnMPM archive for the current state,
+        packed on the device (mpmgpu_archive_records)."""
+        L = lib()
+        rec = int(L.mpmgpu_archive_record_size(int(self.model.grid.dim), order.encode("ascii")))
+        if rec < 0:
+            raise GpuError(-rec, L.mpmgpu_last_error(None).decode())
+        buf = np.empty(self.model.n * rec, dtype=np.uint8)
+        self._check(L.mpmgpu_archive_records(self.h, order.encode("ascii"), float(thickness),
+                                             buf.ctypes.data_as(C.c_void_p), buf.nbytes))
+        return buf.tobytes()
 
     def launch_count(self) -> int:
         return int(lib().mpmgpu_launch_count(self.h))
