@@ -70,6 +70,8 @@ def parse():
     ap.add_argument("--contact-runs", type=int, default=48,
                     help="runs of the batched 3D contact instance mix (0: skip)")
     ap.add_argument("--contact-steps", type=int, default=40, help="timed steps of the batched contact measurement")
+    ap.add_argument("--contact-serve-requests", type=int, default=32,
+                    help="requests of the served 3D contact stream (0: skip)")
     ap.add_argument("--config3-steps", type=int, default=10,
                     help="timed steps of the 3D contact (config 3) measurement (0: skip)")
     return ap.parse_args()
@@ -490,6 +492,67 @@ def served_measurement(args, dist):
                                "policy": "admit while fewer than 3 M particles are resident, least work first"}}
 
 
+def contact_served_measurement(args, dist):
+    """The served form on the 3D contact instance mix: a seeded Poisson stream
+    (20 requests/s) of two-material contact runs of the contact_3d form
+    (20k-500k particles, 200-1,500 steps), submitted at their arrival times to
+    the serving loop (3D lCPDI batch, two material fields, mixed precision).
+    Beside it: every 4th request alone on the plain single-run FP64 path."""
+    import numpy as np
+    from nairn_gb300 import gpu, model
+    n_req = args.contact_serve_requests
+    rng = np.random.default_rng(404)
+    arrivals = np.cumsum(rng.exponential(1. / 20., n_req))
+    steps = rng.integers(200, 1501, n_req)
+    ms = model.contact_models(n_req, seed=404, steps=1500)
+    for m, k in zip(ms, steps):
+        m.nsteps = int(k)
+    srv = gpu.GpuServer(model.USAVG, model.SHAPE_LCPDI, 1, hbm_budget_bytes=int(args.serve_budget_gb * 1e9),
+                        max_runs=256, steps_per_round=10, frac_3d=1.0, nodes_per_particle=1.5, max_fields=2)
+    dist.barrier()
+    t0 = time.perf_counter()
+    ids = []
+    for t_arr, m in zip(arrivals, ms):
+        delay = t_arr - (time.perf_counter() - t0)
+        if delay > 0:
+            time.sleep(delay)
+        ids.append(srv.submit(m))
+    srv.drain(3600)
+    wall = time.perf_counter() - t0
+    infos = [srv.poll(r) for r in ids]
+    st = srv.stats()
+    srv.close()
+    lat = np.array([i["total_ms"] for i in infos])
+    work = float(sum(m.n * m.nsteps for m in ms))
+    alone_ps, alone_s, alone = 0.0, 0.0, []
+    for j in range(0, len(ms), 4):
+        m = ms[j]
+        t1 = time.perf_counter()
+        r = gpu.GpuRun(m)
+        r.upload(m.particles)
+        r.step(2)
+        k = 10
+        step_ms = r.step_timed(k) / k
+        r.close()
+        setup_ms = 1e3 * (time.perf_counter() - t1) - step_ms * (k + 2)
+        a = max(setup_ms, 0.0) + step_ms * m.nsteps
+        alone.append(a)
+        alone_ps += m.n * m.nsteps
+        alone_s += a / 1e3
+    return {"value": work / wall, "unit": METRIC, "requests": n_req, "completed": st["completed"],
+            "failed": st["failed"], "p50_ms": float(np.percentile(lat, 50)), "p99_ms": float(np.percentile(lat, 99)),
+            "wall_s": wall, "particle_steps": work, "dtype": "mixed",
+            "config": {"workload": "seeded Poisson(20/s) stream of %d 3D two-material contact runs (Neo-Hookean "
+                                   "block on elastic plate, Coulomb 0.3, lCPDI, 0.5 mm cells, 8 particles/cell, "
+                                   "USAVG), 20k-500k particles, 200-1500 steps (seed 404)" % n_req,
+                       "policy": "every request admitted on arrival (FIFO)", "hbm_budget_gb": args.serve_budget_gb,
+                       "steps_per_round": 10, "rounds": st["rounds"]},
+            "alone_plain_fp64": {"throughput": alone_ps / alone_s, "unit": METRIC, "requests": len(alone),
+                                 "p50_ms": float(np.percentile(alone, 50)), "p99_ms": float(np.percentile(alone, 99)),
+                                 "sample": "every 4th request alone: setup + 10 timed steps scaled to its steps"},
+            "speedup_vs_plain_fp64": (work / wall) / (alone_ps / alone_s)}
+
+
 def config3_measurement(args, dist, local):
     """The 3D two-material contact form: a Neo-Hookean block (G 10 MPa, K 50 MPa,
     rho 1.1) pressed and sliding (4 m/s down, 4 m/s along) on an elastic plate
@@ -683,6 +746,8 @@ def main():
         line["batched"] = batched_measurement(args, dist, local)
     if args.serve_requests > 0:
         line["served"] = served_measurement(args, dist)
+    if args.contact_serve_requests > 0:
+        line["contact3d_served"] = contact_served_measurement(args, dist)
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
         line["cpu_baseline"] = cpu_baseline(workload(args), args.cpu_seconds)
     dist.close()
