@@ -60,6 +60,10 @@ struct MpmGpuCtx {
     nmg::DevDet det{nullptr, 0, nullptr, nullptr};     // deterministic node sums (p2g option 1)
     void *archive_buf = nullptr;         // device staging of archive records
     size_t archive_cap = 0;
+    // regression contact normals: link counts, offsets, links, results, scan scratch
+    int *lr_cnt = nullptr, *lr_start = nullptr, *lr_list = nullptr, *lr_sums = nullptr;
+    double *lr_out = nullptr;
+    long long lr_cap = 0;                // links the list holds
 };
 
 namespace nmg {

@@ -82,9 +82,10 @@ struct DevNodes {
 struct DevContact {
     int nf;          // material velocity fields (1: single material mode)
     int fstride;     // node-index offset between fields
-    int normals;     // MeshInfo::materialNormalMethod 0, 1 or 2
+    int normals;     // MeshInfo::materialNormalMethod 0, 1, 2, 5 or 6
     int style;       // CoulombFriction: 0 stick, 1 frictionless, 2 frictional
     double friction; // Coulomb coefficient
+    const double *lr;  // regression normals (5, 6): 4 per field-node (n, deln)
 };
 
 // Deterministic node sums (MPMGPU_P2G_DETERMINISTIC): three 64-bit integer

@@ -393,10 +393,10 @@ int mpmgpu_set_contact(MpmGpuCtx *c, const MpmGpuContact *contact) {
         c->contact_on = false;
         return MPMGPU_OK;
     }
-    if (contact->normals < 0 || contact->normals > 2)
+    if (contact->normals < 0 || (contact->normals > 2 && contact->normals != 5 && contact->normals != 6))
         return set_err(c, MPMGPU_ERR_UNSUPPORTED,
-                       "contact normals: only volume-gradient methods 0 (max gradient), 1 (max volume) and 2 "
-                       "(average gradient) are implemented on the device");
+                       "contact normals: methods 0 (max gradient), 1 (max volume), 2 (average gradient), 5 (linear "
+                       "regression) and 6 (logistic regression) are implemented on the device");
     if (contact->contact_cutoff > 0.)
         return set_err(c, MPMGPU_ERR_UNSUPPORTED, "position-based contact is not implemented on the device");
     c->ct.normals = contact->normals;
@@ -585,6 +585,30 @@ int step_impl(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
         return set_err(c, MPMGPU_ERR_INVALID, "several material fields need multimaterial contact (mpmgpu_set_contact)");
     for (auto &pr : c->prof) pr.ms = 0.;
     if (c->profile && ensure_events(c, nsteps) != 0) return set_err(c, MPMGPU_ERR_CUDA, "event creation failed");
+    if (c->ct.nf > 1 && c->ct.normals >= 5) {
+        // regression normals: links of at most 64 nodes per particle (the
+        // largest lCPDI domain), a result per material field of each node
+        const long long need = (long long)c->p.n * (c->dim == 3 ? 64 : 16);
+        if (c->lr_cap < need) {
+            for (void *q : {(void *)c->lr_cnt, (void *)c->lr_start, (void *)c->lr_list, (void *)c->lr_sums,
+                            (void *)c->lr_out})
+                if (q) cudaFree(q);
+            const size_t m = (size_t)c->g.nnodes + 1, nsums = (m + kScanChunk - 1) / kScanChunk + 1;
+            cudaError_t e = cudaMalloc(&c->lr_cnt, m * sizeof(int));
+            if (e == cudaSuccess) e = cudaMalloc(&c->lr_start, m * sizeof(int));
+            if (e == cudaSuccess) e = cudaMalloc(&c->lr_list, (size_t)need * sizeof(int));
+            if (e == cudaSuccess) e = cudaMalloc(&c->lr_sums, nsums * sizeof(int));
+            if (e == cudaSuccess) e = cudaMalloc(&c->lr_out, (size_t)c->g.nnodes * c->ct.nf * 4 * sizeof(double));
+            if (e != cudaSuccess) {
+                c->lr_cnt = c->lr_start = c->lr_list = c->lr_sums = nullptr;
+                c->lr_out = nullptr;
+                c->lr_cap = 0;
+                return set_err(c, MPMGPU_ERR_OOM, "regression normal buffers");
+            }
+            c->lr_cap = need;
+        }
+        c->ct.lr = c->lr_out;
+    }
     std::vector<char> sorted((size_t)nsteps, 0);
     cudaEvent_t w0 = nullptr, w1 = nullptr;
     if (ms) {
@@ -759,6 +783,8 @@ void mpmgpu_destroy(MpmGpuCtx *c) {
     if (c->bc_block) cudaFree(c->bc_block);
     if (c->err) cudaFree(c->err);
     if (c->archive_buf) cudaFree(c->archive_buf);
+    for (void *q : {(void *)c->lr_cnt, (void *)c->lr_start, (void *)c->lr_list, (void *)c->lr_sums, (void *)c->lr_out})
+        if (q) cudaFree(q);
     if (c->det.lim) cudaFree(c->det.lim);
     if (c->det.bnd) cudaFree(c->det.bnd);
     if (c->det.nbnd) cudaFree(c->det.nbnd);

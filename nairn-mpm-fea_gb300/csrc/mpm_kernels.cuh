@@ -1470,7 +1470,9 @@ __device__ __forceinline__ bool coulomb_delta(const DevContact &ct, double delPi
                                               double dotn, double deln, double mred, const double *delFi,
                                               double dt) {
     if (ct.style == 0) return true;
-    if (delFi) deln += dt * (dotn - 0.5 * dot3(delFi, norm) * dt) / mred;
+    // the separation adjustment after the momentum update is skipped for
+    // regression normals (CoulombFriction.cpp:161-170)
+    if (delFi && ct.normals < 5) deln += dt * (dotn - 0.5 * dot3(delFi, norm) * dt) / mred;
     const bool inContact = deln < 0. && dotn < 0.;
     if (ct.style == 1) {
         if (!inContact) return false;
@@ -1561,7 +1563,18 @@ __device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, in
                            Pc[2] * massRatio - nd.pz[ki]};
         const double normi[3] = {cterm<MIX>(nd.gvx, ki), cterm<MIX>(nd.gvy, ki), cterm<MIX>(nd.gvz, ki)};
         double norm[3];
-        if (ct.normals == 0) {
+        bool hasDeln = false;
+        double lrDeln = 0.;
+        if (ct.normals >= 5) {
+            // regression normal and separation of this material against the
+            // others lumped (GetNormalVector, CrackVelocityFieldMulti.cpp:1033-1062)
+            const double *o = ct.lr + 4 * (size_t)ki;
+            norm[0] = o[0];
+            norm[1] = o[1];
+            norm[2] = o[2];
+            lrDeln = o[3];
+            hasDeln = true;
+        } else if (ct.normals == 0) {
             const double magi = sqrt(dot3(normi, normi)), magj = sqrt(dot3(gradj, gradj));
             const bool useI = magi >= magj;
             const double s = 1. / (useI ? magi : magj);
@@ -1587,7 +1600,7 @@ __device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, in
         double dispb[3];
 #pragma unroll
         for (int a = 0; a < 3; a++) dispb[a] = (dispc[a] - dispa[a]) * rmred + dispa[a];
-        const double deln = dot3(dispb, norm) - dot3(dispa, norm);
+        const double deln = hasDeln ? lrDeln : dot3(dispb, norm) - dot3(dispa, norm);
         mred *= massi;
         double delFi[3];
         const double *dfp = nullptr;
@@ -1864,3 +1877,5 @@ static __global__ void k_advance_runs(DevRun *runs, int nruns) {
 }
 
 }  // namespace nmg
+
+#include "lr.cuh"

@@ -1005,7 +1005,9 @@ typedef struct {
     long nn;                /* nodes + 1: stride between fields */
     long nfn;               /* nf * nn */
     int mm;                 /* multimaterial mode: contact terms and contact */
-    int normals;            /* MeshInfo::materialNormalMethod (0, 1 or 2) */
+    int normals;            /* MeshInfo::materialNormalMethod (0, 1, 2, 5 or 6) */
+    long *lr_start;         /* regression normals: particle lists of the contact */
+    long *lr_list;          /*   nodes, node n's at lr_list[lr_start[n] .. lr_start[n+1]) */
     int friction_style;     /* CoulombFriction: 0 stick, 1 frictionless, 2 frictional */
     double friction;        /* Coulomb coefficient */
 } OCtx;
@@ -1433,7 +1435,9 @@ static void change_momentum(OCtx *c, long k, const double *d, int callType) {
 static int coulomb_delta(const OCtx *c, double *delPi, const double *norm, double dotn, double deln, double mred,
                          const double *delFi) {
     if (c->friction_style == 0) return 1;
-    if (delFi) {
+    /* the separation adjustment after the momentum update is skipped for
+     * regression normals (CoulombFriction.cpp:161-170) */
+    if (delFi && c->normals < 5) {
         double fn = dot3(delFi, norm);
         deln += c->dt * (dotn - 0.5 * fn * c->dt) / mred;
     }
@@ -1476,6 +1480,294 @@ static int coulomb_delta(const OCtx *c, double *delPi, const double *norm, doubl
  * momentum changes), normals from volume gradients (GetNormalVector, :960-1069,
  * methods 0-2), separation from extrapolated displacements
  * (CrackSurfaceContact::MaterialSeparation), Coulomb friction. */
+/* ---- regression normals (LINEAR_REGRESSION 5, LOGISTIC_REGRESSION 6) ---- */
+
+/* a node with particles of two or more materials (NodalPoint::CalcTotalMassAndCount
+ * in PostExtrapolationTask.cpp:72-78) */
+static int contact_node(const OCtx *c, long n) {
+    int nm = 0;
+    for (int fl = 0; fl < c->nf; fl++)
+        if (c->f.npts[fl * c->nn + n] > 0) nm++;
+    return nm > 1;
+}
+
+/* MaterialContactNode::GetMaterialContactData (MaterialContactNode.cpp:238-353):
+ * each contact node lists every particle whose shape-function nodes include
+ * it, in particle order */
+static void lr_build_lists(OCtx *c) {
+    long nnodes = c->g.nnodes;
+    long *cnt = c->lr_start;
+    for (long n = 0; n <= nnodes + 1; n++) cnt[n] = 0;
+    char *isc = (char *)malloc((size_t)nnodes + 1);
+    for (long n = 1; n <= nnodes; n++) isc[n] = (char)contact_node(c, n);
+    for (int pass = 0; pass < 2; pass++) {
+        if (pass == 1) {
+            long acc = 0;
+            for (long n = 0; n <= nnodes; n++) {
+                long k = cnt[n + 1];
+                cnt[n + 1] = acc;
+                acc += k;
+            }
+        }
+        for (long q = 0; q < c->p->n; q++) {
+            OShape sh;
+            particle_shape(c, q, 0, &sh);
+            for (int j = 0; j < sh.n; j++) {
+                long n = sh.nds[j];
+                if (!isc[n]) continue;
+                if (pass == 0) cnt[n + 1]++;
+                else c->lr_list[cnt[n + 1]++] = q;
+            }
+        }
+    }
+    /* after the fill, cnt[n+1] is the end of node n's list = start of node n+1's */
+    cnt[0] = 0;
+    free(isc);
+}
+
+/* node position of 1-based node n */
+static void node_xyz(const OGrid *g, long n, double *x) {
+    long i = n - 1;
+    long nx1 = g->nx + 1, ny1 = g->ny + 1;
+    x[0] = g->xn[i % nx1];
+    x[1] = g->yn[(i / nx1) % ny1];
+    x[2] = g->dim == 3 ? g->zn[i / (nx1 * ny1)] : 0.;
+}
+
+/* inverse of a symmetric 3x3 [a b c; b d e; c e f] (Matrix3::Inverse) */
+static void inv3_sym(const double m[6], double r[9]) {
+    double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5];
+    double c00 = d * f - e * e, c01 = -(b * f - c * e), c02 = b * e - c * d;
+    double det = a * c00 + b * c01 + c * c02;
+    double c11 = a * f - c * c, c12 = -(a * e - b * c), c22 = a * d - b * b;
+    r[0] = c00 / det; r[1] = c01 / det; r[2] = c02 / det;
+    r[3] = c01 / det; r[4] = c11 / det; r[5] = c12 / det;
+    r[6] = c02 / det; r[7] = c12 / det; r[8] = c22 / det;
+}
+
+/* inverse of a symmetric 4x4 stored as its upper triangle
+ * mt[0..9] = (00 01 02 03 11 12 13 22 23 33) (Matrix4::Inverse, cofactors) */
+static void inv4_sym(const double mt[10], double r[16]) {
+    double m[4][4] = {{mt[0], mt[1], mt[2], mt[3]}, {mt[1], mt[4], mt[5], mt[6]},
+                      {mt[2], mt[5], mt[7], mt[8]}, {mt[3], mt[6], mt[8], mt[9]}};
+    double cof[4][4];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) {
+            double s3[3][3];
+            int ri = 0;
+            for (int a = 0; a < 4; a++) {
+                if (a == i) continue;
+                int cj = 0;
+                for (int b = 0; b < 4; b++) {
+                    if (b == j) continue;
+                    s3[ri][cj++] = m[a][b];
+                }
+                ri++;
+            }
+            double d3 = s3[0][0] * (s3[1][1] * s3[2][2] - s3[1][2] * s3[2][1]) -
+                        s3[0][1] * (s3[1][0] * s3[2][2] - s3[1][2] * s3[2][0]) +
+                        s3[0][2] * (s3[1][0] * s3[2][1] - s3[1][1] * s3[2][0]);
+            cof[i][j] = ((i + j) & 1) ? -d3 : d3;
+        }
+    double det = m[0][0] * cof[0][0] + m[0][1] * cof[0][1] + m[0][2] * cof[0][2] + m[0][3] * cof[0][3];
+    for (int i = 0; i < 4; i++)
+        for (int j = 0; j < 4; j++) r[4 * i + j] = cof[j][i] / det;
+}
+
+/* MatPoint2D/3D::GetDeformedRadius, ellipse method (MatPoint2D.cpp:482-495,
+ * MatPoint3D.cpp:497-510): distance from the particle centre to its deformed
+ * inscribed ellipse(oid) along the unit vector n */
+static double deformed_radius(const OCtx *c, long q, const double *n) {
+    const MpmGpuParticles *p = c->p;
+    double x0, x1, y0, y1, z0, z1;
+    elem_extent(&c->g, p->elem[q], &x0, &x1, &y0, &y1, &z0, &z1);
+    double px = 0.5 * p->lpx[q] * (x1 - x0), py = 0.5 * p->lpy[q] * (y1 - y0);
+    double F00 = 1. + p->exx[q], F11 = 1. + p->eyy[q];
+    double F01 = 0.5 * (p->exy[q] - p->wxy[q]), F10 = 0.5 * (p->exy[q] + p->wxy[q]);
+    if (c->g.dim == 2) {
+        double rdet = 1. / (F00 * F11 - F01 * F10);
+        double n0x = (F11 * n[0] - F10 * n[1]) * rdet;
+        double n0y = (-F01 * n[0] + F00 * n[1]) * rdet;
+        double rd = sqrt(n0x * n0x / (px * px) + n0y * n0y / (py * py));
+        return 1. / rd;
+    }
+    double pz = 0.5 * p->lpz[q] * (z1 - z0);
+    double F22 = 1. + p->ezz[q];
+    double F02 = 0.5 * (p->exz[q] - p->wxz[q]), F20 = 0.5 * (p->exz[q] + p->wxz[q]);
+    double F12 = 0.5 * (p->eyz[q] - p->wyz[q]), F21 = 0.5 * (p->eyz[q] + p->wyz[q]);
+    double c00 = F11 * F22 - F12 * F21, c01 = F12 * F20 - F10 * F22, c02 = F10 * F21 - F11 * F20;
+    double det = F00 * c00 + F01 * c01 + F02 * c02;
+    double i00 = c00 / det, i01 = (F02 * F21 - F01 * F22) / det, i02 = (F01 * F12 - F02 * F11) / det;
+    double i10 = c01 / det, i11 = (F00 * F22 - F02 * F20) / det, i12 = (F02 * F10 - F00 * F12) / det;
+    double i20 = c02 / det, i21 = (F01 * F20 - F00 * F21) / det, i22 = (F00 * F11 - F01 * F10) / det;
+    double n0x = i00 * n[0] + i01 * n[1] + i02 * n[2];
+    double n0y = i10 * n[0] + i11 * n[1] + i12 * n[2];
+    double n0z = i20 * n[0] + i21 * n[1] + i22 * n[2];
+    double rd = sqrt(n0x * n0x / (px * px) + n0y * n0y / (py * py) + n0z * n0z / (pz * pz));
+    return 1. / rd;
+}
+
+/* CrackVelocityFieldMulti::LinearRegressionNormal and LogisticRegressionNormal
+ * (MachineLearning.cpp:58-620) for material field a against all others
+ * lumped (b < 0), with PENALIZE_NORMALS: the unit normal and the separation
+ * deln from the two point clouds' supports along it (delMats.x) */
+static void lr_normal(const OCtx *c, long n, int a, int logistic, double *norm, double *deln) {
+    const MpmGpuParticles *p = c->p;
+    int is3d = c->g.dim == 3;
+    long s0 = c->lr_start[n], s1 = c->lr_start[n + 1];
+    double nd[3];
+    node_xyz(&c->g, n, nd);
+    double cell = is3d ? fmin(c->g.gx, fmin(c->g.gy, c->g.gz)) : fmin(c->g.gx, c->g.gy);
+    double cell2 = cell * cell;
+    const double offsetLin = 0.1, normLog = 1.e-7, offsetLog = 0., tol = 1.e-5;
+    const int maxIter = 15;
+    double nrm[3] = {0., 0., 0.};
+    if (is3d) {
+        double mt[10] = {0.}, rhs[4] = {0.}, lam[4];
+        double pen = logistic ? normLog * cell2 : 0.;
+        lam[0] = lam[1] = lam[2] = pen;
+        lam[3] = logistic ? offsetLog : offsetLin;
+        for (long k = s0; k < s1; k++) {
+            long q = c->lr_list[k];
+            double mi = particle_field(c, q) == a ? -1. : 1.;
+            double x = p->x[q] - nd[0], y = p->y[q] - nd[1], z = p->z[q] - nd[2];
+            mt[0] += x * x; mt[1] += x * y; mt[2] += x * z; mt[3] += x;
+            mt[4] += y * y; mt[5] += y * z; mt[6] += y;
+            mt[7] += z * z; mt[8] += z; mt[9] += 1.;
+            rhs[0] += mi * x; rhs[1] += mi * y; rhs[2] += mi * z; rhs[3] += mi;
+        }
+        double m[10] = {mt[0] + lam[0], mt[1], mt[2], mt[3], mt[4] + lam[1], mt[5], mt[6], mt[7] + lam[2], mt[8],
+                        mt[9] + lam[3]};
+        double inv[16], beta[4];
+        inv4_sym(m, inv);
+        for (int i = 0; i < 4; i++) beta[i] = inv[4 * i] * rhs[0] + inv[4 * i + 1] * rhs[1] + inv[4 * i + 2] * rhs[2] +
+                                                inv[4 * i + 3] * rhs[3];
+        if (!logistic) {
+            for (int i = 0; i < 3; i++) nrm[i] = beta[i];
+        } else {
+            for (int i = 0; i < 4; i++) { beta[i] *= 2.; lam[i] *= 1.; }
+            double prev[3] = {beta[0], beta[1], beta[2]};
+            double nmag = sqrt(dot3(prev, prev));
+            for (int i = 0; i < 3; i++) prev[i] *= 1. / nmag;
+            double lin[3] = {prev[0], prev[1], prev[2]};
+            double dcos = 1.;
+            int iter = 0;
+            while (dcos > tol && iter < maxIter) {
+                for (int i = 0; i < 10; i++) mt[i] = 0.;
+                for (int i = 0; i < 4; i++) rhs[i] = -lam[i] * beta[i];
+                for (long k = s0; k < s1; k++) {
+                    long q = c->lr_list[k];
+                    double mi = particle_field(c, q) == a ? -1. : 1.;
+                    double x = p->x[q] - nd[0], y = p->y[q] - nd[1], z = p->z[q] - nd[2];
+                    double dotp = x * beta[0] + y * beta[1] + z * beta[2] + beta[3];
+                    double arg = 1. + exp(-dotp);
+                    double phi = 2. * (arg - 1.) / (arg * arg);
+                    double phi2 = phi * phi;
+                    mt[0] += phi2 * x * x; mt[1] += phi2 * x * y; mt[2] += phi2 * x * z; mt[3] += phi2 * x;
+                    mt[4] += phi2 * y * y; mt[5] += phi2 * y * z; mt[6] += phi2 * y;
+                    mt[7] += phi2 * z * z; mt[8] += phi2 * z; mt[9] += phi2;
+                    double mifi = (mi - 2. / arg + 1.) * phi;
+                    rhs[0] += mifi * x; rhs[1] += mifi * y; rhs[2] += mifi * z; rhs[3] += mifi;
+                }
+                double mm[10] = {mt[0] + lam[0], mt[1], mt[2], mt[3], mt[4] + lam[1], mt[5], mt[6],
+                                 mt[7] + lam[2], mt[8], mt[9] + lam[3]};
+                inv4_sym(mm, inv);
+                for (int i = 0; i < 4; i++)
+                    beta[i] += inv[4 * i] * rhs[0] + inv[4 * i + 1] * rhs[1] + inv[4 * i + 2] * rhs[2] +
+                               inv[4 * i + 3] * rhs[3];
+                double cur[3] = {beta[0], beta[1], beta[2]};
+                nmag = sqrt(dot3(cur, cur));
+                for (int i = 0; i < 3; i++) cur[i] *= 1. / nmag;
+                dcos = 1. - dot3(cur, prev);
+                iter++;
+                for (int i = 0; i < 3; i++) prev[i] = nrm[i] = cur[i];
+            }
+            if (iter == 0) for (int i = 0; i < 3; i++) nrm[i] = prev[i];
+            if (nrm[0] != nrm[0]) for (int i = 0; i < 3; i++) nrm[i] = lin[i];
+        }
+    } else {
+        double mt[6] = {0.}, rhs[3] = {0.}, lam[3];
+        double pen = logistic ? normLog * cell2 : 0.;
+        lam[0] = lam[1] = pen;
+        lam[2] = logistic ? offsetLog : offsetLin;
+        for (long k = s0; k < s1; k++) {
+            long q = c->lr_list[k];
+            double mi = particle_field(c, q) == a ? -1. : 1.;
+            double x = p->x[q] - nd[0], y = p->y[q] - nd[1];
+            mt[0] += x * x; mt[1] += x * y; mt[2] += x;
+            mt[3] += y * y; mt[4] += y; mt[5] += 1.;
+            rhs[0] += mi * x; rhs[1] += mi * y; rhs[2] += mi;
+        }
+        double m[6] = {mt[0] + lam[0], mt[1], mt[2], mt[3] + lam[1], mt[4], mt[5] + lam[2]};
+        double inv[9], beta[3];
+        inv3_sym(m, inv);
+        for (int i = 0; i < 3; i++) beta[i] = inv[3 * i] * rhs[0] + inv[3 * i + 1] * rhs[1] + inv[3 * i + 2] * rhs[2];
+        if (!logistic) {
+            nrm[0] = beta[0];
+            nrm[1] = beta[1];
+        } else {
+            for (int i = 0; i < 3; i++) { beta[i] *= 2.; lam[i] *= 1.; }
+            double prev[2], nmag = sqrt(beta[0] * beta[0] + beta[1] * beta[1]);
+            prev[0] = beta[0] / nmag;
+            prev[1] = beta[1] / nmag;
+            double lin[2] = {prev[0], prev[1]};
+            double dcos = 1.;
+            int iter = 0;
+            nrm[0] = prev[0];
+            nrm[1] = prev[1];
+            while (dcos > tol && iter < maxIter) {
+                for (int i = 0; i < 6; i++) mt[i] = 0.;
+                for (int i = 0; i < 3; i++) rhs[i] = -lam[i] * beta[i];
+                for (long k = s0; k < s1; k++) {
+                    long q = c->lr_list[k];
+                    double mi = particle_field(c, q) == a ? -1. : 1.;
+                    double x = p->x[q] - nd[0], y = p->y[q] - nd[1];
+                    double arg = 1. + exp(-(x * beta[0] + y * beta[1] + beta[2]));
+                    double phi = 2. * (arg - 1.) / (arg * arg);
+                    double phi2 = phi * phi;
+                    mt[0] += phi2 * x * x; mt[1] += phi2 * x * y; mt[2] += phi2 * x;
+                    mt[3] += phi2 * y * y; mt[4] += phi2 * y; mt[5] += phi2;
+                    double mifi = (mi - 2. / arg + 1.) * phi;
+                    rhs[0] += mifi * x; rhs[1] += mifi * y; rhs[2] += mifi;
+                }
+                double mm[6] = {mt[0] + lam[0], mt[1], mt[2], mt[3] + lam[1], mt[4], mt[5] + lam[2]};
+                inv3_sym(mm, inv);
+                for (int i = 0; i < 3; i++)
+                    beta[i] += inv[3 * i] * rhs[0] + inv[3 * i + 1] * rhs[1] + inv[3 * i + 2] * rhs[2];
+                nmag = sqrt(beta[0] * beta[0] + beta[1] * beta[1]);
+                nrm[0] = beta[0] / nmag;
+                nrm[1] = beta[1] / nmag;
+                dcos = 1. - nrm[0] * prev[0] - nrm[1] * prev[1];
+                iter++;
+                prev[0] = nrm[0];
+                prev[1] = nrm[1];
+            }
+            if (nrm[0] != nrm[0]) { nrm[0] = lin[0]; nrm[1] = lin[1]; }
+        }
+        nrm[2] = 0.;
+    }
+    if (!logistic) {
+        double mag = sqrt(dot3(nrm, nrm));
+        for (int i = 0; i < 3; i++) nrm[i] *= 1. / mag;
+    }
+    /* separation: the supports of the two clouds along the normal */
+    double supA = 1.e30, supB = 1.e30;
+    for (long k = s0; k < s1; k++) {
+        long q = c->lr_list[k];
+        double xp[3] = {p->x[q], p->y[q], is3d ? p->z[q] : 0.};
+        double r = deformed_radius(c, q, nrm);
+        if (particle_field(c, q) == a) {
+            double t = -dot3(nrm, xp) - r;
+            if (t < supA) supA = t;
+        } else {
+            double t = dot3(nrm, xp) - r;
+            if (t < supB) supB = t;
+        }
+    }
+    for (int i = 0; i < 3; i++) norm[i] = nrm[i];
+    *deln = supA + supB;
+}
+
 static void material_contact(OCtx *c, int callType) {
     OField *f = &c->f;
     int nf = c->nf;
@@ -1537,7 +1829,13 @@ static void material_contact(OCtx *c, int callType) {
             delPi[1] += Pc[1] * massRatio;
             delPi[2] += Pc[2] * massRatio;
             double normi[3] = {f->gvx[ki] * 1., f->gvy[ki] * 1., f->gvz[ki] * 1.}, norm[3];
-            if (c->normals == 0) {
+            int hasDeln = 0;
+            double lrDeln = 0.;
+            if (c->normals >= 5) {
+                /* GetNormalVector's regression cases (CrackVelocityFieldMulti.cpp:1033-1062) */
+                lr_normal(c, n, act[mi], c->normals == 6, norm, &lrDeln);
+                hasDeln = 1;
+            } else if (c->normals == 0) {
                 double magi = sqrt(dot3(normi, normi)), magj = sqrt(dot3(gradj, gradj));
                 if (magi >= 1. * magj) for (int a = 0; a < 3; a++) norm[a] = normi[a] * (1. / magi);
                 else for (int a = 0; a < 3; a++) norm[a] = gradj[a] * (1. / magj);
@@ -1560,7 +1858,7 @@ static void material_contact(OCtx *c, int callType) {
             double rmred = 1. / mred;
             for (int a = 0; a < 3; a++) delta[a] *= rmred;
             double dispb[3] = {delta[0] + dispa[0], delta[1] + dispa[1], delta[2] + dispa[2]};
-            double deln = dot3(dispb, norm) - dot3(dispa, norm);
+            double deln = hasDeln ? lrDeln : dot3(dispb, norm) - dot3(dispa, norm);
             mred *= massi;
             double delFi[3], *dfp = NULL;
             if (postUpdate) {
@@ -1618,6 +1916,7 @@ static int one_step(OCtx *c) {
     for (long i = 1; i < nn; i++) {
         if (f->npts[i] > 0) { f->cx[i] = f->px[i]; f->cy[i] = f->py[i]; f->cz[i] = f->pz[i]; }
     }
+    if (c->mm && c->normals >= 5) lr_build_lists(c);
     if (c->mm) material_contact(c, MASS_MOMENTUM_CALL);
     if (method == MPMGPU_USF || method == MPMGPU_USAVG) velocity_bc_loop(c, MASS_MOMENTUM_CALL);
 
@@ -1678,8 +1977,8 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI)
         return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: shape function not implemented");
     if (contact && contact->enabled) {
-        if (contact->normals < 0 || contact->normals > 2)
-            return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: contact normals must be method 0, 1 or 2");
+        if (contact->normals < 0 || (contact->normals > 2 && contact->normals != 5 && contact->normals != 6))
+            return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: contact normals must be method 0, 1, 2, 5 or 6");
         if (contact->contact_cutoff > 0.)
             return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: position-based contact not implemented");
     }
@@ -1732,6 +2031,10 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     c.f.npts = (int *)calloc((size_t)nn, sizeof(int));
     c.xi = (double *)calloc((size_t)(3 * (p->n > 0 ? p->n : 1)), sizeof(double));
     if (opts->shape == MPMGPU_SHAPE_LCPDI) c.cpdi = (OCpdi *)calloc((size_t)(p->n > 0 ? p->n : 1), sizeof(OCpdi));
+    if (c.mm && c.normals >= 5) {
+        c.lr_start = (long *)calloc((size_t)c.g.nnodes + 2, sizeof(long));
+        c.lr_list = (long *)calloc((size_t)(p->n > 0 ? p->n : 1) * 64, sizeof(long));
+    }
     c.mtime = t0;
     for (int s = 0; s < nsteps && st == MPMGPU_OK; s++) {
         st = one_step(&c);
@@ -1741,6 +2044,8 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     free(c.f.npts);
     free(c.xi);
     free(c.cpdi);
+    free(c.lr_start);
+    free(c.lr_list);
     free(c.mats);
     return st;
 }

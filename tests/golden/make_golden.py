@@ -68,6 +68,16 @@ CASES = {
     "contact2d_fric_cpdi_usf": ("contact_2d", dict(steps=150, friction=0.3, normals=2, gimp="lCPDI", method=0)),
     "contact3d_fric_cpdi": ("contact_3d", dict(steps=60, friction=0.3, normals=2)),
     "contact3d_fric_ugimp_maxg": ("contact_3d", dict(steps=60, friction=0.5, normals=0, gimp="uGIMP")),
+    "contact2d_fric_logreg": ("contact_2d", dict(steps=150, friction=0.3, normals=6)),
+    "contact2d_stick_linreg_usl": ("contact_2d", dict(steps=120, friction=-1.0, normals=5, method=3)),
+    "contact2d_fric_logreg_cpdi": ("contact_2d", dict(steps=120, friction=0.3, normals=6, gimp="lCPDI")),
+    # a one-cell gap closed by a fast block: point clouds that start touching
+    # face to face have a regression separation of exactly zero, whose sign
+    # is then a matter of rounding
+    "contact3d_fric_logreg_cpdi": ("contact_3d", dict(steps=70, friction=0.3, normals=6, gap=0.5,
+                                                      v=(50000., 0., -200000.))),
+    "contact3d_fric_logreg_ugimp_usf": ("contact_3d", dict(steps=70, friction=0.3, normals=6, gimp="uGIMP",
+                                                           method=0, gap=0.5, v=(50000., 0., -200000.))),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")

