@@ -108,7 +108,9 @@ typedef struct {
     int32_t enabled;
     int32_t normals;          /* MeshInfo materialNormalMethod (MeshInfo.hpp:31):
                                  0 MAXIMUM_VOLUME_GRADIENT, 1 MAXIMUM_VOLUME,
-                                 2 AVERAGE_MAT_VOLUME_GRADIENTS; others refused */
+                                 2 AVERAGE_MAT_VOLUME_GRADIENTS, 5 LINEAR_REGRESSION,
+                                 6 LOGISTIC_REGRESSION (the reference's default;
+                                 5 and 6 in single-run contexts); others refused */
     double friction;          /* Coulomb coefficient; <0 stick; 0 frictionless */
     double contact_cutoff;    /* position-based contact cutoff (cells); <0 displacement based */
     double rigid_gradient_bias;
