@@ -74,6 +74,9 @@ def parse():
                     help="requests of the served 3D contact stream (0: skip)")
     ap.add_argument("--config3-steps", type=int, default=10,
                     help="timed steps of the 3D contact (config 3) measurement (0: skip)")
+    ap.add_argument("--archive-steps", type=int, default=60,
+                    help="steps of the archiving measurement on the headline workload (0: skip)")
+    ap.add_argument("--archive-every", type=int, default=10, help="steps between archives")
     return ap.parse_args()
 
 
@@ -553,6 +556,49 @@ def contact_served_measurement(args, dist):
             "speedup_vs_plain_fp64": (work / wall) / (alone_ps / alone_s)}
 
 
+ARCHIVE_ORDER = "iYYYYYNYNYNNNYNNNN"  # position, velocity, stress, strain, plastic strain, energies, history
+
+
+def archive_measurement(args, run, m, dist):
+    """The headline run taking a NairnMPM archive (the particle records of
+    ArchiveData::ArchiveResults) every `archive_every` steps: without
+    archives, with mpmgpu_archive_records (pack, copy, wait) and with
+    mpmgpu_archive_records_async (the copy to pinned host memory overlaps the
+    following steps).  Host wall time around whole step sequences."""
+    import numpy as np
+    from nairn_gb300 import gpu
+    L = gpu.lib()
+    rec = int(L.mpmgpu_archive_record_size(m.grid.dim, ARCHIVE_ORDER.encode()))
+    buf = np.empty(m.n * rec, dtype=np.uint8)
+    held = gpu.pin({"records": buf})
+    every, total = max(1, args.archive_every), max(args.archive_every, args.archive_steps)
+    total -= total % every
+
+    def timed(mode):
+        run.step(1)
+        dist.barrier()
+        t0 = time.perf_counter()
+        for _ in range(total // every):
+            run.step(every)
+            if mode == "sync":
+                run.archive_records(ARCHIVE_ORDER)
+            elif mode == "async":
+                run.archive_records_async(ARCHIVE_ORDER, buf)
+        run.archive_wait()
+        t = time.perf_counter() - t0
+        dist.barrier()
+        return dist.max(t) * 1e3 / total
+
+    out = {"every": every, "steps": total, "order": ARCHIVE_ORDER, "record_bytes": rec,
+           "archive_bytes": m.n * rec}
+    for mode in ("none", "sync", "async"):
+        out[mode + "_ms_per_step"] = timed(mode)
+    gpu.unpin(held)
+    out["sync_overhead"] = out["sync_ms_per_step"] / out["none_ms_per_step"] - 1.
+    out["async_overhead"] = out["async_ms_per_step"] / out["none_ms_per_step"] - 1.
+    return out
+
+
 def config3_measurement(args, dist, local):
     """The 3D two-material contact form: a Neo-Hookean block (G 10 MPa, K 50 MPa,
     rho 1.1) pressed and sliding (4 m/s down, 4 m/s along) on an elastic plate
@@ -701,6 +747,7 @@ def main():
     gpu.unpin(pinned)
     t_e2e = dist.max(t_e2e)
     e2e_value = total_particles * ke / t_e2e
+    archived = archive_measurement(args, run, m, dist) if args.archive_steps > 0 else None
     run.close()
 
     # roofline of the dominant kernel (largest share of the timed region)
@@ -738,6 +785,8 @@ def main():
                     "d2h_bytes_per_step": d2h * ws, "steps": ke,
                     "note": "per step: upload full particle state from pinned host memory, one step, download"},
             "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk}
+    if archived:
+        line["archived"] = archived
     if args.config3_steps > 0:
         line["contact3d"] = config3_measurement(args, dist, local)
     if args.contact_runs > 0:

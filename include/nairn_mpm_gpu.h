@@ -110,7 +110,7 @@ typedef struct {
                                  0 MAXIMUM_VOLUME_GRADIENT, 1 MAXIMUM_VOLUME,
                                  2 AVERAGE_MAT_VOLUME_GRADIENTS, 5 LINEAR_REGRESSION,
                                  6 LOGISTIC_REGRESSION (the reference's default;
-                                 5 and 6 in single-run contexts); others refused */
+                                 in a batch 5 and 6 need lr_links); others refused */
     double friction;          /* Coulomb coefficient; <0 stick; 0 frictionless */
     double contact_cutoff;    /* position-based contact cutoff (cells); <0 displacement based */
     double rigid_gradient_bias;
@@ -259,6 +259,16 @@ int64_t mpmgpu_archive_record_size(int32_t dim, const char *mpm_order);
 int mpmgpu_archive_records(MpmGpuCtx *ctx, const char *mpm_order, double thickness, void *host_records,
                            int64_t capacity);
 
+/* The same records without waiting for them: packed in stream order after the
+ * steps enqueued so far, then copied to host_records on a copy stream while
+ * later mpmgpu_step calls run.  host_records should be pinned
+ * (mpmgpu_host_register); it must stay valid and is complete only after
+ * mpmgpu_archive_wait.  A later archive call waits for this copy first. */
+int mpmgpu_archive_records_async(MpmGpuCtx *ctx, const char *mpm_order, double thickness, void *host_records,
+                                 int64_t capacity);
+/* Wait for the copy of the last mpmgpu_archive_records_async (no-op if none). */
+int mpmgpu_archive_wait(MpmGpuCtx *ctx);
+
 /* ---- extensions without a counterpart in the reference ----------------------
  * Host-integration and measurement helpers of this library; a NairnMPM
  * integration does not need them. */
@@ -317,6 +327,12 @@ typedef struct {
     int32_t inc_defgrad_terms;/* Exponential() terms of hyperelastic F (0: 2 in 2D, 1 in 3D) */
     int32_t max_fields;       /* material velocity fields per run (0, 1: single
                                  material mode; up to 8 for multimaterial contact) */
+    int32_t lr_links;         /* particle-to-contact-node links reserved per
+                                 particle slot for regression normals (methods
+                                 5, 6; needs max_fields >= 2): 0 refuses those
+                                 methods; 64 in 3D, 16 in 2D always suffice; a
+                                 run whose links do not fit fails with
+                                 MPMGPU_ERR_RANGE */
 } MpmGpuBatchOptions;
 
 /* run states returned by mpmgpu_batch_run_state; a failed run reports the
@@ -393,6 +409,8 @@ typedef struct {
     int32_t order;              /* admission order: 0 arrival (FIFO), 1 least
                                    work first (particles x steps)            */
     int32_t max_fields;         /* material velocity fields per run (0: 1)     */
+    int32_t lr_links;           /* links per particle slot for regression normals
+                                   (MpmGpuBatchOptions; capped at 16 in 2D)   */
 } MpmGpuServerOptions;
 
 enum { MPMGPU_REQ_QUEUED = 1, MPMGPU_REQ_RUNNING = 2, MPMGPU_REQ_DONE = 3, MPMGPU_REQ_FAILED = 4 };

@@ -70,6 +70,7 @@ struct BatchRun {
     int np = 0;
     long long node_base = 0, nnodes = 0, cell_base = 0, nelems = 0, mat_base = 0, nmat = 0;
     int steps_total = 0, steps_done = 0;
+    bool lr = false;               // regression contact normals (methods 5, 6)
     std::vector<MpmGpuVelBC> bcs;  // batch-global 1-based node numbers
 };
 
@@ -191,6 +192,11 @@ struct MpmGpuBatch {
     int *keys[2] = {nullptr, nullptr}, *vals[2] = {nullptr, nullptr}, *hist = nullptr, *sums = nullptr;
     int sort_bits = 1;
     long long since_sort = 1LL << 40;
+    // regression-normal links (lr_links per particle slot) and results
+    int *lr_cnt = nullptr, *lr_start = nullptr, *lr_list = nullptr, *lr_sums = nullptr;
+    double *lr_out = nullptr;
+    long long lr_cap = 0;
+    int lr_runs = 0;  // resident runs with regression normals
     // materials, runs, velocity conditions
     DevMat *mats = nullptr;
     DevRun *runs_dev = nullptr;
@@ -260,7 +266,8 @@ void batch_free(MpmGpuBatch *b) {
     batch_drop_graphs(b);
     void *ptrs[] = {b->pbuf[0], b->pbuf[1], b->ibuf[0], b->ibuf[1], b->nblock, b->fblock, b->coords, b->nrun,
                     b->bc_group, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->sums, b->mats,
-                    b->runs_dev, b->bc_block, b->flag, b->cpdi};
+                    b->runs_dev, b->bc_block, b->flag, b->cpdi, b->lr_cnt, b->lr_start, b->lr_list, b->lr_sums,
+                    b->lr_out};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -376,19 +383,43 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     sp.nrun = b->nrun;
     sp.ct.nf = b->nf;
     sp.ct.fstride = b->ncap;
+    sp.ct.lr = b->lr_out;
     k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN, b->nf, b->ncap);
     k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    const bool lr = b->lr_runs > 0;
+    auto lr_normals = [&]() {
+        k_lr_normals<DIM, true><<<(NN * 32 + NTB - 1) / NTB, NTB, 0, s>>>(sp, b->p, b->nd, b->mats, b->lr_start,
+                                                                         b->lr_list, b->lr_out, NN, b->lr_cap, 1);
+    };
+    if (lr) {
+        // link the particles of regression-normal runs to their contact nodes
+        const int m = NN + 1, nsb = (m + kScanChunk - 1) / kScanChunk;
+        cudaMemsetAsync(b->lr_cnt, 0, (size_t)m * sizeof(int), s);
+        k_lr_link<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->lr_cnt, b->lr_start, b->lr_list,
+                                                           b->lr_cap, 0);
+        cudaMemcpyAsync(b->lr_start, b->lr_cnt, (size_t)m * sizeof(int), cudaMemcpyDeviceToDevice, s);
+        k_scan_reduce<<<nsb, kScanBlock, 0, s>>>(b->lr_start, m, b->lr_sums);
+        k_scan_sums<<<1, kScanBlock, 0, s>>>(b->lr_sums, nsb);
+        k_scan_apply<<<nsb, kScanBlock, 0, s>>>(b->lr_start, m, b->lr_sums);
+        cudaMemsetAsync(b->lr_cnt, 0, (size_t)m * sizeof(int), s);
+        k_lr_link<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->lr_cnt, b->lr_start, b->lr_list,
+                                                           b->lr_cap, 1);
+        k_lr_order<<<nb, NTB, 0, s>>>(b->lr_start, b->lr_list, b->orig, NN, b->lr_cap);
+        lr_normals();
+    }
     k_node_post<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, method != MPMGPU_USL);
     if (method == MPMGPU_USL)
         k_strain_forces<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     else
         k_strain_forces<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    if (lr) lr_normals();  // the deformed radii changed with the strain update
     k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group,
                                                     b->nf > 1 && method != MPMGPU_USF);
     if (method == MPMGPU_USF) {
         k_g2p<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     } else {
         k_g2p<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+        if (lr) lr_normals();  // the particles moved
         k_node_usl<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group);
         k_strain_last<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     }
@@ -408,7 +439,10 @@ void batch_enqueue_any(MpmGpuBatch *b) {
     else mix ? batch_enqueue_shape<2, true>(b) : batch_enqueue_shape<2, false>(b);
 }
 
-int batch_step_launches(const MpmGpuBatch *b) { return b->o.method == MPMGPU_USF ? 7 : 9; }
+int batch_step_launches(const MpmGpuBatch *b) {
+    const bool usf = b->o.method == MPMGPU_USF;
+    return (usf ? 7 : 9) + (b->lr_runs > 0 ? 6 + (usf ? 2 : 3) : 0);
+}
 
 long long batch_graph_key(const MpmGpuBatch *b) {
     return ((b->layout * 1000003LL + b->n_used) * 1000003LL + b->node_used) * 1031LL + b->tb;
@@ -466,6 +500,7 @@ int batch_prepare(MpmGpuBatch *b) {
 }
 
 int batch_status(unsigned bits) {
+    if (bits & ERR_RANGE) return MPMGPU_ERR_RANGE;  // a cause: what follows it may be NaN
     if (bits & ERR_NAN) return MPMGPU_ERR_NAN;
     if (bits & (ERR_LEFT_GRID | ERR_EDGE)) return MPMGPU_ERR_LEFT_GRID;
     if (bits & ERR_CPDI_NODES) return MPMGPU_ERR_CPDI_NODES;
@@ -573,6 +608,11 @@ int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *o) {
     bytes += N * nf * (int64_t)((nf > 1 ? 26 : 19) * sizeof(double) + 12 * sizeof(float) + 1);
     bytes += N * (int64_t)(2 * sizeof(int) + sizeof(double));
     bytes += (int64_t)o->max_materials * (int64_t)sizeof(DevMat) + (int64_t)o->max_runs * (int64_t)sizeof(DevRun);
+    if (nf > 1 && o->lr_links > 0) {
+        // regression-normal links, counts, offsets, scan sums, results
+        bytes += P * o->lr_links * (int64_t)sizeof(int) + 2 * (N + 1) * (int64_t)sizeof(int);
+        bytes += ((N + 1 + kScanChunk - 1) / kScanChunk + 1) * (int64_t)sizeof(int) + 4 * N * nf * (int64_t)sizeof(double);
+    }
     return bytes;
 }
 
@@ -589,6 +629,7 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "precision must be MPMGPU_PREC_FP64 or MPMGPU_PREC_MIXED");
     if (o->max_fields < 0 || o->max_fields > kMaxFields)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "max_fields must be 0 to 8");
+    if (o->lr_links < 0 || o->lr_links > 64) return berr(nullptr, MPMGPU_ERR_INVALID, "lr_links must be 0 to 64");
     if (o->max_particles <= 0 || o->max_particles > (1LL << 31) - 1 || o->max_nodes <= 0 ||
         o->max_nodes > (1LL << 30) || o->max_runs <= 0 || o->max_runs > (1 << 20) || o->max_materials <= 0 ||
         o->max_materials > (1 << 24))
@@ -629,7 +670,16 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     A((void **)&b->mats, (size_t)o->max_materials * sizeof(DevMat));
     A((void **)&b->runs_dev, (size_t)o->max_runs * sizeof(DevRun));
     A((void **)&b->flag, sizeof(unsigned));
+    if (b->nf > 1 && o->lr_links > 0) {
+        b->lr_cap = (long long)P * o->lr_links;
+        A((void **)&b->lr_cnt, (N + 1) * sizeof(int));
+        A((void **)&b->lr_start, (N + 1) * sizeof(int));
+        A((void **)&b->lr_sums, ((N + 1 + kScanChunk - 1) / kScanChunk + 1) * sizeof(int));
+        A((void **)&b->lr_list, (size_t)b->lr_cap * sizeof(int));
+        A((void **)&b->lr_out, 4 * NT * sizeof(double));
+    }
     if (e == cudaSuccess) e = cudaMemsetAsync(b->nblock, 0, NT * ncols * sizeof(double) + NT, b->stream);
+    if (e == cudaSuccess && b->lr_out) e = cudaMemsetAsync(b->lr_out, 0, 4 * NT * sizeof(double), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->fblock, 0, NT * 12 * sizeof(float), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->nrun, 0xFF, N * sizeof(int), b->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(b->bc_group, 0xFF, N * sizeof(int), b->stream);
@@ -709,8 +759,10 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
         return berr(b, MPMGPU_ERR_INVALID, "a run with several material fields needs multimaterial contact");
     if (mm) {
         if (b->nf < 2) return berr(b, MPMGPU_ERR_INVALID, "contact needs a batch with max_fields >= 2");
-        if (contact->normals < 0 || contact->normals > 2)
-            return berr(b, MPMGPU_ERR_UNSUPPORTED, "contact normals: methods 0, 1 and 2 are implemented");
+        if (contact->normals < 0 || (contact->normals > 2 && contact->normals < 5) || contact->normals > 6)
+            return berr(b, MPMGPU_ERR_UNSUPPORTED, "contact normals: methods 0, 1, 2, 5 and 6 are implemented");
+        if (contact->normals >= 5 && b->lr_cap == 0)
+            return berr(b, MPMGPU_ERR_INVALID, "regression contact normals need a batch with lr_links > 0");
         if (contact->contact_cutoff > 0.)
             return berr(b, MPMGPU_ERR_UNSUPPORTED, "position-based contact is not implemented on the device");
     }
@@ -809,6 +861,8 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     br.nmat = nmat;
     br.steps_total = nsteps;
     br.state = MPMGPU_RUN_RUNNING;
+    br.lr = mm && contact->normals >= 5;
+    b->lr_runs += br.lr ? 1 : 0;
     br.bcs.reserve((size_t)nbc);
     for (int k = 0; k < nbc; k++) {
         MpmGpuVelBC bc = bcs[k];
@@ -900,6 +954,7 @@ int mpmgpu_batch_remove_run(MpmGpuBatch *b, int32_t run_id, MpmGpuParticles *out
     b->cells.release(br.cell_base, br.nelems);
     b->matslots.release(br.mat_base, br.nmat);
     b->node_used = (int)b->nodes.high_water();
+    b->lr_runs -= br.lr ? 1 : 0;
     br = BatchRun{};
     b->bcs_dirty = true;
     b->layout++;

@@ -60,6 +60,9 @@ struct MpmGpuCtx {
     nmg::DevDet det{nullptr, 0, nullptr, nullptr};     // deterministic node sums (p2g option 1)
     void *archive_buf = nullptr;         // device staging of archive records
     size_t archive_cap = 0;
+    cudaStream_t archive_stream = nullptr;  // copies of packed records to the host
+    cudaEvent_t archive_packed = nullptr, archive_copied = nullptr;
+    bool archive_pending = false;           // an asynchronous copy not yet waited for
     // regression contact normals: link counts, offsets, links, results, scan scratch
     int *lr_cnt = nullptr, *lr_start = nullptr, *lr_list = nullptr, *lr_sums = nullptr;
     double *lr_out = nullptr;

@@ -15,7 +15,9 @@
 // slots sorted by the particles' host order (the reference's particle order),
 // and the result (nx, ny, nz, deln) per material field of each node.  One warp
 // per node does the regressions; its sums over the linked particles are warp
-// reductions.
+// reductions.  In a batch (BATCH = true) the nodes and particles of runs with
+// other normal methods have no links, and a node's particles all belong to the
+// node's run, so host order is the run's upload order.
 #pragma once
 
 namespace nmg {
@@ -30,10 +32,11 @@ __device__ __forceinline__ bool lr_contact_node(const StepParams &sp, const DevN
 // the distinct shape-function nodes of particle i with nonzero weight, as the
 // step's transfers visit them
 template <int DIM, int SHAPE, bool MIX>
-__device__ __forceinline__ int lr_particle_nodes(const DevGrid &g, const DevParticles &p, int i, int out[64]) {
+__device__ __forceinline__ int lr_particle_nodes(const DevGrid &g, int nb, const DevParticles &p, int i,
+                                                 int out[64]) {
     using T = typename Wt<MIX>::T;
     int cnt = 0;
-    visit_nodes<DIM, SHAPE, false, T>(g, 0, p, i, [&](int n, T N, T, T, T) {
+    visit_nodes<DIM, SHAPE, false, T>(g, nb, p, i, [&](int n, T N, T, T, T) {
         if (N == T(0)) return;
         for (int k = 0; k < cnt; k++)
             if (out[k] == n) return;
@@ -43,27 +46,36 @@ __device__ __forceinline__ int lr_particle_nodes(const DevGrid &g, const DevPart
 }
 
 // pass 0 counts the links of each contact node; pass 1 writes them at the
-// node's offset (cnt cleared in between serves as the cursor)
-template <int DIM, int SHAPE, bool MIX>
+// node's offset (cnt cleared in between serves as the cursor).  Links past
+// `cap` are dropped and fail the particle's run with ERR_RANGE.
+template <int DIM, int SHAPE, bool MIX, bool BATCH>
 static __global__ void __launch_bounds__(256) k_lr_link(StepParams sp, DevParticles p, DevNodes nd, int *cnt,
-                                                        const int *start, int *list, int pass) {
+                                                        const int *start, int *list, long long cap, int pass) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
+    RunView rv;
+    if (!particle_run<BATCH>(sp, p, i, rv)) return;
+    if (BATCH && sp.runs[p.run[i]].normals < 5) return;
     int nodes[64];
-    const int m = lr_particle_nodes<DIM, SHAPE, MIX>(sp.g, p, i, nodes);
+    const int m = lr_particle_nodes<DIM, SHAPE, MIX>(rv.g, rv.nb, p, i, nodes);
     for (int k = 0; k < m; k++) {
         const int n = nodes[k];
         if (!lr_contact_node(sp, nd, n)) continue;
         const int slot = atomicAdd(cnt + n, 1);
-        if (pass == 1) list[start[n] + slot] = i;
+        if (pass == 1) {
+            const long long at = (long long)start[n] + slot;
+            if (at < cap) list[at] = i;
+            else atomicOr(rv.err, ERR_RANGE);
+        }
     }
 }
 
 // each node's links in the particles' host order (insertion sort)
-static __global__ void k_lr_order(const int *start, int *list, const int *orig, int nnodes) {
+static __global__ void k_lr_order(const int *start, int *list, const int *orig, int nnodes, long long cap) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes) return;
     const int s0 = start[n], s1 = start[n + 1];
+    if (s1 > cap) return;  // dropped links (the run has failed)
     for (int k = s0 + 1; k < s1; k++) {
         const int v = list[k], key = orig[v];
         int j = k - 1;
@@ -173,18 +185,28 @@ __device__ __forceinline__ double lr_radius(const DevGrid &g, const DevParticles
 // of MachineLearning.cpp with PENALIZE_NORMALS: linear offset penalty 0.1;
 // logistic normal penalty 1e-7 cell^2, no offset penalty, the linear beta
 // doubled as the start, convergence 1 - cos < 1e-5 within 15 iterations.
-template <int DIM>
+template <int DIM, bool BATCH>
 static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevParticles p, DevNodes nd,
                                                            const DevMat *mats, const int *start, const int *list,
-                                                           double *out, int nnodes, int logistic) {
+                                                           double *out, int nnodes, long long cap, int logistic) {
     const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
     const int lane = threadIdx.x & 31;
     if (n >= nnodes) return;  // whole warps
     const int s0 = start[n], s1 = start[n + 1];
-    if (s1 == s0) return;
-    const DevGrid &g = sp.g;
+    if (s1 == s0 || s1 > cap) return;
+    DevGrid g = sp.g;
+    int nl = n;  // the node's index in its grid
+    if (BATCH) {
+        const int r = sp.nrun[n];
+        if (r < 0) return;
+        const DevRun &R = sp.runs[r];
+        if (!R.active || R.normals < 5) return;
+        g = R.g;
+        nl = n - R.node_base;
+        logistic = R.normals == 6 ? 1 : 0;
+    }
     const int nx1 = g.nx + 1, ny1 = g.ny + 1;
-    const double ndx = g.xn[n % nx1], ndy = g.yn[(n / nx1) % ny1], ndz = DIM == 3 ? g.zn[n / (nx1 * ny1)] : 0.;
+    const double ndx = g.xn[nl % nx1], ndy = g.yn[(nl / nx1) % ny1], ndz = DIM == 3 ? g.zn[nl / (nx1 * ny1)] : 0.;
     double cell = fmin(g.gx, g.gy);
     if (DIM == 3) cell = fmin(cell, g.gz);
     const double cell2 = cell * cell;

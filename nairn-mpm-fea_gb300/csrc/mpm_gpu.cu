@@ -741,24 +741,34 @@ int64_t mpmgpu_archive_record_size(int32_t dim, const char *mpm_order) {
     return L.rec;
 }
 
-int mpmgpu_archive_records(MpmGpuCtx *c, const char *mpm_order, double thickness, void *host_records,
-                           int64_t capacity) {
-    if (!c || !host_records) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_archive_records: null argument");
-    if (c->p.n <= 0 || !c->mats) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_archive_records: no particles");
+namespace {
+
+// pack the records of the current state into the staging buffer on the
+// context stream; *bytes receives their size
+int archive_pack(MpmGpuCtx *c, const char *what, const char *mpm_order, double thickness, const void *host_records,
+                 int64_t capacity, size_t *bytes) {
+    const std::string w(what);
+    if (!c || !host_records) return set_err(c, MPMGPU_ERR_INVALID, w + ": null argument");
+    if (c->p.n <= 0 || !c->mats) return set_err(c, MPMGPU_ERR_INVALID, w + ": no particles");
     ArchiveLayout L{};
     std::string why;
     const int st = archive_layout(c->dim, mpm_order, L, why);
-    if (st != MPMGPU_OK) return set_err(c, st, "mpmgpu_archive_records: " + why);
+    if (st != MPMGPU_OK) return set_err(c, st, w + ": " + why);
     L.thickness = thickness;
-    const size_t bytes = (size_t)c->p.n * L.rec;
-    if (capacity < (int64_t)bytes) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_archive_records: buffer too small");
-    if (c->archive_cap < bytes) {
+    *bytes = (size_t)c->p.n * L.rec;
+    if (capacity < (int64_t)*bytes) return set_err(c, MPMGPU_ERR_INVALID, w + ": buffer too small");
+    if (c->archive_pending) {
+        // the previous asynchronous copy still reads the staging buffer
+        const int ws = mpmgpu_archive_wait(c);
+        if (ws != MPMGPU_OK) return ws;
+    }
+    if (c->archive_cap < *bytes) {
         if (c->archive_buf) cudaFree(c->archive_buf);
         c->archive_buf = nullptr;
         c->archive_cap = 0;
-        cudaError_t e = cudaMalloc(&c->archive_buf, bytes);
+        cudaError_t e = cudaMalloc(&c->archive_buf, *bytes);
         if (e != cudaSuccess) return set_err(c, MPMGPU_ERR_OOM, "archive staging buffer");
-        c->archive_cap = bytes;
+        c->archive_cap = *bytes;
     }
     const int TB = 256, nb = (c->p.n + TB - 1) / TB;
     if (c->dim == 3)
@@ -766,9 +776,49 @@ int mpmgpu_archive_records(MpmGpuCtx *c, const char *mpm_order, double thickness
     else
         k_archive_pack<2><<<nb, TB, 0, c->stream>>>(L, c->p, c->orig, c->mats, (char *)c->archive_buf);
     c->launches++;
+    CK(cudaGetLastError());
+    return MPMGPU_OK;
+}
+
+}  // namespace
+
+int mpmgpu_archive_records(MpmGpuCtx *c, const char *mpm_order, double thickness, void *host_records,
+                           int64_t capacity) {
+    size_t bytes = 0;
+    const int st = archive_pack(c, "mpmgpu_archive_records", mpm_order, thickness, host_records, capacity, &bytes);
+    if (st != MPMGPU_OK) return st;
     CK(cudaMemcpyAsync(host_records, c->archive_buf, bytes, cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));
     CK(cudaGetLastError());
+    return MPMGPU_OK;
+}
+
+int mpmgpu_archive_records_async(MpmGpuCtx *c, const char *mpm_order, double thickness, void *host_records,
+                                 int64_t capacity) {
+    size_t bytes = 0;
+    const int st =
+        archive_pack(c, "mpmgpu_archive_records_async", mpm_order, thickness, host_records, capacity, &bytes);
+    if (st != MPMGPU_OK) return st;
+    if (!c->archive_stream) {
+        CK(cudaStreamCreateWithFlags(&c->archive_stream, cudaStreamNonBlocking));
+        CK(cudaEventCreateWithFlags(&c->archive_packed, cudaEventDisableTiming));
+        CK(cudaEventCreateWithFlags(&c->archive_copied, cudaEventDisableTiming));
+    }
+    // the copy waits for the pack; later steps on the context stream do not
+    // wait for the copy (the next pack does)
+    CK(cudaEventRecord(c->archive_packed, c->stream));
+    CK(cudaStreamWaitEvent(c->archive_stream, c->archive_packed, 0));
+    CK(cudaMemcpyAsync(host_records, c->archive_buf, bytes, cudaMemcpyDeviceToHost, c->archive_stream));
+    CK(cudaEventRecord(c->archive_copied, c->archive_stream));
+    c->archive_pending = true;
+    return MPMGPU_OK;
+}
+
+int mpmgpu_archive_wait(MpmGpuCtx *c) {
+    if (!c) return set_err(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_archive_wait: null context");
+    if (!c->archive_pending) return MPMGPU_OK;
+    c->archive_pending = false;
+    CK(cudaEventSynchronize(c->archive_copied));
     return MPMGPU_OK;
 }
 
@@ -782,7 +832,11 @@ void mpmgpu_destroy(MpmGpuCtx *c) {
     if (c->bc_group) cudaFree(c->bc_group);
     if (c->bc_block) cudaFree(c->bc_block);
     if (c->err) cudaFree(c->err);
+    if (c->archive_pending) cudaEventSynchronize(c->archive_copied);
     if (c->archive_buf) cudaFree(c->archive_buf);
+    if (c->archive_packed) cudaEventDestroy(c->archive_packed);
+    if (c->archive_copied) cudaEventDestroy(c->archive_copied);
+    if (c->archive_stream) cudaStreamDestroy(c->archive_stream);
     for (void *q : {(void *)c->lr_cnt, (void *)c->lr_start, (void *)c->lr_list, (void *)c->lr_sums, (void *)c->lr_out})
         if (q) cudaFree(q);
     if (c->det.lim) cudaFree(c->det.lim);

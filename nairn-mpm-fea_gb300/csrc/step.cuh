@@ -54,22 +54,24 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     const bool lr = c->ct.nf > 1 && c->ct.normals >= 5;
     const int lrb = (NN * 32 + TB - 1) / TB;  // a warp per node
     auto lr_normals = [&]() {
-        k_lr_normals<DIM><<<lrb, TB, 0, s>>>(sp, c->p, c->nd, c->mats, c->lr_start, c->lr_list, c->lr_out, NN,
-                                             c->ct.normals == 6 ? 1 : 0);
+        k_lr_normals<DIM, false><<<lrb, TB, 0, s>>>(sp, c->p, c->nd, c->mats, c->lr_start, c->lr_list, c->lr_out,
+                                                    NN, c->lr_cap, c->ct.normals == 6 ? 1 : 0);
         c->launches++;
     };
     if (lr) {
         // link the particles to the contact nodes, in the particles' host order
         const int m = NN + 1, nsb = (m + kScanChunk - 1) / kScanChunk;
         cudaMemsetAsync(c->lr_cnt, 0, (size_t)m * sizeof(int), s);
-        k_lr_link<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->lr_cnt, c->lr_start, c->lr_list, 0);
+        k_lr_link<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->lr_cnt, c->lr_start, c->lr_list,
+                                                            c->lr_cap, 0);
         cudaMemcpyAsync(c->lr_start, c->lr_cnt, (size_t)m * sizeof(int), cudaMemcpyDeviceToDevice, s);
         k_scan_reduce<<<nsb, kScanBlock, 0, s>>>(c->lr_start, m, c->lr_sums);
         k_scan_sums<<<1, kScanBlock, 0, s>>>(c->lr_sums, nsb);
         k_scan_apply<<<nsb, kScanBlock, 0, s>>>(c->lr_start, m, c->lr_sums);
         cudaMemsetAsync(c->lr_cnt, 0, (size_t)m * sizeof(int), s);
-        k_lr_link<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->lr_cnt, c->lr_start, c->lr_list, 1);
-        k_lr_order<<<nb, TB, 0, s>>>(c->lr_start, c->lr_list, c->orig, NN);
+        k_lr_link<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->lr_cnt, c->lr_start, c->lr_list,
+                                                            c->lr_cap, 1);
+        k_lr_order<<<nb, TB, 0, s>>>(c->lr_start, c->lr_list, c->orig, NN, c->lr_cap);
         c->launches += 6;
         lr_normals();
     }

@@ -144,7 +144,8 @@ class MpmGpuBatchOptions(C.Structure):
     _fields_ = [("np", C.c_int32), ("method", C.c_int32), ("shape", C.c_int32), ("precision", C.c_int32),
                 ("sort_interval", C.c_int32), ("block", C.c_int32), ("max_runs", C.c_int32),
                 ("max_materials", C.c_int32), ("max_particles", C.c_int64), ("max_nodes", C.c_int64),
-                ("fraction_usf", C.c_double), ("inc_defgrad_terms", C.c_int32), ("max_fields", C.c_int32)]
+                ("fraction_usf", C.c_double), ("inc_defgrad_terms", C.c_int32), ("max_fields", C.c_int32),
+                ("lr_links", C.c_int32)]
 
 
 class MpmGpuBatchInfo(C.Structure):
@@ -161,7 +162,8 @@ class MpmGpuServerOptions(C.Structure):
                 ("steps_per_round", C.c_int32), ("backfill", C.c_int32), ("sort_interval", C.c_int32),
                 ("block", C.c_int32), ("hbm_budget_bytes", C.c_int64), ("frac_3d", C.c_double),
                 ("nodes_per_particle", C.c_double), ("fraction_usf", C.c_double),
-                ("max_resident_particles", C.c_int64), ("order", C.c_int32), ("max_fields", C.c_int32)]
+                ("max_resident_particles", C.c_int64), ("order", C.c_int32), ("max_fields", C.c_int32),
+                ("lr_links", C.c_int32)]
 
 
 class MpmGpuRequestInfo(C.Structure):

@@ -59,6 +59,10 @@ def lib():
     L.mpmgpu_archive_record_size.restype = C.c_int64
     L.mpmgpu_archive_records.argtypes = [C.c_void_p, C.c_char_p, C.c_double, C.c_void_p, C.c_int64]
     L.mpmgpu_archive_records.restype = C.c_int
+    L.mpmgpu_archive_records_async.argtypes = [C.c_void_p, C.c_char_p, C.c_double, C.c_void_p, C.c_int64]
+    L.mpmgpu_archive_records_async.restype = C.c_int
+    L.mpmgpu_archive_wait.argtypes = [C.c_void_p]
+    L.mpmgpu_archive_wait.restype = C.c_int
     L.mpmgpu_step_timed.restype = C.c_int
     L.mpmgpu_launch_count.argtypes = [C.c_void_p]
     L.mpmgpu_launch_count.restype = C.c_longlong
@@ -113,6 +117,7 @@ def lib():
 
 # every symbol the header declares (checked by the CPU tests)
 EXPORTED = ("mpmgpu_step_timed", "mpmgpu_autotune_sort", "mpmgpu_archive_record_size", "mpmgpu_archive_records",
+            "mpmgpu_archive_records_async", "mpmgpu_archive_wait",
             "mpmgpu_set_profiling", "mpmgpu_stream", "mpmgpu_launch_count",
             "mpmgpu_host_register", "mpmgpu_host_unregister", "mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
             "mpmgpu_set_velocity_bcs", "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles",
@@ -183,6 +188,16 @@ class GpuRun:
                                              buf.ctypes.data_as(C.c_void_p), buf.nbytes))
         return buf.tobytes()
 
+    def archive_records_async(self, order: str, buf: np.ndarray, thickness: float = 1.0):
+        """Start packing the records of the current state into `buf` (uint8,
+        n * record size bytes, best pinned with pin()); they are complete
+        after archive_wait(), while steps may run meanwhile."""
+        self._check(lib().mpmgpu_archive_records_async(self.h, order.encode("ascii"), float(thickness),
+                                                       buf.ctypes.data_as(C.c_void_p), buf.nbytes))
+
+    def archive_wait(self):
+        self._check(lib().mpmgpu_archive_wait(self.h))
+
     def launch_count(self) -> int:
         return int(lib().mpmgpu_launch_count(self.h))
 
@@ -223,6 +238,15 @@ class GpuRun:
             pass
 
 
+def lr_links_for(models) -> int:
+    """Links per particle slot a batch of `models` reserves for regression
+    contact normals: every shape-function node of a particle (64 in 3D, 16 in
+    2D) when one of them uses methods 5 or 6, else none."""
+    if not any(((m.extra or {}).get("contact") or {}).get("normals", 0) >= 5 for m in models):
+        return 0
+    return 64 if models[0].grid.dim == 3 else 16
+
+
 class GpuBatch:
     """Many independent runs resident on the current GPU, advanced together by
     one graph-captured batched step (mpmgpu_batch_* in the C ABI).  All runs
@@ -232,11 +256,12 @@ class GpuBatch:
 
     def __init__(self, np_: int, method: int, shape: int, precision: int = 0, *, max_runs: int,
                  max_particles: int, max_nodes: int, max_materials: int | None = None, sort_interval: int = 1,
-                 block: int = 0, fraction_usf: float = 0.5, inc_defgrad_terms: int = 0, max_fields: int = 1):
+                 block: int = 0, fraction_usf: float = 0.5, inc_defgrad_terms: int = 0, max_fields: int = 1,
+                 lr_links: int = 0):
         L = lib()
         self.opts = abi.MpmGpuBatchOptions(np_, method, shape, precision, sort_interval, block, max_runs,
                                            max_materials or max_runs, max_particles, max_nodes, fraction_usf,
-                                           inc_defgrad_terms, max_fields)
+                                           inc_defgrad_terms, max_fields, lr_links)
         self.bytes = int(L.mpmgpu_batch_bytes(C.byref(self.opts)))
         h = C.c_void_p()
         st = L.mpmgpu_batch_create(C.byref(self.opts), C.byref(h))
@@ -254,7 +279,8 @@ class GpuBatch:
                    max_nodes=int(slack * sum(m.grid.nnodes for m in models)),
                    max_materials=int(slack * sum(len(m.materials) for m in models)) + 1,
                    fraction_usf=o.get("fraction_usf", 0.5), inc_defgrad_terms=o.get("inc_defgrad_terms", 0),
-                   max_fields=kw.pop("max_fields", max(m.options.get("nfields", 1) for m in models)), **kw)
+                   max_fields=kw.pop("max_fields", max(m.options.get("nfields", 1) for m in models)),
+                   lr_links=kw.pop("lr_links", lr_links_for(models)), **kw)
 
     @staticmethod
     def bytes_for(models, precision: int = 0) -> int:
@@ -262,7 +288,7 @@ class GpuBatch:
         opts = abi.MpmGpuBatchOptions(o["np"], o["method"], o["shape"], precision, 1, 0, len(models),
                                       sum(len(m.materials) for m in models) + 1, sum(m.n for m in models),
                                       sum(m.grid.nnodes for m in models), 0.5, o.get("inc_defgrad_terms", 0),
-                                      max(m.options.get("nfields", 1) for m in models))
+                                      max(m.options.get("nfields", 1) for m in models), lr_links_for(models))
         return int(lib().mpmgpu_batch_bytes(C.byref(opts)))
 
     def _check(self, st):
@@ -349,12 +375,12 @@ class GpuServer:
     def __init__(self, method: int, shape: int, precision: int = 1, *, hbm_budget_bytes: int,
                  max_runs: int = 256, steps_per_round: int = 10, backfill: bool = True, sort_interval: int = 1,
                  block: int = 0, frac_3d: float = 0.5, nodes_per_particle: float = 0.5, fraction_usf: float = 0.5,
-                 max_resident_particles: int = 0, order: str = "fifo", max_fields: int = 1):
+                 max_resident_particles: int = 0, order: str = "fifo", max_fields: int = 1, lr_links: int = 0):
         L = lib()
         o = abi.MpmGpuServerOptions(method, shape, precision, max_runs, steps_per_round, 1 if backfill else 0,
                                     sort_interval, block, int(hbm_budget_bytes), frac_3d, nodes_per_particle,
                                     fraction_usf, int(max_resident_particles),
-                                    {"fifo": 0, "least_work": 1}[order], int(max_fields))
+                                    {"fifo": 0, "least_work": 1}[order], int(max_fields), int(lr_links))
         h = C.c_void_p()
         st = L.mpmgpu_server_create(C.byref(o), C.byref(h))
         if st != 0:

@@ -41,6 +41,9 @@ def main(argv=None):
     ap.add_argument("--runs", type=int, default=64, help="runs of the batch workloads")
     ap.add_argument("--plate", type=int, nargs=3, default=(64, 64, 16), help="plate cells (contact3d)")
     ap.add_argument("--block", type=int, nargs=3, default=(20, 20, 8), help="block cells (contact3d)")
+    ap.add_argument("--normals", type=int, choices=(0, 1, 2, 5, 6), default=2,
+                    help="contact normal method (contact3d): 0-2 volume gradients, 5/6 regressions")
+    ap.add_argument("--gap", type=float, default=0.0, help="block-to-plate gap in mm (contact3d)")
     ap.add_argument("--p2g", choices=("atomic", "deterministic"), default="atomic")
     ap.add_argument("--profile", action="store_true", help="per-kernel ms of the timed steps (single runs)")
     a = ap.parse_args(argv)
@@ -72,7 +75,8 @@ def main(argv=None):
             bx0 = 0.5 * (a.plate[0] - a.block[0]) * 0.5
             by0 = 0.5 * (a.plate[1] - a.block[1]) * 0.5
             m = model.contact_3d(plate=tuple(a.plate), block=tuple(a.block), block_x0=bx0, block_y0=by0, cell=0.5,
-                                 v=(4000., 0., -4000.), steps=total, gimp="lCPDI", friction=0.3, normals=2)
+                                 v=(4000., 0., -4000.), steps=total, gimp="lCPDI", friction=0.3, normals=a.normals,
+                                 gap=a.gap)
         else:
             m = model.block_3d(ncx=a.cells, ncy=a.cells, ncz=a.cells, steps=total)
         r = gpu.GpuRun(m, precision=prec, sort_interval=a.sort_interval, p2g=1 if a.p2g == "deterministic" else 0)
@@ -89,6 +93,8 @@ def main(argv=None):
     out["precision"] = a.precision
     out["sort_interval"] = a.sort_interval
     out["p2g"] = a.p2g
+    if a.workload == "contact3d":
+        out["normals"] = a.normals
     print(json.dumps(out))
     return 0
 

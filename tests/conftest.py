@@ -45,6 +45,25 @@ def rel_l2(a, b):
     return float(np.linalg.norm(a - b) / (nb if nb > 0 else 1.0))
 
 
+def regression_sensitivity(m, steps):
+    """How far the reference's own result moves (relative L2 per quantity)
+    when the initial velocities are perturbed by 1e-9 relative: regression
+    contact normals decide contact from point-cloud supports that sit near
+    zero separation, so such a run is chaotic -- the oracle, which matches the
+    reference to 1e-13, shows it."""
+    import oracle_lib
+    from nairn_gb300 import abi
+    outs = []
+    for eps in (0., 1e-9):
+        p = abi.copy_particles(m.particles)
+        rng = np.random.default_rng(1)
+        for k in ("vx", "vy"):
+            p[k] = p[k] * (1. + eps * rng.standard_normal(p[k].shape))
+        oracle_lib.run(m, p, steps, nthreads=4)
+        outs.append(view_for(p, m))
+    return {k: rel_l2(outs[1][k], outs[0][k]) for k in ("pos", "vel", "stress", "strain")}
+
+
 def archive_view(p, dim, rho_gcc, mat_type=1):
     """Particle dict -> the quantities a NairnMPM archive stores (ArchiveData.cpp:807-930).
     The stress is (s - P) rho0 / J, with J the relative volume: 1 for the

@@ -42,3 +42,35 @@ def test_create_rejects_bad_options_without_gpu_work(gpu_lib):
     st = gpu_lib.mpmgpu_create(C.byref(g), C.byref(o), C.byref(h))
     assert st == 2 and not h.value
     assert b"p2g" in gpu_lib.mpmgpu_last_error(None)
+
+
+def test_ctypes_structs_match_the_header(tmp_path):
+    """Every POD struct of the header has the size and field offsets of its
+    ctypes mirror (compiled with the host C compiler from the header)."""
+    import shutil
+    import subprocess
+    import sys
+    if shutil.which("gcc") is None:
+        import pytest
+        pytest.skip("no host C compiler")
+    sys.path.insert(0, os.path.join(ROOT, "nairn-mpm-fea_gb300", "python"))
+    from nairn_gb300 import abi
+    structs = [v for k, v in vars(abi).items()
+               if k.startswith("MpmGpu") and isinstance(v, type) and issubclass(v, ctypes.Structure)]
+    assert len(structs) >= 11
+    lines = ["#include <stdio.h>", "#include <stddef.h>", '#include "nairn_mpm_gpu.h"', "int main(void) {"]
+    expect = []
+    for s in structs:
+        lines.append(f'printf("%zu\\n", sizeof({s.__name__}));')
+        expect.append(ctypes.sizeof(s))
+        for name, *_ in s._fields_:
+            cname = name[:-1] if name.endswith("_") else name  # Python keywords carry a trailing _
+            lines.append(f'printf("%zu\\n", offsetof({s.__name__}, {cname}));')
+            expect.append(getattr(s, name).offset)
+    lines += ["return 0;", "}"]
+    src = tmp_path / "layout.c"
+    src.write_text("\n".join(lines))
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
+    assert got == expect

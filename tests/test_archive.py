@@ -100,3 +100,40 @@ def test_device_archive_matches_reference_archive(case, gpu_lib):
             assert np.abs(a[k]).max() == 0., k
             continue
         assert rel_l2(a[k], g["final_" + k]) <= 1e-10, (k, rel_l2(a[k], g["final_" + k]))
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("pinned", [True, False])
+def test_async_archives_equal_the_synchronous_ones(pinned, gpu_lib):
+    """Archives taken without waiting (mpmgpu_archive_records_async) while
+    later steps run hold the state at the point they were requested: the
+    same bytes as a synchronous archive of a second run stopped there (both
+    runs with deterministic node sums).  Three archives in a row also check
+    that each waits for the one before."""
+    from nairn_gb300 import model
+    from nairn_gb300.gpu import GpuRun, pin, unpin
+    gpu_lib.mpmgpu_archive_record_size.restype = C.c_int64
+    m = model.contact_3d(plate=(8, 8, 3), block=(3, 3, 2), block_x0=1.0, block_y0=1.5, steps=30)
+    rec = int(gpu_lib.mpmgpu_archive_record_size(3, ORDER.encode()))
+    at = (5, 12, 20)
+    bufs = [np.zeros(m.n * rec, dtype=np.uint8) for _ in at]
+    held = pin({str(k): b for k, b in enumerate(bufs)}) if pinned else []
+    r = GpuRun(m, p2g=1)
+    r.upload(m.particles)
+    done = 0
+    for k, buf in zip(at, bufs):
+        r.step(k - done)
+        done = k
+        r.archive_records_async(ORDER, buf)
+    r.step(m.nsteps - done)
+    r.archive_wait()
+    r.close()
+    s = GpuRun(m, p2g=1)
+    s.upload(m.particles)
+    done = 0
+    for k, buf in zip(at, bufs):
+        s.step(k - done)
+        done = k
+        assert buf.tobytes() == s.archive_records(ORDER), k
+    s.close()
+    unpin(held)

@@ -242,3 +242,92 @@ def test_contact_run_needs_a_multifield_batch(gpu_lib):
     with pytest.raises(GpuError, match="INVALID"):
         b.add(c)
     b.close()
+
+
+REGRESSION_CASES = ("contact2d_fric_logreg", "contact2d_fric_logreg_cpdi", "contact2d_stick_linreg_usl",
+                    "contact3d_fric_logreg_cpdi", "contact3d_fric_logreg_ugimp_usf")
+
+
+def with_normals(m, normals):
+    """The same problem with another contact normal method."""
+    import copy
+    o = copy.deepcopy(m)
+    o.extra["contact"]["normals"] = normals
+    o.name = f"{m.name}_normals{normals}"
+    return o
+
+
+@pytest.mark.parametrize("case", REGRESSION_CASES)
+def test_batched_regression_normals_match_reference(case, gpu_lib):
+    """A regression-normal run (linear 5, logistic 6) shares a batch with the
+    same problem under maximum-volume-gradient normals: the first matches the
+    reference's golden result within the FP64 tolerance, the second the
+    oracle."""
+    from conftest import load_golden, model_for, view_for
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import abi
+    meta, g = load_golden(case)
+    m = model_for(meta)
+    other = with_normals(m, 0)
+    steps = meta["steps"]
+    b = GpuBatch.for_models([other, m])
+    assert b.opts.lr_links == (64 if m.grid.dim == 3 else 16)
+    ids = [b.add(other), b.add(m)]
+    b.step(steps)
+    assert b.state(ids[1]) == (abi.RUN_FINISHED, steps)
+    v = view_for(b.download(ids[1]), m)
+    for k in ("pos", "vel", "stress", "strain"):
+        assert rel_l2(v[k], g["final_" + k]) <= TOL, (k, rel_l2(v[k], g["final_" + k]))
+    assert np.array_equal(v["elem"], g["final_elem"])
+    out, ref = b.download(ids[0]), oracle(other, steps)
+    (assert_close_3d if m.grid.dim == 3 else assert_close)(out, ref, TOL, other.name)
+    b.close()
+
+
+def test_batched_logistic_normals_mixed(gpu_lib):
+    """Mixed precision with logistic normals in a batch: within twice the
+    reference's own sensitivity to a 1e-9 perturbation (these runs are
+    chaotic), as the single-run mixed path."""
+    from conftest import load_golden, model_for, regression_sensitivity, view_for
+    from nairn_gb300.gpu import GpuBatch
+    meta, g = load_golden("contact3d_fric_logreg_cpdi")
+    m = model_for(meta)
+    b = GpuBatch.for_models([m], precision=1)
+    rid = b.add(m)
+    b.step(meta["steps"])
+    v = view_for(b.download(rid), m)
+    sens = regression_sensitivity(m, meta["steps"])
+    for k in ("pos", "vel", "stress", "strain"):
+        tol = max(TOL_MIXED, 2. * sens[k])
+        assert rel_l2(v[k], g["final_" + k]) <= tol, (k, rel_l2(v[k], g["final_" + k]), tol)
+    b.close()
+
+
+def test_regression_links_overflow_fails_only_that_run(gpu_lib):
+    """Links beyond the batch's lr_links reserve fail the run that made them
+    with RANGE; a run beside it is unaffected.  The overflowing run has its
+    two materials interleaved particle by particle, so nearly every node is a
+    contact node and the links far outnumber the particle slots."""
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import model, abi
+    plain = model.block_2d(ncx=8, ncy=5, vel=(0., 1500., 0.3, 0., -700., 1.1), steps=10)  # deforming
+    c = model.contact_2d(plate=(16, 4), block=(5, 3), normals=6, steps=10)
+    p = abi.copy_particles(c.particles)
+    p["mat"][::2] = 1 - p["mat"][::2]
+    b = GpuBatch.for_models([plain, c], lr_links=1)
+    ids = [b.add(plain), b.add(c, particles=p)]
+    b.step(10)
+    assert b.state(ids[1])[0] == -10  # -MPMGPU_ERR_RANGE
+    assert b.state(ids[0]) == (abi.RUN_FINISHED, 10)
+    assert_close(b.download(ids[0]), oracle(plain, 10), TOL, plain.name)
+    b.close()
+
+
+def test_regression_normals_need_a_link_reserve(gpu_lib):
+    from nairn_gb300.gpu import GpuBatch, GpuError
+    from nairn_gb300 import model
+    c = model.contact_2d(plate=(16, 4), block=(5, 3), normals=5, steps=5)
+    b = GpuBatch.for_models([c], lr_links=0)
+    with pytest.raises(GpuError, match="INVALID"):
+        b.add(c)
+    b.close()

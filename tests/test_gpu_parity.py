@@ -2,7 +2,7 @@
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden, model_for, rel_l2, view_for
+from conftest import golden_cases, load_golden, model_for, regression_sensitivity, rel_l2, view_for
 
 pytestmark = pytest.mark.gpu
 
@@ -89,25 +89,6 @@ def test_cell_sort_is_a_stable_argsort(n, nelems, gpu_lib):
 
 
 TOL_MIXED = 1e-5  # relative L2, FP32 transfers + FP64 constitutive vs the reference's FP64 path
-
-
-def regression_sensitivity(m, steps):
-    """How far the reference's own result moves (relative L2 per quantity)
-    when the initial velocities are perturbed by 1e-9 relative: regression
-    contact normals decide contact from point-cloud supports that sit near
-    zero separation, so such a run is chaotic -- the oracle, which matches the
-    reference to 1e-13, shows it."""
-    import oracle_lib
-    from nairn_gb300 import abi
-    outs = []
-    for eps in (0., 1e-9):
-        p = abi.copy_particles(m.particles)
-        rng = np.random.default_rng(1)
-        for k in ("vx", "vy"):
-            p[k] = p[k] * (1. + eps * rng.standard_normal(p[k].shape))
-        oracle_lib.run(m, p, steps, nthreads=4)
-        outs.append(view_for(p, m))
-    return {k: rel_l2(outs[1][k], outs[0][k]) for k in ("pos", "vel", "stress", "strain")}
 
 
 @pytest.mark.parametrize("case", golden_cases())
