@@ -136,6 +136,14 @@ typedef struct {
     int32_t sort_interval;    /* re-sort particles by cell every k steps (>=1) */
     double timestep;          /* s                                           */
     double fraction_usf;      /* USAVG split (0.5)                           */
+    /* PeriodicXPIC custom task (NairnMPM/src/Custom_Tasks/PeriodicXPIC.cpp):
+     * XPIC(k) or FMPM(k) grid-to-particle updates on every xpic_period-th step
+     * (steps counted from 1 at time 0, step s at time (s-1) dt), FLIP on the
+     * others.  xpic_order 0: FLIP on every step. */
+    int32_t xpic_order;       /* XPICOrder or FMPMOrder (k >= 1; 1 is PIC)   */
+    int32_t xpic_fmpm;        /* 1: FMPM(k) (FMPMOrder), 0: XPIC(k)          */
+    int32_t xpic_period;      /* periodicSteps (>= 1 when xpic_order > 0)    */
+    int32_t xpic_reserved;    /* 0                                           */
 } MpmGpuOptions;
 
 /* Particle state, structure of arrays, length n each.  Fields mirror MPMBase

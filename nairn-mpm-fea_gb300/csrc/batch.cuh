@@ -387,8 +387,9 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN, b->nf, b->ncap);
     k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     const bool lr = b->lr_runs > 0;
+    const int lrb = (int)(((long long)NN * 32 + NTB - 1) / NTB);  // a warp per node
     auto lr_normals = [&]() {
-        k_lr_normals<DIM, true><<<(NN * 32 + NTB - 1) / NTB, NTB, 0, s>>>(sp, b->p, b->nd, b->mats, b->lr_start,
+        k_lr_normals<DIM, true><<<lrb, NTB, 0, s>>>(sp, b->p, b->nd, b->mats, b->lr_start,
                                                                          b->lr_list, b->lr_out, NN, b->lr_cap, 1);
     };
     if (lr) {
@@ -404,7 +405,7 @@ void batch_enqueue_step(MpmGpuBatch *b) {
         cudaMemsetAsync(b->lr_cnt, 0, (size_t)m * sizeof(int), s);
         k_lr_link<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->lr_cnt, b->lr_start, b->lr_list,
                                                            b->lr_cap, 1);
-        k_lr_order<<<nb, NTB, 0, s>>>(b->lr_start, b->lr_list, b->orig, NN, b->lr_cap);
+        k_lr_order<<<lrb, NTB, 0, s>>>(b->lr_start, b->lr_list, b->orig, NN, b->lr_cap);
         lr_normals();
     }
     k_node_post<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, method != MPMGPU_USL);

@@ -70,20 +70,43 @@ static __global__ void __launch_bounds__(256) k_lr_link(StepParams sp, DevPartic
     }
 }
 
-// each node's links in the particles' host order (insertion sort)
-static __global__ void k_lr_order(const int *start, int *list, const int *orig, int nnodes, long long cap) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nnodes) return;
-    const int s0 = start[n], s1 = start[n + 1];
-    if (s1 > cap) return;  // dropped links (the run has failed)
-    for (int k = s0 + 1; k < s1; k++) {
-        const int v = list[k], key = orig[v];
-        int j = k - 1;
-        while (j >= s0 && orig[list[j]] > key) {
-            list[j + 1] = list[j];
-            --j;
-        }
-        list[j + 1] = v;
+// each node's links in the particles' host order: one warp per node ranks its
+// links by host index in shared memory (host indices are distinct within a
+// node, whose particles all belong to one run); lists longer than the
+// shared-memory slice are sorted by insertion by one lane
+constexpr int kLrSortCap = 256;
+static __global__ void __launch_bounds__(256) k_lr_order(const int *start, int *list, const int *orig, int nnodes,
+                                                         long long cap) {
+    __shared__ int skey[8][kLrSortCap], sval[8][kLrSortCap];
+    const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+    const int n = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    if (n >= nnodes) return;  // whole warps
+    const int s0 = start[n], s1 = start[n + 1], L = s1 - s0;
+    if (L < 2 || s1 > cap) return;  // nothing to order, or dropped links (the run has failed)
+    if (L > kLrSortCap) {
+        if (lane == 0)
+            for (int k = s0 + 1; k < s1; k++) {
+                const int v = list[k], key = orig[v];
+                int j = k - 1;
+                while (j >= s0 && orig[list[j]] > key) {
+                    list[j + 1] = list[j];
+                    --j;
+                }
+                list[j + 1] = v;
+            }
+        return;
+    }
+    for (int k = lane; k < L; k += 32) {
+        const int v = list[s0 + k];
+        sval[w][k] = v;
+        skey[w][k] = orig[v];
+    }
+    __syncwarp();
+    for (int k = lane; k < L; k += 32) {
+        const int key = skey[w][k];
+        int rank = 0;
+        for (int j = 0; j < L; j++) rank += skey[w][j] < key ? 1 : 0;
+        list[s0 + rank] = sval[w][k];
     }
 }
 
@@ -99,58 +122,47 @@ __device__ __forceinline__ double lr_wmin(double v) {
     return v;
 }
 
-// inverse of the symmetric 3x3 (a b c; b d e; c e f), by cofactors
-__device__ __forceinline__ void lr_inv3(const double m[6], double r[9]) {
+// Inverses of the symmetric regression matrices by cofactors, each entry's
+// cofactor and quotient taken by its own lane of the warp (lane l and l + 16
+// or l + 9k hold entry l), then the whole inverse handed to every lane.  The
+// FP64 pipe is the bound: one quotient per lane instead of 16 (9) per lane.
+constexpr unsigned kFullWarp = 0xffffffffu;
+
+// the symmetric 3x3 (a b c; b d e; c e f)
+__device__ __forceinline__ void lr_inv3_warp(const double m[6], double r[9], int lane) {
     const double a = m[0], b = m[1], c = m[2], d = m[3], e = m[4], f = m[5];
     const double c00 = d * f - e * e, c01 = -(b * f - c * e), c02 = b * e - c * d;
     const double det = a * c00 + b * c01 + c * c02;
     const double c11 = a * f - c * c, c12 = -(a * e - b * c), c22 = a * d - b * b;
-    r[0] = c00 / det;
-    r[1] = c01 / det;
-    r[2] = c02 / det;
-    r[3] = c01 / det;
-    r[4] = c11 / det;
-    r[5] = c12 / det;
-    r[6] = c02 / det;
-    r[7] = c12 / det;
-    r[8] = c22 / det;
+    const double cof[9] = {c00, c01, c02, c01, c11, c12, c02, c12, c22};
+    const double q = cof[lane % 9] / det;
+#pragma unroll
+    for (int k = 0; k < 9; k++) r[k] = __shfl_sync(kFullWarp, q, k);
 }
 
-// inverse of the symmetric 4x4 whose upper triangle is mt
-// (00 01 02 03 11 12 13 22 23 33), by cofactors
-__device__ __forceinline__ void lr_inv4(const double mt[10], double r[16]) {
-    const double m[4][4] = {{mt[0], mt[1], mt[2], mt[3]},
-                            {mt[1], mt[4], mt[5], mt[6]},
-                            {mt[2], mt[5], mt[7], mt[8]},
-                            {mt[3], mt[6], mt[8], mt[9]}};
-    double cof[4][4];
+// the symmetric 4x4 whose upper triangle is mt (00 01 02 03 11 12 13 22 23 33)
+__device__ __forceinline__ void lr_inv4_warp(const double mt[10], double r[16], int lane) {
+    const double m[16] = {mt[0], mt[1], mt[2], mt[3], mt[1], mt[4], mt[5], mt[6],
+                          mt[2], mt[5], mt[7], mt[8], mt[3], mt[6], mt[8], mt[9]};
+    // cofactor (i, j): the minor without row i and column j
+    const int i = (lane >> 2) & 3, j = lane & 3;
+    const int a0 = i == 0 ? 1 : 0, a1 = i <= 1 ? 2 : 1, a2 = i <= 2 ? 3 : 2;
+    const int b0 = j == 0 ? 1 : 0, b1 = j <= 1 ? 2 : 1, b2 = j <= 2 ? 3 : 2;
+    const double s3[3][3] = {{m[4 * a0 + b0], m[4 * a0 + b1], m[4 * a0 + b2]},
+                             {m[4 * a1 + b0], m[4 * a1 + b1], m[4 * a1 + b2]},
+                             {m[4 * a2 + b0], m[4 * a2 + b1], m[4 * a2 + b2]}};
+    const double d3 = s3[0][0] * (s3[1][1] * s3[2][2] - s3[1][2] * s3[2][1]) -
+                      s3[0][1] * (s3[1][0] * s3[2][2] - s3[1][2] * s3[2][0]) +
+                      s3[0][2] * (s3[1][0] * s3[2][1] - s3[1][1] * s3[2][0]);
+    const double cof = ((i + j) & 1) ? -d3 : d3;
+    double c0[4];
 #pragma unroll
-    for (int i = 0; i < 4; i++)
+    for (int k = 0; k < 4; k++) c0[k] = __shfl_sync(kFullWarp, cof, k);
+    const double det = m[0] * c0[0] + m[1] * c0[1] + m[2] * c0[2] + m[3] * c0[3];
+    // inverse entry (i, j) = cofactor (j, i) / det
+    const double q = __shfl_sync(kFullWarp, cof, 4 * j + i) / det;
 #pragma unroll
-        for (int j = 0; j < 4; j++) {
-            double s3[3][3];
-            int ri = 0;
-#pragma unroll
-            for (int a = 0; a < 4; a++) {
-                if (a == i) continue;
-                int cj = 0;
-#pragma unroll
-                for (int b = 0; b < 4; b++) {
-                    if (b == j) continue;
-                    s3[ri][cj++] = m[a][b];
-                }
-                ri++;
-            }
-            const double d3 = s3[0][0] * (s3[1][1] * s3[2][2] - s3[1][2] * s3[2][1]) -
-                              s3[0][1] * (s3[1][0] * s3[2][2] - s3[1][2] * s3[2][0]) +
-                              s3[0][2] * (s3[1][0] * s3[2][1] - s3[1][1] * s3[2][0]);
-            cof[i][j] = ((i + j) & 1) ? -d3 : d3;
-        }
-    const double det = m[0][0] * cof[0][0] + m[0][1] * cof[0][1] + m[0][2] * cof[0][2] + m[0][3] * cof[0][3];
-#pragma unroll
-    for (int i = 0; i < 4; i++)
-#pragma unroll
-        for (int j = 0; j < 4; j++) r[4 * i + j] = cof[j][i] / det;
+    for (int k = 0; k < 16; k++) r[k] = __shfl_sync(kFullWarp, q, k);
 }
 
 // MatPoint2D/3D::GetDeformedRadius, ellipse method (MatPoint2D.cpp:482-495,
@@ -189,7 +201,7 @@ template <int DIM, bool BATCH>
 static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevParticles p, DevNodes nd,
                                                            const DevMat *mats, const int *start, const int *list,
                                                            double *out, int nnodes, long long cap, int logistic) {
-    const int n = (blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
     const int lane = threadIdx.x & 31;
     if (n >= nnodes) return;  // whole warps
     const int s0 = start[n], s1 = start[n + 1];
@@ -279,7 +291,7 @@ static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevPar
                 const double m4[10] = {mt[0] + lam[0], mt[1], mt[2], mt[3], mt[4] + lam[1],
                                        mt[5], mt[6], mt[7] + lam[2], mt[8], mt[9] + lam[3]};
                 double inv[16];
-                lr_inv4(m4, inv);
+                lr_inv4_warp(m4, inv, lane);
 #pragma unroll
                 for (int r = 0; r < 4; r++)
                     sol[r] = inv[4 * r] * rhs[0] + inv[4 * r + 1] * rhs[1] + inv[4 * r + 2] * rhs[2] +
@@ -287,7 +299,7 @@ static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevPar
             } else {
                 const double m3[6] = {mt[0] + lam[0], mt[1], mt[2], mt[3] + lam[1], mt[4], mt[5] + lam[2]};
                 double inv[9];
-                lr_inv3(m3, inv);
+                lr_inv3_warp(m3, inv, lane);
 #pragma unroll
                 for (int r = 0; r < 3; r++) sol[r] = inv[3 * r] * rhs[0] + inv[3 * r + 1] * rhs[1] + inv[3 * r + 2] * rhs[2];
             }

@@ -52,7 +52,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
         c->launches += 2;
     }
     const bool lr = c->ct.nf > 1 && c->ct.normals >= 5;
-    const int lrb = (NN * 32 + TB - 1) / TB;  // a warp per node
+    const int lrb = (int)(((long long)NN * 32 + TB - 1) / TB);  // a warp per node
     auto lr_normals = [&]() {
         k_lr_normals<DIM, false><<<lrb, TB, 0, s>>>(sp, c->p, c->nd, c->mats, c->lr_start, c->lr_list, c->lr_out,
                                                     NN, c->lr_cap, c->ct.normals == 6 ? 1 : 0);
@@ -71,7 +71,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
         cudaMemsetAsync(c->lr_cnt, 0, (size_t)m * sizeof(int), s);
         k_lr_link<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->lr_cnt, c->lr_start, c->lr_list,
                                                             c->lr_cap, 1);
-        k_lr_order<<<nb, TB, 0, s>>>(c->lr_start, c->lr_list, c->orig, NN, c->lr_cap);
+        k_lr_order<<<lrb, TB, 0, s>>>(c->lr_start, c->lr_list, c->orig, NN, c->lr_cap);
         c->launches += 6;
         lr_normals();
     }

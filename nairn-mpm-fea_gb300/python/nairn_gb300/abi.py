@@ -45,7 +45,9 @@ class MpmGpuVelBC(C.Structure):
 class MpmGpuOptions(C.Structure):
     _fields_ = [("np", C.c_int32), ("method", C.c_int32), ("shape", C.c_int32), ("precision", C.c_int32),
                 ("p2g", C.c_int32), ("inc_defgrad_terms", C.c_int32), ("nfields", C.c_int32),
-                ("sort_interval", C.c_int32), ("timestep", C.c_double), ("fraction_usf", C.c_double)]
+                ("sort_interval", C.c_int32), ("timestep", C.c_double), ("fraction_usf", C.c_double),
+                ("xpic_order", C.c_int32), ("xpic_fmpm", C.c_int32), ("xpic_period", C.c_int32),
+                ("xpic_reserved", C.c_int32)]
 
 
 _PFIELDS = ["x", "y", "z", "vx", "vy", "vz", "x0", "y0", "z0", "mass", "mat", "elem", "lpx", "lpy", "lpz",
@@ -85,7 +87,8 @@ def grid_struct(m: Model, b: Bound) -> MpmGpuGrid:
 def options_struct(m: Model, precision: int = 0, p2g: int = 0, sort_interval: int = 1) -> MpmGpuOptions:
     o = m.options
     return MpmGpuOptions(o["np"], o["method"], o["shape"], precision, p2g, o.get("inc_defgrad_terms", 1),
-                         o.get("nfields", 1), sort_interval, o["timestep"], o.get("fraction_usf", 0.5))
+                         o.get("nfields", 1), sort_interval, o["timestep"], o.get("fraction_usf", 0.5),
+                         o.get("xpic_order", 0), o.get("xpic_fmpm", 0), o.get("xpic_period", 1), 0)
 
 
 def materials_array(m: Model):

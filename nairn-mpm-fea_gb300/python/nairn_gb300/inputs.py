@@ -81,6 +81,23 @@ def _header(analysis: int, method: int, gimp: str, maxtime_s: float, cfl: float,
 """
 
 
+def xpic_xml(xpic) -> str:
+    """The PeriodicXPIC custom task (Custom_Tasks/PeriodicXPIC.cpp:55-145) for
+    xpic = (order, fmpm, period): XPICOrder (or FMPMOrder when fmpm) on every
+    period-th step; empty for None."""
+    if not xpic:
+        return ""
+    order, fmpm, period = xpic
+    key = "FMPMOrder" if fmpm else "XPICOrder"
+    return f"""  <CustomTasks>
+    <Schedule name='PeriodicXPIC'>
+      <Parameter name='{key}'>{int(order)}</Parameter>
+      <Parameter name='periodicSteps'>{int(period)}</Parameter>
+    </Schedule>
+  </CustomTasks>
+"""
+
+
 # archive items: velocity, stress, strain, plastic strain, work energy,
 # plastic energy, history 1 (ArchiveData.hpp:22-32)
 ARCHIVE_ORDER = "iYYYYYNYNYNNNYNNNN"
@@ -90,7 +107,7 @@ def cantilever_2d(nx: int = 100, ny: int = 20, cell: float = 1.0, ppc_side: int 
                   E: float = 1000., nu: float = 0.33, rho: float = 1.0, v0: float = 1000.,
                   steps: int = 1000, cfl: float = 0.4, gimp: str = "uGIMP", method: int = 2,
                   margin_cells: int = 4, archive_root: str = "Results/cant.", mat_type: int = 1,
-                  G: float = 0., K: float = 0., uj: int = 0, inc_terms: int = 0) -> tuple[str, dict]:
+                  G: float = 0., K: float = 0., uj: int = 0, inc_terms: int = 0, xpic=None) -> tuple[str, dict]:
     """2D plane-strain cantilever of nx*ny cells, left edge fixed, initial
     v_y = v0*sin(pi*x/(2L)) (mm/s); elastic (mat_type 1, E and nu) or
     Neo-Hookean (mat_type 28, G and K).  Returns (xml, info)."""
@@ -120,7 +137,7 @@ def cantilever_2d(nx: int = 100, ny: int = 20, cell: float = 1.0, ppc_side: int 
       <DisBC dir="2" disp="0"/>
     </BCLine>
   </GridBCs>
-</JANFEAInput>
+{xpic_xml(xpic)}</JANFEAInput>
 """
     return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 2}
 
@@ -130,7 +147,7 @@ def taylor_3d(radius: float = 5.0, length: float = 25.0, cell: float = 0.25, ppc
               Ep: float = 2000., rho: float = 7.8, steps: int = 2000, cfl: float = 0.5,
               gimp: str = "uGIMP", method: int = 2, lateral_margin: float | None = None,
               archive_root: str = "Results/taylor.", mat_type: int = 9, G: float = 0., K: float = 0.,
-              uj: int = 0, inc_terms: int = 0) -> tuple[str, dict]:
+              uj: int = 0, inc_terms: int = 0, xpic=None) -> tuple[str, dict]:
     """3D Taylor impact: cylinder along z from z=0 to z=length moving at v0
     (mm/s) onto a rigid wall at z=0 (zero z-velocity on the z=0 node plane);
     von Mises (mat_type 9), elastic (1) or Neo-Hookean (28)."""
@@ -157,7 +174,7 @@ def taylor_3d(radius: float = 5.0, length: float = 25.0, cell: float = 0.25, ppc
       <DisBC dir="3" disp="0"/>
     </BCBox>
   </GridBCs>
-</JANFEAInput>
+{xpic_xml(xpic)}</JANFEAInput>
 """
     return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 3}
 

@@ -226,9 +226,16 @@ def _initial_material_state(p, mat):
             p[k][:] = 1.
 
 
+def _xpic_options(opts: dict, xpic) -> None:
+    """PeriodicXPIC settings (inputs.xpic_xml): xpic = (order, fmpm, period)."""
+    if xpic:
+        order, fmpm, period = xpic
+        opts.update(xpic_order=int(order), xpic_fmpm=1 if fmpm else 0, xpic_period=int(period))
+
+
 def cantilever_2d(nx=100, ny=20, cell=1.0, ppc_side=2, E=1000., nu=0.33, rho=1.0, v0=1000.,
                   steps=1000, cfl=0.4, gimp="uGIMP", method=USAVG, margin_cells=4, mat_type=MAT_ISO,
-                  G=0., K=0., uj=0, inc_terms=0, **_ignored) -> Model:
+                  G=0., K=0., uj=0, inc_terms=0, xpic=None, **_ignored) -> Model:
     """Model of inputs.cantilever_2d (same arguments)."""
     from . import inputs
     shape = GIMP_NAMES[gimp]
@@ -258,6 +265,7 @@ def cantilever_2d(nx=100, ny=20, cell=1.0, ppc_side=2, E=1000., nu=0.33, rho=1.0
     dt = inputs.cfl_timestep(g.dx, c, cfl)  # MeshInfo::GetMinCellDimension: grid.x for square grids
     opts = dict(np=PLANE_STRAIN, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
                 inc_defgrad_terms=inc_terms if inc_terms > 0 else 2, nfields=1)
+    _xpic_options(opts, xpic)
     return Model(g, p, mats, bcs, opts, steps, name=f"cantilever_2d_{nx}x{ny}")
 
 
@@ -274,7 +282,7 @@ def _line_contains(x, y, x1, y1, x2, y2, tol):
 
 def taylor_3d(radius=5.0, length=25.0, cell=0.25, ppc_side=2, v0=-200000., E=200000., nu=0.3,
               yield_=300., Ep=2000., rho=7.8, steps=2000, cfl=0.5, gimp="uGIMP", method=USAVG,
-              lateral_margin=None, mat_type=MAT_PLASTIC, G=0., K=0., uj=0, inc_terms=0, **_ignored) -> Model:
+              lateral_margin=None, mat_type=MAT_PLASTIC, G=0., K=0., uj=0, inc_terms=0, xpic=None, **_ignored) -> Model:
     """Model of inputs.taylor_3d (same arguments)."""
     from . import inputs
     shape = GIMP_NAMES[gimp]
@@ -313,6 +321,7 @@ def taylor_3d(radius=5.0, length=25.0, cell=0.25, ppc_side=2, v0=-200000., E=200
     dt = inputs.cfl_timestep(g.dx, c, cfl)  # cubic grid: grid.x
     opts = dict(np=THREED, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
                 inc_defgrad_terms=inc_terms if inc_terms > 0 else 1, nfields=1)
+    _xpic_options(opts, xpic)
     return Model(g, p, mats, bcs, opts, steps, name=f"taylor_3d_r{radius}_c{cell}")
 
 

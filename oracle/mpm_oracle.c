@@ -1010,6 +1010,9 @@ typedef struct {
     long *lr_list;          /*   nodes, node n's at lr_list[lr_start[n] .. lr_start[n+1]) */
     int friction_style;     /* CoulombFriction: 0 stick, 1 frictionless, 2 frictional */
     double friction;        /* Coulomb coefficient */
+    int xpic;               /* this step: 0 FLIP, k > 0 FMPM(k), -k XPIC(k) (GridToParticleExtrap::m) */
+    double *vpx, *vpy, *vpz;  /* XPIC v*(prev) (MatVelocityField vk[VSTARPREV_VEC]) */
+    double *vnx, *vny, *vnz;  /* XPIC v*(next) (vk[VSTARNEXT_VEC]) */
 } OCtx;
 
 /* field of particle q (MaterialBase::GetField) */
@@ -1229,11 +1232,16 @@ static void grid_velocity(OCtx *c) {
 /* UpdateStrainsFirstTask::FullStrainUpdate (UpdateStrainsFirstTask.cpp:101-168),
  * MatPoint2D/3D::UpdateStrain and ExtrapVelocityGradient
  * (MatPoint2D.cpp:37-87, MatPoint3D.cpp:40-75). */
+static void xpic_extrapolate(OCtx *c, int order, int particle_update);
+static void xpic_move(MpmGpuParticles *p, long q, int is3d, int m, double dt, double Svx, double Svy, double Svz);
+
 static void strain_update(OCtx *c, double strainTime) {
     MpmGpuParticles *p = c->p;
     OField *f = &c->f;
     int is3d = c->g.dim == 3;
-    grid_velocity(c);
+    /* FMPM(k > 1) takes v(k) of the XPIC expansion (UpdateStrainsFirstTask.cpp:106-125) */
+    if (c->xpic > 1) xpic_extrapolate(c, c->xpic, 0);
+    else grid_velocity(c);
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
     for (long q = 0; q < p->n; q++) {
         OShape s;
@@ -1323,7 +1331,12 @@ static void g2p_move(OCtx *c) {
     OField *f = &c->f;
     int is3d = c->g.dim == 3;
     double dt = c->dt;
-    grid_velocity(c);
+    /* UpdateParticlesTask::Execute (UpdateParticlesTask.cpp:66-82): FMPM(k > 1)
+     * and XPIC(k > 1) take v(k) of the XPIC expansion, FLIP and PIC the lumped
+     * velocity; m > 0 FMPM, m < 0 XPIC, 0 FLIP */
+    const int m = c->xpic;
+    if (m > 1 || m < -1) xpic_extrapolate(c, m > 0 ? m : -m, 1);
+    else grid_velocity(c);
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
     for (long q = 0; q < p->n; q++) {
         OShape s;
@@ -1341,6 +1354,10 @@ static void g2p_move(OCtx *c) {
             Say += f->fy[nd] * mnode;
             Saz += f->fz[nd] * mnode;
         }
+        if (m != 0) {
+            xpic_move(p, q, is3d, m, dt, Svx, Svy, Svz);
+            continue;
+        }
         double vmx = Svx - Sax * dt, vmy = Svy - Say * dt, vmz = Svz - Saz * dt;
         /* Adamp0 = 0 (no grid or particle damping) */
         double a0x = 0. * vmx + 0. * p->vx[q], a0y = 0. * vmy + 0. * p->vy[q];
@@ -1353,6 +1370,134 @@ static void g2p_move(OCtx *c) {
             double a0z = 0. * vmz + 0. * p->vz[q];
             double dvz = (Saz - a0z) * dt;
             p->vz[q] += dvz;
+            p->z[q] += (vmz + 0.5 * dvz) * dt;
+        }
+    }
+}
+
+/* PeriodicXPIC::PrepareForStep / StepCalculation (PeriodicXPIC.cpp:351-370,
+ * 427-445) with the custom tasks run once before the first step and after
+ * every step (NairnMPM.cpp:171-200): step s (from 1) uses the task's order
+ * when s is a multiple of periodicSteps, FLIP otherwise */
+static int xpic_step_order(const MpmGpuOptions *o, long s) {
+    if (o->xpic_order <= 0 || o->xpic_period <= 0) return 0;
+    if (s % o->xpic_period != 0) return 0;
+    return o->xpic_fmpm ? o->xpic_order : -o->xpic_order;
+}
+
+/* XPICExtrapolationTask::Execute (XPICExtrapolationTask.cpp:50-160) with
+ * MatVelocityField::XPICSupport (MatVelocityField.cpp:318-399), single
+ * material field: v(k) of the order-k expansion in f->v (VSTAR_VEC is vk[0]).
+ * FMPM starts from the lumped velocity p/m, XPIC from (p - f dt)/m and adds
+ * f dt/m to v*.  Each pass adds (I - S+S) v*(prev) after zeroing the velocity
+ * conditions' directions (NodalVelBC::GridVelocityConditions, XPIC passes,
+ * NodalVelBC.cpp:327-334; MatVelocityField::ZeroVelocityBC :530-541). */
+static void xpic_extrapolate(OCtx *c, int order, int particle_update) {
+    MpmGpuParticles *p = c->p;
+    OField *f = &c->f;
+    const long nn = c->nfn;
+    const double dt = c->dt;
+    const int fmpm = c->xpic > 0;
+    (void)particle_update;
+    /* INITIALIZE_XPIC */
+    for (long i = 1; i < nn; i++) {
+        c->vnx[i] = 0.; c->vny[i] = 0.; c->vnz[i] = 0.;
+        if (f->npts[i] == 0) continue;
+        if (fmpm) {
+            double r = 1. / f->mass[i];
+            c->vpx[i] = f->px[i] * r; c->vpy[i] = f->py[i] * r; c->vpz[i] = f->pz[i] * r;
+            f->vx[i] = c->vpx[i]; f->vy[i] = c->vpy[i]; f->vz[i] = c->vpz[i];
+        } else {
+            double r = 1. / f->mass[i];
+            c->vpx[i] = f->px[i]; c->vpy[i] = f->py[i]; c->vpz[i] = f->pz[i];
+            c->vpx[i] += f->fx[i] * (-dt); c->vpy[i] += f->fy[i] * (-dt); c->vpz[i] += f->fz[i] * (-dt);
+            c->vpx[i] *= r; c->vpy[i] *= r; c->vpz[i] *= r;
+            double s = dt / f->mass[i];
+            f->vx[i] = c->vpx[i]; f->vy[i] = c->vpy[i]; f->vz[i] = c->vpz[i];
+            f->vx[i] += f->fx[i] * s; f->vy[i] += f->fy[i] * s; f->vz[i] += f->fz[i] * s;
+        }
+    }
+    for (int k = 2; k <= order; k++) {
+        /* XPICDoubleLoop (XPICExtrapolationTask.cpp:182-211): v*(next) = S+S v*(prev) */
+        for (long q = 0; q < p->n; q++) {
+            OShape s;
+            particle_shape(c, q, 0, &s);
+            long off = (long)particle_field(c, q) * c->nn;
+            for (int a = 0; a < s.n; a++) {
+                long ni = off + s.nds[a];
+                double mass = f->mass[ni];
+                for (int b = 0; b < s.n; b++) {
+                    long nj = off + s.nds[b];
+                    double weight = s.fn[a] * s.fn[b];
+                    double w = p->mass[q] * weight / mass;
+                    c->vnx[ni] += w * c->vpx[nj];
+                    c->vny[ni] += w * c->vpy[nj];
+                    c->vnz[ni] += w * c->vpz[nj];
+                }
+            }
+        }
+        /* GET_DELTAV: Delta v(k) = v*(prev) - v*(next) */
+        for (long i = 1; i < nn; i++) {
+            if (f->npts[i] == 0) continue;
+            c->vpx[i] -= c->vnx[i]; c->vpy[i] -= c->vny[i]; c->vpz[i] -= c->vnz[i];
+        }
+        /* velocity conditions zero their directions of Delta v(k) */
+        for (int fld = 0; fld < c->nf; fld++)
+            for (int b = 0; b < c->nbc; b++) {
+                const MpmGpuVelBC *bc = &c->bcs[b];
+                if (c->mtime < bc->ftime) continue;
+                long i = (long)fld * c->nn + bc->node;
+                if (f->npts[i] <= 0) continue;
+                double n[3];
+                bc_norm(bc->dir, n);
+                double dotn = c->vpx[i] * n[0] + c->vpy[i] * n[1] + c->vpz[i] * n[2];
+                c->vpx[i] += n[0] * (-dotn); c->vpy[i] += n[1] * (-dotn); c->vpz[i] += n[2] * (-dotn);
+            }
+        /* UPDATE_VSTAR: v* += Delta v(k), v*(next) = 0 */
+        for (long i = 1; i < nn; i++) {
+            if (f->npts[i] == 0) continue;
+            f->vx[i] += c->vpx[i]; f->vy[i] += c->vpy[i]; f->vz[i] += c->vpz[i];
+            c->vnx[i] = 0.; c->vny[i] = 0.; c->vnz[i] = 0.;
+        }
+    }
+}
+
+/* MatPoint2D/3D::MoveParticle (MatPoint2D.cpp:99-196, MatPoint3D.cpp:103-200)
+ * for FMPM (m > 0) and XPIC (m < 0) with Svk = S v(k) (S v(k) + a dt for XPIC,
+ * the lumped S v+ for order 1); no damping */
+static void xpic_move(MpmGpuParticles *p, long q, int is3d, int m, double dt, double Svx, double Svy, double Svz) {
+    double vmx = Svx, vmy = Svy, vmz = Svz;
+    double a0x = 0. * vmx + 0. * p->vx[q], a0y = 0. * vmy + 0. * p->vy[q];
+    double a0z = is3d ? 0. * vmz + 0. * p->vz[q] : 0.;
+    if (m > 0) {
+        double ox = p->vx[q], oy = p->vy[q], oz = is3d ? p->vz[q] : 0.;
+        p->vx[q] = vmx - a0x * dt;
+        p->vy[q] = vmy - a0y * dt;
+        if (!is3d) {
+            ox += p->vx[q];
+            oy += p->vy[q];
+            p->x[q] += 0.5 * ox * dt;
+            p->y[q] += 0.5 * oy * dt;
+        } else {
+            p->vz[q] = vmz - a0z * dt;
+            ox += p->vx[q];
+            oy += p->vy[q];
+            oz += p->vz[q];
+            double h = 0.5 * dt;
+            p->x[q] += ox * h;
+            p->y[q] += oy * h;
+            p->z[q] += oz * h;
+        }
+    } else {
+        double ox = p->vx[q], oy = p->vy[q], oz = is3d ? p->vz[q] : 0.;
+        p->vx[q] = Svx - a0x * dt;
+        p->vy[q] = Svy - a0y * dt;
+        double dvx = p->vx[q] - ox, dvy = p->vy[q] - oy;
+        p->x[q] += (vmx + 0.5 * dvx) * dt;
+        p->y[q] += (vmy + 0.5 * dvy) * dt;
+        if (is3d) {
+            p->vz[q] = Svz - a0z * dt;
+            double dvz = p->vz[q] - oz;
             p->z[q] += (vmz + 0.5 * dvz) * dt;
         }
     }
@@ -1899,6 +2044,8 @@ static int one_step(OCtx *c) {
     double stLast = method == MPMGPU_USAVG ? dt - stFirst : dt;
     int is3d = c->g.dim == 3;
 
+    c->xpic = xpic_step_order(c->o, (long)llround(c->mtime / dt) + 1);
+
     /* InitializationTask: zero nodes; ElementBase::GetShapeFunctionData: CPDI
      * corners (lCPDI) and natural coordinates (MoreMPMElementBase.cpp:50-57) */
     zero_field(f, nn);
@@ -1941,7 +2088,8 @@ static int one_step(OCtx *c) {
         }
     }
     if (c->mm) material_contact(c, UPDATE_MOMENTUM_CALL);
-    velocity_bc_loop(c, UPDATE_MOMENTUM_CALL);
+    /* NodalVelBC::GridVelocityConditions (NodalVelBC.cpp:367-374): not for XPIC/FMPM(k > 1) */
+    if (c->xpic >= -1 && c->xpic <= 1) velocity_bc_loop(c, UPDATE_MOMENTUM_CALL);
 
     /* UpdateParticlesTask */
     g2p_move(c);
@@ -2035,6 +2183,15 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
         c.lr_start = (long *)calloc((size_t)c.g.nnodes + 2, sizeof(long));
         c.lr_list = (long *)calloc((size_t)(p->n > 0 ? p->n : 1) * 64, sizeof(long));
     }
+    if (opts->xpic_order > 0) {
+        if (c.mm) {
+            free(c.mats);
+            return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: XPIC/FMPM with multimaterial contact not implemented");
+        }
+        if (opts->xpic_period < 1) { free(c.mats); return fail(MPMGPU_ERR_INVALID, "oracle: xpic_period < 1"); }
+        double **xv[] = {&c.vpx, &c.vpy, &c.vpz, &c.vnx, &c.vny, &c.vnz};
+        for (unsigned k = 0; k < 6; k++) *xv[k] = (double *)calloc((size_t)nn, sizeof(double));
+    }
     c.mtime = t0;
     for (int s = 0; s < nsteps && st == MPMGPU_OK; s++) {
         st = one_step(&c);
@@ -2046,6 +2203,7 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     free(c.cpdi);
     free(c.lr_start);
     free(c.lr_list);
+    free(c.vpx); free(c.vpy); free(c.vpz); free(c.vnx); free(c.vny); free(c.vnz);
     free(c.mats);
     return st;
 }

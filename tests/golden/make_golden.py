@@ -78,6 +78,19 @@ CASES = {
                                                       v=(50000., 0., -200000.))),
     "contact3d_fric_logreg_ugimp_usf": ("contact_3d", dict(steps=70, friction=0.3, normals=6, gimp="uGIMP",
                                                            method=0, gap=0.5, v=(50000., 0., -200000.))),
+    # PeriodicXPIC: XPIC(k) and FMPM(k) grid-to-particle updates, every step or
+    # every few steps (xpic = (order, fmpm, period))
+    "cant2d_xpic2": ("cantilever_2d", dict(nx=10, ny=4, steps=60, xpic=(2, 0, 1))),
+    "cant2d_pic_every3": ("cantilever_2d", dict(nx=10, ny=4, steps=60, xpic=(1, 0, 3))),
+    "cant2d_fmpm3": ("cantilever_2d", dict(nx=10, ny=4, steps=60, xpic=(3, 1, 1))),
+    "cant2d_fmpm1_usl": ("cantilever_2d", dict(nx=10, ny=4, steps=60, method=3, xpic=(1, 1, 1))),
+    "cant2d_fmpm2_usl_every2": ("cantilever_2d", dict(nx=10, ny=4, steps=60, method=3, xpic=(2, 1, 2))),
+    "cant2d_xpic2_cpdi_every2": ("cantilever_2d", dict(nx=10, ny=4, steps=60, gimp="lCPDI", xpic=(2, 0, 2))),
+    "taylor3d_xpic3": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, xpic=(3, 0, 1))),
+    "taylor3d_fmpm2_cpdi_usf": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, gimp="lCPDI",
+                                                  method=0, xpic=(2, 1, 1))),
+    "taylor3d_neo_fmpm4_usl": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=40, mat_type=28, G=10.,
+                                                 K=50., rho=1.1, v0=-30000., method=3, xpic=(4, 1, 1))),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")
