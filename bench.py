@@ -77,6 +77,8 @@ def parse():
     ap.add_argument("--archive-steps", type=int, default=60,
                     help="steps of the archiving measurement on the headline workload (0: skip)")
     ap.add_argument("--archive-every", type=int, default=10, help="steps between archives")
+    ap.add_argument("--xpic-steps", type=int, default=20,
+                    help="timed steps of the XPIC/FMPM measurement on the headline workload (0: skip)")
     return ap.parse_args()
 
 
@@ -599,6 +601,30 @@ def archive_measurement(args, run, m, dist):
     return out
 
 
+def xpic_measurement(args, dist, sort_interval: int, precision: int):
+    """The headline workload with the PeriodicXPIC custom task on every step:
+    XPIC(k) and FMPM(k) grid-to-particle updates (each order k > 1 adds k - 1
+    particle passes to the particle update, FMPM also to both strain
+    updates).  CUDA events around the timed steps, as the headline."""
+    from nairn_gb300 import gpu, model
+    out = {"workload": "the headline Taylor impact with PeriodicXPIC on every step", "steps": args.xpic_steps,
+           "sort_interval": sort_interval, "dtype": "mixed" if precision else "f64"}
+    total = dist.sum(1.)
+    for order, fmpm in ((1, 0), (2, 0), (4, 0), (2, 1), (4, 1)):
+        m = model.taylor_3d(radius=args.radius, length=args.length, cell=args.cell,
+                            steps=args.warmup + args.xpic_steps, xpic=(order, fmpm, 1))
+        run = gpu.GpuRun(m, sort_interval=sort_interval, precision=precision)
+        run.upload(m.particles)
+        run.step(args.warmup)
+        dist.barrier()
+        ms = dist.max(run.step_timed(args.xpic_steps))
+        run.close()
+        name = ("FMPM(%d)" if fmpm else "XPIC(%d)") % order
+        out[name] = {"ms_per_step": ms / args.xpic_steps,
+                     "particle_steps_per_s": total * m.n * args.xpic_steps / (ms / 1e3)}
+    return out
+
+
 def config3_measurement(args, dist, local):
     """The 3D two-material contact form: a Neo-Hookean block (G 10 MPa, K 50 MPa,
     rho 1.1) pressed and sliding (4 m/s down, 4 m/s along) on an elastic plate
@@ -787,6 +813,8 @@ def main():
             "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk}
     if archived:
         line["archived"] = archived
+    if args.xpic_steps > 0:
+        line["xpic"] = xpic_measurement(args, dist, head["sort_interval"], prec)
     if args.config3_steps > 0:
         line["contact3d"] = config3_measurement(args, dist, local)
     if args.contact_runs > 0:

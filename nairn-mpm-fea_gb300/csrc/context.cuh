@@ -67,9 +67,22 @@ struct MpmGpuCtx {
     int *lr_cnt = nullptr, *lr_start = nullptr, *lr_list = nullptr, *lr_sums = nullptr;
     double *lr_out = nullptr;
     long long lr_cap = 0;                // links the list holds
+    // PeriodicXPIC expansion columns (7 FP64 and 7 FP32 per node, allocated at the first step)
+    nmg::DevXpic xpic{};
+    double *xpic_block = nullptr;
 };
 
 namespace nmg {
+
+// PeriodicXPIC::PrepareForStep / StepCalculation (NairnMPM/src/Custom_Tasks/
+// PeriodicXPIC.cpp:351-370, 427-445), the custom tasks running once before
+// the first step and after each step (NairnMPM.cpp:171-200): step s (from 1)
+// uses the task's order when s is a multiple of periodicSteps, FLIP (0)
+// otherwise; FMPM(k) as +k, XPIC(k) as -k
+inline int xpic_step_order(const MpmGpuOptions &o, long long s) {
+    if (o.xpic_order <= 0 || o.xpic_period <= 0 || s % o.xpic_period != 0) return 0;
+    return o.xpic_fmpm ? o.xpic_order : -o.xpic_order;
+}
 
 // event of kernel family k in step slot `slot` of the current call
 inline cudaEvent_t &event_at(MpmGpuCtx *c, int slot, int k, bool begin) {

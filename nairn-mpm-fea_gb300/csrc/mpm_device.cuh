@@ -127,6 +127,7 @@ struct StepParams {
     const int *nrun;   // run of each node (-1: unused)
     DevContact ct;     // one field unless multimaterial mode
     DevDet det;        // deterministic node sums (single-run contexts only)
+    int xpic;          // particle update of this step: 0 FLIP, k > 0 FMPM(k), -k XPIC(k)
 };
 
 // Velocity conditions grouped by node, list order kept inside a node.

@@ -221,6 +221,14 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     if (opts->p2g != MPMGPU_P2G_ATOMIC && opts->p2g != MPMGPU_P2G_DETERMINISTIC)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "p2g must be MPMGPU_P2G_ATOMIC or MPMGPU_P2G_DETERMINISTIC");
     if (!(opts->timestep > 0.)) return set_err(nullptr, MPMGPU_ERR_INVALID, "timestep must be > 0");
+    if (opts->xpic_order < 0 || opts->xpic_order > 64 || (opts->xpic_fmpm != 0 && opts->xpic_fmpm != 1) ||
+        (opts->xpic_order > 0 && opts->xpic_period < 1))
+        return set_err(nullptr, MPMGPU_ERR_INVALID, "xpic_order must be 0 to 64, xpic_fmpm 0 or 1, xpic_period >= 1");
+    if (opts->xpic_order > 0 && opts->nfields > 1)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "XPIC/FMPM with multimaterial contact is not implemented");
+    if (opts->xpic_order > 1 && opts->p2g == MPMGPU_P2G_DETERMINISTIC)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED,
+                       "XPIC/FMPM of order > 1 with deterministic node sums is not implemented");
     if (grid->nx < 3 || grid->ny < 3 || (grid->dim == 3 && grid->nz < 3) || !grid->xnodes || !grid->ynodes ||
         (grid->dim == 3 && !grid->znodes))
         return set_err(nullptr, MPMGPU_ERR_INVALID, "grid needs >= 3 elements per axis and node coordinates");
@@ -609,6 +617,20 @@ int step_impl(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
         }
         c->ct.lr = c->lr_out;
     }
+    if (c->opts.xpic_order > 1 && !c->xpic_block) {
+        // PeriodicXPIC expansion: v*(prev), v*(next) and 1 / mass of every
+        // node, in FP64 and FP32
+        const size_t nn = (size_t)c->g.nnodes;
+        cudaError_t e = cudaMalloc(&c->xpic_block, 7 * nn * (sizeof(double) + sizeof(float)));
+        if (e != cudaSuccess) {
+            c->xpic_block = nullptr;
+            return set_err(c, MPMGPU_ERR_OOM, "XPIC node columns");
+        }
+        double *b = c->xpic_block;
+        float *f = (float *)(b + 7 * nn);
+        c->xpic = DevXpic{b,     b + nn,     b + 2 * nn, b + 3 * nn, b + 4 * nn, b + 5 * nn, b + 6 * nn,
+                          f,     f + nn,     f + 2 * nn, f + 3 * nn, f + 4 * nn, f + 5 * nn, f + 6 * nn};
+    }
     std::vector<char> sorted((size_t)nsteps, 0);
     cudaEvent_t w0 = nullptr, w1 = nullptr;
     if (ms) {
@@ -834,6 +856,7 @@ void mpmgpu_destroy(MpmGpuCtx *c) {
     if (c->err) cudaFree(c->err);
     if (c->archive_pending) cudaEventSynchronize(c->archive_copied);
     if (c->archive_buf) cudaFree(c->archive_buf);
+    if (c->xpic_block) cudaFree(c->xpic_block);
     if (c->archive_packed) cudaEventDestroy(c->archive_packed);
     if (c->archive_copied) cudaEventDestroy(c->archive_copied);
     if (c->archive_stream) cudaStreamDestroy(c->archive_stream);

@@ -1213,14 +1213,28 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
         }
     });
     double xp[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
+    if (sp.xpic == 0) {
+        // FLIP (MatPoint2D/3D::MoveParticle, m == 0)
 #pragma unroll
-    for (int a = 0; a < DIM; a++) {
-        const double sv = MIX ? v[a] + (double)Sv[a] : (double)Sv[a];
-        const double sa = (double)Sa[a];
-        const double vm = sv - sa * dt;
-        const double dv = sa * dt;
-        v[a] += dv;
-        xp[a] += (vm + 0.5 * dv) * dt;
+        for (int a = 0; a < DIM; a++) {
+            const double sv = MIX ? v[a] + (double)Sv[a] : (double)Sv[a];
+            const double sa = (double)Sa[a];
+            const double vm = sv - sa * dt;
+            const double dv = sa * dt;
+            v[a] += dv;
+            xp[a] += (vm + 0.5 * dv) * dt;
+        }
+    } else {
+        // FMPM (m > 0) and XPIC (m < 0) take the particle velocity S v(k)
+        // (MatPoint2D.cpp:120-182, MatPoint3D.cpp:124-181); no damping
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            const double sv = MIX ? v[a] + (double)Sv[a] : (double)Sv[a];
+            const double vold = v[a];
+            v[a] = sv;
+            if (sp.xpic > 0) xp[a] += DIM == 3 ? (vold + sv) * (0.5 * dt) : 0.5 * (vold + sv) * dt;
+            else xp[a] += (sv + 0.5 * (sv - vold)) * dt;
+        }
     }
     p.vx[i] = v[0];
     p.vy[i] = v[1];
@@ -1703,7 +1717,7 @@ static __global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBC
 // extrapolation.
 template <int DIM, bool MIX, bool BATCH>
 static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, DevBCs b, const int *bc_group,
-                              int zero_contact) {
+                              int zero_contact, int update_bcs = 1) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !node_active(sp, nd, n)) return;
     double t, dt;
@@ -1739,7 +1753,9 @@ static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, Dev
             nd.fz[k] = fr[2];
             continue;
         }
-        if (grp >= 0) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, fr);
+        // NodalVelBC::GridVelocityConditions skips this pass for XPIC/FMPM(k > 1)
+        // (NodalVelBC.cpp:367-374)
+        if (grp >= 0 && update_bcs) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, fr);
         node_finish_update<DIM, MIX>(nd, k, m, p, fr);
     }
     if (!mm) return;
@@ -1879,3 +1895,4 @@ static __global__ void k_advance_runs(DevRun *runs, int nruns) {
 }  // namespace nmg
 
 #include "lr.cuh"
+#include "xpic.cuh"

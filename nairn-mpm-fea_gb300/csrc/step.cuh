@@ -39,6 +39,21 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     sp.runs = nullptr;
     sp.nrun = nullptr;
     sp.det = c->det;
+    // PeriodicXPIC: this step's order (steps counted from 1 at time 0)
+    const int xm = xpic_step_order(c->opts, (long long)llround(t / dt) + 1);
+    sp.xpic = xm;
+    const int xk = xm < 0 ? -xm : xm;
+    const DevXpic xp = c->xpic;
+    // XPIC(k)/FMPM(k) expansion of the node velocities (k > 1)
+    auto xpic_expand = [&](int fmpm) {
+        k_xpic_init<DIM, MIX><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, fmpm);
+        c->launches++;
+        for (int k = 2; k <= xk; k++) {
+            k_xpic_pass<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, xp);
+            k_xpic_delta<DIM, MIX><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, c->bcs, c->bc_group);
+            c->launches += 2;
+        }
+    };
     const int NT = NN * c->ct.nf, ntb = (NT + TB - 1) / TB;
     mark(0, true);
     if (DET) {
@@ -80,6 +95,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     k_node_post<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL);
     mark(1, false);
     mark(2, true);
+    if (xm > 1 && method != MPMGPU_USL) xpic_expand(1);  // FMPM(k) velocities of the first strain update
     if (method == MPMGPU_USL)
         k_strain_forces<DIM, SHAPE, false, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     else
@@ -93,9 +109,10 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     mark(3, true);
     if (lr) lr_normals();  // the deformed radii changed with the strain update
     k_node_update<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group,
-                                                     c->ct.nf > 1 && method != MPMGPU_USF);
+                                                     c->ct.nf > 1 && method != MPMGPU_USF, xk > 1 ? 0 : 1);
     mark(3, false);
     mark(4, true);
+    if (xk > 1) xpic_expand(xm > 0 ? 1 : 0);  // v(k) of the particle update
     if (method == MPMGPU_USF) {
         k_g2p<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
         mark(4, false);
@@ -113,6 +130,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     k_node_usl<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
     mark(5, false);
     mark(6, true);
+    if (xm > 1) xpic_expand(1);  // FMPM(k) velocities of the second strain update
     k_strain_last<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     mark(6, false);
 }

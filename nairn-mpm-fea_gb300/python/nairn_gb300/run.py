@@ -44,6 +44,9 @@ def main(argv=None):
     ap.add_argument("--normals", type=int, choices=(0, 1, 2, 5, 6), default=2,
                     help="contact normal method (contact3d): 0-2 volume gradients, 5/6 regressions")
     ap.add_argument("--gap", type=float, default=0.0, help="block-to-plate gap in mm (contact3d)")
+    ap.add_argument("--xpic", type=int, default=0, help="PeriodicXPIC order (cantilever, taylor; 0: FLIP)")
+    ap.add_argument("--fmpm", action="store_true", help="FMPM(k) instead of XPIC(k)")
+    ap.add_argument("--xpic-period", type=int, default=1, help="PeriodicXPIC periodicSteps")
     ap.add_argument("--p2g", choices=("atomic", "deterministic"), default="atomic")
     ap.add_argument("--profile", action="store_true", help="per-kernel ms of the timed steps (single runs)")
     a = ap.parse_args(argv)
@@ -65,10 +68,11 @@ def main(argv=None):
                "particle_steps_per_s": n * a.steps / (t / 1e3), "info": b.info()}
         b.close()
     else:
+        xp = (a.xpic, 1 if a.fmpm else 0, a.xpic_period) if a.xpic > 0 else None
         if a.workload == "cantilever":
-            m = model.cantilever_2d(nx=a.nx, ny=a.ny, steps=total)
+            m = model.cantilever_2d(nx=a.nx, ny=a.ny, steps=total, xpic=xp)
         elif a.workload == "taylor":
-            m = model.taylor_3d(radius=a.radius, length=a.length, cell=a.cell, steps=total)
+            m = model.taylor_3d(radius=a.radius, length=a.length, cell=a.cell, steps=total, xpic=xp)
         elif a.workload == "block2d":
             m = model.block_2d(ncx=a.cells, ncy=a.cells, steps=total)
         elif a.workload == "contact3d":
@@ -93,6 +97,8 @@ def main(argv=None):
     out["precision"] = a.precision
     out["sort_interval"] = a.sort_interval
     out["p2g"] = a.p2g
+    if a.xpic > 0:
+        out["xpic"] = {"order": a.xpic, "fmpm": a.fmpm, "period": a.xpic_period}
     if a.workload == "contact3d":
         out["normals"] = a.normals
     print(json.dumps(out))

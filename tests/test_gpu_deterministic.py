@@ -33,6 +33,8 @@ def same_bits(a, b, what=""):
 def test_deterministic_mode_matches_reference(case, gpu_lib):
     meta, g = load_golden(case)
     m = model_for(meta)
+    if m.options.get("xpic_order", 0) > 1:
+        pytest.skip("XPIC/FMPM of order > 1 runs with atomic node sums only (refused with UNSUPPORTED)")
     v = view_for(run(m, meta["steps"], p2g=DET), m)
     for k in ("pos", "vel", "stress", "strain"):
         assert rel_l2(v[k], g["final_" + k]) <= TOL, (k, rel_l2(v[k], g["final_" + k]))

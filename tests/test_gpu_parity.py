@@ -184,3 +184,37 @@ def test_sort_autotune_keeps_results(gpu_lib):
     oracle_lib.run(m, ref, 4 + 64 + 4)
     for k in ("x", "y", "z", "vx", "vz", "szz", "sxy", "hist0"):
         assert rel_l2(out[k], ref[k]) <= TOL, k
+
+
+def test_xpic_schedule_follows_the_step_time(gpu_lib):
+    """The PeriodicXPIC schedule counts steps from the time each call starts
+    at: a run split into calls of odd lengths meets the reference's golden
+    (FMPM(2) on every second step, USL)."""
+    from nairn_gb300.gpu import GpuRun
+    meta, g = load_golden("cant2d_fmpm2_usl_every2")
+    m = model_for(meta)
+    r = GpuRun(m)
+    r.upload(m.particles)
+    for n in (7, 12, meta["steps"] - 19):
+        r.step(n)
+    v = view_for(r.download(m.particles), m)
+    r.close()
+    for k in ("pos", "vel", "stress", "strain"):
+        assert rel_l2(v[k], g["final_" + k]) <= TOL, (k, rel_l2(v[k], g["final_" + k]))
+
+
+def test_xpic_refusals(gpu_lib):
+    """XPIC/FMPM is refused with multimaterial contact, and orders above 1
+    with deterministic node sums; a bad period is invalid."""
+    from nairn_gb300 import model
+    from nairn_gb300.gpu import GpuRun, GpuError
+    c = model.contact_2d(plate=(16, 4), block=(5, 3), steps=5)
+    c.options.update(xpic_order=2, xpic_fmpm=0, xpic_period=1)
+    with pytest.raises(GpuError, match="UNSUPPORTED"):
+        GpuRun(c)
+    m = model.cantilever_2d(nx=10, ny=4, steps=5, xpic=(2, 1, 1))
+    with pytest.raises(GpuError, match="UNSUPPORTED"):
+        GpuRun(m, p2g=1)
+    m.options["xpic_period"] = 0
+    with pytest.raises(GpuError, match="INVALID"):
+        GpuRun(m)

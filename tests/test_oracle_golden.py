@@ -22,18 +22,21 @@ def test_model_builder_matches_reference_setup(case):
 
 @pytest.mark.parametrize("case", golden_cases())
 def test_oracle_matches_reference(case):
-    """The FP64 restatement reproduces the reference's final state (bit-exact in practice)."""
+    """The FP64 restatement reproduces the reference's final state (bit-exact in
+    practice; within 1e-12 with XPIC/FMPM of order > 1, whose double loop over
+    each particle's nodes may add in another order)."""
     import oracle_lib
     meta, g = load_golden(case)
     m = model_for(meta)
     p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
     oracle_lib.run(m, p, meta["steps"], nthreads=1)
     v = view_for(p, m)
+    tol = 1e-12 if m.options.get("xpic_order", 0) > 1 else 1e-13
     for k in ("pos", "vel", "stress", "strain"):
-        assert rel_l2(v[k], g["final_" + k]) <= 1e-13, k
+        assert rel_l2(v[k], g["final_" + k]) <= tol, (k, rel_l2(v[k], g["final_" + k]))
     if g["final_hist1"].any():
-        assert rel_l2(v["hist1"], g["final_hist1"]) <= 1e-13
-        assert rel_l2(v["plastic"], g["final_plastic"]) <= 1e-13
+        assert rel_l2(v["hist1"], g["final_hist1"]) <= tol
+        assert rel_l2(v["plastic"], g["final_plastic"]) <= tol
     assert np.array_equal(v["elem"], g["final_elem"])
 
 
@@ -99,3 +102,16 @@ def test_regression_contact_is_chaotic_and_gradient_contact_is_not():
 
     assert moved("contact2d_fric_logreg") > 1e-4
     assert moved("contact2d_fric_avgg") < 1e-7
+
+
+def test_xpic_and_fmpm_change_the_result():
+    """The PeriodicXPIC goldens are not FLIP runs: the same problem with FLIP
+    on every step ends far from them (so their parity tests test XPIC/FMPM)."""
+    import oracle_lib
+    for case in [c for c in golden_cases() if load_golden(c)[0]["kwargs"].get("xpic")]:
+        meta, g = load_golden(case)
+        kw = {k: v for k, v in meta["kwargs"].items() if k != "xpic"}
+        m = model_for(dict(meta, kwargs=kw))
+        p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
+        oracle_lib.run(m, p, meta["steps"], nthreads=1)
+        assert rel_l2(view_for(p, m)["vel"], g["final_vel"]) > 0.1, case
