@@ -389,7 +389,7 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     const bool lr = b->lr_runs > 0;
     const int lrb = (int)(((long long)NN * 32 + NTB - 1) / NTB);  // a warp per node
     auto lr_normals = [&]() {
-        k_lr_normals<DIM, true><<<lrb, NTB, 0, s>>>(sp, b->p, b->nd, b->mats, b->lr_start,
+        k_lr_normals<DIM, true><<<lrb * b->nf, NTB, 0, s>>>(sp, b->p, b->nd, b->mats, b->lr_start,
                                                                          b->lr_list, b->lr_out, NN, b->lr_cap, 1);
     };
     if (lr) {

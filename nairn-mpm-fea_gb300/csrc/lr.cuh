@@ -191,7 +191,7 @@ __device__ __forceinline__ double lr_radius(const DevGrid &g, const DevParticles
     return 1. / sqrt(n0x * n0x / (px * px) + n0y * n0y / (py * py) + n0z * n0z / (pz * pz));
 }
 
-// One warp per grid node with links: for every material field present, the
+// One warp per grid node with links and material field present: the
 // regression normal against the other materials lumped and the separation
 // deln, written as (nx, ny, nz, deln) at out[4 (f fstride + n)].  Constants
 // of MachineLearning.cpp with PENALIZE_NORMALS: linear offset penalty 0.1;
@@ -201,7 +201,9 @@ template <int DIM, bool BATCH>
 static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevParticles p, DevNodes nd,
                                                            const DevMat *mats, const int *start, const int *list,
                                                            double *out, int nnodes, long long cap, int logistic) {
-    const int n = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
+    // one warp per (node, material field): the fields' regressions are independent
+    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
+    const int n = (int)(w / sp.ct.nf), a0 = (int)(w % sp.ct.nf);
     const int lane = threadIdx.x & 31;
     if (n >= nnodes) return;  // whole warps
     const int s0 = start[n], s1 = start[n + 1];
@@ -225,7 +227,26 @@ static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevPar
     const double offsetLin = 0.1, normLog = 1.e-7, offsetLog = 0., tol = 1.e-5;
     const int maxIter = 15;
     constexpr int NB = DIM == 3 ? 4 : 3, NM = DIM == 3 ? 10 : 6;
-    for (int a = 0; a < sp.ct.nf; a++) {
+    // the lane's first kLrCached linked particles (positions relative to the
+    // node and material field) stay in registers through all the regression
+    // steps; longer lists read the rest from memory at each step
+    constexpr int kLrCached = 4;
+    double cx[kLrCached], cy[kLrCached], cz[kLrCached];
+    int cf[kLrCached];
+#pragma unroll
+    for (int r = 0; r < kLrCached; r++) {
+        const int k = s0 + lane + 32 * r;
+        cx[r] = cy[r] = cz[r] = 0.;
+        cf[r] = -1;
+        if (k < s1) {
+            const int q = list[k];
+            cf[r] = mats[p.mat[q]].field;
+            cx[r] = p.x[q] - ndx;
+            cy[r] = p.y[q] - ndy;
+            cz[r] = DIM == 3 ? p.z[q] - ndz : 0.;
+        }
+    }
+    for (int a = a0; a <= a0; a++) {  // this warp's field
         const int ka = a * sp.ct.fstride + n;
         if (!nd.active[ka]) continue;
         double nrm[3] = {0., 0., 0.};
@@ -240,10 +261,7 @@ static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevPar
             for (int k = 0; k < NM; k++) mt[k] = 0.;
 #pragma unroll
             for (int k = 0; k < NB; k++) rhs[k] = 0.;
-            for (int k = s0 + lane; k < s1; k += 32) {
-                const int q = list[k];
-                const double mi = mats[p.mat[q]].field == a ? -1. : 1.;
-                const double x = p.x[q] - ndx, y = p.y[q] - ndy, z = DIM == 3 ? p.z[q] - ndz : 0.;
+            auto add = [&](double x, double y, double z, double mi) {
                 double w2 = 1., wr = mi;
                 if (!lin) {
                     const double dotp = DIM == 3 ? x * beta[0] + y * beta[1] + z * beta[2] + beta[3]
@@ -279,6 +297,14 @@ static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevPar
                     rhs[1] += wr * y;
                     rhs[2] += wr;
                 }
+            };
+#pragma unroll
+            for (int r = 0; r < kLrCached; r++)
+                if (s0 + lane + 32 * r < s1) add(cx[r], cy[r], cz[r], cf[r] == a ? -1. : 1.);
+            for (int k = s0 + lane + 32 * kLrCached; k < s1; k += 32) {
+                const int q = list[k];
+                const double mi = mats[p.mat[q]].field == a ? -1. : 1.;
+                add(p.x[q] - ndx, p.y[q] - ndy, DIM == 3 ? p.z[q] - ndz : 0., mi);
             }
 #pragma unroll
             for (int k = 0; k < NM; k++) mt[k] = lr_wsum(mt[k]);

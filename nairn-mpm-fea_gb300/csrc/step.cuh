@@ -69,7 +69,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     const bool lr = c->ct.nf > 1 && c->ct.normals >= 5;
     const int lrb = (int)(((long long)NN * 32 + TB - 1) / TB);  // a warp per node
     auto lr_normals = [&]() {
-        k_lr_normals<DIM, false><<<lrb, TB, 0, s>>>(sp, c->p, c->nd, c->mats, c->lr_start, c->lr_list, c->lr_out,
+        k_lr_normals<DIM, false><<<lrb * c->ct.nf, TB, 0, s>>>(sp, c->p, c->nd, c->mats, c->lr_start, c->lr_list, c->lr_out,
                                                     NN, c->lr_cap, c->ct.normals == 6 ? 1 : 0);
         c->launches++;
     };
