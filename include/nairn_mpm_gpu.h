@@ -341,6 +341,9 @@ typedef struct {
                                  methods; 64 in 3D, 16 in 2D always suffice; a
                                  run whose links do not fit fails with
                                  MPMGPU_ERR_RANGE */
+    int32_t xpic_order;       /* PeriodicXPIC of every run (MpmGpuOptions;  */
+    int32_t xpic_fmpm;        /* each run counts its own steps from 1);    */
+    int32_t xpic_period;      /* one material field only; 0: FLIP          */
 } MpmGpuBatchOptions;
 
 /* run states returned by mpmgpu_batch_run_state; a failed run reports the
@@ -419,6 +422,8 @@ typedef struct {
     int32_t max_fields;         /* material velocity fields per run (0: 1)     */
     int32_t lr_links;           /* links per particle slot for regression normals
                                    (MpmGpuBatchOptions; capped at 16 in 2D)   */
+    int32_t xpic_order, xpic_fmpm, xpic_period;  /* PeriodicXPIC of every request
+                                   (MpmGpuBatchOptions)                       */
 } MpmGpuServerOptions;
 
 enum { MPMGPU_REQ_QUEUED = 1, MPMGPU_REQ_RUNNING = 2, MPMGPU_REQ_DONE = 3, MPMGPU_REQ_FAILED = 4 };

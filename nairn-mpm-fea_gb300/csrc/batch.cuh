@@ -197,6 +197,9 @@ struct MpmGpuBatch {
     double *lr_out = nullptr;
     long long lr_cap = 0;
     int lr_runs = 0;  // resident runs with regression normals
+    // PeriodicXPIC expansion columns (xpic_order > 1)
+    DevXpic xpic{};
+    double *xpic_block = nullptr;
     // materials, runs, velocity conditions
     DevMat *mats = nullptr;
     DevRun *runs_dev = nullptr;
@@ -267,7 +270,7 @@ void batch_free(MpmGpuBatch *b) {
     void *ptrs[] = {b->pbuf[0], b->pbuf[1], b->ibuf[0], b->ibuf[1], b->nblock, b->fblock, b->coords, b->nrun,
                     b->bc_group, b->keys[0], b->keys[1], b->vals[0], b->vals[1], b->hist, b->sums, b->mats,
                     b->runs_dev, b->bc_block, b->flag, b->cpdi, b->lr_cnt, b->lr_start, b->lr_list, b->lr_sums,
-                    b->lr_out};
+                    b->lr_out, b->xpic_block};
     for (void *q : ptrs)
         if (q) cudaFree(q);
     if (b->stream) cudaStreamDestroy(b->stream);
@@ -409,6 +412,16 @@ void batch_enqueue_step(MpmGpuBatch *b) {
         lr_normals();
     }
     k_node_post<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, method != MPMGPU_USL);
+    // PeriodicXPIC expansions: every run whose mode of this step takes part
+    const int xo = b->o.xpic_order, xf = b->o.xpic_fmpm;
+    auto xpic_expand = [&](int phase) {
+        k_xpic_init<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, phase);
+        for (int k = 2; k <= xo; k++) {
+            k_xpic_pass<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->xpic, phase, k);
+            k_xpic_delta<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, b->bcs, b->bc_group, phase, k);
+        }
+    };
+    if (xo > 1 && xf && method != MPMGPU_USL) xpic_expand(XPIC_STRAIN);  // FMPM: first strain update
     if (method == MPMGPU_USL)
         k_strain_forces<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     else
@@ -416,15 +429,18 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     if (lr) lr_normals();  // the deformed radii changed with the strain update
     k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group,
                                                     b->nf > 1 && method != MPMGPU_USF);
+    if (xo > 1) xpic_expand(XPIC_PARTICLE);  // v(k) of the particle update
     if (method == MPMGPU_USF) {
         k_g2p<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     } else {
         k_g2p<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
         if (lr) lr_normals();  // the particles moved
         k_node_usl<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group);
+        if (xo > 1 && xf) xpic_expand(XPIC_STRAIN);  // FMPM: second strain update
         k_strain_last<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     }
-    k_advance_runs<<<(b->o.max_runs + 127) / 128, 128, 0, s>>>(b->runs_dev, b->o.max_runs);
+    k_advance_runs<<<(b->o.max_runs + 127) / 128, 128, 0, s>>>(b->runs_dev, b->o.max_runs, xo, xf,
+                                                                b->o.xpic_period);
 }
 
 template <int DIM, bool MIX>
@@ -442,7 +458,12 @@ void batch_enqueue_any(MpmGpuBatch *b) {
 
 int batch_step_launches(const MpmGpuBatch *b) {
     const bool usf = b->o.method == MPMGPU_USF;
-    return (usf ? 7 : 9) + (b->lr_runs > 0 ? 6 + (usf ? 2 : 3) : 0);
+    // an expansion: init, then a particle and a node pass per order above 1;
+    // one before the particle update, FMPM one before each strain update
+    const int xo = b->o.xpic_order, expand = xo > 1 ? 1 + 2 * (xo - 1) : 0;
+    const int strain_updates = (b->o.method != MPMGPU_USL ? 1 : 0) + (usf ? 0 : 1);
+    const int expansions = xo > 1 ? 1 + (b->o.xpic_fmpm ? strain_updates : 0) : 0;
+    return (usf ? 7 : 9) + (b->lr_runs > 0 ? 6 + (usf ? 2 : 3) : 0) + expansions * expand;
 }
 
 long long batch_graph_key(const MpmGpuBatch *b) {
@@ -609,6 +630,7 @@ int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *o) {
     bytes += N * nf * (int64_t)((nf > 1 ? 26 : 19) * sizeof(double) + 12 * sizeof(float) + 1);
     bytes += N * (int64_t)(2 * sizeof(int) + sizeof(double));
     bytes += (int64_t)o->max_materials * (int64_t)sizeof(DevMat) + (int64_t)o->max_runs * (int64_t)sizeof(DevRun);
+    if (o->xpic_order > 1) bytes += 7 * N * (int64_t)(sizeof(double) + sizeof(float));  // XPIC columns
     if (nf > 1 && o->lr_links > 0) {
         // regression-normal links, counts, offsets, scan sums, results
         bytes += P * o->lr_links * (int64_t)sizeof(int) + 2 * (N + 1) * (int64_t)sizeof(int);
@@ -631,6 +653,11 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     if (o->max_fields < 0 || o->max_fields > kMaxFields)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "max_fields must be 0 to 8");
     if (o->lr_links < 0 || o->lr_links > 64) return berr(nullptr, MPMGPU_ERR_INVALID, "lr_links must be 0 to 64");
+    if (o->xpic_order < 0 || o->xpic_order > 64 || (o->xpic_fmpm != 0 && o->xpic_fmpm != 1) ||
+        (o->xpic_order > 0 && o->xpic_period < 1))
+        return berr(nullptr, MPMGPU_ERR_INVALID, "xpic_order must be 0 to 64, xpic_fmpm 0 or 1, xpic_period >= 1");
+    if (o->xpic_order > 0 && o->max_fields > 1)
+        return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "XPIC/FMPM with multimaterial contact is not implemented");
     if (o->max_particles <= 0 || o->max_particles > (1LL << 31) - 1 || o->max_nodes <= 0 ||
         o->max_nodes > (1LL << 30) || o->max_runs <= 0 || o->max_runs > (1 << 20) || o->max_materials <= 0 ||
         o->max_materials > (1 << 24))
@@ -671,6 +698,15 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     A((void **)&b->mats, (size_t)o->max_materials * sizeof(DevMat));
     A((void **)&b->runs_dev, (size_t)o->max_runs * sizeof(DevRun));
     A((void **)&b->flag, sizeof(unsigned));
+    if (o->xpic_order > 1) {
+        A((void **)&b->xpic_block, 7 * N * (sizeof(double) + sizeof(float)));
+        if (e == cudaSuccess) {
+            double *d = b->xpic_block;
+            float *f = (float *)(d + 7 * N);
+            b->xpic = DevXpic{d, d + N, d + 2 * N, d + 3 * N, d + 4 * N, d + 5 * N, d + 6 * N,
+                              f, f + N, f + 2 * N, f + 3 * N, f + 4 * N, f + 5 * N, f + 6 * N};
+        }
+    }
     if (b->nf > 1 && o->lr_links > 0) {
         b->lr_cap = (long long)P * o->lr_links;
         A((void **)&b->lr_cnt, (N + 1) * sizeof(int));
@@ -846,6 +882,7 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     R.normals = mm ? contact->normals : 2;
     R.friction = mm ? contact->friction : 0.;
     R.style = !mm ? 2 : (contact->friction < 0. ? 0 : (contact->friction == 0. ? 1 : 2));
+    R.xpic = xpic_mode(b->o.xpic_order, b->o.xpic_fmpm, b->o.xpic_period, 1);  // its first step
     BCK(cudaMemcpyAsync(b->runs_dev + r, &R, sizeof(DevRun), cudaMemcpyHostToDevice, s));
     unsigned bad = 0;
     BCK(cudaMemcpyAsync(&bad, b->flag, sizeof(unsigned), cudaMemcpyDeviceToHost, s));

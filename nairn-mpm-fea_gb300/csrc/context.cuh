@@ -74,14 +74,9 @@ struct MpmGpuCtx {
 
 namespace nmg {
 
-// PeriodicXPIC::PrepareForStep / StepCalculation (NairnMPM/src/Custom_Tasks/
-// PeriodicXPIC.cpp:351-370, 427-445), the custom tasks running once before
-// the first step and after each step (NairnMPM.cpp:171-200): step s (from 1)
-// uses the task's order when s is a multiple of periodicSteps, FLIP (0)
-// otherwise; FMPM(k) as +k, XPIC(k) as -k
+// the PeriodicXPIC mode of step s (from 1) of a single-run context
 inline int xpic_step_order(const MpmGpuOptions &o, long long s) {
-    if (o.xpic_order <= 0 || o.xpic_period <= 0 || s % o.xpic_period != 0) return 0;
-    return o.xpic_fmpm ? o.xpic_order : -o.xpic_order;
+    return xpic_mode(o.xpic_order, o.xpic_fmpm, o.xpic_period, s);
 }
 
 // event of kernel family k in step slot `slot` of the current call

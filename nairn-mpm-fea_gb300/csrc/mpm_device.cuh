@@ -114,7 +114,18 @@ struct DevRun {
     int mm;            // multimaterial contact on for this run
     int normals, style;
     double friction;   // the run's contact law (DevContact fields)
+    int xpic;          // this step's PeriodicXPIC mode (0 FLIP, k FMPM(k), -k XPIC(k))
 };
+
+// PeriodicXPIC::PrepareForStep / StepCalculation (NairnMPM/src/Custom_Tasks/
+// PeriodicXPIC.cpp:351-370, 427-445), the custom tasks running once before
+// the first step and after each step (NairnMPM.cpp:171-200): step s (from 1)
+// uses the task's order when s is a multiple of periodicSteps, FLIP (0)
+// otherwise; FMPM(k) as +k, XPIC(k) as -k
+__host__ __device__ __forceinline__ int xpic_mode(int order, int fmpm, int period, long long s) {
+    if (order <= 0 || period <= 0 || s % period != 0) return 0;
+    return fmpm ? order : -order;
+}
 
 // Per-launch step parameters.  A single-run context uses g, dt, st_first,
 // st_last, t and err directly; a batch (BATCH = true in the kernels) reads the

@@ -1213,7 +1213,8 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
         }
     });
     double xp[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
-    if (sp.xpic == 0) {
+    const int xmode = BATCH ? sp.runs[p.run[i]].xpic : sp.xpic;
+    if (xmode == 0) {
         // FLIP (MatPoint2D/3D::MoveParticle, m == 0)
 #pragma unroll
         for (int a = 0; a < DIM; a++) {
@@ -1232,7 +1233,7 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
             const double sv = MIX ? v[a] + (double)Sv[a] : (double)Sv[a];
             const double vold = v[a];
             v[a] = sv;
-            if (sp.xpic > 0) xp[a] += DIM == 3 ? (vold + sv) * (0.5 * dt) : 0.5 * (vold + sv) * dt;
+            if (xmode > 0) xp[a] += DIM == 3 ? (vold + sv) * (0.5 * dt) : 0.5 * (vold + sv) * dt;
             else xp[a] += (sv + 0.5 * (sv - vold)) * dt;
         }
     }
@@ -1725,6 +1726,10 @@ static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, Dev
     const int grp = bc_group[n];
     const DevContact ct = node_contact_params<BATCH>(sp, n);
     const bool mm = ct.nf > 1;
+    if (BATCH) {
+        const int xm = sp.runs[sp.nrun[n]].xpic;
+        update_bcs = xm >= -1 && xm <= 1;
+    }
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;
         if (!nd.active[k]) continue;
@@ -1879,7 +1884,7 @@ static __global__ void k_det_resolve(StepParams sp, DevNodes nd, int nn, int pha
 // End of a batched step: advance the time of every active run and retire
 // runs that have taken all their steps.  A run that raised an error stops
 // here, so the error stays confined to its own particles and nodes.
-static __global__ void k_advance_runs(DevRun *runs, int nruns) {
+static __global__ void k_advance_runs(DevRun *runs, int nruns, int xpic_order, int xpic_fmpm, int xpic_period) {
     const int r = blockIdx.x * blockDim.x + threadIdx.x;
     if (r >= nruns) return;
     DevRun &R = runs[r];
@@ -1890,6 +1895,8 @@ static __global__ void k_advance_runs(DevRun *runs, int nruns) {
     }
     R.t += R.dt;
     if (--R.steps_left <= 0) R.active = 0;
+    // the PeriodicXPIC mode of the run's next step
+    R.xpic = xpic_mode(xpic_order, xpic_fmpm, xpic_period, (long long)floor(R.t / R.dt + 0.5) + 1);
 }
 
 }  // namespace nmg

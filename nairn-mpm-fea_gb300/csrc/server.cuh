@@ -285,6 +285,9 @@ int mpmgpu_server_create(const MpmGpuServerOptions *o, MpmGpuServer **out) {
         bo.max_materials = 4 * o->max_runs;
         bo.max_fields = o->max_fields;
         bo.lr_links = o->lr_links > 0 ? std::min(o->lr_links, d == 1 ? 64 : 16) : 0;
+        bo.xpic_order = o->xpic_order;
+        bo.xpic_fmpm = o->xpic_fmpm;
+        bo.xpic_period = o->xpic_period;
         bo.fraction_usf = o->fraction_usf;
         const int64_t P = server_capacity(bo, bytes, s->o.nodes_per_particle);
         if (P < 1000) {

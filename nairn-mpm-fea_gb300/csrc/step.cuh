@@ -45,12 +45,12 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     const int xk = xm < 0 ? -xm : xm;
     const DevXpic xp = c->xpic;
     // XPIC(k)/FMPM(k) expansion of the node velocities (k > 1)
-    auto xpic_expand = [&](int fmpm) {
-        k_xpic_init<DIM, MIX><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, fmpm);
+    auto xpic_expand = [&](int phase) {
+        k_xpic_init<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, phase);
         c->launches++;
         for (int k = 2; k <= xk; k++) {
-            k_xpic_pass<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, xp);
-            k_xpic_delta<DIM, MIX><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, c->bcs, c->bc_group);
+            k_xpic_pass<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, xp, phase, k);
+            k_xpic_delta<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, c->bcs, c->bc_group, phase, k);
             c->launches += 2;
         }
     };
@@ -95,7 +95,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     k_node_post<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group, method != MPMGPU_USL);
     mark(1, false);
     mark(2, true);
-    if (xm > 1 && method != MPMGPU_USL) xpic_expand(1);  // FMPM(k) velocities of the first strain update
+    if (xm > 1 && method != MPMGPU_USL) xpic_expand(XPIC_STRAIN);  // FMPM(k) velocities of the first strain update
     if (method == MPMGPU_USL)
         k_strain_forces<DIM, SHAPE, false, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     else
@@ -112,7 +112,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
                                                      c->ct.nf > 1 && method != MPMGPU_USF, xk > 1 ? 0 : 1);
     mark(3, false);
     mark(4, true);
-    if (xk > 1) xpic_expand(xm > 0 ? 1 : 0);  // v(k) of the particle update
+    if (xk > 1) xpic_expand(XPIC_PARTICLE);  // v(k) of the particle update
     if (method == MPMGPU_USF) {
         k_g2p<DIM, SHAPE, false, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
         mark(4, false);
@@ -130,7 +130,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     k_node_usl<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
     mark(5, false);
     mark(6, true);
-    if (xm > 1) xpic_expand(1);  // FMPM(k) velocities of the second strain update
+    if (xm > 1) xpic_expand(XPIC_STRAIN);  // FMPM(k) velocities of the second strain update
     k_strain_last<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     mark(6, false);
 }

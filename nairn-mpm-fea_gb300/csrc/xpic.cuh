@@ -31,6 +31,19 @@ struct DevXpic {
     float *frm;
 };
 
+// Expansion phases: before a strain update (FMPM only) or before the
+// particle update.  A run takes part in phase `phase` at pass k (init: k = 1)
+// when its mode of this step has order >= k and >= 2 (FMPM for phase 0).  A
+// single-run context reads the mode from StepParams, a batch run from its
+// DevRun.
+enum { XPIC_STRAIN = 0, XPIC_PARTICLE = 1 };
+
+__device__ __forceinline__ bool xpic_takes_part(int mode, int phase, int k) {
+    const int order = mode < 0 ? -mode : mode;
+    if (order < 2 || order < k) return false;
+    return phase == XPIC_PARTICLE || mode > 0;
+}
+
 // v* into the velocity columns the particle kernels read (FP32 pairs too in
 // the mixed mode)
 template <bool MIX>
@@ -46,11 +59,16 @@ __device__ __forceinline__ void xpic_store_velocity(const DevNodes &nd, int n, c
 }
 
 // INITIALIZE_XPIC from the node momentum (and, for XPIC, force)
-template <int DIM, bool MIX>
-static __global__ void k_xpic_init(StepParams sp, DevNodes nd, DevXpic x, int nnodes, int fmpm) {
+template <int DIM, bool MIX, bool BATCH>
+static __global__ void k_xpic_init(StepParams sp, DevNodes nd, DevXpic x, int nnodes, int phase) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !nd.active[n]) return;
-    const double dt = sp.dt, m = nd.mass[n];
+    double t, dt;
+    if (!node_run<BATCH>(sp, n, t, dt)) return;
+    const int mode = BATCH ? sp.runs[sp.nrun[n]].xpic : sp.xpic;
+    if (!xpic_takes_part(mode, phase, 1)) return;
+    const bool fmpm = phase == XPIC_STRAIN || mode > 0;
+    const double m = nd.mass[n];
     const double p[3] = {nd.px[n], nd.py[n], DIM == 3 ? nd.pz[n] : 0.};
     double vp[3], vs[3];
     if (fmpm) {
@@ -90,15 +108,18 @@ static __global__ void k_xpic_init(StepParams sp, DevNodes nd, DevXpic x, int nn
 
 // XPICDoubleLoop (XPICExtrapolationTask.cpp:182-211) of one particle:
 // v*(next)_i += m_p S_ip / m_i Sum_j S_jp v*(prev)_j
-template <int DIM, int SHAPE, bool MIX>
+template <int DIM, int SHAPE, bool MIX, bool BATCH>
 static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
-    k_xpic_pass(StepParams sp, DevParticles p, DevXpic x) {
+    k_xpic_pass(StepParams sp, DevParticles p, DevXpic x, int phase, int k) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
-    const DevGrid &g = sp.g;
+    RunView rv;
+    if (!particle_run<BATCH>(sp, p, i, rv)) return;
+    if (!xpic_takes_part(BATCH ? sp.runs[p.run[i]].xpic : sp.xpic, phase, k)) return;
+    const DevGrid &g = rv.g;
     T s[3] = {0, 0, 0};
-    visit_nodes<DIM, SHAPE, false, T>(g, 0, p, i, [&](int n, T N, T, T, T) {
+    visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, [&](int n, T N, T, T, T) {
         if (N == T(0)) return;
         if (MIX) {
             s[0] += x.fpx[n] * N;
@@ -111,7 +132,7 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
         }
     });
     const T mp = (T)p.mass[i];
-    visit_nodes<DIM, SHAPE, false, T>(g, 0, p, i, [&](int n, T N, T, T, T) {
+    visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, [&](int n, T N, T, T, T) {
         if (N == T(0)) return;
         if (MIX) {
             const float w = mp * N * x.frm[n];
@@ -130,11 +151,14 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
 // GET_DELTAV, the velocity conditions' zero directions (NodalVelBC::
 // GridVelocityConditions for the XPIC passes, NodalVelBC.cpp:327-334, and
 // MatVelocityField::ZeroVelocityBC, MatVelocityField.cpp:530-541), UPDATE_VSTAR
-template <int DIM, bool MIX>
+template <int DIM, bool MIX, bool BATCH>
 static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int nnodes, DevBCs b,
-                                    const int *bc_group) {
+                                    const int *bc_group, int phase, int k) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !nd.active[n]) return;
+    double t, dt;
+    if (!node_run<BATCH>(sp, n, t, dt)) return;
+    if (!xpic_takes_part(BATCH ? sp.runs[sp.nrun[n]].xpic : sp.xpic, phase, k)) return;
     double d[3];
     if (MIX) {
         d[0] = x.px[n] - (double)x.fnx[n];
@@ -147,9 +171,9 @@ static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int n
     }
     const int grp = bc_group[n];
     if (grp >= 0) {
-        for (int k = b.start[grp]; k < b.start[grp + 1]; k++) {
-            if (sp.t < b.ftime[k]) continue;
-            const int dir = b.dir[k];
+        for (int e = b.start[grp]; e < b.start[grp + 1]; e++) {
+            if (t < b.ftime[e]) continue;
+            const int dir = b.dir[e];
             const double nrm[3] = {dir == 1 ? 1. : 0., dir == 2 ? 1. : 0., dir == 4 ? 1. : 0.};
             const double dotn = d[0] * nrm[0] + d[1] * nrm[1] + d[2] * nrm[2];
 #pragma unroll

@@ -148,7 +148,8 @@ class MpmGpuBatchOptions(C.Structure):
                 ("sort_interval", C.c_int32), ("block", C.c_int32), ("max_runs", C.c_int32),
                 ("max_materials", C.c_int32), ("max_particles", C.c_int64), ("max_nodes", C.c_int64),
                 ("fraction_usf", C.c_double), ("inc_defgrad_terms", C.c_int32), ("max_fields", C.c_int32),
-                ("lr_links", C.c_int32)]
+                ("lr_links", C.c_int32), ("xpic_order", C.c_int32), ("xpic_fmpm", C.c_int32),
+                ("xpic_period", C.c_int32)]
 
 
 class MpmGpuBatchInfo(C.Structure):
@@ -166,7 +167,8 @@ class MpmGpuServerOptions(C.Structure):
                 ("block", C.c_int32), ("hbm_budget_bytes", C.c_int64), ("frac_3d", C.c_double),
                 ("nodes_per_particle", C.c_double), ("fraction_usf", C.c_double),
                 ("max_resident_particles", C.c_int64), ("order", C.c_int32), ("max_fields", C.c_int32),
-                ("lr_links", C.c_int32)]
+                ("lr_links", C.c_int32), ("xpic_order", C.c_int32), ("xpic_fmpm", C.c_int32),
+                ("xpic_period", C.c_int32)]
 
 
 class MpmGpuRequestInfo(C.Structure):

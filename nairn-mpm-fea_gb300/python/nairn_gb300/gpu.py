@@ -238,6 +238,12 @@ class GpuRun:
             pass
 
 
+def xpic_of(m) -> tuple | None:
+    """The PeriodicXPIC settings (order, fmpm, period) of a model, or None."""
+    o = m.options
+    return (o["xpic_order"], o.get("xpic_fmpm", 0), o.get("xpic_period", 1)) if o.get("xpic_order", 0) > 0 else None
+
+
 def lr_links_for(models) -> int:
     """Links per particle slot a batch of `models` reserves for regression
     contact normals: every shape-function node of a particle (64 in 3D, 16 in
@@ -257,11 +263,12 @@ class GpuBatch:
     def __init__(self, np_: int, method: int, shape: int, precision: int = 0, *, max_runs: int,
                  max_particles: int, max_nodes: int, max_materials: int | None = None, sort_interval: int = 1,
                  block: int = 0, fraction_usf: float = 0.5, inc_defgrad_terms: int = 0, max_fields: int = 1,
-                 lr_links: int = 0):
+                 lr_links: int = 0, xpic=None):
         L = lib()
+        xo, xf, xp = xpic if xpic else (0, 0, 1)
         self.opts = abi.MpmGpuBatchOptions(np_, method, shape, precision, sort_interval, block, max_runs,
                                            max_materials or max_runs, max_particles, max_nodes, fraction_usf,
-                                           inc_defgrad_terms, max_fields, lr_links)
+                                           inc_defgrad_terms, max_fields, lr_links, xo, xf, xp)
         self.bytes = int(L.mpmgpu_batch_bytes(C.byref(self.opts)))
         h = C.c_void_p()
         st = L.mpmgpu_batch_create(C.byref(self.opts), C.byref(h))
@@ -280,7 +287,8 @@ class GpuBatch:
                    max_materials=int(slack * sum(len(m.materials) for m in models)) + 1,
                    fraction_usf=o.get("fraction_usf", 0.5), inc_defgrad_terms=o.get("inc_defgrad_terms", 0),
                    max_fields=kw.pop("max_fields", max(m.options.get("nfields", 1) for m in models)),
-                   lr_links=kw.pop("lr_links", lr_links_for(models)), **kw)
+                   lr_links=kw.pop("lr_links", lr_links_for(models)), xpic=kw.pop("xpic", xpic_of(models[0])),
+                   **kw)
 
     @staticmethod
     def bytes_for(models, precision: int = 0) -> int:
@@ -288,7 +296,8 @@ class GpuBatch:
         opts = abi.MpmGpuBatchOptions(o["np"], o["method"], o["shape"], precision, 1, 0, len(models),
                                       sum(len(m.materials) for m in models) + 1, sum(m.n for m in models),
                                       sum(m.grid.nnodes for m in models), 0.5, o.get("inc_defgrad_terms", 0),
-                                      max(m.options.get("nfields", 1) for m in models), lr_links_for(models))
+                                      max(m.options.get("nfields", 1) for m in models), lr_links_for(models),
+                                      *(xpic_of(models[0]) or (0, 0, 1)))
         return int(lib().mpmgpu_batch_bytes(C.byref(opts)))
 
     def _check(self, st):
@@ -375,12 +384,15 @@ class GpuServer:
     def __init__(self, method: int, shape: int, precision: int = 1, *, hbm_budget_bytes: int,
                  max_runs: int = 256, steps_per_round: int = 10, backfill: bool = True, sort_interval: int = 1,
                  block: int = 0, frac_3d: float = 0.5, nodes_per_particle: float = 0.5, fraction_usf: float = 0.5,
-                 max_resident_particles: int = 0, order: str = "fifo", max_fields: int = 1, lr_links: int = 0):
+                 max_resident_particles: int = 0, order: str = "fifo", max_fields: int = 1, lr_links: int = 0,
+                 xpic=None):
         L = lib()
+        xo, xf, xp = xpic if xpic else (0, 0, 1)
         o = abi.MpmGpuServerOptions(method, shape, precision, max_runs, steps_per_round, 1 if backfill else 0,
                                     sort_interval, block, int(hbm_budget_bytes), frac_3d, nodes_per_particle,
                                     fraction_usf, int(max_resident_particles),
-                                    {"fifo": 0, "least_work": 1}[order], int(max_fields), int(lr_links))
+                                    {"fifo": 0, "least_work": 1}[order], int(max_fields), int(lr_links),
+                                    int(xo), int(xf), int(xp))
         h = C.c_void_p()
         st = L.mpmgpu_server_create(C.byref(o), C.byref(h))
         if st != 0:

@@ -331,3 +331,40 @@ def test_regression_normals_need_a_link_reserve(gpu_lib):
     with pytest.raises(GpuError, match="INVALID"):
         b.add(c)
     b.close()
+
+
+@pytest.mark.parametrize("case,precision,tol", [("cant2d_xpic2", 0, TOL), ("cant2d_fmpm2_usl_every2", 0, TOL),
+                                                ("cant2d_xpic2_cpdi_every2", 0, TOL), ("cant2d_fmpm3", 1, TOL_MIXED)])
+def test_batched_xpic_runs_match_reference(case, precision, tol, gpu_lib):
+    """PeriodicXPIC in a batch (XPIC(k) and FMPM(k), every step or every
+    second step): the golden run matches the reference; a larger run of the
+    same settings admitted five steps later counts its own steps (its
+    schedule starts at its admission) and matches the oracle."""
+    from conftest import load_golden, model_for, view_for
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import model, abi
+    meta, g = load_golden(case)
+    m = model_for(meta)
+    kw = dict(meta["kwargs"], nx=14, ny=5, steps=meta["steps"] - 5)
+    late = model_for(dict(meta, kwargs=kw))
+    b = GpuBatch.for_models([m, late], precision=precision)
+    assert b.opts.xpic_order == m.options["xpic_order"]
+    r0 = b.add(m)
+    b.step(5)
+    r1 = b.add(late)
+    b.step(meta["steps"])
+    assert b.state(r0) == (abi.RUN_FINISHED, meta["steps"])
+    assert b.state(r1) == (abi.RUN_FINISHED, late.nsteps)
+    v = view_for(b.download(r0), m)
+    for k in ("pos", "vel", "stress", "strain"):
+        assert rel_l2(v[k], g["final_" + k]) <= tol, (k, rel_l2(v[k], g["final_" + k]))
+    assert_close(b.download(r1), oracle(late, late.nsteps), tol, "late")
+    b.close()
+
+
+def test_batched_xpic_refused_with_contact(gpu_lib):
+    from nairn_gb300.gpu import GpuBatch, GpuError
+    from nairn_gb300 import model
+    with pytest.raises(GpuError, match="UNSUPPORTED"):
+        GpuBatch(model.PLANE_STRAIN, model.USAVG, model.SHAPE_UGIMP, max_runs=2, max_particles=1000,
+                 max_nodes=1000, max_fields=2, xpic=(2, 0, 1))

@@ -163,3 +163,20 @@ def test_served_contact_runs(precision, tol, gpu_lib):
         assert info["state"] == abi.REQ_DONE and info["steps_done"] == m.nsteps, info
         check(s.result(rid), oracle(m), 3, tol, m.name)
     s.close()
+
+
+def test_served_fmpm_runs(gpu_lib):
+    """Requests under FMPM(2) on every second step, served together: each
+    result is the oracle's (each request counts its steps from admission)."""
+    from nairn_gb300 import model, abi
+    from nairn_gb300.gpu import GpuServer
+    ms = [model.cantilever_2d(nx=8 + 2 * k, ny=3 + k, steps=20 + 5 * k, xpic=(2, 1, 2)) for k in range(3)]
+    s = GpuServer(model.USAVG, model.SHAPE_UGIMP, 0, hbm_budget_bytes=256 << 20, frac_3d=0.0, steps_per_round=3,
+                  xpic=(2, 1, 2))
+    ids = [s.submit(m) for m in ms]
+    s.drain(600)
+    for rid, m in zip(ids, ms):
+        info = s.poll(rid)
+        assert info["state"] == abi.REQ_DONE and info["steps_done"] == m.nsteps, info
+        check(s.result(rid), oracle(m), 2, TOL, m.name)
+    s.close()
