@@ -232,6 +232,35 @@ __device__ __forceinline__ void gimp_window(T xi, T lp, T inv_size, T idx, Win<T
     }
 }
 
+// Quadratic B-spline (B2SPLINE) window: FourNodeIsoparam /
+// EightNodeIsoparamBrick::SplineShapeFunction (Common/Elements/
+// FourNodeIsoparam.cpp:217-293, NairnMPM/src/Elements/
+// EightNodeIsoparamBrick.cpp:110-205) take the candidates within 3 half cells:
+// the one at +3 exactly when xi > 0, else the one at -3 (zero at xi = 0).  The
+// factor is (3 - d^2)/4 for |d| <= 1 and (3 - |d|)^2/8 beyond; idx = 1 / dx.
+template <typename T, bool kGrad>
+__device__ __forceinline__ void bspline_window(T xi, T idx, Win<T> &w) {
+    w.s = xi > T(0) ? 1 : 0;
+#pragma unroll
+    for (int j = 0; j < 3; j++) {
+        const T d = xi - (T)(2 * (w.s + j) - 3);
+        const T ad = fabs(d);
+        T S = T(0), dS = T(0);
+        if (ad < T(3)) {
+            if (ad <= T(1)) {
+                S = T(0.25) * (T(3) - d * d);
+                if (kGrad) dS = -d * idx;
+            } else {
+                const T arg = T(3) - ad;
+                S = T(0.125) * arg * arg;
+                if (kGrad) dS = (d >= T(0) ? T(0.5) * (d - T(3)) : T(0.5) * (d + T(3))) * idx;
+            }
+        }
+        w.S[j] = S;
+        w.dS[j] = dS;
+    }
+}
+
 // FP64 value as an FP32 pair hi + lo (hi = nearest float, lo = nearest float of the rest)
 __device__ __forceinline__ void split2(double v, float &hi, float &lo) {
     hi = __double2float_rn(v);

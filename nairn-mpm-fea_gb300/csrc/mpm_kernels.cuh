@@ -19,7 +19,7 @@
 
 namespace nmg {
 
-enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2 };
+enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2, SHAPE_BSPLINE = 3 };
 
 // Resident 256-thread blocks per SM the strain kernels are compiled for (this
 // caps their registers at 80): their FP64 constitutive updates are latency
@@ -197,12 +197,18 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
         }
         return;
     }
-    // uGIMP over the particle's window (see gimp_window); f is called for
-    // every window node, with N == 0 marking a node outside the support.
+    // uGIMP or B2SPLINE over the particle's window (see gimp_window and
+    // bspline_window); f is called for every window node, with N == 0
+    // marking a node outside the support.
     const T lpx = (T)lpx_d, lpy = (T)lpy_d, lpz = (T)lpz_d;
     Win<T> wx, wy;
-    gimp_window<T, DIM == 3, GRAD>(xi, lpx, T(1) / (T(4) * lpx), GRAD ? T(2) / DX : T(0), wx);
-    gimp_window<T, DIM == 3, GRAD>(eta, lpy, T(1) / (T(4) * lpy), GRAD ? T(2) / DY : T(0), wy);
+    if constexpr (SHAPE == SHAPE_BSPLINE) {
+        bspline_window<T, GRAD>(xi, GRAD ? T(1) / DX : T(0), wx);
+        bspline_window<T, GRAD>(eta, GRAD ? T(1) / DY : T(0), wy);
+    } else {
+        gimp_window<T, DIM == 3, GRAD>(xi, lpx, T(1) / (T(4) * lpx), GRAD ? T(2) / DX : T(0), wx);
+        gimp_window<T, DIM == 3, GRAD>(eta, lpy, T(1) / (T(4) * lpy), GRAD ? T(2) / DY : T(0), wy);
+    }
     const int base = n0 + (wx.s - 1) + (wy.s - 1) * g.yplane;
     if (DIM == 2) {
 #pragma unroll
@@ -220,7 +226,8 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
         }
     } else {
         Win<T> wz;
-        gimp_window<T, true, GRAD>(zeta, lpz, T(1) / (T(4) * lpy), GRAD ? T(2) / DZ : T(0), wz);
+        if constexpr (SHAPE == SHAPE_BSPLINE) bspline_window<T, GRAD>(zeta, GRAD ? T(1) / DZ : T(0), wz);
+        else gimp_window<T, true, GRAD>(zeta, lpz, T(1) / (T(4) * lpy), GRAD ? T(2) / DZ : T(0), wz);
         const int base3 = base + (wz.s - 1) * g.zplane;
 #pragma unroll
         for (int jz = 0; jz < 3; jz++) {

@@ -142,10 +142,12 @@ void enqueue_prec(MpmGpuCtx *c, double t, int slot) {
     if (d3) {
         if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<3, SHAPE_LINEAR, MIX, DET>(c, t, slot);
         else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<3, SHAPE_LCPDI, MIX, DET>(c, t, slot);
+        else if (shape == MPMGPU_SHAPE_BSPLINE) enqueue_step<3, SHAPE_BSPLINE, MIX, DET>(c, t, slot);
         else enqueue_step<3, SHAPE_UGIMP, MIX, DET>(c, t, slot);
     } else {
         if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<2, SHAPE_LINEAR, MIX, DET>(c, t, slot);
         else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<2, SHAPE_LCPDI, MIX, DET>(c, t, slot);
+        else if (shape == MPMGPU_SHAPE_BSPLINE) enqueue_step<2, SHAPE_BSPLINE, MIX, DET>(c, t, slot);
         else enqueue_step<2, SHAPE_UGIMP, MIX, DET>(c, t, slot);
     }
 }

@@ -297,6 +297,63 @@ static void shape_eval(const OGrid *g, int shape, int e, const double *xi, const
         }
         return;
     }
+    if (shape == MPMGPU_SHAPE_BSPLINE) {
+        /* B2SPLINE: FourNodeIsoparam::SplineShapeFunction (Common/Elements/
+         * FourNodeIsoparam.cpp:217-293) and EightNodeIsoparamBrick::
+         * SplineShapeFunction (EightNodeIsoparamBrick.cpp:110-205): the
+         * candidates of the 4x4(x4) block around the element within 3 half
+         * cells, quadratic B-spline factors per axis */
+        double inv_dx = 0., inv_dy = 0., inv_dz = 0.;
+        if (grad) {
+            inv_dx = 1. / DX;
+            inv_dy = 1. / DY;
+            inv_dz = 1. / DZ;
+        }
+        int three = g->dim == 3, i = 0;
+        for (int id = 0; id < (three ? 64 : 16); id++) {
+            double gx = three ? (double)(2 * x3off[id] - 1) : gxii[id];
+            double gy = three ? (double)(2 * y3off[id] - 1) : geti[id];
+            double etai = xi[0] - gx, t1 = fabs(etai);
+            if (t1 >= 3.) continue;
+            double netai = xi[1] - gy, t2 = fabs(netai);
+            if (t2 >= 3.) continue;
+            double zetai = 0., t3 = 0.;
+            if (three) {
+                zetai = xi[2] - (double)(2 * z3off[id] - 1);
+                t3 = fabs(zetai);
+                if (t3 >= 3.) continue;
+            }
+            double sx, sy, sz = 1., arg;
+            if (t1 <= 1.0) sx = 0.25 * (3. - etai * etai);
+            else { arg = 3. - t1; sx = 0.125 * arg * arg; }
+            if (t2 <= 1.0) sy = 0.25 * (3. - netai * netai);
+            else { arg = 3. - t2; sy = 0.125 * arg * arg; }
+            if (three) {
+                if (t3 <= 1.0) sz = 0.25 * (3. - zetai * zetai);
+                else { arg = 3. - t3; sz = 0.125 * arg * arg; }
+            }
+            s->fn[i] = three ? sx * sy * sz : sx * sy;
+            if (grad) {
+                double fx = t1 <= 1.0 ? -etai : (etai >= 0. ? 0.5 * (etai - 3) : 0.5 * (etai + 3));
+                double fy = t2 <= 1.0 ? -netai : (netai >= 0. ? 0.5 * (netai - 3) : 0.5 * (netai + 3));
+                if (three) {
+                    double fz = t3 <= 1.0 ? -zetai : (zetai >= 0. ? 0.5 * (zetai - 3) : 0.5 * (zetai + 3));
+                    s->dx[i] = fx * sy * sz * inv_dx;
+                    s->dy[i] = fy * sx * sz * inv_dy;
+                    s->dz[i] = fz * sx * sy * inv_dz;
+                } else {
+                    s->dx[i] = fx * sy * inv_dx;
+                    s->dy[i] = fy * sx * inv_dy;
+                    s->dz[i] = 0.;
+                }
+            }
+            s->nds[i] = three ? n0 + x3off[id] * g->xplane + y3off[id] * g->yplane + z3off[id] * g->zplane
+                              : n0 + xoff2[id] * g->xplane + yoff2[id] * g->yplane;
+            i++;
+        }
+        s->n = i;
+        return;
+    }
     /* UNIFORM_GIMP */
     if (g->dim == 2) {
         /* FourNodeIsoparam::GimpShapeFunction, FourNodeIsoparam.cpp:431-519 */
@@ -2122,7 +2179,8 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
                    int nsteps, double t0, int nthreads) {
     g_err[0] = 0;
     if (!grid || !opts || !mats || !p) return fail(MPMGPU_ERR_INVALID, "oracle: null argument");
-    if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI)
+    if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI &&
+        opts->shape != MPMGPU_SHAPE_BSPLINE)
         return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: shape function not implemented");
     if (contact && contact->enabled) {
         if (contact->normals < 0 || (contact->normals > 2 && contact->normals != 5 && contact->normals != 6))

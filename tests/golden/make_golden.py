@@ -91,6 +91,16 @@ CASES = {
                                                   method=0, xpic=(2, 1, 1))),
     "taylor3d_neo_fmpm4_usl": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=40, mat_type=28, G=10.,
                                                  K=50., rho=1.1, v0=-30000., method=3, xpic=(4, 1, 1))),
+    # quadratic B-spline shape functions (B2SPLINE)
+    "cant2d_b2spline": ("cantilever_2d", dict(nx=10, ny=4, steps=60, gimp="B2SPLINE")),
+    "cant2d_b2spline_usl_neo": ("cantilever_2d", dict(nx=10, ny=4, steps=100, gimp="B2SPLINE", method=3, mat_type=28,
+                                                      G=3., K=30., rho=1.1, v0=20000., margin_cells=8)),
+    "taylor3d_b2spline": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, gimp="B2SPLINE")),
+    "taylor3d_b2spline_usf_xpic2": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, gimp="B2SPLINE",
+                                                      method=0, xpic=(2, 0, 1))),
+    "contact2d_b2spline_fric": ("contact_2d", dict(steps=150, friction=0.3, normals=2, gimp="B2SPLINE")),
+    "contact3d_b2spline_logreg": ("contact_3d", dict(steps=70, friction=0.3, normals=6, gimp="B2SPLINE", gap=0.5,
+                                                     v=(50000., 0., -200000.))),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")

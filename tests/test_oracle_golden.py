@@ -24,14 +24,16 @@ def test_model_builder_matches_reference_setup(case):
 def test_oracle_matches_reference(case):
     """The FP64 restatement reproduces the reference's final state (bit-exact in
     practice; within 1e-12 with XPIC/FMPM of order > 1, whose double loop over
-    each particle's nodes may add in another order)."""
+    each particle's nodes may add in another order, and with regression
+    normals, whose exponentials and sums may round differently)."""
     import oracle_lib
     meta, g = load_golden(case)
     m = model_for(meta)
     p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
     oracle_lib.run(m, p, meta["steps"], nthreads=1)
     v = view_for(p, m)
-    tol = 1e-12 if m.options.get("xpic_order", 0) > 1 else 1e-13
+    lr = m.extra and m.extra.get("contact") and m.extra["contact"]["normals"] >= 5
+    tol = 1e-12 if m.options.get("xpic_order", 0) > 1 or lr else 1e-13
     for k in ("pos", "vel", "stress", "strain"):
         assert rel_l2(v[k], g["final_" + k]) <= tol, (k, rel_l2(v[k], g["final_" + k]))
     if g["final_hist1"].any():
@@ -115,3 +117,15 @@ def test_xpic_and_fmpm_change_the_result():
         p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
         oracle_lib.run(m, p, meta["steps"], nthreads=1)
         assert rel_l2(view_for(p, m)["vel"], g["final_vel"]) > 0.1, case
+
+
+def test_b2spline_goldens_are_not_ugimp_runs():
+    """The B2SPLINE goldens are quadratic B-spline runs: the same problems
+    with uGIMP end far from them (so their parity tests test B-splines)."""
+    import oracle_lib
+    for case in [c for c in golden_cases() if load_golden(c)[0]["kwargs"].get("gimp") == "B2SPLINE"]:
+        meta, g = load_golden(case)
+        m = model_for(dict(meta, kwargs=dict(meta["kwargs"], gimp="uGIMP")))
+        p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
+        oracle_lib.run(m, p, meta["steps"], nthreads=1)
+        assert rel_l2(view_for(p, m)["stress"], g["final_stress"]) > 1e-3, case
