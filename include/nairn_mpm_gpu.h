@@ -56,7 +56,13 @@ enum {
 /* MPMMethod: NairnMPM/src/System/MPMPrefix.hpp:110 */
 enum { MPMGPU_USF = 0, MPMGPU_USAVG = 2, MPMGPU_USL = 3 };
 /* GIMP type: NairnMPM/src/System/MPMPrefix.hpp:127-140 */
-enum { MPMGPU_SHAPE_LINEAR = 0, MPMGPU_SHAPE_UGIMP = 1, MPMGPU_SHAPE_BSPLINE = 6, MPMGPU_SHAPE_LCPDI = 10 };
+enum {
+    MPMGPU_SHAPE_LINEAR = 0,  /* Classic (POINT_GIMP)        */
+    MPMGPU_SHAPE_UGIMP = 1,   /* uGIMP (UNIFORM_GIMP)        */
+    MPMGPU_SHAPE_BGIMP = 5,   /* B2GIMP (BSPLINE_GIMP)       */
+    MPMGPU_SHAPE_BSPLINE = 6, /* B2SPLINE (BSPLINE)          */
+    MPMGPU_SHAPE_LCPDI = 10   /* lCPDI (LINEAR_CPDI)         */
+};
 /* Analysis type (np): NairnMPM/src/System/MPMPrefix.hpp:115 */
 enum { MPMGPU_PLANE_STRAIN = 10, MPMGPU_THREED = 12 };
 /* Arithmetic of the transfers (P2G/G2P and grid); the constitutive update,
@@ -323,7 +329,7 @@ typedef struct MpmGpuBatch MpmGpuBatch;
 typedef struct {
     int32_t np;               /* MPMGPU_PLANE_STRAIN or MPMGPU_THREED        */
     int32_t method;           /* MPMGPU_USF / _USAVG / _USL                  */
-    int32_t shape;            /* MPMGPU_SHAPE_LINEAR, _UGIMP, _BSPLINE or _LCPDI */
+    int32_t shape;            /* MPMGPU_SHAPE_LINEAR, _UGIMP, _BGIMP, _BSPLINE or _LCPDI */
     int32_t precision;        /* MPMGPU_PREC_*                               */
     int32_t sort_interval;    /* cell sort every k steps (0: never)          */
     int32_t block;            /* threads per block of particle kernels (0: 256) */
@@ -403,7 +409,7 @@ typedef struct MpmGpuServer MpmGpuServer;
 
 typedef struct {
     int32_t method;             /* MPMGPU_USF / _USAVG / _USL                  */
-    int32_t shape;              /* MPMGPU_SHAPE_LINEAR, _UGIMP, _BSPLINE or _LCPDI */
+    int32_t shape;              /* MPMGPU_SHAPE_LINEAR, _UGIMP, _BGIMP, _BSPLINE or _LCPDI */
     int32_t precision;          /* MPMGPU_PREC_*                               */
     int32_t max_runs;           /* run slots per dimension                     */
     int32_t steps_per_round;    /* steps between admissions/retirements (0: 10) */

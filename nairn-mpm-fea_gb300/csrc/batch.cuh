@@ -448,6 +448,7 @@ void batch_enqueue_shape(MpmGpuBatch *b) {
     if (b->o.shape == MPMGPU_SHAPE_LINEAR) batch_enqueue_step<DIM, SHAPE_LINEAR, MIX>(b);
     else if (b->o.shape == MPMGPU_SHAPE_LCPDI) batch_enqueue_step<DIM, SHAPE_LCPDI, MIX>(b);
     else if (b->o.shape == MPMGPU_SHAPE_BSPLINE) batch_enqueue_step<DIM, SHAPE_BSPLINE, MIX>(b);
+    else if (b->o.shape == MPMGPU_SHAPE_BGIMP) batch_enqueue_step<DIM, SHAPE_BGIMP, MIX>(b);
     else batch_enqueue_step<DIM, SHAPE_UGIMP, MIX>(b);
 }
 
@@ -646,7 +647,7 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     if (o->np != MPMGPU_PLANE_STRAIN && o->np != MPMGPU_THREED)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "batch analysis type must be 2D plane strain or 3D");
     if (o->shape != MPMGPU_SHAPE_LINEAR && o->shape != MPMGPU_SHAPE_UGIMP && o->shape != MPMGPU_SHAPE_LCPDI &&
-        o->shape != MPMGPU_SHAPE_BSPLINE)
+        o->shape != MPMGPU_SHAPE_BSPLINE && o->shape != MPMGPU_SHAPE_BGIMP)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
     if (o->method != MPMGPU_USF && o->method != MPMGPU_USAVG && o->method != MPMGPU_USL)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");

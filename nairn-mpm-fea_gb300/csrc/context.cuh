@@ -1,7 +1,7 @@
 // context.cuh -- the single-run context (MpmGpuCtx of include/nairn_mpm_gpu.h),
 // shared by the C ABI (mpm_gpu.cu) and the step translation units
-// (step_fp64.cu, step_mixed.cu), which instantiate the step kernels of one
-// transfer precision each so the library builds in parallel.
+// (step_<precision>_<dim>_<sums>.cu), which instantiate the step kernels of
+// one combination each so the library builds in parallel.
 #pragma once
 
 #include <cuda_runtime.h>
@@ -85,7 +85,9 @@ inline cudaEvent_t &event_at(MpmGpuCtx *c, int slot, int k, bool begin) {
 }
 
 // enqueue one step of a context (FP64 / mixed transfers; deterministic node sums)
-void enqueue_fp64(MpmGpuCtx *c, double t, int slot, bool det);
-void enqueue_mixed(MpmGpuCtx *c, double t, int slot, bool det);
+// one step of a context (defined in step.cuh, each combination instantiated
+// in its own translation unit)
+template <int DIM, bool MIX, bool DET>
+void enqueue_dim(MpmGpuCtx *c, double t, int slot);
 
 }  // namespace nmg

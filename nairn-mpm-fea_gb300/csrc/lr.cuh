@@ -250,7 +250,7 @@ static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevPar
         const int ka = a * sp.ct.fstride + n;
         if (!nd.active[ka]) continue;
         double nrm[3] = {0., 0., 0.};
-        double mt[NM], rhs[NB], lam[NB], beta[NB];
+        double mt[NM], rhs[NB], lam[NB], beta[NB] = {};  // beta is set by the linear step first
         const double pen = logistic ? normLog * cell2 : 0.;
 #pragma unroll
         for (int k = 0; k < NB; k++) lam[k] = k < NB - 1 ? pen : (logistic ? offsetLog : offsetLin);

@@ -261,6 +261,67 @@ __device__ __forceinline__ void bspline_window(T xi, T idx, Win<T> &w) {
     }
 }
 
+// B2GIMP window: FourNodeIsoparam / EightNodeIsoparamBrick::
+// BGimpShapeFunction (Common/Elements/FourNodeIsoparam.cpp:770-883) support
+// 3 + lp half cells, so all four candidates per axis (at -3, -1, 1, 3, node
+// offsets -1..2) may carry weight; those beyond the support get zero.  The
+// gradient takes its sign from `sgn`: the particle's coordinate on the same
+// axis, except that the reference's 3D z gradient compares the y coordinate.
+// idx = 2 / dx.
+template <typename T>
+struct Win4 {
+    T S[4], dS[4];
+};
+
+template <typename T, bool kThreeD, bool kGrad>
+__device__ __forceinline__ void bgimp_window(T xi, T lp, T idx, T sgn, Win4<T> &w) {
+    const T b1 = T(1) - lp, b2 = T(1) + lp, b3 = T(3) - lp, b4 = T(3) + lp;
+    const T inv_size = T(1) / (T(48) * lp), oneTwelth = T(1) / T(12);
+    const T lp2 = lp * lp;
+#pragma unroll
+    for (int j = 0; j < 4; j++) {
+        const T gk = (T)(2 * j - 3);
+        const T xp = fabs(xi - gk);
+        T S = T(0), dS = T(0);
+        if (xp < b4) {
+            T arg = T(0);
+            if (xp < b1) {
+                S = (T(9) - lp2 - T(3) * xp * xp) * oneTwelth;
+            } else if (xp < b2) {
+                arg = xp - T(1);
+                S = kThreeD ? (T(9) * lp2 * arg + T(3) * arg * arg * arg + T(3) * lp * (T(15) - xp * (T(6) + xp)) -
+                               lp2 * lp) * inv_size
+                            : (lp2 * (T(9) * arg - lp) + T(3) * arg * arg * arg + T(3) * lp * (T(15) - xp * (T(6) + xp))) *
+                                  inv_size;
+            } else if (xp <= b3) {
+                arg = xp - T(3);
+                S = (lp2 + T(3) * arg * arg) * T(0.5) * oneTwelth;
+            } else {
+                arg = T(3) + lp - xp;
+                S = arg * arg * arg * inv_size;
+            }
+            if (kGrad) {
+                T d;
+                if (xp < b1) {
+                    d = T(-0.5) * xp;
+                } else if (xp < b2) {
+                    arg = xp - T(1);
+                    d = ((kThreeD ? T(3) * lp * lp : T(3) * lp2) + T(3) * arg * arg - T(2) * lp * (T(3) + xp)) * T(3) *
+                        inv_size;
+                } else if (xp <= b3) {
+                    d = T(0.25) * (xp - T(3));
+                } else {
+                    arg = T(3) + lp - xp;
+                    d = -arg * arg * T(3) * inv_size;
+                }
+                dS = (sgn > gk ? d : -d) * idx;
+            }
+        }
+        w.S[j] = S;
+        w.dS[j] = dS;
+    }
+}
+
 // FP64 value as an FP32 pair hi + lo (hi = nearest float, lo = nearest float of the rest)
 __device__ __forceinline__ void split2(double v, float &hi, float &lo) {
     hi = __double2float_rn(v);

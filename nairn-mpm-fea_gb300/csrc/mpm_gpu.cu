@@ -213,7 +213,7 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
         (grid->dim == 2 && opts->np != MPMGPU_PLANE_STRAIN))
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "analysis type must be 2D plane strain or 3D");
     if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI &&
-        opts->shape != MPMGPU_SHAPE_BSPLINE)
+        opts->shape != MPMGPU_SHAPE_BSPLINE && opts->shape != MPMGPU_SHAPE_BGIMP)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
     if (opts->method != MPMGPU_USF && opts->method != MPMGPU_USAVG && opts->method != MPMGPU_USL)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
@@ -552,8 +552,14 @@ namespace {
 
 void enqueue(MpmGpuCtx *c, double t, int slot) {
     const bool det = c->det.lim != nullptr;
-    if (c->opts.precision == MPMGPU_PREC_MIXED) enqueue_mixed(c, t, slot, det);
-    else enqueue_fp64(c, t, slot, det);
+    const bool mix = c->opts.precision == MPMGPU_PREC_MIXED;
+    if (c->dim == 3) {
+        if (mix) det ? enqueue_dim<3, true, true>(c, t, slot) : enqueue_dim<3, true, false>(c, t, slot);
+        else det ? enqueue_dim<3, false, true>(c, t, slot) : enqueue_dim<3, false, false>(c, t, slot);
+    } else {
+        if (mix) det ? enqueue_dim<2, true, true>(c, t, slot) : enqueue_dim<2, true, false>(c, t, slot);
+        else det ? enqueue_dim<2, false, true>(c, t, slot) : enqueue_dim<2, false, false>(c, t, slot);
+    }
 }
 
 int ensure_events(MpmGpuCtx *c, int nsteps) {

@@ -19,7 +19,7 @@
 
 namespace nmg {
 
-enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2, SHAPE_BSPLINE = 3 };
+enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2, SHAPE_BSPLINE = 3, SHAPE_BGIMP = 4 };
 
 // Resident 256-thread blocks per SM the strain kernels are compiled for (this
 // caps their registers at 80): their FP64 constitutive updates are latency
@@ -197,10 +197,41 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
         }
         return;
     }
+    const T lpx = (T)lpx_d, lpy = (T)lpy_d, lpz = (T)lpz_d;
+    if constexpr (SHAPE == SHAPE_BGIMP) {
+        // B2GIMP over its four-node window per axis (see bgimp_window)
+        Win4<T> wx, wy;
+        bgimp_window<T, DIM == 3, GRAD>(xi, lpx, GRAD ? T(2) / DX : T(0), xi, wx);
+        bgimp_window<T, DIM == 3, GRAD>(eta, lpy, GRAD ? T(2) / DY : T(0), eta, wy);
+        const int base = n0 - 1 - g.yplane;
+        if (DIM == 2) {
+#pragma unroll
+            for (int jy = 0; jy < 4; jy++)
+#pragma unroll
+                for (int jx = 0; jx < 4; jx++)
+                    f(base + jx + jy * g.yplane, wx.S[jx] * wy.S[jy], GRAD ? wx.dS[jx] * wy.S[jy] : T(0),
+                      GRAD ? wx.S[jx] * wy.dS[jy] : T(0), T(0));
+        } else {
+            Win4<T> wz;
+            bgimp_window<T, true, GRAD>(zeta, lpz, GRAD ? T(2) / DZ : T(0), eta, wz);
+            const int base3 = base - g.zplane;
+#pragma unroll
+            for (int jz = 0; jz < 4; jz++)
+#pragma unroll
+                for (int jy = 0; jy < 4; jy++) {
+                    const T Syz = wy.S[jy] * wz.S[jz];
+#pragma unroll
+                    for (int jx = 0; jx < 4; jx++)
+                        f(base3 + jx + jy * g.yplane + jz * g.zplane, wx.S[jx] * Syz,
+                          GRAD ? wx.dS[jx] * Syz : T(0), GRAD ? wx.S[jx] * wy.dS[jy] * wz.S[jz] : T(0),
+                          GRAD ? wx.S[jx] * wy.S[jy] * wz.dS[jz] : T(0));
+                }
+        }
+        return;
+    }
     // uGIMP or B2SPLINE over the particle's window (see gimp_window and
     // bspline_window); f is called for every window node, with N == 0
     // marking a node outside the support.
-    const T lpx = (T)lpx_d, lpy = (T)lpy_d, lpz = (T)lpz_d;
     Win<T> wx, wy;
     if constexpr (SHAPE == SHAPE_BSPLINE) {
         bspline_window<T, GRAD>(xi, GRAD ? T(1) / DX : T(0), wx);

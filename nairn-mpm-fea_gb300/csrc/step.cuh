@@ -1,5 +1,5 @@
 // step.cuh -- the kernel sequence of one explicit step of a single-run
-// context, included by step_fp64.cu and step_mixed.cu.
+// context, included by the step_<precision>_<dim>_<sums>.cu translation units.
 #pragma once
 
 #include "context.cuh"
@@ -135,22 +135,19 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     mark(6, false);
 }
 
-template <bool MIX, bool DET>
-void enqueue_prec(MpmGpuCtx *c, double t, int slot) {
-    const bool d3 = c->dim == 3;
+}  // namespace
+
+// one step of a context of dimension DIM, transfer precision MIX and node-sum
+// mode DET, for its shape-function option; each combination is instantiated
+// in its own translation unit (step_<precision>_<dim>_<sums>.cu)
+template <int DIM, bool MIX, bool DET>
+void enqueue_dim(MpmGpuCtx *c, double t, int slot) {
     const int shape = c->opts.shape;
-    if (d3) {
-        if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<3, SHAPE_LINEAR, MIX, DET>(c, t, slot);
-        else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<3, SHAPE_LCPDI, MIX, DET>(c, t, slot);
-        else if (shape == MPMGPU_SHAPE_BSPLINE) enqueue_step<3, SHAPE_BSPLINE, MIX, DET>(c, t, slot);
-        else enqueue_step<3, SHAPE_UGIMP, MIX, DET>(c, t, slot);
-    } else {
-        if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<2, SHAPE_LINEAR, MIX, DET>(c, t, slot);
-        else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<2, SHAPE_LCPDI, MIX, DET>(c, t, slot);
-        else if (shape == MPMGPU_SHAPE_BSPLINE) enqueue_step<2, SHAPE_BSPLINE, MIX, DET>(c, t, slot);
-        else enqueue_step<2, SHAPE_UGIMP, MIX, DET>(c, t, slot);
-    }
+    if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<DIM, SHAPE_LINEAR, MIX, DET>(c, t, slot);
+    else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<DIM, SHAPE_LCPDI, MIX, DET>(c, t, slot);
+    else if (shape == MPMGPU_SHAPE_BSPLINE) enqueue_step<DIM, SHAPE_BSPLINE, MIX, DET>(c, t, slot);
+    else if (shape == MPMGPU_SHAPE_BGIMP) enqueue_step<DIM, SHAPE_BGIMP, MIX, DET>(c, t, slot);
+    else enqueue_step<DIM, SHAPE_UGIMP, MIX, DET>(c, t, slot);
 }
 
-}  // namespace
 }  // namespace nmg

@@ -1,0 +1,6 @@
+// step_fp64_2d_atomic.cu -- the single-run step of 2D contexts with FP64 transfers and
+// atomic node sums (one instantiation per translation unit, so the library
+// builds in parallel).
+#include "step.cuh"
+
+template void nmg::enqueue_dim<2, false, false>(MpmGpuCtx *c, double t, int slot);

@@ -1,0 +1,6 @@
+// step_fp64_3d_atomic.cu -- the single-run step of 3D contexts with FP64 transfers and
+// atomic node sums (one instantiation per translation unit, so the library
+// builds in parallel).
+#include "step.cuh"
+
+template void nmg::enqueue_dim<3, false, false>(MpmGpuCtx *c, double t, int slot);

@@ -297,6 +297,84 @@ static void shape_eval(const OGrid *g, int shape, int e, const double *xi, const
         }
         return;
     }
+    if (shape == MPMGPU_SHAPE_BGIMP) {
+        /* B2GIMP: FourNodeIsoparam::BGimpShapeFunction (Common/Elements/
+         * FourNodeIsoparam.cpp:770-883) and EightNodeIsoparamBrick::
+         * BGimpShapeFunction: the quadratic B-spline convolved with the
+         * particle domain, every candidate within 3 + lp half cells.  The 3D
+         * gradient takes its z sign from the y coordinate, as the reference does. */
+        int three = g->dim == 3, i = 0;
+        double inv_d[3] = {0., 0., 0.};
+        if (grad) {
+            inv_d[0] = 2.0 / DX;
+            inv_d[1] = 2.0 / DY;
+            inv_d[2] = 2.0 / DZ;
+        }
+        for (int id = 0; id < (three ? 64 : 16); id++) {
+            double gc[3] = {three ? (double)(2 * x3off[id] - 1) : gxii[id],
+                            three ? (double)(2 * y3off[id] - 1) : geti[id],
+                            three ? (double)(2 * z3off[id] - 1) : 0.};
+            double S[3] = {1., 1., 1.}, dS[3] = {0., 0., 0.};
+            int out = 0;
+            for (int a = 0; a < (three ? 3 : 2) && !out; a++) {
+                double l = lp[a], b1 = 1. - l, b2 = 1. + l, b3 = 3. - l, b4 = 3. + l;
+                double inv_size = 1. / (48. * l), oneTwelth = 1. / 12.;
+                double xp = fabs(xi[a] - gc[a]), arg;
+                if (xp >= b4) { out = 1; break; }
+                if (xp < b1) S[a] = (9. - l * l - 3. * xp * xp) * oneTwelth;
+                else if (xp < b2) {
+                    arg = xp - 1.;
+                    if (three) {
+                        double lp2 = l * l, lp3 = lp2 * l;
+                        S[a] = (9. * lp2 * arg + 3. * arg * arg * arg + 3. * l * (15. - xp * (6. + xp)) - lp3) * inv_size;
+                    } else {
+                        double lp2 = l * l;
+                        S[a] = (lp2 * (9. * arg - l) + 3. * arg * arg * arg + 3. * l * (15. - xp * (6. + xp))) * inv_size;
+                    }
+                } else if (xp <= b3) {
+                    arg = xp - 3.;
+                    S[a] = (l * l + 3. * arg * arg) * 0.5 * oneTwelth;
+                } else {
+                    arg = 3. + l - xp;
+                    S[a] = arg * arg * arg * inv_size;
+                }
+                if (grad) {
+                    if (xp < b1) dS[a] = -0.5 * xp;
+                    else if (xp < b2) {
+                        arg = xp - 1.;
+                        double l3 = three ? 3 * l * l : 3 * (l * l);  /* 3D: (3 lp) lp; 2D: 3 (lp lp) */
+                        dS[a] = (l3 + 3. * arg * arg - 2. * l * (3. + xp)) * 3. * inv_size;
+                    }
+                    else if (xp <= b3) dS[a] = 0.25 * (xp - 3.);
+                    else { arg = 3. + l - xp; dS[a] = -arg * arg * 3. * inv_size; }
+                }
+            }
+            if (out) continue;
+            if (three) {
+                s->fn[i] = S[0] * S[1] * S[2];
+                if (grad) {
+                    double xsign = xi[0] > gc[0] ? 1. : -1., ysign = xi[1] > gc[1] ? 1. : -1.;
+                    double zsign = xi[1] > gc[2] ? 1. : -1.;
+                    s->dx[i] = xsign * dS[0] * S[1] * S[2] * inv_d[0];
+                    s->dy[i] = ysign * S[0] * dS[1] * S[2] * inv_d[1];
+                    s->dz[i] = zsign * S[0] * S[1] * dS[2] * inv_d[2];
+                }
+                s->nds[i] = n0 + x3off[id] * g->xplane + y3off[id] * g->yplane + z3off[id] * g->zplane;
+            } else {
+                s->fn[i] = S[0] * S[1];
+                if (grad) {
+                    double xsign = xi[0] > gc[0] ? 1. : -1., ysign = xi[1] > gc[1] ? 1. : -1.;
+                    s->dx[i] = xsign * dS[0] * S[1] * inv_d[0];
+                    s->dy[i] = ysign * S[0] * dS[1] * inv_d[1];
+                    s->dz[i] = 0.;
+                }
+                s->nds[i] = n0 + xoff2[id] * g->xplane + yoff2[id] * g->yplane;
+            }
+            i++;
+        }
+        s->n = i;
+        return;
+    }
     if (shape == MPMGPU_SHAPE_BSPLINE) {
         /* B2SPLINE: FourNodeIsoparam::SplineShapeFunction (Common/Elements/
          * FourNodeIsoparam.cpp:217-293) and EightNodeIsoparamBrick::
@@ -2180,7 +2258,7 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     g_err[0] = 0;
     if (!grid || !opts || !mats || !p) return fail(MPMGPU_ERR_INVALID, "oracle: null argument");
     if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI &&
-        opts->shape != MPMGPU_SHAPE_BSPLINE)
+        opts->shape != MPMGPU_SHAPE_BSPLINE && opts->shape != MPMGPU_SHAPE_BGIMP)
         return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: shape function not implemented");
     if (contact && contact->enabled) {
         if (contact->normals < 0 || (contact->normals > 2 && contact->normals != 5 && contact->normals != 6))

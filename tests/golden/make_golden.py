@@ -101,6 +101,13 @@ CASES = {
     "contact2d_b2spline_fric": ("contact_2d", dict(steps=150, friction=0.3, normals=2, gimp="B2SPLINE")),
     "contact3d_b2spline_logreg": ("contact_3d", dict(steps=70, friction=0.3, normals=6, gimp="B2SPLINE", gap=0.5,
                                                      v=(50000., 0., -200000.))),
+    # B-spline GIMP shape functions (B2GIMP)
+    "cant2d_b2gimp": ("cantilever_2d", dict(nx=10, ny=4, steps=60, gimp="B2GIMP")),
+    "cant2d_b2gimp_ppc3_usl": ("cantilever_2d", dict(nx=8, ny=3, steps=40, ppc_side=3, gimp="B2GIMP", method=3)),
+    "taylor3d_b2gimp": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, gimp="B2GIMP")),
+    "taylor3d_b2gimp_neo_usf": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=60, gimp="B2GIMP", method=0,
+                                                  mat_type=28, G=10., K=50., rho=1.1, v0=-30000.)),
+    "contact2d_b2gimp_fric": ("contact_2d", dict(steps=150, friction=0.3, normals=2, gimp="B2GIMP")),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")
