@@ -181,6 +181,25 @@ void nmg::hcols(const MpmGpuParticles *h, double *out[kParticleDoubles]) {
 
 namespace {
 
+// Runs of host columns that sit back to back in the device's column order
+// (hcols), each moved with one copy: a host that keeps its particle columns in
+// one block in that order transfers them at the link's full rate instead of
+// paying a copy per column.  f(k, e) moves columns k .. e-1.
+template <class F>
+void column_runs(double *const hc[kParticleDoubles], size_t n, F &&f) {
+    int k = 0;
+    while (k < kParticleDoubles) {
+        if (!hc[k]) {
+            k++;
+            continue;
+        }
+        int e = k + 1;
+        while (e < kParticleDoubles && hc[e] && hc[e] == hc[e - 1] + n) e++;
+        f(k, e);
+        k = e;
+    }
+}
+
 void free_particles(MpmGpuCtx *c) {
     if (c->pblock) cudaFree(c->pblock);
     if (c->iblock) cudaFree(c->iblock);
@@ -520,13 +539,15 @@ int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
     }
     double *hc[kParticleDoubles];
     hcols(h, hc);
-    for (int k = 0; k < kParticleDoubles; k++) {
-        double *dst = c->pblock + (size_t)k * n;
-        if (hc[k])
-            CK(cudaMemcpyAsync(dst, hc[k], (size_t)n * sizeof(double), cudaMemcpyHostToDevice, c->stream));
-        else
-            CK(cudaMemsetAsync(dst, 0, (size_t)n * sizeof(double), c->stream));
-    }
+    for (int k = 0; k < kParticleDoubles; k++)
+        if (!hc[k]) CK(cudaMemsetAsync(c->pblock + (size_t)k * n, 0, (size_t)n * sizeof(double), c->stream));
+    cudaError_t ce = cudaSuccess;
+    column_runs(hc, (size_t)n, [&](int k, int e) {
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(c->pblock + (size_t)k * n, hc[k], (size_t)(e - k) * n * sizeof(double),
+                                 cudaMemcpyHostToDevice, c->stream);
+    });
+    CK(ce);
     CK(cudaMemcpyAsync(c->p.mat, h->mat, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     CK(cudaMemcpyAsync(c->p.elem, h->elem, (size_t)n * sizeof(int), cudaMemcpyHostToDevice, c->stream));
     // identity slot order and a range check of the indices the kernels use
@@ -750,9 +771,13 @@ int mpmgpu_download_particles(MpmGpuCtx *c, MpmGpuParticles *h) {
     if (st != 0) return set_err(c, MPMGPU_ERR_CUDA, "unsort failed");
     double *hc[kParticleDoubles];
     hcols(h, hc);
-    for (int k = 0; k < kParticleDoubles; k++)
-        if (hc[k]) CK(cudaMemcpyAsync(hc[k], c->sort.scratch + (size_t)k * n, (size_t)n * sizeof(double),
-                                      cudaMemcpyDeviceToHost, c->stream));
+    cudaError_t ce = cudaSuccess;
+    column_runs(hc, (size_t)n, [&](int k, int e) {
+        if (ce == cudaSuccess)
+            ce = cudaMemcpyAsync(hc[k], c->sort.scratch + (size_t)k * n, (size_t)(e - k) * n * sizeof(double),
+                                 cudaMemcpyDeviceToHost, c->stream);
+    });
+    CK(ce);
     CK(cudaMemcpyAsync(h->mat, c->sort.iscratch, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaMemcpyAsync(h->elem, c->sort.iscratch + n, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, c->stream));
     CK(cudaStreamSynchronize(c->stream));

@@ -139,6 +139,29 @@ def copy_particles(p: dict) -> dict:
     return {k: np.array(v, copy=True) for k, v in p.items()}
 
 
+# the library's device column order of the FP64 particle columns (nmg::hcols)
+DEVICE_COLUMNS = ["x", "y", "z", "vx", "vy", "vz", "mass", "lpx", "lpy", "lpz",
+                  "exx", "eyy", "ezz", "exy", "exz", "eyz", "wxy", "wxz", "wyz",
+                  "sxx", "syy", "szz", "sxy", "sxz", "syz", "pressure",
+                  "pxx", "pyy", "pzz", "pxy", "pxz", "pyz", "hist0", "hist1", "work", "plast", "x0", "y0", "z0"]
+
+
+def contiguous_particles(p: dict) -> tuple[dict, np.ndarray]:
+    """A copy of p whose FP64 columns are rows of one block in the library's
+    device column order, so uploads and downloads move them with one copy
+    each; returns (columns, block)."""
+    n = len(p["x"])
+    block = np.empty((len(DEVICE_COLUMNS), n), dtype=np.float64)
+    out = {}
+    for i, k in enumerate(DEVICE_COLUMNS):
+        block[i] = p[k]
+        out[k] = block[i]
+    for k, v in p.items():
+        if k not in out:
+            out[k] = np.array(v, copy=True)
+    return out, block
+
+
 def empty_like_particles(p: dict) -> dict:
     return {k: np.zeros_like(v) for k, v in p.items()}
 
