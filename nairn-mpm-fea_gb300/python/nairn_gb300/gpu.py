@@ -279,8 +279,11 @@ class GpuBatch:
 
     @classmethod
     def for_models(cls, models, precision: int = 0, slack: float = 1.0, **kw) -> "GpuBatch":
-        """A batch sized to hold all `models` at once (times `slack`)."""
+        """A batch sized to hold all `models` at once (times `slack`).  The
+        runs of a batch share its analysis options, PeriodicXPIC included."""
         o = models[0].options
+        if "xpic" not in kw and len({xpic_of(m) for m in models}) > 1:
+            raise ValueError("the runs of a batch share one PeriodicXPIC setting")
         return cls(o["np"], o["method"], o["shape"], precision, max_runs=kw.pop("max_runs", len(models)),
                    max_particles=int(slack * sum(m.n for m in models)),
                    max_nodes=int(slack * sum(m.grid.nnodes for m in models)),
