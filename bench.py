@@ -70,6 +70,9 @@ def parse():
     ap.add_argument("--contact-runs", type=int, default=48,
                     help="runs of the batched 3D contact instance mix (0: skip)")
     ap.add_argument("--contact-steps", type=int, default=40, help="timed steps of the batched contact measurement")
+    ap.add_argument("--contact-normals", type=int, choices=(0, 1, 2, 5, 6), default=2,
+                    help="contact normal method of the contact legs (2: average volume gradients; 6: logistic "
+                         "regression, the reference's default)")
     ap.add_argument("--contact-serve-requests", type=int, default=32,
                     help="requests of the served 3D contact stream (0: skip)")
     ap.add_argument("--config3-steps", type=int, default=10,
@@ -509,11 +512,12 @@ def contact_served_measurement(args, dist):
     rng = np.random.default_rng(404)
     arrivals = np.cumsum(rng.exponential(1. / 20., n_req))
     steps = rng.integers(200, 1501, n_req)
-    ms = model.contact_models(n_req, seed=404, steps=1500)
+    ms = model.contact_models(n_req, seed=404, steps=1500, normals=args.contact_normals)
     for m, k in zip(ms, steps):
         m.nsteps = int(k)
     srv = gpu.GpuServer(model.USAVG, model.SHAPE_LCPDI, 1, hbm_budget_bytes=int(args.serve_budget_gb * 1e9),
-                        max_runs=256, steps_per_round=10, frac_3d=1.0, nodes_per_particle=1.5, max_fields=2)
+                        max_runs=256, steps_per_round=10, frac_3d=1.0, nodes_per_particle=1.5, max_fields=2,
+                        lr_links=64 if args.contact_normals >= 5 else 0)
     dist.barrier()
     t0 = time.perf_counter()
     ids = []
@@ -551,7 +555,7 @@ def contact_served_measurement(args, dist):
                                    "block on elastic plate, Coulomb 0.3, lCPDI, 0.5 mm cells, 8 particles/cell, "
                                    "USAVG), 20k-500k particles, 200-1500 steps (seed 404)" % n_req,
                        "policy": "every request admitted on arrival (FIFO)", "hbm_budget_gb": args.serve_budget_gb,
-                       "steps_per_round": 10, "rounds": st["rounds"]},
+                       "steps_per_round": 10, "rounds": st["rounds"], "normals": args.contact_normals},
             "alone_plain_fp64": {"throughput": alone_ps / alone_s, "unit": METRIC, "requests": len(alone),
                                  "p50_ms": float(np.percentile(alone, 50)), "p99_ms": float(np.percentile(alone, 99)),
                                  "sample": "every 4th request alone: setup + 10 timed steps scaled to its steps"},
@@ -633,7 +637,7 @@ def config3_measurement(args, dist, local):
     and mixed precision on the same steps, with the mixed state's error."""
     from nairn_gb300 import gpu, model
     m = model.contact_3d(plate=(128, 128, 30), block=(40, 40, 16), block_x0=22.0, block_y0=22.0, cell=0.5,
-                         v=(4000., 0., -4000.), steps=1500, gimp="lCPDI", friction=0.3, normals=2)
+                         v=(4000., 0., -4000.), steps=1500, gimp="lCPDI", friction=0.3, normals=args.contact_normals)
     k = args.config3_steps
     out, finals = {}, {}
     for prec in (0, 1):
@@ -659,7 +663,7 @@ def config3_measurement(args, dist, local):
             "steps": k, "gpu_launches": out[1]["gpu_launches"], "clocks": out[1]["clocks"],
             "config": {"workload": "3D multimaterial contact: Neo-Hookean block pressed and sliding on an elastic "
                                    "plate, Coulomb friction 0.3, lCPDI, 0.5 mm cells, 2x2x2 particles/cell, USAVG",
-                       "particles": m.n, "grid_nodes": m.grid.nnodes, "material_fields": 2,
+                       "particles": m.n, "grid_nodes": m.grid.nnodes, "material_fields": 2, "normals": args.contact_normals,
                        "sort_interval": out[1]["sort_interval"],
                        "l2": "particle state %.2f GB vs 129 MB L2: no flush needed" % (m.n * 42 * 8 / 1e9)},
             "plain_fp64": {"value": out[0]["value"], "ms_per_step": out[0]["ms_per_step"],
@@ -678,7 +682,7 @@ def contact_batched_measurement(args, dist, local):
     precision, autotuned.  Beside it: every run alone on the plain single-run
     FP64 path (the same steps) and each batched result's error against it."""
     from nairn_gb300 import gpu, model
-    ms = model.contact_models(args.contact_runs, seed=303, steps=1500)
+    ms = model.contact_models(args.contact_runs, seed=303, steps=1500, normals=args.contact_normals)
     n = sum(m.n for m in ms)
     b = gpu.GpuBatch.for_models(ms, precision=1)
     ids = [b.add(m) for m in ms]
@@ -713,7 +717,7 @@ def contact_batched_measurement(args, dist, local):
                                    "plate, Coulomb 0.3, lCPDI, 0.5 mm cells, 8 particles/cell, USAVG), "
                                    "20k-500k particles each (log-uniform, seed 303); one graph-captured "
                                    "batched step" % len(ms),
-                       "particles": n, "grid_nodes": info["nodes_used"], "runs": len(ms), "material_fields": 2,
+                       "particles": n, "grid_nodes": info["nodes_used"], "runs": len(ms), "material_fields": 2, "normals": args.contact_normals,
                        "autotuned": {"block": blk, "sort_interval": si},
                        "timed_window": "steps %d-%d of each run" % (done - k + 1, done),
                        "l2": "batch state %.1f GB vs 129 MB L2: no flush needed" % (n * 42 * 8 / 1e9)},
