@@ -198,7 +198,7 @@ __device__ __forceinline__ double lr_radius(const DevGrid &g, const DevParticles
 // logistic normal penalty 1e-7 cell^2, no offset penalty, the linear beta
 // doubled as the start, convergence 1 - cos < 1e-5 within 15 iterations.
 template <int DIM, bool BATCH>
-static __global__ void __launch_bounds__(256) k_lr_normals(StepParams sp, DevParticles p, DevNodes nd,
+static __global__ void __launch_bounds__(256, 3) k_lr_normals(StepParams sp, DevParticles p, DevNodes nd,
                                                            const DevMat *mats, const int *start, const int *list,
                                                            double *out, int nnodes, long long cap, int logistic) {
     // one warp per (node, material field): the fields' regressions are independent

@@ -57,7 +57,7 @@ def main(argv=None):
         if a.workload == "batch":
             ms = model.batch_models(512, seed=2024)[:a.runs]
         else:
-            ms = model.contact_models(a.runs, seed=303, steps=1500)
+            ms = model.contact_models(a.runs, seed=303, steps=1500, normals=a.normals)
         b = gpu.GpuBatch.for_models(ms, precision=prec, sort_interval=a.sort_interval)
         for m in ms:
             b.add(m)
