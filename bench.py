@@ -4,24 +4,34 @@
 Workload (default): the 3D elastic-plastic Taylor impact -- von Mises with
 linear hardening (E=200 GPa, nu=0.3, yield 300 MPa, Ep 2 GPa, rho 7.8 g/cm^3),
 cylinder r=5 mm, L=25 mm at 200 m/s onto a rigid wall (zero normal velocity on
-the wall node plane), 0.25 mm cells, 2x2x2 particles per cell (~1.0 M
-particles), uGIMP, USAVG, all-FP64 path.  Inputs are synthetic (seeded,
+the wall node plane), 0.25 mm cells, 2x2x2 particles per cell (1,004,800
+particles), uGIMP, USAVG, 2,000 steps.  Inputs are synthetic (seeded,
 deterministic), built exactly as the reference's XML generator builds them.
 
 One "step" = one explicit MPM step over all particles (P2G, grid update with
 velocity BCs, strain/constitutive update, internal forces, momentum update,
 G2P, second extrapolation and strain update, element reset).
 
+The headline `value` is the plain single-run FP64 path -- the arithmetic of
+the reference -- timed over a window in the middle of the 2,000-step run
+(the run is advanced untimed to --window-start, default step 1,000, where the
+plastic zone has grown; then W warm-up and K timed steps).  The reference arm
+(--impl reference: the CPU restatement of the reference step, all host
+threads) times the same window of the same run.
+
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-The line also carries "batched": 512 independent seeded 2D runs (2k-200k
-particles each) advanced by one graph-captured batched step in mixed
-precision, against the same runs on the plain single-run FP64 path, with the
-error of the batched results against that path; "contact3d": the 3D
-two-material contact problem (4.1 M particles, lCPDI) in FP64 and mixed
-precision; "contact3d_batched": 48 seeded contact runs of 20k-500k particles
-in one batched mixed step against each run alone on the plain FP64 path; and
-"served": a seeded request stream through the continuous-batching server.
+The line also carries "mixed": the same window in the mixed-precision mode
+(FP32 transfers, FP64 constitutive update) with its error against the FP64
+path; "batched": 512 independent seeded 2D runs (2k-200k particles each)
+advanced by one graph-captured batched step in mixed precision, against the
+same runs on the plain single-run FP64 path, with the error of the batched
+results against that path; "contact3d": the 3D two-material contact problem
+(4.1 M particles, lCPDI) in FP64 and mixed precision; "contact3d_batched": 48
+seeded contact runs of 20k-500k particles in one batched mixed step against
+each run alone on the plain FP64 path; "served": a seeded request stream
+through the continuous-batching server; and "batched_vs_plain", the ratio the
+batched/served forms reach over the plain FP64 path at their stated error.
 
 Under torchrun (N>1) every rank runs an independent replica of the workload
 (the runs do not exchange data), so scaling is weak.
@@ -59,8 +69,8 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
-    ap.add_argument("--precision", choices=("mixed", "fp64"), default="mixed",
-                    help="transfer arithmetic of the headline run (the FP64 path is always measured too)")
+    ap.add_argument("--window-start", type=int, default=1000,
+                    help="step at which the timed window opens (the run is advanced to it untimed)")
     ap.add_argument("--batch-runs", type=int, default=512,
                     help="runs of the batched measurement (0: skip it)")
     ap.add_argument("--batch-steps", type=int, default=100, help="timed steps of the batched measurement")
@@ -134,15 +144,30 @@ class Dist:
 
 def workload(args):
     from nairn_gb300 import model
-    return model.taylor_3d(radius=args.radius, length=args.length, cell=args.cell,
-                           steps=args.steps + args.warmup)
+    return model.taylor_3d(radius=args.radius, length=args.length, cell=args.cell, steps=2000)
+
+
+TUNE_STEPS = 64  # real steps the sort-interval autotuner takes (2 rounds x 4 intervals x 8 steps)
+
+
+def window_open(args) -> int:
+    """Step the run is advanced to, untimed, before the warm-up steps."""
+    return max(args.window_start, TUNE_STEPS if args.sort_interval <= 0 else 0)
+
+
+def window_first(args) -> int:
+    """Steps completed when the timed window opens."""
+    return window_open(args) + args.warmup
 
 
 def workload_config(args, m, extra=None):
     cfg = {"workload": "3D elastic-plastic Taylor impact (von Mises, linear hardening), r=%g mm, L=%g mm, "
-                       "%g mm cells, 2x2x2 particles/cell, uGIMP, USAVG, FP64" % (args.radius, args.length, args.cell),
+                       "%g mm cells, 2x2x2 particles/cell, uGIMP, USAVG, 2,000 steps" % (args.radius, args.length,
+                                                                                         args.cell),
            "particles": m.n, "grid_nodes": m.grid.nnodes, "material": "IsoPlasticity + LinearHardening",
            "timestep_s": m.options["timestep"],
+           "timed_window": "steps %d-%d of the run (advanced untimed to step %d, then %d warm-up steps)" % (
+               window_first(args) + 1, window_first(args) + args.steps, window_open(args), args.warmup),
            "l2": ("particle state %.0f MB vs 129 MB L2: inputs larger than L2, no flush needed"
                   if m.n * 39 * 8 > 129e6 else "particle state %.0f MB fits in L2") % (m.n * 39 * 8 / 1e6),
            "parallelism": "replicas" if int(os.environ.get("WORLD_SIZE", "1")) > 1 else "single GPU"}
@@ -274,60 +299,82 @@ class ClockSampler:
                 "samples": len(sm), "reasons": sorted(reasons)}
 
 
-def cpu_baseline(m, seconds: float):
-    """The CPU restatement of the reference step (oracle port), all host threads,
-    on a bounded sample of the same workload (the first steps of the run)."""
+def cpu_baseline(m, p, first_step: int, seconds: float):
+    """The CPU restatement of the reference step (oracle port), all host
+    threads, on a bounded sample of the same workload: steps from the particle
+    state p, which is the state after `first_step` steps."""
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle_lib
     from nairn_gb300 import abi
     threads = os.cpu_count() or 1
-    p = abi.copy_particles(m.particles)
+    dt = m.options["timestep"]
+    p = abi.copy_particles(p)
     t0 = time.perf_counter()
-    oracle_lib.run(m, p, 1, 0.0, nthreads=threads)
+    oracle_lib.run(m, p, 1, first_step * dt, nthreads=threads)
     t1 = time.perf_counter() - t0
     steps = max(1, min(200, int(seconds / max(t1, 1e-6))))
     t0 = time.perf_counter()
-    oracle_lib.run(m, p, steps, m.options["timestep"], nthreads=threads)
-    dt = time.perf_counter() - t0
-    return {"value": m.n * steps / dt, "unit": METRIC, "cores": threads, "kind": "port",
-            "sample": f"{steps} steps (after 1 untimed) of the same {m.n}-particle workload, "
-                      f"{threads} OpenMP threads, FP64"}
+    oracle_lib.run(m, p, steps, (first_step + 1) * dt, nthreads=threads)
+    el = time.perf_counter() - t0
+    return {"value": m.n * steps / el, "unit": METRIC, "cores": threads, "kind": "port",
+            "sample": f"steps {first_step + 2}-{first_step + 1 + steps} (after 1 untimed) of the same {m.n}-particle "
+                      f"run, from its state after {first_step} steps, {threads} OpenMP threads, FP64"}
 
 
 def run_reference(args, ws, rank, local):
+    """The reference arm: the CPU restatement of the reference's step (the
+    reference itself is C++ built for this container's host, not for the GPU
+    host), all host threads, FP64, on the same window of the same run as the
+    GPU arm: advanced untimed to the window, W warm-up steps, K timed steps."""
     if rank != 0:
         return 0
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle_lib
+    from nairn_gb300 import abi
     m = workload(args)
-    b = cpu_baseline(m, args.cpu_seconds * max(1, args.steps) / 200.0 + 5.0)
-    line = {"metric": METRIC, "value": b["value"], "unit": METRIC, "n_gpus": args.gpus, "steps": args.steps,
-            "warmup": args.warmup, "ms_per_step": 1e3 * m.n / b["value"], "higher_is_better": True,
+    threads = os.cpu_count() or 1
+    dt = m.options["timestep"]
+    p = abi.copy_particles(m.particles)
+    t_adv = time.perf_counter()
+    oracle_lib.run(m, p, window_open(args), 0.0, nthreads=threads)
+    oracle_lib.run(m, p, args.warmup, window_open(args) * dt, nthreads=threads)
+    t_adv = time.perf_counter() - t_adv
+    k = max(1, args.steps)
+    t0 = time.perf_counter()
+    oracle_lib.run(m, p, k, window_first(args) * dt, nthreads=threads)
+    el = time.perf_counter() - t0
+    value = m.n * k / el
+    b = {"value": value, "unit": METRIC, "cores": threads, "kind": "port",
+         "sample": "steps %d-%d of the %d-particle run (advanced untimed to step %d in %.0f s), %d OpenMP "
+                   "threads, FP64" % (window_first(args) + 1, window_first(args) + k, m.n, window_first(args), t_adv,
+                                      threads)}
+    line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": args.gpus, "steps": k,
+            "warmup": args.warmup, "ms_per_step": 1e3 * el / k, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "impl": "reference", "config": workload_config(args, m),
-            "cpu_baseline": b, "e2e": {"value": b["value"], "unit": METRIC, "h2d_bytes_per_step": 0,
+            "cpu_baseline": b, "e2e": {"value": value, "unit": METRIC, "h2d_bytes_per_step": 0,
                                         "d2h_bytes_per_step": 0}}
     print(json.dumps(line))
     return 0
 
 
-def timed_run(args, m, dist, precision: int, local: int):
-    """W warm-up steps, then K steps timed with CUDA events on the context
-    stream (per-kernel event pairs in the same region).  Returns the run
-    (still open), its timings and the state after W+K steps."""
+def window_run(args, m, dist, precision: int, local: int):
+    """The run advanced untimed to the window (the sort interval autotuned
+    on its last TUNE_STEPS steps), W warm-up steps, then K steps timed with
+    CUDA events on the context stream -- nothing else is recorded in that
+    region -- and a second pass of K steps with per-kernel event pairs that
+    gives the kernel split.  Returns the run (still open), its timings and
+    the state at the end."""
     from nairn_gb300 import gpu
     si = args.sort_interval
-    if si <= 0:
-        # the sort interval, tuned on a separate context over the same early
-        # steps, so the measured run covers steps W+1 .. W+K like any other
-        tune = gpu.GpuRun(m, precision=precision)
-        tune.upload(m.particles)
-        tune.step(args.warmup)
-        si, _ = tune.autotune_sort(16)
-        tune.close()
-    run = gpu.GpuRun(m, sort_interval=si, precision=precision)
+    run = gpu.GpuRun(m, sort_interval=si if si > 0 else 8, precision=precision)
     run.upload(m.particles)
+    if si <= 0:
+        run.step(window_open(args) - TUNE_STEPS)
+        si, _ = run.autotune_sort(16)
+    else:
+        run.step(window_open(args))
     run.step(args.warmup)
-    tuned = 0
-    run.set_profiling(True)
     launches0 = run.launch_count()
     clocks = ClockSampler(local)
     clocks.start()
@@ -336,11 +383,13 @@ def timed_run(args, m, dist, precision: int, local: int):
     dist.barrier()
     clk = clocks.stop()
     launches = run.launch_count() - launches0
+    run.set_profiling(True)
+    ms_prof = run.step_timed(args.steps)
     prof = run.profile()
     run.set_profiling(False)
     final = run.download(m.particles)
-    return run, {"ms": ms, "prof": prof, "launches": launches, "clocks": clk, "sort_interval": si,
-                 "tuning_steps": tuned}, final
+    return run, {"ms": ms, "prof": prof, "ms_profiled_pass": ms_prof, "launches": launches, "clocks": clk,
+                 "sort_interval": si, "steps_done": window_first(args) + 2 * args.steps}, final
 
 
 def state_error(a: dict, b: dict, dim: int) -> dict:
@@ -729,6 +778,59 @@ def contact_batched_measurement(args, dist, local):
                                         target="<= 1e-5 relative L2")}
 
 
+def fp64_flops_from_profiles(kernel: str, n_particles: int):
+    """FP64 flops per launch (2 per DFMA, 1 per DADD/DMUL) from the committed
+    ncu instruction counts of the FP64 path, scaled to this particle count."""
+    p = os.path.join(ROOT, "profiles", "ncu_fp64_ops.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as fh:
+        d = json.load(fh)
+    k = d.get("kernels", {}).get(kernel)
+    if not k:
+        return None
+    return k["fp64_flops_per_launch"] * n_particles / d["particles"]
+
+
+def kernel_table(prof: dict, steps: int, bytes_model: dict, launches_of) -> dict:
+    fams = {k: v for k, v in prof.items() if v > 0}
+    total = sum(fams.values())
+    return {k: {"ms_per_step": v / steps, "share": v / total,
+                "algorithmic_GBps": (bytes_model.get(k, 0) / ((v / launches_of(k)) / 1e3) / 1e9)
+                if bytes_model.get(k, 0) > 0 else None}
+            for k, v in fams.items()}
+
+
+def roofline_of(prof: dict, steps: int, sort_interval: int, m, nodes: int, fp64_peak_tflops):
+    """HBM roofline of the dominant kernel (largest share of the profiled
+    pass), and for the FP64 path its FP64-pipe roofline against the FP64 FMA
+    rate measured on this GPU."""
+    fams = {k: v for k, v in prof.items() if v > 0}
+    dom = max(fams, key=fams.get)
+
+    def launches_of(k):
+        return steps if k != "sort" else max(1, steps // sort_interval)
+
+    avg_ms = fams[dom] / launches_of(dom)
+    bytes_model = algorithmic_bytes(m, nodes)
+    peak, peak_kind = peaks()
+    achieved = bytes_model[dom] / (avg_ms / 1e3) / 1e9
+    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
+            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
+            "traffic": traffic_from_profiles(dom, m.n), "algorithmic_bytes_per_launch": bytes_model[dom],
+            "avg_launch_ms": avg_ms,
+            "note": "per-launch time from CUDA events of a separate profiled pass over the same window"}
+    fl = fp64_flops_from_profiles(dom, m.n)
+    fp64 = None
+    if fl is not None and fp64_peak_tflops:
+        ach = fl / (avg_ms / 1e3) / 1e12
+        fp64 = {"kernel": dom, "bound": "fp64", "achieved": ach, "peak": fp64_peak_tflops, "unit": "TFLOP/s",
+                "frac": ach / fp64_peak_tflops, "flops_per_launch": fl,
+                "peak_source": "measured in this run (mpmgpu_fp64_fma_rate: independent DFMA chains)",
+                "flops_source": "ncu instruction counts (profiles/ncu_fp64_ops.json), scaled to this size"}
+    return roof, fp64, kernel_table(prof, steps, bytes_model, launches_of)
+
+
 def main():
     args = parse()
     ws, rank, local = dist_setup()
@@ -741,26 +843,21 @@ def main():
     m = workload(args)
     n = m.n
     total_particles = dist.sum(float(n))
-    prec = 1 if args.precision == "mixed" else 0
+    fp64_peak = gpu.fma_rate(True)
+    fp32_peak = gpu.fma_rate(False)
+    nodes = active_nodes(m)
 
-    # the plain FP64 path, measured on the same workload and step count
-    plain_run, plain, plain_final = timed_run(args, m, dist, 0, local)
-    plain_run.close()
-    plain_value = total_particles * args.steps / (dist.max(plain["ms"]) / 1e3)
-    if prec == 0:
-        run, head, final = timed_run(args, m, dist, 0, local)
-    else:
-        run, head, final = timed_run(args, m, dist, prec, local)
-    err = state_error(final, plain_final, m.grid.dim)
+    # the headline: the plain FP64 path over the window
+    run, head, final = window_run(args, m, dist, 0, local)
     ms_max = dist.max(head["ms"])
     value = total_particles * args.steps / (ms_max / 1e3)
-    prof, launches, clk = head["prof"], head["launches"], head["clocks"]
+    roof, roof64, kernels = roofline_of(head["prof"], args.steps, head["sort_interval"], m, nodes, fp64_peak)
 
     # end to end through the C ABI with host-resident particle state: every
     # step uploads the state from pinned host memory and downloads the result
     # the host keeps its FP64 columns in one block in the library's column
     # order, so each direction moves them in one copy
-    host, block = abi.contiguous_particles(m.particles)
+    host, block = abi.contiguous_particles(final)
     pinned = gpu.pin({"block": block, "mat": host["mat"], "elem": host["elem"]})
     h2d = block.nbytes + host["mat"].nbytes + host["elem"].nbytes
     d2h = h2d
@@ -779,49 +876,42 @@ def main():
     gpu.unpin(pinned)
     t_e2e = dist.max(t_e2e)
     e2e_value = total_particles * ke / t_e2e
-    archived = archive_measurement(args, run, m, dist) if args.archive_steps > 0 else None
     run.close()
 
-    # roofline of the dominant kernel (largest share of the timed region)
-    fams = {k: v for k, v in prof.items() if v > 0}
-    dom = max(fams, key=fams.get)
-    launches_dom = args.steps if dom != "sort" else max(1, args.steps // head["sort_interval"])
-    avg_ms = fams[dom] / launches_dom
-    nodes = active_nodes(m)
-    bytes_model = algorithmic_bytes(m, nodes)
-    peak, peak_kind = peaks()
-    achieved = bytes_model[dom] / (avg_ms / 1e3) / 1e9
-    roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
-            "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": traffic_from_profiles(dom, n), "algorithmic_bytes_per_launch": bytes_model[dom],
-            "avg_launch_ms": avg_ms,
-            "note": "FP64-pipe bound on GB300 (ncu: profiles/), so the HBM fraction is low by construction"}
-    kernels = {k: {"ms_per_step": v / args.steps, "share": v / sum(fams.values()),
-                   "algorithmic_GBps": (bytes_model.get(k, 0) / ((v / launches_dom) / 1e3) / 1e9)
-                   if v > 0 and bytes_model.get(k, 0) > 0 else None}
-               for k, v in fams.items()}
-    dtype = "mixed: f32 transfers, f64 constitutive" if prec else "f64"
+    # the mixed-precision mode over the same window, with its error against
+    # the FP64 path at the same step
+    mrun, mixed, mfinal = window_run(args, m, dist, 1, local)
+    archived = archive_measurement(args, mrun, m, dist) if args.archive_steps > 0 else None
+    mrun.close()
+    mroof, _, mkernels = roofline_of(mixed["prof"], args.steps, mixed["sort_interval"], m, nodes, None)
+    err = state_error(mfinal, final, m.grid.dim)
+    mixed_value = total_particles * args.steps / (dist.max(mixed["ms"]) / 1e3)
+
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": dtype, "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
             "config": workload_config(args, m, {"sort_interval": head["sort_interval"],
                                                 "sort_interval_autotuned": args.sort_interval <= 0,
-                                                "active_nodes_t0": nodes, "precision": args.precision}),
-            "plain_fp64": {"value": plain_value, "ms_per_step": dist.max(plain["ms"]) / args.steps,
-                           "sort_interval": plain["sort_interval"],
-                           "kernels_ms_per_step": {k: v / args.steps for k, v in plain["prof"].items() if v > 0}},
-            "error_vs_fp64_path": dict(err, steps=args.warmup + head["tuning_steps"] + args.steps,
-                                       note="relative L2 of the headline run against the all-FP64 GPU path, "
-                                            "which matches the reference within 1e-10"),
+                                                "active_nodes_t0": nodes, "precision": "fp64"}),
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d * ws,
                     "d2h_bytes_per_step": d2h * ws, "steps": ke,
-                    "note": "per step: upload the full particle state from pinned host memory (FP64 columns "
-                            "in one block), one step, download it again"},
-            "gpu_launches": launches, "roofline": roof, "kernels": kernels, "clocks": clk}
+                    "note": "FP64 path; per step: upload the full particle state from pinned host memory (FP64 "
+                            "columns in one block), one step, download it again"},
+            "gpu_launches": head["launches"], "roofline": roof, "roofline_fp64": roof64, "kernels": kernels,
+            "clocks": head["clocks"],
+            "measured_peaks": {"fp64_fma_tflops": fp64_peak, "fp32_fma_tflops": fp32_peak,
+                               "ratio_fp32_to_fp64": fp32_peak / fp64_peak},
+            "mixed": {"value": mixed_value, "unit": METRIC, "ms_per_step": dist.max(mixed["ms"]) / args.steps,
+                      "dtype": "mixed: f32 transfers, f64 constitutive", "sort_interval": mixed["sort_interval"],
+                      "speedup_vs_fp64": mixed_value / value, "gpu_launches": mixed["launches"],
+                      "clocks": mixed["clocks"], "roofline": mroof, "kernels": mkernels,
+                      "error_vs_fp64_path": dict(err, steps=head["steps_done"],
+                                                 note="relative L2 against the FP64 GPU path after the same "
+                                                      "steps; that path matches the reference within 1e-10")}}
     if archived:
         line["archived"] = archived
     if args.xpic_steps > 0:
-        line["xpic"] = xpic_measurement(args, dist, head["sort_interval"], prec)
+        line["xpic"] = xpic_measurement(args, dist, mixed["sort_interval"], 1)
     if args.config3_steps > 0:
         line["contact3d"] = config3_measurement(args, dist, local)
     if args.contact_runs > 0:
@@ -832,8 +922,20 @@ def main():
         line["served"] = served_measurement(args, dist)
     if args.contact_serve_requests > 0:
         line["contact3d_served"] = contact_served_measurement(args, dist)
+    bvp = {}
+    for key, what in (("batched", "512 independent 2D runs in one batched mixed step"),
+                      ("contact3d_batched", "48 independent 3D contact runs in one batched mixed step"),
+                      ("served", "served 2D/3D elastic-plastic stream (mixed)"),
+                      ("contact3d_served", "served 3D contact stream (mixed)")):
+        if key in line:
+            r = line[key]
+            bvp[key] = {"form": what, "speedup_vs_plain_fp64": r["speedup_vs_plain_fp64"],
+                        "error_vs_plain_fp64": r.get("error_vs_plain_fp64")}
+    if bvp:
+        line["batched_vs_plain"] = dict(bvp, target=">= 3x the plain single-run FP64 path at <= 1e-5 relative "
+                                                    "stress error")
     if rank == 0 and ws == 1 and not args.no_cpu_baseline:
-        line["cpu_baseline"] = cpu_baseline(workload(args), args.cpu_seconds)
+        line["cpu_baseline"] = cpu_baseline(m, final, head["steps_done"], args.cpu_seconds)
     dist.close()
     if rank == 0:
         print(json.dumps(line))

@@ -245,11 +245,17 @@ int mpmgpu_sort_by_cell(const int32_t *d_elem, int32_t n, int32_t nelems, int32_
  * MPMGPU_ERR_INVALID before any device work.  Its scratch is a fixed device
  * array inside this library (2.25 MiB per GPU, held until the process
  * exits), so it calls no cudaMalloc, cudaFree or allocating library routine.
- * The first call on a device looks up that array's device address (once per
- * device); make that first call before any stream capture.  All calls share
- * the one array: calls whose work overlaps on a GPU (different streams or
- * host threads without ordering) race and must be serialised by the caller.
- * The call synchronizes `stream`. */
+ * Every call looks up that array's device address in the context current on
+ * the calling thread (cudaGetSymbolAddress, which allocates nothing); the
+ * first call on a device also loads the library's module there, so make that
+ * first call before any stream capture.  Nothing is cached between calls, so
+ * a cudaDeviceReset or another context made current on the device leaves
+ * nothing stale for the caller to redo.  A CUDA error already pending when
+ * the call starts is returned as MPMGPU_ERR_CUDA (and left pending) before
+ * any work.  All calls share the one array, which keeps the last call's
+ * contents: calls whose work overlaps on a GPU (different streams or host
+ * threads without ordering) race and must be serialised by the caller.  The
+ * call synchronizes `stream`. */
 int mpmgpu_sort_by_cell_noalloc(const int32_t *d_elem, int32_t n, int32_t nelems, int32_t *d_perm, void *stream);
 
 /* ---- archive output ----------------------------------------------------------
@@ -313,6 +319,14 @@ long long mpmgpu_launch_count(const MpmGpuCtx *ctx);
  * particle columns run as asynchronous DMA; unregister before freeing. */
 int mpmgpu_host_register(void *ptr, uint64_t bytes);
 int mpmgpu_host_unregister(void *ptr);
+
+/* Extension (measurement): FMA throughput of the current device in TFLOP/s
+ * (2 flops per FMA), measured by one kernel of independent FMA chains timed
+ * with CUDA events; *ms receives the kernel time.  The FP64 path of the step
+ * is bound by the FP64 pipe, so its roofline is taken against this rate.  No
+ * counterpart in the reference. */
+int mpmgpu_fp64_fma_rate(int32_t iters, double *tflops, double *ms);
+int mpmgpu_fp32_fma_rate(int32_t iters, double *tflops, double *ms);
 
 /* ---- batch: many independent runs in one graph-captured step ----------------
  * A batch holds the state of many runs on the device and advances all of them
@@ -468,8 +482,10 @@ int mpmgpu_server_drain(MpmGpuServer *s, double timeout_s);
 int mpmgpu_server_release(MpmGpuServer *s, int64_t request_id);
 int mpmgpu_server_stats(MpmGpuServer *s, MpmGpuServerStats *stats);
 const char *mpmgpu_server_last_error(const MpmGpuServer *s);
-/* Stop the loop (queued and running requests are abandoned) and free the
- * device memory; no other call may be waiting on the server. */
+/* Stop the loop and free the device memory.  Requests still queued or
+ * running end as failed (MPMGPU_ERR_BUSY, "server stopped ...") and waiters
+ * are woken, but every mpmgpu_server_wait / _drain must have returned before
+ * this call: the server, its mutex and its condition variable are freed. */
 void mpmgpu_server_destroy(MpmGpuServer *s);
 
 #ifdef __cplusplus

@@ -19,4 +19,7 @@ int derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::string &wh
 // natural coordinates)
 void hcols(const MpmGpuParticles *h, double *out[kParticleDoubles]);
 
+// sets the message of mpmgpu_last_error(NULL) and returns code
+int fail_static(int code, const std::string &m);
+
 }  // namespace nmg

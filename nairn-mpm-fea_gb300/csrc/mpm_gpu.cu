@@ -46,6 +46,14 @@ int cuda_fail(MpmGpuCtx *c, cudaError_t e, const char *where) {
     return set_err(c, MPMGPU_ERR_CUDA, std::string(where) + ": " + cudaGetErrorString(e));
 }
 
+}  // namespace
+
+// message of a failed call that has no context (mpmgpu_last_error(NULL)),
+// for the other translation units
+int nmg::fail_static(int code, const std::string &m) { return set_err(nullptr, code, m); }
+
+namespace {
+
 #define CK(call)                                            \
     do {                                                    \
         cudaError_t e_ = (call);                            \
@@ -961,34 +969,25 @@ namespace {
 constexpr int kNoAllocTiles = (MPMGPU_NOALLOC_MAX_PARTICLES + kTile - 1) / kTile;
 constexpr size_t kNoAllocSums = (256 * (size_t)kNoAllocTiles + kScanChunk - 1) / kScanChunk + 1;
 constexpr size_t kNoAllocInts = 4 * (size_t)MPMGPU_NOALLOC_MAX_PARTICLES + 256 * (size_t)kNoAllocTiles + kNoAllocSums;
-constexpr int kNoAllocMaxDevices = 64;
 }  // namespace
 
 static __device__ __align__(256) int g_noalloc_sort_scratch[kNoAllocInts];
 
 namespace {
-// Device address of g_noalloc_sort_scratch per device ordinal.  In host code
-// the array's name only stands in for the symbol; the address must come from
-// cudaGetSymbolAddress with that device current.
-std::mutex g_noalloc_mutex;
-int *g_noalloc_base[kNoAllocMaxDevices] = {};
-
+// Device address of g_noalloc_sort_scratch in the context current on the
+// calling thread.  In host code the array's name only stands in for the
+// symbol; its address comes from cudaGetSymbolAddress with the device
+// current.  The lookup is repeated on every call (it is a host-side query that
+// allocates nothing), so an address never outlives the context it came from:
+// after cudaDeviceReset, or with another context current on the same device,
+// the next call finds the array's address there.
 int noalloc_scratch(int **base) {
-    int dev = -1;
-    cudaError_t e = cudaGetDevice(&dev);
-    if (e != cudaSuccess) return cuda_fail(nullptr, e, "mpmgpu_sort_by_cell_noalloc: cudaGetDevice");
-    if (dev < 0 || dev >= kNoAllocMaxDevices)
-        return set_err(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_sort_by_cell_noalloc: device ordinal out of range");
-    std::lock_guard<std::mutex> lock(g_noalloc_mutex);
-    if (!g_noalloc_base[dev]) {
-        int *p = nullptr;
-        e = cudaGetSymbolAddress((void **)&p, g_noalloc_sort_scratch);
-        if (e != cudaSuccess || !p)
-            return cuda_fail(nullptr, e != cudaSuccess ? e : cudaErrorInvalidSymbol,
-                             "mpmgpu_sort_by_cell_noalloc: cudaGetSymbolAddress");
-        g_noalloc_base[dev] = p;
-    }
-    *base = g_noalloc_base[dev];
+    int *p = nullptr;
+    cudaError_t e = cudaGetSymbolAddress((void **)&p, g_noalloc_sort_scratch);
+    if (e != cudaSuccess || !p)
+        return cuda_fail(nullptr, e != cudaSuccess ? e : cudaErrorInvalidSymbol,
+                         "mpmgpu_sort_by_cell_noalloc: cudaGetSymbolAddress");
+    *base = p;
     return MPMGPU_OK;
 }
 }  // namespace
@@ -1003,6 +1002,13 @@ int mpmgpu_sort_by_cell_noalloc(const int32_t *d_elem, int32_t n, int32_t nelems
                        "mpmgpu_sort_by_cell_noalloc: n = " + std::to_string(n) + " exceeds the maximum of " +
                            std::to_string(MPMGPU_NOALLOC_MAX_PARTICLES) +
                            " particles this allocation-free variant supports; use mpmgpu_sort_by_cell");
+    // an error left pending by earlier, unrelated work is reported as such
+    // (and left pending for its owner) rather than blamed on this sort
+    cudaError_t pending = cudaPeekAtLastError();
+    if (pending != cudaSuccess)
+        return set_err(nullptr, MPMGPU_ERR_CUDA,
+                       std::string("mpmgpu_sort_by_cell_noalloc: a CUDA error was pending before the call: ") +
+                           cudaGetErrorString(pending));
     int *base = nullptr;
     int st = noalloc_scratch(&base);
     if (st != MPMGPU_OK) return st;

@@ -200,9 +200,15 @@ void server_loop(MpmGpuServer *s) {
             if (status[d] == MPMGPU_OK && launched[d]) status[d] = batch_collect(s->batch[d]);
         for (int d = 0; d < 2; d++) {
             if (status[d] != MPMGPU_OK) {
-                // a CUDA error on this batch: its running requests fail
+                // an error on this batch: its running requests fail.  Their
+                // runs leave the batch, so their particle slots, nodes and
+                // cells are free again; after a sticky CUDA error the removal
+                // fails as well and the batch stays unusable
+                const std::string why = mpmgpu_batch_last_error(s->batch[d]);
+                for (ServerRequest *q : s->running[d])
+                    if (q->run_id >= 0) mpmgpu_batch_remove_run(s->batch[d], q->run_id, nullptr);
                 std::lock_guard<std::mutex> lk(s->mu);
-                s->loop_error = mpmgpu_batch_last_error(s->batch[d]);
+                s->loop_error = why;
                 for (ServerRequest *q : s->running[d]) {
                     q->state = MPMGPU_REQ_FAILED;
                     q->status = status[d];
@@ -254,6 +260,23 @@ void server_loop(MpmGpuServer *s) {
             s->stats.busy_ms += ms_between(t0, ServerClock::now());
         }
     }
+    // stopping: requests still queued or running end as failed, and every
+    // waiter is woken before the server goes away
+    std::lock_guard<std::mutex> lk(s->mu);
+    auto stopped = [&](ServerRequest *q) {
+        q->state = MPMGPU_REQ_FAILED;
+        q->status = MPMGPU_ERR_BUSY;
+        q->msg = "server stopped before the request finished";
+        q->t_done = ServerClock::now();
+        s->stats.failed++;
+    };
+    for (ServerRequest *q : s->queue) stopped(q);
+    s->queue.clear();
+    for (int d = 0; d < 2; d++) {
+        for (ServerRequest *q : s->running[d]) stopped(q);
+        s->running[d].clear();
+    }
+    s->done.notify_all();
 }
 
 }  // namespace

@@ -74,6 +74,9 @@ def lib():
     L.mpmgpu_sort_by_cell_noalloc.restype = C.c_int
     L.mpmgpu_host_unregister.argtypes = [C.c_void_p]
     L.mpmgpu_host_unregister.restype = C.c_int
+    for f in ("mpmgpu_fp64_fma_rate", "mpmgpu_fp32_fma_rate"):
+        getattr(L, f).argtypes = [C.c_int32, P(C.c_double), P(C.c_double)]
+        getattr(L, f).restype = C.c_int
     VP = C.c_void_p
     batch_sigs = {
         "mpmgpu_batch_bytes": ([P(abi.MpmGpuBatchOptions)], C.c_int64),
@@ -119,7 +122,8 @@ def lib():
 EXPORTED = ("mpmgpu_step_timed", "mpmgpu_autotune_sort", "mpmgpu_archive_record_size", "mpmgpu_archive_records",
             "mpmgpu_archive_records_async", "mpmgpu_archive_wait",
             "mpmgpu_set_profiling", "mpmgpu_stream", "mpmgpu_launch_count",
-            "mpmgpu_host_register", "mpmgpu_host_unregister", "mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
+            "mpmgpu_host_register", "mpmgpu_host_unregister", "mpmgpu_fp64_fma_rate", "mpmgpu_fp32_fma_rate",
+            "mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
             "mpmgpu_set_velocity_bcs", "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles",
             "mpmgpu_last_error", "mpmgpu_destroy", "mpmgpu_profile")
 
@@ -455,6 +459,16 @@ class GpuServer:
             self.close()
         except Exception:
             pass
+
+
+def fma_rate(fp64: bool = True, iters: int = 20000) -> float:
+    """Measured FMA throughput of the current GPU in TFLOP/s (FP64 or FP32)."""
+    tf, ms = C.c_double(), C.c_double()
+    f = lib().mpmgpu_fp64_fma_rate if fp64 else lib().mpmgpu_fp32_fma_rate
+    st = f(int(iters), C.byref(tf), C.byref(ms))
+    if st != 0:
+        raise GpuError(st, lib().mpmgpu_last_error(None).decode())
+    return tf.value
 
 
 def pin(arrays: dict) -> list:

@@ -3,7 +3,8 @@
 Run in a container that has the reference tree and the oracle build:
 
     make -C oracle/ref -j8            # builds oracle/_ref/NairnMPM
-    python tests/golden/make_golden.py
+    python tests/golden/make_golden.py                 # the small cases
+    python tests/golden/make_golden.py --full [name]   # the benchmark configurations at full size
 
 For every case it writes the synthetic XML (nairn_gb300.inputs), runs
 ``NairnMPM -np 1`` (single patch, the reference's deterministic order), reads
@@ -112,6 +113,28 @@ CASES = {
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")
 
+# The benchmark configurations at their full sizes and lengths, each run once
+# by the reference (-np 1) and written to tests/golden/full/<name>.npz.
+# name -> (generator, kwargs, archive interval in steps or None for the final
+# step only, sample size or 0 to keep every particle).  For a sampled case the
+# file holds the records of a seeded sample of particles at every archived
+# step, and for every particle the sum of squares of each quantity and a CRC32
+# of the element column, so a test checks the sample element by element and
+# the whole state through its norms and the element checksum.
+FULL_CASES = {
+    # 100x20 cells of 1 mm, 2x2 particles per cell (8,000), uGIMP, USAVG, 1,000 steps
+    "full_c1_cantilever": ("cantilever_2d", dict(nx=100, ny=20, steps=1000), None, 0),
+    # the 1,004,800-particle Taylor bar: the first 20 steps, and the whole
+    # 2,000-step run archived every 500 steps
+    "full_c2_taylor_20": ("taylor_3d", dict(steps=20), None, 4096),
+    "full_c2_taylor": ("taylor_3d", dict(steps=2000), 500, 4096),
+    # the 4,136,960-particle contact problem (lCPDI, Coulomb 0.3, volume-gradient normals)
+    "full_c3_contact": ("contact_3d", dict(plate=(128, 128, 30), block=(40, 40, 16), block_x0=22.0, block_y0=22.0,
+                                           cell=0.5, v=(4000., 0., -4000.), steps=10, gimp="lCPDI", friction=0.3,
+                                           normals=2), None, 4096),
+}
+FULL_DIR = os.path.join(HERE, "full")
+
 
 def run_case(name, gen, kw, workdir):
     xml, info = getattr(inputs, gen)(archive_root="Results/out.", **kw)
@@ -138,12 +161,70 @@ def run_case(name, gen, kw, workdir):
     return steps, len(a0["mass"])
 
 
+def run_full_case(name, gen, kw, every, sample, workdir):
+    """One benchmark configuration at full size (see FULL_CASES)."""
+    import re
+    import zlib
+    xml, info = getattr(inputs, gen)(archive_root="Results/out.", **kw)
+    if every:
+        # archive every `every` steps: ArchiveData::ArchiveResults writes when
+        # the time reaches the next multiple of the archive time, which sits a
+        # hair below every-th step times so rounding cannot skip one
+        t_ms = every * info["dt"] * 1e3 * (1. - 1e-9)
+        xml = re.sub(r'<ArchiveTime units="ms">[^<]*</ArchiveTime>',
+                     f'<ArchiveTime units="ms">{t_ms!r}</ArchiveTime>', xml)
+    d = os.path.join(workdir, name)
+    os.makedirs(os.path.join(d, "Results"), exist_ok=True)
+    with open(os.path.join(d, "in.xml"), "w") as fh:
+        fh.write(xml)
+    out = subprocess.run([REF, "-np", "1", "in.xml"], cwd=d, capture_output=True, text=True)
+    if out.returncode != 0 or "RUN COMPLETED" not in out.stdout:
+        raise RuntimeError(f"{name}: reference failed\n{out.stdout[-2000:]}\n{out.stderr[-2000:]}")
+    steps = int(out.stdout.split("Calculation Steps:")[1].split()[0])
+    assert steps == kw["steps"], (name, steps)
+    per_step_ms = float(out.stdout.split("Elapsed Time per Step:")[1].split()[0])
+    archived = sorted(int(f.split(".")[-1]) for f in os.listdir(os.path.join(d, "Results"))
+                      if re.fullmatch(r"out\.\d+", f))
+    a0 = read_archive(os.path.join(d, "Results", "out.0"))
+    n = len(a0["mass"])
+    idx = np.sort(np.random.default_rng(2025).choice(n, sample, replace=False)) if sample else np.arange(n)
+    arrays = {"sample": idx.astype(np.int64)}
+    for k in KEEP:
+        if k in a0:
+            arrays["init_" + k] = a0[k][idx]
+    for s in archived[1:]:
+        a = read_archive(os.path.join(d, "Results", f"out.{s}"))
+        for k in KEEP:
+            if k not in a:
+                continue
+            arrays[f"s{s}_{k}"] = a[k][idx]
+            if k != "elem" and a[k].dtype.kind == "f":
+                arrays[f"s{s}_sumsq_{k}"] = np.array(np.sum(a[k].astype(np.float64) ** 2))
+        arrays[f"s{s}_elem_crc32"] = np.array(zlib.crc32(np.ascontiguousarray(a["elem"], dtype="<i4").tobytes()))
+    meta = dict(generator=gen, kwargs=kw, steps=steps, archived=archived[1:], particles=n,
+                sampled=bool(sample), three_d=bool(a0["three_d"]), order=a0["order"],
+                reference_ms_per_step=per_step_ms, reference_threads=1)
+    os.makedirs(FULL_DIR, exist_ok=True)
+    np.savez_compressed(os.path.join(FULL_DIR, name + ".npz"), meta=json.dumps(meta), **arrays)
+    return steps, n, per_step_ms
+
+
 def main():
     if not os.path.exists(REF):
         sys.exit(f"{REF} not built: make -C oracle/ref -j8")
     work = tempfile.mkdtemp(prefix="nairn_golden_")
     try:
         only = sys.argv[1:]
+        full = bool(only) and only[0] == "--full"
+        if full:
+            only = only[1:]
+            for name, (gen, kw, every, sample) in FULL_CASES.items():
+                if only and name not in only:
+                    continue
+                steps, n, ms = run_full_case(name, gen, kw, every, sample, work)
+                print(f"{name}: {n} particles, {steps} steps, reference {ms:.1f} ms/step")
+                shutil.rmtree(os.path.join(work, name), ignore_errors=True)
+            return
         for name, (gen, kw) in CASES.items():
             if only and name not in only:
                 continue
