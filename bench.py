@@ -69,6 +69,7 @@ def parse():
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-mixed", action="store_true", help="skip the mixed-precision window (and its archive leg)")
     ap.add_argument("--window-start", type=int, default=1000,
                     help="step at which the timed window opens (the run is advanced to it untimed)")
     ap.add_argument("--batch-runs", type=int, default=512,
@@ -880,12 +881,21 @@ def main():
 
     # the mixed-precision mode over the same window, with its error against
     # the FP64 path at the same step
-    mrun, mixed, mfinal = window_run(args, m, dist, 1, local)
-    archived = archive_measurement(args, mrun, m, dist) if args.archive_steps > 0 else None
-    mrun.close()
-    mroof, _, mkernels = roofline_of(mixed["prof"], args.steps, mixed["sort_interval"], m, nodes, None)
-    err = state_error(mfinal, final, m.grid.dim)
-    mixed_value = total_particles * args.steps / (dist.max(mixed["ms"]) / 1e3)
+    archived, mixed_line = None, None
+    if not args.no_mixed:
+        mrun, mixed, mfinal = window_run(args, m, dist, 1, local)
+        archived = archive_measurement(args, mrun, m, dist) if args.archive_steps > 0 else None
+        mrun.close()
+        mroof, _, mkernels = roofline_of(mixed["prof"], args.steps, mixed["sort_interval"], m, nodes, None)
+        err = state_error(mfinal, final, m.grid.dim)
+        mixed_value = total_particles * args.steps / (dist.max(mixed["ms"]) / 1e3)
+        mixed_line = {"value": mixed_value, "unit": METRIC, "ms_per_step": dist.max(mixed["ms"]) / args.steps,
+                      "dtype": "mixed: f32 transfers, f64 constitutive", "sort_interval": mixed["sort_interval"],
+                      "speedup_vs_fp64": mixed_value / value, "gpu_launches": mixed["launches"],
+                      "clocks": mixed["clocks"], "roofline": mroof, "kernels": mkernels,
+                      "error_vs_fp64_path": dict(err, steps=head["steps_done"],
+                                                 note="relative L2 against the FP64 GPU path after the same "
+                                                      "steps; that path matches the reference within 1e-10")}
 
     line = {"metric": METRIC, "value": value, "unit": METRIC, "n_gpus": ws, "steps": args.steps,
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
@@ -901,17 +911,11 @@ def main():
             "clocks": head["clocks"],
             "measured_peaks": {"fp64_fma_tflops": fp64_peak, "fp32_fma_tflops": fp32_peak,
                                "ratio_fp32_to_fp64": fp32_peak / fp64_peak},
-            "mixed": {"value": mixed_value, "unit": METRIC, "ms_per_step": dist.max(mixed["ms"]) / args.steps,
-                      "dtype": "mixed: f32 transfers, f64 constitutive", "sort_interval": mixed["sort_interval"],
-                      "speedup_vs_fp64": mixed_value / value, "gpu_launches": mixed["launches"],
-                      "clocks": mixed["clocks"], "roofline": mroof, "kernels": mkernels,
-                      "error_vs_fp64_path": dict(err, steps=head["steps_done"],
-                                                 note="relative L2 against the FP64 GPU path after the same "
-                                                      "steps; that path matches the reference within 1e-10")}}
+            "mixed": mixed_line}
     if archived:
         line["archived"] = archived
     if args.xpic_steps > 0:
-        line["xpic"] = xpic_measurement(args, dist, mixed["sort_interval"], 1)
+        line["xpic"] = xpic_measurement(args, dist, head["sort_interval"], 1)
     if args.config3_steps > 0:
         line["contact3d"] = config3_measurement(args, dist, local)
     if args.contact_runs > 0:

@@ -73,9 +73,14 @@ enum { MPMGPU_PREC_FP64 = 0, MPMGPU_PREC_MIXED = 1 };
  * the last bits of a result -- varies from run to run; or exact integer sums
  * (each contribution rounded once to a multiple of 2^-102 of the step's bound
  * on it, then added as 64-bit integer limbs), which give the same bits in every
- * run whatever the thread scheduling, launch shape or particle order.
- * Single-run contexts only. */
-enum { MPMGPU_P2G_ATOMIC = 0, MPMGPU_P2G_DETERMINISTIC = 1 };
+ * run whatever the thread scheduling, launch shape or particle order
+ * (single-run contexts only).  With MPMGPU_P2G_ATOMIC the mixed mode
+ * accumulates each block's scatters (one material field; linear, uGIMP,
+ * B2SPLINE or B2GIMP shape functions) in a shared-memory node tile of FP32
+ * two-sum pairs and adds every touched node once to the FP64 node columns;
+ * MPMGPU_P2G_UNTILED scatters every (particle, node) pair straight to the
+ * node columns instead. */
+enum { MPMGPU_P2G_ATOMIC = 0, MPMGPU_P2G_DETERMINISTIC = 1, MPMGPU_P2G_UNTILED = 2 };
 /* Material types: Common/Read_XML/MaterialController.cpp:105-231 */
 enum { MPMGPU_MAT_ISOTROPIC = 1, MPMGPU_MAT_ISOPLASTICITY = 9, MPMGPU_MAT_NEOHOOKEAN = 28 };
 

@@ -131,6 +131,23 @@ __global__ void k_gather_cap(const T *__restrict__ src, T *__restrict__ dst, con
     for (int k = 0; k < ncols; k++) dst[(size_t)k * cap + j] = src[(size_t)k * cap + s];
 }
 
+// A new run's node range: clear the velocity and acceleration columns its
+// nodes may keep from an earlier run (a failed one may have left non-finite
+// values); the separable gradient sums read every node of a particle's window,
+// weighting those outside its support by zero.
+__global__ void k_clear_run_nodes(DevNodes nd, long long nbase, long long nn, int nf, int fstride) {
+    const long long j = blockIdx.x * (long long)blockDim.x + threadIdx.x;
+    if (j >= nn) return;
+    for (int f = 0; f < nf; f++) {
+        const long long k = f * (long long)fstride + nbase + j;
+        nd.vx[k] = nd.vy[k] = nd.vz[k] = 0.;
+        nd.ax[k] = nd.ay[k] = nd.az[k] = 0.;
+        nd.vhx[k] = nd.vhy[k] = nd.vhz[k] = 0.f;
+        nd.vlx[k] = nd.vly[k] = nd.vlz[k] = 0.f;
+        nd.bx[k] = nd.by[k] = nd.bz[k] = 0.f;
+    }
+}
+
 // step-start clear of the accumulated node columns of the used node range
 // (every material field, and the contact terms when there are several)
 template <bool MIX>
@@ -388,7 +405,17 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     sp.ct.fstride = b->ncap;
     sp.ct.lr = b->lr_out;
     k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN, b->nf, b->ncap);
-    k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    // mixed mode, one material field, window shape functions: the scatters
+    // accumulate in shared-memory node tiles (each block's runs beyond its
+    // first scatter straight to the node columns)
+    constexpr bool kTileable = MIX && SHAPE != SHAPE_LCPDI;
+    const bool tile = kTileable && b->nf == 1;
+    if constexpr (kTileable) {
+        if (tile) k_p2g_tile<DIM, SHAPE, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
+        else k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    } else {
+        k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    }
     const bool lr = b->lr_runs > 0;
     const int lrb = (int)(((long long)NN * 32 + NTB - 1) / NTB);  // a warp per node
     auto lr_normals = [&]() {
@@ -422,10 +449,22 @@ void batch_enqueue_step(MpmGpuBatch *b) {
         }
     };
     if (xo > 1 && xf && method != MPMGPU_USL) xpic_expand(XPIC_STRAIN);  // FMPM: first strain update
-    if (method == MPMGPU_USL)
-        k_strain_forces<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
-    else
-        k_strain_forces<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    bool forces_done = false;
+    if constexpr (kTileable) {
+        if (tile) {
+            if (method == MPMGPU_USL)
+                k_strain_forces_tile<DIM, SHAPE, false, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+            else
+                k_strain_forces_tile<DIM, SHAPE, true, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+            forces_done = true;
+        }
+    }
+    if (!forces_done) {
+        if (method == MPMGPU_USL)
+            k_strain_forces<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+        else
+            k_strain_forces<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+    }
     if (lr) lr_normals();  // the deformed radii changed with the strain update
     k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group,
                                                     b->nf > 1 && method != MPMGPU_USF);
@@ -433,7 +472,14 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     if (method == MPMGPU_USF) {
         k_g2p<DIM, SHAPE, false, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     } else {
-        k_g2p<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
+        bool g2p_done = false;
+        if constexpr (kTileable) {
+            if (tile) {
+                k_g2p_tile<DIM, SHAPE, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
+                g2p_done = true;
+            }
+        }
+        if (!g2p_done) k_g2p<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
         if (lr) lr_normals();  // the particles moved
         k_node_usl<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group);
         if (xo > 1 && xf) xpic_expand(XPIC_STRAIN);  // FMPM: second strain update
@@ -849,7 +895,8 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     k_batch_admit<<<(np + TB - 1) / TB, TB, 0, s>>>(b->p.mat, b->p.elem, b->orig, b->p.run, start, np, r,
                                                     (int)mbase, nmat, (int)nelems, b->flag);
     k_fill_int<<<(int)((nnodes + TB - 1) / TB), TB, 0, s>>>(b->nrun, nbase, nnodes, r);
-    b->launches += 2;
+    k_clear_run_nodes<<<(int)((nnodes + TB - 1) / TB), TB, 0, s>>>(b->nd, nbase, nnodes, b->nf, b->ncap);
+    b->launches += 3;
     BCK(cudaGetLastError());
     DevRun R{};
     R.g.dim = b->dim;

@@ -199,9 +199,13 @@ struct Win {
     int s;
 };
 
-// T = double in the FP64 path, float in the mixed-precision transfer mode
+// T = double in the FP64 path, float in the mixed-precision transfer mode.
+// inv_size: 1/(4 lp) of the axis (the 3D z axis takes lp.y's, as the
+// reference does); hinv: 1/(2 lp) of the axis, for the 3D gradient, which the
+// reference forms as -xp/(2 lp) -- multiplying by the reciprocal differs from
+// that quotient by rounding only and keeps divisions out of the candidate loop.
 template <typename T, bool kThreeD, bool kGrad>
-__device__ __forceinline__ void gimp_window(T xi, T lp, T inv_size, T idx, Win<T> &w) {
+__device__ __forceinline__ void gimp_window(T xi, T lp, T inv_size, T hinv, T idx, Win<T> &w) {
     const T q1 = T(2) - lp, q2 = T(2) + lp;
     w.s = fabs(xi - T(3)) < q2 ? 1 : 0;
 #pragma unroll
@@ -221,7 +225,7 @@ __device__ __forceinline__ void gimp_window(T xi, T lp, T inv_size, T idx, Win<T
             }
             if (kGrad) {
                 T d;
-                if (xp < lp) d = kThreeD ? -xp / (T(2) * lp) : -xp * inv_size * T(2);
+                if (xp < lp) d = kThreeD ? -xp * hinv : -xp * inv_size * T(2);
                 else if (xp <= q1) d = T(-0.5);
                 else d = -arg;
                 dS = (xi > gk ? d : -d) * idx;

@@ -246,8 +246,9 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
     if (opts->precision != MPMGPU_PREC_FP64 && opts->precision != MPMGPU_PREC_MIXED)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "precision must be MPMGPU_PREC_FP64 or MPMGPU_PREC_MIXED");
-    if (opts->p2g != MPMGPU_P2G_ATOMIC && opts->p2g != MPMGPU_P2G_DETERMINISTIC)
-        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "p2g must be MPMGPU_P2G_ATOMIC or MPMGPU_P2G_DETERMINISTIC");
+    if (opts->p2g != MPMGPU_P2G_ATOMIC && opts->p2g != MPMGPU_P2G_DETERMINISTIC && opts->p2g != MPMGPU_P2G_UNTILED)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED,
+                       "p2g must be MPMGPU_P2G_ATOMIC, MPMGPU_P2G_DETERMINISTIC or MPMGPU_P2G_UNTILED");
     if (!(opts->timestep > 0.)) return set_err(nullptr, MPMGPU_ERR_INVALID, "timestep must be > 0");
     if (opts->xpic_order < 0 || opts->xpic_order > 64 || (opts->xpic_fmpm != 0 && opts->xpic_fmpm != 1) ||
         (opts->xpic_order > 0 && opts->xpic_period < 1))

@@ -13,6 +13,7 @@
 // the two halves, and the grid data both halves read is complete beforehand.
 #pragma once
 
+#include <climits>
 #include <type_traits>
 
 #include "mpm_device.cuh"
@@ -157,9 +158,11 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
     int col, row, zr;
     elem_coords(g, e, col, row, zr);
     const int n0 = nb + zr * g.zplane + row * g.yplane + col;  // first node (global index)
-    const T DX = (T)(g.xn[col + 1] - g.xn[col]);
-    const T DY = (T)(g.yn[row + 1] - g.yn[row]);
-    const T DZ = DIM == 3 ? (T)(g.zn[zr + 1] - g.zn[zr]) : T(1);
+    // reciprocal element sizes, formed once (a gradient times 1/dx differs from
+    // the reference's quotient by rounding only)
+    const T iDX = T(1) / (T)(g.xn[col + 1] - g.xn[col]);
+    const T iDY = T(1) / (T)(g.yn[row + 1] - g.yn[row]);
+    const T iDZ = DIM == 3 ? T(1) / (T)(g.zn[zr + 1] - g.zn[zr]) : T(1);
     const T xi = (T)xi_d, eta = (T)eta_d, zeta = (T)zeta_d;
     if (SHAPE == SHAPE_LINEAR) {
         if (DIM == 2) {
@@ -171,8 +174,8 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
                 const T t1 = T(1) + xs[i] * xi, t2 = T(1) + es[i] * eta;
                 T dx = 0, dy = 0;
                 if (GRAD) {
-                    dx = T(0.5) * xs[i] * t2 / DX;
-                    dy = T(0.5) * es[i] * t1 / DY;
+                    dx = T(0.5) * xs[i] * t2 * iDX;
+                    dy = T(0.5) * es[i] * t1 * iDY;
                 }
                 f(n0 + off[i], T(0.25) * t1 * t2, dx, dy, T(0));
             }
@@ -188,9 +191,9 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
                 const T t1 = T(1) + xs[i] * xi, t2 = T(1) + es[i] * eta, t3 = T(1) + zs[i] * zeta;
                 T dx = 0, dy = 0, dz = 0;
                 if (GRAD) {
-                    dx = T(0.25) * xs[i] * t2 * t3 / DX;
-                    dy = T(0.25) * es[i] * t1 * t3 / DY;
-                    dz = T(0.25) * zs[i] * t1 * t2 / DZ;
+                    dx = T(0.25) * xs[i] * t2 * t3 * iDX;
+                    dy = T(0.25) * es[i] * t1 * t3 * iDY;
+                    dz = T(0.25) * zs[i] * t1 * t2 * iDZ;
                 }
                 f(n0 + off, T(0.125) * t1 * t2 * t3, dx, dy, dz);
             }
@@ -201,8 +204,8 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
     if constexpr (SHAPE == SHAPE_BGIMP) {
         // B2GIMP over its four-node window per axis (see bgimp_window)
         Win4<T> wx, wy;
-        bgimp_window<T, DIM == 3, GRAD>(xi, lpx, GRAD ? T(2) / DX : T(0), xi, wx);
-        bgimp_window<T, DIM == 3, GRAD>(eta, lpy, GRAD ? T(2) / DY : T(0), eta, wy);
+        bgimp_window<T, DIM == 3, GRAD>(xi, lpx, GRAD ? T(2) * iDX : T(0), xi, wx);
+        bgimp_window<T, DIM == 3, GRAD>(eta, lpy, GRAD ? T(2) * iDY : T(0), eta, wy);
         const int base = n0 - 1 - g.yplane;
         if (DIM == 2) {
 #pragma unroll
@@ -213,7 +216,7 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
                       GRAD ? wx.S[jx] * wy.dS[jy] : T(0), T(0));
         } else {
             Win4<T> wz;
-            bgimp_window<T, true, GRAD>(zeta, lpz, GRAD ? T(2) / DZ : T(0), eta, wz);
+            bgimp_window<T, true, GRAD>(zeta, lpz, GRAD ? T(2) * iDZ : T(0), eta, wz);
             const int base3 = base - g.zplane;
 #pragma unroll
             for (int jz = 0; jz < 4; jz++)
@@ -234,11 +237,12 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
     // marking a node outside the support.
     Win<T> wx, wy;
     if constexpr (SHAPE == SHAPE_BSPLINE) {
-        bspline_window<T, GRAD>(xi, GRAD ? T(1) / DX : T(0), wx);
-        bspline_window<T, GRAD>(eta, GRAD ? T(1) / DY : T(0), wy);
+        bspline_window<T, GRAD>(xi, GRAD ? iDX : T(0), wx);
+        bspline_window<T, GRAD>(eta, GRAD ? iDY : T(0), wy);
     } else {
-        gimp_window<T, DIM == 3, GRAD>(xi, lpx, T(1) / (T(4) * lpx), GRAD ? T(2) / DX : T(0), wx);
-        gimp_window<T, DIM == 3, GRAD>(eta, lpy, T(1) / (T(4) * lpy), GRAD ? T(2) / DY : T(0), wy);
+        const T ix = T(1) / (T(4) * lpx), iy = T(1) / (T(4) * lpy);
+        gimp_window<T, DIM == 3, GRAD>(xi, lpx, ix, T(2) * ix, GRAD ? T(2) * iDX : T(0), wx);
+        gimp_window<T, DIM == 3, GRAD>(eta, lpy, iy, T(2) * iy, GRAD ? T(2) * iDY : T(0), wy);
     }
     const int base = n0 + (wx.s - 1) + (wy.s - 1) * g.yplane;
     if (DIM == 2) {
@@ -257,8 +261,15 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
         }
     } else {
         Win<T> wz;
-        if constexpr (SHAPE == SHAPE_BSPLINE) bspline_window<T, GRAD>(zeta, GRAD ? T(1) / DZ : T(0), wz);
-        else gimp_window<T, true, GRAD>(zeta, lpz, T(1) / (T(4) * lpy), GRAD ? T(2) / DZ : T(0), wz);
+        if constexpr (SHAPE == SHAPE_BSPLINE) {
+            bspline_window<T, GRAD>(zeta, GRAD ? iDZ : T(0), wz);
+        } else {
+            // the z factor is sized by lp.y (EightNodeIsoparamBrick.cpp:289-403); its
+            // gradient by lp.z
+            const T iy = T(1) / (T(4) * lpy);
+            const T hz = !GRAD ? T(0) : (lpz == lpy ? T(2) * iy : T(1) / (T(2) * lpz));
+            gimp_window<T, true, GRAD>(zeta, lpz, iy, hz, GRAD ? T(2) * iDZ : T(0), wz);
+        }
         const int base3 = base + (wz.s - 1) * g.zplane;
 #pragma unroll
         for (int jz = 0; jz < 3; jz++) {
@@ -760,6 +771,332 @@ struct Wt<true> {
     using T = float;
 };
 
+// ---------------------------------------------------------------------------
+// Per-axis node windows.  For the shape functions whose nodes form a box
+// around the element -- linear (2 per axis), uGIMP and B2SPLINE (3), B2GIMP
+// (4) -- the weight of node (jx, jy, jz) of the window is the product of one
+// factor per axis, as in for_each_node; AxisWin holds those factors, their
+// gradient factors and the window's first node column, row and layer.
+// ---------------------------------------------------------------------------
+template <int SHAPE>
+constexpr int kWinNodes = SHAPE == SHAPE_LINEAR ? 2 : (SHAPE == SHAPE_BGIMP ? 4 : 3);
+// node offsets of a window relative to the element's first node: lowest, highest
+template <int SHAPE>
+constexpr int kWinLo = SHAPE == SHAPE_LINEAR ? 0 : -1;
+template <int SHAPE>
+constexpr int kWinHi = SHAPE == SHAPE_LINEAR ? 1 : 2;
+
+template <int SHAPE, typename T>
+struct AxisWin {
+    T S[3][kWinNodes<SHAPE>], dS[3][kWinNodes<SHAPE>];
+    int c[3];  // node column, row and layer of the window's first node
+};
+
+// The factors of for_each_node for element (col, row, zr) and natural
+// coordinates xi, eta, zeta (the reference's candidate tests and the 3D
+// uGIMP z factor sized by lp.y included).
+template <int DIM, int SHAPE, bool GRAD, typename T>
+__device__ __forceinline__ void axis_windows(const DevGrid &g, int col, int row, int zr, double xi_d, double eta_d,
+                                             double zeta_d, double lpx_d, double lpy_d, double lpz_d,
+                                             AxisWin<SHAPE, T> &w) {
+    static_assert(SHAPE != SHAPE_LCPDI, "lCPDI nodes do not form a window");
+    const T xi = (T)xi_d, eta = (T)eta_d, zeta = (T)zeta_d;
+    const T iD[3] = {T(1) / (T)(g.xn[col + 1] - g.xn[col]), T(1) / (T)(g.yn[row + 1] - g.yn[row]),
+                     DIM == 3 ? T(1) / (T)(g.zn[zr + 1] - g.zn[zr]) : T(1)};
+    const int cc[3] = {col, row, zr};
+    const T nat[3] = {xi, eta, zeta};
+    w.c[2] = 0;
+    if constexpr (SHAPE == SHAPE_LINEAR) {
+        // FourNodeIsoparam / EightNodeIsoparamBrick::ShapeFunction: (1 -/+ xi)/2 per axis
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            w.S[a][0] = T(0.5) * (T(1) - nat[a]);
+            w.S[a][1] = T(0.5) * (T(1) + nat[a]);
+            w.dS[a][0] = GRAD ? -iD[a] : T(0);
+            w.dS[a][1] = GRAD ? iD[a] : T(0);
+            w.c[a] = cc[a];
+        }
+    } else if constexpr (SHAPE == SHAPE_BGIMP) {
+        const T lp[3] = {(T)lpx_d, (T)lpy_d, (T)lpz_d};
+        const T sgn[3] = {xi, eta, eta};  // the reference's 3D z gradient compares y
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            Win4<T> q;
+            bgimp_window<T, DIM == 3, GRAD>(nat[a], lp[a], GRAD ? T(2) * iD[a] : T(0), sgn[a], q);
+#pragma unroll
+            for (int j = 0; j < 4; j++) {
+                w.S[a][j] = q.S[j];
+                w.dS[a][j] = q.dS[j];
+            }
+            w.c[a] = cc[a] - 1;
+        }
+    } else {
+        const T lp[3] = {(T)lpx_d, (T)lpy_d, (T)lpz_d};
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            Win<T> q;
+            if constexpr (SHAPE == SHAPE_BSPLINE) {
+                bspline_window<T, GRAD>(nat[a], GRAD ? iD[a] : T(0), q);
+            } else {
+                // uGIMP: the 3D z factor is sized by lp.y (EightNodeIsoparamBrick.cpp:289-403),
+                // its gradient by lp.z
+                const T inv = T(1) / (T(4) * (a == 2 ? lp[1] : lp[a]));
+                const T hinv = !GRAD ? T(0) : (a < 2 || lp[2] == lp[1] ? T(2) * inv : T(1) / (T(2) * lp[2]));
+                gimp_window<T, DIM == 3, GRAD>(nat[a], lp[a], inv, hinv, GRAD ? T(2) * iD[a] : T(0), q);
+            }
+#pragma unroll
+            for (int j = 0; j < 3; j++) {
+                w.S[a][j] = q.S[j];
+                w.dS[a][j] = q.dS[j];
+            }
+            w.c[a] = cc[a] + q.s - 1;
+        }
+    }
+}
+
+// Calls f(jx, jy, jz, N, dNx, dNy, dNz) for every node of the windows, with the
+// products for_each_node forms (2D: jz = 0 and dNz = 0).
+template <int DIM, int SHAPE, bool GRAD, typename T, class F>
+__device__ __forceinline__ void for_each_window_node(const AxisWin<SHAPE, T> &w, F &&f) {
+    constexpr int K = kWinNodes<SHAPE>;
+#pragma unroll
+    for (int jz = 0; jz < (DIM == 3 ? K : 1); jz++)
+#pragma unroll
+        for (int jy = 0; jy < K; jy++) {
+            const T Syz = DIM == 3 ? w.S[1][jy] * w.S[2][jz] : w.S[1][jy];
+            const T dySz = GRAD ? (DIM == 3 ? w.dS[1][jy] * w.S[2][jz] : w.dS[1][jy]) : T(0);
+            const T SydZ = GRAD && DIM == 3 ? w.S[1][jy] * w.dS[2][jz] : T(0);
+#pragma unroll
+            for (int jx = 0; jx < K; jx++) {
+                const T Sx = w.S[0][jx];
+                f(jx, jy, jz, Sx * Syz, GRAD ? w.dS[0][jx] * Syz : T(0), GRAD ? Sx * dySz : T(0),
+                  GRAD ? Sx * SydZ : T(0));
+            }
+        }
+}
+
+// Separable gradient sums over a window.  With N = X(jx) Y(jy) Z(jz), the
+// velocity gradient sum_nodes v_a dN/dx_b and the internal force
+// -mp (sigma - P I) . grad N factor axis by axis: contracting x first, then y,
+// then z takes about 270 multiply-adds in 3D instead of the ~380 of forming
+// every node's weight and gradient (and the per-node zero tests), which is
+// what bounds these kernels on the FP64 pipe.  The sums equal the node-by-node
+// ones up to rounding.
+//
+// out[a*3+b] = sum over window nodes of val_a(node) * dN(node)/dx_b, where
+// val(node, v) loads the node's vector (node = global index).
+template <int DIM, int SHAPE, typename T, class V>
+__device__ __forceinline__ void window_grad_gather(const AxisWin<SHAPE, T> &w, int n0, int yplane, int zplane,
+                                                   V &&val, T out[9]) {
+    constexpr int K = kWinNodes<SHAPE>;
+#pragma unroll
+    for (int k = 0; k < 9; k++) out[k] = T(0);
+#pragma unroll
+    for (int jz = 0; jz < (DIM == 3 ? K : 1); jz++) {
+        T C[3] = {0, 0, 0}, D[3] = {0, 0, 0}, E[3] = {0, 0, 0};  // sum_y Y A, sum_y Y' A, sum_y Y B
+#pragma unroll
+        for (int jy = 0; jy < K; jy++) {
+            T A[3] = {0, 0, 0}, B[3] = {0, 0, 0};  // sum_x X v, sum_x X' v
+#pragma unroll
+            for (int jx = 0; jx < K; jx++) {
+                T v[3];
+                val(n0 + jx + jy * yplane + jz * zplane, v);
+#pragma unroll
+                for (int a = 0; a < DIM; a++) {
+                    A[a] += w.S[0][jx] * v[a];
+                    B[a] += w.dS[0][jx] * v[a];
+                }
+            }
+#pragma unroll
+            for (int a = 0; a < DIM; a++) {
+                C[a] += w.S[1][jy] * A[a];
+                D[a] += w.dS[1][jy] * A[a];
+                E[a] += w.S[1][jy] * B[a];
+            }
+        }
+#pragma unroll
+        for (int a = 0; a < DIM; a++) {
+            if (DIM == 3) {
+                out[a * 3 + 0] += w.S[2][jz] * E[a];
+                out[a * 3 + 1] += w.S[2][jz] * D[a];
+                out[a * 3 + 2] += w.dS[2][jz] * C[a];
+            } else {
+                out[a * 3 + 0] = E[a];
+                out[a * 3 + 1] = D[a];
+            }
+        }
+    }
+}
+
+// add(jx, jy, jz, f) for every window node with a non-zero weight, f_a =
+// sum_b s[a][b] dN/dx_b for the symmetric tensor s (the prescaled stress).
+template <int DIM, int SHAPE, typename T, class F>
+__device__ __forceinline__ void window_grad_scatter(const AxisWin<SHAPE, T> &w, const T s[3][3], F &&add) {
+    constexpr int K = kWinNodes<SHAPE>;
+#pragma unroll
+    for (int jz = 0; jz < (DIM == 3 ? K : 1); jz++)
+#pragma unroll
+        for (int jy = 0; jy < K; jy++) {
+            const T P = DIM == 3 ? w.S[1][jy] * w.S[2][jz] : w.S[1][jy];   // Y Z
+            const T Q = DIM == 3 ? w.dS[1][jy] * w.S[2][jz] : w.dS[1][jy]; // Y' Z
+            const T R = DIM == 3 ? w.S[1][jy] * w.dS[2][jz] : T(0);        // Y Z'
+            if (P == T(0)) continue;  // the row is outside the support
+            T wx[3], u[3];
+#pragma unroll
+            for (int a = 0; a < DIM; a++) {
+                wx[a] = s[a][0] * P;
+                u[a] = DIM == 3 ? s[a][1] * Q + s[a][2] * R : s[a][1] * Q;
+            }
+#pragma unroll
+            for (int jx = 0; jx < K; jx++) {
+                if (w.S[0][jx] == T(0)) continue;
+                T f[3] = {0, 0, 0};
+#pragma unroll
+                for (int a = 0; a < DIM; a++) f[a] = w.dS[0][jx] * wx[a] + w.S[0][jx] * u[a];
+                add(jx, jy, jz, f);
+            }
+        }
+}
+
+// ---------------------------------------------------------------------------
+// Shared-memory node tiles (mixed-precision scatters).  A block's particles
+// are consecutive slots, which the cell sort keeps in cell order, so their
+// windows cover a small box of grid nodes.  The block accumulates its
+// contributions there in shared memory -- each quantity as an FP32 two-sum
+// pair (hi, lo): every add returns the old hi, and the rounding error of that
+// exact addition goes into lo, so a node's tile sum carries ~2^-48 of its
+// terms' magnitude -- and then adds each touched node's sum once to the FP64
+// node columns.  Momentum is accumulated relative to a reference velocity of
+// the block (that of its first particle), so the bulk motion is added back in
+// FP64 at the flush and the FP32 sums only carry velocity differences.
+// Particles of another run (batches) or blocks whose box exceeds the tile
+// scatter straight to the node columns.
+// ---------------------------------------------------------------------------
+constexpr int kTileCap = 1280;  // nodes of one block's tile (42 KB of shared memory)
+constexpr int kTileQ = 4;       // quantities per node
+
+struct TileBox {
+    int run, first;        // the tile's run; lowest thread index of its particles
+    int lo[3], hi[3];      // element column, row and layer range of those particles
+    int x0, y0, z0;        // node column, row and layer of the box's first node
+    int bx, by, bz;        // box extent in nodes
+    int nb, yplane, zplane;  // the run's node base and strides
+    int on;                // the box fits the tile
+};
+
+struct NodeTile {
+    TileBox box;
+    double ref[3];                 // reference velocity
+    float hi[kTileQ][kTileCap];
+    float lo[kTileQ][kTileCap];
+    unsigned char touched[kTileCap];
+};
+
+// Every thread of the block calls this (it synchronises).  valid: the thread
+// has a particle; run, col, row, zr: its run and element coordinates; ref:
+// its velocity (the first tiled particle's becomes the tile's reference).
+// Returns whether the thread's particle accumulates into the tile, which is
+// cleared for nq quantities.
+template <int DIM, int SHAPE>
+__device__ __forceinline__ bool tile_open(NodeTile &t, bool valid, int run, int col, int row, int zr,
+                                          const RunView &rv, const double ref[3], int nq) {
+    TileBox &b = t.box;
+    if (threadIdx.x == 0) {
+        b.run = b.first = INT_MAX;
+        b.lo[0] = b.lo[1] = b.lo[2] = INT_MAX;
+        b.hi[0] = b.hi[1] = b.hi[2] = INT_MIN;
+        b.on = 0;
+    }
+    __syncthreads();
+    if (valid) atomicMin(&b.run, run);
+    __syncthreads();
+    const bool mine = valid && run == b.run;
+    if (mine) {
+        atomicMin(&b.first, (int)threadIdx.x);
+        atomicMin(&b.lo[0], col);
+        atomicMax(&b.hi[0], col);
+        atomicMin(&b.lo[1], row);
+        atomicMax(&b.hi[1], row);
+        if (DIM == 3) {
+            atomicMin(&b.lo[2], zr);
+            atomicMax(&b.hi[2], zr);
+        }
+    }
+    __syncthreads();
+    if (mine && (int)threadIdx.x == b.first) {
+        constexpr int lo = kWinLo<SHAPE>, span = kWinHi<SHAPE> - kWinLo<SHAPE> + 1;
+        b.x0 = b.lo[0] + lo;
+        b.bx = b.hi[0] - b.lo[0] + span;
+        b.y0 = b.lo[1] + lo;
+        b.by = b.hi[1] - b.lo[1] + span;
+        if (DIM == 3) {
+            b.z0 = b.lo[2] + lo;
+            b.bz = b.hi[2] - b.lo[2] + span;
+        } else {
+            b.z0 = 0;
+            b.bz = 1;
+        }
+        b.nb = rv.nb;
+        b.yplane = rv.g.yplane;
+        b.zplane = rv.g.zplane;
+        b.on = (long long)b.bx * b.by * b.bz <= kTileCap ? 1 : 0;
+        t.ref[0] = ref[0];
+        t.ref[1] = ref[1];
+        t.ref[2] = ref[2];
+    }
+    __syncthreads();
+    if (b.on) {
+        const int total = b.bx * b.by * b.bz;
+        for (int k = threadIdx.x; k < total; k += blockDim.x) {
+            for (int q = 0; q < nq; q++) t.hi[q][k] = t.lo[q][k] = 0.f;
+            t.touched[k] = 0;
+        }
+    }
+    __syncthreads();
+    return mine && b.on;
+}
+
+// tile slot of window node (jx, jy, jz) of a window starting at c
+__device__ __forceinline__ int tile_slot(const TileBox &b, const int c[3], int jx, int jy, int jz) {
+    return (c[0] + jx - b.x0) + b.bx * ((c[1] + jy - b.y0) + b.by * (c[2] + jz - b.z0));
+}
+
+// two-sum accumulation of v into quantity q of slot k
+__device__ __forceinline__ void tile_add(NodeTile &t, int q, int k, float v) {
+    const float old = atomicAdd(&t.hi[q][k], v);
+    const float s = old + v;
+    const float bp = s - old;
+    atomicAdd(&t.lo[q][k], (old - (s - bp)) + (v - bp));
+}
+
+__device__ __forceinline__ double tile_sum(const NodeTile &t, int q, int k) {
+    return (double)t.hi[q][k] + (double)t.lo[q][k];
+}
+
+// Particle slot of this thread in a tiled kernel: lane l of warp w of the
+// block takes slot l * (warps per block) + w of the block's range.  The block
+// still covers consecutive slots, but the lanes of one warp hold particles of
+// different cells (sorted particles of one cell are neighbours), so the
+// lanes' shared-memory adds go to different nodes instead of queueing on the
+// same address.
+__device__ __forceinline__ int tile_particle() {
+    return blockIdx.x * blockDim.x + (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
+}
+
+// Calls f(node, slot) for every touched slot of the tile (after a
+// __syncthreads that ends the accumulation); node is the global node index.
+template <class F>
+__device__ __forceinline__ void tile_flush(const NodeTile &t, F &&f) {
+    const TileBox &b = t.box;
+    if (!b.on) return;
+    const int total = b.bx * b.by * b.bz;
+    for (int k = threadIdx.x; k < total; k += blockDim.x) {
+        if (!t.touched[k]) continue;
+        const int kx = k % b.bx, r = k / b.bx, ky = r % b.by, kz = r / b.by;
+        f(b.nb + (b.x0 + kx) + b.yplane * (b.y0 + ky) + b.zplane * (b.z0 + kz), k);
+    }
+}
+
 // node-index offset of the particle's material velocity field
 __device__ __forceinline__ int field_offset(const StepParams &sp, const DevMat *mats, const DevParticles &p, int i) {
     return sp.ct.nf > 1 ? mats[p.mat[i]].field * sp.ct.fstride : 0;
@@ -994,6 +1331,79 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_p2
     }
 }
 
+// k_p2g of the mixed mode through a shared-memory node tile (single material
+// field; linear, uGIMP, B2SPLINE and B2GIMP windows): FP32 weights and
+// products, accumulated per block as two-sum pairs of mass and of mass times
+// the velocity's difference from the block's reference velocity, added once
+// per touched node to the FP64 mass and momentum columns.
+template <int DIM, int SHAPE, bool BATCH>
+static __global__ void __launch_bounds__(256) k_p2g_tile(StepParams sp, DevParticles p, DevNodes nd) {
+    __shared__ NodeTile t;
+    const int i = tile_particle();
+    RunView rv;
+    const bool valid = i < p.n && particle_run<BATCH>(sp, p, i, rv);
+    int col = 0, row = 0, zr = 0;
+    double xi = 0., eta = 0., zeta = 0., mp = 0., v[3] = {0., 0., 0.};
+    if (valid) {
+        const int e = p.elem[i];
+        elem_coords(rv.g, e, col, row, zr);
+        // natural coordinates in FP32 from the offset to the element's first
+        // node (an FP64 difference): the mixed-mode kernels take them as floats
+        const DevGrid &g = rv.g;
+        xi = (double)(2.f * (float)(p.x[i] - g.xn[col]) * (float)g.igx - 1.f);
+        eta = (double)(2.f * (float)(p.y[i] - g.yn[row]) * (float)g.igy - 1.f);
+        if (DIM == 3) zeta = (double)(2.f * (float)(p.z[i] - g.zn[zr]) * (float)g.igz - 1.f);
+        p.xi[i] = xi;
+        p.eta[i] = eta;
+        if (DIM == 3) p.zeta[i] = zeta;
+        mp = p.mass[i];
+        v[0] = p.vx[i];
+        v[1] = p.vy[i];
+        if (DIM == 3) v[2] = p.vz[i];
+    }
+    const bool tiled = tile_open<DIM, SHAPE>(t, valid, BATCH && valid ? p.run[i] : 0, col, row, zr, rv, v, DIM + 1);
+    if (valid) {
+        AxisWin<SHAPE, float> w;
+        axis_windows<DIM, SHAPE, false, float>(rv.g, col, row, zr, xi, eta, zeta, p.lpx[i], p.lpy[i],
+                                               DIM == 3 ? p.lpz[i] : 1., w);
+        if (tiled) {
+            const float mpf = (float)mp;
+            const float d[3] = {(float)(v[0] - t.ref[0]), (float)(v[1] - t.ref[1]), (float)(v[2] - t.ref[2])};
+            for_each_window_node<DIM, SHAPE, false, float>(w, [&](int jx, int jy, int jz, float N, float, float, float) {
+                if (N == 0.f) return;
+                const int k = tile_slot(t.box, w.c, jx, jy, jz);
+                const float wm = N * mpf;
+                tile_add(t, 0, k, wm);
+#pragma unroll
+                for (int a = 0; a < DIM; a++) tile_add(t, 1 + a, k, wm * d[a]);
+                t.touched[k] = 1;
+            });
+        } else {
+            // outside the tile: straight to the node columns, as k_p2g
+            const DevGrid &g = rv.g;
+            for_each_window_node<DIM, SHAPE, false, float>(w, [&](int jx, int jy, int jz, float N, float, float, float) {
+                if (N == 0.f) return;
+                const int n = rv.nb + (w.c[0] + jx) + g.yplane * (w.c[1] + jy) + g.zplane * (w.c[2] + jz);
+                const double fnmp = (double)N * mp;
+                atomicAdd(&nd.mass[n], fnmp);
+                atomicAdd(&nd.px[n], v[0] * fnmp);
+                atomicAdd(&nd.py[n], v[1] * fnmp);
+                if (DIM == 3) atomicAdd(&nd.pz[n], v[2] * fnmp);
+                nd.active[n] = 1;
+            });
+        }
+    }
+    __syncthreads();
+    tile_flush(t, [&](int n, int k) {
+        const double m = tile_sum(t, 0, k);
+        atomicAdd(&nd.mass[n], m);
+        atomicAdd(&nd.px[n], t.ref[0] * m + tile_sum(t, 1, k));
+        atomicAdd(&nd.py[n], t.ref[1] * m + tile_sum(t, 2, k));
+        if (DIM == 3) atomicAdd(&nd.pz[n], t.ref[2] * m + tile_sum(t, 3, k));
+        nd.active[n] = 1;
+    });
+}
+
 template <int DIM>
 __device__ __forceinline__ void constitutive(const DevMat *mats, const DevParticles &p, int i, const double du[9]) {
     const DevMat &m = mats[p.mat[i]];
@@ -1027,6 +1437,29 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, cons
         split2(p.vx[i], ph[0], pl[0]);
         split2(p.vy[i], ph[1], pl[1]);
         if (DIM == 3) split2(p.vz[i], ph[2], pl[2]);
+    }
+    if constexpr (SHAPE != SHAPE_LCPDI) {
+        // window shape functions: the separable sum (window_grad_gather)
+        int col, row, zr;
+        elem_coords(g, p.elem[i], col, row, zr);
+        AxisWin<SHAPE, T> w;
+        axis_windows<DIM, SHAPE, true, T>(g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
+                                          p.lpy[i], DIM == 3 ? p.lpz[i] : 1., w);
+        const int n0 = nb + off + w.c[0] + g.yplane * w.c[1] + g.zplane * w.c[2];
+        window_grad_gather<DIM, SHAPE, T>(w, n0, g.yplane, g.zplane, [&](int n, T v[3]) {
+            if (MIX) {
+                v[0] = (T)((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0]));
+                v[1] = (T)((nd.vhy[n] - ph[1]) + (nd.vly[n] - pl[1]));
+                v[2] = DIM == 3 ? (T)((nd.vhz[n] - ph[2]) + (nd.vlz[n] - pl[2])) : T(0);
+            } else {
+                v[0] = (T)nd.vx[n];
+                v[1] = (T)nd.vy[n];
+                v[2] = DIM == 3 ? (T)nd.vz[n] : T(0);
+            }
+        }, d);
+#pragma unroll
+        for (int k = 0; k < 9; k++) du[k] = (double)d[k] * st;
+        return;
     }
     visit_nodes<DIM, SHAPE, true, T>(g, nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
@@ -1071,6 +1504,33 @@ __device__ __forceinline__ void forces_scatter(const StepParams &sp, const DevPa
     const T sxx = (T)(-mp * (p.sxx[i] - P)), syy = (T)(-mp * (p.syy[i] - P)), sxy = (T)(-mp * p.sxy[i]);
     const T szz = DIM == 3 ? (T)(-mp * (p.szz[i] - P)) : T(0), sxz = DIM == 3 ? (T)(-mp * p.sxz[i]) : T(0),
             syz = DIM == 3 ? (T)(-mp * p.syz[i]) : T(0);
+    if constexpr (SHAPE != SHAPE_LCPDI) {
+        // window shape functions: the separable products (window_grad_scatter)
+        int col, row, zr;
+        elem_coords(g, p.elem[i], col, row, zr);
+        AxisWin<SHAPE, T> w;
+        axis_windows<DIM, SHAPE, true, T>(g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
+                                          p.lpy[i], DIM == 3 ? p.lpz[i] : 1., w);
+        const T sg[3][3] = {{sxx, sxy, sxz}, {sxy, syy, syz}, {sxz, syz, szz}};
+        const int n0 = nb + off + w.c[0] + g.yplane * w.c[1] + g.zplane * w.c[2];
+        window_grad_scatter<DIM, SHAPE, T>(w, sg, [&](int jx, int jy, int jz, const T f[3]) {
+            const int n = n0 + jx + jy * g.yplane + jz * g.zplane;
+            if constexpr (DET) {
+                det_add(sp.det, DQ_FX, n, (double)f[0], sF, sp.err);
+                det_add(sp.det, DQ_FY, n, (double)f[1], sF, sp.err);
+                if (DIM == 3) det_add(sp.det, DQ_FZ, n, (double)f[2], sF, sp.err);
+            } else if (MIX) {
+                atomicAdd(&nd.gx[n], (float)f[0]);
+                atomicAdd(&nd.gy[n], (float)f[1]);
+                if (DIM == 3) atomicAdd(&nd.gz[n], (float)f[2]);
+            } else {
+                atomicAdd(&nd.fx[n], (double)f[0]);
+                atomicAdd(&nd.fy[n], (double)f[1]);
+                if (DIM == 3) atomicAdd(&nd.fz[n], (double)f[2]);
+            }
+        });
+        return;
+    }
     visit_nodes<DIM, SHAPE, true, T>(g, nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
                                            if (N == T(0)) return;
                                            n += off;
@@ -1130,6 +1590,63 @@ static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_for
         return;
     }
     forces_scatter<DIM, SHAPE, MIX, false>(sp, p, nd, i, g, rv.nb, off);
+}
+
+// k_strain_forces of the mixed mode through a shared-memory node tile (single
+// material field, window shape functions): the strain and constitutive
+// update, then the FP32 internal-force products accumulated per block as
+// two-sum pairs and added once per touched node to the FP64 force columns
+// (particles outside the tile add to the FP32 columns, which the momentum
+// update adds to the FP64 ones).
+template <int DIM, int SHAPE, bool STRAIN, bool BATCH>
+static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_forces_tile(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+    __shared__ NodeTile t;
+    const int i = tile_particle();
+    RunView rv;
+    const bool valid = i < p.n && particle_run<BATCH>(sp, p, i, rv);
+    int col = 0, row = 0, zr = 0;
+    if (valid) {
+        if (STRAIN) {
+            double du[9];
+            velocity_gradient<DIM, SHAPE, true>(rv.g, rv.nb, p, nd, i, rv.st_first, du, 0);
+            constitutive<DIM>(mats, p, i, du);
+        }
+        elem_coords(rv.g, p.elem[i], col, row, zr);
+    }
+    const double zero[3] = {0., 0., 0.};
+    const bool tiled = tile_open<DIM, SHAPE>(t, valid, BATCH && valid ? p.run[i] : 0, col, row, zr, rv, zero, DIM);
+    if (valid) {
+        // -mp * (sigma - P I): the internal force of GetFintPlusFext, scaled once
+        const double mp = p.mass[i], P = p.pressure[i];
+        const float sxx = (float)(-mp * (p.sxx[i] - P)), syy = (float)(-mp * (p.syy[i] - P)),
+                    sxy = (float)(-mp * p.sxy[i]);
+        const float szz = DIM == 3 ? (float)(-mp * (p.szz[i] - P)) : 0.f, sxz = DIM == 3 ? (float)(-mp * p.sxz[i]) : 0.f,
+                    syz = DIM == 3 ? (float)(-mp * p.syz[i]) : 0.f;
+        AxisWin<SHAPE, float> w;
+        axis_windows<DIM, SHAPE, true, float>(rv.g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0.,
+                                              p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1., w);
+        const DevGrid &g = rv.g;
+        const float sg[3][3] = {{sxx, sxy, sxz}, {sxy, syy, syz}, {sxz, syz, szz}};
+        window_grad_scatter<DIM, SHAPE, float>(w, sg, [&](int jx, int jy, int jz, const float f[3]) {
+            if (tiled) {
+                const int k = tile_slot(t.box, w.c, jx, jy, jz);
+#pragma unroll
+                for (int a = 0; a < DIM; a++) tile_add(t, a, k, f[a]);
+                t.touched[k] = 1;
+            } else {
+                const int n = rv.nb + (w.c[0] + jx) + g.yplane * (w.c[1] + jy) + g.zplane * (w.c[2] + jz);
+                atomicAdd(&nd.gx[n], f[0]);
+                atomicAdd(&nd.gy[n], f[1]);
+                if (DIM == 3) atomicAdd(&nd.gz[n], f[2]);
+            }
+        });
+    }
+    __syncthreads();
+    tile_flush(t, [&](int n, int k) {
+        atomicAdd(&nd.fx[n], tile_sum(t, 0, k));
+        atomicAdd(&nd.fy[n], tile_sum(t, 1, k));
+        if (DIM == 3) atomicAdd(&nd.fz[n], tile_sum(t, 2, k));
+    });
 }
 
 // Deterministic mode: the internal-force scatter of k_strain_forces as its own
@@ -1197,35 +1714,32 @@ __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticl
     p.elem[i] = num - 1;
 }
 
-// UpdateParticlesTask::Execute, MatVelocityField::IncrementNodalVelAcc and
-// the FLIP branch of MatPoint2D/3D::MoveParticle without damping
-// (UpdateParticlesTask.cpp:75-178, MatVelocityField.cpp:410-426,
-// MatPoint2D.cpp:99-196), fused with the momentum re-extrapolation of
-// UpdateStrainsLastContactTask (UpdateStrainsLastContactTask.cpp:71-146,
-// NodalPoint::AddMassMomentumLast NodalPointMPM.cpp:470-486), which uses the
-// same natural coordinates of the step.  Mixed mode: S v is formed as
+// The particle update of particle i: UpdateParticlesTask::Execute,
+// MatVelocityField::IncrementNodalVelAcc and MatPoint2D/3D::MoveParticle
+// without damping (UpdateParticlesTask.cpp:75-178, MatVelocityField.cpp:410-426,
+// MatPoint2D.cpp:99-196) -- FLIP, or the XPIC/FMPM form of the step.  Gathers
+// S v and S a from the nodes, moves the particle and writes its velocity and
+// position; returns them in v and xp.  Mixed mode: S v is formed as
 // v_particle + sum N (v_node - v_particle) (the weights sum to one) with the
 // differences from FP32 pairs, S a in FP32; the update itself is FP64.
-template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH, bool DET = false>
-static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+template <int DIM, int SHAPE, bool MIX, bool BATCH>
+__device__ __forceinline__ void g2p_move(const StepParams &sp, const DevParticles &p, const DevNodes &nd, int i,
+                                         const RunView &rv, int off, double v[3], double xp[3]) {
     using T = typename Wt<MIX>::T;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
-    RunView rv;
-    if (!particle_run<BATCH>(sp, p, i, rv)) return;
     const DevGrid &g = rv.g;
     const double dt = rv.dt;
     T Sv[3] = {0, 0, 0}, Sa[3] = {0, 0, 0};
     const int e = p.elem[i];
     const double xi = p.xi[i], eta = p.eta[i], zeta = DIM == 3 ? p.zeta[i] : 0.;
     const double lx = p.lpx[i], ly = p.lpy[i], lz = DIM == 3 ? p.lpz[i] : 1.;
-    double v[3] = {p.vx[i], p.vy[i], DIM == 3 ? p.vz[i] : 0.};
+    v[0] = p.vx[i];
+    v[1] = p.vy[i];
+    v[2] = DIM == 3 ? p.vz[i] : 0.;
     float ph[3] = {0.f, 0.f, 0.f}, pl[3] = {0.f, 0.f, 0.f};
     if (MIX) {
 #pragma unroll
         for (int a = 0; a < DIM; a++) split2(v[a], ph[a], pl[a]);
     }
-    const int off = field_offset(sp, mats, p, i);
     // the particle's nodes for this step (CPDI corners or the element window)
     auto visit = [&](auto &&fn) {
         if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
@@ -1250,7 +1764,9 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
             if (DIM == 3) Sa[2] += nd.az[n] * N;
         }
     });
-    double xp[3] = {p.x[i], p.y[i], DIM == 3 ? p.z[i] : 0.};
+    xp[0] = p.x[i];
+    xp[1] = p.y[i];
+    xp[2] = DIM == 3 ? p.z[i] : 0.;
     const int xmode = BATCH ? sp.runs[p.run[i]].xpic : sp.xpic;
     if (xmode == 0) {
         // FLIP (MatPoint2D/3D::MoveParticle, m == 0)
@@ -1283,6 +1799,31 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
         p.vz[i] = v[2];
         p.z[i] = xp[2];
     }
+}
+
+// g2p_move fused with the momentum re-extrapolation of
+// UpdateStrainsLastContactTask (UpdateStrainsLastContactTask.cpp:71-146,
+// NodalPoint::AddMassMomentumLast NodalPointMPM.cpp:470-486), which uses the
+// same natural coordinates of the step (USL), or with the element reset.
+template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH, bool DET = false>
+static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+    using T = typename Wt<MIX>::T;
+    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    if (i >= p.n) return;
+    RunView rv;
+    if (!particle_run<BATCH>(sp, p, i, rv)) return;
+    const DevGrid &g = rv.g;
+    const int e = p.elem[i];
+    const double xi = p.xi[i], eta = p.eta[i], zeta = DIM == 3 ? p.zeta[i] : 0.;
+    const double lx = p.lpx[i], ly = p.lpy[i], lz = DIM == 3 ? p.lpz[i] : 1.;
+    const int off = field_offset(sp, mats, p, i);
+    // the particle's nodes for this step (CPDI corners or the element window)
+    auto visit = [&](auto &&fn) {
+        if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
+        else for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, fn);
+    };
+    double v[3], xp[3];
+    g2p_move<DIM, SHAPE, MIX, BATCH>(sp, p, nd, i, rv, off, v, xp);
     if (USL && DET) {
         // bounds of the second extrapolation, which k_det_usl then sums
         const double mp = p.mass[i];
@@ -1324,6 +1865,62 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
     } else {
         reset_element<DIM>(g, p, i, rv.err);
     }
+}
+
+// k_g2p with USL in the mixed mode through a shared-memory node tile (single
+// material field, window shape functions): the particle update, then the
+// second extrapolation accumulated per block as two-sum pairs of mass and of
+// mass times the new velocity's difference from the block's reference, added
+// once per touched node to the FP64 columns of the second momentum.
+template <int DIM, int SHAPE, bool BATCH>
+static __global__ void __launch_bounds__(256) k_g2p_tile(StepParams sp, DevParticles p, DevNodes nd) {
+    __shared__ NodeTile t;
+    const int i = tile_particle();
+    RunView rv;
+    const bool valid = i < p.n && particle_run<BATCH>(sp, p, i, rv);
+    int col = 0, row = 0, zr = 0;
+    double v[3] = {0., 0., 0.}, xp[3];
+    if (valid) {
+        g2p_move<DIM, SHAPE, true, BATCH>(sp, p, nd, i, rv, 0, v, xp);
+        elem_coords(rv.g, p.elem[i], col, row, zr);
+    }
+    const bool tiled = tile_open<DIM, SHAPE>(t, valid, BATCH && valid ? p.run[i] : 0, col, row, zr, rv, v, DIM + 1);
+    if (valid) {
+        const double mp = p.mass[i];
+        AxisWin<SHAPE, float> w;
+        axis_windows<DIM, SHAPE, false, float>(rv.g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0.,
+                                               p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1., w);
+        if (tiled) {
+            const float mpf = (float)mp;
+            const float d[3] = {(float)(v[0] - t.ref[0]), (float)(v[1] - t.ref[1]), (float)(v[2] - t.ref[2])};
+            for_each_window_node<DIM, SHAPE, false, float>(w, [&](int jx, int jy, int jz, float N, float, float, float) {
+                if (N == 0.f) return;
+                const int k = tile_slot(t.box, w.c, jx, jy, jz);
+                const float wm = N * mpf;
+                tile_add(t, 0, k, wm);
+#pragma unroll
+                for (int a = 0; a < DIM; a++) tile_add(t, 1 + a, k, wm * d[a]);
+                t.touched[k] = 1;
+            });
+        } else {
+            const DevGrid &g = rv.g;
+            for_each_window_node<DIM, SHAPE, false, float>(w, [&](int jx, int jy, int jz, float N, float, float, float) {
+                if (N == 0.f) return;
+                const int n = rv.nb + (w.c[0] + jx) + g.yplane * (w.c[1] + jy) + g.zplane * (w.c[2] + jz);
+                const double fnmp = (double)N * mp;
+                atomicAdd(&nd.ux[n], v[0] * fnmp);
+                atomicAdd(&nd.uy[n], v[1] * fnmp);
+                if (DIM == 3) atomicAdd(&nd.uz[n], v[2] * fnmp);
+            });
+        }
+    }
+    __syncthreads();
+    tile_flush(t, [&](int n, int k) {
+        const double m = tile_sum(t, 0, k);
+        atomicAdd(&nd.ux[n], t.ref[0] * m + tile_sum(t, 1, k));
+        atomicAdd(&nd.uy[n], t.ref[1] * m + tile_sum(t, 2, k));
+        if (DIM == 3) atomicAdd(&nd.uz[n], t.ref[2] * m + tile_sum(t, 3, k));
+    });
 }
 
 // Deterministic mode: the second extrapolation of k_g2p (momentum at the
@@ -1774,9 +2371,10 @@ static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, Dev
         double p[3] = {nd.cx[k], nd.cy[k], DIM == 3 ? nd.cz[k] : 0.};
         double fr[3];
         if (MIX) {
-            fr[0] = (double)nd.gx[k];
-            fr[1] = (double)nd.gy[k];
-            fr[2] = DIM == 3 ? (double)nd.gz[k] : 0.;
+            // FP64 sums of tiled blocks plus FP32 sums of the other particles
+            fr[0] = nd.fx[k] + (double)nd.gx[k];
+            fr[1] = nd.fy[k] + (double)nd.gy[k];
+            fr[2] = DIM == 3 ? nd.fz[k] + (double)nd.gz[k] : 0.;
         } else {
             fr[0] = nd.fx[k];
             fr[1] = nd.fy[k];

@@ -61,7 +61,16 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
         cudaMemsetAsync(c->det.nbnd, 0, (size_t)NT * sizeof(unsigned long long), s);
         k_det_bounds<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, c->mats);
     }
-    k_p2g<DIM, SHAPE, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    // mixed mode, one material field, window shape functions: the scatters
+    // accumulate in shared-memory node tiles (unless MPMGPU_P2G_UNTILED)
+    constexpr bool kTileable = MIX && !DET && SHAPE != SHAPE_LCPDI;
+    const bool tile = kTileable && c->ct.nf == 1 && c->opts.p2g != MPMGPU_P2G_UNTILED;
+    if constexpr (kTileable) {
+        if (tile) k_p2g_tile<DIM, SHAPE, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
+        else k_p2g<DIM, SHAPE, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    } else {
+        k_p2g<DIM, SHAPE, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    }
     if (DET) {
         k_det_resolve<DIM, MIX><<<ntb, TB, 0, s>>>(sp, c->nd, NT, 0);
         c->launches += 2;
@@ -96,10 +105,22 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     mark(1, false);
     mark(2, true);
     if (xm > 1 && method != MPMGPU_USL) xpic_expand(XPIC_STRAIN);  // FMPM(k) velocities of the first strain update
-    if (method == MPMGPU_USL)
-        k_strain_forces<DIM, SHAPE, false, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
-    else
-        k_strain_forces<DIM, SHAPE, true, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    bool forces_done = false;
+    if constexpr (kTileable) {
+        if (tile) {
+            if (method == MPMGPU_USL)
+                k_strain_forces_tile<DIM, SHAPE, false, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+            else
+                k_strain_forces_tile<DIM, SHAPE, true, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+            forces_done = true;
+        }
+    }
+    if (!forces_done) {
+        if (method == MPMGPU_USL)
+            k_strain_forces<DIM, SHAPE, false, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+        else
+            k_strain_forces<DIM, SHAPE, true, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    }
     if (DET) {
         k_det_forces<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
         k_det_resolve<DIM, MIX><<<ntb, TB, 0, s>>>(sp, c->nd, NT, 1);
@@ -118,7 +139,14 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
         mark(4, false);
         return;
     }
-    k_g2p<DIM, SHAPE, true, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
+    bool g2p_done = false;
+    if constexpr (kTileable) {
+        if (tile) {
+            k_g2p_tile<DIM, SHAPE, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
+            g2p_done = true;
+        }
+    }
+    if (!g2p_done) k_g2p<DIM, SHAPE, true, MIX, false, DET><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
     if (DET) {
         k_det_usl<DIM, SHAPE, MIX><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->mats);
         k_det_resolve<DIM, MIX><<<ntb, TB, 0, s>>>(sp, c->nd, NT, 2);

@@ -47,7 +47,9 @@ def main(argv=None):
     ap.add_argument("--xpic", type=int, default=0, help="PeriodicXPIC order (cantilever, taylor; 0: FLIP)")
     ap.add_argument("--fmpm", action="store_true", help="FMPM(k) instead of XPIC(k)")
     ap.add_argument("--xpic-period", type=int, default=1, help="PeriodicXPIC periodicSteps")
-    ap.add_argument("--p2g", choices=("atomic", "deterministic"), default="atomic")
+    ap.add_argument("--p2g", choices=("atomic", "deterministic", "untiled"), default="atomic",
+                    help="node sums: atomic (shared-memory tiles in the mixed mode), deterministic, or untiled "
+                         "(every particle-node pair straight to the node columns)")
     ap.add_argument("--profile", action="store_true", help="per-kernel ms of the timed steps (single runs)")
     a = ap.parse_args(argv)
     from nairn_gb300 import gpu, model
@@ -83,7 +85,8 @@ def main(argv=None):
                                  gap=a.gap)
         else:
             m = model.block_3d(ncx=a.cells, ncy=a.cells, ncz=a.cells, steps=total)
-        r = gpu.GpuRun(m, precision=prec, sort_interval=a.sort_interval, p2g=1 if a.p2g == "deterministic" else 0)
+        r = gpu.GpuRun(m, precision=prec, sort_interval=a.sort_interval,
+                       p2g={"atomic": 0, "deterministic": 1, "untiled": 2}[a.p2g])
         r.upload(m.particles)
         r.step(a.warmup)
         if a.profile:

@@ -38,7 +38,7 @@ def test_create_rejects_bad_options_without_gpu_work(gpu_lib):
     st = gpu_lib.mpmgpu_create(C.byref(g), C.byref(o), C.byref(h))
     assert st == 2 and not h.value
     assert b"shape" in gpu_lib.mpmgpu_last_error(None)
-    o = abi.options_struct(m, p2g=2)  # only atomic (0) and deterministic (1) node sums
+    o = abi.options_struct(m, p2g=3)  # node sums: atomic (0), deterministic (1) or untiled (2) only
     st = gpu_lib.mpmgpu_create(C.byref(g), C.byref(o), C.byref(h))
     assert st == 2 and not h.value
     assert b"p2g" in gpu_lib.mpmgpu_last_error(None)
