@@ -81,8 +81,14 @@ enum { MPMGPU_PREC_FP64 = 0, MPMGPU_PREC_MIXED = 1 };
  * MPMGPU_P2G_UNTILED scatters every (particle, node) pair straight to the
  * node columns instead. */
 enum { MPMGPU_P2G_ATOMIC = 0, MPMGPU_P2G_DETERMINISTIC = 1, MPMGPU_P2G_UNTILED = 2 };
-/* Material types: Common/Read_XML/MaterialController.cpp:105-231 */
-enum { MPMGPU_MAT_ISOTROPIC = 1, MPMGPU_MAT_ISOPLASTICITY = 9, MPMGPU_MAT_NEOHOOKEAN = 28 };
+/* Material types: Common/Read_XML/MaterialController.cpp:105-231.  Type 35 is
+ * RigidMaterial in multimaterial mode (RIGIDCONTACTMATERIAL,
+ * NairnMPM/src/Materials/RigidMaterial.hpp:14): particles that move at their
+ * own constant velocity and take part in contact only; their mass is their
+ * volume in mm^3 (the reference's rho = 1 for rigid materials), the rho of
+ * their MpmGpuMaterial is ignored, and they need multimaterial contact. */
+enum { MPMGPU_MAT_ISOTROPIC = 1, MPMGPU_MAT_ISOPLASTICITY = 9, MPMGPU_MAT_NEOHOOKEAN = 28,
+       MPMGPU_MAT_RIGID_CONTACT = 35 };
 
 /* Structured background grid, as MPMReadHandler::grid() builds it
  * (NairnMPM/src/Read_MPM/Generators.cpp:1675-1990): nx*ny(*nz) elements

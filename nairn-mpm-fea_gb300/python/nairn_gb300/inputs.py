@@ -33,10 +33,13 @@ def wave_speed(mat_type: int, rho: float, E: float = 0., nu: float = 0., G: floa
     return neo_wave_speed(G, K, rho) if mat_type == 28 else iso_wave_speed(E, nu, rho)
 
 
-def material_xml(mat_type: int, name: str, rho: float, E: float = 0., nu: float = 0., yield_: float = 0.,
+def material_xml(mat_type: int, name: str, rho: float = 1., E: float = 0., nu: float = 0., yield_: float = 0.,
                  Ep: float = 0., G: float = 0., K: float = 0., uj: int = 0) -> str:
     """<Material> block of type 1 (IsotropicMat), 9 (IsoPlasticity with linear
-    hardening) or 28 (Neohookean, G and K input, U(J) option uj)."""
+    hardening), 28 (Neohookean, G and K input, U(J) option uj) or 35 (rigid
+    contact material, RigidMaterial in multimaterial mode: no properties)."""
+    if mat_type == 35:
+        return f'  <Material Type="35" Name="{name}">\n  </Material>\n'
     body = f"    <rho>{_fmt(rho)}</rho>\n"
     if mat_type == 28:
         body += f"    <G>{_fmt(G)}</G>\n    <K>{_fmt(K)}</K>\n    <UJOption>{int(uj)}</UJOption>\n"
@@ -275,5 +278,86 @@ def contact_3d(plate=(12, 12, 3), block=(4, 4, 3), block_x0=4.0, block_y0=4.0, g
     </BCBox>
   </GridBCs>
 </JANFEAInput>
+"""
+    return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 3}
+
+
+def rigid_contact_2d(plate=(20, 4), indenter=(6, 3), indenter_x0=7.0, gap=0.5, cell=1.0, ppc_side=2,
+                     v=(0., -2000.), plate_mat=None, friction=0.3, normals=2, steps=150, cfl=0.4, gimp="uGIMP",
+                     method=2, margin_cells=4, archive_root: str = "Results/rigid.", inc_terms: int = 0) -> tuple[str, dict]:
+    """2D plane-strain contact with a rigid material: a rigid indenter
+    (RigidMaterial type 35, moving at the constant velocity v) pressed into
+    an elastic plate whose base is held.  The plate's body comes first, so the
+    reference keeps the particles in input order (non-rigid first)."""
+    pm = dict(mat_type=1, rho=2.7, E=70000., nu=0.33) if plate_mat is None else dict(plate_mat)
+    Lp, Hp = plate[0] * cell, plate[1] * cell
+    Li, Hi = indenter[0] * cell, indenter[1] * cell
+    y0 = Hp + gap
+    c = wave_speed(pm["mat_type"], pm["rho"], E=pm.get("E", 0.), nu=pm.get("nu", 0.), G=pm.get("G", 0.),
+                   K=pm.get("K", 0.))
+    dt = cfl_timestep(cell, c, cfl)
+    maxtime = (steps - 0.5) * dt
+    m = margin_cells * cell
+    xml = _header(10, method, gimp, maxtime, cfl, archive_root, ppc_side * ppc_side, ARCHIVE_ORDER, inc_terms)
+    xml = xml.replace("  </MPMHeader>\n", _mm_mode(normals, friction) + "  </MPMHeader>\n")
+    xml += f"""  <Mesh output="file">
+    <Grid xmin="{_fmt(-m)}" xmax="{_fmt(Lp + m)}" ymin="{_fmt(-m)}" ymax="{_fmt(y0 + Hi + m)}" thickness="1">
+      <Horiz cellsize="{_fmt(cell)}"/>
+      <Vert cellsize="{_fmt(cell)}"/>
+    </Grid>
+  </Mesh>
+  <MaterialPoints>
+    <Body mat="1" angle="0" thick="1" vx="0" vy="0">
+      <Rect xmin="0" xmax="{_fmt(Lp)}" ymin="0" ymax="{_fmt(Hp)}"/>
+    </Body>
+    <Body mat="2" angle="0" thick="1" vx="{_fmt(v[0])}" vy="{_fmt(v[1])}">
+      <Rect xmin="{_fmt(indenter_x0)}" xmax="{_fmt(indenter_x0 + Li)}" ymin="{_fmt(y0)}" ymax="{_fmt(y0 + Hi)}"/>
+    </Body>
+  </MaterialPoints>
+{material_xml(pm.pop("mat_type"), "plate", **pm)}{material_xml(35, "indenter")}  <GridBCs>
+    <BCLine x1="{_fmt(-0.5 * cell)}" y1="0" x2="{_fmt(Lp + 0.5 * cell)}" y2="0" tolerance="{_fmt(0.01)}">
+      <DisBC dir="1" disp="0"/>
+      <DisBC dir="2" disp="0"/>
+    </BCLine>
+  </GridBCs>
+</JANFEAInput>
+"""
+    return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 2}
+
+
+def rigid_taylor_3d(radius: float = 1.0, length: float = 2.0, cell: float = 0.5, ppc_side: int = 2,
+                    v0: float = -200000., E: float = 200000., nu: float = 0.3, yield_: float = 300.,
+                    Ep: float = 2000., rho: float = 7.8, slab_cells: int = 2, friction: float = 0.0,
+                    normals: int = 2, steps: int = 40, cfl: float = 0.5, gimp: str = "uGIMP", method: int = 2,
+                    archive_root: str = "Results/rtaylor.", inc_terms: int = 0) -> tuple[str, dict]:
+    """The Taylor impact with a rigid wall made of particles: the bar
+    (von Mises, linear hardening) moving at v0 (mm/s) onto a stationary slab of
+    rigid contact material (type 35) occupying -slab_cells*cell <= z <= 0,
+    in place of the zero-velocity grid condition on the z = 0 plane;
+    multimaterial contact with Coulomb friction."""
+    c = wave_speed(9, rho, E=E, nu=nu)
+    dt = cfl_timestep(cell, c, cfl)
+    maxtime = (steps - 0.5) * dt
+    lm = max(4 * cell, 0.8 * radius)
+    xr = radius + lm
+    zs = slab_cells * cell
+    xml = _header(12, method, gimp, maxtime, cfl, archive_root, ppc_side ** 3, ARCHIVE_ORDER, inc_terms)
+    xml = xml.replace("  </MPMHeader>\n", _mm_mode(normals, friction) + "  </MPMHeader>\n")
+    xml += f"""  <Mesh output="file">
+    <Grid xmin="{_fmt(-xr)}" xmax="{_fmt(xr)}" ymin="{_fmt(-xr)}" ymax="{_fmt(xr)}" zmin="{_fmt(-zs - 4 * cell)}" zmax="{_fmt(length + 4 * cell)}">
+      <Horiz cellsize="{_fmt(cell)}"/>
+      <Vert cellsize="{_fmt(cell)}"/>
+      <Depth cellsize="{_fmt(cell)}"/>
+    </Grid>
+  </Mesh>
+  <MaterialPoints>
+    <Body mat="1" angle="0" vx="0" vy="0" vz="{_fmt(v0)}">
+      <Cylinder xmin="{_fmt(-radius)}" xmax="{_fmt(radius)}" ymin="{_fmt(-radius)}" ymax="{_fmt(radius)}" zmin="0" zmax="{_fmt(length)}" axis="z"/>
+    </Body>
+    <Body mat="2" angle="0" vx="0" vy="0" vz="0">
+      <Box xmin="{_fmt(-xr + cell)}" xmax="{_fmt(xr - cell)}" ymin="{_fmt(-xr + cell)}" ymax="{_fmt(xr - cell)}" zmin="{_fmt(-zs)}" zmax="0"/>
+    </Body>
+  </MaterialPoints>
+{material_xml(9, "bar", rho, E=E, nu=nu, yield_=yield_, Ep=Ep)}{material_xml(35, "wall")}</JANFEAInput>
 """
     return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 3}

@@ -23,7 +23,7 @@ import numpy as np
 PLANE_STRAIN, THREED = 10, 12
 USF, USAVG, USL = 0, 2, 3
 SHAPE_LINEAR, SHAPE_UGIMP, SHAPE_BGIMP, SHAPE_BSPLINE, SHAPE_LCPDI = 0, 1, 5, 6, 10
-MAT_ISO, MAT_PLASTIC, MAT_NEOHOOKEAN = 1, 9, 28
+MAT_ISO, MAT_PLASTIC, MAT_NEOHOOKEAN, MAT_RIGID = 1, 9, 28, 35
 
 PARTICLE_FIELDS = ("x", "y", "z", "vx", "vy", "vz", "x0", "y0", "z0", "mass", "lpx", "lpy", "lpz",
                    "exx", "eyy", "ezz", "exy", "exz", "eyz", "wxy", "wxz", "wyz",
@@ -665,3 +665,89 @@ def contact_models(count=64, seed=303, **kw) -> list:
         m.name = name
         out.append(m)
     return out
+
+
+# A rigid contact material (RigidMaterial, type 35): rho = 1 g/mm^3 in the
+# reference's units, so each particle's mass is its volume in mm^3 (1000 g/cm^3
+# here, which _new_particles scales by 1e-3 to exactly 1).
+RIGID_RHO_GCC = 1000.
+
+
+def _rigid_material():
+    return dict(type=MAT_RIGID, field=0, rho=RIGID_RHO_GCC, E=0., nu=0., yield_=0., Ep=0., G=0., K=0., UJOption=0)
+
+
+def rigid_contact_2d(plate=(20, 4), indenter=(6, 3), indenter_x0=7.0, gap=0.5, cell=1.0, ppc_side=2,
+                     v=(0., -2000.), plate_mat=None, friction=0.3, normals=2, steps=150, cfl=0.4, gimp="uGIMP",
+                     method=USAVG, margin_cells=4, inc_terms=0, **_ignored) -> Model:
+    """Model of inputs.rigid_contact_2d (same arguments): elastic plate in
+    material field 0 (base held), rigid indenter in field 1 moving at v."""
+    from . import inputs
+    shape = GIMP_NAMES[gimp]
+    pm = _mat_from(plate_mat, dict(mat_type=MAT_ISO, rho=2.7, E=70000., nu=0.33))
+    rm = _rigid_material()
+    pm["field"], rm["field"] = 0, 1
+    Lp, Hp = plate[0] * cell, plate[1] * cell
+    Li, Hi = indenter[0] * cell, indenter[1] * cell
+    y0 = Hp + gap
+    m = margin_cells * cell
+    g = make_grid(2, (-m, Lp + m), (-m, y0 + Hi + m), None, cell, 1.0)
+    pos, elem = _element_points(g, ppc_side)
+    x, y = pos[:, 0], pos[:, 1]
+    in_p = (x <= Lp) & (x >= 0.) & (y <= Hp) & (y >= 0.)
+    in_i = (x <= indenter_x0 + Li) & (x >= indenter_x0) & (y <= y0 + Hi) & (y >= y0) & ~in_p
+    p = _concat([_body_particles(g, pos, elem, in_p, ppc_side, pm, 0, (0., 0., 0.)),
+                 _body_particles(g, pos, elem, in_i, ppc_side, rm, 1, (v[0], v[1], 0.))])
+    ids = np.arange(1, g.nnodes + 1)
+    ndx = g.xnodes[(ids - 1) % (g.nx + 1)]
+    ndy = g.ynodes[(ids - 1) // (g.nx + 1)]
+    nodes = ids[_line_contains(ndx, ndy, -0.5 * cell, 0., Lp + 0.5 * cell, 0., 0.01)]
+    bcs = np.zeros(2 * nodes.size, dtype=BC_DTYPE)
+    bcs["node"][:nodes.size] = nodes
+    bcs["dir"][:nodes.size] = 1
+    bcs["node"][nodes.size:] = nodes
+    bcs["dir"][nodes.size:] = 2
+    c = inputs.wave_speed(pm["type"], pm["rho"], E=pm["E"], nu=pm["nu"], G=pm["G"], K=pm["K"])
+    dt = inputs.cfl_timestep(g.dx, c, cfl)
+    opts = dict(np=PLANE_STRAIN, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
+                inc_defgrad_terms=inc_terms if inc_terms > 0 else 2, nfields=2)
+    return Model(g, p, [pm, rm], bcs, opts, steps, name="rigid_contact_2d",
+                 extra={"contact": _contact_options(normals, friction)})
+
+
+def rigid_taylor_3d(radius=1.0, length=2.0, cell=0.5, ppc_side=2, v0=-200000., E=200000., nu=0.3, yield_=300.,
+                    Ep=2000., rho=7.8, slab_cells=2, friction=0.0, normals=2, steps=40, cfl=0.5, gimp="uGIMP",
+                    method=USAVG, inc_terms=0, **_ignored) -> Model:
+    """Model of inputs.rigid_taylor_3d (same arguments): the bar in material
+    field 0, the stationary rigid slab (z in [-slab_cells*cell, 0]) in field 1,
+    no grid velocity conditions."""
+    from . import inputs
+    shape = GIMP_NAMES[gimp]
+    lm = max(4 * cell, 0.8 * radius)
+    xr = radius + lm
+    zs = slab_cells * cell
+    g = make_grid(3, (-xr, xr), (-xr, xr), (-zs - 4 * cell, length + 4 * cell), cell)
+    pos, elem = _element_points(g, ppc_side)
+    # BoxController::ContainsPoint, cylinder along z (BoxController.cpp:47-98)
+    xmin, xmax, ymin, ymax, zmin, zmax = -radius, radius, -radius, radius, 0., length
+    xmid, ymid = (xmin + xmax) / 2., (ymin + ymax) / 2.
+    a2 = (xmax - xmid) ** 2
+    b2 = (ymax - ymid) ** 2
+    x, y, z = pos[:, 0], pos[:, 1], pos[:, 2]
+    R = (zmax - z + 1. * (z - zmin)) / (zmax - zmin)
+    ddx, ddy = x - xmid, y - ymid
+    in_bar = (z <= zmax) & (z >= zmin) & ((ddx * ddx / a2 + ddy * ddy / b2) <= R * R)
+    in_slab = ((x <= xr - cell) & (x >= -xr + cell) & (y <= xr - cell) & (y >= -xr + cell) & (z <= 0.)
+               & (z >= -zs) & ~in_bar)
+    bm = _material(MAT_PLASTIC, rho, E=E, nu=nu, yield_=yield_, Ep=Ep)
+    rm = _rigid_material()
+    bm["field"], rm["field"] = 0, 1
+    p = _concat([_body_particles(g, pos, elem, in_bar, ppc_side, bm, 0, (0., 0., v0)),
+                 _body_particles(g, pos, elem, in_slab, ppc_side, rm, 1, (0., 0., 0.))])
+    bcs = np.zeros(0, dtype=BC_DTYPE)
+    c = inputs.wave_speed(MAT_PLASTIC, rho, E=E, nu=nu)
+    dt = inputs.cfl_timestep(g.dx, c, cfl)
+    opts = dict(np=THREED, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
+                inc_defgrad_terms=inc_terms if inc_terms > 0 else 1, nfields=2)
+    return Model(g, p, [bm, rm], bcs, opts, steps, name=f"rigid_taylor_3d_r{radius}_c{cell}",
+                 extra={"contact": _contact_options(normals, friction)})

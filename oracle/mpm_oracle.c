@@ -129,6 +129,10 @@ static int load_materials(const MpmGpuMaterial *in, int nmat, int np, OMat *out)
             m->Lamesp = Lame / m->rho;
             m->Ksp = m->Lamesp + 2. * m->Gsp / 3.;
             m->uj = in[i].UJOption;
+        } else if (m->type == MPMGPU_MAT_RIGID_CONTACT) {
+            /* RigidMaterial (RigidMaterial.cpp:26-60): rho = 1, so a particle's
+             * mass is its volume; no mechanical properties */
+            m->rho = 1.;
         } else {
             return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: material type not implemented");
         }
@@ -157,6 +161,7 @@ double mpm_oracle_cfl_timestep(const MpmGpuGrid *grid, const MpmGpuMaterial *mat
     double tmin = 1.e30;
     for (int i = 0; i < nmat; i++) {
         if (mat_used && !mat_used[i]) continue;
+        if (om[i].type == MPMGPU_MAT_RIGID_CONTACT) continue;  /* rigid materials set no time step */
         double tst = dcell / wave_speed(&om[i]);
         if (tst < tmin) tmin = tst;
     }
@@ -1148,11 +1153,19 @@ typedef struct {
     int xpic;               /* this step: 0 FLIP, k > 0 FMPM(k), -k XPIC(k) (GridToParticleExtrap::m) */
     double *vpx, *vpy, *vpz;  /* XPIC v*(prev) (MatVelocityField vk[VSTARPREV_VEC]) */
     double *vnx, *vny, *vnz;  /* XPIC v*(next) (vk[VSTARNEXT_VEC]) */
+    int rigid_field[64];    /* field f holds a rigid contact material (MatVelocityField::IsRigidField) */
+    int has_rigid;          /* some material is rigid */
+    double rigid_bias;      /* MeshInfo::rigidGradientBias, squared (MeshInfo.cpp:1191) */
 } OCtx;
 
 /* field of particle q (MaterialBase::GetField) */
 static int particle_field(const OCtx *c, long q) {
     return c->nf > 1 ? c->mats[c->p->mat[q]].field : 0;
+}
+
+/* particle q is of a rigid contact material (MaterialBase::IsRigid) */
+static int particle_rigid(const OCtx *c, long q) {
+    return c->mats[c->p->mat[q]].type == MPMGPU_MAT_RIGID_CONTACT;
 }
 
 /* shape functions of particle q for this step (GetShapeFunctions/GetShapeGradients) */
@@ -1243,8 +1256,11 @@ static void velocity_bc_field(OCtx *c, int pass, int fld) {
     }
 }
 
+/* CrackVelocityFieldMulti::ZeroVelocityBC / AddVelocityBC apply to the
+ * non-rigid fields only (CrackVelocityFieldMulti.cpp:1243-1259) */
 static void velocity_bc_loop(OCtx *c, int pass) {
-    for (int fld = 0; fld < c->nf; fld++) velocity_bc_field(c, pass, fld);
+    for (int fld = 0; fld < c->nf; fld++)
+        if (!c->rigid_field[fld]) velocity_bc_field(c, pass, fld);
 }
 
 static long particle_order(const OCtx *c, long k) {
@@ -1283,6 +1299,11 @@ static void p2g_mass_momentum(OCtx *c, int last) {
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
     for (long k = 0; k < p->n; k++) {
         long q = particle_order(c, k);
+        /* the second extrapolation takes the non-rigid particles only
+         * (UpdateStrainsLastContactTask.cpp:90); rigid particles add to their
+         * field like any other on the first (NodalPointMPM.cpp:419-453, with
+         * the unscaled volume, equal to the deformed one for F = I) */
+        if (last && particle_rigid(c, q)) continue;
         OShape s;
         particle_shape(c, q, c->mm, &s);
         long off = (long)particle_field(c, q) * c->nn;
@@ -1379,6 +1400,7 @@ static void strain_update(OCtx *c, double strainTime) {
     else grid_velocity(c);
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
     for (long q = 0; q < p->n; q++) {
+        if (particle_rigid(c, q)) continue;  /* non-rigid particles only (UpdateStrainsFirstTask.cpp:123) */
         OShape s;
         particle_shape(c, q, 1, &s);
         long off = (long)particle_field(c, q) * c->nn;
@@ -1424,6 +1446,7 @@ static void p2g_forces(OCtx *c) {
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
     for (long k = 0; k < p->n; k++) {
         long q = particle_order(c, k);
+        if (particle_rigid(c, q)) continue;  /* non-rigid particles only (GridForcesTask.cpp:53) */
         OShape s;
         particle_shape(c, q, 1, &s);
         long off = (long)particle_field(c, q) * c->nn;
@@ -1474,6 +1497,14 @@ static void g2p_move(OCtx *c) {
     else grid_velocity(c);
 #pragma omp parallel for num_threads(c->nthreads) schedule(static) if (c->nthreads > 1)
     for (long q = 0; q < p->n; q++) {
+        if (particle_rigid(c, q)) {
+            /* rigid materials move at their current velocity (UpdateParticlesTask.cpp:291-295,
+             * MatPoint2D/3D::MovePosition) */
+            p->x[q] += dt * p->vx[q];
+            p->y[q] += dt * p->vy[q];
+            if (is3d) p->z[q] += dt * p->vz[q];
+            continue;
+        }
         OShape s;
         particle_shape(c, q, 0, &s);
         long off = (long)particle_field(c, q) * c->nn;
@@ -2048,6 +2079,78 @@ static void lr_normal(const OCtx *c, long n, int a, int logistic, double *norm, 
     *deln = supA + supB;
 }
 
+/* CrackVelocityFieldMulti::RigidMaterialContactOnCVF (CrackVelocityFieldMulti.cpp:676-958)
+ * at node n for the Coulomb law: the rigid field with the largest contact
+ * volume, and each non-rigid field moved toward the rigid field's velocity
+ * (mred = its own mass; only the non-rigid field's momentum changes), with
+ * the normal of GetNormalVector for a rigid partner (:960-1030). */
+static void rigid_contact_node(OCtx *c, long n, int callType) {
+    OField *f = &c->f;
+    int postUpdate = callType == UPDATE_MOMENTUM_CALL;
+    int rigidFld = -1;
+    double rigidVolume = 0.;
+    for (int fl = 0; fl < c->nf; fl++) {
+        long k = fl * c->nn + n;
+        if (f->npts[k] <= 0 || !c->rigid_field[fl]) continue;
+        if (rigidFld < 0 || f->vol[k] > rigidVolume) {
+            rigidFld = fl;
+            rigidVolume = f->vol[k];
+        }
+    }
+    long kr = (long)rigidFld * c->nn + n;
+    double actualRigidVolume = f->mass[kr];
+    double rr = 1. / actualRigidVolume;
+    double rvel[3] = {f->px[kr] * rr, f->py[kr] * rr, f->pz[kr] * rr};
+    double gradj[3] = {f->gvx[kr] * -1., f->gvy[kr] * -1., f->gvz[kr] * -1.};
+    for (int fl = 0; fl < c->nf; fl++) {
+        long ki = fl * c->nn + n;
+        if (f->npts[ki] <= 0 || c->rigid_field[fl]) continue;
+        double massi = f->mass[ki], voli = f->vol[ki];
+        double delPi[3] = {f->px[ki] * -1., f->py[ki] * -1., f->pz[ki] * -1.};
+        for (int a = 0; a < 3; a++) delPi[a] += rvel[a] * massi;
+        double normi[3] = {f->gvx[ki] * 1., f->gvy[ki] * 1., f->gvz[ki] * 1.}, norm[3];
+        if (c->normals == 0) {
+            double magi = sqrt(dot3(normi, normi)), magj = sqrt(dot3(gradj, gradj));
+            if (magi >= c->rigid_bias * magj) for (int a = 0; a < 3; a++) norm[a] = normi[a] * (1. / magi);
+            else for (int a = 0; a < 3; a++) norm[a] = gradj[a] * (1. / magj);
+        } else if (c->normals == 1) {
+            if (voli >= rigidVolume) for (int a = 0; a < 3; a++) norm[a] = normi[a];
+            else for (int a = 0; a < 3; a++) norm[a] = gradj[a];
+            double sc = 1. / sqrt(dot3(norm, norm));
+            for (int a = 0; a < 3; a++) norm[a] = norm[a] * sc;
+        } else {
+            for (int a = 0; a < 3; a++) norm[a] = normi[a] + gradj[a];
+            double magi = dot3(norm, norm);
+            double vRatio = (voli + rigidVolume) / rigidVolume;
+            double magj = dot3(gradj, gradj);
+            if (magi >= c->rigid_bias * magj * vRatio * vRatio) {
+                double sc = 1. / sqrt(magi);
+                for (int a = 0; a < 3; a++) norm[a] *= sc;
+            } else {
+                double sc = 1. / sqrt(magj);
+                for (int a = 0; a < 3; a++) norm[a] = gradj[a] * sc;
+            }
+        }
+        if (norm[0] != norm[0] || norm[1] != norm[1] || norm[2] != norm[2]) continue;
+        double dotn = dot3(delPi, norm);
+        double dispRigid[3] = {f->ux[kr] * rr, f->uy[kr] * rr, f->uz[kr] * rr};
+        double rmi = 1. / massi;
+        double dispi[3] = {f->ux[ki] * rmi, f->uy[ki] * rmi, f->uz[ki] * rmi};
+        /* CrackSurfaceContact::MaterialSeparation with displacements (CrackSurfaceContact.cpp:278-303) */
+        double deln = dot3(dispRigid, norm) - dot3(dispi, norm);
+        double delFi[3], *dfp = NULL;
+        if (postUpdate) {
+            /* dF = -F_i for an infinitely massive partner */
+            delFi[0] = f->fx[ki] * -1.;
+            delFi[1] = f->fy[ki] * -1.;
+            delFi[2] = f->fz[ki] * -1.;
+            dfp = delFi;
+        }
+        if (!coulomb_delta(c, delPi, norm, dotn, deln, massi, dfp)) continue;
+        change_momentum(c, ki, delPi, callType);
+    }
+}
+
 static void material_contact(OCtx *c, int callType) {
     OField *f = &c->f;
     int nf = c->nf;
@@ -2066,6 +2169,15 @@ static void material_contact(OCtx *c, int callType) {
             act[nm++] = fl;
         }
         if (nm <= 1) continue;
+        if (c->has_rigid) {
+            /* a rigid field at the node: contact against it alone (MaterialContactOnCVF, :302-347) */
+            int rigid_here = 0;
+            for (int q = 0; q < nm; q++) rigid_here |= c->rigid_field[act[q]];
+            if (rigid_here) {
+                rigid_contact_node(c, n, callType);
+                continue;
+            }
+        }
         int doingPairs = nm == 2;
         int miMax = doingPairs ? nm - 1 : nm;
         double dispc[3] = {0., 0., 0.};
@@ -2234,6 +2346,14 @@ static int one_step(OCtx *c) {
         /* RezeroNodeTask6: momenta and contact terms */
         for (long i = 1; i < nn; i++) {
             if (f->npts[i] > 0) {
+                if (c->rigid_field[i / c->nn]) {
+                    /* a rigid field keeps its momentum, volume and volume gradient; its
+                     * displacement moves by p dt (CrackVelocityFieldMulti::RezeroNodeTask6, :157-176) */
+                    f->ux[i] += f->px[i] * dt;
+                    f->uy[i] += f->py[i] * dt;
+                    f->uz[i] += f->pz[i] * dt;
+                    continue;
+                }
                 f->px[i] = 0.; f->py[i] = 0.; f->pz[i] = 0.;
                 if (c->mm) {
                     f->vol[i] = 0.;
@@ -2299,7 +2419,22 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     if (c.nf > 64) { free(c.mats); return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: more than 64 material fields"); }
     c.mm = c.nf > 1 && contact && contact->enabled;
     if (c.nf > 1 && !c.mm) { free(c.mats); return fail(MPMGPU_ERR_INVALID, "oracle: several material fields need contact"); }
+    for (int i = 0; i < nmat; i++)
+        if (c.mats[i].type == MPMGPU_MAT_RIGID_CONTACT) {
+            c.rigid_field[c.mats[i].field] = 1;
+            c.has_rigid = 1;
+        }
+    if (c.has_rigid && (!c.mm || c.nf < 2)) {
+        free(c.mats);
+        return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: rigid contact materials need multimaterial contact");
+    }
+    if (c.has_rigid && contact->normals >= 5) {
+        free(c.mats);
+        return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: regression normals with rigid materials not implemented");
+    }
     if (c.mm) {
+        c.rigid_bias = contact->rigid_gradient_bias > 0. ? contact->rigid_gradient_bias : 1.;
+        c.rigid_bias *= c.rigid_bias;
         c.normals = contact->normals;
         c.friction = contact->friction;
         /* CoulombFriction::VerifyAndLoadProperties: <0 stick, 0 frictionless */

@@ -109,6 +109,14 @@ CASES = {
     "taylor3d_b2gimp_neo_usf": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=60, gimp="B2GIMP", method=0,
                                                   mat_type=28, G=10., K=50., rho=1.1, v0=-30000.)),
     "contact2d_b2gimp_fric": ("contact_2d", dict(steps=150, friction=0.3, normals=2, gimp="B2GIMP")),
+    # rigid contact materials (type 35): a rigid indenter moving at constant
+    # velocity into an elastic plate, and the Taylor bar onto a rigid slab
+    "rigid2d_indent_fric": ("rigid_contact_2d", dict(steps=150, friction=0.3, normals=2)),
+    "rigid2d_indent_maxg_usl": ("rigid_contact_2d", dict(steps=120, friction=0.0, normals=0, method=3)),
+    "rigid2d_indent_maxv_stick": ("rigid_contact_2d", dict(steps=120, friction=-1.0, normals=1, v=(1000., -1500.))),
+    "rigid2d_indent_cpdi_usf": ("rigid_contact_2d", dict(steps=120, friction=0.3, normals=2, gimp="lCPDI", method=0)),
+    "rigid3d_taylor_wall": ("rigid_taylor_3d", dict(steps=40, friction=0.0, normals=2)),
+    "rigid3d_taylor_wall_fric_usl": ("rigid_taylor_3d", dict(steps=40, friction=0.3, normals=0, method=3)),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")
