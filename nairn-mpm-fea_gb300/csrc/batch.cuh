@@ -71,6 +71,7 @@ struct BatchRun {
     long long node_base = 0, nnodes = 0, cell_base = 0, nelems = 0, mat_base = 0, nmat = 0;
     int steps_total = 0, steps_done = 0;
     bool lr = false;               // regression contact normals (methods 5, 6)
+    bool rigid = false;            // rigid contact materials
     std::vector<MpmGpuVelBC> bcs;  // batch-global 1-based node numbers
 };
 
@@ -214,6 +215,7 @@ struct MpmGpuBatch {
     double *lr_out = nullptr;
     long long lr_cap = 0;
     int lr_runs = 0;  // resident runs with regression normals
+    int rigid_runs = 0;  // resident runs with rigid contact materials
     // PeriodicXPIC expansion columns (xpic_order > 1)
     DevXpic xpic{};
     double *xpic_block = nullptr;
@@ -404,6 +406,7 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     sp.ct.nf = b->nf;
     sp.ct.fstride = b->ncap;
     sp.ct.lr = b->lr_out;
+    sp.ct.rigid = b->rigid_runs > 0 ? 1u : 0u;  // some particle may be rigid (the runs' masks are per run)
     k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN, b->nf, b->ncap);
     // mixed mode, one material field, window shape functions: the scatters
     // accumulate in shared-memory node tiles (each block's runs beyond its
@@ -843,6 +846,13 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     const bool mm = contact && contact->enabled;
     if (maxfield > 0 && !mm)
         return berr(b, MPMGPU_ERR_INVALID, "a run with several material fields needs multimaterial contact");
+    unsigned rigid = 0u;  // the run's rigid contact fields
+    for (int i = 0; i < nmat; i++)
+        if (dm[i].type == kMatRigid) rigid |= 1u << dm[i].field;
+    if (rigid && (!mm || maxfield < 1))
+        return berr(b, MPMGPU_ERR_UNSUPPORTED, "rigid contact materials need multimaterial contact");
+    if (rigid && contact->normals >= 5)
+        return berr(b, MPMGPU_ERR_UNSUPPORTED, "regression normals with rigid materials are not implemented");
     if (mm) {
         if (b->nf < 2) return berr(b, MPMGPU_ERR_INVALID, "contact needs a batch with max_fields >= 2");
         if (contact->normals < 0 || (contact->normals > 2 && contact->normals < 5) || contact->normals > 6)
@@ -932,6 +942,11 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     R.normals = mm ? contact->normals : 2;
     R.friction = mm ? contact->friction : 0.;
     R.style = !mm ? 2 : (contact->friction < 0. ? 0 : (contact->friction == 0. ? 1 : 2));
+    R.rigid = rigid;
+    {
+        const double bias = mm && contact->rigid_gradient_bias > 0. ? contact->rigid_gradient_bias : 1.;
+        R.rigid_bias = bias * bias;  // MeshInfo::rigidGradientBias, squared
+    }
     R.xpic = xpic_mode(b->o.xpic_order, b->o.xpic_fmpm, b->o.xpic_period, 1);  // its first step
     BCK(cudaMemcpyAsync(b->runs_dev + r, &R, sizeof(DevRun), cudaMemcpyHostToDevice, s));
     unsigned bad = 0;
@@ -951,6 +966,8 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
     br.state = MPMGPU_RUN_RUNNING;
     br.lr = mm && contact->normals >= 5;
     b->lr_runs += br.lr ? 1 : 0;
+    br.rigid = rigid != 0u;
+    b->rigid_runs += br.rigid ? 1 : 0;
     br.bcs.reserve((size_t)nbc);
     for (int k = 0; k < nbc; k++) {
         MpmGpuVelBC bc = bcs[k];
@@ -1043,6 +1060,7 @@ int mpmgpu_batch_remove_run(MpmGpuBatch *b, int32_t run_id, MpmGpuParticles *out
     b->matslots.release(br.mat_base, br.nmat);
     b->node_used = (int)b->nodes.high_water();
     b->lr_runs -= br.lr ? 1 : 0;
+    b->rigid_runs -= br.rigid ? 1 : 0;
     br = BatchRun{};
     b->bcs_dirty = true;
     b->layout++;

@@ -15,6 +15,8 @@ enum : unsigned { ERR_NAN = 1u, ERR_LEFT_GRID = 2u, ERR_EDGE = 4u, ERR_CPDI_NODE
 
 // material type ids (MaterialController.cpp:105-231)
 constexpr int kMatIsotropic = 1, kMatIsoPlasticity = 9, kMatNeohookean = 28;
+// rigid contact material (RigidMaterial in multimaterial mode, RigidMaterial.hpp:14)
+constexpr int kMatRigid = 35;
 
 struct DevGrid {
     int dim, nx, ny, nz;
@@ -86,6 +88,8 @@ struct DevContact {
     int style;       // CoulombFriction: 0 stick, 1 frictionless, 2 frictional
     double friction; // Coulomb coefficient
     const double *lr;  // regression normals (5, 6): 4 per field-node (n, deln)
+    unsigned rigid;    // bit f set: field f holds a rigid contact material (MatVelocityField::IsRigidField)
+    double rigid_bias; // MeshInfo::rigidGradientBias, squared (MeshInfo.cpp:1191)
 };
 
 // Deterministic node sums (MPMGPU_P2G_DETERMINISTIC): three 64-bit integer
@@ -115,6 +119,8 @@ struct DevRun {
     int normals, style;
     double friction;   // the run's contact law (DevContact fields)
     int xpic;          // this step's PeriodicXPIC mode (0 FLIP, k FMPM(k), -k XPIC(k))
+    unsigned rigid;    // the run's rigid contact fields (DevContact::rigid)
+    double rigid_bias;
 };
 
 // PeriodicXPIC::PrepareForStep / StepCalculation (NairnMPM/src/Custom_Tasks/

@@ -96,6 +96,12 @@ int nmg::derive_material(const MpmGpuMaterial &in, int np, DevMat &m, std::strin
         m.uj = in.UJOption;
         return MPMGPU_OK;
     }
+    if (in.type == MPMGPU_MAT_RIGID_CONTACT) {
+        // RigidMaterial::VerifyAndLoadProperties (RigidMaterial.cpp:44-66): rho = 1,
+        // so a particle's mass is its volume (mm^3); no mechanical properties
+        m.rho = 1.;
+        return MPMGPU_OK;
+    }
     if (in.type != MPMGPU_MAT_ISOTROPIC && in.type != MPMGPU_MAT_ISOPLASTICITY) {
         why = "material type " + std::to_string(in.type) + " is not implemented on the device";
         return MPMGPU_ERR_UNSUPPORTED;
@@ -439,6 +445,9 @@ int mpmgpu_set_contact(MpmGpuCtx *c, const MpmGpuContact *contact) {
     c->ct.normals = contact->normals;
     c->ct.friction = contact->friction;
     c->ct.style = contact->friction < 0. ? 0 : (contact->friction == 0. ? 1 : 2);
+    // MeshInfo::rigidGradientBias (default 1), squared (MeshInfo.cpp:44, 1191)
+    const double bias = contact->rigid_gradient_bias > 0. ? contact->rigid_gradient_bias : 1.;
+    c->ct.rigid_bias = bias * bias;
     c->contact_on = true;
     return MPMGPU_OK;
 }
@@ -628,6 +637,17 @@ int step_impl(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
     if (c->p.n <= 0 || !c->mats) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step: no particles or materials");
     if (c->ct.nf > 1 && !c->contact_on)
         return set_err(c, MPMGPU_ERR_INVALID, "several material fields need multimaterial contact (mpmgpu_set_contact)");
+    // rigid contact materials: the fields they occupy, and the options they work with
+    c->ct.rigid = 0u;
+    for (const DevMat &m : c->hmats)
+        if (m.type == kMatRigid) c->ct.rigid |= 1u << m.field;
+    if (c->ct.rigid) {
+        if (c->ct.nf < 2 || !c->contact_on)
+            return set_err(c, MPMGPU_ERR_UNSUPPORTED,
+                           "rigid contact materials need multimaterial contact (RigidMaterial::SetField)");
+        if (c->ct.normals >= 5)
+            return set_err(c, MPMGPU_ERR_UNSUPPORTED, "regression normals with rigid materials are not implemented");
+    }
     for (auto &pr : c->prof) pr.ms = 0.;
     if (c->profile && ensure_events(c, nsteps) != 0) return set_err(c, MPMGPU_ERR_CUDA, "event creation failed");
     if (c->ct.nf > 1 && c->ct.normals >= 5) {

@@ -1102,6 +1102,13 @@ __device__ __forceinline__ int field_offset(const StepParams &sp, const DevMat *
     return sp.ct.nf > 1 ? mats[p.mat[i]].field * sp.ct.fstride : 0;
 }
 
+// particle i is of a rigid contact material (MaterialBase::IsRigid); only
+// asked when some field of the step is rigid
+__device__ __forceinline__ bool particle_rigid(const StepParams &sp, const DevMat *mats, const DevParticles &p,
+                                               int i) {
+    return sp.ct.rigid != 0u && mats[p.mat[i]].type == kMatRigid;
+}
+
 // particle volume for contact (MatPoint2D/3D::GetVolume with DEFORMED_AREA,
 // MatPoint2D.cpp:407-417, MatPoint3D.cpp:395-408): det F * mp / rho, the 2D
 // form without F_zz
@@ -1570,6 +1577,9 @@ static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_for
     if (i >= p.n) return;
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
+    // rigid particles have no strain update and no internal force
+    // (UpdateStrainsFirstTask.cpp:123, GridForcesTask.cpp:53)
+    if (particle_rigid(sp, mats, p, i)) return;
     const DevGrid &g = rv.g;
     const int off = field_offset(sp, mats, p, i);
     if (STRAIN) {
@@ -1654,7 +1664,7 @@ static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_for
 template <int DIM, int SHAPE, bool MIX>
 static __global__ void __launch_bounds__(256) k_det_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+    if (i >= p.n || particle_rigid(sp, mats, p, i)) return;
     forces_scatter<DIM, SHAPE, MIX, true>(sp, p, nd, i, sp.g, 0, field_offset(sp, mats, p, i));
 }
 
@@ -1822,6 +1832,16 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
         if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
         else for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, fn);
     };
+    if (particle_rigid(sp, mats, p, i)) {
+        // rigid materials move at their current velocity and do not take part
+        // in the second extrapolation (UpdateParticlesTask.cpp:291-295,
+        // MatPoint2D/3D::MovePosition, UpdateStrainsLastContactTask.cpp:90)
+        p.x[i] += rv.dt * p.vx[i];
+        p.y[i] += rv.dt * p.vy[i];
+        if (DIM == 3) p.z[i] += rv.dt * p.vz[i];
+        if (!USL) reset_element<DIM>(g, p, i, rv.err);
+        return;
+    }
     double v[3], xp[3];
     g2p_move<DIM, SHAPE, MIX, BATCH>(sp, p, nd, i, rv, off, v, xp);
     if (USL && DET) {
@@ -1930,7 +1950,7 @@ template <int DIM, int SHAPE, bool MIX>
 static __global__ void __launch_bounds__(256) k_det_usl(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
-    if (i >= p.n) return;
+    if (i >= p.n || particle_rigid(sp, mats, p, i)) return;  // non-rigid particles only
     const DevGrid &g = sp.g;
     const int off = field_offset(sp, mats, p, i);
     const bool mm = sp.ct.nf > 1;
@@ -1980,9 +2000,11 @@ static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_las
     if (i >= p.n) return;
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
-    double du[9];
-    velocity_gradient<DIM, SHAPE, MIX>(rv.g, rv.nb, p, nd, i, rv.st_last, du, field_offset(sp, mats, p, i));
-    constitutive<DIM>(mats, p, i, du);
+    if (!particle_rigid(sp, mats, p, i)) {
+        double du[9];
+        velocity_gradient<DIM, SHAPE, MIX>(rv.g, rv.nb, p, nd, i, rv.st_last, du, field_offset(sp, mats, p, i));
+        constitutive<DIM>(mats, p, i, du);
+    }
     reset_element<DIM>(rv.g, p, i, rv.err);
 }
 
@@ -2086,9 +2108,14 @@ __device__ __forceinline__ DevContact node_contact_params(const StepParams &sp, 
         ct.normals = R.normals;
         ct.style = R.style;
         ct.friction = R.friction;
+        ct.rigid = R.rigid;
+        ct.rigid_bias = R.rigid_bias;
     }
     return ct;
 }
+
+// field f of the node's contact holds a rigid contact material
+__device__ __forceinline__ bool rigid_field(const DevContact &ct, int f) { return ((ct.rigid >> f) & 1u) != 0u; }
 
 // ---------------------------------------------------------------------------
 // multimaterial contact
@@ -2164,6 +2191,74 @@ __device__ __forceinline__ bool coulomb_delta(const DevContact &ct, double delPi
 // (GetNormalVector :960-1069, methods 0-2), separation from the extrapolated
 // displacements (CrackSurfaceContact::MaterialSeparation), Coulomb friction.
 constexpr int kMaxFields = 8;
+// CrackVelocityFieldMulti::RigidMaterialContactOnCVF (CrackVelocityFieldMulti.cpp:676-958)
+// for the Coulomb law: every non-rigid field of the node moves toward the
+// velocity of the rigid field rf (whose own momentum never changes), with
+// mred = the field's mass and, after the momentum update, dF = -F; the normal
+// is GetNormalVector's with a rigid partner (:960-1030), the rigid volume
+// gradient preferred by the squared bias; the separation comes from the
+// displacements (CrackSurfaceContact::MaterialSeparation).
+template <bool MIX>
+__device__ void rigid_contact(const DevContact &ct, const DevNodes &nd, int n, const int *act, int nm, int rf,
+                              double rvol, int pass, double dt) {
+    const int S = ct.fstride, kr = rf * S + n;
+    const double rr = 1. / nd.mass[kr];  // the rigid field's mass is its volume
+    const double rvel[3] = {nd.px[kr] * rr, nd.py[kr] * rr, nd.pz[kr] * rr};
+    const double gradj[3] = {-cterm<MIX>(nd.gvx, kr), -cterm<MIX>(nd.gvy, kr), -cterm<MIX>(nd.gvz, kr)};
+    const double dispR[3] = {nd.dsx[kr] * rr, nd.dsy[kr] * rr, nd.dsz[kr] * rr};
+    for (int q = 0; q < nm; q++) {
+        const int f = act[q];
+        if (rigid_field(ct, f)) continue;
+        const int ki = f * S + n;
+        const double massi = nd.mass[ki], voli = cterm<MIX>(nd.vol, ki);
+        double delPi[3] = {rvel[0] * massi - nd.px[ki], rvel[1] * massi - nd.py[ki], rvel[2] * massi - nd.pz[ki]};
+        const double normi[3] = {cterm<MIX>(nd.gvx, ki), cterm<MIX>(nd.gvy, ki), cterm<MIX>(nd.gvz, ki)};
+        double norm[3];
+        if (ct.normals == 0) {
+            const double magi = sqrt(dot3(normi, normi)), magj = sqrt(dot3(gradj, gradj));
+            const bool useI = magi >= ct.rigid_bias * magj;
+            const double s = 1. / (useI ? magi : magj);
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] = (useI ? normi[a] : gradj[a]) * s;
+        } else if (ct.normals == 1) {
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] = voli >= rvol ? normi[a] : gradj[a];
+            const double s = 1. / sqrt(dot3(norm, norm));
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] *= s;
+        } else {
+#pragma unroll
+            for (int a = 0; a < 3; a++) norm[a] = normi[a] + gradj[a];
+            const double magi = dot3(norm, norm), magj = dot3(gradj, gradj);
+            const double vRatio = (voli + rvol) / rvol;
+            if (magi >= ct.rigid_bias * magj * vRatio * vRatio) {
+                const double s = 1. / sqrt(magi);
+#pragma unroll
+                for (int a = 0; a < 3; a++) norm[a] *= s;
+            } else {
+                const double s = 1. / sqrt(magj);
+#pragma unroll
+                for (int a = 0; a < 3; a++) norm[a] = gradj[a] * s;
+            }
+        }
+        if (norm[0] != norm[0] || norm[1] != norm[1] || norm[2] != norm[2]) continue;
+        const double dotn = dot3(delPi, norm);
+        const double rmi = 1. / massi;
+        const double dispi[3] = {nd.dsx[ki] * rmi, nd.dsy[ki] * rmi, nd.dsz[ki] * rmi};
+        const double deln = dot3(dispR, norm) - dot3(dispi, norm);
+        double delFi[3];
+        const double *dfp = nullptr;
+        if (pass == BC_UPDATE_MOMENTUM) {
+            delFi[0] = -nd.fx[ki];
+            delFi[1] = -nd.fy[ki];
+            delFi[2] = -nd.fz[ki];
+            dfp = delFi;
+        }
+        if (!coulomb_delta(ct, delPi, norm, dotn, deln, massi, dfp, dt)) continue;
+        change_momentum(nd, ki, delPi, pass, dt);
+    }
+}
+
 template <bool MIX>
 __device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, int pass, double dt) {
     const int S = ct.fstride;
@@ -2183,6 +2278,25 @@ __device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, in
         act[nm++] = f;
     }
     if (nm <= 1) return;
+    if (ct.rigid) {
+        // a rigid field at the node: contact against it alone (the one with
+        // the largest contact volume when several), CrackVelocityFieldMulti::
+        // MaterialContactOnCVF (CrackVelocityFieldMulti.cpp:302-347, 688-706)
+        int rf = -1;
+        double rvol = 0.;
+        for (int q = 0; q < nm; q++) {
+            if (!rigid_field(ct, act[q])) continue;
+            const double v = cterm<MIX>(nd.vol, act[q] * S + n);
+            if (rf < 0 || v > rvol) {
+                rf = act[q];
+                rvol = v;
+            }
+        }
+        if (rf >= 0) {
+            rigid_contact<MIX>(ct, nd, n, act, nm, rf, rvol, pass, dt);
+            return;
+        }
+    }
     const bool pairs = nm == 2;
     const int miMax = pairs ? 1 : nm;
     const double rMc = 1. / Mc;
@@ -2325,16 +2439,15 @@ static __global__ void k_node_post(StepParams sp, DevNodes nd, int nnodes, DevBC
         nd.cy[k] = nd.py[k];
         if (DIM == 3) nd.cz[k] = nd.pz[k];
     }
-    {
-        const DevContact ct = node_contact_params<BATCH>(sp, n);
-        if (ct.nf > 1) node_contact<MIX>(ct, nd, n, BC_MASS_MOMENTUM, dt);
-    }
+    const DevContact ct = node_contact_params<BATCH>(sp, n);
+    if (ct.nf > 1) node_contact<MIX>(ct, nd, n, BC_MASS_MOMENTUM, dt);
     for (int f = 0; f < sp.ct.nf; f++) {
         const int k = f * sp.ct.fstride + n;
         if (!nd.active[k]) continue;
         double p[3] = {nd.px[k], nd.py[k], DIM == 3 ? nd.pz[k] : 0.};
         const double m = nd.mass[k];
-        if (do_bcs && grp >= 0) {
+        // velocity conditions apply to the non-rigid fields only (CrackVelocityFieldMulti.cpp:1243-1259)
+        if (do_bcs && grp >= 0 && !rigid_field(ct, f)) {
             double fz[3] = {0., 0., 0.};
             node_bcs(b, grp, BC_MASS_MOMENTUM, m, t, dt, p, fz);
             nd.px[k] = p[0];
@@ -2381,7 +2494,8 @@ static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, Dev
             fr[2] = DIM == 3 ? nd.fz[k] : 0.;
         }
         const double m = nd.mass[k];
-        if (grp >= 0) node_bcs(b, grp, BC_GRID_FORCES, m, t, dt, p, fr);
+        const bool rigid = rigid_field(ct, f);  // no forces, no conditions: its momentum stays as extrapolated
+        if (grp >= 0 && !rigid) node_bcs(b, grp, BC_GRID_FORCES, m, t, dt, p, fr);
 #pragma unroll
         for (int a = 0; a < 3; a++) p[a] += fr[a] * dt;
         if (mm) {
@@ -2406,9 +2520,17 @@ static __global__ void k_node_update(StepParams sp, DevNodes nd, int nnodes, Dev
         if (!nd.active[k]) continue;
         double p[3] = {nd.px[k], nd.py[k], nd.pz[k]}, fr[3] = {nd.fx[k], nd.fy[k], nd.fz[k]};
         const double m = nd.mass[k];
-        if (grp >= 0) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, fr);
+        const bool rigid = rigid_field(ct, f);
+        if (grp >= 0 && !rigid) node_bcs(b, grp, BC_UPDATE_MOMENTUM, m, t, dt, p, fr);
         node_finish_update<DIM, MIX>(nd, k, m, p, fr);
-        if (zero_contact) {
+        if (zero_contact && rigid) {
+            // a rigid field keeps its momentum, volume and volume gradient for the
+            // second extrapolation; its displacement moves by p dt
+            // (CrackVelocityFieldMulti::RezeroNodeTask6, :157-176)
+            nd.dsx[k] += p[0] * dt;
+            nd.dsy[k] += p[1] * dt;
+            nd.dsz[k] += p[2] * dt;
+        } else if (zero_contact) {
             cterm_set<MIX>(nd.vol, k, 0.);
             nd.dsx[k] = nd.dsy[k] = nd.dsz[k] = 0.;
             cterm_set<MIX>(nd.gvx, k, 0.);
@@ -2433,7 +2555,7 @@ static __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs
     if (mm) {
         for (int f = 0; f < sp.ct.nf; f++) {
             const int k = f * sp.ct.fstride + n;
-            if (!nd.active[k]) continue;
+            if (!nd.active[k] || rigid_field(ct, f)) continue;  // rigid: the first extrapolation's momentum
             nd.px[k] = nd.ux[k];
             nd.py[k] = nd.uy[k];
             nd.pz[k] = nd.uz[k];
@@ -2454,7 +2576,7 @@ static __global__ void k_node_usl(StepParams sp, DevNodes nd, int nnodes, DevBCs
             p[2] = DIM == 3 ? nd.uz[k] : 0.;
         }
         const double m = nd.mass[k];
-        if (grp >= 0) {
+        if (grp >= 0 && !rigid_field(ct, f)) {
             double fz[3] = {0., 0., 0.};
             node_bcs(b, grp, BC_UPDATE_STRAINS_LAST, m, t, dt, p, fz);
         }
@@ -2493,6 +2615,9 @@ static __global__ void k_det_resolve(StepParams sp, DevNodes nd, int nn, int pha
         return;
     }
     const bool usl = phase == 2;
+    // a rigid field has no second extrapolation: it keeps the first one's
+    // momentum and contact terms (its limbs of this phase stay zero)
+    if (usl && sp.ct.rigid && ((sp.ct.rigid >> (n / sp.ct.fstride)) & 1u)) return;
     if (usl) {
         nd.ux[n] = take2(DQ_UX, DB_UMOM);
         nd.uy[n] = take2(DQ_UY, DB_UMOM);

@@ -11,7 +11,7 @@ import tempfile
 import numpy as np
 import pytest
 
-from conftest import golden_cases, load_golden, model_for, rel_l2
+from conftest import contact_tolerance, golden_cases, load_golden, model_for, rel_l2
 
 ORDER = "iYYYYYNYNYNNNYNNNN"  # the golden archives' MPMArchiveOrder
 
@@ -60,7 +60,8 @@ def test_packer_matches_reference_archives(case):
     meta, g = load_golden(case)
     m = model_for(meta)
     p = abi.copy_particles(m.particles)
-    oracle_lib.run(m, p, meta["steps"], nthreads=4)
+    # one thread: the reference's summation order (some contact runs are chaotic)
+    oracle_lib.run(m, p, meta["steps"], nthreads=1)
     three_d = m.grid.dim == 3
     rec = np.frombuffer(archive.pack_records(p, m.materials, ORDER, three_d), archive.record_dtype(ORDER, three_d))
     for k in ("elem", "mass", "mat", "origpos"):
@@ -95,11 +96,16 @@ def test_device_archive_matches_reference_archive(case, gpu_lib):
         a = archive.read_archive(path)
     for k in ("elem", "mass", "mat", "origpos"):
         assert np.array_equal(a[k], g["final_" + k]), k
+    ctol = contact_tolerance(case, m, 1e-10)
+    chaotic = ctol["vel"] > 1e-10
     for k in ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1"):
         if np.abs(g["final_" + k]).max() == 0.:
             assert np.abs(a[k]).max() == 0., k
             continue
-        assert rel_l2(a[k], g["final_" + k]) <= 1e-10, (k, rel_l2(a[k], g["final_" + k]))
+        # a run chaotic in the reference itself: its own sensitivity bounds the
+        # archived quantities (energies and history follow stress and strain)
+        tol = ctol.get(k, max(ctol["stress"], ctol["strain"]) if chaotic else 1e-10)
+        assert rel_l2(a[k], g["final_" + k]) <= tol, (k, rel_l2(a[k], g["final_" + k]), tol)
 
 
 @pytest.mark.gpu

@@ -368,3 +368,33 @@ def test_batched_xpic_refused_with_contact(gpu_lib):
     with pytest.raises(GpuError, match="UNSUPPORTED"):
         GpuBatch(model.PLANE_STRAIN, model.USAVG, model.SHAPE_UGIMP, max_runs=2, max_particles=1000,
                  max_nodes=1000, max_fields=2, xpic=(2, 0, 1))
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
+@pytest.mark.parametrize("case", ["rigid2d_indent_fric", "rigid3d_taylor_wall"])
+def test_batched_rigid_contact_matches_reference(case, precision, tol, gpu_lib):
+    """A run with a rigid contact material shares a batch with a contact run
+    of deformable materials only: the first matches the reference's golden
+    result, the second the oracle."""
+    from conftest import contact_tolerance, load_golden, model_for, view_for
+    from nairn_gb300 import abi, model
+    from nairn_gb300.gpu import GpuBatch
+    meta, g = load_golden(case)
+    m = model_for(meta)
+    steps = meta["steps"]
+    if m.grid.dim == 2:
+        other = model.contact_2d(steps=steps, friction=0.3, normals=2)
+    else:
+        other = model.contact_3d(steps=steps, friction=0.3, normals=2, gimp="uGIMP")
+    b = GpuBatch.for_models([other, m], precision=precision)
+    ids = [b.add(other), b.add(m)]
+    b.step(steps)
+    assert b.state(ids[1]) == (abi.RUN_FINISHED, steps)
+    v = view_for(b.download(ids[1]), m)
+    ctol = contact_tolerance(case, m, tol)
+    for k in ("pos", "vel", "stress", "strain"):
+        assert rel_l2(v[k], g["final_" + k]) <= ctol[k], (k, rel_l2(v[k], g["final_" + k]), ctol[k])
+    out, ref = b.download(ids[0]), oracle(other, steps)
+    for k in ("x", "y", "vx", "vy", "sxx", "syy", "sxy"):
+        assert rel_l2(out[k], ref[k]) <= tol, (k, rel_l2(out[k], ref[k]))
+    b.close()

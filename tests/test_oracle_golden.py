@@ -129,3 +129,28 @@ def test_b2spline_goldens_are_not_ugimp_runs():
         p = {k: np.array(v, copy=True) for k, v in m.particles.items()}
         oracle_lib.run(m, p, meta["steps"], nthreads=1)
         assert rel_l2(view_for(p, m)["stress"], g["final_stress"]) > 1e-3, case
+
+
+def test_oracle_rigid_material_options():
+    """Rigid contact materials need multimaterial contact and are refused with
+    regression normals, as on the device; the rigid particles keep their
+    velocity and move by it, and the golden cases exercise the contact (the
+    plate under the indenter moves)."""
+    import oracle_lib
+    from nairn_gb300 import abi, model
+    m = model.rigid_contact_2d(steps=5)
+    rigid = m.particles["mat"] == 1
+    p = abi.copy_particles(m.particles)
+    oracle_lib.run(m, p, 60, nthreads=1)
+    dt = m.options["timestep"]
+    assert np.array_equal(p["vy"][rigid], m.particles["vy"][rigid])
+    assert np.allclose(p["y"][rigid], m.particles["y"][rigid] + 60 * dt * m.particles["vy"][rigid], rtol=0, atol=1e-12)
+    assert np.abs(p["vy"][~rigid]).max() > 100.
+    bad = abi.copy_particles(m.particles)
+    ct = abi.contact_struct(m)
+    ct.normals = 6
+    with pytest.raises(RuntimeError, match="rigid"):
+        oracle_lib.run(m, bad, 1, nthreads=1, contact=ct)
+    ct.enabled = 0
+    with pytest.raises(RuntimeError):
+        oracle_lib.run(m, bad, 1, nthreads=1, contact=ct)
