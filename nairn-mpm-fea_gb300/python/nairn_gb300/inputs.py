@@ -327,11 +327,12 @@ def rigid_contact_2d(plate=(20, 4), indenter=(6, 3), indenter_x0=7.0, gap=0.5, c
 
 def rigid_taylor_3d(radius: float = 1.0, length: float = 2.0, cell: float = 0.5, ppc_side: int = 2,
                     v0: float = -200000., E: float = 200000., nu: float = 0.3, yield_: float = 300.,
-                    Ep: float = 2000., rho: float = 7.8, slab_cells: int = 2, friction: float = 0.0,
+                    Ep: float = 2000., rho: float = 7.8, slab_cells: int = 2, vx0: float = 0., friction: float = 0.0,
                     normals: int = 2, steps: int = 40, cfl: float = 0.5, gimp: str = "uGIMP", method: int = 2,
                     archive_root: str = "Results/rtaylor.", inc_terms: int = 0) -> tuple[str, dict]:
     """The Taylor impact with a rigid wall made of particles: the bar
-    (von Mises, linear hardening) moving at v0 (mm/s) onto a stationary slab of
+    (von Mises, linear hardening) moving at v0 (mm/s; vx0 along x for an
+    oblique impact) onto a stationary slab of
     rigid contact material (type 35) occupying -slab_cells*cell <= z <= 0,
     in place of the zero-velocity grid condition on the z = 0 plane;
     multimaterial contact with Coulomb friction."""
@@ -351,7 +352,7 @@ def rigid_taylor_3d(radius: float = 1.0, length: float = 2.0, cell: float = 0.5,
     </Grid>
   </Mesh>
   <MaterialPoints>
-    <Body mat="1" angle="0" vx="0" vy="0" vz="{_fmt(v0)}">
+    <Body mat="1" angle="0" vx="{_fmt(vx0)}" vy="0" vz="{_fmt(v0)}">
       <Cylinder xmin="{_fmt(-radius)}" xmax="{_fmt(radius)}" ymin="{_fmt(-radius)}" ymax="{_fmt(radius)}" zmin="0" zmax="{_fmt(length)}" axis="z"/>
     </Body>
     <Body mat="2" angle="0" vx="0" vy="0" vz="0">

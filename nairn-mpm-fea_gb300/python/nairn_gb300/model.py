@@ -716,7 +716,7 @@ def rigid_contact_2d(plate=(20, 4), indenter=(6, 3), indenter_x0=7.0, gap=0.5, c
 
 
 def rigid_taylor_3d(radius=1.0, length=2.0, cell=0.5, ppc_side=2, v0=-200000., E=200000., nu=0.3, yield_=300.,
-                    Ep=2000., rho=7.8, slab_cells=2, friction=0.0, normals=2, steps=40, cfl=0.5, gimp="uGIMP",
+                    Ep=2000., rho=7.8, slab_cells=2, vx0=0., friction=0.0, normals=2, steps=40, cfl=0.5, gimp="uGIMP",
                     method=USAVG, inc_terms=0, **_ignored) -> Model:
     """Model of inputs.rigid_taylor_3d (same arguments): the bar in material
     field 0, the stationary rigid slab (z in [-slab_cells*cell, 0]) in field 1,
@@ -742,7 +742,7 @@ def rigid_taylor_3d(radius=1.0, length=2.0, cell=0.5, ppc_side=2, v0=-200000., E
     bm = _material(MAT_PLASTIC, rho, E=E, nu=nu, yield_=yield_, Ep=Ep)
     rm = _rigid_material()
     bm["field"], rm["field"] = 0, 1
-    p = _concat([_body_particles(g, pos, elem, in_bar, ppc_side, bm, 0, (0., 0., v0)),
+    p = _concat([_body_particles(g, pos, elem, in_bar, ppc_side, bm, 0, (vx0, 0., v0)),
                  _body_particles(g, pos, elem, in_slab, ppc_side, rm, 1, (0., 0., 0.))])
     bcs = np.zeros(0, dtype=BC_DTYPE)
     c = inputs.wave_speed(MAT_PLASTIC, rho, E=E, nu=nu)

@@ -77,7 +77,7 @@ def contact_sensitivity(case):
         from nairn_gb300 import abi
         meta, _ = load_golden(case)
         m = model_for(meta)
-        keys = ("pos", "vel", "stress", "strain")
+        keys = ("pos", "vel", "stress", "strain", "plastic", "hist1")
 
         def final(seed):
             p = abi.copy_particles(m.particles)
@@ -100,7 +100,7 @@ def contact_tolerance(case, m, tol):
     decisions that sit on near-zero separations, so that a 1e-9 perturbation
     of the input moves the result by more than 1e-6 -- which is held to twice
     that movement (any other summation order moves it as much)."""
-    keys = ("pos", "vel", "stress", "strain")
+    keys = ("pos", "vel", "stress", "strain", "plastic", "hist1")
     if not (m.extra and m.extra.get("contact")):
         return {k: tol for k in keys}
     sens = contact_sensitivity(case)

@@ -111,12 +111,17 @@ CASES = {
     "contact2d_b2gimp_fric": ("contact_2d", dict(steps=150, friction=0.3, normals=2, gimp="B2GIMP")),
     # rigid contact materials (type 35): a rigid indenter moving at constant
     # velocity into an elastic plate, and the Taylor bar onto a rigid slab
-    "rigid2d_indent_fric": ("rigid_contact_2d", dict(steps=150, friction=0.3, normals=2)),
+    # (an off-centre indenter sliding as it presses, and an oblique impact:
+    # with a symmetric normal approach the stick/slip decision sits on a
+    # near-zero tangential momentum and the reference's run is chaotic)
+    "rigid2d_indent_fric": ("rigid_contact_2d", dict(steps=150, friction=0.3, normals=2, v=(1500., -2000.),
+                                                     indenter_x0=5.0)),
     "rigid2d_indent_maxg_usl": ("rigid_contact_2d", dict(steps=120, friction=0.0, normals=0, method=3)),
     "rigid2d_indent_maxv_stick": ("rigid_contact_2d", dict(steps=120, friction=-1.0, normals=1, v=(1000., -1500.))),
     "rigid2d_indent_cpdi_usf": ("rigid_contact_2d", dict(steps=120, friction=0.3, normals=2, gimp="lCPDI", method=0)),
     "rigid3d_taylor_wall": ("rigid_taylor_3d", dict(steps=40, friction=0.0, normals=2)),
-    "rigid3d_taylor_wall_fric_usl": ("rigid_taylor_3d", dict(steps=40, friction=0.3, normals=0, method=3)),
+    "rigid3d_taylor_wall_fric_usl": ("rigid_taylor_3d", dict(steps=40, friction=0.3, normals=0, method=3,
+                                                             vx0=40000.)),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")
