@@ -160,9 +160,9 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
     const int n0 = nb + zr * g.zplane + row * g.yplane + col;  // first node (global index)
     // reciprocal element sizes, formed once (a gradient times 1/dx differs from
     // the reference's quotient by rounding only)
-    const T iDX = T(1) / (T)(g.xn[col + 1] - g.xn[col]);
-    const T iDY = T(1) / (T)(g.yn[row + 1] - g.yn[row]);
-    const T iDZ = DIM == 3 ? T(1) / (T)(g.zn[zr + 1] - g.zn[zr]) : T(1);
+    const T iDX = GRAD ? T(1) / (T)(g.xn[col + 1] - g.xn[col]) : T(0);
+    const T iDY = GRAD ? T(1) / (T)(g.yn[row + 1] - g.yn[row]) : T(0);
+    const T iDZ = GRAD && DIM == 3 ? T(1) / (T)(g.zn[zr + 1] - g.zn[zr]) : T(0);
     const T xi = (T)xi_d, eta = (T)eta_d, zeta = (T)zeta_d;
     if (SHAPE == SHAPE_LINEAR) {
         if (DIM == 2) {
@@ -801,8 +801,9 @@ __device__ __forceinline__ void axis_windows(const DevGrid &g, int col, int row,
                                              AxisWin<SHAPE, T> &w) {
     static_assert(SHAPE != SHAPE_LCPDI, "lCPDI nodes do not form a window");
     const T xi = (T)xi_d, eta = (T)eta_d, zeta = (T)zeta_d;
-    const T iD[3] = {T(1) / (T)(g.xn[col + 1] - g.xn[col]), T(1) / (T)(g.yn[row + 1] - g.yn[row]),
-                     DIM == 3 ? T(1) / (T)(g.zn[zr + 1] - g.zn[zr]) : T(1)};
+    const T iD[3] = {GRAD ? T(1) / (T)(g.xn[col + 1] - g.xn[col]) : T(0),
+                     GRAD ? T(1) / (T)(g.yn[row + 1] - g.yn[row]) : T(0),
+                     GRAD && DIM == 3 ? T(1) / (T)(g.zn[zr + 1] - g.zn[zr]) : T(0)};
     const int cc[3] = {col, row, zr};
     const T nat[3] = {xi, eta, zeta};
     w.c[2] = 0;
