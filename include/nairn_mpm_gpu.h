@@ -449,12 +449,31 @@ typedef struct {
                                    particles than this (0: no cap); a request
                                    is always admitted when nothing runs      */
     int32_t order;              /* admission order: 0 arrival (FIFO), 1 least
-                                   work first (particles x steps)            */
+                                   work first (particles x steps), 2 deadline:
+                                   least work first, a request admitted only
+                                   while every running request's predicted
+                                   latency stays within slowdown_target times
+                                   its predicted time alone, and while the
+                                   resident particles of its dimension stay
+                                   within the load at which the fitted step
+                                   time reaches 90 % of the batch's asymptotic
+                                   throughput (see below)                    */
     int32_t max_fields;         /* material velocity fields per run (0: 1)     */
     int32_t lr_links;           /* links per particle slot for regression normals
                                    (MpmGpuBatchOptions; capped at 16 in 2D)   */
     int32_t xpic_order, xpic_fmpm, xpic_period;  /* PeriodicXPIC of every request
                                    (MpmGpuBatchOptions)                       */
+    double slowdown_target;     /* order 2: the bound k (0: 4).  The server fits
+                                   step time = a + b x resident particles per
+                                   dimension from CUDA-event timings of its
+                                   rounds; a request of n particles and s steps
+                                   takes s (a + b n) alone.  A queued request
+                                   is admitted when nothing runs, or when with
+                                   it resident every running request r (and
+                                   itself) still has elapsed_r + steps_left_r x
+                                   (a + b R) <= k x its time alone; requests
+                                   already past that bound do not block, and a
+                                   queued request past it goes first.        */
 } MpmGpuServerOptions;
 
 enum { MPMGPU_REQ_QUEUED = 1, MPMGPU_REQ_RUNNING = 2, MPMGPU_REQ_DONE = 3, MPMGPU_REQ_FAILED = 4 };
@@ -477,6 +496,19 @@ typedef struct {
 } MpmGpuServerStats;
 
 int mpmgpu_server_create(const MpmGpuServerOptions *opts, MpmGpuServer **out);
+
+/* Extension: the deadline order's admission rule (order 2 above) as a pure
+ * function, for hosts that schedule runs themselves.  a_ms, b_ms: step time
+ * a + b R of R resident particles; running: n, steps_left, elapsed_ms and
+ * steps_total of each running request; (cand_n, cand_steps, cand_waited_ms):
+ * the queued request.  Returns 1 to admit, 0 to wait, or -MPMGPU_ERR_INVALID. */
+typedef struct {
+    int64_t n;
+    int32_t steps_left, steps_total;
+    double elapsed_ms;
+} MpmGpuRunLoad;
+int mpmgpu_server_admits(double a_ms, double b_ms, double slowdown_target, const MpmGpuRunLoad *running,
+                         int32_t nrunning, int64_t cand_n, int32_t cand_steps, double cand_waited_ms);
 /* Queue one run.  The particle arrays of p are borrowed: they must stay valid
  * and unchanged until the request is done or failed; they are read at
  * admission and receive the final state (upload order) at completion.  Grid

@@ -420,10 +420,9 @@ void batch_enqueue_step(MpmGpuBatch *b) {
         k_p2g<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     }
     const bool lr = b->lr_runs > 0;
-    const int lrb = (int)(((long long)NN * 32 + NTB - 1) / NTB);  // a warp per node
-    auto lr_normals = [&]() {
-        k_lr_normals<DIM, true><<<lrb * b->nf, NTB, 0, s>>>(sp, b->p, b->nd, b->mats, b->lr_start,
-                                                                         b->lr_list, b->lr_out, NN, b->lr_cap, 1);
+    auto lr_normals = [&](int supports_only) {
+        k_lr_normals<DIM, true><<<lr_loop_blocks((long long)NN * b->nf, NTB), NTB, 0, s>>>(
+            sp, b->p, b->nd, b->mats, b->lr_start, b->lr_list, b->lr_cnt, b->lr_out, NN, b->lr_cap, 1, supports_only);
     };
     if (lr) {
         // link the particles of regression-normal runs to their contact nodes
@@ -438,8 +437,11 @@ void batch_enqueue_step(MpmGpuBatch *b) {
         cudaMemsetAsync(b->lr_cnt, 0, (size_t)m * sizeof(int), s);
         k_lr_link<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->lr_cnt, b->lr_start, b->lr_list,
                                                            b->lr_cap, 1);
-        k_lr_order<<<lrb, NTB, 0, s>>>(b->lr_start, b->lr_list, b->orig, NN, b->lr_cap);
-        lr_normals();
+        // the nodes with links, listed in b->lr_cnt (no longer needed as the cursor)
+        cudaMemsetAsync(b->lr_cnt + NN, 0, sizeof(int), s);
+        k_lr_compact<<<(NN + TB - 1) / TB, TB, 0, s>>>(b->lr_start, b->lr_cnt, NN);
+        k_lr_order<<<lr_loop_blocks(NN, NTB), NTB, 0, s>>>(b->lr_start, b->lr_list, b->orig, b->lr_cnt, NN, b->lr_cap);
+        lr_normals(0);
     }
     k_node_post<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, method != MPMGPU_USL);
     // PeriodicXPIC expansions: every run whose mode of this step takes part
@@ -447,8 +449,9 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     auto xpic_expand = [&](int phase) {
         k_xpic_init<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, phase);
         for (int k = 2; k <= xo; k++) {
-            k_xpic_pass<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->xpic, phase, k);
-            k_xpic_delta<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, b->bcs, b->bc_group, phase, k);
+            k_xpic_pass<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->xpic, b->mats, phase, k);
+            k_xpic_delta<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, b->bcs, b->bc_group, phase, k,
+                                                            0);
         }
     };
     if (xo > 1 && xf && method != MPMGPU_USL) xpic_expand(XPIC_STRAIN);  // FMPM: first strain update
@@ -468,7 +471,7 @@ void batch_enqueue_step(MpmGpuBatch *b) {
         else
             k_strain_forces<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
     }
-    if (lr) lr_normals();  // the deformed radii changed with the strain update
+    if (lr) lr_normals(1);  // same positions, deformed radii changed with the strain update
     k_node_update<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group,
                                                     b->nf > 1 && method != MPMGPU_USF);
     if (xo > 1) xpic_expand(XPIC_PARTICLE);  // v(k) of the particle update
@@ -483,7 +486,7 @@ void batch_enqueue_step(MpmGpuBatch *b) {
             }
         }
         if (!g2p_done) k_g2p<DIM, SHAPE, true, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
-        if (lr) lr_normals();  // the particles moved
+        if (lr) lr_normals(0);  // the particles moved
         k_node_usl<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group);
         if (xo > 1 && xf) xpic_expand(XPIC_STRAIN);  // FMPM: second strain update
         k_strain_last<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd, b->mats);
@@ -514,7 +517,7 @@ int batch_step_launches(const MpmGpuBatch *b) {
     const int xo = b->o.xpic_order, expand = xo > 1 ? 1 + 2 * (xo - 1) : 0;
     const int strain_updates = (b->o.method != MPMGPU_USL ? 1 : 0) + (usf ? 0 : 1);
     const int expansions = xo > 1 ? 1 + (b->o.xpic_fmpm ? strain_updates : 0) : 0;
-    return (usf ? 7 : 9) + (b->lr_runs > 0 ? 6 + (usf ? 2 : 3) : 0) + expansions * expand;
+    return (usf ? 7 : 9) + (b->lr_runs > 0 ? 7 + (usf ? 2 : 3) : 0) + expansions * expand;
 }
 
 long long batch_graph_key(const MpmGpuBatch *b) {
@@ -681,7 +684,7 @@ int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *o) {
     bytes += N * nf * (int64_t)((nf > 1 ? 26 : 19) * sizeof(double) + 12 * sizeof(float) + 1);
     bytes += N * (int64_t)(2 * sizeof(int) + sizeof(double));
     bytes += (int64_t)o->max_materials * (int64_t)sizeof(DevMat) + (int64_t)o->max_runs * (int64_t)sizeof(DevRun);
-    if (o->xpic_order > 1) bytes += 7 * N * (int64_t)(sizeof(double) + sizeof(float));  // XPIC columns
+    if (o->xpic_order > 1) bytes += N * (int64_t)(7 * sizeof(double) + 6 * sizeof(float));  // XPIC columns
     if (nf > 1 && o->lr_links > 0) {
         // regression-normal links, counts, offsets, scan sums, results
         bytes += P * o->lr_links * (int64_t)sizeof(int) + 2 * (N + 1) * (int64_t)sizeof(int);
@@ -751,12 +754,12 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     A((void **)&b->runs_dev, (size_t)o->max_runs * sizeof(DevRun));
     A((void **)&b->flag, sizeof(unsigned));
     if (o->xpic_order > 1) {
-        A((void **)&b->xpic_block, 7 * N * (sizeof(double) + sizeof(float)));
+        A((void **)&b->xpic_block, 7 * N * sizeof(double) + 6 * N * sizeof(float));
         if (e == cudaSuccess) {
             double *d = b->xpic_block;
             float *f = (float *)(d + 7 * N);
             b->xpic = DevXpic{d, d + N, d + 2 * N, d + 3 * N, d + 4 * N, d + 5 * N, d + 6 * N,
-                              f, f + N, f + 2 * N, f + 3 * N, f + 4 * N, f + 5 * N, f + 6 * N};
+                              f, f + N, f + 2 * N, f + 3 * N, f + 4 * N, f + 5 * N};
         }
     }
     if (b->nf > 1 && o->lr_links > 0) {

@@ -29,15 +29,17 @@ __device__ __forceinline__ bool lr_contact_node(const StepParams &sp, const DevN
     return nm > 1;
 }
 
-// the distinct shape-function nodes of particle i with nonzero weight, as the
-// step's transfers visit them
+// the distinct contact nodes among the shape-function nodes of particle i
+// with nonzero weight (the contact test first: most nodes are not contact
+// nodes, so few reach the duplicate search)
 template <int DIM, int SHAPE, bool MIX>
-__device__ __forceinline__ int lr_particle_nodes(const DevGrid &g, int nb, const DevParticles &p, int i,
-                                                 int out[64]) {
+__device__ __forceinline__ int lr_particle_nodes(const StepParams &sp, const DevNodes &nd, const DevGrid &g, int nb,
+                                                 const DevParticles &p, int i, int out[64]) {
     using T = typename Wt<MIX>::T;
     int cnt = 0;
     visit_nodes<DIM, SHAPE, false, T>(g, nb, p, i, [&](int n, T N, T, T, T) {
-        if (N == T(0)) return;
+        if (zero_weight(N)) return;
+        if (!lr_contact_node(sp, nd, n)) return;
         for (int k = 0; k < cnt; k++)
             if (out[k] == n) return;
         if (cnt < 64) out[cnt++] = n;
@@ -57,10 +59,9 @@ static __global__ void __launch_bounds__(256) k_lr_link(StepParams sp, DevPartic
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
     if (BATCH && sp.runs[p.run[i]].normals < 5) return;
     int nodes[64];
-    const int m = lr_particle_nodes<DIM, SHAPE, MIX>(rv.g, rv.nb, p, i, nodes);
+    const int m = lr_particle_nodes<DIM, SHAPE, MIX>(sp, nd, rv.g, rv.nb, p, i, nodes);
     for (int k = 0; k < m; k++) {
         const int n = nodes[k];
-        if (!lr_contact_node(sp, nd, n)) continue;
         const int slot = atomicAdd(cnt + n, 1);
         if (pass == 1) {
             const long long at = (long long)start[n] + slot;
@@ -70,43 +71,66 @@ static __global__ void __launch_bounds__(256) k_lr_link(StepParams sp, DevPartic
     }
 }
 
-// each node's links in the particles' host order: one warp per node ranks its
-// links by host index in shared memory (host indices are distinct within a
-// node, whose particles all belong to one run); lists longer than the
-// shared-memory slice are sorted by insertion by one lane
+// The nodes with links, in no particular order, at nodes[0 .. nodes[nnodes]):
+// the regression kernels below run warps over these contact nodes only (a
+// few per cent of the grid) instead of over every node.  nodes[nnodes] must
+// be zero on entry.
+static __global__ void k_lr_compact(const int *start, int *nodes, int nnodes) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nnodes || start[n + 1] == start[n]) return;
+    nodes[atomicAdd(nodes + nnodes, 1)] = n;
+}
+
+// grid of the warp loops over contact nodes: enough warps to fill the GPU,
+// never more than the work
+constexpr int kLrMaxBlocks = 4096;
+inline int lr_loop_blocks(long long warps, int threads) {
+    const long long b = (warps * 32 + threads - 1) / threads;
+    return (int)std::max<long long>(1, std::min<long long>(b, kLrMaxBlocks));
+}
+
+// each node's links in the particles' host order: one warp per contact node
+// ranks its links by host index in shared memory (host indices are distinct
+// within a node, whose particles all belong to one run); lists longer than
+// the shared-memory slice are sorted by insertion by one lane
 constexpr int kLrSortCap = 256;
-static __global__ void __launch_bounds__(256) k_lr_order(const int *start, int *list, const int *orig, int nnodes,
-                                                         long long cap) {
+static __global__ void __launch_bounds__(256) k_lr_order(const int *start, int *list, const int *orig,
+                                                         const int *nodes, int nnodes, long long cap) {
     __shared__ int skey[8][kLrSortCap], sval[8][kLrSortCap];
     const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
-    const int n = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5);
-    if (n >= nnodes) return;  // whole warps
-    const int s0 = start[n], s1 = start[n + 1], L = s1 - s0;
-    if (L < 2 || s1 > cap) return;  // nothing to order, or dropped links (the run has failed)
-    if (L > kLrSortCap) {
-        if (lane == 0)
-            for (int k = s0 + 1; k < s1; k++) {
-                const int v = list[k], key = orig[v];
-                int j = k - 1;
-                while (j >= s0 && orig[list[j]] > key) {
-                    list[j + 1] = list[j];
-                    --j;
+    const int nc = nodes[nnodes];
+    const int nw = (int)(((long long)gridDim.x * blockDim.x) >> 5);
+    for (int c = (int)(((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5); c < nc; c += nw) {
+        const int n = nodes[c];
+        const int s0 = start[n], s1 = start[n + 1], L = s1 - s0;
+        if (L < 2 || s1 > cap) continue;  // nothing to order, or dropped links (the run has failed)
+        if (L > kLrSortCap) {
+            if (lane == 0)
+                for (int k = s0 + 1; k < s1; k++) {
+                    const int v = list[k], key = orig[v];
+                    int j = k - 1;
+                    while (j >= s0 && orig[list[j]] > key) {
+                        list[j + 1] = list[j];
+                        --j;
+                    }
+                    list[j + 1] = v;
                 }
-                list[j + 1] = v;
-            }
-        return;
-    }
-    for (int k = lane; k < L; k += 32) {
-        const int v = list[s0 + k];
-        sval[w][k] = v;
-        skey[w][k] = orig[v];
-    }
-    __syncwarp();
-    for (int k = lane; k < L; k += 32) {
-        const int key = skey[w][k];
-        int rank = 0;
-        for (int j = 0; j < L; j++) rank += skey[w][j] < key ? 1 : 0;
-        list[s0 + rank] = sval[w][k];
+            __syncwarp();
+            continue;
+        }
+        for (int k = lane; k < L; k += 32) {
+            const int v = list[s0 + k];
+            sval[w][k] = v;
+            skey[w][k] = orig[v];
+        }
+        __syncwarp();
+        for (int k = lane; k < L; k += 32) {
+            const int key = skey[w][k];
+            int rank = 0;
+            for (int j = 0; j < L; j++) rank += skey[w][j] < key ? 1 : 0;
+            list[s0 + rank] = sval[w][k];
+        }
+        __syncwarp();  // the slice is rewritten by the warp's next node
     }
 }
 
@@ -191,23 +215,57 @@ __device__ __forceinline__ double lr_radius(const DevGrid &g, const DevParticles
     return 1. / sqrt(n0x * n0x / (px * px) + n0y * n0y / (py * py) + n0z * n0z / (pz * pz));
 }
 
+// Separation of the two point clouds of a node along the unit normal nrm: the
+// supports of material field a's linked particles and of the others', each
+// through the particles' deformed radii (every lane of the warp calls this and
+// gets the warp's result).
+template <int DIM>
+__device__ __forceinline__ double lr_supports(const DevGrid &g, const DevParticles &p, const DevMat *mats,
+                                              const int *list, int s0, int s1, int a, const double nrm[3]) {
+    double supA = 1.e30, supB = 1.e30;
+    for (int k = s0 + (int)(threadIdx.x & 31); k < s1; k += 32) {
+        const int q = list[k];
+        const double xp[3] = {p.x[q], p.y[q], DIM == 3 ? p.z[q] : 0.};
+        const double r = lr_radius<DIM>(g, p, q, nrm);
+        const double d = nrm[0] * xp[0] + nrm[1] * xp[1] + nrm[2] * xp[2];
+        if (mats[p.mat[q]].field == a) supA = fmin(supA, -d - r);
+        else supB = fmin(supB, d - r);
+    }
+    return lr_wmin(supA) + lr_wmin(supB);
+}
+
 // One warp per grid node with links and material field present: the
 // regression normal against the other materials lumped and the separation
 // deln, written as (nx, ny, nz, deln) at out[4 (f fstride + n)].  Constants
 // of MachineLearning.cpp with PENALIZE_NORMALS: linear offset penalty 0.1;
 // logistic normal penalty 1e-7 cell^2, no offset penalty, the linear beta
 // doubled as the start, convergence 1 - cos < 1e-5 within 15 iterations.
+//
+// supports_only: the particles have not moved since the last full pass (the
+// momentum-update pass follows the mass-and-momentum pass with only the
+// strain update in between), so the regression -- a function of the linked
+// particles' positions and materials alone -- would give the same normal bit
+// for bit; only the supports, whose deformed radii follow the strain update,
+// are taken again, along the stored normal.
 template <int DIM, bool BATCH>
-static __global__ void __launch_bounds__(256, 3) k_lr_normals(StepParams sp, DevParticles p, DevNodes nd,
-                                                           const DevMat *mats, const int *start, const int *list,
-                                                           double *out, int nnodes, long long cap, int logistic) {
-    // one warp per (node, material field): the fields' regressions are independent
-    const long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5;
-    const int n = (int)(w / sp.ct.nf), a0 = (int)(w % sp.ct.nf);
+__device__ __forceinline__ void lr_node_field(const StepParams &sp, const DevParticles &p, const DevNodes &nd,
+                                              const DevMat *mats, const int *start, const int *list, double *out,
+                                              int n, int a0, long long cap, int logistic, int supports_only) {
     const int lane = threadIdx.x & 31;
-    if (n >= nnodes) return;  // whole warps
     const int s0 = start[n], s1 = start[n + 1];
     if (s1 == s0 || s1 > cap) return;
+    {
+        // a node with two materials applies the law once, from its first
+        // active field (the pair, MaterialContactOnCVF's doingPairs), so only
+        // that field's normal is ever read
+        int nm = 0, first = -1;
+        for (int f = 0; f < sp.ct.nf; f++)
+            if (nd.active[f * sp.ct.fstride + n]) {
+                if (first < 0) first = f;
+                nm++;
+            }
+        if (nm == 2 && a0 != first) return;
+    }
     DevGrid g = sp.g;
     int nl = n;  // the node's index in its grid
     if (BATCH) {
@@ -218,6 +276,15 @@ static __global__ void __launch_bounds__(256, 3) k_lr_normals(StepParams sp, Dev
         g = R.g;
         nl = n - R.node_base;
         logistic = R.normals == 6 ? 1 : 0;
+    }
+    if (supports_only) {
+        const int ka = a0 * sp.ct.fstride + n;
+        if (!nd.active[ka]) return;
+        const double *o = out + 4 * (size_t)ka;
+        const double nrm[3] = {o[0], o[1], o[2]};
+        const double dn = lr_supports<DIM>(g, p, mats, list, s0, s1, a0, nrm);
+        if (lane == 0) out[4 * (size_t)ka + 3] = dn;
+        return;
     }
     const int nx1 = g.nx + 1, ny1 = g.ny + 1;
     const double ndx = g.xn[nl % nx1], ndy = g.yn[(nl / nx1) % ny1], ndz = DIM == 3 ? g.zn[nl / (nx1 * ny1)] : 0.;
@@ -384,26 +451,29 @@ static __global__ void __launch_bounds__(256, 3) k_lr_normals(StepParams sp, Dev
 #pragma unroll
                 for (int k = 0; k < 3; k++) nrm[k] = lin[k];
         }
-        // separation: the supports of the two clouds along the normal
-        double supA = 1.e30, supB = 1.e30;
-        for (int k = s0 + lane; k < s1; k += 32) {
-            const int q = list[k];
-            const double xp[3] = {p.x[q], p.y[q], DIM == 3 ? p.z[q] : 0.};
-            const double r = lr_radius<DIM>(g, p, q, nrm);
-            const double d = nrm[0] * xp[0] + nrm[1] * xp[1] + nrm[2] * xp[2];
-            if (mats[p.mat[q]].field == a) supA = fmin(supA, -d - r);
-            else supB = fmin(supB, d - r);
-        }
-        supA = lr_wmin(supA);
-        supB = lr_wmin(supB);
+        const double dn = lr_supports<DIM>(g, p, mats, list, s0, s1, a, nrm);
         if (lane == 0) {
             double *o = out + 4 * (size_t)ka;
             o[0] = nrm[0];
             o[1] = nrm[1];
             o[2] = nrm[2];
-            o[3] = supA + supB;
+            o[3] = dn;
         }
     }
+}
+
+// one warp per (contact node, material field): the fields' regressions are
+// independent
+template <int DIM, bool BATCH>
+static __global__ void __launch_bounds__(256, 3) k_lr_normals(StepParams sp, DevParticles p, DevNodes nd,
+                                                           const DevMat *mats, const int *start, const int *list,
+                                                           const int *nodes, double *out, int nnodes, long long cap,
+                                                           int logistic, int supports_only) {
+    const long long total = (long long)nodes[nnodes] * sp.ct.nf;
+    const long long nw = ((long long)gridDim.x * blockDim.x) >> 5;
+    for (long long w = ((long long)blockIdx.x * blockDim.x + threadIdx.x) >> 5; w < total; w += nw)
+        lr_node_field<DIM, BATCH>(sp, p, nd, mats, start, list, out, nodes[w / sp.ct.nf], (int)(w % sp.ct.nf), cap,
+                                  logistic, supports_only);
 }
 
 }  // namespace nmg

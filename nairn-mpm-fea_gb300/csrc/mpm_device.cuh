@@ -90,7 +90,17 @@ struct DevContact {
     const double *lr;  // regression normals (5, 6): 4 per field-node (n, deln)
     unsigned rigid;    // bit f set: field f holds a rigid contact material (MatVelocityField::IsRigidField)
     double rigid_bias; // MeshInfo::rigidGradientBias, squared (MeshInfo.cpp:1191)
+    // XPIC/FMPM(k > 1) with contact: the FMPMContact cache of every field-node
+    // (Common/System/DataTypes.hpp:90-104), set by each contact call of a step
+    // whose order is > 1 (xcache != 0) -- 13 doubles at xc[13 k]: deltaDotn,
+    // norm (3), priorDelPiZero (3), netDelPi (3), startDelFi (3) -- and the
+    // paired field at xc_pair[k] (-1: lumped, below -1: not set this step)
+    double *xc;
+    int *xc_pair;
+    int xcache;
 };
+
+constexpr int kXcDoubles = 13;
 
 // Deterministic node sums (MPMGPU_P2G_DETERMINISTIC): three 64-bit integer
 // limbs per accumulated node quantity -- limb l of quantity q at node n is
@@ -331,6 +341,15 @@ __device__ __forceinline__ void bgimp_window(T xi, T lp, T idx, T sgn, Win4<T> &
         w.dS[j] = dS;
     }
 }
+
+// A shape-function weight of exactly zero (+0 or -0): a node outside the
+// particle's support.  For doubles the test is on the bits, in the integer
+// pipe: a double compare would take a slot of the FP64 pipe, which bounds the
+// FP64 kernels on this GPU.
+__device__ __forceinline__ bool zero_weight(double v) {
+    return ((unsigned long long)__double_as_longlong(v) << 1) == 0ull;
+}
+__device__ __forceinline__ bool zero_weight(float v) { return v == 0.f; }
 
 // FP64 value as an FP32 pair hi + lo (hi = nearest float, lo = nearest float of the rest)
 __device__ __forceinline__ void split2(double v, float &hi, float &lo) {

@@ -259,8 +259,6 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
     if (opts->xpic_order < 0 || opts->xpic_order > 64 || (opts->xpic_fmpm != 0 && opts->xpic_fmpm != 1) ||
         (opts->xpic_order > 0 && opts->xpic_period < 1))
         return set_err(nullptr, MPMGPU_ERR_INVALID, "xpic_order must be 0 to 64, xpic_fmpm 0 or 1, xpic_period >= 1");
-    if (opts->xpic_order > 0 && opts->nfields > 1)
-        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "XPIC/FMPM with multimaterial contact is not implemented");
     if (opts->xpic_order > 1 && opts->p2g == MPMGPU_P2G_DETERMINISTIC)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED,
                        "XPIC/FMPM of order > 1 with deterministic node sums is not implemented");
@@ -647,6 +645,8 @@ int step_impl(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
                            "rigid contact materials need multimaterial contact (RigidMaterial::SetField)");
         if (c->ct.normals >= 5)
             return set_err(c, MPMGPU_ERR_UNSUPPORTED, "regression normals with rigid materials are not implemented");
+        if (c->opts.xpic_order > 1)
+            return set_err(c, MPMGPU_ERR_UNSUPPORTED, "XPIC/FMPM of order > 1 with rigid materials is not implemented");
     }
     for (auto &pr : c->prof) pr.ms = 0.;
     if (c->profile && ensure_events(c, nsteps) != 0) return set_err(c, MPMGPU_ERR_CUDA, "event creation failed");
@@ -676,17 +676,23 @@ int step_impl(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
     }
     if (c->opts.xpic_order > 1 && !c->xpic_block) {
         // PeriodicXPIC expansion: v*(prev), v*(next) and 1 / mass of every
-        // node, in FP64 and FP32
-        const size_t nn = (size_t)c->g.nnodes;
-        cudaError_t e = cudaMalloc(&c->xpic_block, 7 * nn * (sizeof(double) + sizeof(float)));
+        // field-node, in FP64 and FP32; with contact, each field-node's
+        // contact state for the incremental contact of the passes
+        const size_t nn = (size_t)c->g.nnodes * c->ct.nf;
+        const size_t xc = c->ct.nf > 1 ? nn * (kXcDoubles * sizeof(double) + sizeof(int)) : 0;
+        cudaError_t e = cudaMalloc(&c->xpic_block, 7 * nn * sizeof(double) + 6 * nn * sizeof(float) + xc);
         if (e != cudaSuccess) {
             c->xpic_block = nullptr;
             return set_err(c, MPMGPU_ERR_OOM, "XPIC node columns");
         }
         double *b = c->xpic_block;
         float *f = (float *)(b + 7 * nn);
-        c->xpic = DevXpic{b,     b + nn,     b + 2 * nn, b + 3 * nn, b + 4 * nn, b + 5 * nn, b + 6 * nn,
-                          f,     f + nn,     f + 2 * nn, f + 3 * nn, f + 4 * nn, f + 5 * nn, f + 6 * nn};
+        c->xpic = DevXpic{b, b + nn, b + 2 * nn, b + 3 * nn, b + 4 * nn, b + 5 * nn, b + 6 * nn,
+                          f, f + nn, f + 2 * nn, f + 3 * nn, f + 4 * nn, f + 5 * nn};
+        if (c->ct.nf > 1) {
+            c->ct.xc = (double *)(f + 6 * nn);  // 8-byte aligned: 6 nn floats
+            c->ct.xc_pair = (int *)(c->ct.xc + kXcDoubles * nn);
+        }
     }
     std::vector<char> sorted((size_t)nsteps, 0);
     cudaEvent_t w0 = nullptr, w1 = nullptr;

@@ -876,6 +876,16 @@ __device__ __forceinline__ void for_each_window_node(const AxisWin<SHAPE, T> &w,
         }
 }
 
+// for_each_node's callback f(node, N, 0, 0, 0) over a precomputed window
+// (node = global index, run node base nb)
+template <int DIM, int SHAPE, typename T, class F>
+__device__ __forceinline__ void for_each_window_node_at(const AxisWin<SHAPE, T> &w, const DevGrid &g, int nb, F &&f) {
+    const int n0 = nb + w.c[0] + w.c[1] * g.yplane + (DIM == 3 ? w.c[2] * g.zplane : 0);
+    for_each_window_node<DIM, SHAPE, false, T>(w, [&](int jx, int jy, int jz, T N, T, T, T) {
+        f(n0 + jx + jy * g.yplane + (DIM == 3 ? jz * g.zplane : 0), N, T(0), T(0), T(0));
+    });
+}
+
 // Separable gradient sums over a window.  With N = X(jx) Y(jy) Z(jz), the
 // velocity gradient sum_nodes v_a dN/dx_b and the internal force
 // -mp (sigma - P I) . grad N factor axis by axis: contracting x first, then y,
@@ -941,7 +951,7 @@ __device__ __forceinline__ void window_grad_scatter(const AxisWin<SHAPE, T> &w, 
             const T P = DIM == 3 ? w.S[1][jy] * w.S[2][jz] : w.S[1][jy];   // Y Z
             const T Q = DIM == 3 ? w.dS[1][jy] * w.S[2][jz] : w.dS[1][jy]; // Y' Z
             const T R = DIM == 3 ? w.S[1][jy] * w.dS[2][jz] : T(0);        // Y Z'
-            if (P == T(0)) continue;  // the row is outside the support
+            if (zero_weight(P)) continue;  // the row is outside the support
             T wx[3], u[3];
 #pragma unroll
             for (int a = 0; a < DIM; a++) {
@@ -950,7 +960,7 @@ __device__ __forceinline__ void window_grad_scatter(const AxisWin<SHAPE, T> &w, 
             }
 #pragma unroll
             for (int jx = 0; jx < K; jx++) {
-                if (w.S[0][jx] == T(0)) continue;
+                if (zero_weight(w.S[0][jx])) continue;
                 T f[3] = {0, 0, 0};
 #pragma unroll
                 for (int a = 0; a < DIM; a++) f[a] = w.dS[0][jx] * wx[a] + w.S[0][jx] * u[a];
@@ -1074,12 +1084,12 @@ __device__ __forceinline__ double tile_sum(const NodeTile &t, int q, int k) {
     return (double)t.hi[q][k] + (double)t.lo[q][k];
 }
 
-// Particle slot of this thread in a tiled kernel: lane l of warp w of the
-// block takes slot l * (warps per block) + w of the block's range.  The block
-// still covers consecutive slots, but the lanes of one warp hold particles of
-// different cells (sorted particles of one cell are neighbours), so the
-// lanes' shared-memory adds go to different nodes instead of queueing on the
-// same address.
+// Particle slot of this thread in a scattering kernel: lane l of warp w of
+// the block takes slot l * (warps per block) + w of the block's range.  The
+// block still covers consecutive slots, but the lanes of one warp hold
+// particles of different cells (sorted particles of one cell are neighbours),
+// so the lanes' atomic adds -- to a shared-memory tile or to the node columns
+// -- go to different nodes instead of queueing on the same address.
 __device__ __forceinline__ int tile_particle() {
     return blockIdx.x * blockDim.x + (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
 }
@@ -1230,7 +1240,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
     const bool mm = sp.ct.nf > 1;
     unsigned long long *nb = sp.det.nbnd;
     auto node = [&](int n, T N, T, T, T) {
-        if (N == T(0)) return;
+        if (zero_weight(N)) return;
         atomicMax(nb + n + off, (unsigned long long)__double_as_longlong((double)N * mp));
     };
     if (ok) {
@@ -1266,7 +1276,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
 template <int DIM, int SHAPE, bool MIX, bool BATCH, bool DET = false>
 static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tile_particle();
     if (i >= p.n) return;
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
@@ -1298,7 +1308,7 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_p2
         sG = pow2(det_shift(sp.det.bnd[DB_GV]));
     }
     auto scatter = [&](int n, T N, T gx, T gy, T gz) {
-        if (N == T(0)) return;
+        if (zero_weight(N)) return;
         n += off;
         const double fnmp = (double)N * mp;
         if constexpr (DET) {
@@ -1470,7 +1480,7 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, cons
         return;
     }
     visit_nodes<DIM, SHAPE, true, T>(g, nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
-                                           if (N == T(0)) return;
+                                           if (zero_weight(N)) return;
                                            n += off;
                                            T vx, vy, vz = 0;
                                            if (MIX) {
@@ -1540,7 +1550,7 @@ __device__ __forceinline__ void forces_scatter(const StepParams &sp, const DevPa
         return;
     }
     visit_nodes<DIM, SHAPE, true, T>(g, nb, p, i, [&](int n, T N, T dx, T dy, T dz) {
-                                           if (N == T(0)) return;
+                                           if (zero_weight(N)) return;
                                            n += off;
                                            T fx, fy, fz = 0;
                                            if (DIM == 2) {
@@ -1574,7 +1584,7 @@ __device__ __forceinline__ void forces_scatter(const StepParams &sp, const DevPa
 // Mixed mode: internal-force products in FP32 into FP32 accumulators.
 template <int DIM, int SHAPE, bool STRAIN, bool MIX, bool BATCH, bool DET = false>
 static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tile_particle();
     if (i >= p.n) return;
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
@@ -1733,9 +1743,12 @@ __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticl
 // position; returns them in v and xp.  Mixed mode: S v is formed as
 // v_particle + sum N (v_node - v_particle) (the weights sum to one) with the
 // differences from FP32 pairs, S a in FP32; the update itself is FP64.
+// win: the particle's window factors when the caller has them (window shapes),
+// so they are not formed again here.
 template <int DIM, int SHAPE, bool MIX, bool BATCH>
 __device__ __forceinline__ void g2p_move(const StepParams &sp, const DevParticles &p, const DevNodes &nd, int i,
-                                         const RunView &rv, int off, double v[3], double xp[3]) {
+                                         const RunView &rv, int off, double v[3], double xp[3],
+                                         const AxisWin<SHAPE, typename Wt<MIX>::T> *win = nullptr) {
     using T = typename Wt<MIX>::T;
     const DevGrid &g = rv.g;
     const double dt = rv.dt;
@@ -1753,11 +1766,15 @@ __device__ __forceinline__ void g2p_move(const StepParams &sp, const DevParticle
     }
     // the particle's nodes for this step (CPDI corners or the element window)
     auto visit = [&](auto &&fn) {
-        if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
-        else for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, fn);
+        if constexpr (SHAPE == SHAPE_LCPDI) {
+            visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
+        } else {
+            if (win) for_each_window_node_at<DIM, SHAPE, T>(*win, g, rv.nb, fn);
+            else for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, fn);
+        }
     };
     visit([&](int n, T N, T, T, T) {
-        if (N == T(0)) return;
+        if (zero_weight(N)) return;
         n += off;
         if (MIX) {
             Sv[0] += ((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0])) * N;
@@ -1819,7 +1836,7 @@ __device__ __forceinline__ void g2p_move(const StepParams &sp, const DevParticle
 template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH, bool DET = false>
 static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
-    const int i = blockIdx.x * blockDim.x + threadIdx.x;
+    const int i = tile_particle();
     if (i >= p.n) return;
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
@@ -1844,7 +1861,19 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
         return;
     }
     double v[3], xp[3];
-    g2p_move<DIM, SHAPE, MIX, BATCH>(sp, p, nd, i, rv, off, v, xp);
+    // window shapes, FP64: the factors once for the particle update and the
+    // second extrapolation (both at the step's natural coordinates).  The
+    // mixed mode forms its FP32 factors twice: keeping them live costs more
+    // (registers) than forming them.
+    AxisWin<SHAPE, T> w;
+    if constexpr (SHAPE != SHAPE_LCPDI && !MIX) {
+        int col, row, zr;
+        elem_coords(g, e, col, row, zr);
+        axis_windows<DIM, SHAPE, false, T>(g, col, row, zr, xi, eta, zeta, lx, ly, lz, w);
+        g2p_move<DIM, SHAPE, MIX, BATCH>(sp, p, nd, i, rv, off, v, xp, &w);
+    } else {
+        g2p_move<DIM, SHAPE, MIX, BATCH>(sp, p, nd, i, rv, off, v, xp);
+    }
     if (USL && DET) {
         // bounds of the second extrapolation, which k_det_usl then sums
         const double mp = p.mass[i];
@@ -1869,7 +1898,7 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
             if (DIM == 3) d[2] = xp[2] - p.z0[i];
         }
         auto scatter = [&](int n, T N, T gx, T gy, T gz) {
-            if (N == T(0)) return;
+            if (zero_weight(N)) return;
             n += off;
             const double fnmp = (double)N * mp;
             atomicAdd(&nd.ux[n], v[0] * fnmp);
@@ -1880,6 +1909,8 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2
         if (rv.mm) {
             if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
             else for_each_node<DIM, SHAPE, true, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, scatter);
+        } else if constexpr (SHAPE != SHAPE_LCPDI && !MIX) {
+            for_each_window_node_at<DIM, SHAPE, T>(w, g, rv.nb, scatter);
         } else {
             visit(scatter);
         }
@@ -1901,16 +1932,16 @@ static __global__ void __launch_bounds__(256) k_g2p_tile(StepParams sp, DevParti
     const bool valid = i < p.n && particle_run<BATCH>(sp, p, i, rv);
     int col = 0, row = 0, zr = 0;
     double v[3] = {0., 0., 0.}, xp[3];
+    AxisWin<SHAPE, float> w;
     if (valid) {
-        g2p_move<DIM, SHAPE, true, BATCH>(sp, p, nd, i, rv, 0, v, xp);
         elem_coords(rv.g, p.elem[i], col, row, zr);
+        axis_windows<DIM, SHAPE, false, float>(rv.g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0.,
+                                               p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1., w);
+        g2p_move<DIM, SHAPE, true, BATCH>(sp, p, nd, i, rv, 0, v, xp, &w);
     }
     const bool tiled = tile_open<DIM, SHAPE>(t, valid, BATCH && valid ? p.run[i] : 0, col, row, zr, rv, v, DIM + 1);
     if (valid) {
         const double mp = p.mass[i];
-        AxisWin<SHAPE, float> w;
-        axis_windows<DIM, SHAPE, false, float>(rv.g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0.,
-                                               p.lpx[i], p.lpy[i], DIM == 3 ? p.lpz[i] : 1., w);
         if (tiled) {
             const float mpf = (float)mp;
             const float d[3] = {(float)(v[0] - t.ref[0]), (float)(v[1] - t.ref[1]), (float)(v[2] - t.ref[2])};
@@ -1967,7 +1998,7 @@ static __global__ void __launch_bounds__(256) k_det_usl(StepParams sp, DevPartic
         if (DIM == 3) d[2] = p.z[i] - p.z0[i];
     }
     auto scatter = [&](int n, T N, T gx, T gy, T gz) {
-        if (N == T(0)) return;
+        if (zero_weight(N)) return;
         n += off;
         const double fnmp = (double)N * mp;
         const unsigned long long nb = sp.det.nbnd[n];
@@ -2367,6 +2398,19 @@ __device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, in
         for (int a = 0; a < 3; a++) dispb[a] = (dispc[a] - dispa[a]) * rmred + dispa[a];
         const double deln = hasDeln ? lrDeln : dot3(dispb, norm) - dot3(dispa, norm);
         mred *= massi;
+        // MaterialContactNode::SetContactInfo (MaterialContactNode.cpp:133-151)
+        double *xc = ct.xcache ? ct.xc + kXcDoubles * (size_t)ki : nullptr;
+        if (xc) {
+            ct.xc_pair[ki] = pairs ? j : -1;
+            xc[0] = deln;
+#pragma unroll
+            for (int a = 0; a < 3; a++) {
+                xc[1 + a] = norm[a];
+                xc[4 + a] = delPi[a];
+                xc[7 + a] = 0.;
+                xc[10 + a] = 0.;
+            }
+        }
         double delFi[3];
         const double *dfp = nullptr;
         if (pass == BC_UPDATE_MOMENTUM) {
@@ -2381,9 +2425,16 @@ __device__ void node_contact(const DevContact &ct, const DevNodes &nd, int n, in
             delFi[1] = Fc[1] * massRatio - nd.fy[ki];
             delFi[2] = Fc[2] * massRatio - nd.fz[ki];
             dfp = delFi;
+            if (xc)
+#pragma unroll
+                for (int a = 0; a < 3; a++) xc[10 + a] = delFi[a];
         }
         if (!coulomb_delta(ct, delPi, norm, dotn, deln, mred, dfp, dt)) continue;
         change_momentum(nd, ki, delPi, pass, dt);
+        // MaterialContactNode::ContactSetDelPi
+        if (xc)
+#pragma unroll
+            for (int a = 0; a < 3; a++) xc[7 + a] = delPi[a];
         if (pairs) {
             const double neg[3] = {-delPi[0], -delPi[1], -delPi[2]};
             change_momentum(nd, j * S + n, neg, pass, dt);

@@ -6,7 +6,8 @@
 // creation so that both together stay within the HBM budget, and one host
 // thread that runs the loop
 //
-//     admit queued requests that fit (FIFO; optionally backfilling)
+//     admit queued requests that fit (FIFO, least work first, or the
+//     deadline order that bounds running requests' predicted slowdown)
 //     enqueue `steps_per_round` batched steps on every batch with running runs
 //     wait for them, retire finished and failed runs (results written back)
 //
@@ -53,8 +54,44 @@ double ms_between(ServerClock::time_point a, ServerClock::time_point b) {
 
 }  // namespace
 
+// Step time of one batch as a + b R (ms per step, R resident particles): a
+// least-squares line through the rounds' CUDA-event timings, each older round
+// weighted down by kModelDecay, with priors until two different loads have
+// been seen.
+struct StepModel {
+    static constexpr double kModelDecay = 0.95;
+    double a = 0.1, b = 1e-6;  // priors, replaced by the fit
+    double w = 0., sr = 0., srr = 0., st = 0., srt = 0.;
+    void add(double R, double t) {
+        w = w * kModelDecay + 1.;
+        sr = sr * kModelDecay + R;
+        srr = srr * kModelDecay + R * R;
+        st = st * kModelDecay + t;
+        srt = srt * kModelDecay + R * t;
+        const double den = w * srr - sr * sr, tm = st / w, rm = sr / w;
+        if (w > 2.5 && den > 1e-3 * w * srr) {
+            b = (w * srt - sr * st) / den;
+            a = (st - b * sr) / w;
+        } else {
+            a = std::min(a, tm);
+            b = rm > 0. ? (tm - a) / rm : b;
+        }
+        a = std::min(std::max(a, kMinStepMs), tm);
+        b = std::max(b, 0.);
+    }
+    // the resident load at which a step runs at kEfficiency of the batch's
+    // asymptotic throughput 1/b: a + b R = b R / kEfficiency
+    double efficient_load() const {
+        return b > 0. ? a * kEfficiency / (1. - kEfficiency) / b : 1e300;
+    }
+    static constexpr double kMinStepMs = 0.05;  // a graph-launched step's launch floor
+    static constexpr double kEfficiency = 0.9;
+};
+
 struct MpmGpuServer {
     MpmGpuServerOptions o{};
+    StepModel model[2];
+    cudaEvent_t ev[2][2] = {{nullptr, nullptr}, {nullptr, nullptr}};
     int device = 0;
     MpmGpuBatch *batch[2] = {nullptr, nullptr};  // [0] 2D, [1] 3D
     int64_t reserved = 0;
@@ -97,16 +134,39 @@ int64_t server_capacity(MpmGpuBatchOptions o, int64_t bytes, double nodes_per_pa
     return lo;
 }
 
+double slowdown_target(const MpmGpuServerOptions &o) { return o.slowdown_target > 0. ? o.slowdown_target : 4.; }
+
 // admission: FIFO per dimension; with backfill a request that does not fit
-// now is passed by later ones of its dimension
+// now is passed by later ones of its dimension.  The deadline order (2) sorts
+// by work with requests already past their bound first, and admits a request
+// only while the running requests of its dimension stay within theirs.
 void server_admit(MpmGpuServer *s, std::vector<ServerRequest *> &admitted, std::vector<ServerRequest *> &failed) {
     std::vector<ServerRequest *> cand;
+    std::vector<MpmGpuRunLoad> load[2];
+    const auto now = ServerClock::now();
     {
         std::lock_guard<std::mutex> lk(s->mu);
         cand.assign(s->queue.begin(), s->queue.end());
+        for (int d = 0; d < 2; d++)
+            for (const ServerRequest *q : s->running[d])
+                load[d].push_back({q->p.n, q->nsteps - q->steps_done, q->nsteps, ms_between(q->t_submit, now)});
     }
+    const bool deadline = s->o.order == 2;
+    const double k = slowdown_target(s->o);
+    auto alone_ms = [&](const ServerRequest *q) {
+        const StepModel &m = s->model[q->dim == 3 ? 1 : 0];
+        return q->nsteps * (m.a + m.b * (double)q->p.n);
+    };
+    auto late = [&](const ServerRequest *q) { return ms_between(q->t_submit, now) > (k - 1.) * alone_ms(q); };
     if (s->o.order == 1)
         std::stable_sort(cand.begin(), cand.end(), [](const ServerRequest *a, const ServerRequest *b) {
+            return (double)a->p.n * a->nsteps < (double)b->p.n * b->nsteps;
+        });
+    else if (deadline)
+        std::stable_sort(cand.begin(), cand.end(), [&](const ServerRequest *a, const ServerRequest *b) {
+            const bool la = late(a), lb = late(b);
+            if (la != lb) return la;
+            if (la) return ms_between(a->t_submit, now) - k * alone_ms(a) > ms_between(b->t_submit, now) - k * alone_ms(b);
             return (double)a->p.n * a->nsteps < (double)b->p.n * b->nsteps;
         });
     int64_t resident = 0;
@@ -118,6 +178,22 @@ void server_admit(MpmGpuServer *s, std::vector<ServerRequest *> &admitted, std::
         const int d = q->dim == 3 ? 1 : 0;
         MpmGpuBatch *b = s->batch[d];
         if (blocked[d]) continue;
+        if (deadline) {
+            // admitted while the dimension's resident load stays within the
+            // model's efficient load (whatever the request's size when nothing
+            // runs) and the running requests within their bounds
+            double R = 0.;
+            for (const MpmGpuRunLoad &u : load[d]) R += (double)u.n;
+            const bool fits = R == 0. || R + (double)q->p.n <= s->model[d].efficient_load();
+            if (!fits || mpmgpu_server_admits(s->model[d].a, s->model[d].b, k, load[d].data(),
+                                              (int32_t)load[d].size(), q->p.n, q->nsteps,
+                                              ms_between(q->t_submit, now)) != 1) {
+                // a request past its bound waits first: nothing later of its
+                // dimension passes it, so the load drains until it fits
+                if (late(q)) blocked[d] = true;
+                continue;
+            }
+        }
         if (s->o.max_resident_particles > 0 && resident > 0 && resident + q->p.n > s->o.max_resident_particles) {
             // over the resident cap: wait (or let a smaller later request pass)
             if (!s->o.backfill) capped = true;
@@ -134,6 +210,7 @@ void server_admit(MpmGpuServer *s, std::vector<ServerRequest *> &admitted, std::
             q->t_admit = ServerClock::now();
             admitted.push_back(q);
             resident += q->p.n;
+            load[d].push_back({q->p.n, q->nsteps, q->nsteps, ms_between(q->t_submit, now)});
         } else if (st == MPMGPU_ERR_BUSY) {
             MpmGpuBatchInfo bi{};
             mpmgpu_batch_info(b, &bi);
@@ -193,11 +270,25 @@ void server_loop(MpmGpuServer *s) {
         const auto t0 = ServerClock::now();
         bool launched[2] = {false, false};
         int status[2] = {MPMGPU_OK, MPMGPU_OK};
-        // enqueue on both batches first, then wait for both: their steps overlap
+        // enqueue on both batches first, then wait for both: their steps overlap.
+        // Each batch's rounds are timed with events on its stream for the
+        // step-time model.
+        double load_now[2] = {0., 0.};
+        for (int d = 0; d < 2; d++) {
+            if (s->running[d].empty()) continue;
+            for (const ServerRequest *q : s->running[d]) load_now[d] += (double)q->p.n;
+            status[d] = batch_launch(s->batch[d], chunk, s->ev[d][0], &launched[d]);
+            if (status[d] == MPMGPU_OK && launched[d] &&
+                cudaEventRecord(s->ev[d][1], (cudaStream_t)mpmgpu_batch_stream(s->batch[d])) != cudaSuccess)
+                status[d] = MPMGPU_ERR_CUDA;
+        }
         for (int d = 0; d < 2; d++)
-            if (!s->running[d].empty()) status[d] = batch_launch(s->batch[d], chunk, nullptr, &launched[d]);
-        for (int d = 0; d < 2; d++)
-            if (status[d] == MPMGPU_OK && launched[d]) status[d] = batch_collect(s->batch[d]);
+            if (status[d] == MPMGPU_OK && launched[d]) {
+                status[d] = batch_collect(s->batch[d]);
+                float ms = 0.f;
+                if (status[d] == MPMGPU_OK && cudaEventElapsedTime(&ms, s->ev[d][0], s->ev[d][1]) == cudaSuccess)
+                    s->model[d].add(load_now[d], (double)ms / chunk);
+            }
         for (int d = 0; d < 2; d++) {
             if (status[d] != MPMGPU_OK) {
                 // an error on this batch: its running requests fail.  Their
@@ -279,19 +370,64 @@ void server_loop(MpmGpuServer *s) {
     s->done.notify_all();
 }
 
+// the server's batches and events (not the server itself)
+void server_free(MpmGpuServer *s) {
+    for (auto *&b : s->batch) {
+        mpmgpu_batch_destroy(b);
+        b = nullptr;
+    }
+    for (auto &pair : s->ev)
+        for (auto &e : pair)
+            if (e) {
+                cudaEventDestroy(e);
+                e = nullptr;
+            }
+}
+
 }  // namespace
 
 extern "C" {
+
+int mpmgpu_server_admits(double a_ms, double b_ms, double k, const MpmGpuRunLoad *running, int32_t nrunning,
+                         int64_t cand_n, int32_t cand_steps, double cand_waited_ms) {
+    if (!(a_ms >= 0.) || !(b_ms >= 0.) || !(k >= 1.) || nrunning < 0 || (nrunning > 0 && !running) || cand_n <= 0 ||
+        cand_steps <= 0 || !(cand_waited_ms >= 0.))
+        return -MPMGPU_ERR_INVALID;
+    if (nrunning == 0) return 1;
+    double R = 0.;
+    for (int32_t r = 0; r < nrunning; r++) R += (double)running[r].n;
+    const double t_now = a_ms + b_ms * R, t_with = a_ms + b_ms * (R + (double)cand_n);
+    for (int32_t r = 0; r < nrunning; r++) {
+        const MpmGpuRunLoad &u = running[r];
+        const double bound = k * u.steps_total * (a_ms + b_ms * (double)u.n);
+        if (u.elapsed_ms + u.steps_left * t_now > bound) continue;  // past its bound already: does not block
+        if (u.elapsed_ms + u.steps_left * t_with > bound) return 0;
+    }
+    return 1;
+}
 
 int mpmgpu_server_create(const MpmGpuServerOptions *o, MpmGpuServer **out) {
     if (!o || !out) return serr(nullptr, MPMGPU_ERR_INVALID, "mpmgpu_server_create: null argument");
     *out = nullptr;
     if (o->hbm_budget_bytes <= 0 || o->max_runs <= 0 || !(o->frac_3d >= 0. && o->frac_3d <= 1.))
         return serr(nullptr, MPMGPU_ERR_INVALID, "server needs a positive HBM budget, run slots and 0 <= frac_3d <= 1");
+    if (o->order < 0 || o->order > 2 || !(o->slowdown_target == 0. || o->slowdown_target >= 1.))
+        return serr(nullptr, MPMGPU_ERR_INVALID, "server order must be 0, 1 or 2 and slowdown_target 0 or >= 1");
     auto s = std::make_unique<MpmGpuServer>();
     s->o = *o;
     if (!(s->o.nodes_per_particle > 0.)) s->o.nodes_per_particle = 0.5;
     cudaGetDevice(&s->device);
+    // priors of the step-time model until rounds have been timed
+    s->model[0].b = 0.7e-6;
+    s->model[1].b = 2.0e-6;
+    for (auto &pair : s->ev)
+        for (auto &e : pair)
+            if (cudaEventCreate(&e) != cudaSuccess) {
+                for (auto &pr : s->ev)
+                    for (auto &x : pr)
+                        if (x) cudaEventDestroy(x);
+                return serr(nullptr, MPMGPU_ERR_CUDA, "server: cudaEventCreate failed");
+            }
     const double frac[2] = {1. - o->frac_3d, o->frac_3d};
     const int np[2] = {MPMGPU_PLANE_STRAIN, MPMGPU_THREED};
     for (int d = 0; d < 2; d++) {
@@ -314,7 +450,7 @@ int mpmgpu_server_create(const MpmGpuServerOptions *o, MpmGpuServer **out) {
         bo.fraction_usf = o->fraction_usf;
         const int64_t P = server_capacity(bo, bytes, s->o.nodes_per_particle);
         if (P < 1000) {
-            for (auto *b : s->batch) mpmgpu_batch_destroy(b);
+            server_free(s.get());
             return serr(nullptr, MPMGPU_ERR_INVALID, "HBM budget too small for a batch");
         }
         bo.max_particles = P;
@@ -322,7 +458,7 @@ int mpmgpu_server_create(const MpmGpuServerOptions *o, MpmGpuServer **out) {
         const int st = mpmgpu_batch_create(&bo, &s->batch[d]);
         if (st != MPMGPU_OK) {
             std::string m = mpmgpu_batch_last_error(nullptr);
-            for (auto *b : s->batch) mpmgpu_batch_destroy(b);
+            server_free(s.get());
             return serr(nullptr, st, "server batch: " + m);
         }
         s->reserved += mpmgpu_batch_bytes(&bo);
@@ -455,7 +591,7 @@ void mpmgpu_server_destroy(MpmGpuServer *s) {
         s->wake.notify_all();
     }
     if (s->worker.joinable()) s->worker.join();
-    for (auto *b : s->batch) mpmgpu_batch_destroy(b);
+    server_free(s);
     delete s;
 }
 

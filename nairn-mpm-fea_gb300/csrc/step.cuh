@@ -45,13 +45,26 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     const int xk = xm < 0 ? -xm : xm;
     const DevXpic xp = c->xpic;
     // XPIC(k)/FMPM(k) expansion of the node velocities (k > 1)
+    // (every field-node; with contact, each pass's Delta v also takes the
+    // incremental contact of the contact nodes)
+    const bool xcontact = c->ct.nf > 1;
+    sp.ct.xcache = xk > 1 && xcontact ? 1 : 0;
+    if (sp.ct.xcache)  // this step's contact state: none yet
+        cudaMemsetAsync(c->ct.xc_pair, 0x80, (size_t)NN * c->ct.nf * sizeof(int), s);
     auto xpic_expand = [&](int phase) {
-        k_xpic_init<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, phase);
+        const int XN = NN * c->ct.nf, xb = (XN + TB - 1) / TB;
+        k_xpic_init<DIM, MIX, false><<<xb, TB, 0, s>>>(sp, c->nd, xp, XN, phase);
         c->launches++;
         for (int k = 2; k <= xk; k++) {
-            k_xpic_pass<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, xp, phase, k);
-            k_xpic_delta<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, c->bcs, c->bc_group, phase, k);
+            k_xpic_pass<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, xp, c->mats, phase, k);
+            k_xpic_delta<DIM, MIX, false><<<xb, TB, 0, s>>>(sp, c->nd, xp, XN, c->bcs, c->bc_group, phase, k,
+                                                            xcontact ? 1 : 0);
             c->launches += 2;
+            if (xcontact) {
+                k_xpic_contact<DIM, MIX><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, phase, k);
+                k_xpic_apply<DIM, MIX><<<xb, TB, 0, s>>>(sp, c->nd, xp, XN, phase, k);
+                c->launches += 2;
+            }
         }
     };
     const int NT = NN * c->ct.nf, ntb = (NT + TB - 1) / TB;
@@ -76,10 +89,10 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
         c->launches += 2;
     }
     const bool lr = c->ct.nf > 1 && c->ct.normals >= 5;
-    const int lrb = (int)(((long long)NN * 32 + TB - 1) / TB);  // a warp per node
-    auto lr_normals = [&]() {
-        k_lr_normals<DIM, false><<<lrb * c->ct.nf, TB, 0, s>>>(sp, c->p, c->nd, c->mats, c->lr_start, c->lr_list, c->lr_out,
-                                                    NN, c->lr_cap, c->ct.normals == 6 ? 1 : 0);
+    auto lr_normals = [&](int supports_only) {
+        k_lr_normals<DIM, false><<<lr_loop_blocks((long long)NN * c->ct.nf, TB), TB, 0, s>>>(
+            sp, c->p, c->nd, c->mats, c->lr_start, c->lr_list, c->lr_cnt, c->lr_out, NN, c->lr_cap,
+            c->ct.normals == 6 ? 1 : 0, supports_only);
         c->launches++;
     };
     if (lr) {
@@ -95,9 +108,12 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
         cudaMemsetAsync(c->lr_cnt, 0, (size_t)m * sizeof(int), s);
         k_lr_link<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd, c->lr_cnt, c->lr_start, c->lr_list,
                                                             c->lr_cap, 1);
-        k_lr_order<<<lrb, TB, 0, s>>>(c->lr_start, c->lr_list, c->orig, NN, c->lr_cap);
-        c->launches += 6;
-        lr_normals();
+        // the nodes with links, listed in c->lr_cnt (no longer needed as the cursor)
+        cudaMemsetAsync(c->lr_cnt + NN, 0, sizeof(int), s);
+        k_lr_compact<<<(NN + TB - 1) / TB, TB, 0, s>>>(c->lr_start, c->lr_cnt, NN);
+        k_lr_order<<<lr_loop_blocks(NN, TB), TB, 0, s>>>(c->lr_start, c->lr_list, c->orig, c->lr_cnt, NN, c->lr_cap);
+        c->launches += 7;
+        lr_normals(0);
     }
     mark(0, false);
     mark(1, true);
@@ -128,7 +144,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     }
     mark(2, false);
     mark(3, true);
-    if (lr) lr_normals();  // the deformed radii changed with the strain update
+    if (lr) lr_normals(1);  // same positions, deformed radii changed with the strain update
     k_node_update<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group,
                                                      c->ct.nf > 1 && method != MPMGPU_USF, xk > 1 ? 0 : 1);
     mark(3, false);
@@ -154,7 +170,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     }
     mark(4, false);
     mark(5, true);
-    if (lr) lr_normals();  // the particles moved
+    if (lr) lr_normals(0);  // the particles moved
     k_node_usl<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, NN, c->bcs, c->bc_group);
     mark(5, false);
     mark(6, true);

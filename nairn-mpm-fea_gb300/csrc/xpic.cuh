@@ -1,5 +1,6 @@
-// xpic.cuh -- PeriodicXPIC grid velocities (XPIC(k) and FMPM(k)) of a
-// single-run context with one material velocity field.
+// xpic.cuh -- PeriodicXPIC grid velocities (XPIC(k) and FMPM(k)): single-run
+// contexts (any number of material velocity fields, with multimaterial
+// contact) and batches (one field).
 //
 // XPICExtrapolationTask::Execute (NairnMPM/src/NairnMPM_Class/
 // XPICExtrapolationTask.cpp:50-160) expands the grid velocity in k terms:
@@ -16,19 +17,24 @@
 // node i (1 / m_i kept per node).  It is the reference's sum in another
 // order.  The FP64 mode sums in FP64; the mixed mode gathers and scatters
 // FP32 copies (FP32 atomics) and keeps v*(prev), Delta v and v* in FP64.
+//
+// Every column is per field-node (field f of node n at f fstride + n); a
+// particle's passes use its material's field.  With multimaterial contact the
+// pass's Delta v is completed in three kernels: GET_DELTAV and the velocity
+// conditions (k_xpic_delta with defer), the incremental contact of every
+// contact node (k_xpic_contact), then UPDATE_VSTAR (k_xpic_apply).
 #pragma once
 
 namespace nmg {
 
-// v*(prev) / Delta v, v*(next) and 1 / mass of each node (single material
-// field), and their FP32 copies of the mixed mode's particle passes
+// v*(prev) / Delta v, v*(next) and 1 / mass of each field-node, and the FP32
+// copies of v*(prev) and v*(next) for the mixed mode's particle passes
 struct DevXpic {
     double *px, *py, *pz;
     double *nx, *ny, *nz;
     double *rm;
     float *fpx, *fpy, *fpz;
     float *fnx, *fny, *fnz;
-    float *frm;
 };
 
 // Expansion phases: before a strain update (FMPM only) or before the
@@ -101,7 +107,6 @@ static __global__ void k_xpic_init(StepParams sp, DevNodes nd, DevXpic x, int nn
         x.fnx[n] = 0.f;
         x.fny[n] = 0.f;
         x.fnz[n] = 0.f;
-        x.frm[n] = (float)(1. / m);
     }
     xpic_store_velocity<MIX>(nd, n, vs);
 }
@@ -110,7 +115,7 @@ static __global__ void k_xpic_init(StepParams sp, DevNodes nd, DevXpic x, int nn
 // v*(next)_i += m_p S_ip / m_i Sum_j S_jp v*(prev)_j
 template <int DIM, int SHAPE, bool MIX, bool BATCH>
 static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
-    k_xpic_pass(StepParams sp, DevParticles p, DevXpic x, int phase, int k) {
+    k_xpic_pass(StepParams sp, DevParticles p, DevXpic x, const DevMat *mats, int phase, int k) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;
     if (i >= p.n) return;
@@ -118,9 +123,10 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
     if (!xpic_takes_part(BATCH ? sp.runs[p.run[i]].xpic : sp.xpic, phase, k)) return;
     const DevGrid &g = rv.g;
+    const int nb = rv.nb + field_offset(sp, mats, p, i);
     T s[3] = {0, 0, 0};
-    visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, [&](int n, T N, T, T, T) {
-        if (N == T(0)) return;
+    visit_nodes<DIM, SHAPE, false, T>(g, nb, p, i, [&](int n, T N, T, T, T) {
+        if (zero_weight(N)) return;
         if (MIX) {
             s[0] += x.fpx[n] * N;
             s[1] += x.fpy[n] * N;
@@ -132,10 +138,12 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
         }
     });
     const T mp = (T)p.mass[i];
-    visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, [&](int n, T N, T, T, T) {
-        if (N == T(0)) return;
+    visit_nodes<DIM, SHAPE, false, T>(g, nb, p, i, [&](int n, T N, T, T, T) {
+        if (zero_weight(N)) return;
         if (MIX) {
-            const float w = mp * N * x.frm[n];
+            // m_p S_ip s in FP32; the division by m_i is FP64, in k_xpic_delta (an
+            // FP32 1/m_i overflows at nodes that only a support's edge reaches)
+            const float w = mp * N;
             atomicAdd(&x.fnx[n], w * s[0]);
             atomicAdd(&x.fny[n], w * s[1]);
             if (DIM == 3) atomicAdd(&x.fnz[n], w * s[2]);
@@ -150,10 +158,12 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
 
 // GET_DELTAV, the velocity conditions' zero directions (NodalVelBC::
 // GridVelocityConditions for the XPIC passes, NodalVelBC.cpp:327-334, and
-// MatVelocityField::ZeroVelocityBC, MatVelocityField.cpp:530-541), UPDATE_VSTAR
+// MatVelocityField::ZeroVelocityBC, MatVelocityField.cpp:530-541), UPDATE_VSTAR.
+// defer: stop after the velocity conditions with Delta v in v*(prev), for the
+// incremental contact and k_xpic_apply.
 template <int DIM, bool MIX, bool BATCH>
 static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int nnodes, DevBCs b,
-                                    const int *bc_group, int phase, int k) {
+                                    const int *bc_group, int phase, int k, int defer) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes || !nd.active[n]) return;
     double t, dt;
@@ -161,15 +171,16 @@ static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int n
     if (!xpic_takes_part(BATCH ? sp.runs[sp.nrun[n]].xpic : sp.xpic, phase, k)) return;
     double d[3];
     if (MIX) {
-        d[0] = x.px[n] - (double)x.fnx[n];
-        d[1] = x.py[n] - (double)x.fny[n];
-        d[2] = DIM == 3 ? x.pz[n] - (double)x.fnz[n] : 0.;
+        const double rm = x.rm[n];
+        d[0] = x.px[n] - (double)x.fnx[n] * rm;
+        d[1] = x.py[n] - (double)x.fny[n] * rm;
+        d[2] = DIM == 3 ? x.pz[n] - (double)x.fnz[n] * rm : 0.;
     } else {
         d[0] = x.px[n] - x.nx[n];
         d[1] = x.py[n] - x.ny[n];
         d[2] = DIM == 3 ? x.pz[n] - x.nz[n] : 0.;
     }
-    const int grp = bc_group[n];
+    const int grp = bc_group[sp.ct.nf > 1 ? n % sp.ct.fstride : n];
     if (grp >= 0) {
         for (int e = b.start[grp]; e < b.start[grp + 1]; e++) {
             if (t < b.ftime[e]) continue;
@@ -180,10 +191,22 @@ static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int n
             for (int a = 0; a < 3; a++) d[a] += nrm[a] * (-dotn);
         }
     }
-    const double v[3] = {nd.vx[n] + d[0], nd.vy[n] + d[1], DIM == 3 ? nd.vz[n] + d[2] : 0.};
     x.px[n] = d[0];
     x.py[n] = d[1];
     x.pz[n] = d[2];
+    if (defer) {
+        if (MIX) {
+            x.fnx[n] = 0.f;
+            x.fny[n] = 0.f;
+            x.fnz[n] = 0.f;
+        } else {
+            x.nx[n] = 0.;
+            x.ny[n] = 0.;
+            x.nz[n] = 0.;
+        }
+        return;
+    }
+    const double v[3] = {nd.vx[n] + d[0], nd.vy[n] + d[1], DIM == 3 ? nd.vz[n] + d[2] : 0.};
     if (MIX) {
         x.fpx[n] = (float)d[0];
         x.fpy[n] = (float)d[1];
@@ -196,6 +219,108 @@ static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int n
         x.ny[n] = 0.;
         x.nz[n] = 0.;
     }
+    xpic_store_velocity<MIX>(nd, n, v);
+}
+
+// XPICExtrapolationTask::ImposeIncrementalContact (XPICExtrapolationTask.cpp:
+// 246-258) for material contact: MaterialContactNode::NodalXPICIncrement ->
+// CrackVelocityFieldMulti::MaterialXPICIncrementOnCVF (CrackVelocityFieldMulti.
+// cpp:1333-1514), Coulomb friction, no rigid fields.  One thread per node with
+// two or more fields: each field's Delta v (in v*(prev)) moves by the increment
+// of the contact law applied to the node's cached contact state -- the
+// momentum change toward the centre of mass of the Delta v's, accumulated over
+// the passes in priorDelPiZero, less what earlier passes applied (netDelPi);
+// with two fields the other moves by the opposite change.  The reference also
+// moves the node force (XPIC's particle update only), which nothing after
+// the expansion reads, so it is left out.
+template <int DIM, bool MIX>
+static __global__ void k_xpic_contact(StepParams sp, DevNodes nd, DevXpic x, int nnodes, int phase, int k) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nnodes) return;
+    if (!xpic_takes_part(sp.xpic, phase, k)) return;
+    const DevContact &ct = sp.ct;
+    const int S = ct.fstride;
+    int nm = 0;
+    for (int f = 0; f < ct.nf; f++) nm += nd.active[f * S + n] ? 1 : 0;
+    if (nm <= 1) return;
+    bool hasCOM = false;
+    double Pc[3] = {0., 0., 0.}, Mc = 0.;
+    for (int i = 0; i < ct.nf; i++) {
+        const int ki = i * S + n;
+        if (!nd.active[ki]) continue;
+        const int pair = ct.xc_pair[ki];
+        if (pair < -1) continue;  // no contact state from this step's last contact call
+        const bool isPaired = pair >= 0;
+        if (!hasCOM) {
+            for (int f = 0; f < ct.nf; f++) {
+                const int kk = f * S + n;
+                if (!nd.active[kk]) continue;
+                Pc[0] += x.px[kk] * nd.mass[kk];
+                Pc[1] += x.py[kk] * nd.mass[kk];
+                Pc[2] += x.pz[kk] * nd.mass[kk];
+                Mc += nd.mass[kk];
+            }
+            hasCOM = true;
+        }
+        const double mi = nd.mass[ki];
+        const double mred = mi * (1. - mi / Mc), r = mi / Mc;
+        double delPi[3] = {Pc[0] * r, Pc[1] * r, Pc[2] * r};
+        delPi[0] += x.px[ki] * -mi;
+        delPi[1] += x.py[ki] * -mi;
+        delPi[2] += x.pz[ki] * -mi;
+        double *xc = ct.xc + kXcDoubles * (size_t)ki;
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            delPi[a] += xc[4 + a];
+            xc[4 + a] = delPi[a];
+        }
+        const double norm[3] = {xc[1], xc[2], xc[3]};
+        const double dotn = dot3(delPi, norm);
+        const double dfi[3] = {xc[10], xc[11], xc[12]};
+        if (!coulomb_delta(ct, delPi, norm, dotn, xc[0], mred, dfi, sp.dt)) {
+            // out of contact now: undo what earlier passes applied, if anything
+            const bool zero = xc[7] == 0. && xc[8] == 0. && (DIM == 2 || xc[9] == 0.);
+            if (zero) {
+                if (isPaired) break;
+                continue;
+            }
+            delPi[0] = delPi[1] = delPi[2] = 0.;
+        }
+#pragma unroll
+        for (int a = 0; a < 3; a++) {
+            const double net = delPi[a];
+            delPi[a] -= xc[7 + a];
+            xc[7 + a] = net;
+        }
+        const double rm = 1. / mi;
+        x.px[ki] += delPi[0] * rm;
+        x.py[ki] += delPi[1] * rm;
+        x.pz[ki] += delPi[2] * rm;
+        if (isPaired) {
+            const int kj = pair * S + n;
+            const double rmj = -1. / nd.mass[kj];
+            x.px[kj] += delPi[0] * rmj;
+            x.py[kj] += delPi[1] * rmj;
+            x.pz[kj] += delPi[2] * rmj;
+            break;
+        }
+    }
+}
+
+// UPDATE_VSTAR after the incremental contact: v* += Delta v, and the FP32
+// copy of Delta v for the next pass (mixed mode)
+template <int DIM, bool MIX>
+static __global__ void k_xpic_apply(StepParams sp, DevNodes nd, DevXpic x, int nnodes, int phase, int k) {
+    const int n = blockIdx.x * blockDim.x + threadIdx.x;
+    if (n >= nnodes || !nd.active[n]) return;
+    if (!xpic_takes_part(sp.xpic, phase, k)) return;
+    const double d[3] = {x.px[n], x.py[n], DIM == 3 ? x.pz[n] : 0.};
+    if (MIX) {
+        x.fpx[n] = (float)d[0];
+        x.fpy[n] = (float)d[1];
+        x.fpz[n] = (float)d[2];
+    }
+    const double v[3] = {nd.vx[n] + d[0], nd.vy[n] + d[1], DIM == 3 ? nd.vz[n] + d[2] : 0.};
     xpic_store_velocity<MIX>(nd, n, v);
 }
 

@@ -175,6 +175,10 @@ class MpmGpuBatchOptions(C.Structure):
                 ("xpic_period", C.c_int32)]
 
 
+class MpmGpuRunLoad(C.Structure):
+    _fields_ = [("n", C.c_int64), ("steps_left", C.c_int32), ("steps_total", C.c_int32), ("elapsed_ms", C.c_double)]
+
+
 class MpmGpuBatchInfo(C.Structure):
     _fields_ = [("runs", C.c_int32), ("running", C.c_int32), ("block", C.c_int32), ("sort_interval", C.c_int32),
                 ("particles_used", C.c_int64), ("particles_dead", C.c_int64), ("nodes_used", C.c_int64),
@@ -191,7 +195,7 @@ class MpmGpuServerOptions(C.Structure):
                 ("nodes_per_particle", C.c_double), ("fraction_usf", C.c_double),
                 ("max_resident_particles", C.c_int64), ("order", C.c_int32), ("max_fields", C.c_int32),
                 ("lr_links", C.c_int32), ("xpic_order", C.c_int32), ("xpic_fmpm", C.c_int32),
-                ("xpic_period", C.c_int32)]
+                ("xpic_period", C.c_int32), ("slowdown_target", C.c_double)]
 
 
 class MpmGpuRequestInfo(C.Structure):

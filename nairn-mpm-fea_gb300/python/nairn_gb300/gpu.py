@@ -106,6 +106,8 @@ def lib():
         "mpmgpu_server_stats": ([VP, P(abi.MpmGpuServerStats)], C.c_int),
         "mpmgpu_server_last_error": ([VP], C.c_char_p),
         "mpmgpu_server_destroy": ([VP], None),
+        "mpmgpu_server_admits": ([C.c_double, C.c_double, C.c_double, P(abi.MpmGpuRunLoad), C.c_int32, C.c_int64,
+                                  C.c_int32, C.c_double], C.c_int),
     }
     for f, (args, res) in batch_sigs.items():
         getattr(L, f).argtypes = args
@@ -382,6 +384,17 @@ class GpuBatch:
             pass
 
 
+SERVER_ORDERS = {"fifo": 0, "least_work": 1, "deadline": 2}
+
+
+def server_admits(a_ms: float, b_ms: float, k: float, running, cand_n: int, cand_steps: int,
+                  cand_waited_ms: float) -> int:
+    """The deadline order's admission rule (mpmgpu_server_admits): running is
+    a list of (n, steps_left, steps_total, elapsed_ms)."""
+    arr = (abi.MpmGpuRunLoad * max(1, len(running)))(*[abi.MpmGpuRunLoad(*r) for r in running])
+    return lib().mpmgpu_server_admits(a_ms, b_ms, k, arr, len(running), cand_n, cand_steps, cand_waited_ms)
+
+
 class GpuServer:
     """Continuous-batching request loop on the current GPU (mpmgpu_server_*):
     a C++ thread admits submitted runs against the HBM budget, advances all
@@ -392,14 +405,14 @@ class GpuServer:
                  max_runs: int = 256, steps_per_round: int = 10, backfill: bool = True, sort_interval: int = 1,
                  block: int = 0, frac_3d: float = 0.5, nodes_per_particle: float = 0.5, fraction_usf: float = 0.5,
                  max_resident_particles: int = 0, order: str = "fifo", max_fields: int = 1, lr_links: int = 0,
-                 xpic=None):
+                 xpic=None, slowdown_target: float = 0.0):
         L = lib()
         xo, xf, xp = xpic if xpic else (0, 0, 1)
         o = abi.MpmGpuServerOptions(method, shape, precision, max_runs, steps_per_round, 1 if backfill else 0,
                                     sort_interval, block, int(hbm_budget_bytes), frac_3d, nodes_per_particle,
                                     fraction_usf, int(max_resident_particles),
-                                    {"fifo": 0, "least_work": 1}[order], int(max_fields), int(lr_links),
-                                    int(xo), int(xf), int(xp))
+                                    SERVER_ORDERS[order], int(max_fields), int(lr_links),
+                                    int(xo), int(xf), int(xp), float(slowdown_target))
         h = C.c_void_p()
         st = L.mpmgpu_server_create(C.byref(o), C.byref(h))
         if st != 0:

@@ -192,10 +192,12 @@ def _mm_mode(normals: int, friction: float) -> str:
 
 def contact_2d(plate=(20, 4), block=(6, 4), block_x0=5.0, gap=0.0, cell=1.0, ppc_side=2, v=(2000., -2000.),
                plate_mat=None, block_mat=None, friction=0.3, normals=2, steps=200, cfl=0.4, gimp="uGIMP",
-               method=2, margin_cells=4, archive_root: str = "Results/contact.", inc_terms: int = 0) -> tuple[str, dict]:
+               method=2, margin_cells=4, archive_root: str = "Results/contact.", inc_terms: int = 0,
+               xpic=None) -> tuple[str, dict]:
     """2D plane-strain multimaterial contact: a block (plate=(nx, ny) and
     block=(nx, ny) in cells) moving at v onto an elastic plate whose base is
-    held; materials (type, properties) as dicts for material_xml."""
+    held; materials (type, properties) as dicts for material_xml; optionally
+    a PeriodicXPIC task (xpic_xml)."""
     pm = dict(mat_type=1, rho=2.7, E=70000., nu=0.33) if plate_mat is None else dict(plate_mat)
     bm = dict(mat_type=28, rho=1.1, G=10., K=50.) if block_mat is None else dict(block_mat)
     Lp, Hp = plate[0] * cell, plate[1] * cell
@@ -230,7 +232,7 @@ def contact_2d(plate=(20, 4), block=(6, 4), block_x0=5.0, gap=0.0, cell=1.0, ppc
       <DisBC dir="2" disp="0"/>
     </BCLine>
   </GridBCs>
-</JANFEAInput>
+{xpic_xml(xpic)}</JANFEAInput>
 """
     return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 2}
 
@@ -238,9 +240,10 @@ def contact_2d(plate=(20, 4), block=(6, 4), block_x0=5.0, gap=0.0, cell=1.0, ppc
 def contact_3d(plate=(12, 12, 3), block=(4, 4, 3), block_x0=4.0, block_y0=4.0, gap=0.0, cell=0.5, ppc_side=2,
                v=(4000., 0., -4000.), plate_mat=None, block_mat=None, friction=0.3, normals=2, steps=100, cfl=0.5,
                gimp="lCPDI", method=2, margin_cells=4, archive_root: str = "Results/contact3.",
-               inc_terms: int = 0) -> tuple[str, dict]:
+               inc_terms: int = 0, xpic=None) -> tuple[str, dict]:
     """3D multimaterial contact (the config-3 form): a Neo-Hookean block
-    pressed and sliding on an elastic plate whose base plane is held."""
+    pressed and sliding on an elastic plate whose base plane is held;
+    optionally a PeriodicXPIC task (xpic_xml)."""
     pm = dict(mat_type=1, rho=2.7, E=70000., nu=0.33) if plate_mat is None else dict(plate_mat)
     bm = dict(mat_type=28, rho=1.1, G=10., K=50.) if block_mat is None else dict(block_mat)
     Lx, Ly, Hp = plate[0] * cell, plate[1] * cell, plate[2] * cell
@@ -277,7 +280,7 @@ def contact_3d(plate=(12, 12, 3), block=(4, 4, 3), block_x0=4.0, block_y0=4.0, g
       <DisBC dir="3" disp="0"/>
     </BCBox>
   </GridBCs>
-</JANFEAInput>
+{xpic_xml(xpic)}</JANFEAInput>
 """
     return xml, {"dt": dt, "steps": steps, "maxtime": maxtime, "dim": 3}
 

@@ -545,7 +545,7 @@ def _mat_from(d, default):
 
 def contact_2d(plate=(20, 4), block=(6, 4), block_x0=5.0, gap=0.0, cell=1.0, ppc_side=2, v=(2000., -2000.),
                plate_mat=None, block_mat=None, friction=0.3, normals=2, steps=200, cfl=0.4, gimp="uGIMP",
-               method=USAVG, margin_cells=4, inc_terms=0, **_ignored) -> Model:
+               method=USAVG, margin_cells=4, inc_terms=0, xpic=None, **_ignored) -> Model:
     """Model of inputs.contact_2d (same arguments): plate in material field 0,
     block in field 1, multimaterial contact on."""
     from . import inputs
@@ -577,13 +577,14 @@ def contact_2d(plate=(20, 4), block=(6, 4), block_x0=5.0, gap=0.0, cell=1.0, ppc
     dt = inputs.cfl_timestep(g.dx, c, cfl)
     opts = dict(np=PLANE_STRAIN, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
                 inc_defgrad_terms=inc_terms if inc_terms > 0 else 2, nfields=2)
+    _xpic_options(opts, xpic)
     return Model(g, p, [pm, bm], bcs, opts, steps, name="contact_2d",
                  extra={"contact": _contact_options(normals, friction)})
 
 
 def contact_3d(plate=(12, 12, 3), block=(4, 4, 3), block_x0=4.0, block_y0=4.0, gap=0.0, cell=0.5, ppc_side=2,
                v=(4000., 0., -4000.), plate_mat=None, block_mat=None, friction=0.3, normals=2, steps=100, cfl=0.5,
-               gimp="lCPDI", method=USAVG, margin_cells=4, inc_terms=0, **_ignored) -> Model:
+               gimp="lCPDI", method=USAVG, margin_cells=4, inc_terms=0, xpic=None, **_ignored) -> Model:
     """Model of inputs.contact_3d (same arguments)."""
     from . import inputs
     shape = GIMP_NAMES[gimp]
@@ -618,6 +619,7 @@ def contact_3d(plate=(12, 12, 3), block=(4, 4, 3), block_x0=4.0, block_y0=4.0, g
     dt = inputs.cfl_timestep(g.dx, c, cfl)
     opts = dict(np=THREED, method=method, shape=shape, timestep=dt, fraction_usf=0.5,
                 inc_defgrad_terms=inc_terms if inc_terms > 0 else 1, nfields=2)
+    _xpic_options(opts, xpic)
     return Model(g, p, [pm, bm], bcs, opts, steps, name="contact_3d",
                  extra={"contact": _contact_options(normals, friction)})
 

@@ -1153,6 +1153,15 @@ typedef struct {
     int xpic;               /* this step: 0 FLIP, k > 0 FMPM(k), -k XPIC(k) (GridToParticleExtrap::m) */
     double *vpx, *vpy, *vpz;  /* XPIC v*(prev) (MatVelocityField vk[VSTARPREV_VEC]) */
     double *vnx, *vny, *vnz;  /* XPIC v*(next) (vk[VSTARNEXT_VEC]) */
+    /* XPIC/FMPM(k > 1) with contact: each contact node's FMPMContact cache
+     * (Common/System/DataTypes.hpp:90-104) per field, set at every contact call */
+    char *xc_valid;         /* the cache was set this step (MaterialContactNode is per step) */
+    int *xc_paired;         /* the other field when doing pairs, else -1 */
+    double *xc_deln;        /* deltaDotn */
+    double *xc_n;           /* norm (3 per field-node) */
+    double *xc_prior;       /* priorDelPiZero (3) */
+    double *xc_net;         /* netDelPi (3) */
+    double *xc_dfi;         /* startDelFi (3) */
     int rigid_field[64];    /* field f holds a rigid contact material (MatVelocityField::IsRigidField) */
     int has_rigid;          /* some material is rigid */
     double rigid_bias;      /* MeshInfo::rigidGradientBias, squared (MeshInfo.cpp:1191) */
@@ -1551,6 +1560,94 @@ static int xpic_step_order(const MpmGpuOptions *o, long s) {
     return o->xpic_fmpm ? o->xpic_order : -o->xpic_order;
 }
 
+static int coulomb_delta(const OCtx *c, double *delPi, const double *norm, double dotn, double deln, double mred,
+                         const double *delFi);
+static double dot3(const double *a, const double *b);
+
+/* XPICExtrapolationTask::ImposeIncrementalContact (XPICExtrapolationTask.cpp:
+ * 246-258) for material contact: MaterialContactNode::NodalXPICIncrement and
+ * CrackVelocityFieldMulti::MaterialXPICIncrementOnCVF (CrackVelocityFieldMulti.
+ * cpp:1333-1514) on every node with two or more material fields, Coulomb
+ * friction, no rigid fields.  Each field's Delta v(k) (v*(prev) here) is moved
+ * by the increment of the contact law applied to the cached contact state of
+ * the last contact call; XPIC's particle update also moves the node force. */
+static void xpic_contact(OCtx *c, int particle_update) {
+    OField *f = &c->f;
+    const int nf = c->nf, is3d = c->g.dim == 3;
+    const int xpic_force = particle_update && c->xpic < 0;
+    const double dt = c->dt;
+    for (long n = 1; n <= c->g.nnodes; n++) {
+        int nm = 0;
+        for (int fl = 0; fl < nf; fl++) nm += f->npts[fl * c->nn + n] > 0 ? 1 : 0;
+        if (nm <= 1) continue;
+        int hasCOM = 0;
+        double Pc[3] = {0., 0., 0.}, Mc = 0.;
+        for (int i = 0; i < nf; i++) {
+            long ki = i * c->nn + n;
+            if (f->npts[ki] <= 0) continue;
+            if (!c->xc_valid[ki]) continue;
+            int isPaired = c->xc_paired[ki] >= 0;
+            if (!hasCOM) {
+                for (int ii = 0; ii < nf; ii++) {
+                    long kk = ii * c->nn + n;
+                    if (f->npts[kk] <= 0) continue;
+                    Pc[0] += c->vpx[kk] * f->mass[kk];
+                    Pc[1] += c->vpy[kk] * f->mass[kk];
+                    Pc[2] += c->vpz[kk] * f->mass[kk];
+                    Mc += f->mass[kk];
+                }
+                hasCOM = 1;
+            }
+            double mi = f->mass[ki];
+            double mred = mi * (1. - mi / Mc);
+            double r = mi / Mc;
+            double delPi[3] = {Pc[0] * r, Pc[1] * r, Pc[2] * r};
+            delPi[0] += c->vpx[ki] * -mi;
+            delPi[1] += c->vpy[ki] * -mi;
+            delPi[2] += c->vpz[ki] * -mi;
+            double *prior = &c->xc_prior[3 * ki], *net = &c->xc_net[3 * ki];
+            for (int a = 0; a < 3; a++) delPi[a] += prior[a];
+            for (int a = 0; a < 3; a++) prior[a] = delPi[a];
+            const double *norm = &c->xc_n[3 * ki];
+            double dotn = dot3(delPi, norm);
+            if (!coulomb_delta(c, delPi, norm, dotn, c->xc_deln[ki], mred, &c->xc_dfi[3 * ki])) {
+                int zero = net[0] == 0. && net[1] == 0. && (!is3d || net[2] == 0.);
+                if (!zero) {
+                    delPi[0] = delPi[1] = delPi[2] = 0.;
+                } else {
+                    if (isPaired) break;
+                    continue;
+                }
+            }
+            double newDelPi[3] = {delPi[0], delPi[1], delPi[2]};
+            for (int a = 0; a < 3; a++) delPi[a] -= net[a];
+            for (int a = 0; a < 3; a++) net[a] = newDelPi[a];
+            double rm = 1. / mi, rdt = 1. / dt;
+            c->vpx[ki] += delPi[0] * rm;
+            c->vpy[ki] += delPi[1] * rm;
+            c->vpz[ki] += delPi[2] * rm;
+            if (xpic_force) {
+                f->fx[ki] += delPi[0] * rdt;
+                f->fy[ki] += delPi[1] * rdt;
+                f->fz[ki] += delPi[2] * rdt;
+            }
+            if (isPaired) {
+                long kj = (long)c->xc_paired[ki] * c->nn + n;
+                double rmj = -1. / f->mass[kj], rdtj = -1. / dt;
+                c->vpx[kj] += delPi[0] * rmj;
+                c->vpy[kj] += delPi[1] * rmj;
+                c->vpz[kj] += delPi[2] * rmj;
+                if (xpic_force) {
+                    f->fx[kj] += delPi[0] * rdtj;
+                    f->fy[kj] += delPi[1] * rdtj;
+                    f->fz[kj] += delPi[2] * rdtj;
+                }
+                break;
+            }
+        }
+    }
+}
+
 /* XPICExtrapolationTask::Execute (XPICExtrapolationTask.cpp:50-160) with
  * MatVelocityField::XPICSupport (MatVelocityField.cpp:318-399), single
  * material field: v(k) of the order-k expansion in f->v (VSTAR_VEC is vk[0]).
@@ -1564,7 +1661,6 @@ static void xpic_extrapolate(OCtx *c, int order, int particle_update) {
     const long nn = c->nfn;
     const double dt = c->dt;
     const int fmpm = c->xpic > 0;
-    (void)particle_update;
     /* INITIALIZE_XPIC */
     for (long i = 1; i < nn; i++) {
         c->vnx[i] = 0.; c->vny[i] = 0.; c->vnz[i] = 0.;
@@ -1619,6 +1715,8 @@ static void xpic_extrapolate(OCtx *c, int order, int particle_update) {
                 double dotn = c->vpx[i] * n[0] + c->vpy[i] * n[1] + c->vpz[i] * n[2];
                 c->vpx[i] += n[0] * (-dotn); c->vpy[i] += n[1] * (-dotn); c->vpz[i] += n[2] * (-dotn);
             }
+        /* incremental material contact */
+        if (c->mm) xpic_contact(c, particle_update);
         /* UPDATE_VSTAR: v* += Delta v(k), v*(next) = 0 */
         for (long i = 1; i < nn; i++) {
             if (f->npts[i] == 0) continue;
@@ -2252,6 +2350,19 @@ static void material_contact(OCtx *c, int callType) {
             double dispb[3] = {delta[0] + dispa[0], delta[1] + dispa[1], delta[2] + dispa[2]};
             double deln = hasDeln ? lrDeln : dot3(dispb, norm) - dot3(dispa, norm);
             mred *= massi;
+            /* MaterialContactNode::SetContactInfo (MaterialContactNode.cpp:133-151) */
+            const int xcache = c->xc_valid && (c->xpic > 1 || c->xpic < -1);
+            if (xcache) {
+                c->xc_valid[ki] = 1;
+                c->xc_paired[ki] = doingPairs ? j : -1;
+                c->xc_deln[ki] = deln;
+                for (int a = 0; a < 3; a++) {
+                    c->xc_n[3 * ki + a] = norm[a];
+                    c->xc_prior[3 * ki + a] = delPi[a];
+                    c->xc_net[3 * ki + a] = 0.;
+                    c->xc_dfi[3 * ki + a] = 0.;
+                }
+            }
             double delFi[3], *dfp = NULL;
             if (postUpdate) {
                 double Fc[3] = {0., 0., 0.};
@@ -2267,9 +2378,14 @@ static void material_contact(OCtx *c, int callType) {
                 delFi[1] = Fc[1] * r + f->fy[ki] * -1.;
                 delFi[2] = Fc[2] * r + f->fz[ki] * -1.;
                 dfp = delFi;
+                if (xcache)
+                    for (int a = 0; a < 3; a++) c->xc_dfi[3 * ki + a] = delFi[a];
             }
             if (!coulomb_delta(c, delPi, norm, dotn, deln, mred, dfp)) continue;
             change_momentum(c, ki, delPi, callType);
+            /* MaterialContactNode::ContactSetDelPi */
+            if (xcache)
+                for (int a = 0; a < 3; a++) c->xc_net[3 * ki + a] = delPi[a];
             if (doingPairs) {
                 for (int a = 0; a < 3; a++) delPi[a] *= -1.;
                 change_momentum(c, (long)j * c->nn + n, delPi, callType);
@@ -2311,6 +2427,8 @@ static int one_step(OCtx *c) {
         if (f->npts[i] > 0) { f->cx[i] = f->px[i]; f->cy[i] = f->py[i]; f->cz[i] = f->pz[i]; }
     }
     if (c->mm && c->normals >= 5) lr_build_lists(c);
+    /* the step's MaterialContactNodes are new (PostExtrapolationTask.cpp:74-79) */
+    if (c->xc_valid) memset(c->xc_valid, 0, (size_t)c->nfn);
     if (c->mm) material_contact(c, MASS_MOMENTUM_CALL);
     if (method == MPMGPU_USF || method == MPMGPU_USAVG) velocity_bc_loop(c, MASS_MOMENTUM_CALL);
 
@@ -2455,13 +2573,20 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
         c.lr_list = (long *)calloc((size_t)(p->n > 0 ? p->n : 1) * 64, sizeof(long));
     }
     if (opts->xpic_order > 0) {
-        if (c.mm) {
+        if (c.mm && c.has_rigid) {
             free(c.mats);
-            return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: XPIC/FMPM with multimaterial contact not implemented");
+            return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: XPIC/FMPM with rigid contact materials not implemented");
         }
         if (opts->xpic_period < 1) { free(c.mats); return fail(MPMGPU_ERR_INVALID, "oracle: xpic_period < 1"); }
         double **xv[] = {&c.vpx, &c.vpy, &c.vpz, &c.vnx, &c.vny, &c.vnz};
         for (unsigned k = 0; k < 6; k++) *xv[k] = (double *)calloc((size_t)nn, sizeof(double));
+        if (c.mm) {
+            c.xc_valid = (char *)calloc((size_t)nn, 1);
+            c.xc_paired = (int *)calloc((size_t)nn, sizeof(int));
+            c.xc_deln = (double *)calloc((size_t)nn, sizeof(double));
+            double **xc[] = {&c.xc_n, &c.xc_prior, &c.xc_net, &c.xc_dfi};
+            for (unsigned k = 0; k < 4; k++) *xc[k] = (double *)calloc((size_t)nn * 3, sizeof(double));
+        }
     }
     c.mtime = t0;
     for (int s = 0; s < nsteps && st == MPMGPU_OK; s++) {
@@ -2475,6 +2600,8 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     free(c.lr_start);
     free(c.lr_list);
     free(c.vpx); free(c.vpy); free(c.vpz); free(c.vnx); free(c.vny); free(c.vnz);
+    free(c.xc_valid); free(c.xc_paired); free(c.xc_deln);
+    free(c.xc_n); free(c.xc_prior); free(c.xc_net); free(c.xc_dfi);
     free(c.mats);
     return st;
 }

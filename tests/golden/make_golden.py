@@ -122,6 +122,16 @@ CASES = {
     "rigid3d_taylor_wall": ("rigid_taylor_3d", dict(steps=40, friction=0.0, normals=2)),
     "rigid3d_taylor_wall_fric_usl": ("rigid_taylor_3d", dict(steps=40, friction=0.3, normals=0, method=3,
                                                              vx0=40000.)),
+    # PeriodicXPIC with multimaterial contact: the contact law re-applied to
+    # every expansion pass's increment from the last contact call's state
+    "contact2d_xpic2_fric": ("contact_2d", dict(steps=120, friction=0.3, normals=2, xpic=(2, 0, 1))),
+    "contact2d_fmpm2_fric_usl": ("contact_2d", dict(steps=120, friction=0.3, normals=2, method=3, xpic=(2, 1, 1))),
+    "contact2d_fmpm3_frictionless": ("contact_2d", dict(steps=120, friction=0.0, normals=0, xpic=(3, 1, 1))),
+    "contact2d_xpic3_stick_every2": ("contact_2d", dict(steps=120, friction=-1.0, normals=1, xpic=(3, 0, 2))),
+    "contact2d_xpic2_logreg": ("contact_2d", dict(steps=100, friction=0.3, normals=6, xpic=(2, 0, 1))),
+    "contact3d_xpic2_fric_cpdi": ("contact_3d", dict(steps=50, friction=0.3, normals=2, xpic=(2, 0, 1))),
+    "contact3d_fmpm2_fric_ugimp_usf": ("contact_3d", dict(steps=50, friction=0.3, normals=2, gimp="uGIMP",
+                                                          method=0, xpic=(2, 1, 1))),
 }
 
 KEEP = ("pos", "vel", "stress", "strain", "plastic", "work", "plastE", "hist1", "elem", "mass", "mat", "origpos")

@@ -208,14 +208,18 @@ def test_xpic_schedule_follows_the_step_time(gpu_lib):
 
 
 def test_xpic_refusals(gpu_lib):
-    """XPIC/FMPM is refused with multimaterial contact, and orders above 1
-    with deterministic node sums; a bad period is invalid."""
+    """XPIC/FMPM of order > 1 is refused with rigid contact materials and with
+    deterministic node sums; a bad period is invalid.  (With multimaterial
+    contact it runs: the XPIC contact goldens.)"""
     from nairn_gb300 import model
     from nairn_gb300.gpu import GpuRun, GpuError
-    c = model.contact_2d(plate=(16, 4), block=(5, 3), steps=5)
+    c = model.rigid_contact_2d(steps=5)
     c.options.update(xpic_order=2, xpic_fmpm=0, xpic_period=1)
+    r = GpuRun(c)
+    r.upload(c.particles)
     with pytest.raises(GpuError, match="UNSUPPORTED"):
-        GpuRun(c)
+        r.step(1)
+    r.close()
     m = model.cantilever_2d(nx=10, ny=4, steps=5, xpic=(2, 1, 1))
     with pytest.raises(GpuError, match="UNSUPPORTED"):
         GpuRun(m, p2g=1)

@@ -143,6 +143,31 @@ def test_resident_cap_serialises_runs(gpu_lib):
     s.close()
 
 
+def test_deadline_order_runs_every_request(gpu_lib):
+    """The deadline order (online step-time model, slowdown bound 1.5) with a
+    burst of requests: every request completes with the oracle's result, and
+    the server's step-time model has been fitted from its rounds."""
+    from nairn_gb300 import abi
+    ms = requests(10, seed=41)
+    s = server(0, steps_per_round=4, order="deadline", slowdown_target=1.5)
+    ids = [s.submit(m) for m in ms]
+    s.drain(600)
+    for rid, m in zip(ids, ms):
+        info = s.poll(rid)
+        assert info["state"] == abi.REQ_DONE and info["steps_done"] == m.nsteps, info
+        check(s.result(rid), oracle(m), m.grid.dim, TOL, m.name)
+    st = s.stats()
+    assert st["completed"] == len(ms) and st["failed"] == 0 and st["rounds"] > 0
+    s.close()
+
+
+def test_bad_server_orders_are_refused(gpu_lib):
+    from nairn_gb300.gpu import GpuError
+    for kw in (dict(order="deadline", slowdown_target=0.5),):
+        with pytest.raises(GpuError):
+            server(0, **kw)
+
+
 @pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
 def test_served_contact_runs(precision, tol, gpu_lib):
     """3D two-material contact requests (lCPDI, Coulomb friction) served
