@@ -180,17 +180,27 @@ __device__ __forceinline__ void elem_coords(const DevGrid &g, int e, int &col, i
 // FourNodeIsoparam::GetXiPos / EightNodeIsoparamBrick::GetXiPos for
 // rectangular elements (Common/Elements/FourNodeIsoparam.cpp:351-366,
 // NairnMPM/src/Elements/EightNodeIsoparamBrick.cpp:276-281).
+// a / b, as a product when b is a power of two (the exact reciprocal from the
+// exponent bits: the same bits as the quotient, without an FP64 division)
+__device__ __forceinline__ double quotient(double a, double b) {
+    const unsigned long long bb = (unsigned long long)__double_as_longlong(b);
+    const unsigned long long e = (bb >> 52) & 0x7ffull;
+    if ((bb & 0x000fffffffffffffull) == 0ull && e >= 1ull && e <= 2045ull)
+        return a * __longlong_as_double((long long)((bb & 0x8000000000000000ull) | ((2046ull - e) << 52)));
+    return a / b;
+}
+
 __device__ __forceinline__ void xi_position(const DevGrid &g, int e, double x, double y, double z,
                                             double &xi, double &eta, double &zeta) {
     int col, row, zr;
     elem_coords(g, e, col, row, zr);
     double x0 = g.xn[col], x1 = g.xn[col + 1];
     double y0 = g.yn[row], y1 = g.yn[row + 1];
-    xi = (2. * x - x0 - x1) / (x1 - x0);
-    eta = (2. * y - y0 - y1) / (y1 - y0);
+    xi = quotient(2. * x - x0 - x1, x1 - x0);
+    eta = quotient(2. * y - y0 - y1, y1 - y0);
     if (g.dim == 3) {
         double z0 = g.zn[zr], z1 = g.zn[zr + 1];
-        zeta = (2. * z - z0 - z1) / (z1 - z0);
+        zeta = quotient(2. * z - z0 - z1, z1 - z0);
     } else {
         zeta = 0.;
     }
@@ -341,6 +351,19 @@ __device__ __forceinline__ void bgimp_window(T xi, T lp, T idx, T sgn, Win4<T> &
         w.dS[j] = dS;
     }
 }
+
+// 1 / x.  When x is a power of two -- the usual cell sizes and particle
+// semi-sizes -- the reciprocal is exact and is built from the exponent bits
+// in the integer pipe, the same bits a division gives; otherwise the IEEE
+// quotient.  A double division is a dozen instructions of the FP64 pipe.
+__device__ __forceinline__ double recip(double x) {
+    const unsigned long long b = (unsigned long long)__double_as_longlong(x);
+    const unsigned long long e = (b >> 52) & 0x7ffull;
+    if ((b & 0x000fffffffffffffull) == 0ull && e >= 1ull && e <= 2045ull)
+        return __longlong_as_double((long long)((b & 0x8000000000000000ull) | ((2046ull - e) << 52)));
+    return 1. / x;
+}
+__device__ __forceinline__ float recip(float x) { return 1.f / x; }
 
 // A shape-function weight of exactly zero (+0 or -0): a node outside the
 // particle's support.  For doubles the test is on the bits, in the integer

@@ -160,9 +160,9 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
     const int n0 = nb + zr * g.zplane + row * g.yplane + col;  // first node (global index)
     // reciprocal element sizes, formed once (a gradient times 1/dx differs from
     // the reference's quotient by rounding only)
-    const T iDX = GRAD ? T(1) / (T)(g.xn[col + 1] - g.xn[col]) : T(0);
-    const T iDY = GRAD ? T(1) / (T)(g.yn[row + 1] - g.yn[row]) : T(0);
-    const T iDZ = GRAD && DIM == 3 ? T(1) / (T)(g.zn[zr + 1] - g.zn[zr]) : T(0);
+    const T iDX = GRAD ? recip((T)(g.xn[col + 1] - g.xn[col])) : T(0);
+    const T iDY = GRAD ? recip((T)(g.yn[row + 1] - g.yn[row])) : T(0);
+    const T iDZ = GRAD && DIM == 3 ? recip((T)(g.zn[zr + 1] - g.zn[zr])) : T(0);
     const T xi = (T)xi_d, eta = (T)eta_d, zeta = (T)zeta_d;
     if (SHAPE == SHAPE_LINEAR) {
         if (DIM == 2) {
@@ -240,7 +240,7 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
         bspline_window<T, GRAD>(xi, GRAD ? iDX : T(0), wx);
         bspline_window<T, GRAD>(eta, GRAD ? iDY : T(0), wy);
     } else {
-        const T ix = T(1) / (T(4) * lpx), iy = T(1) / (T(4) * lpy);
+        const T ix = recip(T(4) * lpx), iy = recip(T(4) * lpy);
         gimp_window<T, DIM == 3, GRAD>(xi, lpx, ix, T(2) * ix, GRAD ? T(2) * iDX : T(0), wx);
         gimp_window<T, DIM == 3, GRAD>(eta, lpy, iy, T(2) * iy, GRAD ? T(2) * iDY : T(0), wy);
     }
@@ -266,8 +266,8 @@ __device__ __forceinline__ void for_each_node(const DevGrid &g, int nb, int e, d
         } else {
             // the z factor is sized by lp.y (EightNodeIsoparamBrick.cpp:289-403); its
             // gradient by lp.z
-            const T iy = T(1) / (T(4) * lpy);
-            const T hz = !GRAD ? T(0) : (lpz == lpy ? T(2) * iy : T(1) / (T(2) * lpz));
+            const T iy = recip(T(4) * lpy);
+            const T hz = !GRAD ? T(0) : (lpz == lpy ? T(2) * iy : recip(T(2) * lpz));
             gimp_window<T, true, GRAD>(zeta, lpz, iy, hz, GRAD ? T(2) * iDZ : T(0), wz);
         }
         const int base3 = base + (wz.s - 1) * g.zplane;
@@ -801,9 +801,9 @@ __device__ __forceinline__ void axis_windows(const DevGrid &g, int col, int row,
                                              AxisWin<SHAPE, T> &w) {
     static_assert(SHAPE != SHAPE_LCPDI, "lCPDI nodes do not form a window");
     const T xi = (T)xi_d, eta = (T)eta_d, zeta = (T)zeta_d;
-    const T iD[3] = {GRAD ? T(1) / (T)(g.xn[col + 1] - g.xn[col]) : T(0),
-                     GRAD ? T(1) / (T)(g.yn[row + 1] - g.yn[row]) : T(0),
-                     GRAD && DIM == 3 ? T(1) / (T)(g.zn[zr + 1] - g.zn[zr]) : T(0)};
+    const T iD[3] = {GRAD ? recip((T)(g.xn[col + 1] - g.xn[col])) : T(0),
+                     GRAD ? recip((T)(g.yn[row + 1] - g.yn[row])) : T(0),
+                     GRAD && DIM == 3 ? recip((T)(g.zn[zr + 1] - g.zn[zr])) : T(0)};
     const int cc[3] = {col, row, zr};
     const T nat[3] = {xi, eta, zeta};
     w.c[2] = 0;
@@ -841,8 +841,8 @@ __device__ __forceinline__ void axis_windows(const DevGrid &g, int col, int row,
             } else {
                 // uGIMP: the 3D z factor is sized by lp.y (EightNodeIsoparamBrick.cpp:289-403),
                 // its gradient by lp.z
-                const T inv = T(1) / (T(4) * (a == 2 ? lp[1] : lp[a]));
-                const T hinv = !GRAD ? T(0) : (a < 2 || lp[2] == lp[1] ? T(2) * inv : T(1) / (T(2) * lp[2]));
+                const T inv = recip(T(4) * (a == 2 ? lp[1] : lp[a]));
+                const T hinv = !GRAD ? T(0) : (a < 2 || lp[2] == lp[1] ? T(2) * inv : recip(T(2) * lp[2]));
                 gimp_window<T, DIM == 3, GRAD>(nat[a], lp[a], inv, hinv, GRAD ? T(2) * iD[a] : T(0), q);
             }
 #pragma unroll
@@ -1274,7 +1274,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
 // mass accumulate in FP64 in both modes: grid velocities carry the bulk motion
 // and their differences across a cell are the strain rate.
 template <int DIM, int SHAPE, bool MIX, bool BATCH, bool DET = false>
-static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 3) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = tile_particle();
     if (i >= p.n) return;
@@ -1834,7 +1834,7 @@ __device__ __forceinline__ void g2p_move(const StepParams &sp, const DevParticle
 // NodalPoint::AddMassMomentumLast NodalPointMPM.cpp:470-486), which uses the
 // same natural coordinates of the step (USL), or with the element reset.
 template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH, bool DET = false>
-static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256, 2) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = tile_particle();
     if (i >= p.n) return;
