@@ -59,7 +59,7 @@ def check_state(v, g, step, tol, what):
 
 
 def test_full_goldens_present():
-    assert {"full_c1_cantilever", "full_c2_taylor_20", "full_c3_contact"} <= set(full_cases())
+    assert {"full_c1_cantilever", "full_c2_taylor_20", "full_c2_taylor", "full_c3_contact"} <= set(full_cases())
 
 
 def test_cantilever_builder_and_oracle_match_reference_full_length():
