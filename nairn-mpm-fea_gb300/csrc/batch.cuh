@@ -219,6 +219,8 @@ struct MpmGpuBatch {
     // PeriodicXPIC expansion columns (xpic_order > 1)
     DevXpic xpic{};
     double *xpic_block = nullptr;
+    double *xc = nullptr;     // XPIC contact state (in xpic_block), with several fields
+    int *xc_pair = nullptr;
     // materials, runs, velocity conditions
     DevMat *mats = nullptr;
     DevRun *runs_dev = nullptr;
@@ -407,6 +409,10 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     sp.ct.fstride = b->ncap;
     sp.ct.lr = b->lr_out;
     sp.ct.rigid = b->rigid_runs > 0 ? 1u : 0u;  // some particle may be rigid (the runs' masks are per run)
+    sp.ct.xc = b->xc;
+    sp.ct.xc_pair = b->xc_pair;
+    if (b->xc_pair)  // this step's contact state: none yet
+        cudaMemsetAsync(b->xc_pair, 0x80, (size_t)b->nf * b->ncap * sizeof(int), s);
     k_clear_nodes<MIX><<<nb, NTB, 0, s>>>(b->nd, NN, b->nf, b->ncap);
     // mixed mode, one material field, window shape functions: the scatters
     // accumulate in shared-memory node tiles (each block's runs beyond its
@@ -446,12 +452,20 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     k_node_post<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, NN, b->bcs, b->bc_group, method != MPMGPU_USL);
     // PeriodicXPIC expansions: every run whose mode of this step takes part
     const int xo = b->o.xpic_order, xf = b->o.xpic_fmpm;
+    // (every field-node; with several fields, each pass's Delta v also takes
+    // the incremental contact of the contact nodes of contact runs)
+    const bool xcontact = b->nf > 1;
     auto xpic_expand = [&](int phase) {
-        k_xpic_init<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, phase);
+        const int xb = (NN * b->nf + NTB - 1) / NTB;
+        k_xpic_init<DIM, MIX, true><<<xb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, phase);
         for (int k = 2; k <= xo; k++) {
             k_xpic_pass<DIM, SHAPE, MIX, true><<<pb, TB, 0, s>>>(sp, b->p, b->xpic, b->mats, phase, k);
-            k_xpic_delta<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, b->bcs, b->bc_group, phase, k,
-                                                            0);
+            k_xpic_delta<DIM, MIX, true><<<xb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, b->bcs, b->bc_group, phase, k,
+                                                            xcontact ? 1 : 0);
+            if (xcontact) {
+                k_xpic_contact<DIM, MIX, true><<<nb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, phase, k);
+                k_xpic_apply<DIM, MIX, true><<<xb, NTB, 0, s>>>(sp, b->nd, b->xpic, NN, phase, k);
+            }
         }
     };
     if (xo > 1 && xf && method != MPMGPU_USL) xpic_expand(XPIC_STRAIN);  // FMPM: first strain update
@@ -684,7 +698,9 @@ int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *o) {
     bytes += N * nf * (int64_t)((nf > 1 ? 26 : 19) * sizeof(double) + 12 * sizeof(float) + 1);
     bytes += N * (int64_t)(2 * sizeof(int) + sizeof(double));
     bytes += (int64_t)o->max_materials * (int64_t)sizeof(DevMat) + (int64_t)o->max_runs * (int64_t)sizeof(DevRun);
-    if (o->xpic_order > 1) bytes += N * (int64_t)(7 * sizeof(double) + 6 * sizeof(float));  // XPIC columns
+    if (o->xpic_order > 1)  // XPIC columns of every field-node, contact state with several fields
+        bytes += N * nf * (int64_t)(7 * sizeof(double) + 6 * sizeof(float) +
+                                    (nf > 1 ? kXcDoubles * sizeof(double) + sizeof(int) : 0));
     if (nf > 1 && o->lr_links > 0) {
         // regression-normal links, counts, offsets, scan sums, results
         bytes += P * o->lr_links * (int64_t)sizeof(int) + 2 * (N + 1) * (int64_t)sizeof(int);
@@ -711,8 +727,6 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     if (o->xpic_order < 0 || o->xpic_order > 64 || (o->xpic_fmpm != 0 && o->xpic_fmpm != 1) ||
         (o->xpic_order > 0 && o->xpic_period < 1))
         return berr(nullptr, MPMGPU_ERR_INVALID, "xpic_order must be 0 to 64, xpic_fmpm 0 or 1, xpic_period >= 1");
-    if (o->xpic_order > 0 && o->max_fields > 1)
-        return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "XPIC/FMPM with multimaterial contact is not implemented");
     if (o->max_particles <= 0 || o->max_particles > (1LL << 31) - 1 || o->max_nodes <= 0 ||
         o->max_nodes > (1LL << 30) || o->max_runs <= 0 || o->max_runs > (1 << 20) || o->max_materials <= 0 ||
         o->max_materials > (1 << 24))
@@ -754,12 +768,20 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     A((void **)&b->runs_dev, (size_t)o->max_runs * sizeof(DevRun));
     A((void **)&b->flag, sizeof(unsigned));
     if (o->xpic_order > 1) {
-        A((void **)&b->xpic_block, 7 * N * sizeof(double) + 6 * N * sizeof(float));
+        // every field-node's expansion columns, and with several fields each
+        // field-node's contact state for the passes' incremental contact
+        const size_t XN = N * (size_t)b->nf;
+        const size_t xc = b->nf > 1 ? XN * (kXcDoubles * sizeof(double) + sizeof(int)) : 0;
+        A((void **)&b->xpic_block, 7 * XN * sizeof(double) + 6 * XN * sizeof(float) + xc);
         if (e == cudaSuccess) {
             double *d = b->xpic_block;
-            float *f = (float *)(d + 7 * N);
-            b->xpic = DevXpic{d, d + N, d + 2 * N, d + 3 * N, d + 4 * N, d + 5 * N, d + 6 * N,
-                              f, f + N, f + 2 * N, f + 3 * N, f + 4 * N, f + 5 * N};
+            float *f = (float *)(d + 7 * XN);
+            b->xpic = DevXpic{d, d + XN, d + 2 * XN, d + 3 * XN, d + 4 * XN, d + 5 * XN, d + 6 * XN,
+                              f, f + XN, f + 2 * XN, f + 3 * XN, f + 4 * XN, f + 5 * XN};
+            if (b->nf > 1) {
+                b->xc = (double *)(f + 6 * XN);  // 8-byte aligned: 6 XN floats
+                b->xc_pair = (int *)(b->xc + kXcDoubles * XN);
+            }
         }
     }
     if (b->nf > 1 && o->lr_links > 0) {
@@ -856,6 +878,8 @@ int mpmgpu_batch_add_run(MpmGpuBatch *b, const MpmGpuGrid *grid, const MpmGpuMat
         return berr(b, MPMGPU_ERR_UNSUPPORTED, "rigid contact materials need multimaterial contact");
     if (rigid && contact->normals >= 5)
         return berr(b, MPMGPU_ERR_UNSUPPORTED, "regression normals with rigid materials are not implemented");
+    if (rigid && b->o.xpic_order > 1)
+        return berr(b, MPMGPU_ERR_UNSUPPORTED, "XPIC/FMPM of order > 1 with rigid materials is not implemented");
     if (mm) {
         if (b->nf < 2) return berr(b, MPMGPU_ERR_INVALID, "contact needs a batch with max_fields >= 2");
         if (contact->normals < 0 || (contact->normals > 2 && contact->normals < 5) || contact->normals > 6)

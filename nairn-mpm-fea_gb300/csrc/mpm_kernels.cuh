@@ -2142,6 +2142,8 @@ __device__ __forceinline__ DevContact node_contact_params(const StepParams &sp, 
         ct.friction = R.friction;
         ct.rigid = R.rigid;
         ct.rigid_bias = R.rigid_bias;
+        // the run's step keeps the contact state for XPIC/FMPM of order > 1
+        ct.xcache = ct.xc != nullptr && (R.xpic > 1 || R.xpic < -1) ? 1 : 0;
     }
     return ct;
 }

@@ -52,17 +52,17 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     if (sp.ct.xcache)  // this step's contact state: none yet
         cudaMemsetAsync(c->ct.xc_pair, 0x80, (size_t)NN * c->ct.nf * sizeof(int), s);
     auto xpic_expand = [&](int phase) {
-        const int XN = NN * c->ct.nf, xb = (XN + TB - 1) / TB;
-        k_xpic_init<DIM, MIX, false><<<xb, TB, 0, s>>>(sp, c->nd, xp, XN, phase);
+        const int XN = NN * c->ct.nf, xb = (XN + TB - 1) / TB;  // every field-node
+        k_xpic_init<DIM, MIX, false><<<xb, TB, 0, s>>>(sp, c->nd, xp, NN, phase);
         c->launches++;
         for (int k = 2; k <= xk; k++) {
             k_xpic_pass<DIM, SHAPE, MIX, false><<<pb, TB, 0, s>>>(sp, c->p, xp, c->mats, phase, k);
-            k_xpic_delta<DIM, MIX, false><<<xb, TB, 0, s>>>(sp, c->nd, xp, XN, c->bcs, c->bc_group, phase, k,
+            k_xpic_delta<DIM, MIX, false><<<xb, TB, 0, s>>>(sp, c->nd, xp, NN, c->bcs, c->bc_group, phase, k,
                                                             xcontact ? 1 : 0);
             c->launches += 2;
             if (xcontact) {
-                k_xpic_contact<DIM, MIX><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, phase, k);
-                k_xpic_apply<DIM, MIX><<<xb, TB, 0, s>>>(sp, c->nd, xp, XN, phase, k);
+                k_xpic_contact<DIM, MIX, false><<<nb, TB, 0, s>>>(sp, c->nd, xp, NN, phase, k);
+                k_xpic_apply<DIM, MIX, false><<<xb, TB, 0, s>>>(sp, c->nd, xp, NN, phase, k);
                 c->launches += 2;
             }
         }

@@ -50,6 +50,17 @@ __device__ __forceinline__ bool xpic_takes_part(int mode, int phase, int k) {
     return phase == XPIC_PARTICLE || mode > 0;
 }
 
+// The field-node of this thread in a node pass over every field: field
+// t / nnodes, node t % nnodes (nnodes: nodes per field in use), at array index
+// n = field fstride + node.  False past the last one.
+__device__ __forceinline__ bool xpic_field_node(const StepParams &sp, int nnodes, int &n, int &node) {
+    const int t = blockIdx.x * blockDim.x + threadIdx.x;
+    if (t >= nnodes * sp.ct.nf) return false;
+    node = t % nnodes;
+    n = (t / nnodes) * sp.ct.fstride + node;
+    return true;
+}
+
 // v* into the velocity columns the particle kernels read (FP32 pairs too in
 // the mixed mode)
 template <bool MIX>
@@ -67,11 +78,11 @@ __device__ __forceinline__ void xpic_store_velocity(const DevNodes &nd, int n, c
 // INITIALIZE_XPIC from the node momentum (and, for XPIC, force)
 template <int DIM, bool MIX, bool BATCH>
 static __global__ void k_xpic_init(StepParams sp, DevNodes nd, DevXpic x, int nnodes, int phase) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nnodes || !nd.active[n]) return;
+    int n, node;
+    if (!xpic_field_node(sp, nnodes, n, node) || !nd.active[n]) return;
     double t, dt;
-    if (!node_run<BATCH>(sp, n, t, dt)) return;
-    const int mode = BATCH ? sp.runs[sp.nrun[n]].xpic : sp.xpic;
+    if (!node_run<BATCH>(sp, node, t, dt)) return;
+    const int mode = BATCH ? sp.runs[sp.nrun[node]].xpic : sp.xpic;
     if (!xpic_takes_part(mode, phase, 1)) return;
     const bool fmpm = phase == XPIC_STRAIN || mode > 0;
     const double m = nd.mass[n];
@@ -164,11 +175,11 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
 template <int DIM, bool MIX, bool BATCH>
 static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int nnodes, DevBCs b,
                                     const int *bc_group, int phase, int k, int defer) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nnodes || !nd.active[n]) return;
+    int n, node;
+    if (!xpic_field_node(sp, nnodes, n, node) || !nd.active[n]) return;
     double t, dt;
-    if (!node_run<BATCH>(sp, n, t, dt)) return;
-    if (!xpic_takes_part(BATCH ? sp.runs[sp.nrun[n]].xpic : sp.xpic, phase, k)) return;
+    if (!node_run<BATCH>(sp, node, t, dt)) return;
+    if (!xpic_takes_part(BATCH ? sp.runs[sp.nrun[node]].xpic : sp.xpic, phase, k)) return;
     double d[3];
     if (MIX) {
         const double rm = x.rm[n];
@@ -180,7 +191,7 @@ static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int n
         d[1] = x.py[n] - x.ny[n];
         d[2] = DIM == 3 ? x.pz[n] - x.nz[n] : 0.;
     }
-    const int grp = bc_group[sp.ct.nf > 1 ? n % sp.ct.fstride : n];
+    const int grp = bc_group[node];
     if (grp >= 0) {
         for (int e = b.start[grp]; e < b.start[grp + 1]; e++) {
             if (t < b.ftime[e]) continue;
@@ -233,12 +244,15 @@ static __global__ void k_xpic_delta(StepParams sp, DevNodes nd, DevXpic x, int n
 // with two fields the other moves by the opposite change.  The reference also
 // moves the node force (XPIC's particle update only), which nothing after
 // the expansion reads, so it is left out.
-template <int DIM, bool MIX>
+template <int DIM, bool MIX, bool BATCH>
 static __global__ void k_xpic_contact(StepParams sp, DevNodes nd, DevXpic x, int nnodes, int phase, int k) {
     const int n = blockIdx.x * blockDim.x + threadIdx.x;
     if (n >= nnodes) return;
-    if (!xpic_takes_part(sp.xpic, phase, k)) return;
-    const DevContact &ct = sp.ct;
+    double t, dt;
+    if (!node_run<BATCH>(sp, n, t, dt)) return;
+    if (!xpic_takes_part(BATCH ? sp.runs[sp.nrun[n]].xpic : sp.xpic, phase, k)) return;
+    const DevContact ct = node_contact_params<BATCH>(sp, n);
+    if (ct.nf < 2) return;
     const int S = ct.fstride;
     int nm = 0;
     for (int f = 0; f < ct.nf; f++) nm += nd.active[f * S + n] ? 1 : 0;
@@ -277,7 +291,7 @@ static __global__ void k_xpic_contact(StepParams sp, DevNodes nd, DevXpic x, int
         const double norm[3] = {xc[1], xc[2], xc[3]};
         const double dotn = dot3(delPi, norm);
         const double dfi[3] = {xc[10], xc[11], xc[12]};
-        if (!coulomb_delta(ct, delPi, norm, dotn, xc[0], mred, dfi, sp.dt)) {
+        if (!coulomb_delta(ct, delPi, norm, dotn, xc[0], mred, dfi, dt)) {
             // out of contact now: undo what earlier passes applied, if anything
             const bool zero = xc[7] == 0. && xc[8] == 0. && (DIM == 2 || xc[9] == 0.);
             if (zero) {
@@ -309,11 +323,13 @@ static __global__ void k_xpic_contact(StepParams sp, DevNodes nd, DevXpic x, int
 
 // UPDATE_VSTAR after the incremental contact: v* += Delta v, and the FP32
 // copy of Delta v for the next pass (mixed mode)
-template <int DIM, bool MIX>
+template <int DIM, bool MIX, bool BATCH>
 static __global__ void k_xpic_apply(StepParams sp, DevNodes nd, DevXpic x, int nnodes, int phase, int k) {
-    const int n = blockIdx.x * blockDim.x + threadIdx.x;
-    if (n >= nnodes || !nd.active[n]) return;
-    if (!xpic_takes_part(sp.xpic, phase, k)) return;
+    int n, node;
+    if (!xpic_field_node(sp, nnodes, n, node) || !nd.active[n]) return;
+    double t, dt;
+    if (!node_run<BATCH>(sp, node, t, dt)) return;
+    if (!xpic_takes_part(BATCH ? sp.runs[sp.nrun[node]].xpic : sp.xpic, phase, k)) return;
     const double d[3] = {x.px[n], x.py[n], DIM == 3 ? x.pz[n] : 0.};
     if (MIX) {
         x.fpx[n] = (float)d[0];

@@ -362,12 +362,44 @@ def test_batched_xpic_runs_match_reference(case, precision, tol, gpu_lib):
     b.close()
 
 
-def test_batched_xpic_refused_with_contact(gpu_lib):
+@pytest.mark.parametrize("case,precision,tol", [("contact2d_xpic2_fric", 0, TOL), ("contact2d_fmpm2_fric_usl", 1, TOL_MIXED),
+                                                ("contact3d_xpic2_fric_cpdi", 0, TOL)])
+def test_batched_xpic_contact_runs_match_reference(case, precision, tol, gpu_lib):
+    """PeriodicXPIC with multimaterial contact in a batch: the golden run
+    matches the reference, and a run of another plate and block size admitted
+    five steps later (its own XPIC schedule) matches the oracle."""
+    from conftest import contact_tolerance, load_golden, model_for, view_for
+    from nairn_gb300.gpu import GpuBatch
+    from nairn_gb300 import abi
+    meta, g = load_golden(case)
+    m = model_for(meta)
+    bigger = dict(plate=(24, 5), block=(7, 4)) if m.grid.dim == 2 else dict(plate=(14, 12, 3), block=(5, 4, 3))
+    late = model_for(dict(meta, kwargs=dict(meta["kwargs"], steps=meta["steps"] - 5, **bigger)))
+    b = GpuBatch.for_models([m, late], precision=precision)
+    assert b.opts.xpic_order == m.options["xpic_order"]
+    r0 = b.add(m)
+    b.step(5)
+    r1 = b.add(late)
+    b.step(meta["steps"])
+    assert b.state(r0) == (abi.RUN_FINISHED, meta["steps"])
+    assert b.state(r1) == (abi.RUN_FINISHED, late.nsteps)
+    v = view_for(b.download(r0), m)
+    ctol = contact_tolerance(case, m, tol)
+    for k in ("pos", "vel", "stress", "strain"):
+        assert rel_l2(v[k], g["final_" + k]) <= ctol[k], (k, rel_l2(v[k], g["final_" + k]), ctol[k])
+    (assert_close if m.grid.dim == 2 else assert_close_3d)(b.download(r1), oracle(late, late.nsteps), tol, "late")
+    b.close()
+
+
+def test_batched_xpic_refused_with_rigid_materials(gpu_lib):
     from nairn_gb300.gpu import GpuBatch, GpuError
     from nairn_gb300 import model
+    c = model.rigid_contact_2d(steps=5)
+    c.options.update(xpic_order=2, xpic_fmpm=0, xpic_period=1)
+    b = GpuBatch.for_models([c])
     with pytest.raises(GpuError, match="UNSUPPORTED"):
-        GpuBatch(model.PLANE_STRAIN, model.USAVG, model.SHAPE_UGIMP, max_runs=2, max_particles=1000,
-                 max_nodes=1000, max_fields=2, xpic=(2, 0, 1))
+        b.add(c)
+    b.close()
 
 
 @pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
