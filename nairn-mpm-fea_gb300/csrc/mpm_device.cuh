@@ -225,6 +225,20 @@ struct Win {
     int s;
 };
 
+// a < b and a <= b for non-negative a and finite b (no NaN): for doubles the
+// order of the bit patterns as signed integers, which is the order of the
+// values there (a negative b has a negative pattern, below every non-negative
+// a), in the integer pipe instead of the FP64 pipe.  x > 0 likewise from the
+// pattern (a positive double's pattern is a positive integer).
+__device__ __forceinline__ bool nn_less(double a, double b) { return __double_as_longlong(a) < __double_as_longlong(b); }
+__device__ __forceinline__ bool nn_less_eq(double a, double b) {
+    return __double_as_longlong(a) <= __double_as_longlong(b);
+}
+__device__ __forceinline__ bool positive(double x) { return __double_as_longlong(x) > 0; }
+__device__ __forceinline__ bool nn_less(float a, float b) { return a < b; }
+__device__ __forceinline__ bool nn_less_eq(float a, float b) { return a <= b; }
+__device__ __forceinline__ bool positive(float x) { return x > 0.f; }
+
 // T = double in the FP64 path, float in the mixed-precision transfer mode.
 // inv_size: 1/(4 lp) of the axis (the 3D z axis takes lp.y's, as the
 // reference does); hinv: 1/(2 lp) of the axis, for the 3D gradient, which the
@@ -233,17 +247,18 @@ struct Win {
 template <typename T, bool kThreeD, bool kGrad>
 __device__ __forceinline__ void gimp_window(T xi, T lp, T inv_size, T hinv, T idx, Win<T> &w) {
     const T q1 = T(2) - lp, q2 = T(2) + lp;
-    w.s = fabs(xi - T(3)) < q2 ? 1 : 0;
+    w.s = nn_less(fabs(xi - T(3)), q2) ? 1 : 0;
 #pragma unroll
     for (int j = 0; j < 3; j++) {
-        const T gk = (T)(2 * (w.s + j) - 3);
-        const T xp = fabs(xi - gk);
+        const T gk = w.s ? T(2 * j - 1) : T(2 * j - 3);  // candidate at 2 (s + j) - 3
+        const T dx = xi - gk;
+        const T xp = fabs(dx);
         T S = T(0), dS = T(0);
-        if (xp < q2) {
+        if (nn_less(xp, q2)) {
             T arg = T(0);
-            if (xp < lp) {
+            if (nn_less(xp, lp)) {
                 S = ((T(4) - lp) * lp - xp * xp) * inv_size;
-            } else if (xp <= q1) {
+            } else if (nn_less_eq(xp, q1)) {
                 S = kThreeD ? T(0.5) * (T(2) - xp) : (T(2) - xp) / T(2);
             } else {
                 arg = (q2 - xp) * inv_size;
@@ -251,10 +266,10 @@ __device__ __forceinline__ void gimp_window(T xi, T lp, T inv_size, T hinv, T id
             }
             if (kGrad) {
                 T d;
-                if (xp < lp) d = kThreeD ? -xp * hinv : -xp * inv_size * T(2);
-                else if (xp <= q1) d = T(-0.5);
+                if (nn_less(xp, lp)) d = kThreeD ? -xp * hinv : -xp * inv_size * T(2);
+                else if (nn_less_eq(xp, q1)) d = T(-0.5);
                 else d = -arg;
-                dS = (xi > gk ? d : -d) * idx;
+                dS = (positive(dx) ? d : -d) * idx;
             }
         }
         w.S[j] = S;
