@@ -235,6 +235,17 @@ __device__ __forceinline__ bool nn_less_eq(double a, double b) {
     return __double_as_longlong(a) <= __double_as_longlong(b);
 }
 __device__ __forceinline__ bool positive(double x) { return __double_as_longlong(x) > 0; }
+// An integer key with the order of the (non-NaN) double x: its magnitude
+// bits, negated for negative x (-0 and +0 both give 0, as they compare equal)
+__device__ __forceinline__ long long order_key(double x) {
+    const long long b = __double_as_longlong(x);
+    const long long m = b & 0x7fffffffffffffffll;
+    return b < 0 ? -m : m;
+}
+// x is NaN: all exponent bits set and a non-zero fraction
+__device__ __forceinline__ bool is_nan_bits(double x) {
+    return ((unsigned long long)__double_as_longlong(x) << 1) > 0xffe0000000000000ull;
+}
 __device__ __forceinline__ bool nn_less(float a, float b) { return a < b; }
 __device__ __forceinline__ bool nn_less_eq(float a, float b) { return a <= b; }
 __device__ __forceinline__ bool positive(float x) { return x > 0.f; }

@@ -1685,15 +1685,22 @@ static __global__ void __launch_bounds__(256) k_det_forces(StepParams sp, DevPar
 template <int DIM>
 __device__ __forceinline__ void reset_element(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
     const double x = p.x[i], y = p.y[i], z = DIM == 3 ? p.z[i] : 0.;
-    if (x != x || y != y || z != z) {
+    // the NaN and in-cell tests on integer order keys (the same outcomes as
+    // the double compares, in the integer pipe)
+    if (is_nan_bits(x) || is_nan_bits(y) || is_nan_bits(z)) {
         atomicOr(err, ERR_NAN);
         return;
     }
     const int e = p.elem[i];
     int col, row, zr;
     elem_coords(g, e, col, row, zr);
-    bool in = !(x < g.xn[col] || x >= g.xn[col + 1]) && !(y < g.yn[row] || y >= g.yn[row + 1]);
-    if (DIM == 3) in = in && !(z < g.zn[zr] || z >= g.zn[zr + 1]);
+    const long long kx = order_key(x), ky = order_key(y);
+    bool in = kx >= order_key(g.xn[col]) && kx < order_key(g.xn[col + 1]) && ky >= order_key(g.yn[row]) &&
+              ky < order_key(g.yn[row + 1]);
+    if (DIM == 3) {
+        const long long kz = order_key(z);
+        in = in && kz >= order_key(g.zn[zr]) && kz < order_key(g.zn[zr + 1]);
+    }
     if (in) return;
     int c = (int)((x - g.xmin) / g.gx);
     bool bad = false;
