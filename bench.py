@@ -912,11 +912,19 @@ def main():
     run.step(1)
     run.download_into(host)
     dist.barrier()
+    split = {"upload": 0., "step": 0., "download": 0.}
     t0 = time.perf_counter()
     for _ in range(ke):
+        a = time.perf_counter()
         run.upload(host)
+        b = time.perf_counter()
         run.step(1)
+        c = time.perf_counter()
         run.download_into(host)
+        d = time.perf_counter()
+        split["upload"] += b - a
+        split["step"] += c - b
+        split["download"] += d - c
     t_e2e = time.perf_counter() - t0
     dist.barrier()
     gpu.unpin(pinned)
@@ -950,6 +958,7 @@ def main():
                                                 "active_nodes_t0": nodes, "precision": "fp64"}),
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d * ws,
                     "d2h_bytes_per_step": d2h * ws, "steps": ke,
+                    "ms_per_call": {k: 1e3 * v / ke for k, v in split.items()},
                     "note": "FP64 path; per step: upload the full particle state from pinned host memory (FP64 "
                             "columns in one block), one step, download it again"},
             "gpu_launches": head["launches"], "roofline": roof, "roofline_fp64": roof64, "kernels": kernels,

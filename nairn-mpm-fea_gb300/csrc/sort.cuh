@@ -181,21 +181,14 @@ static __global__ void k_gather_ints(const int *__restrict__ src, int *__restric
     for (int k = 0; k < ncols; k++) dst[(size_t)k * n + j] = src[(size_t)k * n + s];
 }
 
-// dst[k*n + orig[j]] = src[k*n + j] (slot j holds host particle orig[j])
-static __global__ void k_unsort_cols(const double *__restrict__ src, double *__restrict__ dst, const int *__restrict__ orig,
-                              int n, int ncols) {
+// slot[orig[j]] = j: the slot that holds host particle i (orig is a
+// permutation of 0..n-1), so the host order can be gathered -- scattered
+// reads, sequential writes -- instead of scattered (partial-sector writes of
+// every column)
+static __global__ void k_invert_perm(const int *__restrict__ orig, int *__restrict__ slot, int n) {
     const int j = blockIdx.x * blockDim.x + threadIdx.x;
     if (j >= n) return;
-    const int o = orig[j];
-    for (int k = 0; k < ncols; k++) dst[(size_t)k * n + o] = src[(size_t)k * n + j];
-}
-
-static __global__ void k_unsort_ints(const int *__restrict__ src, int *__restrict__ dst, const int *__restrict__ orig, int n,
-                              int ncols) {
-    const int j = blockIdx.x * blockDim.x + threadIdx.x;
-    if (j >= n) return;
-    const int o = orig[j];
-    for (int k = 0; k < ncols; k++) dst[(size_t)k * n + o] = src[(size_t)k * n + j];
+    slot[orig[j]] = j;
 }
 
 inline void sort_free(SortWorkspace &w) {
@@ -307,8 +300,10 @@ inline int unsort_to_scratch(SortWorkspace &w, const DevParticles &p, const int 
                              cudaStream_t s) {
     const int n = p.n;
     const int TB = 256, pb = (n + TB - 1) / TB;
-    k_unsort_cols<<<pb, TB, 0, s>>>(pblock, w.scratch, orig, n, ncols);
-    k_unsort_ints<<<pb, TB, 0, s>>>(p.mat, w.iscratch, orig, n, 2);
+    int *slot = w.iscratch + 2 * (size_t)n;  // the third of the int scratch's columns
+    k_invert_perm<<<pb, TB, 0, s>>>(orig, slot, n);
+    k_gather_cols<<<pb, TB, 0, s>>>(pblock, w.scratch, slot, n, ncols);
+    k_gather_ints<<<pb, TB, 0, s>>>(p.mat, w.iscratch, slot, n, 2);  // mat, elem
     return cudaGetLastError() == cudaSuccess ? 0 : 1;
 }
 
