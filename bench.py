@@ -903,8 +903,11 @@ def main():
     # step uploads the state from pinned host memory and downloads the result
     # the host keeps its FP64 columns in one block in the library's column
     # order, so each direction moves them in one copy
-    host, block = abi.contiguous_particles(final)
-    pinned = gpu.pin({"block": block, "mat": host["mat"], "elem": host["elem"]})
+    # (the block in page-locked memory the driver allocated, mpmgpu_host_alloc)
+    hb = gpu.HostBlock((len(abi.DEVICE_COLUMNS), n))
+    host, block = abi.contiguous_particles(final, hb.array)
+    pinned = gpu.pin({"mat": host["mat"], "elem": host["elem"]})
+    pin_error = None if len(pinned) == 2 else gpu.lib().mpmgpu_last_error(None).decode()
     h2d = block.nbytes + host["mat"].nbytes + host["elem"].nbytes
     d2h = h2d
     ke = max(1, args.e2e_steps)
@@ -928,6 +931,8 @@ def main():
     t_e2e = time.perf_counter() - t0
     dist.barrier()
     gpu.unpin(pinned)
+    host = block = None
+    hb.close()
     t_e2e = dist.max(t_e2e)
     e2e_value = total_particles * ke / t_e2e
     run.close()
@@ -959,8 +964,10 @@ def main():
             "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d * ws,
                     "d2h_bytes_per_step": d2h * ws, "steps": ke,
                     "ms_per_call": {k: 1e3 * v / ke for k, v in split.items()},
+                    "host_buffers_page_locked": pin_error is None, "page_lock_error": pin_error,
                     "note": "FP64 path; per step: upload the full particle state from pinned host memory (FP64 "
-                            "columns in one block), one step, download it again"},
+                            "columns in one block the driver allocated, mpmgpu_host_alloc), one step, download it "
+                            "again"},
             "gpu_launches": head["launches"], "roofline": roof, "roofline_fp64": roof64, "kernels": kernels,
             "clocks": head["clocks"],
             "measured_peaks": {"fp64_fma_tflops": fp64_peak, "fp32_fma_tflops": fp32_peak,

@@ -331,6 +331,14 @@ long long mpmgpu_launch_count(const MpmGpuCtx *ctx);
 int mpmgpu_host_register(void *ptr, uint64_t bytes);
 int mpmgpu_host_unregister(void *ptr);
 
+/* Page-locked host memory allocated by the driver (cudaHostAlloc), for a host
+ * that keeps its particle columns in memory of the library's choosing;
+ * mpmgpu_host_free releases it.  Copies to memory the driver allocated run at
+ * the host link's rate in both directions, where registered caller memory was
+ * measured at a third of it for device-to-host copies in some runs. */
+int mpmgpu_host_alloc(uint64_t bytes, void **ptr);
+void mpmgpu_host_free(void *ptr);
+
 /* Extension (measurement): FMA throughput of the current device in TFLOP/s
  * (2 flops per FMA), measured by one kernel of independent FMA chains timed
  * with CUDA events; *ms receives the kernel time.  The FP64 path of the step

@@ -1073,4 +1073,19 @@ int mpmgpu_host_unregister(void *ptr) {
     return e == cudaSuccess ? MPMGPU_OK : cuda_fail(nullptr, e, "cudaHostUnregister");
 }
 
+int mpmgpu_host_alloc(uint64_t bytes, void **ptr) {
+    if (!ptr || !bytes) return MPMGPU_ERR_INVALID;
+    *ptr = nullptr;
+    cudaError_t e = cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault);
+    if (e != cudaSuccess) {
+        *ptr = nullptr;
+        return cuda_fail(nullptr, e, "cudaHostAlloc");
+    }
+    return MPMGPU_OK;
+}
+
+void mpmgpu_host_free(void *ptr) {
+    if (ptr) cudaFreeHost(ptr);
+}
+
 }  // extern "C"

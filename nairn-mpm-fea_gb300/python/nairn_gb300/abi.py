@@ -146,12 +146,15 @@ DEVICE_COLUMNS = ["x", "y", "z", "vx", "vy", "vz", "mass", "lpx", "lpy", "lpz",
                   "pxx", "pyy", "pzz", "pxy", "pxz", "pyz", "hist0", "hist1", "work", "plast", "x0", "y0", "z0"]
 
 
-def contiguous_particles(p: dict) -> tuple[dict, np.ndarray]:
+def contiguous_particles(p: dict, block: np.ndarray | None = None) -> tuple[dict, np.ndarray]:
     """A copy of p whose FP64 columns are rows of one block in the library's
     device column order, so uploads and downloads move them with one copy
-    each; returns (columns, block)."""
+    each; returns (columns, block).  `block` (len(DEVICE_COLUMNS) x n FP64),
+    when given, receives the columns -- e.g. page-locked memory."""
     n = len(p["x"])
-    block = np.empty((len(DEVICE_COLUMNS), n), dtype=np.float64)
+    if block is None:
+        block = np.empty((len(DEVICE_COLUMNS), n), dtype=np.float64)
+    assert block.shape == (len(DEVICE_COLUMNS), n) and block.dtype == np.float64
     out = {}
     for i, k in enumerate(DEVICE_COLUMNS):
         block[i] = p[k]

@@ -484,6 +484,32 @@ def fma_rate(fp64: bool = True, iters: int = 20000) -> float:
     return tf.value
 
 
+class HostBlock:
+    """Page-locked host memory allocated by the driver (mpmgpu_host_alloc),
+    seen as a numpy array of the given shape and dtype; close() frees it."""
+
+    def __init__(self, shape, dtype=np.float64):
+        L = lib()
+        L.mpmgpu_host_alloc.argtypes = [C.c_uint64, C.POINTER(C.c_void_p)]
+        L.mpmgpu_host_alloc.restype = C.c_int
+        L.mpmgpu_host_free.argtypes = [C.c_void_p]
+        L.mpmgpu_host_free.restype = None
+        dt = np.dtype(dtype)
+        nbytes = int(np.prod(shape)) * dt.itemsize
+        self.ptr = C.c_void_p()
+        st = L.mpmgpu_host_alloc(nbytes, C.byref(self.ptr))
+        if st != 0:
+            raise GpuError(st, L.mpmgpu_last_error(None).decode())
+        buf = (C.c_char * nbytes).from_address(self.ptr.value)
+        self.array = np.frombuffer(buf, dtype=dt).reshape(shape)
+
+    def close(self):
+        if self.ptr:
+            self.array = None
+            lib().mpmgpu_host_free(self.ptr)
+            self.ptr = None
+
+
 def pin(arrays: dict) -> list:
     """Page-lock numpy arrays for DMA transfers; returns the registered list."""
     done = []
