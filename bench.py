@@ -238,14 +238,15 @@ def peaks():
     return 6800.0, "fallback"
 
 
-def traffic_from_profiles(kernel: str, n_particles: int):
-    """Per-launch DRAM bytes from the committed ncu summary, scaled to this size."""
+def traffic_from_profiles(kernel: str, n_particles: int, precision: int):
+    """Per-launch DRAM bytes of the kernel in the given precision from the
+    committed ncu summary, scaled to this size."""
     p = os.path.join(ROOT, "profiles", "ncu_traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as fh:
         d = json.load(fh)
-    k = d.get("kernels", {}).get(kernel)
+    k = d.get("fp64_kernels" if precision == 0 else "kernels", {}).get(kernel)
     if not k:
         return None
     return k["dram_bytes_per_launch"] * n_particles / d["particles"]
@@ -847,7 +848,7 @@ def kernel_table(prof: dict, steps: int, bytes_model: dict, launches_of) -> dict
             for k, v in fams.items()}
 
 
-def roofline_of(prof: dict, steps: int, sort_interval: int, m, nodes: int, fp64_peak_tflops):
+def roofline_of(prof: dict, steps: int, sort_interval: int, m, nodes: int, fp64_peak_tflops, precision: int = 0):
     """HBM roofline of the dominant kernel (largest share of the profiled
     pass), and for the FP64 path its FP64-pipe roofline against the FP64 FMA
     rate measured on this GPU."""
@@ -863,7 +864,7 @@ def roofline_of(prof: dict, steps: int, sort_interval: int, m, nodes: int, fp64_
     achieved = bytes_model[dom] / (avg_ms / 1e3) / 1e9
     roof = {"kernel": dom, "bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
             "frac": achieved / peak, "peak_source": peak_kind + " (MEASURED_PEAKS.json hbm_gbs)",
-            "traffic": traffic_from_profiles(dom, m.n), "algorithmic_bytes_per_launch": bytes_model[dom],
+            "traffic": traffic_from_profiles(dom, m.n, precision), "algorithmic_bytes_per_launch": bytes_model[dom],
             "avg_launch_ms": avg_ms,
             "note": "per-launch time from CUDA events of a separate profiled pass over the same window"}
     fl = fp64_flops_from_profiles(dom, m.n)
@@ -944,7 +945,7 @@ def main():
         mrun, mixed, mfinal = window_run(args, m, dist, 1, local)
         archived = archive_measurement(args, mrun, m, dist) if args.archive_steps > 0 else None
         mrun.close()
-        mroof, _, mkernels = roofline_of(mixed["prof"], args.steps, mixed["sort_interval"], m, nodes, None)
+        mroof, _, mkernels = roofline_of(mixed["prof"], args.steps, mixed["sort_interval"], m, nodes, None, 1)
         err = state_error(mfinal, final, m.grid.dim)
         mixed_value = total_particles * args.steps / (dist.max(mixed["ms"]) / 1e3)
         mixed_line = {"value": mixed_value, "unit": METRIC, "ms_per_step": dist.max(mixed["ms"]) / args.steps,
