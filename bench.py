@@ -21,6 +21,11 @@ threads) times the same window of the same run.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
+"e2e" is the same FP64 step through the C ABI with the particle state in host
+memory: the state stays in page-locked host memory and each step's kernels
+read and write its columns in place over the host link (mpmgpu_step_host);
+"e2e.copy" is the copying form (upload the state, step, download it).
+
 The line also carries "mixed": the same window in the mixed-precision mode
 (FP32 transfers, FP64 constitutive update) with its error against the FP64
 path; "batched": 512 independent seeded 2D runs (2k-200k particles each)
@@ -211,6 +216,27 @@ def algorithmic_bytes(m, nodes_active: int) -> dict:
         "sort": 0,
     }
     return {k: n * per_particle[k] + nodes_active * per_node[k] for k in per_particle}
+
+
+def host_link_bytes(m) -> tuple[int, int]:
+    """Bytes one step on host-resident state (mpmgpu_step_host) moves over the
+    host link: the host columns each kernel reads, and those it writes
+    (algorithmic, each column once per kernel; the natural coordinates stay
+    on the device)."""
+    dim = m.grid.dim
+    d = 8
+    vec = dim * d
+    plastic = any(mm["type"] == 9 for mm in m.materials)
+    ten = (6 if dim == 3 else 4) * d
+    F = (9 if dim == 3 else 5) * d
+    state = F + ten + (d + ten + d + d if plastic else 0) + d
+    elem, mat, lp = 4, 4, dim * d
+    reads = ((elem + vec + d + vec + lp)            # p2g: elem, x, m, v, lp
+             + (elem + lp + mat + d + state)        # strain_forces: geometry, state
+             + (elem + lp + 2 * vec + d)            # g2p: x, v, m
+             + (elem + lp + mat + vec + state))     # strain_last: geometry, x, state
+    writes = state + 2 * vec + (state + elem)       # strain_forces; g2p x, v; strain_last state, elem
+    return m.n * reads, m.n * writes
 
 
 def active_nodes(m) -> int:
@@ -932,10 +958,28 @@ def main():
     t_e2e = time.perf_counter() - t0
     dist.barrier()
     gpu.unpin(pinned)
+    t_e2e = dist.max(t_e2e)
+    e2e_copy_value = total_particles * ke / t_e2e
+
+    # end to end on host-resident state (mpmgpu_step_host): the particle state
+    # stays in page-locked host memory and the kernels read and write its
+    # columns in place over the host link, so the link traffic overlaps their
+    # arithmetic instead of preceding and following it; one call per step,
+    # each returning when the step's results are in host memory
+    hs = gpu.HostState(host)
     host = block = None
     hb.close()
-    t_e2e = dist.max(t_e2e)
-    e2e_value = total_particles * ke / t_e2e
+    run.step_host(hs.particles, 1)
+    dist.barrier()
+    t0 = time.perf_counter()
+    for _ in range(ke):
+        run.step_host(hs.particles, 1)
+    t_host = time.perf_counter() - t0
+    dist.barrier()
+    hs.close()
+    t_host = dist.max(t_host)
+    e2e_value = total_particles * ke / t_host
+    link_read, link_write = host_link_bytes(m)
     run.close()
 
     # the mixed-precision mode over the same window, with its error against
@@ -962,13 +1006,20 @@ def main():
             "config": workload_config(args, m, {"sort_interval": head["sort_interval"],
                                                 "sort_interval_autotuned": args.sort_interval <= 0,
                                                 "active_nodes_t0": nodes, "precision": "fp64"}),
-            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": h2d * ws,
-                    "d2h_bytes_per_step": d2h * ws, "steps": ke,
-                    "ms_per_call": {k: 1e3 * v / ke for k, v in split.items()},
-                    "host_buffers_page_locked": pin_error is None, "page_lock_error": pin_error,
-                    "note": "FP64 path; per step: upload the full particle state from pinned host memory (FP64 "
-                            "columns in one block the driver allocated, mpmgpu_host_alloc), one step, download it "
-                            "again"},
+            "e2e": {"value": e2e_value, "unit": METRIC, "h2d_bytes_per_step": link_read * ws,
+                    "d2h_bytes_per_step": link_write * ws, "steps": ke, "ms_per_call": 1e3 * t_host / ke,
+                    "form": "host-resident state: mpmgpu_step_host, one call per step",
+                    "note": "FP64 path; the particle state (%.0f MB) stays in page-locked host memory the driver "
+                            "allocated (mpmgpu_host_alloc) and every step's kernels read and write its columns in "
+                            "place over the host link; the byte counts are the host columns the kernels read and "
+                            "write (algorithmic: each column once per kernel)" % (h2d / 1e6),
+                    "copy": {"value": e2e_copy_value, "unit": METRIC, "h2d_bytes_per_step": h2d * ws,
+                             "d2h_bytes_per_step": d2h * ws, "steps": ke,
+                             "ms_per_call": {k: 1e3 * v / ke for k, v in split.items()},
+                             "host_buffers_page_locked": pin_error is None, "page_lock_error": pin_error,
+                             "form": "mpmgpu_upload_particles + mpmgpu_step + mpmgpu_download_particles per step",
+                             "note": "per step: upload the full particle state from pinned host memory (FP64 "
+                                     "columns in one block the driver allocated), one step, download it again"}},
             "gpu_launches": head["launches"], "roofline": roof, "roofline_fp64": roof64, "kernels": kernels,
             "clocks": head["clocks"],
             "measured_peaks": {"fp64_fma_tflops": fp64_peak, "fp32_fma_tflops": fp32_peak,

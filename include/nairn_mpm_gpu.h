@@ -339,6 +339,23 @@ int mpmgpu_host_unregister(void *ptr);
 int mpmgpu_host_alloc(uint64_t bytes, void **ptr);
 void mpmgpu_host_free(void *ptr);
 
+/* Extension: advance nsteps on particle state that stays in host memory.  The
+ * step kernels read and write the caller's columns in place over the host link
+ * (NVLink-C2C on Grace systems), so the link traffic overlaps the kernels'
+ * arithmetic instead of preceding and following it as the copies of
+ * mpmgpu_upload_particles / mpmgpu_download_particles do.  Every non-null
+ * column of *particles, and mat and elem (required), must lie inside one block
+ * from mpmgpu_host_alloc; a null column is taken from the context's uploaded
+ * state (on the device).  particles->n must equal the particle count of the
+ * last mpmgpu_upload_particles, which sizes the work arrays; the device copy of
+ * that state is not advanced.  The host order is kept (no cell sort).  The call
+ * returns when the steps have completed; the caller must not touch the columns
+ * meanwhile.  Errors as mpmgpu_step, plus MPMGPU_ERR_INVALID for a column
+ * outside the blocks or material/element indices out of range (checked before
+ * the steps).  No counterpart in the reference (its particle state is host
+ * memory throughout). */
+int mpmgpu_step_host(MpmGpuCtx *ctx, MpmGpuParticles *particles, int32_t nsteps, double t0);
+
 /* Extension (measurement): FMA throughput of the current device in TFLOP/s
  * (2 flops per FMA), measured by one kernel of independent FMA chains timed
  * with CUDA events; *ms receives the kernel time.  The FP64 path of the step

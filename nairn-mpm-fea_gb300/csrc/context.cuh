@@ -39,6 +39,7 @@ struct MpmGpuCtx {
     double *pblock = nullptr;            // particle double columns
     int *iblock = nullptr;               // mat, elem, original index
     int *orig = nullptr;                 // original (host) index of each slot
+    int *iota = nullptr;                 // identity order of steps on host-resident state (n ints)
     double *nblock = nullptr;            // node double columns
     float *fblock = nullptr;             // node float columns (mixed mode)
     size_t fblock_zero_bytes = 0;

@@ -59,6 +59,10 @@ struct DevParticles {
     // weights cwg[(3c+a)*n+i]
     int *ce;
     double *cxi, *cwg;
+    // 1: the columns are host memory the kernels reach over the host link
+    // (mpmgpu_step_host); the lanes of a warp then take consecutive slots
+    // (tile_particle), so that each warp access is whole lines of the link
+    int host_resident;
 };
 
 struct DevNodes {

@@ -168,17 +168,56 @@ namespace {
 
 // Point the particle columns at a block of kParticleDoubles+1 double columns
 // (the last three are the step's natural coordinates) and 3 int columns.
+// The double columns of p in the device block's order (hcols gives the host
+// columns in the same order; the last three are the natural coordinates).
+void particle_columns(DevParticles &p, double **cols[kParticleDoubles + 1]) {
+    double **tmp[kParticleDoubles + 1] = {&p.x, &p.y, &p.z, &p.vx, &p.vy, &p.vz, &p.mass, &p.lpx, &p.lpy, &p.lpz,
+                                          &p.exx, &p.eyy, &p.ezz, &p.exy, &p.exz, &p.eyz, &p.wxy, &p.wxz, &p.wyz,
+                                          &p.sxx, &p.syy, &p.szz, &p.sxy, &p.sxz, &p.syz, &p.pressure,
+                                          &p.pxx, &p.pyy, &p.pzz, &p.pxy, &p.pxz, &p.pyz,
+                                          &p.hist0, &p.hist1, &p.work, &p.plast, &p.x0, &p.y0, &p.z0,
+                                          &p.xi, &p.eta, &p.zeta};
+    std::memcpy(cols, tmp, sizeof(tmp));
+}
+
 void link_columns(DevParticles &p, double *pb, int *ib, int **orig) {
     const size_t n = (size_t)p.n;
-    double **cols[kParticleDoubles + 1] = {&p.x, &p.y, &p.z, &p.vx, &p.vy, &p.vz, &p.mass, &p.lpx, &p.lpy, &p.lpz,
-                                           &p.exx, &p.eyy, &p.ezz, &p.exy, &p.exz, &p.eyz, &p.wxy, &p.wxz, &p.wyz,
-                                           &p.sxx, &p.syy, &p.szz, &p.sxy, &p.sxz, &p.syz, &p.pressure,
-                                           &p.pxx, &p.pyy, &p.pzz, &p.pxy, &p.pxz, &p.pyz,
-                                           &p.hist0, &p.hist1, &p.work, &p.plast, &p.x0, &p.y0, &p.z0, &p.xi, &p.eta, &p.zeta};
+    double **cols[kParticleDoubles + 1];
+    particle_columns(p, cols);
     for (int k = 0; k <= kParticleDoubles; k++) *cols[k] = pb + (size_t)k * n;
     p.mat = ib;
     p.elem = ib + n;
     *orig = ib + 2 * n;
+}
+
+// Page-locked blocks from mpmgpu_host_alloc (base -> bytes).  The columns a
+// step on host-resident state reads and writes must each lie inside one of
+// them, so that every access of its kernels stays inside memory the device
+// has mapped.
+std::mutex g_host_mu;
+std::map<uintptr_t, size_t> g_host_blocks;
+
+bool in_host_block(const void *ptr, size_t bytes) {
+    const uintptr_t a = (uintptr_t)ptr;
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    auto it = g_host_blocks.upper_bound(a);
+    if (it == g_host_blocks.begin()) return false;
+    --it;
+    const size_t off = a - it->first;
+    return off <= it->second && bytes <= it->second - off;
+}
+
+// The device address of n values of a host column inside one block of
+// mpmgpu_host_alloc; nullptr when the column lies outside every block.
+template <class T>
+T *mapped_column(T *h, size_t n) {
+    if (!h || !in_host_block(h, n * sizeof(T))) return nullptr;
+    void *d = nullptr;
+    if (cudaHostGetDevicePointer(&d, (void *)h, 0) != cudaSuccess) {
+        cudaGetLastError();
+        return nullptr;
+    }
+    return (T *)d;
 }
 
 }  // namespace
@@ -218,9 +257,11 @@ void free_particles(MpmGpuCtx *c) {
     if (c->pblock) cudaFree(c->pblock);
     if (c->iblock) cudaFree(c->iblock);
     if (c->cpdi) cudaFree(c->cpdi);
+    if (c->iota) cudaFree(c->iota);
     c->pblock = nullptr;
     c->iblock = nullptr;
     c->cpdi = nullptr;
+    c->iota = nullptr;
     sort_free(c->sort);
     c->p.n = 0;
 }
@@ -797,6 +838,71 @@ int mpmgpu_step_timed(MpmGpuCtx *c, int32_t nsteps, double t0, double *ms) {
     return step_impl(c, nsteps, t0, ms);
 }
 
+int mpmgpu_step_host(MpmGpuCtx *c, MpmGpuParticles *h, int32_t nsteps, double t0) {
+    if (!c || !h || nsteps < 0) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_step_host: bad argument");
+    if (c->p.n <= 0 || !c->mats || h->n != c->p.n)
+        return set_err(c, MPMGPU_ERR_INVALID,
+                       "mpmgpu_step_host: upload a state of the same particle count first (it sizes the work arrays)");
+    const size_t n = (size_t)c->p.n;
+    // the kernels' view: the caller's columns where it gives them, the
+    // uploaded device columns where it gives none; the natural coordinates
+    // of the step stay on the device
+    DevParticles view = c->p;
+    view.host_resident = 1;
+    double **cols[kParticleDoubles + 1];
+    particle_columns(view, cols);
+    double *hc[kParticleDoubles];
+    hcols(h, hc);
+    for (int k = 0; k < kParticleDoubles; k++) {
+        if (!hc[k]) continue;
+        double *d = mapped_column(hc[k], n);
+        if (!d)
+            return set_err(c, MPMGPU_ERR_INVALID,
+                           "mpmgpu_step_host: a particle column lies outside the blocks of mpmgpu_host_alloc");
+        *cols[k] = d;
+    }
+    view.mat = mapped_column(h->mat, n);
+    view.elem = mapped_column(h->elem, n);
+    if (!view.mat || !view.elem)
+        return set_err(c, MPMGPU_ERR_INVALID,
+                       "mpmgpu_step_host: material and element columns inside the blocks of mpmgpu_host_alloc are required");
+    if (!c->iota) {
+        cudaError_t e = cudaMalloc(&c->iota, n * sizeof(int));
+        if (e != cudaSuccess) {
+            c->iota = nullptr;
+            return set_err(c, MPMGPU_ERR_OOM, std::string("identity order: ") + cudaGetErrorString(e));
+        }
+    }
+    // the caller's material and element indices, range-checked as an upload
+    // checks them (the kernels index tables with them)
+    const int nelems = c->g.nx * c->g.ny * (c->dim == 3 ? c->g.nz : 1);
+    CK(cudaMemsetAsync(c->err, 0, sizeof(unsigned), c->stream));
+    const int TB = 256;
+    k_upload_check<<<(int)((n + TB - 1) / TB), TB, 0, c->stream>>>(view.mat, view.elem, c->iota, (int)n, c->nmat,
+                                                                  nelems, c->err);
+    c->launches++;
+    unsigned flags = 0;
+    CK(cudaMemcpyAsync(&flags, c->err, sizeof(unsigned), cudaMemcpyDeviceToHost, c->stream));
+    CK(cudaStreamSynchronize(c->stream));
+    if (flags) {
+        cudaMemsetAsync(c->err, 0, sizeof(unsigned), c->stream);
+        cudaStreamSynchronize(c->stream);
+        return set_err(c, MPMGPU_ERR_INVALID, "particle material or element index out of range");
+    }
+    // the host order is kept: no cell sort, identity slot order
+    const DevParticles saved = c->p;
+    int *const saved_orig = c->orig;
+    const int saved_sort = c->opts.sort_interval;
+    c->p = view;
+    c->orig = c->iota;
+    c->opts.sort_interval = 0;
+    const int st = step_impl(c, nsteps, t0, nullptr);
+    c->p = saved;
+    c->orig = saved_orig;
+    c->opts.sort_interval = saved_sort;
+    return st;
+}
+
 int mpmgpu_download_particles(MpmGpuCtx *c, MpmGpuParticles *h) {
     if (!c || !h) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_download_particles: null argument");
     if (h->n != c->p.n) return set_err(c, MPMGPU_ERR_INVALID, "mpmgpu_download_particles: particle count mismatch");
@@ -1076,16 +1182,23 @@ int mpmgpu_host_unregister(void *ptr) {
 int mpmgpu_host_alloc(uint64_t bytes, void **ptr) {
     if (!ptr || !bytes) return MPMGPU_ERR_INVALID;
     *ptr = nullptr;
-    cudaError_t e = cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocDefault);
+    cudaError_t e = cudaHostAlloc(ptr, (size_t)bytes, cudaHostAllocPortable | cudaHostAllocMapped);
     if (e != cudaSuccess) {
         *ptr = nullptr;
         return cuda_fail(nullptr, e, "cudaHostAlloc");
     }
+    std::lock_guard<std::mutex> lk(g_host_mu);
+    g_host_blocks[(uintptr_t)*ptr] = (size_t)bytes;
     return MPMGPU_OK;
 }
 
 void mpmgpu_host_free(void *ptr) {
-    if (ptr) cudaFreeHost(ptr);
+    if (!ptr) return;
+    {
+        std::lock_guard<std::mutex> lk(g_host_mu);
+        g_host_blocks.erase((uintptr_t)ptr);
+    }
+    cudaFreeHost(ptr);
 }
 
 }  // extern "C"

@@ -1089,8 +1089,11 @@ __device__ __forceinline__ double tile_sum(const NodeTile &t, int q, int k) {
 // block still covers consecutive slots, but the lanes of one warp hold
 // particles of different cells (sorted particles of one cell are neighbours),
 // so the lanes' atomic adds -- to a shared-memory tile or to the node columns
-// -- go to different nodes instead of queueing on the same address.
-__device__ __forceinline__ int tile_particle() {
+// -- go to different nodes instead of queueing on the same address.  Columns
+// in host memory (p.host_resident) take the plain order instead: there a
+// warp's loads must be whole lines, or the link moves a line per lane.
+__device__ __forceinline__ int tile_particle(const DevParticles &p) {
+    if (p.host_resident) return blockIdx.x * blockDim.x + threadIdx.x;
     return blockIdx.x * blockDim.x + (threadIdx.x & 31) * (blockDim.x >> 5) + (threadIdx.x >> 5);
 }
 
@@ -1276,7 +1279,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
 template <int DIM, int SHAPE, bool MIX, bool BATCH, bool DET = false>
 static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 3) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
-    const int i = tile_particle();
+    const int i = tile_particle(p);
     if (i >= p.n) return;
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
@@ -1357,7 +1360,7 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 3) k_p2
 template <int DIM, int SHAPE, bool BATCH>
 static __global__ void __launch_bounds__(256) k_p2g_tile(StepParams sp, DevParticles p, DevNodes nd) {
     __shared__ NodeTile t;
-    const int i = tile_particle();
+    const int i = tile_particle(p);
     RunView rv;
     const bool valid = i < p.n && particle_run<BATCH>(sp, p, i, rv);
     int col = 0, row = 0, zr = 0;
@@ -1584,7 +1587,7 @@ __device__ __forceinline__ void forces_scatter(const StepParams &sp, const DevPa
 // Mixed mode: internal-force products in FP32 into FP32 accumulators.
 template <int DIM, int SHAPE, bool STRAIN, bool MIX, bool BATCH, bool DET = false>
 static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_forces(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
-    const int i = tile_particle();
+    const int i = tile_particle(p);
     if (i >= p.n) return;
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
@@ -1622,7 +1625,7 @@ static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_for
 template <int DIM, int SHAPE, bool STRAIN, bool BATCH>
 static __global__ void __launch_bounds__(256, kStrainBlocks<SHAPE>) k_strain_forces_tile(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     __shared__ NodeTile t;
-    const int i = tile_particle();
+    const int i = tile_particle(p);
     RunView rv;
     const bool valid = i < p.n && particle_run<BATCH>(sp, p, i, rv);
     int col = 0, row = 0, zr = 0;
@@ -1843,7 +1846,7 @@ __device__ __forceinline__ void g2p_move(const StepParams &sp, const DevParticle
 template <int DIM, int SHAPE, bool USL, bool MIX, bool BATCH, bool DET = false>
 static __global__ void __launch_bounds__(256, 2) k_g2p(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
-    const int i = tile_particle();
+    const int i = tile_particle(p);
     if (i >= p.n) return;
     RunView rv;
     if (!particle_run<BATCH>(sp, p, i, rv)) return;
@@ -1934,7 +1937,7 @@ static __global__ void __launch_bounds__(256, 2) k_g2p(StepParams sp, DevParticl
 template <int DIM, int SHAPE, bool BATCH>
 static __global__ void __launch_bounds__(256) k_g2p_tile(StepParams sp, DevParticles p, DevNodes nd) {
     __shared__ NodeTile t;
-    const int i = tile_particle();
+    const int i = tile_particle(p);
     RunView rv;
     const bool valid = i < p.n && particle_run<BATCH>(sp, p, i, rv);
     int col = 0, row = 0, zr = 0;

@@ -42,6 +42,7 @@ def lib():
     L.mpmgpu_set_velocity_bcs.argtypes = [C.c_void_p, P(abi.MpmGpuVelBC), C.c_int32]
     L.mpmgpu_upload_particles.argtypes = [C.c_void_p, P(abi.MpmGpuParticles)]
     L.mpmgpu_step.argtypes = [C.c_void_p, C.c_int32, C.c_double]
+    L.mpmgpu_step_host.argtypes = [C.c_void_p, C.POINTER(abi.MpmGpuParticles), C.c_int32, C.c_double]
     L.mpmgpu_download_particles.argtypes = [C.c_void_p, P(abi.MpmGpuParticles)]
     L.mpmgpu_last_error.argtypes = [C.c_void_p]
     L.mpmgpu_last_error.restype = C.c_char_p
@@ -114,7 +115,7 @@ def lib():
         getattr(L, f).restype = res
     for f in ("mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact", "mpmgpu_set_velocity_bcs",
               "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles", "mpmgpu_profile",
-              "mpmgpu_set_profiling"):
+              "mpmgpu_set_profiling", "mpmgpu_step_host"):
         getattr(L, f).restype = C.c_int
     _lib = L
     return L
@@ -124,7 +125,8 @@ def lib():
 EXPORTED = ("mpmgpu_step_timed", "mpmgpu_autotune_sort", "mpmgpu_archive_record_size", "mpmgpu_archive_records",
             "mpmgpu_archive_records_async", "mpmgpu_archive_wait",
             "mpmgpu_set_profiling", "mpmgpu_stream", "mpmgpu_launch_count",
-            "mpmgpu_host_register", "mpmgpu_host_unregister", "mpmgpu_fp64_fma_rate", "mpmgpu_fp32_fma_rate",
+            "mpmgpu_host_register", "mpmgpu_host_unregister", "mpmgpu_host_alloc", "mpmgpu_host_free",
+            "mpmgpu_step_host", "mpmgpu_fp64_fma_rate", "mpmgpu_fp32_fma_rate",
             "mpmgpu_abi_version", "mpmgpu_create", "mpmgpu_set_materials", "mpmgpu_set_contact",
             "mpmgpu_set_velocity_bcs", "mpmgpu_upload_particles", "mpmgpu_step", "mpmgpu_download_particles",
             "mpmgpu_last_error", "mpmgpu_destroy", "mpmgpu_profile")
@@ -163,6 +165,15 @@ class GpuRun:
 
     def step(self, nsteps: int):
         self._check(lib().mpmgpu_step(self.h, int(nsteps), float(self.t)))
+        self.t += nsteps * self.model.options["timestep"]
+
+    def step_host(self, particles: dict, nsteps: int):
+        """Advance nsteps on state kept in host memory (mpmgpu_step_host): the
+        kernels read and write the columns of `particles` in place, which must
+        lie in blocks of mpmgpu_host_alloc (HostState)."""
+        b = abi.Bound()
+        ps = abi.particles_struct(particles, b)
+        self._check(lib().mpmgpu_step_host(self.h, C.byref(ps), int(nsteps), float(self.t)))
         self.t += nsteps * self.model.options["timestep"]
 
     def step_timed(self, nsteps: int) -> float:
@@ -329,6 +340,15 @@ class GpuBatch:
 
     def step(self, nsteps: int = 1):
         self._check(lib().mpmgpu_batch_step(self.h, int(nsteps)))
+
+    def step_host(self, particles: dict, nsteps: int):
+        """Advance nsteps on state kept in host memory (mpmgpu_step_host): the
+        kernels read and write the columns of `particles` in place, which must
+        lie in blocks of mpmgpu_host_alloc (HostState)."""
+        b = abi.Bound()
+        ps = abi.particles_struct(particles, b)
+        self._check(lib().mpmgpu_step_host(self.h, C.byref(ps), int(nsteps), float(self.t)))
+        self.t += nsteps * self.model.options["timestep"]
 
     def step_timed(self, nsteps: int) -> float:
         ms = C.c_double()
@@ -508,6 +528,29 @@ class HostBlock:
             self.array = None
             lib().mpmgpu_host_free(self.ptr)
             self.ptr = None
+
+
+class HostState:
+    """A particle state in page-locked blocks the driver allocated: the FP64
+    columns as rows of one block in the library's column order, mat and elem
+    as the rows of a second; `particles` maps the column names to views of
+    them (the form mpmgpu_step_host steps in place).  close() frees both."""
+
+    def __init__(self, p: dict):
+        n = len(p["x"])
+        self._d = HostBlock((len(abi.DEVICE_COLUMNS), n))
+        self._i = HostBlock((2, n), np.int32)
+        out, _ = abi.contiguous_particles(p, self._d.array)
+        self._i.array[0] = p["mat"]
+        self._i.array[1] = p["elem"]
+        out["mat"], out["elem"] = self._i.array[0], self._i.array[1]
+        self.particles = out
+        self.nbytes = self._d.array.nbytes + self._i.array.nbytes
+
+    def close(self):
+        self.particles = None
+        self._d.close()
+        self._i.close()
 
 
 def pin(arrays: dict) -> list:

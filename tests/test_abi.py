@@ -74,3 +74,12 @@ def test_ctypes_structs_match_the_header(tmp_path):
     subprocess.run(["gcc", "-std=c99", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
     got = [int(x) for x in subprocess.run([str(exe)], check=True, capture_output=True, text=True).stdout.split()]
     assert got == expect
+
+
+def test_host_state_step_validates_without_gpu_work(gpu_lib):
+    """mpmgpu_step_host refuses a missing context or particle set on the host."""
+    import ctypes as C
+    from nairn_gb300 import abi
+    ps = abi.MpmGpuParticles()
+    assert gpu_lib.mpmgpu_step_host(None, C.byref(ps), 1, C.c_double(0.0)) == 1
+    assert gpu_lib.mpmgpu_step_host(None, None, 1, C.c_double(0.0)) == 1
