@@ -56,6 +56,7 @@ struct MpmGpuCtx {
     std::vector<cudaEvent_t> ev;         // per-step kernel events when profiling
     long long launches = 0;              // kernels launched by this context
     void *cpdi = nullptr;                // lCPDI corner scratch (ints then doubles)
+    void *winblock = nullptr;            // window cache of FP64 window shapes (doubles then ints)
     nmg::DevContact ct{1, 0, 2, 2, 0.};       // material fields and multimaterial contact
     bool contact_on = false;
     nmg::DevDet det{nullptr, 0, nullptr, nullptr};     // deterministic node sums (p2g option 1)

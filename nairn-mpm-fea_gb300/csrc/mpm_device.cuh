@@ -59,6 +59,13 @@ struct DevParticles {
     // weights cwg[(3c+a)*n+i]
     int *ce;
     double *cxi, *cwg;
+    // FP64 single runs with window shape functions: the step's per-axis
+    // window factors, formed once by k_p2g and reread by the later particle
+    // kernels of the step (S then dS per axis and node: win[k*n+i]), and the
+    // window's first node relative to the run's node base (win_n0[i]).
+    // nullptr: every kernel forms the window from the natural coordinates.
+    double *win;
+    int *win_n0;
     // 1: the columns are host memory the kernels reach over the host link
     // (mpmgpu_step_host); the lanes of a warp then take consecutive slots
     // (tile_particle), so that each warp access is whole lines of the link

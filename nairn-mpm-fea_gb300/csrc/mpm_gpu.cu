@@ -253,14 +253,27 @@ void column_runs(double *const hc[kParticleDoubles], size_t n, F &&f) {
     }
 }
 
+// Columns of the per-particle window cache (DevParticles::win): FP64
+// transfers with a shape function whose nodes form a box around the element
+// (2, 3 or 4 nodes per axis); 0 for lCPDI and the mixed mode.
+int win_cache_cols(const MpmGpuCtx *c) {
+    if (c->opts.precision == MPMGPU_PREC_MIXED) return 0;
+    const int s = c->opts.shape;
+    const int k = s == MPMGPU_SHAPE_LINEAR ? 2 : s == MPMGPU_SHAPE_BGIMP ? 4
+                : (s == MPMGPU_SHAPE_UGIMP || s == MPMGPU_SHAPE_BSPLINE) ? 3 : 0;
+    return 2 * c->dim * k;
+}
+
 void free_particles(MpmGpuCtx *c) {
     if (c->pblock) cudaFree(c->pblock);
     if (c->iblock) cudaFree(c->iblock);
     if (c->cpdi) cudaFree(c->cpdi);
+    if (c->winblock) cudaFree(c->winblock);
     if (c->iota) cudaFree(c->iota);
     c->pblock = nullptr;
     c->iblock = nullptr;
     c->cpdi = nullptr;
+    c->winblock = nullptr;
     c->iota = nullptr;
     sort_free(c->sort);
     c->p.n = 0;
@@ -580,10 +593,19 @@ int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
                 return set_err(c, MPMGPU_ERR_OOM, "CPDI corner allocation failed");
             }
         }
+        if (win_cache_cols(c) > 0) {
+            e = cudaMalloc(&c->winblock, (size_t)n * (win_cache_cols(c) * sizeof(double) + sizeof(int)));
+            if (e != cudaSuccess) {
+                free_particles(c);
+                return set_err(c, MPMGPU_ERR_OOM, "window cache allocation failed");
+            }
+        }
         CK(cudaMemsetAsync(c->pblock, 0, dbytes, c->stream));
         c->p.n = n;
     }
     link_columns(c->p, c->pblock, c->iblock, &c->orig);
+    c->p.win = (double *)c->winblock;
+    c->p.win_n0 = c->winblock ? (int *)(c->p.win + (size_t)win_cache_cols(c) * n) : nullptr;
     if (c->cpdi) {
         // doubles first (8-byte aligned), then the corner elements
         const size_t nc = c->dim == 3 ? 8 : 4;

@@ -790,6 +790,7 @@ template <int SHAPE, typename T>
 struct AxisWin {
     T S[3][kWinNodes<SHAPE>], dS[3][kWinNodes<SHAPE>];
     int c[3];  // node column, row and layer of the window's first node
+    int n0;    // that node's index relative to the run's node base
 };
 
 // The factors of for_each_node for element (col, row, zr) and natural
@@ -853,6 +854,56 @@ __device__ __forceinline__ void axis_windows(const DevGrid &g, int col, int row,
             w.c[a] = cc[a] + q.s - 1;
         }
     }
+    w.n0 = w.c[0] + w.c[1] * g.yplane + (DIM == 3 ? w.c[2] * g.zplane : 0);
+}
+
+// Columns of the window cache (DevParticles::win): S and dS per axis and node
+template <int DIM, int SHAPE>
+constexpr int kWinCacheCols = 2 * DIM * kWinNodes<SHAPE>;
+
+template <int DIM, int SHAPE>
+__device__ __forceinline__ void win_store(const DevParticles &p, int i, const AxisWin<SHAPE, double> &w) {
+    constexpr int K = kWinNodes<SHAPE>;
+    const size_t n = (size_t)p.n;
+    double *c = p.win + i;
+#pragma unroll
+    for (int a = 0; a < DIM; a++)
+#pragma unroll
+        for (int j = 0; j < K; j++) {
+            c[(size_t)(a * K + j) * n] = w.S[a][j];
+            c[(size_t)((DIM + a) * K + j) * n] = w.dS[a][j];
+        }
+    p.win_n0[i] = w.n0;
+}
+
+// The window of particle i for this step.  FP64 with a window cache: the
+// factors k_p2g stored (dS only when GRAD; the node column, row and layer
+// are not restored, only n0).  Otherwise formed from the natural coordinates.
+// Reading the 144 bytes of a 3D uGIMP window costs far less than the ~100
+// FP64 instructions of forming it, on a GPU whose particle kernels are bound
+// by the FP64 pipe.
+template <int DIM, int SHAPE, bool GRAD, typename T>
+__device__ __forceinline__ void particle_window(const DevGrid &g, const DevParticles &p, int i, AxisWin<SHAPE, T> &w) {
+    if constexpr (std::is_same<T, double>::value) {
+        if (p.win) {
+            constexpr int K = kWinNodes<SHAPE>;
+            const size_t n = (size_t)p.n;
+            const double *c = p.win + i;
+#pragma unroll
+            for (int a = 0; a < DIM; a++)
+#pragma unroll
+                for (int j = 0; j < K; j++) {
+                    w.S[a][j] = __ldg(c + (size_t)(a * K + j) * n);
+                    if (GRAD) w.dS[a][j] = __ldg(c + (size_t)((DIM + a) * K + j) * n);
+                }
+            w.n0 = __ldg(p.win_n0 + i);
+            return;
+        }
+    }
+    int col, row, zr;
+    elem_coords(g, p.elem[i], col, row, zr);
+    axis_windows<DIM, SHAPE, GRAD, T>(g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i], p.lpy[i],
+                                      DIM == 3 ? p.lpz[i] : 1., w);
 }
 
 // Calls f(jx, jy, jz, N, dNx, dNy, dNz) for every node of the windows, with the
@@ -880,7 +931,7 @@ __device__ __forceinline__ void for_each_window_node(const AxisWin<SHAPE, T> &w,
 // (node = global index, run node base nb)
 template <int DIM, int SHAPE, typename T, class F>
 __device__ __forceinline__ void for_each_window_node_at(const AxisWin<SHAPE, T> &w, const DevGrid &g, int nb, F &&f) {
-    const int n0 = nb + w.c[0] + w.c[1] * g.yplane + (DIM == 3 ? w.c[2] * g.zplane : 0);
+    const int n0 = nb + w.n0;
     for_each_window_node<DIM, SHAPE, false, T>(w, [&](int jx, int jy, int jz, T N, T, T, T) {
         f(n0 + jx + jy * g.yplane + (DIM == 3 ? jz * g.zplane : 0), N, T(0), T(0), T(0));
     });
@@ -1343,6 +1394,25 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 3) k_p2
         if (mm) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
         else visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, scatter);
     } else {
+        if constexpr (!MIX) {
+            if (p.win) {
+                // the step's window with its gradient factors, kept for the
+                // later particle kernels of the step (particle_window)
+                int col, row, zr;
+                elem_coords(g, e, col, row, zr);
+                AxisWin<SHAPE, double> w;
+                axis_windows<DIM, SHAPE, true, double>(g, col, row, zr, xi, eta, zeta, p.lpx[i], p.lpy[i],
+                                                       DIM == 3 ? p.lpz[i] : 1., w);
+                win_store<DIM, SHAPE>(p, i, w);
+                const int n0 = rv.nb + w.n0;
+                auto at = [&](int jx, int jy, int jz, double N, double dx, double dy, double dz) {
+                    scatter(n0 + jx + jy * g.yplane + jz * g.zplane, N, dx, dy, dz);
+                };
+                if (mm) for_each_window_node<DIM, SHAPE, true, double>(w, at);
+                else for_each_window_node<DIM, SHAPE, false, double>(w, at);
+                return;
+            }
+        }
         if (mm)
             for_each_node<DIM, SHAPE, true, T>(g, rv.nb, e, xi, eta, zeta, p.lpx[i], p.lpy[i],
                                                DIM == 3 ? p.lpz[i] : 1., scatter);
@@ -1461,12 +1531,9 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, cons
     }
     if constexpr (SHAPE != SHAPE_LCPDI) {
         // window shape functions: the separable sum (window_grad_gather)
-        int col, row, zr;
-        elem_coords(g, p.elem[i], col, row, zr);
         AxisWin<SHAPE, T> w;
-        axis_windows<DIM, SHAPE, true, T>(g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
-                                          p.lpy[i], DIM == 3 ? p.lpz[i] : 1., w);
-        const int n0 = nb + off + w.c[0] + g.yplane * w.c[1] + g.zplane * w.c[2];
+        particle_window<DIM, SHAPE, true, T>(g, p, i, w);
+        const int n0 = nb + off + w.n0;
         window_grad_gather<DIM, SHAPE, T>(w, n0, g.yplane, g.zplane, [&](int n, T v[3]) {
             if (MIX) {
                 v[0] = (T)((nd.vhx[n] - ph[0]) + (nd.vlx[n] - pl[0]));
@@ -1527,13 +1594,10 @@ __device__ __forceinline__ void forces_scatter(const StepParams &sp, const DevPa
             syz = DIM == 3 ? (T)(-mp * p.syz[i]) : T(0);
     if constexpr (SHAPE != SHAPE_LCPDI) {
         // window shape functions: the separable products (window_grad_scatter)
-        int col, row, zr;
-        elem_coords(g, p.elem[i], col, row, zr);
         AxisWin<SHAPE, T> w;
-        axis_windows<DIM, SHAPE, true, T>(g, col, row, zr, p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
-                                          p.lpy[i], DIM == 3 ? p.lpz[i] : 1., w);
+        particle_window<DIM, SHAPE, true, T>(g, p, i, w);
         const T sg[3][3] = {{sxx, sxy, sxz}, {sxy, syy, syz}, {sxz, syz, szz}};
-        const int n0 = nb + off + w.c[0] + g.yplane * w.c[1] + g.zplane * w.c[2];
+        const int n0 = nb + off + w.n0;
         window_grad_scatter<DIM, SHAPE, T>(w, sg, [&](int jx, int jy, int jz, const T f[3]) {
             const int n = n0 + jx + jy * g.yplane + jz * g.zplane;
             if constexpr (DET) {
@@ -1877,9 +1941,7 @@ static __global__ void __launch_bounds__(256, 2) k_g2p(StepParams sp, DevParticl
     // (registers) than forming them.
     AxisWin<SHAPE, T> w;
     if constexpr (SHAPE != SHAPE_LCPDI && !MIX) {
-        int col, row, zr;
-        elem_coords(g, e, col, row, zr);
-        axis_windows<DIM, SHAPE, false, T>(g, col, row, zr, xi, eta, zeta, lx, ly, lz, w);
+        particle_window<DIM, SHAPE, false, T>(g, p, i, w);
         g2p_move<DIM, SHAPE, MIX, BATCH>(sp, p, nd, i, rv, off, v, xp, &w);
     } else {
         g2p_move<DIM, SHAPE, MIX, BATCH>(sp, p, nd, i, rv, off, v, xp);
