@@ -61,7 +61,9 @@ enum {
     MPMGPU_SHAPE_UGIMP = 1,   /* uGIMP (UNIFORM_GIMP)        */
     MPMGPU_SHAPE_BGIMP = 5,   /* B2GIMP (BSPLINE_GIMP)       */
     MPMGPU_SHAPE_BSPLINE = 6, /* B2SPLINE (BSPLINE)          */
-    MPMGPU_SHAPE_LCPDI = 10   /* lCPDI (LINEAR_CPDI)         */
+    MPMGPU_SHAPE_LCPDI = 10,  /* lCPDI (LINEAR_CPDI)         */
+    MPMGPU_SHAPE_QCPDI = 11   /* qCPDI (QUADRATIC_CPDI), 2D only: nine domain points
+                                 (MatPoint2D::GetCPDINodesAndWeights, MatPoint2D.cpp:574-640) */
 };
 /* Analysis type (np): NairnMPM/src/System/MPMPrefix.hpp:115 */
 enum { MPMGPU_PLANE_STRAIN = 10, MPMGPU_THREED = 12 };

@@ -22,7 +22,7 @@ import numpy as np
 
 PLANE_STRAIN, THREED = 10, 12
 USF, USAVG, USL = 0, 2, 3
-SHAPE_LINEAR, SHAPE_UGIMP, SHAPE_BGIMP, SHAPE_BSPLINE, SHAPE_LCPDI = 0, 1, 5, 6, 10
+SHAPE_LINEAR, SHAPE_UGIMP, SHAPE_BGIMP, SHAPE_BSPLINE, SHAPE_LCPDI, SHAPE_QCPDI = 0, 1, 5, 6, 10, 11
 MAT_ISO, MAT_PLASTIC, MAT_NEOHOOKEAN, MAT_RIGID = 1, 9, 28, 35
 
 PARTICLE_FIELDS = ("x", "y", "z", "vx", "vy", "vz", "x0", "y0", "z0", "mass", "lpx", "lpy", "lpz",
@@ -207,7 +207,7 @@ def _new_particles(pos, elem, g: Grid, ppc_side: int, rho_gcc: float, thick: flo
 
 GIMP_NAMES = {"Classic": SHAPE_LINEAR, "Dirac": SHAPE_LINEAR, "uGIMP": SHAPE_UGIMP, "GIMP": SHAPE_UGIMP,
               "B2SPLINE": SHAPE_BSPLINE, "B2GIMP": SHAPE_BGIMP,
-              "lCPDI": SHAPE_LCPDI, "CPDI": SHAPE_LCPDI}
+              "lCPDI": SHAPE_LCPDI, "CPDI": SHAPE_LCPDI, "qCPDI": SHAPE_QCPDI}
 
 
 def _material(mat_type, rho, E=0., nu=0., yield_=0., Ep=0., G=0., K=0., uj=0):

@@ -545,10 +545,10 @@ static void shape_eval(const OGrid *g, int shape, int e, const double *xi, const
 /* ------------------------------------------------------------------------ */
 /* Linear CPDI (lCPDI)                                                       */
 /* ------------------------------------------------------------------------ */
-typedef struct {            /* CPDIDomain of each corner, found once per step */
-    int elem[8];
-    double xi[8][3];
-    double wg[8][3];
+typedef struct {            /* CPDIDomain of each domain point, found once per step */
+    int elem[9];
+    double xi[9][3];
+    double wg[9][3];
 } OCpdi;
 
 static const double r1s[8] = {-1., 1., 1., -1., -1., 1., 1., -1.};
@@ -585,7 +585,7 @@ static int find_element(const OGrid *g, double x, double y, double z) {
  * GetParticleSize (MPMBase.cpp:519-524, MatPoint3D.cpp:227-233); no rcrit
  * rescaling (ElementBase::rcrit < 0 by default).  Returns 0, or -1 when a
  * corner is off the grid. */
-static int cpdi_setup(const OGrid *g, const MpmGpuParticles *p, long q, OCpdi *cp) {
+static int cpdi_setup(const OGrid *g, const MpmGpuParticles *p, long q, int quad, OCpdi *cp) {
     int is3d = g->dim == 3;
     double ex0, ex1, ey0, ey1, ez0, ez1;
     elem_extent(g, p->elem[q], &ex0, &ex1, &ey0, &ey1, &ez0, &ez1);
@@ -606,6 +606,43 @@ static int cpdi_setup(const OGrid *g, const MpmGpuParticles *p, long q, OCpdi *c
             if (e < 0) return -1;
             cp->elem[i] = e;
             xi_pos(g, e, cx[i], cy[i], 0., cp->xi[i]);
+        }
+        if (quad) {
+            /* qCPDI (MatPoint2D.cpp:574-640): the four edge midpoints, counter
+             * clockwise from the bottom edge, then the material point itself
+             * in its own element; gradient weights from the linear domain
+             * weights divided by 3 Ap */
+            double ex[4] = {px - r2x, px + r1x, px + r2x, px - r1x};
+            double ey[4] = {py - r2y, py + r1y, py + r2y, py - r1y};
+            for (int i = 0; i < 4; i++) {
+                int e = find_element(g, ex[i], ey[i], 0.);
+                if (e < 0) return -1;
+                cp->elem[4 + i] = e;
+                xi_pos(g, e, ex[i], ey[i], 0., cp->xi[4 + i]);
+            }
+            cp->elem[8] = p->elem[q];
+            xi_pos(g, p->elem[q], px, py, 0., cp->xi[8]);
+            Ap = 1. / (3. * Ap);
+            cp->wg[0][0] = (r1y - r2y) * Ap;
+            cp->wg[0][1] = (-r1x + r2x) * Ap;
+            cp->wg[1][0] = (r1y + r2y) * Ap;
+            cp->wg[1][1] = (-r1x - r2x) * Ap;
+            cp->wg[2][0] = (-r1y + r2y) * Ap;
+            cp->wg[2][1] = (r1x - r2x) * Ap;
+            cp->wg[3][0] = (-r1y - r2y) * Ap;
+            cp->wg[3][1] = (r1x + r2x) * Ap;
+            cp->wg[4][0] = 4. * r1y * Ap;
+            cp->wg[4][1] = -4. * r1x * Ap;
+            cp->wg[5][0] = 4. * r2y * Ap;
+            cp->wg[5][1] = -4. * r2x * Ap;
+            cp->wg[6][0] = -4. * r1y * Ap;
+            cp->wg[6][1] = 4. * r1x * Ap;
+            cp->wg[7][0] = -4. * r2y * Ap;
+            cp->wg[7][1] = 4. * r2x * Ap;
+            cp->wg[8][0] = 0.;
+            cp->wg[8][1] = 0.;
+            for (int i = 0; i < 9; i++) cp->wg[i][2] = 0.;
+            return 0;
         }
         Ap = 1. / Ap;
         cp->wg[0][0] = (r1y - r2y) * Ap;
@@ -673,14 +710,17 @@ static int cpdi_setup(const OGrid *g, const MpmGpuParticles *p, long q, OCpdi *c
  * merged in order of first appearance.  Returns 0, or -1 when the particle
  * needs more than maxShapeNodes-1 nodes (17 in 2D, 50 in 3D,
  * MPMReadHandler.cpp:558-562). */
-static int shape_cpdi(const OGrid *g, const OCpdi *cp, int grad, OShape *s) {
+static int shape_cpdi(const OGrid *g, const OCpdi *cp, int quad, int grad, OShape *s) {
     int is3d = g->dim == 3;
-    int ncorner = is3d ? 8 : 4;
-    int maxnodes = is3d ? 50 : 17;
-    double ws = is3d ? 0.125 : 0.25;
+    int ncorner = quad ? 9 : (is3d ? 8 : 4);
+    int maxnodes = quad ? 37 : (is3d ? 50 : 17);
     double lp1[3] = {1., 1., 1.};
     int ind = 0;
     for (int i = 0; i < ncorner; i++) {
+        /* shape weights of the domain points (MPMBase.cpp:163-173): lCPDI 1/4
+         * (2D) or 1/8 (3D); qCPDI 1/36 at the corners, 1/9 at the edges, 4/9
+         * at the material point */
+        double ws = quad ? (i < 4 ? 1. / 36. : (i < 8 ? 1. / 9. : 4. / 9.)) : (is3d ? 0.125 : 0.25);
         OShape cs;
         shape_eval(g, MPMGPU_SHAPE_LINEAR, cp->elem[i], cp->xi[i], lp1, 0, &cs);
         for (int j = 0; j < cs.n; j++) {
@@ -1179,8 +1219,8 @@ static int particle_rigid(const OCtx *c, long q) {
 
 /* shape functions of particle q for this step (GetShapeFunctions/GetShapeGradients) */
 static void particle_shape(OCtx *c, long q, int grad, OShape *s) {
-    if (c->o->shape == MPMGPU_SHAPE_LCPDI) {
-        if (shape_cpdi(&c->g, &c->cpdi[q], grad, s) != 0) {
+    if (c->o->shape == MPMGPU_SHAPE_LCPDI || c->o->shape == MPMGPU_SHAPE_QCPDI) {
+        if (shape_cpdi(&c->g, &c->cpdi[q], c->o->shape == MPMGPU_SHAPE_QCPDI, grad, s) != 0) {
 #pragma omp atomic write
             c->cpdi_err = 1;
             s->n = 0;
@@ -2413,7 +2453,8 @@ static int one_step(OCtx *c) {
      * corners (lCPDI) and natural coordinates (MoreMPMElementBase.cpp:50-57) */
     zero_field(f, nn);
     for (long q = 0; q < p->n; q++) {
-        if (c->o->shape == MPMGPU_SHAPE_LCPDI && cpdi_setup(&c->g, p, q, &c->cpdi[q]) != 0)
+        if ((c->o->shape == MPMGPU_SHAPE_LCPDI || c->o->shape == MPMGPU_SHAPE_QCPDI) &&
+            cpdi_setup(&c->g, p, q, c->o->shape == MPMGPU_SHAPE_QCPDI, &c->cpdi[q]) != 0)
             return fail(MPMGPU_ERR_LEFT_GRID, "oracle: a CPDI particle domain node has left the grid");
         xi_pos(&c->g, p->elem[q], p->x[q], p->y[q], is3d ? p->z[q] : 0., &c->xi[3 * q]);
     }
@@ -2496,8 +2537,11 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     g_err[0] = 0;
     if (!grid || !opts || !mats || !p) return fail(MPMGPU_ERR_INVALID, "oracle: null argument");
     if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI &&
-        opts->shape != MPMGPU_SHAPE_BSPLINE && opts->shape != MPMGPU_SHAPE_BGIMP)
+        opts->shape != MPMGPU_SHAPE_BSPLINE && opts->shape != MPMGPU_SHAPE_BGIMP && opts->shape != MPMGPU_SHAPE_QCPDI)
         return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: shape function not implemented");
+    /* ElementBase::InitializeCPDI: qCPDI is 2D only (MoreMPMElementBase.cpp:1008-1013) */
+    if (opts->shape == MPMGPU_SHAPE_QCPDI && grid->dim == 3)
+        return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: qCPDI is not defined in 3D; use lCPDI");
     if (contact && contact->enabled) {
         if (contact->normals < 0 || (contact->normals > 2 && contact->normals != 5 && contact->normals != 6))
             return fail(MPMGPU_ERR_UNSUPPORTED, "oracle: contact normals must be method 0, 1, 2, 5 or 6");
@@ -2567,7 +2611,7 @@ int mpm_oracle_run(const MpmGpuGrid *grid, const MpmGpuOptions *opts, const MpmG
     for (unsigned k = 0; k < sizeof(fl) / sizeof(fl[0]); k++) *fl[k] = (double *)calloc((size_t)nn, sizeof(double));
     c.f.npts = (int *)calloc((size_t)nn, sizeof(int));
     c.xi = (double *)calloc((size_t)(3 * (p->n > 0 ? p->n : 1)), sizeof(double));
-    if (opts->shape == MPMGPU_SHAPE_LCPDI) c.cpdi = (OCpdi *)calloc((size_t)(p->n > 0 ? p->n : 1), sizeof(OCpdi));
+    if (opts->shape == MPMGPU_SHAPE_LCPDI || opts->shape == MPMGPU_SHAPE_QCPDI) c.cpdi = (OCpdi *)calloc((size_t)(p->n > 0 ? p->n : 1), sizeof(OCpdi));
     if (c.mm && c.normals >= 5) {
         c.lr_start = (long *)calloc((size_t)c.g.nnodes + 2, sizeof(long));
         c.lr_list = (long *)calloc((size_t)(p->n > 0 ? p->n : 1) * 64, sizeof(long));

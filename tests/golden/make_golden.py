@@ -122,6 +122,13 @@ CASES = {
     "rigid3d_taylor_wall": ("rigid_taylor_3d", dict(steps=40, friction=0.0, normals=2)),
     "rigid3d_taylor_wall_fric_usl": ("rigid_taylor_3d", dict(steps=40, friction=0.3, normals=0, method=3,
                                                              vx0=40000.)),
+    # quadratic CPDI (qCPDI, 2D only): nine domain points per particle
+    "cant2d_qcpdi_usavg": ("cantilever_2d", dict(nx=10, ny=4, steps=60, gimp="qCPDI")),
+    "cant2d_qcpdi_ppc3_usl": ("cantilever_2d", dict(nx=8, ny=3, steps=40, ppc_side=3, gimp="qCPDI", method=3)),
+    "cant2d_qcpdi_neo_usf": ("cantilever_2d", dict(nx=10, ny=4, steps=150, mat_type=28, G=3., K=30., rho=1.1,
+                                                   v0=20000., margin_cells=8, gimp="qCPDI", method=0)),
+    "cant2d_qcpdi_xpic2": ("cantilever_2d", dict(nx=10, ny=4, steps=60, gimp="qCPDI", xpic=(2, 0, 1))),
+    "contact2d_fric_qcpdi": ("contact_2d", dict(steps=120, friction=0.3, normals=2, gimp="qCPDI")),
     # PeriodicXPIC with multimaterial contact: the contact law re-applied to
     # every expansion pass's increment from the last contact call's state
     "contact2d_xpic2_fric": ("contact_2d", dict(steps=120, friction=0.3, normals=2, xpic=(2, 0, 1))),
