@@ -270,8 +270,8 @@ void batch_link(MpmGpuBatch *b) {
     p.run = ib + 3 * cap;
     p.n = b->n_used;
     if (b->cpdi) {
-        // corner scratch, rebuilt at every step start with stride n_used
-        const size_t nc = b->dim == 3 ? 8 : 4;
+        // domain-point scratch, rebuilt at every step start with stride n_used
+        const size_t nc = b->o.shape == MPMGPU_SHAPE_QCPDI ? 9 : (b->dim == 3 ? 8 : 4);
         p.cxi = (double *)b->cpdi;
         p.cwg = p.cxi + 3 * nc * cap;
         p.ce = (int *)(p.cwg + 3 * nc * cap);
@@ -417,7 +417,7 @@ void batch_enqueue_step(MpmGpuBatch *b) {
     // mixed mode, one material field, window shape functions: the scatters
     // accumulate in shared-memory node tiles (each block's runs beyond its
     // first scatter straight to the node columns)
-    constexpr bool kTileable = MIX && SHAPE != SHAPE_LCPDI;
+    constexpr bool kTileable = MIX && !kCpdi<SHAPE>;
     const bool tile = kTileable && b->nf == 1;
     if constexpr (kTileable) {
         if (tile) k_p2g_tile<DIM, SHAPE, true><<<pb, TB, 0, s>>>(sp, b->p, b->nd);
@@ -513,6 +513,9 @@ template <int DIM, bool MIX>
 void batch_enqueue_shape(MpmGpuBatch *b) {
     if (b->o.shape == MPMGPU_SHAPE_LINEAR) batch_enqueue_step<DIM, SHAPE_LINEAR, MIX>(b);
     else if (b->o.shape == MPMGPU_SHAPE_LCPDI) batch_enqueue_step<DIM, SHAPE_LCPDI, MIX>(b);
+    else if (b->o.shape == MPMGPU_SHAPE_QCPDI) {
+        if constexpr (DIM == 2) batch_enqueue_step<DIM, SHAPE_QCPDI, MIX>(b);  // refused in 3D at create
+    }
     else if (b->o.shape == MPMGPU_SHAPE_BSPLINE) batch_enqueue_step<DIM, SHAPE_BSPLINE, MIX>(b);
     else if (b->o.shape == MPMGPU_SHAPE_BGIMP) batch_enqueue_step<DIM, SHAPE_BGIMP, MIX>(b);
     else batch_enqueue_step<DIM, SHAPE_UGIMP, MIX>(b);
@@ -691,10 +694,11 @@ int64_t mpmgpu_batch_bytes(const MpmGpuBatchOptions *o) {
     const int64_t P = o->max_particles, N = o->max_nodes;
     const int64_t ntiles = (P + kTile - 1) / kTile;
     const int64_t nf = o->max_fields > 1 ? o->max_fields : 1;
-    const int64_t nc = o->np == MPMGPU_THREED ? 8 : 4;
+    const int64_t nc = o->shape == MPMGPU_SHAPE_QCPDI ? 9 : (o->np == MPMGPU_THREED ? 8 : 4);
     int64_t bytes = 2 * P * (int64_t)((kParticleDoubles + 1) * sizeof(double) + kBatchIntCols * sizeof(int));
     bytes += 4 * P * (int64_t)sizeof(int) + 2 * 256 * ntiles * (int64_t)sizeof(int);  // sort keys, histograms
-    if (o->shape == MPMGPU_SHAPE_LCPDI) bytes += P * nc * (int64_t)(sizeof(int) + 6 * sizeof(double));
+    if (o->shape == MPMGPU_SHAPE_LCPDI || o->shape == MPMGPU_SHAPE_QCPDI)
+        bytes += P * nc * (int64_t)(sizeof(int) + 6 * sizeof(double));
     bytes += N * nf * (int64_t)((nf > 1 ? 26 : 19) * sizeof(double) + 12 * sizeof(float) + 1);
     bytes += N * (int64_t)(2 * sizeof(int) + sizeof(double));
     bytes += (int64_t)o->max_materials * (int64_t)sizeof(DevMat) + (int64_t)o->max_runs * (int64_t)sizeof(DevRun);
@@ -715,8 +719,10 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     if (o->np != MPMGPU_PLANE_STRAIN && o->np != MPMGPU_THREED)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "batch analysis type must be 2D plane strain or 3D");
     if (o->shape != MPMGPU_SHAPE_LINEAR && o->shape != MPMGPU_SHAPE_UGIMP && o->shape != MPMGPU_SHAPE_LCPDI &&
-        o->shape != MPMGPU_SHAPE_BSPLINE && o->shape != MPMGPU_SHAPE_BGIMP)
+        o->shape != MPMGPU_SHAPE_BSPLINE && o->shape != MPMGPU_SHAPE_BGIMP && o->shape != MPMGPU_SHAPE_QCPDI)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
+    if (o->shape == MPMGPU_SHAPE_QCPDI && o->np == MPMGPU_THREED)
+        return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "qCPDI is defined in 2D only (the reference refuses it in 3D)");
     if (o->method != MPMGPU_USF && o->method != MPMGPU_USAVG && o->method != MPMGPU_USL)
         return berr(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
     if (o->precision != MPMGPU_PREC_FP64 && o->precision != MPMGPU_PREC_MIXED)
@@ -758,7 +764,8 @@ int mpmgpu_batch_create(const MpmGpuBatchOptions *o, MpmGpuBatch **out) {
     }
     A((void **)&b->nblock, NT * ncols * sizeof(double) + NT);
     A((void **)&b->fblock, NT * 12 * sizeof(float));
-    if (o->shape == MPMGPU_SHAPE_LCPDI) A(&b->cpdi, P * (b->dim == 3 ? 8 : 4) * (sizeof(int) + 6 * sizeof(double)));
+    if (o->shape == MPMGPU_SHAPE_LCPDI || o->shape == MPMGPU_SHAPE_QCPDI)
+        A(&b->cpdi, P * (o->shape == MPMGPU_SHAPE_QCPDI ? 9 : (b->dim == 3 ? 8 : 4)) * (sizeof(int) + 6 * sizeof(double)));
     A((void **)&b->coords, N * sizeof(double));
     A((void **)&b->nrun, N * sizeof(int));
     A((void **)&b->bc_group, N * sizeof(int));

@@ -264,6 +264,12 @@ int win_cache_cols(const MpmGpuCtx *c) {
     return 2 * c->dim * k;
 }
 
+// Domain points per particle of the CPDI shape functions (0 for the others)
+int cpdi_points(const MpmGpuCtx *c) {
+    if (c->opts.shape == MPMGPU_SHAPE_QCPDI) return 9;
+    return c->opts.shape == MPMGPU_SHAPE_LCPDI ? (c->dim == 3 ? 8 : 4) : 0;
+}
+
 void free_particles(MpmGpuCtx *c) {
     if (c->pblock) cudaFree(c->pblock);
     if (c->iblock) cudaFree(c->iblock);
@@ -300,8 +306,11 @@ int mpmgpu_create(const MpmGpuGrid *grid, const MpmGpuOptions *opts, MpmGpuCtx *
         (grid->dim == 2 && opts->np != MPMGPU_PLANE_STRAIN))
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "analysis type must be 2D plane strain or 3D");
     if (opts->shape != MPMGPU_SHAPE_LINEAR && opts->shape != MPMGPU_SHAPE_UGIMP && opts->shape != MPMGPU_SHAPE_LCPDI &&
-        opts->shape != MPMGPU_SHAPE_BSPLINE && opts->shape != MPMGPU_SHAPE_BGIMP)
+        opts->shape != MPMGPU_SHAPE_BSPLINE && opts->shape != MPMGPU_SHAPE_BGIMP && opts->shape != MPMGPU_SHAPE_QCPDI)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "shape function option not implemented on the device");
+    // ElementBase::InitializeCPDI refuses qCPDI in 3D (MoreMPMElementBase.cpp:1008-1013)
+    if (opts->shape == MPMGPU_SHAPE_QCPDI && grid->dim == 3)
+        return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "qCPDI is defined in 2D only; use lCPDI in 3D");
     if (opts->method != MPMGPU_USF && opts->method != MPMGPU_USAVG && opts->method != MPMGPU_USL)
         return set_err(nullptr, MPMGPU_ERR_UNSUPPORTED, "MPM method must be USF, USAVG or USL");
     if (opts->precision != MPMGPU_PREC_FP64 && opts->precision != MPMGPU_PREC_MIXED)
@@ -583,9 +592,9 @@ int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
             free_particles(c);
             return set_err(c, MPMGPU_ERR_OOM, "sort workspace allocation failed");
         }
-        if (c->opts.shape == MPMGPU_SHAPE_LCPDI) {
-            // per corner: element (int), natural coordinates and gradient weights (3 doubles each)
-            const size_t nc = c->dim == 3 ? 8 : 4;
+        if (cpdi_points(c) > 0) {
+            // per domain point: element (int), natural coordinates and gradient weights (3 doubles each)
+            const size_t nc = (size_t)cpdi_points(c);
             const size_t bytes = (size_t)n * nc * (sizeof(int) + 6 * sizeof(double)) + 256;
             e = cudaMalloc(&c->cpdi, bytes);
             if (e != cudaSuccess) {
@@ -607,8 +616,8 @@ int mpmgpu_upload_particles(MpmGpuCtx *c, const MpmGpuParticles *h) {
     c->p.win = (double *)c->winblock;
     c->p.win_n0 = c->winblock ? (int *)(c->p.win + (size_t)win_cache_cols(c) * n) : nullptr;
     if (c->cpdi) {
-        // doubles first (8-byte aligned), then the corner elements
-        const size_t nc = c->dim == 3 ? 8 : 4;
+        // doubles first (8-byte aligned), then the domain points' elements
+        const size_t nc = (size_t)cpdi_points(c);
         c->p.cxi = (double *)c->cpdi;
         c->p.cwg = c->p.cxi + 3 * nc * (size_t)n;
         c->p.ce = (int *)(c->p.cwg + 3 * nc * (size_t)n);

@@ -20,14 +20,47 @@
 
 namespace nmg {
 
-enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2, SHAPE_BSPLINE = 3, SHAPE_BGIMP = 4 };
+enum { SHAPE_LINEAR = 0, SHAPE_UGIMP = 1, SHAPE_LCPDI = 2, SHAPE_BSPLINE = 3, SHAPE_BGIMP = 4, SHAPE_QCPDI = 5 };
+
+// CPDI shape functions: the particle domain's points carry the grid's linear
+// shape functions (ElementBase::GetCPDIFunctions, MoreMPMElementBase.cpp:581-656)
+template <int SHAPE>
+constexpr bool kCpdi = SHAPE == SHAPE_LCPDI || SHAPE == SHAPE_QCPDI;
+// domain points per particle (ElementBase::InitializeCPDI, MoreMPMElementBase.cpp:1005-1020):
+// the lCPDI corners, or qCPDI's corners, edge midpoints and material point (2D)
+template <int DIM, int SHAPE>
+constexpr int kCpdiPts = SHAPE == SHAPE_QCPDI ? 9 : (DIM == 3 ? 8 : 4);
+
+// shape weight of domain point c (MPMBase.cpp:163-173)
+template <int DIM, int SHAPE, typename T>
+__device__ __forceinline__ T cpdi_ws(int c) {
+    if constexpr (SHAPE == SHAPE_QCPDI) return c < 4 ? T(1. / 36.) : (c < 8 ? T(1. / 9.) : T(4. / 9.));
+    else return DIM == 3 ? T(0.125) : T(0.25);
+}
+
+// position of domain point c as pos + s1 r1 + s2 r2 + s3 r3 (MatPoint2D.cpp:519-640,
+// MatPoint3D.cpp:538-601): lCPDI corners counter-clockwise (then the upper
+// layer in 3D); qCPDI adds the edge midpoints -r2, +r1, +r2, -r1 and the
+// material point itself
+template <int SHAPE, typename T>
+__device__ __forceinline__ void cpdi_signs(int c, T &s1, T &s2, T &s3) {
+    if constexpr (SHAPE == SHAPE_QCPDI) {
+        s1 = (c == 1 || c == 2 || c == 5) ? T(1) : ((c == 0 || c == 3 || c == 7) ? T(-1) : T(0));
+        s2 = (c == 2 || c == 3 || c == 6) ? T(1) : ((c == 0 || c == 1 || c == 4) ? T(-1) : T(0));
+        s3 = T(0);
+    } else {
+        s1 = (c == 1 || c == 2 || c == 5 || c == 6) ? T(1) : T(-1);
+        s2 = (c == 2 || c == 3 || c == 6 || c == 7) ? T(1) : T(-1);
+        s3 = c >= 4 ? T(1) : T(-1);
+    }
+}
 
 // Resident 256-thread blocks per SM the strain kernels are compiled for (this
 // caps their registers at 80): their FP64 constitutive updates are latency
 // bound at the two blocks the uncapped register count allows.  lCPDI kernels
-// keep their registers (the 27-node window); capping them spills.
+// keep their registers (the 27-node window); capping them spills.  So do qCPDI's.
 template <int SHAPE>
-constexpr int kStrainBlocks = SHAPE == SHAPE_LCPDI ? 2 : 3;
+constexpr int kStrainBlocks = kCpdi<SHAPE> ? 2 : 3;
 
 // ---------------------------------------------------------------------------
 // deterministic node sums (MPMGPU_P2G_DETERMINISTIC)
@@ -334,9 +367,9 @@ __device__ __forceinline__ T cpdi_wg(const DevParticles &p, size_t k) {
 // gradient weights.  The reference throws when a corner is off the grid or the
 // particle touches more than 16 (2D) / 49 (3D) nodes (GetCPDIFunctions); here
 // those set ERR_LEFT_GRID / ERR_CPDI_NODES.  Returns false on an error.
-template <int DIM>
+template <int DIM, int SHAPE>
 static __device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
-    constexpr int NC = DIM == 3 ? 8 : 4;
+    constexpr int NC = kCpdiPts<DIM, SHAPE>;
     const size_t n = (size_t)p.n;
     int col, row, zr;
     elem_coords(g, p.elem[i], col, row, zr);
@@ -367,17 +400,19 @@ static __device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i
     int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
 #pragma unroll
     for (int c = 0; c < NC; c++) {
-        const double s1 = (c == 1 || c == 2 || c == 5 || c == 6) ? 1. : -1.;
-        const double s2 = (c == 2 || c == 3 || c == 6 || c == 7) ? 1. : -1.;
-        const double s3 = c >= 4 ? 1. : -1.;
+        double s1, s2, s3;
+        cpdi_signs<SHAPE>(c, s1, s2, s3);
         double cp[3];
 #pragma unroll
         for (int a = 0; a < DIM; a++) {
             cp[a] = pos[a] + s1 * r1[a] + s2 * r2[a];
             if (DIM == 3) cp[a] += s3 * r3[a];
         }
-        const int cc = find_cell(cp[0], g.xmin, g.gx, g.igx, g.nx);
-        const int cr = find_cell(cp[1], g.ymin, g.gy, g.igy, g.ny);
+        // qCPDI's material point lies in the particle's own element
+        // (MatPoint2D.cpp:627-629); the other points are looked up
+        const bool own = SHAPE == SHAPE_QCPDI && c == 8;
+        const int cc = own ? col : find_cell(cp[0], g.xmin, g.gx, g.igx, g.nx);
+        const int cr = own ? row : find_cell(cp[1], g.ymin, g.gy, g.igy, g.ny);
         const int cz = DIM == 3 ? find_cell(cp[2], g.zmin, g.gz, g.igz, g.nz) : 0;
         if (cc < 0 || cr < 0 || cz < 0) {
             atomicOr(err, ERR_LEFT_GRID);
@@ -398,13 +433,25 @@ static __device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i
     }
     // gradient weights
     if (DIM == 2) {
-        const double Ap = 1. / (4. * (r1[0] * r2[1] - r1[1] * r2[0]));
+        // qCPDI takes the linear weights over 3 Ap, and its edge points 4 r / (3 Ap)
+        // (MatPoint2D.cpp:620-640)
+        const double Ap = SHAPE == SHAPE_QCPDI ? 1. / (3. * (4. * (r1[0] * r2[1] - r1[1] * r2[0])))
+                                               : 1. / (4. * (r1[0] * r2[1] - r1[1] * r2[0]));
         const double wx[4] = {r1[1] - r2[1], r1[1] + r2[1], -r1[1] + r2[1], -r1[1] - r2[1]};
         const double wy[4] = {-r1[0] + r2[0], -r1[0] - r2[0], r1[0] - r2[0], r1[0] + r2[0]};
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             p.cwg[(3 * c + 0) * n + i] = wx[c] * Ap;
             p.cwg[(3 * c + 1) * n + i] = wy[c] * Ap;
+        }
+        if constexpr (SHAPE == SHAPE_QCPDI) {
+            const double ex[5] = {4. * r1[1] * Ap, 4. * r2[1] * Ap, -4. * r1[1] * Ap, -4. * r2[1] * Ap, 0.};
+            const double ey[5] = {-4. * r1[0] * Ap, -4. * r2[0] * Ap, 4. * r1[0] * Ap, 4. * r2[0] * Ap, 0.};
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                p.cwg[(3 * (4 + c) + 0) * n + i] = ex[c];
+                p.cwg[(3 * (4 + c) + 1) * n + i] = ey[c];
+            }
         }
     } else {
         // the reference's per-corner expressions are signed sums of the cross
@@ -474,9 +521,9 @@ static __device__ bool cpdi_setup(const DevGrid &g, const DevParticles &p, int i
 // floats.  A corner within float rounding of a cell face may land in the
 // neighbouring cell; the linear shape functions of the two cells agree on the
 // face, so the weights change by rounding only.
-template <int DIM>
+template <int DIM, int SHAPE>
 static __device__ bool cpdi_setup_f32(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
-    constexpr int NC = DIM == 3 ? 8 : 4;
+    constexpr int NC = kCpdiPts<DIM, SHAPE>;
     const size_t n = (size_t)p.n;
     float *cxf = reinterpret_cast<float *>(p.cxi), *cwf = reinterpret_cast<float *>(p.cwg);
     int col, row, zr;
@@ -506,16 +553,16 @@ static __device__ bool cpdi_setup_f32(const DevGrid &g, const DevParticles &p, i
     int cel[NC][3];
 #pragma unroll
     for (int c = 0; c < NC; c++) {
-        const float s1 = (c == 1 || c == 2 || c == 5 || c == 6) ? 1.f : -1.f;
-        const float s2 = (c == 2 || c == 3 || c == 6 || c == 7) ? 1.f : -1.f;
-        const float s3 = c >= 4 ? 1.f : -1.f;
+        float s1, s2, s3;
+        cpdi_signs<SHAPE>(c, s1, s2, s3);
         int ce[3] = {0, 0, 0};
 #pragma unroll
         for (int a = 0; a < DIM; a++) {
             float cp = rel[a] + s1 * r1[a] + s2 * r2[a];
             if (DIM == 3) cp += s3 * r3[a];
             const float q = cp * ics[a];
-            const int o = __float2int_rd(q);
+            // qCPDI's material point stays in the particle's own element
+            const int o = SHAPE == SHAPE_QCPDI && c == 8 ? 0 : __float2int_rd(q);
             ce[a] = base[a] + o;
             if (ce[a] < 0 || ce[a] >= ncell[a]) {
                 atomicOr(err, ERR_LEFT_GRID);
@@ -531,13 +578,23 @@ static __device__ bool cpdi_setup_f32(const DevGrid &g, const DevParticles &p, i
         p.ce[c * n + i] = DIM == 3 ? g.nx * (ce[2] * g.ny + ce[1]) + ce[0] : ce[1] * g.nx + ce[0];
     }
     if (DIM == 2) {
-        const float Ap = 1.f / (4.f * (r1[0] * r2[1] - r1[1] * r2[0]));
+        const float Ap = SHAPE == SHAPE_QCPDI ? 1.f / (3.f * (4.f * (r1[0] * r2[1] - r1[1] * r2[0])))
+                                              : 1.f / (4.f * (r1[0] * r2[1] - r1[1] * r2[0]));
         const float wx[4] = {r1[1] - r2[1], r1[1] + r2[1], -r1[1] + r2[1], -r1[1] - r2[1]};
         const float wy[4] = {-r1[0] + r2[0], -r1[0] - r2[0], r1[0] - r2[0], r1[0] + r2[0]};
 #pragma unroll
         for (int c = 0; c < 4; c++) {
             cwf[(3 * c + 0) * n + i] = wx[c] * Ap;
             cwf[(3 * c + 1) * n + i] = wy[c] * Ap;
+        }
+        if constexpr (SHAPE == SHAPE_QCPDI) {
+            const float ex[5] = {4.f * r1[1] * Ap, 4.f * r2[1] * Ap, -4.f * r1[1] * Ap, -4.f * r2[1] * Ap, 0.f};
+            const float ey[5] = {-4.f * r1[0] * Ap, -4.f * r2[0] * Ap, 4.f * r1[0] * Ap, 4.f * r2[0] * Ap, 0.f};
+#pragma unroll
+            for (int c = 0; c < 5; c++) {
+                cwf[(3 * (4 + c) + 0) * n + i] = ex[c];
+                cwf[(3 * (4 + c) + 1) * n + i] = ey[c];
+            }
         }
     } else {
         const float a12[3] = {r1[1] * r2[2] - r1[2] * r2[1], r1[2] * r2[0] - r1[0] * r2[2], r1[0] * r2[1] - r1[1] * r2[0]};
@@ -587,23 +644,23 @@ static __device__ bool cpdi_setup_f32(const DevGrid &g, const DevParticles &p, i
 }
 
 // the corner setup of the step in the transfer arithmetic of the mode
-template <int DIM, bool MIX>
+template <int DIM, int SHAPE, bool MIX>
 __device__ __forceinline__ bool cpdi_setup_for(const DevGrid &g, const DevParticles &p, int i, unsigned *err) {
-    if constexpr (MIX) return cpdi_setup_f32<DIM>(g, p, i, err);
-    else return cpdi_setup<DIM>(g, p, i, err);
+    if constexpr (MIX) return cpdi_setup_f32<DIM, SHAPE>(g, p, i, err);
+    else return cpdi_setup<DIM, SHAPE>(g, p, i, err);
 }
 
 // GetCPDIFunctions (MoreMPMElementBase.cpp:581-656) without the node merge:
 // f is called for every (corner, element node) pair with weight ws * N and
 // gradient wg * N (N the corner element's linear shape function, pairs with
 // N < 1e-15 skipped); the sums over pairs equal the merged node values.
-template <int DIM, bool GRAD, typename T, class F>
+template <int DIM, int SHAPE, bool GRAD, typename T, class F>
 __device__ __forceinline__ void cpdi_nodes(const DevGrid &g, int nb, const DevParticles &p, int i, F &&f) {
-    constexpr int NC = DIM == 3 ? 8 : 4;
+    constexpr int NC = kCpdiPts<DIM, SHAPE>;
     const size_t n = (size_t)p.n;
-    const T ws = DIM == 3 ? T(0.125) : T(0.25);
 #pragma unroll 1
     for (int c = 0; c < NC; c++) {
+        const T ws = cpdi_ws<DIM, SHAPE, T>(c);
         int col, row, zr;
         elem_coords(g, p.ce[c * n + i], col, row, zr);
         const int n0 = nb + zr * g.zplane + row * g.yplane + col;
@@ -637,9 +694,9 @@ __device__ __forceinline__ void cpdi_nodes(const DevGrid &g, int nb, const DevPa
 // offset, accumulated in registers; f is then called once per node with a
 // nonzero weight (at most 27 calls instead of 64 pair calls).  Wider domains
 // fall back to the pair visits.  Returns false when it fell back.
-template <int DIM, bool GRAD, class F>
+template <int DIM, int SHAPE, bool GRAD, class F>
 __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevParticles &p, int i, F &&f) {
-    constexpr int NC = DIM == 3 ? 8 : 4;
+    constexpr int NC = kCpdiPts<DIM, SHAPE>;
     const size_t n = (size_t)p.n;
     int lo[3] = {1 << 30, 1 << 30, 1 << 30}, hi[3] = {-1, -1, -1};
     int cell[NC][3];
@@ -656,7 +713,7 @@ __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevP
 #pragma unroll
     for (int a = 0; a < DIM; a++) fits = fits && hi[a] - lo[a] <= 1;
     if (!fits) {
-        cpdi_nodes<DIM, GRAD, float>(g, nb, p, i, f);
+        cpdi_nodes<DIM, SHAPE, GRAD, float>(g, nb, p, i, f);
         return;
     }
     // per corner: natural coordinates, the corner cell's offset in the window
@@ -678,7 +735,6 @@ __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevP
         const float w0 = 0.5f * (1.f - xi[c][a]), w1 = 0.5f * (1.f + xi[c][a]);
         return j == 0 ? (up ? 0.f : w0) : (j == 1 ? (up ? w0 : w1) : (up ? w1 : 0.f));
     };
-    const float ws = DIM == 3 ? 0.125f : 0.25f;
     const int base = nb + (DIM == 3 ? lo[2] * g.zplane : 0) + lo[1] * g.yplane + lo[0];
     // one window row (cy, cz) at a time: sums over the corners in corner order,
     // as the merged node list of the reference accumulates them
@@ -694,7 +750,7 @@ __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevP
                 float sfn = wt(c, 0, cx) * wy;
                 if (DIM == 3) sfn *= wz;
                 if (sfn < 1e-15f) continue;
-                N[cx] += ws * sfn;
+                N[cx] += cpdi_ws<DIM, SHAPE, float>(c) * sfn;
                 if (GRAD) {
                     GX[cx] += wg[c][0] * sfn;
                     GY[cx] += wg[c][1] * sfn;
@@ -713,9 +769,9 @@ __device__ __forceinline__ void cpdi_window(const DevGrid &g, int nb, const DevP
 // the nodes of particle i for this step, whatever the shape-function option
 template <int DIM, int SHAPE, bool GRAD, typename T, class F>
 __device__ __forceinline__ void visit_nodes(const DevGrid &g, int nb, const DevParticles &p, int i, F &&f) {
-    if constexpr (SHAPE == SHAPE_LCPDI) {
-        if constexpr (std::is_same<T, float>::value) cpdi_window<DIM, GRAD>(g, nb, p, i, f);
-        else cpdi_nodes<DIM, GRAD, T>(g, nb, p, i, f);
+    if constexpr (kCpdi<SHAPE>) {
+        if constexpr (std::is_same<T, float>::value) cpdi_window<DIM, SHAPE, GRAD>(g, nb, p, i, f);
+        else cpdi_nodes<DIM, SHAPE, GRAD, T>(g, nb, p, i, f);
     } else {
         for_each_node<DIM, SHAPE, GRAD, T>(g, nb, p.elem[i], p.xi[i], p.eta[i], DIM == 3 ? p.zeta[i] : 0., p.lpx[i],
                                            p.lpy[i], DIM == 3 ? p.lpz[i] : 1., f);
@@ -800,7 +856,7 @@ template <int DIM, int SHAPE, bool GRAD, typename T>
 __device__ __forceinline__ void axis_windows(const DevGrid &g, int col, int row, int zr, double xi_d, double eta_d,
                                              double zeta_d, double lpx_d, double lpy_d, double lpz_d,
                                              AxisWin<SHAPE, T> &w) {
-    static_assert(SHAPE != SHAPE_LCPDI, "lCPDI nodes do not form a window");
+    static_assert(!kCpdi<SHAPE>, "CPDI nodes do not form a window");
     const T xi = (T)xi_d, eta = (T)eta_d, zeta = (T)zeta_d;
     const T iD[3] = {GRAD ? recip((T)(g.xn[col + 1] - g.xn[col])) : T(0),
                      GRAD ? recip((T)(g.yn[row + 1] - g.yn[row])) : T(0),
@@ -1250,9 +1306,9 @@ __device__ __forceinline__ void det_contact_terms(const DevDet &dd, int k, doubl
 // each node gradient is sum_c wg_c N_c(node) with 0 <= N_c <= 1.
 template <int DIM, int SHAPE, bool MIX>
 __device__ __forceinline__ double grad_bound(const DevGrid &g, const DevParticles &p, int i) {
-    if constexpr (SHAPE == SHAPE_LCPDI) {
+    if constexpr (kCpdi<SHAPE>) {
         using T = typename Wt<MIX>::T;
-        constexpr int NC = DIM == 3 ? 8 : 4;
+        constexpr int NC = kCpdiPts<DIM, SHAPE>;
         const size_t n = (size_t)p.n;
         double s = 0.;
 #pragma unroll
@@ -1288,7 +1344,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
     if (i >= p.n) return;
     const DevGrid &g = sp.g;
     bool ok = true;
-    if constexpr (SHAPE == SHAPE_LCPDI) ok = cpdi_setup_for<DIM, MIX>(g, p, i, sp.err);
+    if constexpr (kCpdi<SHAPE>) ok = cpdi_setup_for<DIM, SHAPE, MIX>(g, p, i, sp.err);
     const double mp = p.mass[i];
     const int off = sp.ct.nf > 1 ? sp.ct.fstride * mats[p.mat[i]].field : 0;
     const bool mm = sp.ct.nf > 1;
@@ -1298,7 +1354,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
         atomicMax(nb + n + off, (unsigned long long)__double_as_longlong((double)N * mp));
     };
     if (ok) {
-        if constexpr (SHAPE == SHAPE_LCPDI) {
+        if constexpr (kCpdi<SHAPE>) {
             if (mm) visit_nodes<DIM, SHAPE, true, T>(g, 0, p, i, node);
             else visit_nodes<DIM, SHAPE, false, T>(g, 0, p, i, node);
         } else {
@@ -1328,7 +1384,7 @@ static __global__ void __launch_bounds__(256) k_det_bounds(StepParams sp, DevPar
 // mass accumulate in FP64 in both modes: grid velocities carry the bulk motion
 // and their differences across a cell are the strain rate.
 template <int DIM, int SHAPE, bool MIX, bool BATCH, bool DET = false>
-static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 3) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
+static __global__ void __launch_bounds__(256, kCpdi<SHAPE> ? 2 : 3) k_p2g(StepParams sp, DevParticles p, DevNodes nd, const DevMat *mats) {
     using T = typename Wt<MIX>::T;
     const int i = tile_particle(p);
     if (i >= p.n) return;
@@ -1387,10 +1443,10 @@ static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 3) k_p2
         nd.active[n] = 1;
         if (mm) add_contact_terms<DIM, MIX>(nd, n, N, fnmp, Vp, d, gx, gy, gz);
     };
-    if constexpr (SHAPE == SHAPE_LCPDI) {
+    if constexpr (kCpdi<SHAPE>) {
         // ElementBase::GetShapeFunctionData: the particle's CPDI corners for
         // this step (set by k_det_bounds in the deterministic mode)
-        if (!DET && !cpdi_setup_for<DIM, MIX>(g, p, i, rv.err)) return;
+        if (!DET && !cpdi_setup_for<DIM, SHAPE, MIX>(g, p, i, rv.err)) return;
         if (mm) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
         else visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, scatter);
     } else {
@@ -1529,7 +1585,7 @@ __device__ __forceinline__ void velocity_gradient(const DevGrid &g, int nb, cons
         split2(p.vy[i], ph[1], pl[1]);
         if (DIM == 3) split2(p.vz[i], ph[2], pl[2]);
     }
-    if constexpr (SHAPE != SHAPE_LCPDI) {
+    if constexpr (!kCpdi<SHAPE>) {
         // window shape functions: the separable sum (window_grad_gather)
         AxisWin<SHAPE, T> w;
         particle_window<DIM, SHAPE, true, T>(g, p, i, w);
@@ -1592,7 +1648,7 @@ __device__ __forceinline__ void forces_scatter(const StepParams &sp, const DevPa
     const T sxx = (T)(-mp * (p.sxx[i] - P)), syy = (T)(-mp * (p.syy[i] - P)), sxy = (T)(-mp * p.sxy[i]);
     const T szz = DIM == 3 ? (T)(-mp * (p.szz[i] - P)) : T(0), sxz = DIM == 3 ? (T)(-mp * p.sxz[i]) : T(0),
             syz = DIM == 3 ? (T)(-mp * p.syz[i]) : T(0);
-    if constexpr (SHAPE != SHAPE_LCPDI) {
+    if constexpr (!kCpdi<SHAPE>) {
         // window shape functions: the separable products (window_grad_scatter)
         AxisWin<SHAPE, T> w;
         particle_window<DIM, SHAPE, true, T>(g, p, i, w);
@@ -1840,7 +1896,7 @@ __device__ __forceinline__ void g2p_move(const StepParams &sp, const DevParticle
     }
     // the particle's nodes for this step (CPDI corners or the element window)
     auto visit = [&](auto &&fn) {
-        if constexpr (SHAPE == SHAPE_LCPDI) {
+        if constexpr (kCpdi<SHAPE>) {
             visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
         } else {
             if (win) for_each_window_node_at<DIM, SHAPE, T>(*win, g, rv.nb, fn);
@@ -1921,7 +1977,7 @@ static __global__ void __launch_bounds__(256, 2) k_g2p(StepParams sp, DevParticl
     const int off = field_offset(sp, mats, p, i);
     // the particle's nodes for this step (CPDI corners or the element window)
     auto visit = [&](auto &&fn) {
-        if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
+        if constexpr (kCpdi<SHAPE>) visit_nodes<DIM, SHAPE, false, T>(g, rv.nb, p, i, fn);
         else for_each_node<DIM, SHAPE, false, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, fn);
     };
     if (particle_rigid(sp, mats, p, i)) {
@@ -1940,7 +1996,7 @@ static __global__ void __launch_bounds__(256, 2) k_g2p(StepParams sp, DevParticl
     // mixed mode forms its FP32 factors twice: keeping them live costs more
     // (registers) than forming them.
     AxisWin<SHAPE, T> w;
-    if constexpr (SHAPE != SHAPE_LCPDI && !MIX) {
+    if constexpr (!kCpdi<SHAPE> && !MIX) {
         particle_window<DIM, SHAPE, false, T>(g, p, i, w);
         g2p_move<DIM, SHAPE, MIX, BATCH>(sp, p, nd, i, rv, off, v, xp, &w);
     } else {
@@ -1979,9 +2035,9 @@ static __global__ void __launch_bounds__(256, 2) k_g2p(StepParams sp, DevParticl
             if (rv.mm) add_contact_terms<DIM, MIX>(nd, n, N, fnmp, Vp, d, gx, gy, gz);
         };
         if (rv.mm) {
-            if constexpr (SHAPE == SHAPE_LCPDI) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
+            if constexpr (kCpdi<SHAPE>) visit_nodes<DIM, SHAPE, true, T>(g, rv.nb, p, i, scatter);
             else for_each_node<DIM, SHAPE, true, T>(g, rv.nb, e, xi, eta, zeta, lx, ly, lz, scatter);
-        } else if constexpr (SHAPE != SHAPE_LCPDI && !MIX) {
+        } else if constexpr (!kCpdi<SHAPE> && !MIX) {
             for_each_window_node_at<DIM, SHAPE, T>(w, g, rv.nb, scatter);
         } else {
             visit(scatter);
@@ -2084,7 +2140,7 @@ static __global__ void __launch_bounds__(256) k_det_usl(StepParams sp, DevPartic
                                    sp.err);
         }
     };
-    if constexpr (SHAPE == SHAPE_LCPDI) {
+    if constexpr (kCpdi<SHAPE>) {
         if (mm) visit_nodes<DIM, SHAPE, true, T>(g, 0, p, i, scatter);
         else visit_nodes<DIM, SHAPE, false, T>(g, 0, p, i, scatter);
     } else {

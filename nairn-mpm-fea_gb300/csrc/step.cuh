@@ -76,7 +76,7 @@ void enqueue_step(MpmGpuCtx *c, double t, int slot) {
     }
     // mixed mode, one material field, window shape functions: the scatters
     // accumulate in shared-memory node tiles (unless MPMGPU_P2G_UNTILED)
-    constexpr bool kTileable = MIX && !DET && SHAPE != SHAPE_LCPDI;
+    constexpr bool kTileable = MIX && !DET && !kCpdi<SHAPE>;
     const bool tile = kTileable && c->ct.nf == 1 && c->opts.p2g != MPMGPU_P2G_UNTILED;
     if constexpr (kTileable) {
         if (tile) k_p2g_tile<DIM, SHAPE, false><<<pb, TB, 0, s>>>(sp, c->p, c->nd);
@@ -189,6 +189,9 @@ void enqueue_dim(MpmGpuCtx *c, double t, int slot) {
     const int shape = c->opts.shape;
     if (shape == MPMGPU_SHAPE_LINEAR) enqueue_step<DIM, SHAPE_LINEAR, MIX, DET>(c, t, slot);
     else if (shape == MPMGPU_SHAPE_LCPDI) enqueue_step<DIM, SHAPE_LCPDI, MIX, DET>(c, t, slot);
+    else if (shape == MPMGPU_SHAPE_QCPDI) {
+        if constexpr (DIM == 2) enqueue_step<DIM, SHAPE_QCPDI, MIX, DET>(c, t, slot);  // refused in 3D at create
+    }
     else if (shape == MPMGPU_SHAPE_BSPLINE) enqueue_step<DIM, SHAPE_BSPLINE, MIX, DET>(c, t, slot);
     else if (shape == MPMGPU_SHAPE_BGIMP) enqueue_step<DIM, SHAPE_BGIMP, MIX, DET>(c, t, slot);
     else enqueue_step<DIM, SHAPE_UGIMP, MIX, DET>(c, t, slot);

@@ -125,7 +125,7 @@ static __global__ void k_xpic_init(StepParams sp, DevNodes nd, DevXpic x, int nn
 // XPICDoubleLoop (XPICExtrapolationTask.cpp:182-211) of one particle:
 // v*(next)_i += m_p S_ip / m_i Sum_j S_jp v*(prev)_j
 template <int DIM, int SHAPE, bool MIX, bool BATCH>
-static __global__ void __launch_bounds__(256, SHAPE == SHAPE_LCPDI ? 2 : 1)
+static __global__ void __launch_bounds__(256, kCpdi<SHAPE> ? 2 : 1)
     k_xpic_pass(StepParams sp, DevParticles p, DevXpic x, const DevMat *mats, int phase, int k) {
     using T = typename Wt<MIX>::T;
     const int i = blockIdx.x * blockDim.x + threadIdx.x;

@@ -301,6 +301,9 @@ class GpuBatch:
         o = models[0].options
         if "xpic" not in kw and len({xpic_of(m) for m in models}) > 1:
             raise ValueError("the runs of a batch share one PeriodicXPIC setting")
+        for key in ("np", "method", "shape"):
+            if len({m.options[key] for m in models}) > 1:
+                raise ValueError(f"the runs of a batch share one analysis option {key!r}")
         return cls(o["np"], o["method"], o["shape"], precision, max_runs=kw.pop("max_runs", len(models)),
                    max_particles=int(slack * sum(m.n for m in models)),
                    max_nodes=int(slack * sum(m.grid.nnodes for m in models)),

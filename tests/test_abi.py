@@ -33,11 +33,18 @@ def test_create_rejects_bad_options_without_gpu_work(gpu_lib):
     b = abi.Bound()
     g = abi.grid_struct(m, b)
     o = abi.options_struct(m)
-    o.shape = 11  # qCPDI is not implemented
+    o.shape = 4  # finite GIMP is not implemented
     h = C.c_void_p()
     st = gpu_lib.mpmgpu_create(C.byref(g), C.byref(o), C.byref(h))
     assert st == 2 and not h.value
     assert b"shape" in gpu_lib.mpmgpu_last_error(None)
+    m3 = model.taylor_3d(radius=1.0, length=2.0, cell=0.5, steps=5)
+    g3 = abi.grid_struct(m3, b)
+    o3 = abi.options_struct(m3)
+    o3.shape = model.SHAPE_QCPDI  # qCPDI is 2D only, as in the reference
+    st = gpu_lib.mpmgpu_create(C.byref(g3), C.byref(o3), C.byref(h))
+    assert st == 2 and not h.value
+    assert b"qCPDI" in gpu_lib.mpmgpu_last_error(None)
     o = abi.options_struct(m, p2g=3)  # node sums: atomic (0), deterministic (1) or untiled (2) only
     st = gpu_lib.mpmgpu_create(C.byref(g), C.byref(o), C.byref(h))
     assert st == 2 and not h.value

@@ -430,3 +430,41 @@ def test_batched_rigid_contact_matches_reference(case, precision, tol, gpu_lib):
     for k in ("x", "y", "vx", "vy", "sxx", "syy", "sxy"):
         assert rel_l2(out[k], ref[k]) <= tol, (k, rel_l2(out[k], ref[k]))
     b.close()
+
+
+@pytest.mark.parametrize("precision,tol", [(0, TOL), (1, TOL_MIXED)])
+@pytest.mark.parametrize("case", ["contact2d_fric_qcpdi", "cant2d_qcpdi_neo_usf"])
+def test_batched_qcpdi_runs_match_reference(case, precision, tol, gpu_lib):
+    """qCPDI (2D, nine domain points per particle) in a batch: the golden run
+    matches the reference's result, and a larger qCPDI cantilever admitted
+    five steps later matches the oracle."""
+    from conftest import contact_tolerance, load_golden, model_for, view_for
+    from nairn_gb300 import abi, model
+    from nairn_gb300.gpu import GpuBatch
+    meta, g = load_golden(case)
+    m = model_for(meta)
+    steps = meta["steps"]
+    # the batch's runs share its MPM method: the late run takes the golden run's
+    late = model.cantilever_2d(nx=14, ny=5, steps=steps - 5, gimp="qCPDI", method=meta["kwargs"].get("method", 2))
+    b = GpuBatch.for_models([m, late], precision=precision)
+    r0 = b.add(m)
+    b.step(5)
+    r1 = b.add(late)
+    b.step(steps)
+    assert b.state(r0) == (abi.RUN_FINISHED, steps)
+    assert b.state(r1) == (abi.RUN_FINISHED, late.nsteps)
+    v = view_for(b.download(r0), m)
+    ctol = contact_tolerance(case, m, tol)
+    for k in ("pos", "vel", "stress", "strain"):
+        assert rel_l2(v[k], g["final_" + k]) <= ctol[k], (k, rel_l2(v[k], g["final_" + k]), ctol[k])
+    assert_close(b.download(r1), oracle(late, late.nsteps), tol, "late")
+    b.close()
+
+
+def test_qcpdi_refused_in_3d(gpu_lib):
+    """qCPDI exists in 2D only (the reference refuses it in 3D): a 3D batch
+    of that shape option is refused before any device work."""
+    from nairn_gb300 import model
+    from nairn_gb300.gpu import GpuBatch
+    with pytest.raises(RuntimeError, match="qCPDI"):
+        GpuBatch(model.THREED, model.USAVG, model.SHAPE_QCPDI, 0, max_runs=1, max_particles=1000, max_nodes=1000)
