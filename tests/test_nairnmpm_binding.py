@@ -26,6 +26,7 @@ GPU_BIN = os.path.join(ROOT, "oracle", "_ref", "NairnMPM-gpu")
 CASES = {
     "cantilever_ugimp_usavg": ("cantilever_2d", dict(nx=10, ny=4, steps=60)),
     "cantilever_lcpdi_usl": ("cantilever_2d", dict(nx=10, ny=4, steps=40, gimp="lCPDI", method=3)),
+    "cantilever_qcpdi_usavg": ("cantilever_2d", dict(nx=10, ny=4, steps=40, gimp="qCPDI")),
     "taylor_plastic": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30)),
     "taylor_neohookean_usf": ("taylor_3d", dict(radius=1.0, length=2.0, cell=0.5, steps=30, mat_type=28, G=10., K=50.,
                                                 rho=1.1, v0=-30000., method=0)),
