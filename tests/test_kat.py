@@ -17,6 +17,8 @@ import pytest
 
 
 SHAPES = ("Classic", "uGIMP", "lCPDI")
+# (dim, shape) pairs: every shape in 2D and 3D, and qCPDI, which exists in 2D only
+SHAPE_DIMS = [(d, s) for d in (2, 3) for s in SHAPES] + [(2, "qCPDI")]
 V0 = (1500., -700., 400.)  # mm/s
 
 
@@ -72,8 +74,7 @@ def check_translation(m, out, ref_stress, tol_v, tol_s):
     assert sref > 0. and smax <= tol_s * sref, (smax, sref)
 
 
-@pytest.mark.parametrize("gimp", SHAPES)
-@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("dim,gimp", SHAPE_DIMS)
 def test_oracle_uniform_translation(dim, gimp):
     m = translation_model(dim, gimp)
     out = oracle_run(m, m.nsteps)
@@ -82,8 +83,7 @@ def test_oracle_uniform_translation(dim, gimp):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("gimp", SHAPES)
-@pytest.mark.parametrize("dim", [2, 3])
+@pytest.mark.parametrize("dim,gimp", SHAPE_DIMS)
 @pytest.mark.parametrize("precision,p2g,tol_v,tol_s", [(0, 0, 1e-12, 1e-9), (1, 0, 1e-7, 1e-5),
                                                        (0, 1, 1e-12, 1e-9)])
 def test_gpu_uniform_translation(dim, gimp, precision, p2g, tol_v, tol_s, gpu_lib):
